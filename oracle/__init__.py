@@ -1,0 +1,249 @@
+"""The oracle: CPU projections the GPU module is checked against.
+
+TEST INFRASTRUCTURE. Only ``tests/``, ``__graft_entry__.smoke()`` and the
+CPU-baseline legs of ``bench.py`` import this package; the shipped module
+never does.
+
+Two implementations sit behind the same Python call:
+
+* ``port``: ``oracle/gbp_oracle.c``, a dense C restatement of the reference's
+  ``macpressuresolver{2,3}::project`` (built to ``oracle/liboracle.so``);
+* ``reference``: the reference itself, compiled from its own sources by
+  ``oracle/ref/Makefile`` into ``oracle/_ref/`` and driven through its module
+  loader by ``oracle/ref/ref_harness.cpp``. It can only be built where the
+  reference sources are present.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+REF_SO = os.path.join(REF_DIR, "libref_harness.so")
+DEFAULT_REFERENCE = "/root/reference"
+
+
+def build_port(force: bool = False) -> str:
+    src = os.path.join(HERE, "gbp_oracle.c")
+    if force or not os.path.exists(PORT_SO) or os.path.getmtime(PORT_SO) < os.path.getmtime(src):
+        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", PORT_SO, "-lm"])
+    return PORT_SO
+
+
+def build_reference(ref_dir: str | None = None, jobs: int = 8) -> str | None:
+    """Compile the reference (where its sources exist); returns the harness
+    path or None."""
+    ref_dir = ref_dir or os.environ.get("SHIOKAZE_REFERENCE", DEFAULT_REFERENCE)
+    if not os.path.isdir(os.path.join(ref_dir, "src", "projection")):
+        return REF_SO if os.path.exists(REF_SO) else None
+    subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={ref_dir}", f"-j{jobs}"],
+                          stdout=subprocess.DEVNULL)
+    return REF_SO
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("residual", ctypes.c_double), ("max_iterations", ctypes.c_int), ("warm_start", ctypes.c_int),
+                ("eps_fluid", ctypes.c_double), ("eps_solid", ctypes.c_double),
+                ("second_order_fluid", ctypes.c_int), ("second_order_solid", ctypes.c_int),
+                ("gain", ctypes.c_double)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("reresid", ctypes.c_double),
+                ("unknowns", ctypes.c_longlong), ("b_inf", ctypes.c_double)]
+
+
+@dataclass
+class Result:
+    pressure: np.ndarray
+    u: np.ndarray
+    v: np.ndarray
+    w: np.ndarray | None
+    unknown: np.ndarray  # bool per cell
+    iterations: int
+    reresid: float
+    ms: float = 0.0
+    index: np.ndarray | None = None
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _ptr(a, t=ctypes.c_float):
+    return a.ctypes.data_as(ctypes.POINTER(t)) if a is not None else None
+
+
+_port = None
+
+
+def _port_lib():
+    global _port
+    if _port is None:
+        lib = ctypes.CDLL(build_port())
+        lib.oracle_create.restype = ctypes.c_void_p
+        lib.oracle_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        lib.oracle_destroy.argtypes = [ctypes.c_void_p]
+        lib.oracle_set_target_volume.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
+        fp = ctypes.POINTER(ctypes.c_float)
+        dp = ctypes.POINTER(ctypes.c_double)
+        lp = ctypes.POINTER(ctypes.c_longlong)
+        lib.oracle_project.argtypes = [ctypes.c_void_p, ctypes.c_double, fp, fp, fp, fp, fp,
+                                       ctypes.POINTER(_Params), fp, lp, ctypes.POINTER(_Stats)]
+        lib.oracle_assemble.argtypes = [ctypes.c_void_p, ctypes.c_double, fp, fp, fp, fp, fp,
+                                        ctypes.POINTER(_Params), dp, dp, dp, dp, dp, lp]
+        lib.oracle_face_fractions.argtypes = [ctypes.c_void_p, fp, fp, ctypes.POINTER(_Params), fp, fp, fp, fp, fp,
+                                              fp]
+        _port = lib
+    return _port
+
+
+def make_params(residual=1e-6, max_iterations=30000, warm_start=False, eps_fluid=1e-2, eps_solid=1e-2,
+                second_order_fluid=True, second_order_solid=True, gain=1.0):
+    return _Params(residual, max_iterations, int(warm_start), eps_fluid, eps_solid, int(second_order_fluid),
+                   int(second_order_solid), gain)
+
+
+class PortProjector:
+    """The C restatement, one context per scene shape (holds warm-start state)."""
+
+    def __init__(self, dim, nx, ny, nz, dx, **params):
+        self.lib = _port_lib()
+        self.dim, self.nx, self.ny, self.nz, self.dx = dim, nx, ny, (nz if dim == 3 else 1), dx
+        self.params = make_params(**params)
+        self.ctx = self.lib.oracle_create(dim, nx, ny, self.nz, dx)
+
+    def close(self):
+        if self.ctx:
+            self.lib.oracle_destroy(self.ctx)
+            self.ctx = None
+
+    __del__ = close
+
+    def set_target_volume(self, current, target):
+        self.lib.oracle_set_target_volume(self.ctx, current, target)
+
+    def project(self, dt, solid, fluid, u, v, w=None) -> Result:
+        u, v = _f32(u).copy(), _f32(v).copy()
+        w = _f32(w).copy() if w is not None else None
+        solid, fluid = _f32(solid), _f32(fluid)
+        p = np.zeros(fluid.shape, np.float32)
+        idx = np.zeros(fluid.shape, np.int64)
+        st = _Stats()
+        self.lib.oracle_project(self.ctx, dt, _ptr(solid), _ptr(fluid), _ptr(u), _ptr(v), _ptr(w),
+                                ctypes.byref(self.params), _ptr(p), _ptr(idx, ctypes.c_longlong), ctypes.byref(st))
+        return Result(p, u, v, w, idx >= 0, st.iterations, st.reresid, index=idx)
+
+    def assemble(self, dt, solid, fluid, u, v, w=None):
+        solid, fluid, u, v = _f32(solid), _f32(fluid), _f32(u), _f32(v)
+        w = _f32(w) if w is not None else None
+        shp = fluid.shape
+        out = [np.zeros(shp, np.float64) for _ in range(5)]
+        idx = np.zeros(shp, np.int64)
+        dp = ctypes.c_double
+        self.lib.oracle_assemble(self.ctx, dt, _ptr(solid), _ptr(fluid), _ptr(u), _ptr(v), _ptr(w),
+                                 ctypes.byref(self.params), *[_ptr(o, dp) for o in out],
+                                 _ptr(idx, ctypes.c_longlong))
+        diag, cpx, cpy, cpz, b = out
+        return {"diag": diag, "cpx": cpx, "cpy": cpy, "cpz": cpz, "b": b, "index": idx}
+
+
+_ref = None
+
+
+def _ref_lib():
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO):
+            raise RuntimeError("reference oracle not built (oracle/ref/Makefile needs the reference sources)")
+        lib = ctypes.CDLL(REF_SO, mode=ctypes.RTLD_GLOBAL)
+        fp = ctypes.POINTER(ctypes.c_float)
+        lib.ref_create.restype = ctypes.c_void_p
+        lib.ref_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                   ctypes.c_char_p, ctypes.c_char_p]
+        lib.ref_destroy.argtypes = [ctypes.c_void_p]
+        lib.ref_project.restype = ctypes.c_double
+        lib.ref_project.argtypes = [ctypes.c_void_p, ctypes.c_double, fp, ctypes.c_int, ctypes.c_float, fp,
+                                    ctypes.c_int, ctypes.c_float, fp, fp, fp, fp,
+                                    ctypes.POINTER(ctypes.c_ubyte), ctypes.c_char_p]
+        lib.ref_levelset_roundtrip.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp,
+                                               ctypes.c_int, ctypes.c_float, fp]
+        _ref = lib
+    return _ref
+
+
+_ITER_RE = re.compile(r"Took (\d+) iterations, Reresid=([0-9][0-9.eE+\-]*[0-9]|nan|inf)")
+
+
+class RefProjector:
+    """The reference's own macpressuresolver{2,3}, loaded by name."""
+
+    def __init__(self, dim, nx, ny, nz, dx, residual=1e-6, max_iterations=30000, warm_start=False, eps_fluid=1e-2,
+                 eps_solid=1e-2, second_order_fluid=True, second_order_solid=True, gain=1.0, threads=None):
+        self.lib = _ref_lib()
+        self.dim, self.nx, self.ny, self.nz, self.dx = dim, nx, ny, (nz if dim == 3 else 1), dx
+        kv = (f"Residual={residual!r} MaxIterations={max_iterations} WarmStart={'Yes' if warm_start else 'No'} "
+              f"EpsFluid={eps_fluid!r} EpsSolid={eps_solid!r} "
+              f"SecondOrderAccurateFluid={'Yes' if second_order_fluid else 'No'} "
+              f"SecondOrderAccurateSolid={'Yes' if second_order_solid else 'No'} Gain={gain!r}")
+        if threads:
+            kv += f" Threads={threads}"
+        self._log = tempfile.NamedTemporaryFile(prefix="ref_project_", suffix=".log", delete=False).name
+        self.ctx = self.lib.ref_create(dim, nx, ny, self.nz, dx, kv.encode(), self._log.encode())
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.ref_destroy(self.ctx)
+            self.ctx = None
+            try:
+                os.unlink(self._log)
+            except OSError:
+                pass
+
+    __del__ = close
+
+    def project(self, dt, solid, fluid, u, v, w=None, solid_mode=0, fluid_mode=0, band=None) -> Result:
+        if band is None:
+            band = float(np.float32(np.sqrt(3.0) * self.dx))
+        u, v = _f32(u).copy(), _f32(v).copy()
+        w = _f32(w).copy() if w is not None else None
+        solid, fluid = _f32(solid), _f32(fluid)
+        p = np.zeros(fluid.shape, np.float32)
+        act = np.zeros(fluid.shape, np.uint8)
+        open(self._log, "w").close()
+        ms = self.lib.ref_project(self.ctx, dt, _ptr(solid), solid_mode, band, _ptr(fluid), fluid_mode, band,
+                                  _ptr(u), _ptr(v), _ptr(w), _ptr(p), _ptr(act, ctypes.c_ubyte),
+                                  self._log.encode())
+        with open(self._log, errors="replace") as f:
+            log = f.read()
+        m = _ITER_RE.findall(log)
+        iters, rr = (int(m[-1][0]), float(m[-1][1])) if m else (-1, float("nan"))
+        return Result(p, u, v, w, act.astype(bool), iters, rr, ms=ms)
+
+
+def project_scene(scene, impl="port", **params) -> Result:
+    """One projection of a ``shiokaze_gb300.scenes.Scene`` on the CPU."""
+    if impl == "port":
+        pj = PortProjector(scene.dim, scene.nx, scene.ny, scene.nz, scene.dx, **params)
+        try:
+            return pj.project(scene.dt, scene.solid, scene.fluid, scene.u, scene.v, scene.w)
+        finally:
+            pj.close()
+    pj = RefProjector(scene.dim, scene.nx, scene.ny, scene.nz, scene.dx, **params)
+    try:
+        return pj.project(scene.dt, scene.solid, scene.fluid, scene.u, scene.v, scene.w, scene.solid_mode,
+                          scene.fluid_mode, scene.band)
+    finally:
+        pj.close()

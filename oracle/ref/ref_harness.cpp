@@ -1,0 +1,261 @@
+/*
+ * ref_harness.cpp -- drives the reference's own pressure projection
+ * (src/projection/macpressuresolver{2,3}.cpp, loaded through its module loader
+ * src/core/module.cpp:103-172 by the name "macpressuresolver{2,3}") on dense
+ * inputs, for the oracle.
+ *
+ * TEST INFRASTRUCTURE. This file is compiled against the reference's headers
+ * by oracle/ref/Makefile into oracle/_ref/libref_harness.so. Only tests and
+ * fixture generation load it. The shipped library never does.
+ *
+ * Dense -> sparse conversion follows the reference's scene setup
+ * (src/utility/macutility3.cpp:317-358, assign_initial_variables): a level set
+ * value is stored only where |v| < band, then the array is marked as a level
+ * set of half-width `band` and flood filled, so inactive cells read +band
+ * outside and -band inside. A "constant" level set (mode 1) is an array with
+ * background value v[0] and no active cells, as the smoke scene builds its
+ * fluid (src/smoke/macsmoke3.cpp:106). Velocity faces are all activated.
+ *
+ * After project() the harness reads pressure and velocity back through
+ * operator(), which applies background/fill semantics, and reports which
+ * pressure cells are active (the reference sets pressure only at unknowns,
+ * macpressuresolver3.cpp:245-248).
+ */
+#include <shiokaze/array/array2.h>
+#include <shiokaze/array/array3.h>
+#include <shiokaze/array/macarray2.h>
+#include <shiokaze/array/macarray3.h>
+#include <shiokaze/core/configuration.h>
+#include <shiokaze/core/configurable.h>
+#include <shiokaze/projection/macproject2_interface.h>
+#include <shiokaze/projection/macproject3_interface.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fcntl.h>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <unistd.h>
+
+SHKZ_USING_NAMESPACE
+
+namespace {
+
+struct harness {
+    int dim = 3;
+    int nx = 0, ny = 0, nz = 1;
+    double dx = 0.0;
+    configuration *config = nullptr;
+    std::unique_ptr<macproject3_driver> proj3;
+    std::unique_ptr<macproject2_driver> proj2;
+    shape3 shape3_;
+    shape2 shape2_;
+};
+
+std::map<std::string, std::string> parse_kv(const char *kv) {
+    std::map<std::string, std::string> out;
+    if (!kv) return out;
+    std::istringstream ss(kv);
+    std::string tok;
+    while (ss >> tok) {
+        auto pos = tok.find('=');
+        if (pos != std::string::npos) out[tok.substr(0, pos)] = tok.substr(pos + 1);
+    }
+    return out;
+}
+
+// Runs fn with stdout sent to log_path (appended), so the reference's console
+// output (iteration count, residual, phase timings) can be parsed afterwards.
+template <class F> void with_stdout_to(const char *log_path, F fn) {
+    if (!log_path || !*log_path) { fn(); return; }
+    fflush(stdout);
+    int saved = dup(1);
+    int fd = open(log_path, O_WRONLY | O_CREAT | O_APPEND, 0644);
+    if (fd >= 0) { dup2(fd, 1); close(fd); }
+    fn();
+    fflush(stdout);
+    if (saved >= 0) { dup2(saved, 1); close(saved); }
+}
+
+void fill_levelset3(array3<Real> &a, const shape3 &s, const float *v, int mode, float band) {
+    if (mode == 1) {
+        a.initialize(s, v[0]);
+        return;
+    }
+    a.initialize(s, 0.0);
+    for (int k = 0; k < (int)s.d; ++k)
+        for (int j = 0; j < (int)s.h; ++j)
+            for (int i = 0; i < (int)s.w; ++i) {
+                float x = v[i + (size_t)s.w * (j + (size_t)s.h * k)];
+                if (std::abs(x) < band) a.set(i, j, k, x);
+            }
+    a.set_as_levelset(band);
+    a.flood_fill();
+}
+
+void fill_levelset2(array2<Real> &a, const shape2 &s, const float *v, int mode, float band) {
+    if (mode == 1) {
+        a.initialize(s, v[0]);
+        return;
+    }
+    a.initialize(s, 0.0);
+    for (int j = 0; j < (int)s.h; ++j)
+        for (int i = 0; i < (int)s.w; ++i) {
+            float x = v[i + (size_t)s.w * j];
+            if (std::abs(x) < band) a.set(i, j, x);
+        }
+    a.set_as_levelset(band);
+    a.flood_fill();
+}
+
+}  // namespace
+
+extern "C" {
+
+/* Creates a reference projector. dim is 2 or 3 (nz ignored for 2).
+ * kv: whitespace-separated Key=Value settings of the reference's
+ * configuration (Residual, MaxIterations, WarmStart, EpsFluid, EpsSolid,
+ * SecondOrderAccurateFluid, SecondOrderAccurateSolid, Threads, ...). */
+void *ref_create(int dim, int nx, int ny, int nz, double dx, const char *kv, const char *log_path) {
+    auto *h = new harness();
+    h->dim = dim;
+    h->nx = nx;
+    h->ny = ny;
+    h->nz = (dim == 3) ? nz : 1;
+    h->dx = dx;
+    // The reference's arrays configure themselves from the global
+    // configuration, and every configuration lookup needs a group on the
+    // stack (src/core/configuration.cpp:298-301), as src/ui/ui.cpp:631 pushes.
+    configuration &config = configurable::set_global_configuration(configuration(parse_kv(kv)));
+    config.push_group("Harness", "Harness");
+    h->config = &config;
+    with_stdout_to(log_path, [&]() {
+        if (dim == 3) {
+            h->shape3_ = shape3(nx, ny, nz);
+            h->proj3.reset(new macproject3_driver("macpressuresolver3"));
+            (*h->proj3).set_environment("shape", &h->shape3_);
+            (*h->proj3).set_environment("dx", &h->dx);
+            h->proj3->setup_now(*h->config);
+        } else {
+            h->shape2_ = shape2(nx, ny);
+            h->proj2.reset(new macproject2_driver("macpressuresolver2"));
+            (*h->proj2).set_environment("shape", &h->shape2_);
+            (*h->proj2).set_environment("dx", &h->dx);
+            h->proj2->setup_now(*h->config);
+        }
+    });
+    return h;
+}
+
+void ref_destroy(void *hp) { delete static_cast<harness *>(hp); }
+
+/* One projection. Arrays are dense, x fastest:
+ *   solid: nodal (nx+1)(ny+1)(nz+1), fluid: cells nx*ny*nz,
+ *   u: (nx+1)*ny*nz, v: nx*(ny+1)*nz, w: nx*ny*(nz+1)   (in/out),
+ *   pressure: cells (out), active: cells, 1 where pressure is active (out).
+ * solid_mode/fluid_mode: 0 = narrow-band level set of half-width band,
+ * 1 = constant array (value = first element).
+ * Returns wall-clock milliseconds of project(). */
+double ref_project(void *hp, double dt, const float *solid, int solid_mode, float solid_band,
+                   const float *fluid, int fluid_mode, float fluid_band, float *u, float *v, float *w,
+                   float *pressure, unsigned char *active, const char *log_path) {
+    auto *h = static_cast<harness *>(hp);
+    const int nx = h->nx, ny = h->ny, nz = h->nz;
+    double ms = 0.0;
+    if (h->dim == 3) {
+        const shape3 s = h->shape3_;
+        array3<Real> solid_a, fluid_a;
+        fill_levelset3(solid_a, s.nodal(), solid, solid_mode, solid_band);
+        fill_levelset3(fluid_a, s, fluid, fluid_mode, fluid_band);
+        macarray3<Real> vel(s);
+        vel.activate_all();
+        float *comp[3] = {u, v, w};
+        for (int d = 0; d < 3; ++d) {
+            const shape3 fs = s.face(d);
+            for (int k = 0; k < (int)fs.d; ++k)
+                for (int j = 0; j < (int)fs.h; ++j)
+                    for (int i = 0; i < (int)fs.w; ++i)
+                        vel[d].set(i, j, k, comp[d][i + (size_t)fs.w * (j + (size_t)fs.h * k)]);
+        }
+        with_stdout_to(log_path, [&]() {
+            auto t0 = std::chrono::steady_clock::now();
+            (*h->proj3)->project(dt, vel, solid_a, fluid_a);
+            auto t1 = std::chrono::steady_clock::now();
+            ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        });
+        for (int d = 0; d < 3; ++d) {
+            const shape3 fs = s.face(d);
+            for (int k = 0; k < (int)fs.d; ++k)
+                for (int j = 0; j < (int)fs.h; ++j)
+                    for (int i = 0; i < (int)fs.w; ++i)
+                        comp[d][i + (size_t)fs.w * (j + (size_t)fs.h * k)] = vel[d](i, j, k);
+        }
+        const array3<Real> &p = *(*h->proj3)->get_pressure();
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    size_t n = i + (size_t)nx * (j + (size_t)ny * k);
+                    pressure[n] = p(i, j, k);
+                    active[n] = p.active(i, j, k) ? 1 : 0;
+                }
+    } else {
+        const shape2 s = h->shape2_;
+        array2<Real> solid_a, fluid_a;
+        fill_levelset2(solid_a, s.nodal(), solid, solid_mode, solid_band);
+        fill_levelset2(fluid_a, s, fluid, fluid_mode, fluid_band);
+        macarray2<Real> vel(s);
+        vel.activate_all();
+        float *comp[2] = {u, v};
+        for (int d = 0; d < 2; ++d) {
+            const shape2 fs = s.face(d);
+            for (int j = 0; j < (int)fs.h; ++j)
+                for (int i = 0; i < (int)fs.w; ++i)
+                    vel[d].set(i, j, comp[d][i + (size_t)fs.w * j]);
+        }
+        with_stdout_to(log_path, [&]() {
+            auto t0 = std::chrono::steady_clock::now();
+            (*h->proj2)->project(dt, vel, solid_a, fluid_a);
+            auto t1 = std::chrono::steady_clock::now();
+            ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        });
+        for (int d = 0; d < 2; ++d) {
+            const shape2 fs = s.face(d);
+            for (int j = 0; j < (int)fs.h; ++j)
+                for (int i = 0; i < (int)fs.w; ++i) comp[d][i + (size_t)fs.w * j] = vel[d](i, j);
+        }
+        const array2<Real> &p = *(*h->proj2)->get_pressure();
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                size_t n = i + (size_t)nx * j;
+                pressure[n] = p(i, j);
+                active[n] = p.active(i, j) ? 1 : 0;
+            }
+    }
+    return ms;
+}
+
+/* Reads a level set back through the reference's sparse array semantics
+ * (operator()), to check that the dense input survives the sparse round trip.
+ * shape is the array's own shape (nodal for solid). */
+void ref_levelset_roundtrip(int dim, int sx, int sy, int sz, const float *in, int mode, float band, float *out) {
+    if (dim == 3) {
+        array3<Real> a;
+        shape3 s(sx, sy, sz);
+        fill_levelset3(a, s, in, mode, band);
+        for (int k = 0; k < sz; ++k)
+            for (int j = 0; j < sy; ++j)
+                for (int i = 0; i < sx; ++i) out[i + (size_t)sx * (j + (size_t)sy * k)] = a(i, j, k);
+    } else {
+        array2<Real> a;
+        shape2 s(sx, sy);
+        fill_levelset2(a, s, in, mode, band);
+        for (int j = 0; j < sy; ++j)
+            for (int i = 0; i < sx; ++i) out[i + (size_t)sx * j] = a(i, j);
+    }
+}
+
+}  // extern "C"
