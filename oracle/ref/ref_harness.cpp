@@ -112,6 +112,18 @@ void fill_levelset2(array2<Real> &a, const shape2 &s, const float *v, int mode, 
     a.flood_fill();
 }
 
+bool g_config_ready = false;
+
+// The reference's arrays configure themselves from the global configuration,
+// and every configuration lookup needs a group on the stack
+// (src/core/configuration.cpp:298-301), as src/ui/ui.cpp:631 pushes.
+configuration &install_global_config(const char *kv) {
+    configuration &config = configurable::set_global_configuration(configuration(parse_kv(kv)));
+    config.push_group("Harness", "Harness");
+    g_config_ready = true;
+    return config;
+}
+
 }  // namespace
 
 extern "C" {
@@ -127,12 +139,7 @@ void *ref_create(int dim, int nx, int ny, int nz, double dx, const char *kv, con
     h->ny = ny;
     h->nz = (dim == 3) ? nz : 1;
     h->dx = dx;
-    // The reference's arrays configure themselves from the global
-    // configuration, and every configuration lookup needs a group on the
-    // stack (src/core/configuration.cpp:298-301), as src/ui/ui.cpp:631 pushes.
-    configuration &config = configurable::set_global_configuration(configuration(parse_kv(kv)));
-    config.push_group("Harness", "Harness");
-    h->config = &config;
+    h->config = &install_global_config(kv);
     with_stdout_to(log_path, [&]() {
         if (dim == 3) {
             h->shape3_ = shape3(nx, ny, nz);
@@ -242,6 +249,7 @@ double ref_project(void *hp, double dt, const float *solid, int solid_mode, floa
  * (operator()), to check that the dense input survives the sparse round trip.
  * shape is the array's own shape (nodal for solid). */
 void ref_levelset_roundtrip(int dim, int sx, int sy, int sz, const float *in, int mode, float band, float *out) {
+    if (!g_config_ready) install_global_config("");
     if (dim == 3) {
         array3<Real> a;
         shape3 s(sx, sy, sz);

@@ -1,0 +1,68 @@
+"""The oracle itself: the C restatement against the reference's own outputs.
+
+The golden fixtures were produced by the reference's macpressuresolver{2,3}
+built from its sources (tests/golden/make_golden.py). The restatement must
+reproduce them bit for bit: pressure, projected velocity, the set of unknown
+cells and the CG iteration count.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from golden_io import Case, case_names
+from shiokaze_gb300 import scenes
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_port_matches_reference_fixture(name):
+    c = Case(name)
+    pj = oracle.PortProjector(c.dim, c.nx, c.ny, c.nz, c.dx, **c.params)
+    res = None
+    for s in range(c.steps):
+        u, v, w = c.inputs[s]
+        res = pj.project(c.dt, c.solid, c.fluid, u, v, w)
+    pj.close()
+    assert np.array_equal(res.unknown, c.out_unknown)
+    assert np.array_equal(res.pressure, c.out_pressure)
+    assert np.array_equal(res.u, c.out_u)
+    assert np.array_equal(res.v, c.out_v)
+    if c.dim == 3:
+        assert np.array_equal(res.w, c.out_w)
+        assert res.iterations == c.iterations
+
+
+def test_known_answer_accuracy():
+    """accuracytest3 (src/examples/accuracytest3-example.cpp:108-127): the
+    projected pressure approximates |x-c|^2 - r^2; error shrinks ~2nd order."""
+    errs = []
+    for n in (16, 32):
+        sc, exact = scenes.accuracy3(n, 0.25)
+        r = oracle.project_scene(sc, "port", residual=1e-18, eps_fluid=1e-18)
+        m = r.unknown
+        errs.append(float(np.max(np.abs(r.pressure[m] - exact[m]))))
+    assert errs[1] < errs[0] * 0.6, errs
+
+
+def test_no_fluid_is_identity_away_from_walls():
+    """No fluid anywhere: no unknowns, every fluid fraction reads 1, interior
+    faces keep their velocity and wall faces are zeroed."""
+    sc = scenes.liquid3(8, seed=12)
+    sc.fluid[...] = np.float32(sc.band)
+    r = oracle.project_scene(sc, "port")
+    assert not r.unknown.any()
+    assert np.array_equal(r.u[:, :, 1:-1], sc.u[:, :, 1:-1])
+    assert not r.u[:, :, 0].any() and not r.u[:, :, -1].any()
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference oracle not built here")
+@pytest.mark.parametrize("seed", [21, 22])
+def test_port_matches_live_reference(seed):
+    rng = np.random.default_rng(seed)
+    n = tuple(int(x) for x in rng.integers(9, 20, 3))
+    sc = scenes.liquid3(n, seed=seed, pool=float(rng.uniform(0.2, 0.5)))
+    a = oracle.project_scene(sc, "port")
+    b = oracle.project_scene(sc, "reference")
+    assert np.array_equal(a.unknown, b.unknown)
+    assert np.array_equal(a.pressure, b.pressure)
+    assert np.array_equal(a.w, b.w)
+    assert a.iterations == b.iterations
