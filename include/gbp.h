@@ -1,0 +1,155 @@
+/*
+ * gbp.h -- C ABI of the GB300 pressure-projection library (libgbp.so).
+ *
+ * One call projects a MAC velocity field onto its divergence-free part the
+ * way Shiokaze's pressure projection does it: face fractions from the solid
+ * and fluid level sets, the variational ghost-fluid Poisson system, its
+ * solve, and the pressure-gradient velocity update. It replaces
+ *
+ *   macproject3_interface::project(dt, velocity, solid, fluid, ...)
+ *     include/shiokaze/projection/macproject3_interface.h:67-72
+ *   macproject2_interface::project(...)
+ *     include/shiokaze/projection/macproject2_interface.h:67-72
+ *   as implemented by src/projection/macpressuresolver3.cpp:50-272 and
+ *   src/projection/macpressuresolver2.cpp:48-238,
+ *
+ * with get_pressure() (macproject3_interface.h:79) returned through the
+ * pressure output and set_target_volume() (:50) as its own call.
+ *
+ * Arrays are dense, x fastest (index i + nx*(j + ny*k)):
+ *   solid     nodal level set   (nx+1)*(ny+1)*(nz+1)   [(nx+1)*(ny+1) in 2D]
+ *   fluid     cell level set    nx*ny*nz               [nx*ny]
+ *   u, v, w   face velocities   (nx+1)*ny*nz, nx*(ny+1)*nz, nx*ny*(nz+1)
+ *                               (in/out; w is ignored in 2D)
+ *   pressure  cell pressure     nx*ny*nz, 0 off the unknowns (out, optional)
+ * Level sets are the values the reference reads through its narrow-band
+ * arrays (outside the band they read +-band). Every face is updated.
+ *
+ * Errors are reported as int status codes (GBP_OK == 0). The reference has
+ * no error returns (it asserts or exits); a solve that stops at
+ * max_iterations still writes its last iterate and the velocity update, as
+ * the reference does, and returns GBP_ERR_NOT_CONVERGED.
+ *
+ * Threading: a context and its scenes belong to one host thread at a time.
+ */
+#ifndef GBP_H
+#define GBP_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBP_OK 0
+#define GBP_ERR_INVALID_ARGUMENT 1
+#define GBP_ERR_CUDA 2
+#define GBP_ERR_OUT_OF_MEMORY 3
+#define GBP_ERR_NOT_CONVERGED 4
+#define GBP_ERR_NAN 5
+#define GBP_ERR_NO_DEVICE 6
+#define GBP_ERR_BUDGET 7
+#define GBP_ERR_TIMEOUT 8
+
+/* Linear solver. GBP_SOLVER_CG is the reference's default "pcg" module,
+ * whose preconditioner returns its input (local/include/pcgsolver/
+ * pcg_solver.h:379-384): plain CG, x0 = 0, stop at |r|_inf <= residual*|b|_inf
+ * on the recursively updated residual. GBP_SOLVER_MGPCG is CG preconditioned
+ * by a geometric multigrid V-cycle, same stopping rule. */
+#define GBP_SOLVER_CG 0
+#define GBP_SOLVER_MGPCG 1
+
+/* Arithmetic. FP64: every vector and operator in double.
+ * MIXED: FP64 outer iterative refinement (r = b - A x with the FP64
+ * operator, FP64 x, FP64 norms and dot products) around an FP32 MGPCG inner
+ * solve (FP32 stencil, smoother and transfers). */
+#define GBP_PRECISION_FP64 0
+#define GBP_PRECISION_MIXED 1
+
+typedef struct gbp_ctx gbp_ctx;
+typedef struct gbp_scene gbp_scene;
+
+typedef struct gbp_params {
+    double residual;        /* "Residual", src/linsolver/pcg.cpp:40 (default 1e-4) */
+    int max_iterations;     /* "MaxIterations", pcg.cpp:43 (default 30000) */
+    int warm_start;         /* "WarmStart", macpressuresolver3.cpp:278 (default 0) */
+    double eps_fluid;       /* "EpsFluid", src/utility/macutility3.cpp:408 (default 1e-2) */
+    double eps_solid;       /* "EpsSolid", macutility3.cpp:409 (default 1e-2) */
+    int second_order_fluid; /* "SecondOrderAccurateFluid", macpressuresolver3.cpp:275 (default 1) */
+    int second_order_solid; /* "SecondOrderAccurateSolid", macpressuresolver3.cpp:276 (default 1) */
+    double gain;            /* "Gain", macpressuresolver3.cpp:277 (default 1) */
+    int solver;             /* GBP_SOLVER_* (default GBP_SOLVER_CG) */
+    int precision;          /* GBP_PRECISION_* (default GBP_PRECISION_FP64) */
+    int mg_smooth;          /* red-black sweeps before and after each coarse correction (default 1) */
+    int mg_coarsest;        /* coarsen while any edge exceeds this (default 8) */
+    double inner_tolerance; /* MIXED: relative residual of each inner solve (default 1e-3) */
+    int iterations_per_sync;/* CG iterations between host checks of convergence (default 16) */
+} gbp_params;
+
+typedef struct gbp_stats {
+    int iterations;         /* CG iterations (summed over refinement steps for MIXED) */
+    int outer_iterations;   /* refinement steps (1 unless MIXED) */
+    int converged;          /* stopping rule met */
+    double reresid;         /* |r|_inf / |b|_inf at exit, r the solver's residual (pcg_solver.h:292) */
+    double true_resid_inf;  /* |b - A x|_inf / |b|_inf recomputed in FP64 at exit */
+    double true_resid_l2;   /* |b - A x|_2 / |b|_2 */
+    double b_inf;           /* |b|_inf of the system solved (after warm-start shift) */
+    long long unknowns;     /* pressure unknowns (cells in the linear system) */
+    float ms_assemble;      /* device time, face fractions + labelling + operator + rhs */
+    float ms_solve;         /* device time, the linear solve */
+    float ms_update;        /* device time, velocity update + pressure write */
+    float ms_total;         /* host wall time of the call */
+} gbp_stats;
+
+/* Fills *p with the reference's defaults (and CG / FP64). */
+void gbp_params_default(gbp_params *p);
+
+/* Context on CUDA device `device`: stream, events, graph cache. */
+int gbp_create(int device, gbp_ctx **out);
+void gbp_destroy(gbp_ctx *ctx);
+
+/* A scene holds the device state of one grid: operator, solver vectors,
+ * multigrid hierarchy and warm-start pressure. It replaces a
+ * macpressuresolver{2,3} instance after initialize(shape, dx)
+ * (macpressuresolver3.cpp:281-291). dim is 2 or 3 (nz ignored in 2D). */
+int gbp_scene_create(gbp_ctx *ctx, int dim, int nx, int ny, int nz, double dx, gbp_scene **out);
+void gbp_scene_destroy(gbp_scene *scene);
+
+/* Device bytes a scene of this shape holds once projected with `params`
+ * (used for admission against a memory budget). */
+size_t gbp_scene_device_bytes(int dim, int nx, int ny, int nz, const gbp_params *params);
+
+/* macproject3_interface::set_target_volume (macproject3_interface.h:50,
+ * macpressuresolver3.cpp:45-48): arms the volume-correction term. */
+int gbp_scene_set_target_volume(gbp_scene *scene, double current_volume, double target_volume);
+
+/* One projection with HOST arrays (copied in and out on the context's
+ * stream). params may be NULL (defaults); pressure and stats may be NULL. */
+int gbp_project(gbp_scene *scene, double dt, const float *solid, const float *fluid, float *u, float *v, float *w,
+                const gbp_params *params, float *pressure, gbp_stats *stats);
+
+/* The same with DEVICE arrays, on `stream` (a cudaStream_t; NULL = the
+ * context's stream). Returns after the solve has finished on the device. */
+int gbp_project_device(gbp_scene *scene, double dt, const float *solid, const float *fluid, float *u, float *v,
+                       float *w, const gbp_params *params, float *pressure, gbp_stats *stats, void *stream);
+
+/* Operator and right-hand side as assembled on the device, copied to host
+ * arrays (each nx*ny*nz doubles): diagonal, coupling weight of each cell's
+ * +x/+y/+z face (the negated off-diagonal, 0 unless both cells are
+ * unknowns), and b. For checking the assembly against the reference
+ * (macpressuresolver3.cpp:163-199). cz may be NULL in 2D. */
+int gbp_debug_assemble(gbp_scene *scene, double dt, const float *solid, const float *fluid, const float *u,
+                       const float *v, const float *w, const gbp_params *params, double *diag, double *cx,
+                       double *cy, double *cz, double *b);
+
+/* Number of kernel launches this context has issued (graph nodes count one
+ * each). */
+long long gbp_launch_count(gbp_ctx *ctx);
+
+const char *gbp_strerror(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBP_H */

@@ -1,0 +1,305 @@
+"""GB300 pressure projection for Shiokaze scenes.
+
+Python mirror of the reference's projection plugin interface
+(``include/shiokaze/projection/macproject3_interface.h:38-99``,
+``macproject2_interface.h``), on top of the C ABI in ``include/gbp.h``
+(``libgbp.so``, hand-written sm_103a CUDA kernels):
+
+    proj = MacProject3(nx, ny, nz, dx, Residual=1e-6)     # initialize(shape, dx)
+    proj.project(dt, (u, v, w), solid, fluid)             # in place on u, v, w
+    p = proj.get_pressure()
+
+Configuration keys are the reference's (``Residual``, ``MaxIterations``,
+``WarmStart``, ``EpsFluid``, ``EpsSolid``, ``SecondOrderAccurateFluid``,
+``SecondOrderAccurateSolid``, ``Gain``) plus this module's own
+(``Solver`` = "cg" | "mgpcg", ``Precision`` = "fp64" | "mixed",
+``MGSmooth``, ``MGCoarsest``, ``InnerTolerance``, ``IterationsPerSync``).
+
+Arrays may be numpy arrays (host; copied in and out by the call) or torch
+CUDA tensors (device; used in place). There is no CPU fallback: without the
+built library every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgbp.so")
+
+GBP_OK = 0
+GBP_ERR_NOT_CONVERGED = 4
+GBP_ERR_NAN = 5
+SOLVER_CG, SOLVER_MGPCG = 0, 1
+PRECISION_FP64, PRECISION_MIXED = 0, 1
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("residual", ctypes.c_double), ("max_iterations", ctypes.c_int), ("warm_start", ctypes.c_int),
+                ("eps_fluid", ctypes.c_double), ("eps_solid", ctypes.c_double),
+                ("second_order_fluid", ctypes.c_int), ("second_order_solid", ctypes.c_int),
+                ("gain", ctypes.c_double), ("solver", ctypes.c_int), ("precision", ctypes.c_int),
+                ("mg_smooth", ctypes.c_int), ("mg_coarsest", ctypes.c_int), ("inner_tolerance", ctypes.c_double),
+                ("iterations_per_sync", ctypes.c_int)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("outer_iterations", ctypes.c_int), ("converged", ctypes.c_int),
+                ("reresid", ctypes.c_double), ("true_resid_inf", ctypes.c_double),
+                ("true_resid_l2", ctypes.c_double), ("b_inf", ctypes.c_double), ("unknowns", ctypes.c_longlong),
+                ("ms_assemble", ctypes.c_float), ("ms_solve", ctypes.c_float), ("ms_update", ctypes.c_float),
+                ("ms_total", ctypes.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class GBPError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"gbp error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+EXPORTED = ["gbp_params_default", "gbp_create", "gbp_destroy", "gbp_scene_create", "gbp_scene_destroy",
+            "gbp_scene_device_bytes", "gbp_scene_set_target_volume", "gbp_project", "gbp_project_device",
+            "gbp_debug_assemble", "gbp_launch_count", "gbp_strerror"]
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def load_library():
+    """Loads libgbp.so (building it first if sources are newer is the
+    caller's job: ``python -m shiokaze_gb300.build``). Raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is not built; run `python -m shiokaze_gb300.build` "
+                          "(there is no CPU fallback)")
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, fp, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_double)
+    lib.gbp_params_default.argtypes = [ctypes.POINTER(Params)]
+    lib.gbp_params_default.restype = None
+    lib.gbp_create.argtypes = [ctypes.c_int, ctypes.POINTER(vp)]
+    lib.gbp_destroy.argtypes = [vp]
+    lib.gbp_destroy.restype = None
+    lib.gbp_scene_create.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                     ctypes.POINTER(vp)]
+    lib.gbp_scene_destroy.argtypes = [vp]
+    lib.gbp_scene_destroy.restype = None
+    lib.gbp_scene_device_bytes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(Params)]
+    lib.gbp_scene_device_bytes.restype = ctypes.c_size_t
+    lib.gbp_scene_set_target_volume.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+    lib.gbp_project.argtypes = [vp, ctypes.c_double, fp, fp, fp, fp, fp, ctypes.POINTER(Params), fp,
+                                ctypes.POINTER(Stats)]
+    lib.gbp_project_device.argtypes = [vp, ctypes.c_double, vp, vp, vp, vp, vp, ctypes.POINTER(Params), vp,
+                                       ctypes.POINTER(Stats), vp]
+    lib.gbp_debug_assemble.argtypes = [vp, ctypes.c_double, fp, fp, fp, fp, fp, ctypes.POINTER(Params), dp, dp, dp,
+                                       dp, dp]
+    lib.gbp_launch_count.argtypes = [vp]
+    lib.gbp_launch_count.restype = ctypes.c_longlong
+    lib.gbp_strerror.argtypes = [ctypes.c_int]
+    lib.gbp_strerror.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def check(rc: int, allow=(GBP_OK,)):
+    if rc not in allow:
+        raise GBPError(rc, load_library().gbp_strerror(rc).decode())
+    return rc
+
+
+_KEYMAP = {
+    "Residual": ("residual", float), "MaxIterations": ("max_iterations", int), "WarmStart": ("warm_start", int),
+    "EpsFluid": ("eps_fluid", float), "EpsSolid": ("eps_solid", float),
+    "SecondOrderAccurateFluid": ("second_order_fluid", int), "SecondOrderAccurateSolid": ("second_order_solid", int),
+    "Gain": ("gain", float), "MGSmooth": ("mg_smooth", int), "MGCoarsest": ("mg_coarsest", int),
+    "InnerTolerance": ("inner_tolerance", float), "IterationsPerSync": ("iterations_per_sync", int),
+}
+
+
+def make_params(**keys) -> Params:
+    """Params from the reference's configuration keys (see module docstring)."""
+    p = Params()
+    load_library().gbp_params_default(ctypes.byref(p))
+    for k, val in keys.items():
+        if k == "Solver":
+            p.solver = {"cg": SOLVER_CG, "pcg": SOLVER_CG, "mgpcg": SOLVER_MGPCG}[str(val).lower()]
+        elif k == "Precision":
+            p.precision = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED}[str(val).lower()]
+        elif k in _KEYMAP:
+            name, conv = _KEYMAP[k]
+            if conv is int and isinstance(val, str):
+                val = val.lower() in ("yes", "true", "1")
+            setattr(p, name, conv(val))
+        else:
+            raise KeyError(f"unknown configuration key {k}")
+    return p
+
+
+class Context:
+    """A CUDA device context (stream, events) of libgbp."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        self.handle = ctypes.c_void_p()
+        check(self.lib.gbp_create(device, ctypes.byref(self.handle)))
+
+    def close(self):
+        if self.handle:
+            self.lib.gbp_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def launches(self) -> int:
+        return int(self.lib.gbp_launch_count(self.handle))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _host_f32(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class _MacProject:
+    dim = 3
+
+    def __init__(self, nx, ny, nz, dx, context: Context | None = None, **config):
+        self.ctx = context or default_context()
+        self.lib = self.ctx.lib
+        self.nx, self.ny, self.nz = nx, ny, (nz if self.dim == 3 else 1)
+        self.dx = dx
+        self.config = dict(config)
+        self.params = make_params(**self.config)
+        self.scene = ctypes.c_void_p()
+        check(self.lib.gbp_scene_create(self.ctx.handle, self.dim, nx, ny, self.nz, dx, ctypes.byref(self.scene)))
+        self.pressure = None
+        self.stats = Stats()
+
+    def configure(self, **config):
+        """Sets configuration keys (merged with the ones already set)."""
+        self.config.update(config)
+        self.params = make_params(**self.config)
+        return self
+
+    def close(self):
+        if self.scene:
+            self.lib.gbp_scene_destroy(self.scene)
+            self.scene = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_target_volume(self, current_volume: float, target_volume: float):
+        check(self.lib.gbp_scene_set_target_volume(self.scene, current_volume, target_volume))
+
+    def get_pressure(self):
+        return self.pressure
+
+    def device_bytes(self) -> int:
+        return int(self.lib.gbp_scene_device_bytes(self.dim, self.nx, self.ny, self.nz, ctypes.byref(self.params)))
+
+    def project(self, dt, velocity, solid, fluid, pressure_out=None, stream=None):
+        """Projects ``velocity`` (tuple of face arrays) in place. numpy arrays
+        go through the host call; torch CUDA tensors through the device call.
+        Returns the status code (GBP_OK, or GBP_ERR_NOT_CONVERGED /
+        GBP_ERR_NAN, after which the last iterate was still applied, as in
+        the reference)."""
+        comps = list(velocity) + [None] * (3 - len(velocity))
+        u, v, w = comps[0], comps[1], comps[2] if self.dim == 3 else None
+        if _is_torch_cuda(u):
+            import torch
+            if pressure_out is None:
+                if self.pressure is None or not _is_torch_cuda(self.pressure):
+                    self.pressure = torch.empty((self.nz, self.ny, self.nx) if self.dim == 3 else (self.ny, self.nx),
+                                                dtype=torch.float32, device=u.device)
+                pressure_out = self.pressure
+            else:
+                self.pressure = pressure_out
+            for t in (u, v, w, solid, fluid, pressure_out):
+                if t is not None:
+                    assert t.dtype == torch.float32 and t.is_contiguous(), "device arrays must be contiguous float32"
+            st = stream if stream is not None else torch.cuda.current_stream(u.device).cuda_stream
+            rc = self.lib.gbp_project_device(self.scene, dt, solid.data_ptr(), fluid.data_ptr(), u.data_ptr(),
+                                             v.data_ptr(), w.data_ptr() if w is not None else None, ctypes.byref(self.params),
+                                             pressure_out.data_ptr(), ctypes.byref(self.stats), ctypes.c_void_p(st))
+            return check(rc, (GBP_OK, GBP_ERR_NOT_CONVERGED, GBP_ERR_NAN))
+        arrs = []
+        for a in (u, v, w):
+            if a is None:
+                arrs.append((None, None))
+            else:
+                if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
+                    raise TypeError("host velocity components must be contiguous float32 numpy arrays (updated in place)")
+                arrs.append((a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        solid_a, solid_p = _host_f32(solid)
+        fluid_a, fluid_p = _host_f32(fluid)
+        if self.pressure is None or not isinstance(self.pressure, np.ndarray):
+            self.pressure = np.zeros(fluid_a.shape, np.float32)
+        pp = self.pressure.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        rc = self.lib.gbp_project(self.scene, dt, solid_p, fluid_p, arrs[0][1], arrs[1][1], arrs[2][1],
+                                  ctypes.byref(self.params), pp, ctypes.byref(self.stats))
+        return check(rc, (GBP_OK, GBP_ERR_NOT_CONVERGED, GBP_ERR_NAN))
+
+    def debug_assemble(self, dt, velocity, solid, fluid):
+        """Operator and right-hand side as assembled on the device."""
+        comps = list(velocity) + [None] * (3 - len(velocity))
+        u, up = _host_f32(comps[0])
+        v, vp = _host_f32(comps[1])
+        w, wp = (None, None) if self.dim == 2 else _host_f32(comps[2])
+        s, sp = _host_f32(solid)
+        f, fp = _host_f32(fluid)
+        out = [np.zeros(f.shape, np.float64) for _ in range(5)]
+        ptrs = [o.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for o in out]
+        if self.dim == 2:
+            ptrs[3] = None
+        check(self.lib.gbp_debug_assemble(self.scene, dt, sp, fp, up, vp, wp, ctypes.byref(self.params), *ptrs))
+        return dict(zip(["diag", "cpx", "cpy", "cpz", "b"], out))
+
+
+def _is_torch_cuda(a) -> bool:
+    return type(a).__module__.startswith("torch") and getattr(a, "is_cuda", False)
+
+
+class MacProject3(_MacProject):
+    """macproject3_interface on the GPU (3D)."""
+    dim = 3
+
+
+class MacProject2(_MacProject):
+    """macproject2_interface on the GPU (2D)."""
+    dim = 2
+
+    def __init__(self, nx, ny, dx, context: Context | None = None, **config):
+        super().__init__(nx, ny, 1, dx, context, **config)
+
+
+def projector_for(scene, context: Context | None = None, **config):
+    """A projector shaped for a ``shiokaze_gb300.scenes.Scene``."""
+    if scene.dim == 3:
+        return MacProject3(scene.nx, scene.ny, scene.nz, scene.dx, context, **config)
+    return MacProject2(scene.nx, scene.ny, scene.dx, context, **config)

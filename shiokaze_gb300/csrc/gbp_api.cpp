@@ -1,0 +1,386 @@
+// gbp_api.cpp -- the C ABI of libgbp (include/gbp.h): contexts, scenes and
+// the projection call that sequences the device kernels.
+//
+// One projection (replacing macpressuresolver3::project,
+// src/projection/macpressuresolver3.cpp:50-272) is, on the scene's stream:
+//   assemble   face fractions, labels, operator, right-hand side
+//   solve      CG or MGPCG (FP64 or mixed), iterations captured in a CUDA
+//              graph and replayed in chunks; the host reads the device's
+//              stop flag between chunks
+//   pressure   float pressure (+ warm-start copy)
+//   velocity   pressure-gradient update of every face
+#include "gbp.h"
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "gbp_kernels.h"
+#include "gbp_solver.h"
+
+using namespace gbp;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define GBP_CUDA(call)                                                                                 \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess) {                                                                       \
+            return fail(e_ == cudaErrorMemoryAllocation ? GBP_ERR_OUT_OF_MEMORY : GBP_ERR_CUDA,        \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                          \
+        }                                                                                              \
+    } while (0)
+
+}  // namespace
+
+struct gbp_ctx {
+    int device = 0;
+    int sm_count = 0;
+    int grid_blocks = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    long long launches = 0;
+};
+
+struct gbp_scene {
+    gbp_ctx *ctx = nullptr;
+    Grid g{};
+    double dx = 0.0;
+    // staging for the host-array call
+    float *d_solid = nullptr, *d_fluid = nullptr, *d_u = nullptr, *d_v = nullptr, *d_w = nullptr,
+          *d_p = nullptr;
+    // volume correction state (macpressuresolver3.cpp:316-318)
+    double current_volume = 0.0, target_volume = 0.0, y_prev = 0.0;
+    Solver *solver = nullptr;
+};
+
+extern "C" {
+
+void gbp_params_default(gbp_params *p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->residual = 1e-4;
+    p->max_iterations = 30000;
+    p->warm_start = 0;
+    p->eps_fluid = 1e-2;
+    p->eps_solid = 1e-2;
+    p->second_order_fluid = 1;
+    p->second_order_solid = 1;
+    p->gain = 1.0;
+    p->solver = GBP_SOLVER_CG;
+    p->precision = GBP_PRECISION_FP64;
+    p->mg_smooth = 1;
+    p->mg_coarsest = 8;
+    p->inner_tolerance = 1e-3;
+    p->iterations_per_sync = 16;
+}
+
+const char *gbp_strerror(int status) {
+    switch (status) {
+    case GBP_OK: return "ok";
+    case GBP_ERR_INVALID_ARGUMENT: return g_last_error.empty() ? "invalid argument" : g_last_error.c_str();
+    case GBP_ERR_CUDA: return g_last_error.empty() ? "CUDA error" : g_last_error.c_str();
+    case GBP_ERR_OUT_OF_MEMORY: return g_last_error.empty() ? "out of device memory" : g_last_error.c_str();
+    case GBP_ERR_NOT_CONVERGED: return "linear solve stopped at max_iterations";
+    case GBP_ERR_NAN: return "linear solve broke down (NaN or zero curvature)";
+    case GBP_ERR_NO_DEVICE: return g_last_error.empty() ? "no CUDA device" : g_last_error.c_str();
+    case GBP_ERR_BUDGET: return "device memory budget exceeded";
+    case GBP_ERR_TIMEOUT: return "device wait timed out";
+    default: return "unknown status";
+    }
+}
+
+int gbp_create(int device, gbp_ctx **out) {
+    if (!out) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_create: out is NULL");
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) {
+        cudaGetLastError();
+        return fail(GBP_ERR_NO_DEVICE, "gbp_create: CUDA device " + std::to_string(device) + " not available");
+    }
+    GBP_CUDA(cudaSetDevice(device));
+    auto *c = new (std::nothrow) gbp_ctx();
+    if (!c) return fail(GBP_ERR_OUT_OF_MEMORY, "gbp_create: host allocation");
+    c->device = device;
+    cudaDeviceProp prop;
+    GBP_CUDA(cudaGetDeviceProperties(&prop, device));
+    c->sm_count = prop.multiProcessorCount;
+    c->grid_blocks = c->sm_count * 4;
+    if (c->grid_blocks > MAX_GRID) c->grid_blocks = MAX_GRID;
+    GBP_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    for (auto &e : c->ev) GBP_CUDA(cudaEventCreate(&e));
+    *out = c;
+    return GBP_OK;
+}
+
+void gbp_destroy(gbp_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+long long gbp_launch_count(gbp_ctx *c) { return c ? c->launches : 0; }
+
+size_t gbp_scene_device_bytes(int dim, int nx, int ny, int nz, const gbp_params *params) {
+    gbp_params p;
+    gbp_params_default(&p);
+    if (params) p = *params;
+    Grid g = make_grid(dim, nx, ny, nz);
+    size_t cells = (size_t)g.ncell;
+    size_t nodes = (size_t)(nx + 1) * (ny + 1) * (dim == 3 ? nz + 1 : 1);
+    size_t faces = (size_t)(nx + 1) * ny * g.nz + (size_t)nx * (ny + 1) * g.nz + (dim == 3 ? (size_t)nx * ny * (nz + 1) : 0);
+    size_t staging = 4 * (nodes + cells + faces + cells);
+    return staging + solver_device_bytes(g, p) + sizeof(Scalars) + sizeof(Partials);
+}
+
+int gbp_scene_create(gbp_ctx *c, int dim, int nx, int ny, int nz, double dx, gbp_scene **out) {
+    if (!c || !out) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_scene_create: NULL argument");
+    *out = nullptr;
+    if ((dim != 2 && dim != 3) || nx < 1 || ny < 1 || (dim == 3 && nz < 1) || !(dx > 0.0))
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_scene_create: bad shape or dx");
+    if ((long long)nx * ny * (dim == 3 ? nz : 1) > (1LL << 31))
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_scene_create: more than 2^31 cells");
+    auto *s = new (std::nothrow) gbp_scene();
+    if (!s) return fail(GBP_ERR_OUT_OF_MEMORY, "gbp_scene_create: host allocation");
+    s->ctx = c;
+    s->g = make_grid(dim, nx, ny, nz);
+    s->dx = dx;
+    s->solver = new (std::nothrow) Solver();
+    if (!s->solver) {
+        delete s;
+        return fail(GBP_ERR_OUT_OF_MEMORY, "gbp_scene_create: host allocation");
+    }
+    *out = s;
+    return GBP_OK;
+}
+
+void gbp_scene_destroy(gbp_scene *s) {
+    if (!s) return;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    for (float *p : {s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, s->d_p})
+        if (p) cudaFree(p);
+    if (s->solver) {
+        s->solver->release();
+        delete s->solver;
+    }
+    delete s;
+}
+
+int gbp_scene_set_target_volume(gbp_scene *s, double current_volume, double target_volume) {
+    if (!s) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_scene_set_target_volume: NULL scene");
+    s->current_volume = current_volume;
+    s->target_volume = target_volume;
+    return GBP_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+size_t n_nodes(const Grid &g) { return (size_t)(g.nx + 1) * (g.ny + 1) * (g.dim == 3 ? g.nz + 1 : 1); }
+size_t n_face(const Grid &g, int d) {
+    return (size_t)(g.nx + (d == 0)) * (g.ny + (d == 1)) * (g.dim == 3 ? g.nz + (d == 2) : 1);
+}
+
+int ensure_staging(gbp_scene *s) {
+    const Grid &g = s->g;
+    if (!s->d_solid) GBP_CUDA(cudaMalloc(&s->d_solid, 4 * n_nodes(g)));
+    if (!s->d_fluid) GBP_CUDA(cudaMalloc(&s->d_fluid, 4 * (size_t)g.ncell));
+    if (!s->d_u) GBP_CUDA(cudaMalloc(&s->d_u, 4 * n_face(g, 0)));
+    if (!s->d_v) GBP_CUDA(cudaMalloc(&s->d_v, 4 * n_face(g, 1)));
+    if (g.dim == 3 && !s->d_w) GBP_CUDA(cudaMalloc(&s->d_w, 4 * n_face(g, 2)));
+    if (!s->d_p) GBP_CUDA(cudaMalloc(&s->d_p, 4 * (size_t)g.ncell));
+    return GBP_OK;
+}
+
+// Volume-correction constant (macpressuresolver3.cpp:204-217); advances the
+// controller's integral state once per projection.
+double volume_correction(gbp_scene *s, double dt, const gbp_params &p) {
+    if (!(p.gain && s->target_volume)) return 0.0;
+    double x = (s->current_volume - s->target_volume) / s->target_volume;
+    double y = s->y_prev + x * dt;
+    s->y_prev = y;
+    double kp = p.gain * 2.3 / (25.0 * 0.01);
+    double ki = kp * kp / 16.0;
+    return -(kp * x + ki * y) / (x + 1.0);
+}
+
+int validate(const gbp_params &p) {
+    if (!(p.residual >= 0.0) || p.max_iterations < 0 || !(p.eps_fluid >= 0.0) || !(p.eps_solid >= 0.0))
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_params: negative residual, eps or max_iterations");
+    if (p.solver != GBP_SOLVER_CG && p.solver != GBP_SOLVER_MGPCG)
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_params: unknown solver");
+    if (p.precision != GBP_PRECISION_FP64 && p.precision != GBP_PRECISION_MIXED)
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_params: unknown precision");
+    if (p.precision == GBP_PRECISION_MIXED && p.solver != GBP_SOLVER_MGPCG)
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_params: mixed precision needs the MGPCG solver");
+    return GBP_OK;
+}
+
+int project_device(gbp_scene *s, double dt, const float *solid, const float *fluid, float *u, float *v, float *w,
+                   const gbp_params &p, float *pressure, gbp_stats *stats, cudaStream_t stream) {
+    gbp_ctx *c = s->ctx;
+    const Grid &g = s->g;
+    int rc = validate(p);
+    if (rc) return rc;
+    if (!solid || !fluid || !u || !v || (g.dim == 3 && !w) || !pressure)
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_project: NULL array");
+    GBP_CUDA(cudaSetDevice(c->device));
+    rc = s->solver->prepare(g, p);
+    if (rc) return fail(rc, s->solver->error());
+    SolverState &st = s->solver->state();
+
+    SetupParams sp{p.eps_solid, p.eps_fluid, p.second_order_solid, p.second_order_fluid, 0.0};
+    sp.rhs_correct = volume_correction(s, dt, p);
+
+    GBP_CUDA(cudaEventRecord(c->ev[0], stream));
+    GBP_CUDA(cudaMemsetAsync(st.sc, 0, sizeof(Scalars), stream));
+    GBP_CUDA(launch_assemble(g, dt, s->dx, sp, solid, fluid, u, v, w, st.diag, st.cx, st.cy, st.cz, st.b, st.sc,
+                             c->grid_blocks, stream));
+    c->launches += 1;
+    GBP_CUDA(cudaEventRecord(c->ev[1], stream));
+
+    long long launched = 0;
+    rc = s->solver->solve(g, p, c->grid_blocks, stream, &launched);
+    c->launches += launched;
+    if (rc != GBP_OK && rc != GBP_ERR_NOT_CONVERGED && rc != GBP_ERR_NAN) return fail(rc, s->solver->error());
+    int solve_status = rc;
+    GBP_CUDA(cudaEventRecord(c->ev[2], stream));
+
+    GBP_CUDA(launch_pressure(g, st.diag, st.x, p.warm_start && st.have_prev ? st.prev : nullptr, pressure,
+                             p.warm_start ? st.prev : nullptr, c->grid_blocks, stream));
+    GBP_CUDA(launch_velocity(g, dt, s->dx, sp, solid, fluid, pressure, u, v, w, st.sc, c->grid_blocks, stream));
+    c->launches += 2;
+    if (p.warm_start) st.have_prev = true;
+    GBP_CUDA(cudaEventRecord(c->ev[3], stream));
+    GBP_CUDA(cudaStreamSynchronize(stream));
+
+    if (stats) {
+        Scalars h;
+        GBP_CUDA(cudaMemcpy(&h, st.sc, sizeof(Scalars), cudaMemcpyDeviceToHost));
+        s->solver->fill_stats(h, stats);
+        stats->unknowns = (long long)h.unknowns;
+        cudaEventElapsedTime(&stats->ms_assemble, c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&stats->ms_solve, c->ev[1], c->ev[2]);
+        cudaEventElapsedTime(&stats->ms_update, c->ev[2], c->ev[3]);
+    }
+    return solve_status;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbp_project_device(gbp_scene *s, double dt, const float *solid, const float *fluid, float *u, float *v,
+                       float *w, const gbp_params *params, float *pressure, gbp_stats *stats, void *stream) {
+    if (!s) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_project_device: NULL scene");
+    auto t0 = std::chrono::steady_clock::now();
+    gbp_params p;
+    gbp_params_default(&p);
+    if (params) p = *params;
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
+    if (!stream) {
+        // The caller's work sits on the legacy default stream, which does not
+        // order against the context's non-blocking stream: wait for it.
+        GBP_CUDA(cudaSetDevice(s->ctx->device));
+        GBP_CUDA(cudaEventRecord(s->ctx->ev[0], cudaStreamLegacy));
+        GBP_CUDA(cudaStreamWaitEvent(st, s->ctx->ev[0], 0));
+    }
+    int rc = GBP_OK;
+    if (!pressure) {
+        rc = ensure_staging(s);
+        if (rc) return rc;
+        pressure = s->d_p;
+    }
+    rc = project_device(s, dt, solid, fluid, u, v, w, p, pressure, stats, st);
+    if (stats)
+        stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+int gbp_project(gbp_scene *s, double dt, const float *solid, const float *fluid, float *u, float *v, float *w,
+                const gbp_params *params, float *pressure, gbp_stats *stats) {
+    if (!s) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_project: NULL scene");
+    auto t0 = std::chrono::steady_clock::now();
+    const Grid &g = s->g;
+    if (!solid || !fluid || !u || !v || (g.dim == 3 && !w))
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_project: NULL array");
+    gbp_params p;
+    gbp_params_default(&p);
+    if (params) p = *params;
+    GBP_CUDA(cudaSetDevice(s->ctx->device));
+    int rc = ensure_staging(s);
+    if (rc) return rc;
+    cudaStream_t st = s->ctx->stream;
+    GBP_CUDA(cudaMemcpyAsync(s->d_solid, solid, 4 * n_nodes(g), cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(s->d_fluid, fluid, 4 * (size_t)g.ncell, cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(s->d_u, u, 4 * n_face(g, 0), cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(s->d_v, v, 4 * n_face(g, 1), cudaMemcpyHostToDevice, st));
+    if (g.dim == 3) GBP_CUDA(cudaMemcpyAsync(s->d_w, w, 4 * n_face(g, 2), cudaMemcpyHostToDevice, st));
+    rc = project_device(s, dt, s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, p, s->d_p, stats, st);
+    if (rc != GBP_OK && rc != GBP_ERR_NOT_CONVERGED && rc != GBP_ERR_NAN) return rc;
+    GBP_CUDA(cudaMemcpyAsync(u, s->d_u, 4 * n_face(g, 0), cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaMemcpyAsync(v, s->d_v, 4 * n_face(g, 1), cudaMemcpyDeviceToHost, st));
+    if (g.dim == 3) GBP_CUDA(cudaMemcpyAsync(w, s->d_w, 4 * n_face(g, 2), cudaMemcpyDeviceToHost, st));
+    if (pressure) GBP_CUDA(cudaMemcpyAsync(pressure, s->d_p, 4 * (size_t)g.ncell, cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    if (stats)
+        stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+int gbp_debug_assemble(gbp_scene *s, double dt, const float *solid, const float *fluid, const float *u,
+                       const float *v, const float *w, const gbp_params *params, double *diag, double *cx,
+                       double *cy, double *cz, double *b) {
+    if (!s || !solid || !fluid || !u || !v || !diag || !cx || !cy || !b)
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_debug_assemble: NULL argument");
+    const Grid &g = s->g;
+    if (g.dim == 3 && (!w || !cz)) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_debug_assemble: NULL w/cz in 3D");
+    gbp_params p;
+    gbp_params_default(&p);
+    if (params) p = *params;
+    int rc = validate(p);
+    if (rc) return rc;
+    GBP_CUDA(cudaSetDevice(s->ctx->device));
+    rc = ensure_staging(s);
+    if (rc) return rc;
+    rc = s->solver->prepare(g, p);
+    if (rc) return fail(rc, s->solver->error());
+    SolverState &st = s->solver->state();
+    cudaStream_t str = s->ctx->stream;
+    GBP_CUDA(cudaMemcpyAsync(s->d_solid, solid, 4 * n_nodes(g), cudaMemcpyHostToDevice, str));
+    GBP_CUDA(cudaMemcpyAsync(s->d_fluid, fluid, 4 * (size_t)g.ncell, cudaMemcpyHostToDevice, str));
+    GBP_CUDA(cudaMemcpyAsync(s->d_u, u, 4 * n_face(g, 0), cudaMemcpyHostToDevice, str));
+    GBP_CUDA(cudaMemcpyAsync(s->d_v, v, 4 * n_face(g, 1), cudaMemcpyHostToDevice, str));
+    if (g.dim == 3) GBP_CUDA(cudaMemcpyAsync(s->d_w, w, 4 * n_face(g, 2), cudaMemcpyHostToDevice, str));
+    SetupParams sp{p.eps_solid, p.eps_fluid, p.second_order_solid, p.second_order_fluid, 0.0};
+    GBP_CUDA(cudaMemsetAsync(st.sc, 0, sizeof(Scalars), str));
+    GBP_CUDA(launch_assemble(g, dt, s->dx, sp, s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, st.diag, st.cx,
+                             st.cy, st.cz, st.b, st.sc, s->ctx->grid_blocks, str));
+    s->ctx->launches += 1;
+    const size_t bytes = 8 * (size_t)g.ncell;
+    GBP_CUDA(cudaMemcpyAsync(diag, st.diag, bytes, cudaMemcpyDeviceToHost, str));
+    GBP_CUDA(cudaMemcpyAsync(cx, st.cx, bytes, cudaMemcpyDeviceToHost, str));
+    GBP_CUDA(cudaMemcpyAsync(cy, st.cy, bytes, cudaMemcpyDeviceToHost, str));
+    if (g.dim == 3) GBP_CUDA(cudaMemcpyAsync(cz, st.cz, bytes, cudaMemcpyDeviceToHost, str));
+    GBP_CUDA(cudaMemcpyAsync(b, st.b, bytes, cudaMemcpyDeviceToHost, str));
+    GBP_CUDA(cudaStreamSynchronize(str));
+    return GBP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,169 @@
+// gbp_internal.cuh -- shared device/host definitions of libgbp.
+//
+// Data layout in HBM (one scene): every per-cell array is a dense nx*ny*nz
+// array, x fastest. The operator is stored matrix-free as four per-cell
+// arrays: diag (0 off the unknowns) and the coupling weight of the cell's
+// +x/+y/+z face, cx/cy/cz, which is the negated off-diagonal
+// -A[c][c+e_d] and is 0 unless both cells are unknowns. Vectors are dense
+// with 0 off the unknowns, so A*x is the 7-point (5-point in 2D) stencil
+//   (A x)_c = diag_c x_c - sum_d (cd_c x_{c+e_d} + cd_{c-e_d} x_{c-e_d}).
+//
+// Work is split into tiles of 32 (x) by 8 (y) by TZ (z) cells. A launch runs
+// a fixed number of blocks (a multiple of the SM count); block b handles
+// tiles b, b+G, b+2G, ... in order. Reductions keep one partial per block
+// and the last block to finish sums them in block order, so every result is
+// bitwise reproducible run to run.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbp {
+
+constexpr int TILE_X = 32;
+constexpr int TILE_Y = 8;
+constexpr int BLOCK_THREADS = TILE_X * TILE_Y;  // 256
+constexpr int MAX_GRID = 152 * 8;               // partial-array capacity
+
+struct Grid {
+    int nx, ny, nz;   // cells (nz == 1 in 2D)
+    int dim;          // 2 or 3
+    int tz;           // tile depth in z
+    int ntx, nty, ntz;
+    long long ntiles;
+    long long ncell;
+};
+
+inline Grid make_grid(int dim, int nx, int ny, int nz) {
+    Grid g;
+    g.dim = dim;
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = dim == 3 ? nz : 1;
+    g.tz = g.nz == 1 ? 1 : 4;
+    g.ntx = (nx + TILE_X - 1) / TILE_X;
+    g.nty = (ny + TILE_Y - 1) / TILE_Y;
+    g.ntz = (g.nz + g.tz - 1) / g.tz;
+    g.ntiles = (long long)g.ntx * g.nty * g.ntz;
+    g.ncell = (long long)nx * ny * g.nz;
+    return g;
+}
+
+// Reduction scratch of one solve: per-block partials and scalars that the
+// last block of a launch writes. Lives in device memory.
+struct Scalars {
+    double rho;      // r . z of the current iterate
+    double alpha;
+    double beta;
+    double pap;      // p . A p
+    double tol;      // absolute stopping threshold on |r|_inf
+    double res0;     // |r0|_inf
+    double res;      // |r|_inf of the latest iterate
+    double r2;       // r . r of the latest iterate (for reporting)
+    double aux[4];
+    int iter;        // completed iterations
+    int done;        // nonzero once the solve has stopped
+    int status;      // 0 running, 1 converged, 2 max iterations, 3 breakdown (0/0 or NaN)
+    int max_iter;
+    int fluid_exists;
+    int pad;
+    unsigned long long unknowns;
+    unsigned long long bits_max;  // max of non-negative doubles through their bit patterns
+    unsigned int counter[8];      // last-block tickets, one per reduction site
+};
+
+struct Partials {
+    double a[MAX_GRID];
+    double b[MAX_GRID];
+    double c[MAX_GRID];
+};
+
+#ifdef __CUDACC__
+
+__device__ __forceinline__ long long cell_index(const Grid &g, int i, int j, int k) {
+    return (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * k);
+}
+
+__device__ __forceinline__ void tile_origin(const Grid &g, long long t, int &i0, int &j0, int &k0) {
+    long long tx = t % g.ntx;
+    long long r = t / g.ntx;
+    long long ty = r % g.nty;
+    long long tk = r / g.nty;
+    i0 = (int)tx * TILE_X;
+    j0 = (int)ty * TILE_Y;
+    k0 = (int)tk * g.tz;
+}
+
+template <class T> __device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <class T> __device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide sum in a fixed order; result valid in thread 0.
+template <class T> __device__ __forceinline__ T block_sum(T v, T *sh) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    T r = 0;
+    if (wid == 0) {
+        r = lane < (int)(blockDim.x >> 5) ? sh[lane] : T(0);
+        r = warp_sum(r);
+    }
+    return r;
+}
+
+template <class T> __device__ __forceinline__ T block_max(T v, T *sh) {
+    v = warp_max(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    T r = 0;
+    if (wid == 0) {
+        r = lane < (int)(blockDim.x >> 5) ? sh[lane] : T(0);
+        r = warp_max(r);
+    }
+    return r;
+}
+
+// Publishes this block's partial(s) and returns true in every thread of the
+// block that finished last. Must be called by all threads of the block.
+__device__ __forceinline__ bool last_block(unsigned int *counter) {
+    __shared__ bool is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int ticket = atomicAdd(counter, 1u);
+        is_last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (is_last) __threadfence();
+    return is_last;
+}
+
+// Sums partial[0..n) in a fixed order (strided per thread, then the block
+// tree); result valid in thread 0.
+__device__ __forceinline__ double reduce_partials_sum(const double *partial, int n, double *sh) {
+    double v = 0.0;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) v += __ldcg(partial + t);
+    return block_sum(v, sh);
+}
+
+__device__ __forceinline__ double reduce_partials_max(const double *partial, int n, double *sh) {
+    double v = 0.0;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) v = fmax(v, __ldcg(partial + t));
+    return block_max(v, sh);
+}
+
+#endif  // __CUDACC__
+
+}  // namespace gbp

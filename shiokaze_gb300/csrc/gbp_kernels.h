@@ -1,0 +1,46 @@
+// gbp_kernels.h -- host-side launch functions of libgbp's kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gbp_internal.cuh"
+
+namespace gbp {
+
+struct SetupParams {
+    double eps_solid, eps_fluid;
+    int second_order_solid, second_order_fluid;
+    double rhs_correct;  // volume-correction constant added to every row's b
+};
+
+// Operator arrays of one grid level, in precision T.
+template <class T> struct Operator {
+    const T *diag, *cx, *cy, *cz;  // cz == cy in 2D (never read)
+};
+
+// ---- setup (setup_kernels.cu) ------------------------------------------------
+cudaError_t launch_assemble(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
+                            const float *fluid, const float *u, const float *v, const float *w, double *diag,
+                            double *cx, double *cy, double *cz, double *b, Scalars *sc, int grid_blocks,
+                            cudaStream_t stream);
+cudaError_t launch_pressure(const Grid &g, const double *diag, const double *x, const double *prev, float *p,
+                            double *keep, int grid_blocks, cudaStream_t stream);
+cudaError_t launch_velocity(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
+                            const float *fluid, const float *p, float *u, float *v, float *w, const Scalars *sc,
+                            int grid_blocks, cudaStream_t stream);
+
+// ---- plain CG in FP64 (cg_kernels.cu) ---------------------------------------
+// r = b - A prev (prev may be NULL), x = 0, s = r; stopping threshold.
+cudaError_t launch_cg_init(const Grid &g, Operator<double> A, const double *b, const double *prev, double *x,
+                           double *r, double *s, Scalars *sc, Partials *pt, double residual, int max_iter,
+                           int grid_blocks, cudaStream_t stream);
+// One CG iteration: z = A s; alpha; x += alpha s; r -= alpha z; stop test;
+// beta; s = r + beta s. Three launches; all return at once after the stop.
+cudaError_t launch_cg_iteration(const Grid &g, Operator<double> A, double *x, double *r, double *s, double *z,
+                                Scalars *sc, Partials *pt, int grid_blocks, cudaStream_t stream);
+// |b - A (x + prev)|_inf and _2, |b - A prev|_2 into sc->aux[0..2].
+cudaError_t launch_true_residual(const Grid &g, Operator<double> A, const double *b, const double *x,
+                                 const double *prev, Scalars *sc, Partials *pt, int grid_blocks,
+                                 cudaStream_t stream);
+
+}  // namespace gbp

@@ -1,0 +1,330 @@
+// setup_kernels.cu -- face fractions, labelling, operator and right-hand
+// side assembly, and the pressure-gradient velocity update.
+//
+// Built with --fmad=false: every expression here rounds like the reference's
+// scalar C++ (no fused multiply-add), so the operator, the right-hand side
+// and the velocity update are bit-identical to the reference's given the
+// same pressure.
+//
+// Algorithmic DRAM bytes per cell (3D): assemble reads fluid (4) + solid
+// nodes (4) + u,v,w (12) and writes diag, cx, cy, cz, b (40) = 60 B;
+// velocity update reads solid (4) + fluid (4) + pressure (4) + u,v,w (12)
+// and writes u,v,w (12) = 36 B.
+#include <cfloat>
+
+#include "gbp_internal.cuh"
+#include "gbp_kernels.h"
+
+namespace gbp {
+namespace {
+
+// utility::fraction, include/shiokaze/utility/utility.h:162-170.
+__device__ double fraction(double phi0, double phi1) {
+    if (phi0 * phi1 >= 0.0) {
+        if (phi0 < 0.0 || phi1 < 0.0) return 1.0;
+        return 0.0;
+    }
+    double mn = phi0 < phi1 ? phi0 : phi1;
+    double d = fabs(phi1 - phi0);
+    return -mn / (d > DBL_MIN ? d : DBL_MIN);
+}
+
+// utility::get_area, utility.h:179-214: area of {phi < 0} in the unit square
+// with corner values v0..v3 at (0,0),(1,0),(1,1),(0,1): the marching-squares
+// polygon (corners inside, then edge crossings, in corner order) and its
+// shoelace area.
+__device__ double solid_area(double v0, double v1, double v2, double v3) {
+    // Uniform squares: no corner inside gives an empty polygon (area 0);
+    // all four inside give the unit square (shoelace sum 2, area 1). Both
+    // are what the general path computes, exactly.
+    if (v0 >= 0.0 && v1 >= 0.0 && v2 >= 0.0 && v3 >= 0.0) return 0.0;
+    if (v0 < 0.0 && v1 < 0.0 && v2 < 0.0 && v3 < 0.0) return 1.0;
+    const double v[4] = {v0, v1, v2, v3};
+    const double qx[4] = {0.0, 1.0, 1.0, 0.0};
+    const double qy[4] = {0.0, 0.0, 1.0, 1.0};
+    double px[8], py[8];
+    int pnum = 0;
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+        const int m = (n + 1) & 3;
+        if (v[n] < 0.0) {
+            px[pnum] = qx[n];
+            py[pnum] = qy[n];
+            pnum++;
+        }
+        if (v[n] * v[m] < 0) {
+            double y0 = v[n], y1 = v[m];
+            if (y0 - y1) {
+                double a = y0 / (y0 - y1);
+                px[pnum] = (1.0 - a) * qx[n] + a * qx[m];
+                py[pnum] = (1.0 - a) * qy[n] + a * qy[m];
+                pnum++;
+            }
+        }
+    }
+    double sum = 0.0;
+    for (int q = 0; q < pnum; ++q) {
+        int r = (q + 1 == pnum) ? 0 : q + 1;
+        sum += px[q] * py[r] - py[q] * px[r];
+    }
+    return 0.5 * sum;
+}
+
+struct FaceParams {
+    double eps_solid, eps_fluid;
+    int second_order_solid, second_order_fluid;
+};
+
+// Open (non-solid) fraction of face (i,j,k) normal to d
+// (src/utility/macutility3.cpp:117-143; 2D macutility2.cpp:100-105).
+// Domain-boundary faces read 0; their value never reaches the outputs.
+__device__ float face_area(const Grid &g, const float *__restrict__ solid, int d, int i, int j, int k,
+                           const FaceParams &fp) {
+    const int p[3] = {i, j, k};
+    const int n[3] = {g.nx, g.ny, g.nz};
+    double area;
+    if (p[d] == 0 || p[d] == n[d]) {
+        area = 0.0;
+    } else if (g.dim == 3) {
+        const long long sx = g.nx + 1, sxy = sx * (g.ny + 1);
+        auto S = [&](int a, int b, int c) { return (double)__ldg(solid + a + sx * b + sxy * c); };
+        double q00, q10, q11, q01;
+        if (d == 0) {
+            q00 = S(i, j, k); q10 = S(i, j + 1, k); q11 = S(i, j + 1, k + 1); q01 = S(i, j, k + 1);
+        } else if (d == 1) {
+            q00 = S(i, j, k); q10 = S(i + 1, j, k); q11 = S(i + 1, j, k + 1); q01 = S(i, j, k + 1);
+        } else {
+            q00 = S(i, j, k); q10 = S(i + 1, j, k); q11 = S(i + 1, j + 1, k); q01 = S(i, j + 1, k);
+        }
+        area = 1.0 - solid_area(q00, q10, q11, q01);
+    } else {
+        const long long sx = g.nx + 1;
+        double s0 = __ldg(solid + i + sx * j);
+        double s1 = d == 0 ? __ldg(solid + i + sx * (j + 1)) : __ldg(solid + (i + 1) + sx * j);
+        area = 1.0 - fraction(s0, s1);
+    }
+    if (area && area < fp.eps_solid) area = fp.eps_solid;
+    float a = (float)area;
+    if (!fp.second_order_solid && a) a = 1.0f;  // macpressuresolver3.cpp:76-80
+    return a;
+}
+
+// Liquid fraction of face (i,j,k) normal to d, between the clamped cells
+// (i,j,k) and (i,j,k)-e_d (macutility3.cpp:178-184). With no fluid anywhere
+// the reference fills every fraction with 1 (macutility3.cpp:190-192).
+__device__ float face_rho(const Grid &g, const float *__restrict__ fluid, int d, int i, int j, int k,
+                          const FaceParams &fp, int fluid_exists) {
+    float r;
+    if (!fluid_exists) {
+        r = 1.0f;
+    } else {
+        int a0 = min(max(i, 0), g.nx - 1), a1 = min(max(j, 0), g.ny - 1), a2 = min(max(k, 0), g.nz - 1);
+        int b0 = min(max(i - (d == 0), 0), g.nx - 1), b1 = min(max(j - (d == 1), 0), g.ny - 1),
+            b2 = min(max(k - (d == 2), 0), g.nz - 1);
+        double f0 = __ldg(fluid + a0 + (long long)g.nx * (a1 + (long long)g.ny * a2));
+        double f1 = __ldg(fluid + b0 + (long long)g.nx * (b1 + (long long)g.ny * b2));
+        double rho = fraction(f0, f1);
+        if (rho && rho < fp.eps_fluid) rho = fp.eps_fluid;
+        r = (float)rho;
+    }
+    if (!fp.second_order_fluid && r) r = 1.0f;  // macpressuresolver3.cpp:70-74
+    return r;
+}
+
+__device__ __forceinline__ long long face_index(const Grid &g, int d, int i, int j, int k) {
+    const long long fx = g.nx + (d == 0), fy = g.ny + (d == 1);
+    return i + fx * (j + fy * (long long)k);
+}
+
+// One thread per cell: labels the cell, assembles its row of the operator
+// and its right-hand side (macpressuresolver3.cpp:121-199,
+// macpressuresolver2.cpp:111-179). A cell is an unknown iff it is fluid and
+// has a fluid in-bounds neighbour across a face with area > 0 and rho > 0;
+// since that neighbour is then an unknown too, the +d coupling of a cell is
+// that face's weight whenever both cells are fluid and the face is open.
+__global__ void __launch_bounds__(BLOCK_THREADS) assemble_kernel(
+    Grid g, double dt, double dx, FaceParams fp, double rhs_correct, const float *__restrict__ solid,
+    const float *__restrict__ fluid, const float *__restrict__ u, const float *__restrict__ v,
+    const float *__restrict__ w, double *__restrict__ diag, double *__restrict__ cx, double *__restrict__ cy,
+    double *__restrict__ cz, double *__restrict__ b, Scalars *sc) {
+    __shared__ unsigned long long sh_count[BLOCK_THREADS / 32];
+    const int tx = threadIdx.x & (TILE_X - 1), ty = threadIdx.x / TILE_X;
+    unsigned long long my_count = 0;
+    int my_fluid = 0;
+    const float *vel[3] = {u, v, w};
+    double *cp[3] = {cx, cy, cz};
+    for (long long t = blockIdx.x; t < g.ntiles; t += gridDim.x) {
+        int i0, j0, k0;
+        tile_origin(g, t, i0, j0, k0);
+        const int i = i0 + tx, j = j0 + ty;
+        if (i >= g.nx || j >= g.ny) continue;
+        for (int kk = 0; kk < g.tz; ++kk) {
+            const int k = k0 + kk;
+            if (k >= g.nz) break;
+            const long long c = cell_index(g, i, j, k);
+            const float fc = __ldg(fluid + c);
+            double dg = 0.0, rhs = 0.0, cpl[3] = {0.0, 0.0, 0.0};
+            bool unknown = false;
+            if (fc < 0.0f) {
+                my_fluid = 1;
+                const int n[3] = {g.nx, g.ny, g.nz};
+                for (int nq = 0; nq < 2 * g.dim; ++nq) {
+                    const int d = nq >> 1;
+                    const bool plus = (nq & 1) == 0;
+                    const int sgn = plus ? 1 : -1;
+                    int q[3] = {i, j, k};
+                    q[d] += sgn;
+                    if (q[d] < 0 || q[d] >= n[d]) continue;
+                    int f[3] = {i, j, k};
+                    if (plus) f[d] += 1;
+                    const double area = face_area(g, solid, d, f[0], f[1], f[2], fp);
+                    const float uf = __ldg(vel[d] + face_index(g, d, f[0], f[1], f[2]));
+                    if (area) {
+                        const double rho = face_rho(g, fluid, d, f[0], f[1], f[2], fp, 1);
+                        if (rho) {
+                            const double value = dt * area / (dx * dx * rho);
+                            if (__ldg(fluid + cell_index(g, q[0], q[1], q[2])) < 0.0f) {
+                                unknown = true;
+                                if (plus) cpl[d] = value;
+                            }
+                            dg += value;
+                        }
+                        if (g.dim == 3) rhs += -sgn * area * (double)uf / dx;
+                    }
+                    if (g.dim == 2) rhs += -sgn * area * (double)uf / dx;
+                }
+            }
+            if (unknown) {
+                my_count++;
+                if (rhs_correct) rhs += rhs_correct;  // macpressuresolver3.cpp:212-214
+            } else {
+                dg = 0.0;
+                rhs = 0.0;
+                cpl[0] = cpl[1] = cpl[2] = 0.0;
+            }
+            diag[c] = dg;
+            b[c] = rhs;
+            for (int d = 0; d < g.dim; ++d) cp[d][c] = cpl[d];
+        }
+    }
+    // unknown count and "any fluid" flag
+    unsigned long long wsum = my_count;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wsum += __shfl_down_sync(0xffffffffu, wsum, o);
+    if ((threadIdx.x & 31) == 0) sh_count[threadIdx.x >> 5] = wsum;
+    int any_fluid = __syncthreads_or(my_fluid);
+    if (threadIdx.x == 0) {
+        unsigned long long s = 0;
+        for (int q = 0; q < BLOCK_THREADS / 32; ++q) s += sh_count[q];
+        if (s) atomicAdd(&sc->unknowns, s);
+        if (any_fluid) atomicOr(&sc->fluid_exists, 1);
+    }
+}
+
+// Float pressure of every cell (0 off the unknowns, macpressuresolver3.cpp:
+// 245-248). With warm start the solve found the correction x to the kept
+// pressure prev; the result is x + prev (:239-242), which is kept again.
+__global__ void __launch_bounds__(BLOCK_THREADS) pressure_kernel(Grid g, const double *__restrict__ diag,
+                                                                 const double *__restrict__ x,
+                                                                 const double *prev, float *__restrict__ p,
+                                                                 double *keep) {
+    const long long n = g.ncell;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        const bool unk = __ldg(diag + c) != 0.0;
+        double xv = unk ? __ldg(x + c) : 0.0;
+        if (prev && unk) xv = xv + prev[c];
+        p[c] = (float)xv;
+        if (keep) keep[c] = xv;
+    }
+}
+
+// Velocity update, one thread per node of the (nx+1)(ny+1)(nz+1) lattice,
+// handling the x-, y- and z-face with that lower corner
+// (macpressuresolver3.cpp:252-268, macpressuresolver2.cpp:221-237). Open
+// faces (area > 0, rho > 0) inside the domain get
+//   u -= (float)(dt * (float)(p_c - p_{c-e_d}) / (rho * dx));
+// domain-boundary faces and closed faces end at 0 (set to 0, or
+// deactivated, which reads back as the background 0).
+__global__ void __launch_bounds__(BLOCK_THREADS) velocity_kernel(Grid g, double dt, double dx, FaceParams fp,
+                                                                 const float *__restrict__ solid,
+                                                                 const float *__restrict__ fluid,
+                                                                 const float *__restrict__ p, float *__restrict__ u,
+                                                                 float *__restrict__ v, float *__restrict__ w,
+                                                                 const Scalars *__restrict__ sc) {
+    const int fluid_exists = sc->fluid_exists;
+    const long long NX = g.nx + 1, NY = g.ny + 1, NZ = g.dim == 3 ? g.nz + 1 : 1;
+    const long long total = NX * NY * NZ;
+    float *vel[3] = {u, v, w};
+    const int n[3] = {g.nx, g.ny, g.nz};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % NX);
+        const int j = (int)((t / NX) % NY);
+        const int k = (int)(t / (NX * NY));
+        const int pi[3] = {i, j, k};
+        for (int d = 0; d < g.dim; ++d) {
+            // face (i,j,k) of dimension d exists if the other indices are cells
+            bool exists = true;
+            for (int e = 0; e < g.dim; ++e)
+                if (e != d && pi[e] >= n[e]) exists = false;
+            if (!exists) continue;
+            const long long f = face_index(g, d, i, j, k);
+            const float area = face_area(g, solid, d, i, j, k, fp);
+            const float rho = face_rho(g, fluid, d, i, j, k, fp, fluid_exists);
+            float out;
+            if (area && rho) {
+                if (pi[d] == 0 || pi[d] == n[d]) {
+                    out = 0.0f;
+                } else {
+                    int m[3] = {i, j, k};
+                    m[d] -= 1;
+                    const float pc = __ldg(p + cell_index(g, i, j, k));
+                    const float pm = __ldg(p + cell_index(g, m[0], m[1], m[2]));
+                    const float dp = pc - pm;
+                    const double val = dt * (double)dp / ((double)rho * dx);
+                    out = vel[d][f] - (float)val;
+                }
+            } else {
+                out = 0.0f;
+            }
+            vel[d][f] = out;
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_assemble(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
+                            const float *fluid, const float *u, const float *v, const float *w, double *diag,
+                            double *cx, double *cy, double *cz, double *b, Scalars *sc, int grid_blocks,
+                            cudaStream_t stream) {
+    FaceParams fp{sp.eps_solid, sp.eps_fluid, sp.second_order_solid, sp.second_order_fluid};
+    int blocks = (int)(g.ntiles < grid_blocks ? g.ntiles : grid_blocks);
+    if (blocks < 1) blocks = 1;
+    assemble_kernel<<<blocks, BLOCK_THREADS, 0, stream>>>(g, dt, dx, fp, sp.rhs_correct, solid, fluid, u, v, w, diag,
+                                                          cx, cy, g.dim == 3 ? cz : cy, b, sc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pressure(const Grid &g, const double *diag, const double *x, const double *prev, float *p,
+                            double *keep, int grid_blocks, cudaStream_t stream) {
+    long long need = (g.ncell + BLOCK_THREADS - 1) / BLOCK_THREADS;
+    int blocks = (int)(need < grid_blocks ? need : grid_blocks);
+    if (blocks < 1) blocks = 1;
+    pressure_kernel<<<blocks, BLOCK_THREADS, 0, stream>>>(g, diag, x, prev, p, keep);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_velocity(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
+                            const float *fluid, const float *p, float *u, float *v, float *w, const Scalars *sc,
+                            int grid_blocks, cudaStream_t stream) {
+    FaceParams fp{sp.eps_solid, sp.eps_fluid, sp.second_order_solid, sp.second_order_fluid};
+    long long total = (long long)(g.nx + 1) * (g.ny + 1) * (g.dim == 3 ? g.nz + 1 : 1);
+    long long need = (total + BLOCK_THREADS - 1) / BLOCK_THREADS;
+    int blocks = (int)(need < grid_blocks ? need : grid_blocks);
+    if (blocks < 1) blocks = 1;
+    velocity_kernel<<<blocks, BLOCK_THREADS, 0, stream>>>(g, dt, dx, fp, solid, fluid, p, u, v, w, sc);
+    return cudaGetLastError();
+}
+
+}  // namespace gbp

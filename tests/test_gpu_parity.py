@@ -1,0 +1,122 @@
+"""Parity of the CUDA projection with the reference (GPU tests).
+
+Everything goes through the C ABI of libgbp.so. The checks:
+
+* assembly (labels, operator, right-hand side) is bit-identical to the
+  oracle's, on every golden case and on random scenes;
+* the plain FP64 CG path (the reference's solver) reproduces the reference's
+  golden outputs: the same unknown cells exactly, the CG iteration count
+  within 2 % (+-2), pressure within PRESSURE_RTOL of |p|_inf and projected
+  velocity within VELOCITY_ATOL_REL of |u|_inf. The two CG runs differ only
+  in summation order (the reference sums dot products serially, the GPU in a
+  fixed tree), so their iterates agree to near roundoff;
+* at Residual 1e-12 the pressures agree to float rounding (TIGHT_RTOL).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from golden_io import Case, case_names
+from gpu_util import config_from, rel_inf, run_case_gpu
+from shiokaze_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+PRESSURE_RTOL = 1e-5      # |p_gpu - p_ref|_inf / |p_ref|_inf at Residual 1e-6
+VELOCITY_ATOL_REL = 1e-5  # |u_gpu - u_ref|_inf / |u_ref|_inf at Residual 1e-6
+TIGHT_RTOL = 2e-6         # the same at Residual 1e-12 (p is stored as float)
+
+
+@pytest.fixture(scope="module")
+def gb():
+    import shiokaze_gb300 as gb
+    gb.load_library()
+    return gb
+
+
+def _assert_assembly_equal(gb, sc_like, dt, solid, fluid, u, v, w, params):
+    pj = gb.projector_for(sc_like, **config_from(params))
+    vel = (u, v, w) if sc_like.dim == 3 else (u, v)
+    got = pj.debug_assemble(dt, vel, solid, fluid)
+    pj.close()
+    port = oracle.PortProjector(sc_like.dim, sc_like.nx, sc_like.ny, sc_like.nz, sc_like.dx, **params)
+    want = port.assemble(dt, solid, fluid, u, v, w)
+    port.close()
+    keys = ["diag", "cpx", "cpy", "b"] + (["cpz"] if sc_like.dim == 3 else [])
+    for k in keys:
+        assert np.array_equal(got[k], want[k]), f"{k} differs: max {np.max(np.abs(got[k] - want[k]))}"
+    assert np.array_equal(got["diag"] != 0, want["index"] >= 0)
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_assembly_bit_exact_on_fixtures(gb, name):
+    c = Case(name)
+    u, v, w = c.inputs[0]
+    params = {k: v_ for k, v_ in c.params.items() if k != "warm_start"}
+    _assert_assembly_equal(gb, c, c.dt, c.solid, c.fluid, u, v, w, params)
+
+
+@pytest.mark.parametrize("seed", [31, 32, 33])
+def test_assembly_bit_exact_random(gb, seed):
+    rng = np.random.default_rng(seed)
+    n = tuple(int(x) for x in rng.integers(20, 70, 3))
+    sc = scenes.liquid3(n, seed=seed, pool=float(rng.uniform(0.15, 0.6)),
+                        solid_r=float(rng.uniform(0.05, 0.2)))
+    _assert_assembly_equal(gb, sc, sc.dt, sc.solid, sc.fluid, sc.u, sc.v, sc.w, {})
+
+
+def test_assembly_bit_exact_2d_and_smoke(gb):
+    sc = scenes.liquid2((96, 72), seed=5)
+    _assert_assembly_equal(gb, sc, sc.dt, sc.solid, sc.fluid, sc.u, sc.v, None, {})
+    sc = scenes.smoke3((40, 36, 28), seed=6)
+    _assert_assembly_equal(gb, sc, sc.dt, sc.solid, sc.fluid, sc.u, sc.v, sc.w, {})
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_cg_matches_reference_fixture(gb, name):
+    c = Case(name)
+    p, (u, v, w), stats, statuses = run_case_gpu(c)
+    # the unknown cells are the reference's (pressure is 0 off them)
+    assert stats["unknowns"] == int(c.out_unknown.sum())
+    assert not p[~c.out_unknown].any()
+    tight = c.params.get("residual", 1e-6) < 1e-9
+    rt = TIGHT_RTOL if tight else PRESSURE_RTOL
+    if c.params.get("max_iterations", 30000) < 30000:
+        assert statuses[-1] == gb.GBP_ERR_NOT_CONVERGED
+        assert stats["iterations"] == c.params["max_iterations"]
+    assert rel_inf(p, c.out_pressure) <= rt, rel_inf(p, c.out_pressure)
+    for got, want in ((u, c.out_u), (v, c.out_v), (w, c.out_w)):
+        if want is not None:
+            assert rel_inf(got, want) <= max(rt, VELOCITY_ATOL_REL), rel_inf(got, want)
+    if c.iterations > 0:
+        assert abs(stats["iterations"] - c.iterations) <= max(2, int(0.02 * c.iterations)), \
+            (stats["iterations"], c.iterations)
+
+
+def test_no_fluid(gb):
+    sc = scenes.liquid3(12, seed=12)
+    sc.fluid[...] = np.float32(sc.band)
+    want = oracle.project_scene(sc, "port", residual=1e-6)
+    pj = gb.projector_for(sc, Residual=1e-6)
+    u, v, w = sc.u.copy(), sc.v.copy(), sc.w.copy()
+    assert pj.project(sc.dt, (u, v, w), sc.solid, sc.fluid) == gb.GBP_OK
+    assert pj.stats.unknowns == 0
+    assert np.array_equal(u, want.u) and np.array_equal(v, want.v) and np.array_equal(w, want.w)
+    assert not pj.get_pressure().any()
+
+
+def test_reference_workload_128_divergence(gb):
+    """The 3D liquid workload at full size (128^3): pressure and velocity
+    against the oracle, and the divergence left after projection."""
+    sc = scenes.liquid3(128, seed=2)
+    want = oracle.project_scene(sc, "port", residual=1e-6)
+    pj = gb.projector_for(sc, Residual=1e-6)
+    u, v, w = sc.u.copy(), sc.v.copy(), sc.w.copy()
+    assert pj.project(sc.dt, (u, v, w), sc.solid, sc.fluid) == gb.GBP_OK
+    p = pj.get_pressure()
+    assert pj.stats.unknowns == int(want.unknown.sum())
+    assert rel_inf(p, want.pressure) <= 1e-4
+    assert rel_inf(w, want.w) <= 1e-4
+    assert abs(pj.stats.iterations - want.iterations) <= max(3, int(0.03 * want.iterations))
+    assert pj.stats.reresid <= 1e-6
+    assert pj.stats.true_resid_inf <= 2e-6
