@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 pressure projection.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbp|reference]
+                    [--workload liquid3_128|smoke3_256|liquid2_128]
+                    [--solver cg|mgpcg] [--precision fp64|mixed]
+
+A step is one projection (face fractions, labelling, operator and
+right-hand side assembly, the solve to a relative residual of 1e-6, the
+pressure-gradient velocity update) of one synthetic scene. The default
+workload is the 3D liquid scene at 128^3 (solid sphere, pool and drop, face
+velocities N(0, 0.2^2) plus gravity over dt = 1/60). Inputs are seeded
+synthetic data with the shapes and value distributions of that workload.
+
+Prints one JSON line. `value` is solves/s over all ranks with inputs resident
+in HBM (the velocity is reset from a device copy before each step, inside
+the timed region); `e2e` is the same through the host-array C ABI call
+(gbp_project: host->device copies of the inputs and device->host copies of
+the projected velocity and pressure inside the timing). `roofline` times the
+dominant kernel alone with CUDA events. `cpu_baseline` is the oracle's CPU
+projection of the same scene on this host.
+
+--impl reference times the reference's CPU implementation of the path on
+the host cores instead: the reference built from its sources
+(oracle/_ref) where it is present, else the oracle's C restatement.
+Multi-GPU (torchrun): independent replicas, one per rank, no collective on
+the data path ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "liquid3_128": dict(kind="liquid3", n=128, desc="3D liquid 128^3, solid sphere r=0.12, pool y<0.35 + drop r=0.18"),
+    "smoke3_256": dict(kind="smoke3", n=256, desc="3D smoke 256^3, all fluid, solid cylinder r=0.1 along z"),
+    "liquid2_128": dict(kind="liquid2", n=128, desc="2D liquid 128^2, pool y<0.3 + circle r=0.15"),
+}
+METRIC = "3D pressure solves/s at 1e-6 resid"
+L2_BYTES = 129 * 2 ** 20
+REFERENCE_BUDGET_S = 150.0
+
+
+def make_scene(name):
+    from shiokaze_gb300 import scenes
+    w = WORKLOADS[name]
+    if w["kind"] == "liquid3":
+        return scenes.liquid3(w["n"], seed=2)
+    if w["kind"] == "smoke3":
+        return scenes.smoke3(w["n"], seed=3)
+    return scenes.liquid2(w["n"], seed=1)
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[2:6]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_gbs():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def committed_traffic(workload, kernel):
+    """DRAM bytes per launch of `kernel` on `workload` from the committed ncu
+    summary (profiles/traffic.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            t = json.load(f)
+        return t.get(workload, {}).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline(scene, solver_desc):
+    """The oracle's projection of the same scene on this host (one solve)."""
+    import oracle
+    t0 = time.perf_counter()
+    r = oracle.project_scene(scene, "port", residual=1e-6)
+    dt = time.perf_counter() - t0
+    return {"value": 1.0 / dt, "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": f"one full projection of the same scene by the oracle's C restatement of the reference "
+                      f"(plain CG to 1e-6, {r.iterations} iterations, single thread), {dt:.1f} s",
+            "seconds_per_solve": dt, "iterations": r.iterations}
+
+
+def run_gbp(args):
+    import torch
+    import shiokaze_gb300 as gb
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    scene = make_scene(args.workload)
+    ctx = gb.Context(local)
+    cfg = dict(Residual=1e-6, Solver=args.solver, Precision=args.precision)
+    pj = gb.projector_for(scene, ctx, **cfg)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+
+    def dev_t(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+    solid, fluid = dev_t(scene.solid), dev_t(scene.fluid)
+    comps0 = [dev_t(a) for a in (scene.u, scene.v, scene.w) if a is not None]
+    comps = [c.clone() for c in comps0]
+    p = torch.zeros(scene.fluid.shape, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    def step():
+        for c, c0 in zip(comps, comps0):
+            c.copy_(c0)
+        rc = pj.project(scene.dt, tuple(comps), solid, fluid, pressure_out=p, stream=sh)
+        if rc != gb.GBP_OK:
+            raise RuntimeError(f"projection returned {rc}: {gb.load_library().gbp_strerror(rc).decode()}")
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    stats_warm = pj.stats.as_dict()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    l0 = ctx.launches()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        ev[0].record(stream)
+        for k in range(args.steps):
+            step()
+            ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    launches = ctx.launches() - l0
+    per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[-1])
+    stats = pj.stats.as_dict()
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms / 1000.0)
+
+    # end to end through the host-array call, pinned host buffers
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float32, pin_memory=True)
+        t.numpy()[...] = a
+        return t
+    h_solid, h_fluid = pinned(scene.solid), pinned(scene.fluid)
+    h0 = [a for a in (scene.u, scene.v, scene.w) if a is not None]
+    hc = [pinned(a) for a in h0]
+    e2e_pj = gb.projector_for(scene, ctx, **cfg)
+    h_p = pinned(np.zeros(scene.fluid.shape, np.float32))
+    e2e_pj.pressure = h_p.numpy()
+    e2e_times = []
+    for k in range(args.warmup + args.steps):
+        for t, a in zip(hc, h0):
+            t.numpy()[...] = a
+        t0 = time.perf_counter()
+        e2e_pj.project(scene.dt, tuple(t.numpy() for t in hc), h_solid.numpy(), h_fluid.numpy())
+        t1 = time.perf_counter()
+        if k >= args.warmup:
+            e2e_times.append(t1 - t0)
+    face_bytes = sum(a.nbytes for a in h0)
+    h2d = scene.solid.nbytes + scene.fluid.nbytes + face_bytes
+    d2h = face_bytes + scene.fluid.nbytes
+    e2e_value = world * len(e2e_times) / sum(e2e_times) if world == 1 else None
+    if world > 1:
+        t = torch.tensor([sum(e2e_times)], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_value = world * len(e2e_times) / float(t.item())
+
+    # roofline: the solve's kernels timed alone
+    kernels = {0: "cg_spmv_kernel", 1: "cg_update_kernel", 2: "cg_direction_kernel"}
+    timed = {}
+    for kid, name in kernels.items():
+        ms, nbytes = pj.bench_kernel(kid, reps=50, stream=sh)
+        timed[name] = (ms, nbytes)
+    dom = max(timed, key=lambda n: timed[n][0])
+    ms, nbytes = timed[dom]
+    peak, peak_kind = measured_peak_gbs()
+    achieved = nbytes / (ms * 1e-3) / 1e9
+    traffic = committed_traffic(args.workload, dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": nbytes, "ms_per_launch": round(ms, 5),
+                "kernels": {n: {"ms": round(t[0], 5), "GBps": round(t[1] / (t[0] * 1e-3) / 1e9, 1)}
+                            for n, t in timed.items()}}
+
+    ms_step = total_ms / args.steps
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic (seeded scene generator, shapes and distributions of the workload)",
+        "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]["desc"],
+                   "grid": [scene.nx, scene.ny, scene.nz], "solver": args.solver, "precision": args.precision,
+                   "residual": 1e-6, "unknowns": stats["unknowns"], "iterations": stats["iterations"],
+                   "parallelism": f"replicas x{world}",
+                   "l2": "no flush: working set above the 129 MB L2 (operator + vectors + inputs)"},
+        "latency_ms": {"p50": round(float(np.percentile(per_step, 50)), 4),
+                       "p99": round(float(np.percentile(per_step, 99)), 4)},
+        "voxel_updates_per_s": round(scene.cells * stats["iterations"] / (stats["ms_solve"] * 1e-3), 1)
+        if stats["ms_solve"] > 0 else None,
+        "phase_ms": {"assemble": round(stats["ms_assemble"], 4), "solve": round(stats["ms_solve"], 4),
+                     "update": round(stats["ms_update"], 4)},
+        "e2e": {"value": round(e2e_value, 3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": roofline,
+        "clocks": clocks,
+        "gpu_launches": int(launches),
+        "residual": {"reresid": stats["reresid"], "true_inf": stats["true_resid_inf"],
+                     "true_l2": stats["true_resid_l2"]},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(scene, args.solver)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return
+    import oracle
+    scene = make_scene(args.workload)
+    kind = "port"
+    if oracle.reference_available():
+        try:
+            oracle._ref_lib()
+            kind = "reference"
+        except OSError:
+            kind = "port"
+    # warm-up on a small scene (loader, page faults); every timed step is one
+    # full projection of the workload. A CPU solve takes tens of seconds, so
+    # the timed steps stop once REFERENCE_BUDGET_S is spent (at least one).
+    from shiokaze_gb300 import scenes
+    small = scenes.liquid3(32, seed=2)
+    for _ in range(max(1, min(args.warmup, 3))):
+        oracle.project_scene(small, kind, residual=1e-6)
+    times, iters = [], []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        r = oracle.project_scene(scene, kind, residual=1e-6)
+        dt = time.perf_counter() - t0
+        times.append(dt)
+        iters.append(r.iterations)
+        if sum(times) > REFERENCE_BUDGET_S:
+            break
+    value = len(times) / sum(times)
+    what = ("the reference's macpressuresolver built from its sources" if kind == "reference"
+            else "the oracle's C restatement of the reference's macpressuresolver (the reference's own build "
+                 "is not on this host)")
+    out = {
+        "metric": METRIC, "value": round(value, 5), "unit": "solves/s", "n_gpus": world, "steps": len(times),
+        "warmup": args.warmup, "ms_per_step": round(1000 * sum(times) / len(times), 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+        "data": "synthetic (seeded scene generator, shapes and distributions of the workload)",
+        "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]["desc"],
+                   "grid": [scene.nx, scene.ny, scene.nz], "solver": "cg (reference pcg, identity preconditioner)",
+                   "residual": 1e-6, "iterations": iters[-1] if iters else None},
+        "cpu_baseline": {"value": round(value, 5), "unit": "solves/s", "cores": 1, "kind": kind,
+                         "sample": f"{len(times)} full projections of the workload by {what}, single thread "
+                                   f"(the reference's CG loop is serial); warm-up on a 32^3 scene"},
+        "e2e": {"value": round(value, 5), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbp", choices=["gbp", "reference"])
+    ap.add_argument("--workload", default="liquid3_128", choices=sorted(WORKLOADS))
+    ap.add_argument("--solver", default="cg", choices=["cg", "mgpcg"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gbp":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gbp(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -142,6 +142,19 @@ int gbp_debug_assemble(gbp_scene *scene, double dt, const float *solid, const fl
                        const float *v, const float *w, const gbp_params *params, double *diag, double *cx,
                        double *cy, double *cz, double *b);
 
+/* Benchmark hook: times `reps` back-to-back launches of one kernel on the
+ * scene's last assembled system with CUDA events on `stream` (NULL = the
+ * context's stream), after one untimed launch. which: GBP_KERNEL_*. Writes
+ * the mean milliseconds per launch and the algorithmic DRAM bytes one launch
+ * moves (compulsory traffic over the dense grid). The scene's solver vectors
+ * are overwritten; the next gbp_project recomputes them. No counterpart in
+ * the reference (its timers are per phase, src/core/scoped_timer.cpp). */
+#define GBP_KERNEL_CG_SPMV 0
+#define GBP_KERNEL_CG_UPDATE 1
+#define GBP_KERNEL_CG_DIRECTION 2
+int gbp_bench_kernel(gbp_scene *scene, int which, int reps, void *stream, float *ms_per_launch,
+                     double *bytes_per_launch);
+
 /* Number of kernel launches this context has issued (graph nodes count one
  * each). */
 long long gbp_launch_count(gbp_ctx *ctx);

@@ -65,7 +65,7 @@ class GBPError(RuntimeError):
 _lib = None
 EXPORTED = ["gbp_params_default", "gbp_create", "gbp_destroy", "gbp_scene_create", "gbp_scene_destroy",
             "gbp_scene_device_bytes", "gbp_scene_set_target_volume", "gbp_project", "gbp_project_device",
-            "gbp_debug_assemble", "gbp_launch_count", "gbp_strerror"]
+            "gbp_debug_assemble", "gbp_bench_kernel", "gbp_launch_count", "gbp_strerror"]
 
 
 def library_path() -> str:
@@ -102,6 +102,8 @@ def load_library():
                                        ctypes.POINTER(Stats), vp]
     lib.gbp_debug_assemble.argtypes = [vp, ctypes.c_double, fp, fp, fp, fp, fp, ctypes.POINTER(Params), dp, dp, dp,
                                        dp, dp]
+    lib.gbp_bench_kernel.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, ctypes.POINTER(ctypes.c_float),
+                                     ctypes.POINTER(ctypes.c_double)]
     lib.gbp_launch_count.argtypes = [vp]
     lib.gbp_launch_count.restype = ctypes.c_longlong
     lib.gbp_strerror.argtypes = [ctypes.c_int]
@@ -264,6 +266,13 @@ class _MacProject:
         rc = self.lib.gbp_project(self.scene, dt, solid_p, fluid_p, arrs[0][1], arrs[1][1], arrs[2][1],
                                   ctypes.byref(self.params), pp, ctypes.byref(self.stats))
         return check(rc, (GBP_OK, GBP_ERR_NOT_CONVERGED, GBP_ERR_NAN))
+
+    def bench_kernel(self, which: int, reps: int = 20, stream=None):
+        """Mean ms per launch and algorithmic bytes per launch of one kernel."""
+        ms, nbytes = ctypes.c_float(), ctypes.c_double()
+        check(self.lib.gbp_bench_kernel(self.scene, which, reps, ctypes.c_void_p(stream) if stream else None,
+                                        ctypes.byref(ms), ctypes.byref(nbytes)))
+        return float(ms.value), float(nbytes.value)
 
     def debug_assemble(self, dt, velocity, solid, fluid):
         """Operator and right-hand side as assembled on the device."""

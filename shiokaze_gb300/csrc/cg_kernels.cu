@@ -265,6 +265,24 @@ cudaError_t launch_cg_iteration(const Grid &g, Operator<double> A, double *x, do
     return cudaGetLastError();
 }
 
+cudaError_t launch_cg_spmv(const Grid &g, Operator<double> A, const double *s, double *z, Scalars *sc, Partials *pt,
+                           int grid_blocks, cudaStream_t stream) {
+    cg_spmv_kernel<<<blocks_for(g, grid_blocks), BLOCK_THREADS, 0, stream>>>(g, A, s, z, sc, pt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cg_update(const Grid &g, double *x, double *r, const double *s, const double *z, Scalars *sc,
+                             Partials *pt, int grid_blocks, cudaStream_t stream) {
+    cg_update_kernel<<<blocks_for(g, grid_blocks), BLOCK_THREADS, 0, stream>>>(g, x, r, s, z, sc, pt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cg_direction(const Grid &g, const double *r, double *s, const Scalars *sc, int grid_blocks,
+                                cudaStream_t stream) {
+    cg_direction_kernel<<<blocks_for(g, grid_blocks), BLOCK_THREADS, 0, stream>>>(g, r, s, sc);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_true_residual(const Grid &g, Operator<double> A, const double *b, const double *x,
                                  const double *prev, Scalars *sc, Partials *pt, int grid_blocks,
                                  cudaStream_t stream) {

@@ -344,6 +344,18 @@ int gbp_project(gbp_scene *s, double dt, const float *solid, const float *fluid,
     return rc;
 }
 
+int gbp_bench_kernel(gbp_scene *s, int which, int reps, void *stream, float *ms_per_launch,
+                     double *bytes_per_launch) {
+    if (!s || !ms_per_launch || !bytes_per_launch || reps < 1)
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_bench_kernel: bad argument");
+    GBP_CUDA(cudaSetDevice(s->ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
+    int rc = s->solver->bench_kernel(s->g, which, reps, s->ctx->grid_blocks, st, ms_per_launch, bytes_per_launch);
+    if (rc) return fail(rc, s->solver->error());
+    s->ctx->launches += reps + 1;
+    return GBP_OK;
+}
+
 int gbp_debug_assemble(gbp_scene *s, double dt, const float *solid, const float *fluid, const float *u,
                        const float *v, const float *w, const gbp_params *params, double *diag, double *cx,
                        double *cy, double *cz, double *b) {

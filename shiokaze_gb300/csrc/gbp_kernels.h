@@ -38,6 +38,13 @@ cudaError_t launch_cg_init(const Grid &g, Operator<double> A, const double *b, c
 // beta; s = r + beta s. Three launches; all return at once after the stop.
 cudaError_t launch_cg_iteration(const Grid &g, Operator<double> A, double *x, double *r, double *s, double *z,
                                 Scalars *sc, Partials *pt, int grid_blocks, cudaStream_t stream);
+// The three launches of an iteration, one at a time (benchmarking).
+cudaError_t launch_cg_spmv(const Grid &g, Operator<double> A, const double *s, double *z, Scalars *sc, Partials *pt,
+                           int grid_blocks, cudaStream_t stream);
+cudaError_t launch_cg_update(const Grid &g, double *x, double *r, const double *s, const double *z, Scalars *sc,
+                             Partials *pt, int grid_blocks, cudaStream_t stream);
+cudaError_t launch_cg_direction(const Grid &g, const double *r, double *s, const Scalars *sc, int grid_blocks,
+                                cudaStream_t stream);
 // |b - A (x + prev)|_inf and _2, |b - A prev|_2 into sc->aux[0..2].
 cudaError_t launch_true_residual(const Grid &g, Operator<double> A, const double *b, const double *x,
                                  const double *prev, Scalars *sc, Partials *pt, int grid_blocks,

@@ -131,6 +131,46 @@ int Solver::solve(const Grid &g, const gbp_params &p, int grid_blocks, cudaStrea
     return GBP_OK;
 }
 
+int Solver::bench_kernel(const Grid &g, int which, int reps, int grid_blocks, cudaStream_t stream, float *ms,
+                         double *bytes) {
+    if (!allocated_) return fail(GBP_ERR_INVALID_ARGUMENT, "bench_kernel: scene has not been projected yet");
+    // scalars that keep every launch running: never done, alpha = 0
+    Scalars h;
+    std::memset(&h, 0, sizeof(h));
+    h.rho = 1.0;
+    h.tol = -1.0;
+    h.max_iter = 1 << 30;
+    h.fluid_exists = 1;
+    SOLVER_CUDA(cudaMemcpyAsync(st_.sc, &h, sizeof(h), cudaMemcpyHostToDevice, stream));
+    Operator<double> A{st_.diag, st_.cx, st_.cy, g.dim == 3 ? st_.cz : st_.cy};
+    const double cells = (double)g.ncell;
+    auto launch = [&]() -> cudaError_t {
+        switch (which) {
+        case 0: return launch_cg_spmv(g, A, st_.s, st_.z, st_.sc, st_.pt, grid_blocks, stream);
+        case 1: return launch_cg_update(g, st_.x, st_.r, st_.s, st_.z, st_.sc, st_.pt, grid_blocks, stream);
+        case 2: return launch_cg_direction(g, st_.r, st_.s, st_.sc, grid_blocks, stream);
+        default: return cudaErrorInvalidValue;
+        }
+    };
+    const double per_cell[] = {48.0, 48.0, 24.0};
+    if (which < 0 || which > 2) return fail(GBP_ERR_INVALID_ARGUMENT, "bench_kernel: unknown kernel");
+    *bytes = per_cell[which] * cells;
+    cudaEvent_t e0, e1;
+    SOLVER_CUDA(cudaEventCreate(&e0));
+    SOLVER_CUDA(cudaEventCreate(&e1));
+    SOLVER_CUDA(launch());
+    SOLVER_CUDA(cudaEventRecord(e0, stream));
+    for (int i = 0; i < reps; ++i) SOLVER_CUDA(launch());
+    SOLVER_CUDA(cudaEventRecord(e1, stream));
+    SOLVER_CUDA(cudaEventSynchronize(e1));
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / (reps > 0 ? reps : 1);
+    return GBP_OK;
+}
+
 void Solver::fill_stats(const Scalars &h, gbp_stats *s) const {
     s->iterations = last_inner_total_;
     s->outer_iterations = last_outer_;

@@ -39,6 +39,9 @@ public:
     // Returns GBP_OK, GBP_ERR_NOT_CONVERGED, GBP_ERR_NAN or an error.
     int solve(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches);
     void fill_stats(const Scalars &h, gbp_stats *st) const;
+    // Times reps launches of one solver kernel (see gbp_bench_kernel).
+    int bench_kernel(const Grid &g, int which, int reps, int grid_blocks, cudaStream_t stream, float *ms,
+                     double *bytes);
     void release();
     SolverState &state() { return st_; }
     const char *error() const { return err_.c_str(); }
