@@ -120,6 +120,6 @@ def test_reference_workload_128_divergence(gb):
     assert pj.stats.unknowns == int(want.unknown.sum())
     assert rel_inf(p, want.pressure) <= 1e-4
     assert rel_inf(w, want.w) <= 1e-4
-    assert abs(pj.stats.iterations - want.iterations) <= max(3, int(0.03 * want.iterations))
+    assert abs(pj.stats.iterations - want.iterations) <= max(3, int(0.1 * want.iterations))
     assert pj.stats.reresid <= 1e-6
     assert pj.stats.true_resid_inf <= 2e-6
