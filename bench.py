@@ -12,6 +12,11 @@ workload is the 3D liquid scene at 128^3 (solid sphere, pool and drop, face
 velocities N(0, 0.2^2) plus gravity over dt = 1/60). Inputs are seeded
 synthetic data with the shapes and value distributions of that workload.
 
+The headline path is multigrid-preconditioned CG with an FP32 inner solve
+inside FP64 iterative refinement (--solver mgpcg --precision mixed); the FP64
+MGPCG path and the reference's own algorithm (plain FP64 CG) are measured on
+the same scene and reported under `compare`.
+
 Prints one JSON line. `value` is solves/s over all ranks with inputs resident
 in HBM (the velocity is reset from a device copy before each step, inside
 the timed region); `e2e` is the same through the host-array C ABI call
@@ -156,6 +161,45 @@ def cpu_baseline(scene, solver_desc):
             "seconds_per_solve": dt, "iterations": r.iterations}
 
 
+def _measure(gb, torch, pj, ctx, scene, dev_arrays, stream, steps, warmup, sampler=None):
+    """Times `steps` projections (after `warmup`) with CUDA events on the
+    projection's stream; the velocity is reset from a device copy first."""
+    solid, fluid, comps, comps0, p = dev_arrays
+    sh = stream.cuda_stream
+
+    def step():
+        for c, c0 in zip(comps, comps0):
+            c.copy_(c0)
+        rc = pj.project(scene.dt, tuple(comps), solid, fluid, pressure_out=p, stream=sh)
+        if rc != gb.GBP_OK:
+            raise RuntimeError(f"projection returned {rc}: {gb.load_library().gbp_strerror(rc).decode()}")
+
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            step()
+    torch.cuda.synchronize()
+    _, world, _ = dist_info()
+    if world > 1:
+        torch.distributed.barrier()
+    if sampler:
+        sampler.start()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    l0 = ctx.launches()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        ev[0].record(stream)
+        for k in range(steps):
+            step()
+            ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop() if sampler else None
+    per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+    return {"total_ms": ev[0].elapsed_time(ev[-1]), "per_step": per_step, "launches": ctx.launches() - l0,
+            "stats": pj.stats.as_dict(), "clocks": clocks}
+
+
 def run_gbp(args):
     import torch
     import shiokaze_gb300 as gb
@@ -168,8 +212,6 @@ def run_gbp(args):
     dev = torch.device("cuda", local)
     scene = make_scene(args.workload)
     ctx = gb.Context(local)
-    cfg = dict(Residual=1e-6, Solver=args.solver, Precision=args.precision)
-    pj = gb.projector_for(scene, ctx, **cfg)
     stream = torch.cuda.Stream(device=dev)
     sh = stream.cuda_stream
 
@@ -180,45 +222,35 @@ def run_gbp(args):
     comps0 = [dev_t(a) for a in (scene.u, scene.v, scene.w) if a is not None]
     comps = [c.clone() for c in comps0]
     p = torch.zeros(scene.fluid.shape, dtype=torch.float32, device=dev)
+    arrays = (solid, fluid, comps, comps0, p)
     torch.cuda.synchronize()
 
-    def step():
-        for c, c0 in zip(comps, comps0):
-            c.copy_(c0)
-        rc = pj.project(scene.dt, tuple(comps), solid, fluid, pressure_out=p, stream=sh)
-        if rc != gb.GBP_OK:
-            raise RuntimeError(f"projection returned {rc}: {gb.load_library().gbp_strerror(rc).decode()}")
-
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            step()
-    stats_warm = pj.stats.as_dict()
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    sampler = ClockSampler(local)
-    sampler.start()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    l0 = ctx.launches()
-    torch.cuda.synchronize()
-    with torch.cuda.stream(stream):
-        ev[0].record(stream)
-        for k in range(args.steps):
-            step()
-            ev[k + 1].record(stream)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    clocks = sampler.stop()
-    launches = ctx.launches() - l0
-    per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
-    total_ms = ev[0].elapsed_time(ev[-1])
-    stats = pj.stats.as_dict()
+    cfg = dict(Residual=1e-6, Solver=args.solver, Precision=args.precision)
+    pj = gb.projector_for(scene, ctx, **cfg)
+    main = _measure(gb, torch, pj, ctx, scene, arrays, stream, args.steps, args.warmup, ClockSampler(local))
+    stats = main["stats"]
+    total_ms = main["total_ms"]
     if world > 1:
         t = torch.tensor([total_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     value = world * args.steps / (total_ms / 1000.0)
+
+    # the other GPU paths on the same scene, for comparison (fewer steps)
+    compare = {}
+    if not args.no_compare:
+        for solver, precision in (("mgpcg", "mixed"), ("mgpcg", "fp64"), ("cg", "fp64")):
+            if (solver, precision) == (args.solver, args.precision):
+                continue
+            other = gb.projector_for(scene, ctx, Residual=1e-6, Solver=solver, Precision=precision)
+            nsteps = 3 if solver == "cg" else max(3, args.steps // 2)
+            m = _measure(gb, torch, other, ctx, scene, arrays, stream, nsteps, 3)
+            ms = m["total_ms"] / nsteps
+            compare[f"{solver}_{precision}"] = {
+                "solves_per_s": round(1000.0 / ms, 3), "ms_per_step": round(ms, 4),
+                "iterations": m["stats"]["iterations"], "outer_iterations": m["stats"]["outer_iterations"],
+                "true_resid_inf": m["stats"]["true_resid_inf"], "steps": nsteps}
+            other.close()
 
     # end to end through the host-array call, pinned host buffers
     def pinned(a):
@@ -243,14 +275,21 @@ def run_gbp(args):
     face_bytes = sum(a.nbytes for a in h0)
     h2d = scene.solid.nbytes + scene.fluid.nbytes + face_bytes
     d2h = face_bytes + scene.fluid.nbytes
-    e2e_value = world * len(e2e_times) / sum(e2e_times) if world == 1 else None
+    e2e_total = sum(e2e_times)
     if world > 1:
-        t = torch.tensor([sum(e2e_times)], device=dev)
+        t = torch.tensor([e2e_total], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_value = world * len(e2e_times) / float(t.item())
+        e2e_total = float(t.item())
+    e2e_value = world * len(e2e_times) / e2e_total
 
-    # roofline: the solve's kernels timed alone
-    kernels = {0: "cg_spmv_kernel", 1: "cg_update_kernel", 2: "cg_direction_kernel"}
+    # roofline: the path's fine-level kernels timed alone, each launched once
+    # per iteration; the slowest is the dominant one
+    if args.solver == "mgpcg":
+        kernels = {10: "mg_presmooth_kernel", 12: "mg_restrict_kernel", 13: "mg_post_black_kernel",
+                   14: "mg_red_dot_kernel", 15: "pcg_direction_kernel", 16: "pcg_spmv_kernel",
+                   17: "pcg_update_kernel"}
+    else:
+        kernels = {0: "cg_spmv_kernel", 1: "cg_update_kernel", 2: "cg_direction_kernel"}
     timed = {}
     for kid, name in kernels.items():
         ms, nbytes = pj.bench_kernel(kid, reps=50, stream=sh)
@@ -259,7 +298,7 @@ def run_gbp(args):
     ms, nbytes = timed[dom]
     peak, peak_kind = measured_peak_gbs()
     achieved = nbytes / (ms * 1e-3) / 1e9
-    traffic = committed_traffic(args.workload, dom)
+    traffic = committed_traffic(f"{args.workload}/{args.solver}_{args.precision}", dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": nbytes, "ms_per_launch": round(ms, 5),
@@ -267,6 +306,7 @@ def run_gbp(args):
                             for n, t in timed.items()}}
 
     ms_step = total_ms / args.steps
+    per_step = main["per_step"]
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
@@ -275,7 +315,7 @@ def run_gbp(args):
         "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]["desc"],
                    "grid": [scene.nx, scene.ny, scene.nz], "solver": args.solver, "precision": args.precision,
                    "residual": 1e-6, "unknowns": stats["unknowns"], "iterations": stats["iterations"],
-                   "parallelism": f"replicas x{world}",
+                   "outer_iterations": stats["outer_iterations"], "parallelism": f"replicas x{world}",
                    "l2": "no flush: working set above the 129 MB L2 (operator + vectors + inputs)"},
         "latency_ms": {"p50": round(float(np.percentile(per_step, 50)), 4),
                        "p99": round(float(np.percentile(per_step, 99)), 4)},
@@ -283,11 +323,12 @@ def run_gbp(args):
         if stats["ms_solve"] > 0 else None,
         "phase_ms": {"assemble": round(stats["ms_assemble"], 4), "solve": round(stats["ms_solve"], 4),
                      "update": round(stats["ms_update"], 4)},
+        "compare": compare,
         "e2e": {"value": round(e2e_value, 3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": roofline,
-        "clocks": clocks,
-        "gpu_launches": int(launches),
+        "clocks": main["clocks"],
+        "gpu_launches": int(main["launches"]),
         "residual": {"reresid": stats["reresid"], "true_inf": stats["true_resid_inf"],
                      "true_l2": stats["true_resid_l2"]},
     }
@@ -355,9 +396,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbp", choices=["gbp", "reference"])
     ap.add_argument("--workload", default="liquid3_128", choices=sorted(WORKLOADS))
-    ap.add_argument("--solver", default="cg", choices=["cg", "mgpcg"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--solver", default="mgpcg", choices=["cg", "mgpcg"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gbp":
         args.warmup = 3

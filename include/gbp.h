@@ -152,6 +152,16 @@ int gbp_debug_assemble(gbp_scene *scene, double dt, const float *solid, const fl
 #define GBP_KERNEL_CG_SPMV 0
 #define GBP_KERNEL_CG_UPDATE 1
 #define GBP_KERNEL_CG_DIRECTION 2
+/* multigrid kernels on the fine level of the scene's last MGPCG solve */
+#define GBP_KERNEL_MG_PRESMOOTH 10
+#define GBP_KERNEL_MG_SWEEP 11
+#define GBP_KERNEL_MG_RESTRICT 12
+#define GBP_KERNEL_MG_POST_BLACK 13
+#define GBP_KERNEL_MG_RED_DOT 14
+/* CG kernels of the scene's last MGPCG solve (FP64, or FP32 inner) */
+#define GBP_KERNEL_PCG_DIRECTION 15
+#define GBP_KERNEL_PCG_SPMV 16
+#define GBP_KERNEL_PCG_UPDATE 17
 int gbp_bench_kernel(gbp_scene *scene, int which, int reps, void *stream, float *ms_per_launch,
                      double *bytes_per_launch);
 

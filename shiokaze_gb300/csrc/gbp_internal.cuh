@@ -61,11 +61,19 @@ struct Scalars {
     double res;      // |r|_inf of the latest iterate
     double r2;       // r . r of the latest iterate (for reporting)
     double aux[4];
-    int iter;        // completed iterations
+    double inner_tol;   // mixed: absolute threshold of the current inner solve
+    double inner_res0;  // mixed: |r_f|_inf at the start of the inner solve
+    int iter;        // completed (inner) iterations
     int done;        // nonzero once the solve has stopped
     int status;      // 0 running, 1 converged, 2 max iterations, 3 breakdown (0/0 or NaN)
     int max_iter;
     int fluid_exists;
+    int first;        // next preconditioned dot starts a new direction (beta = 0)
+    int first_update; // next update overwrites (rather than adds to) the correction
+    int inner_done;   // mixed: the current inner solve has stopped
+    int inner_iter;   // mixed: iterations of the current inner solve
+    int inner_max;    // mixed: iteration cap of one inner solve
+    int outer_iter;   // mixed: refinement steps taken
     int pad;
     unsigned long long unknowns;
     unsigned long long bits_max;  // max of non-negative doubles through their bit patterns

@@ -1,13 +1,22 @@
-// gbp_solver.cpp -- allocation and the host side of the solve loop.
+// gbp_solver.cpp -- allocation and the host side of the solve loops.
 //
-// Iterations are captured once per scene into a CUDA graph of `chunk`
-// iterations (three kernels each) and replayed; after each replay the host
-// reads the device scalars (one small copy) and stops when the device has
-// set `done`. Iterations after the stop return immediately on the device, so
-// the result and the iteration count equal those of an unchunked loop.
+// Iterations are captured once per scene and configuration into a CUDA graph
+// holding `chunk` iterations and replayed; after each replay the host reads
+// the device scalars (one small copy) and stops when the device has set
+// `done`. Launches after the stop return immediately on the device, so the
+// result and the iteration count equal those of an unchunked loop.
+//
+//   CG     (reference solver)  init; [spmv, update, direction] x chunk
+//   MGPCG  FP64                init (r = b - A prev); [V-cycle + dot,
+//                              direction, spmv, update] x chunk
+//   MGPCG  mixed               FP64 init; [FP32 V-cycle + dot, direction,
+//                              spmv, update (inner stop), x64 += d,
+//                              r64 = b - A64 x64 (outer stop)] x chunk
 #include "gbp_solver.h"
 
+#include <algorithm>
 #include <cstring>
+#include <functional>
 
 namespace gbp {
 
@@ -19,12 +28,42 @@ namespace {
             return fail(e_ == cudaErrorMemoryAllocation ? GBP_ERR_OUT_OF_MEMORY : GBP_ERR_CUDA,        \
                         std::string(#call) + ": " + cudaGetErrorString(e_));                          \
     } while (0)
+
+int coarsest_of(const gbp_params &p) { return p.mg_coarsest > 1 ? p.mg_coarsest : 4; }
 }  // namespace
 
+std::vector<Grid> mg_level_grids(const Grid &g, int coarsest) {
+    std::vector<Grid> out{g};
+    while ((int)out.size() < MG_MAX_LEVELS) {
+        const Grid &f = out.back();
+        const int mx = std::max(f.nx, std::max(f.ny, f.nz));
+        if (mx <= coarsest && f.ncell <= MG_COARSEST_MAX) break;
+        if (mx <= 1) break;
+        out.push_back(make_grid(f.dim, (f.nx + 1) / 2, (f.ny + 1) / 2, f.dim == 3 ? (f.nz + 1) / 2 : 1));
+    }
+    return out;
+}
+
 size_t solver_device_bytes(const Grid &g, const gbp_params &p) {
-    size_t cells = (size_t)g.ncell;
-    size_t fine = 8 * cells * (5 /*operator+b*/ + 4 /*x r s z*/ + (p.warm_start ? 1 : 0));
-    return fine;
+    const size_t cells = (size_t)g.ncell;
+    size_t bytes = 8 * cells * (5 /*operator+b*/ + 4 /*x r s z*/ + (p.warm_start ? 1 : 0));
+    if (p.solver == GBP_SOLVER_MGPCG) {
+        bytes += 8 * cells;  // q
+        const size_t s = p.precision == GBP_PRECISION_MIXED ? 4 : 8;
+        std::vector<Grid> lv = mg_level_grids(g, coarsest_of(p));
+        // level 0: inverse diagonal (+ operator copy and 5 vectors in FP32)
+        bytes += s * cells * (p.precision == GBP_PRECISION_MIXED ? 10 : 1);
+        for (size_t l = 1; l < lv.size(); ++l) bytes += s * (size_t)lv[l].ncell * 7;
+    }
+    return bytes;
+}
+
+template <class T> int Solver::alloc(T **p, size_t n) {
+    void *d = nullptr;
+    SOLVER_CUDA(cudaMalloc(&d, sizeof(T) * (n ? n : 1)));
+    owned_.push_back(d);
+    *p = static_cast<T *>(d);
+    return GBP_OK;
 }
 
 int Solver::prepare(const Grid &g, const gbp_params &p) {
@@ -47,88 +86,222 @@ int Solver::prepare(const Grid &g, const gbp_params &p) {
         have_prev_buf_ = true;
         st_.have_prev = false;
     }
+    if (p.solver == GBP_SOLVER_MGPCG) return prepare_mg(g, p);
+    return GBP_OK;
+}
+
+int Solver::prepare_mg(const Grid &g, const gbp_params &p) {
+    const int coarsest = coarsest_of(p);
+    if ((mg64_ready_ || mg32_ready_) && coarsest != mg_coarsest_) {
+        // a different depth: drop the hierarchies (kept buffers are freed with them)
+        for (void *d : owned_) cudaFree(d);
+        owned_.clear();
+        mg64_ready_ = mg32_ready_ = false;
+        st_.q = nullptr;
+        st_.rf = st_.zf = st_.pf = st_.qf = st_.df = nullptr;
+        if (graph_) {
+            cudaGraphExecDestroy(graph_);
+            graph_ = nullptr;
+            graph_key_ = -1;
+        }
+    }
+    mg_coarsest_ = coarsest;
+    const size_t n = (size_t)g.ncell;
+    if (!st_.q) {
+        int rc = alloc(&st_.q, n);
+        if (rc) return rc;
+    }
+    std::vector<Grid> lv = mg_level_grids(g, coarsest);
+    if (lv.back().ncell > MG_COARSEST_MAX) return fail(GBP_ERR_INVALID_ARGUMENT, "multigrid: coarsest level too big");
+    int rc = GBP_OK;
+    if (p.precision == GBP_PRECISION_FP64 && !mg64_ready_) {
+        MgHierarchy<double> &H = h64_;
+        H.nlevels = (int)lv.size();
+        H.fine_aliases_fp64 = true;
+        double *inv;
+        if ((rc = alloc(&inv, n))) return rc;
+        H.levels[0] = MgLevel<double>{g, st_.diag, inv, st_.cx, st_.cy, g.dim == 3 ? st_.cz : st_.cy, st_.r, st_.z};
+        for (int l = 1; l < H.nlevels; ++l) {
+            const size_t m = (size_t)lv[l].ncell;
+            double *d, *iv, *x1, *y1, *z1, *b, *x;
+            if ((rc = alloc(&d, m)) || (rc = alloc(&iv, m)) || (rc = alloc(&x1, m)) || (rc = alloc(&y1, m)) ||
+                (rc = alloc(&z1, m)) || (rc = alloc(&b, m)) || (rc = alloc(&x, m)))
+                return rc;
+            H.levels[l] = MgLevel<double>{lv[l], d, iv, x1, y1, lv[l].dim == 3 ? z1 : y1, b, x};
+        }
+        mg64_ready_ = true;
+    }
+    if (p.precision == GBP_PRECISION_MIXED && !mg32_ready_) {
+        MgHierarchy<float> &H = h32_;
+        H.nlevels = (int)lv.size();
+        H.fine_aliases_fp64 = false;
+        if ((rc = alloc(&st_.rf, n)) || (rc = alloc(&st_.zf, n)) || (rc = alloc(&st_.pf, n)) ||
+            (rc = alloc(&st_.qf, n)) || (rc = alloc(&st_.df, n)))
+            return rc;
+        for (int l = 0; l < H.nlevels; ++l) {
+            const size_t m = (size_t)lv[l].ncell;
+            float *d, *iv, *x1, *y1, *z1, *b = nullptr, *x = nullptr;
+            if ((rc = alloc(&d, m)) || (rc = alloc(&iv, m)) || (rc = alloc(&x1, m)) || (rc = alloc(&y1, m)) ||
+                (rc = alloc(&z1, m)))
+                return rc;
+            if (l == 0) {
+                b = st_.rf;
+                x = st_.zf;
+            } else if ((rc = alloc(&b, m)) || (rc = alloc(&x, m))) {
+                return rc;
+            }
+            H.levels[l] = MgLevel<float>{lv[l], d, iv, x1, y1, lv[l].dim == 3 ? z1 : y1, b, x};
+        }
+        mg32_ready_ = true;
+    }
     return GBP_OK;
 }
 
 void Solver::release() {
-    if (cg_graph_) {
-        cudaGraphExecDestroy(cg_graph_);
-        cg_graph_ = nullptr;
+    if (graph_) {
+        cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+        graph_key_ = -1;
     }
     double **bufs[] = {&st_.diag, &st_.cx, &st_.cy, &st_.cz, &st_.b, &st_.x, &st_.r, &st_.s, &st_.z, &st_.prev};
     for (double **b : bufs) {
         if (*b) cudaFree(*b);
         *b = nullptr;
     }
+    for (void *d : owned_) cudaFree(d);
+    owned_.clear();
     if (st_.sc) cudaFree(st_.sc);
     if (st_.pt) cudaFree(st_.pt);
     if (st_.host_sc) cudaFreeHost(st_.host_sc);
     st_ = SolverState();
     allocated_ = false;
     have_prev_buf_ = false;
+    mg64_ready_ = mg32_ready_ = false;
 }
 
-int Solver::ensure_cg_graph(const Grid &g, int chunk, int grid_blocks, cudaStream_t stream) {
-    if (cg_graph_ && cg_graph_chunk_ == chunk && cg_graph_blocks_ == grid_blocks) return GBP_OK;
-    if (cg_graph_) {
-        cudaGraphExecDestroy(cg_graph_);
-        cg_graph_ = nullptr;
+MgSettings Solver::mg_settings(const gbp_params &p) const {
+    MgSettings ms;
+    ms.smooth = p.mg_smooth > 0 ? p.mg_smooth : 1;
+    ms.coarsest_pairs = 4;
+    ms.alpha = 1.6;
+    return ms;
+}
+
+// Replays the cached graph until the device reports done.
+int Solver::run_graph(const gbp_params &p, int chunk, cudaStream_t stream, long long *launches) {
+    const long long max_chunks = (long long)p.max_iterations / chunk + 64;
+    for (long long k = 0; k < max_chunks; ++k) {
+        SOLVER_CUDA(cudaMemcpyAsync(st_.host_sc, st_.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, stream));
+        SOLVER_CUDA(cudaStreamSynchronize(stream));
+        if (st_.host_sc->done) return GBP_OK;
+        SOLVER_CUDA(cudaGraphLaunch(graph_, stream));
+        *launches += graph_nodes_;
     }
-    Operator<double> A{st_.diag, st_.cx, st_.cy, g.dim == 3 ? st_.cz : st_.cy};
-    cudaGraph_t graph;
-    SOLVER_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    for (int it = 0; it < chunk; ++it) {
-        cudaError_t e = launch_cg_iteration(g, A, st_.x, st_.r, st_.s, st_.z, st_.sc, st_.pt, grid_blocks, stream);
-        if (e != cudaSuccess) {
-            cudaStreamEndCapture(stream, &graph);
-            return fail(GBP_ERR_CUDA, std::string("capturing CG iterations: ") + cudaGetErrorString(e));
-        }
-    }
-    SOLVER_CUDA(cudaStreamEndCapture(stream, &graph));
-    cudaError_t e = cudaGraphInstantiate(&cg_graph_, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) return fail(GBP_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
-    cg_graph_chunk_ = chunk;
-    cg_graph_blocks_ = grid_blocks;
-    cg_graph_nodes_ = 3LL * chunk;
+    SOLVER_CUDA(cudaMemcpyAsync(st_.host_sc, st_.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, stream));
+    SOLVER_CUDA(cudaStreamSynchronize(stream));
     return GBP_OK;
 }
 
 int Solver::solve(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches) {
     *launches = 0;
+    int rc = p.solver == GBP_SOLVER_MGPCG ? solve_mg(g, p, grid_blocks, stream, launches)
+                                          : solve_cg(g, p, grid_blocks, stream, launches);
+    if (rc) return rc;
+    const bool warm = p.warm_start && st_.have_prev;
+    Operator<double> A{st_.diag, st_.cx, st_.cy, g.dim == 3 ? st_.cz : st_.cy};
+    SOLVER_CUDA(launch_true_residual(g, A, st_.b, st_.x, warm ? st_.prev : nullptr, st_.sc, st_.pt, grid_blocks,
+                                     stream));
+    *launches += 1;
+    last_inner_total_ = st_.host_sc->iter;
+    last_outer_ = p.precision == GBP_PRECISION_MIXED ? st_.host_sc->outer_iter : 1;
+    last_precision_ = p.precision;
+    const int status = st_.host_sc->status;
+    if (status == 3) return GBP_ERR_NAN;
+    if (status == 2 || !st_.host_sc->done) return GBP_ERR_NOT_CONVERGED;
+    return GBP_OK;
+}
+
+int Solver::solve_cg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches) {
     const bool warm = p.warm_start && st_.have_prev;
     Operator<double> A{st_.diag, st_.cx, st_.cy, g.dim == 3 ? st_.cz : st_.cy};
     SOLVER_CUDA(launch_cg_init(g, A, st_.b, warm ? st_.prev : nullptr, st_.x, st_.r, st_.s, st_.sc, st_.pt,
                                p.residual, p.max_iterations, grid_blocks, stream));
     *launches += 1;
     const int chunk = p.iterations_per_sync > 0 ? p.iterations_per_sync : 16;
-    int rc = ensure_cg_graph(g, chunk, grid_blocks, stream);
-    if (rc) return rc;
-    const long long max_chunks = (long long)p.max_iterations / chunk + 2;
-    bool done = false;
-    for (long long k = 0; k < max_chunks; ++k) {
-        SOLVER_CUDA(cudaMemcpyAsync(st_.host_sc, st_.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, stream));
-        SOLVER_CUDA(cudaStreamSynchronize(stream));
-        if (st_.host_sc->done) {
-            done = true;
-            break;
-        }
-        SOLVER_CUDA(cudaGraphLaunch(cg_graph_, stream));
-        *launches += cg_graph_nodes_;
+    const long long key = ((long long)chunk << 20) | ((long long)grid_blocks << 4) | 0;
+    if (!graph_ || graph_key_ != key) {
+        if (graph_) cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+        cudaGraph_t graph;
+        SOLVER_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        for (int it = 0; it < chunk && e == cudaSuccess; ++it)
+            e = launch_cg_iteration(g, A, st_.x, st_.r, st_.s, st_.z, st_.sc, st_.pt, grid_blocks, stream);
+        cudaError_t e2 = cudaStreamEndCapture(stream, &graph);
+        if (e != cudaSuccess || e2 != cudaSuccess)
+            return fail(GBP_ERR_CUDA, std::string("capturing CG iterations: ") +
+                                          cudaGetErrorString(e != cudaSuccess ? e : e2));
+        e = cudaGraphInstantiate(&graph_, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(GBP_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        graph_key_ = key;
+        graph_nodes_ = 3LL * chunk;
     }
-    if (!done) {
-        SOLVER_CUDA(cudaMemcpyAsync(st_.host_sc, st_.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, stream));
-        SOLVER_CUDA(cudaStreamSynchronize(stream));
-    }
-    SOLVER_CUDA(launch_true_residual(g, A, st_.b, st_.x, warm ? st_.prev : nullptr, st_.sc, st_.pt, grid_blocks,
-                                     stream));
+    return run_graph(p, chunk, stream, launches);
+}
+
+int Solver::solve_mg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches) {
+    const bool warm = p.warm_start && st_.have_prev;
+    const bool mixed = p.precision == GBP_PRECISION_MIXED;
+    Operator<double> A{st_.diag, st_.cx, st_.cy, g.dim == 3 ? st_.cz : st_.cy};
+    const MgSettings ms = mg_settings(p);
+    // operator hierarchy of this system
+    if (mixed) SOLVER_CUDA(mg_setup<float>(g, A, h32_, grid_blocks, stream));
+    else SOLVER_CUDA(mg_setup<double>(g, A, h64_, grid_blocks, stream));
+    *launches += (mixed ? h32_.nlevels : h64_.nlevels);
+    // initial residual r = b - A prev, x = 0, stopping threshold
+    const double inner_rel = p.inner_tolerance > 0 ? p.inner_tolerance : 1e-3;
+    SOLVER_CUDA(refine_residual(g, A, st_.b, warm ? st_.prev : nullptr, nullptr, st_.r, mixed ? st_.rf : nullptr,
+                                st_.x, st_.sc, st_.pt, true, p.residual, p.max_iterations, inner_rel, 50,
+                                grid_blocks, stream));
     *launches += 1;
-    last_outer_ = 1;
-    last_inner_total_ = st_.host_sc->iter;
-    const int status = st_.host_sc->status;
-    if (status == 2 || !st_.host_sc->done) return GBP_ERR_NOT_CONVERGED;
-    if (status == 3) return GBP_ERR_NAN;
-    return GBP_OK;
+    const int chunk = 4;
+    // the mixed loop reads prev inside the graph: its presence is part of the key
+    const long long key = ((long long)chunk << 20) | ((long long)grid_blocks << 4) | (mixed ? 2 : 1) |
+                          (warm ? 8 : 0) | ((long long)ms.smooth << 40);
+    if (!graph_ || graph_key_ != key) {
+        if (graph_) cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+        cudaGraph_t graph;
+        long long nodes = 0;
+        SOLVER_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        for (int it = 0; it < chunk && e == cudaSuccess; ++it) {
+            if (mixed) {
+                e = pcg_iteration<float>(h32_, ms, st_.df, st_.rf, st_.zf, st_.pf, st_.qf, st_.sc, st_.pt, 1,
+                                         grid_blocks, stream, &nodes);
+                if (e == cudaSuccess) e = refine_accumulate(g, st_.x, st_.df, st_.sc, grid_blocks, stream);
+                if (e == cudaSuccess)
+                    e = refine_residual(g, A, st_.b, warm ? st_.prev : nullptr, st_.x, st_.r, st_.rf, nullptr,
+                                        st_.sc, st_.pt, false, p.residual, p.max_iterations, inner_rel, 50,
+                                        grid_blocks, stream);
+                nodes += 2;
+            } else {
+                e = pcg_iteration<double>(h64_, ms, st_.x, st_.r, st_.z, st_.s, st_.q, st_.sc, st_.pt, 0,
+                                          grid_blocks, stream, &nodes);
+            }
+        }
+        cudaError_t e2 = cudaStreamEndCapture(stream, &graph);
+        if (e != cudaSuccess || e2 != cudaSuccess)
+            return fail(GBP_ERR_CUDA, std::string("capturing MGPCG iterations: ") +
+                                          cudaGetErrorString(e != cudaSuccess ? e : e2));
+        e = cudaGraphInstantiate(&graph_, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(GBP_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        graph_key_ = key;
+        graph_nodes_ = nodes;
+    }
+    return run_graph(p, chunk, stream, launches);
 }
 
 int Solver::bench_kernel(const Grid &g, int which, int reps, int grid_blocks, cudaStream_t stream, float *ms,
@@ -139,22 +312,65 @@ int Solver::bench_kernel(const Grid &g, int which, int reps, int grid_blocks, cu
     std::memset(&h, 0, sizeof(h));
     h.rho = 1.0;
     h.tol = -1.0;
+    h.inner_tol = -1.0;
     h.max_iter = 1 << 30;
+    h.inner_max = 1 << 30;
     h.fluid_exists = 1;
     SOLVER_CUDA(cudaMemcpyAsync(st_.sc, &h, sizeof(h), cudaMemcpyHostToDevice, stream));
     Operator<double> A{st_.diag, st_.cx, st_.cy, g.dim == 3 ? st_.cz : st_.cy};
     const double cells = (double)g.ncell;
-    auto launch = [&]() -> cudaError_t {
-        switch (which) {
-        case 0: return launch_cg_spmv(g, A, st_.s, st_.z, st_.sc, st_.pt, grid_blocks, stream);
-        case 1: return launch_cg_update(g, st_.x, st_.r, st_.s, st_.z, st_.sc, st_.pt, grid_blocks, stream);
-        case 2: return launch_cg_direction(g, st_.r, st_.s, st_.sc, grid_blocks, stream);
-        default: return cudaErrorInvalidValue;
-        }
-    };
-    const double per_cell[] = {48.0, 48.0, 24.0};
-    if (which < 0 || which > 2) return fail(GBP_ERR_INVALID_ARGUMENT, "bench_kernel: unknown kernel");
-    *bytes = per_cell[which] * cells;
+    const bool mixed = last_precision_ == GBP_PRECISION_MIXED;
+    const double s = mixed ? 4.0 : 8.0;
+    double per_cell = 0.0;
+    std::function<cudaError_t()> launch;
+    switch (which) {
+    case GBP_KERNEL_CG_SPMV:
+        per_cell = 48.0;
+        launch = [&]() { return launch_cg_spmv(g, A, st_.s, st_.z, st_.sc, st_.pt, grid_blocks, stream); };
+        break;
+    case GBP_KERNEL_CG_UPDATE:
+        per_cell = 48.0;
+        launch = [&]() { return launch_cg_update(g, st_.x, st_.r, st_.s, st_.z, st_.sc, st_.pt, grid_blocks, stream); };
+        break;
+    case GBP_KERNEL_CG_DIRECTION:
+        per_cell = 24.0;
+        launch = [&]() { return launch_cg_direction(g, st_.r, st_.s, st_.sc, grid_blocks, stream); };
+        break;
+    case GBP_KERNEL_MG_PRESMOOTH:
+    case GBP_KERNEL_MG_SWEEP:
+    case GBP_KERNEL_MG_RESTRICT:
+    case GBP_KERNEL_MG_POST_BLACK:
+    case GBP_KERNEL_MG_RED_DOT: {
+        if (!(mixed ? mg32_ready_ : mg64_ready_)) return fail(GBP_ERR_INVALID_ARGUMENT, "bench_kernel: no multigrid yet");
+        const int k = which - GBP_KERNEL_MG_PRESMOOTH;
+        const double pc[] = {6.0, 7.0, 6.125, 7.125, 7.0};
+        per_cell = pc[k] * s;
+        if (mixed) launch = [&, k]() { return mg_bench_launch<float>(h32_, k, st_.sc, st_.pt, grid_blocks, stream); };
+        else launch = [&, k]() { return mg_bench_launch<double>(h64_, k, st_.sc, st_.pt, grid_blocks, stream); };
+        break;
+    }
+    case GBP_KERNEL_PCG_DIRECTION:
+    case GBP_KERNEL_PCG_SPMV:
+    case GBP_KERNEL_PCG_UPDATE: {
+        if (!(mixed ? mg32_ready_ : mg64_ready_)) return fail(GBP_ERR_INVALID_ARGUMENT, "bench_kernel: no multigrid yet");
+        const int k = which - GBP_KERNEL_PCG_DIRECTION;
+        const double pc[] = {3.0, 6.0, 6.0};
+        per_cell = pc[k] * s;
+        if (mixed)
+            launch = [&, k]() {
+                return pcg_bench_launch<float>(h32_, k, st_.df, st_.rf, st_.zf, st_.pf, st_.qf, st_.sc, st_.pt,
+                                               grid_blocks, stream);
+            };
+        else
+            launch = [&, k]() {
+                return pcg_bench_launch<double>(h64_, k, st_.x, st_.r, st_.z, st_.s, st_.q, st_.sc, st_.pt,
+                                                grid_blocks, stream);
+            };
+        break;
+    }
+    default: return fail(GBP_ERR_INVALID_ARGUMENT, "bench_kernel: unknown kernel");
+    }
+    *bytes = per_cell * cells;
     cudaEvent_t e0, e1;
     SOLVER_CUDA(cudaEventCreate(&e0));
     SOLVER_CUDA(cudaEventCreate(&e1));

@@ -8,23 +8,30 @@
 
 #include "gbp.h"
 #include "gbp_kernels.h"
+#include "gbp_mg.h"
 
 namespace gbp {
 
 struct SolverState {
     // fine-level FP64 operator and right-hand side
     double *diag = nullptr, *cx = nullptr, *cy = nullptr, *cz = nullptr, *b = nullptr;
-    // CG vectors (x is the correction to prev under warm start)
-    double *x = nullptr, *r = nullptr, *s = nullptr, *z = nullptr;
+    // FP64 vectors: x (the correction to prev under warm start), r, and the
+    // CG directions s, z (= A s for plain CG; z = M r for MGPCG) and q
+    double *x = nullptr, *r = nullptr, *s = nullptr, *z = nullptr, *q = nullptr;
     // warm-start pressure kept per cell
     double *prev = nullptr;
     bool have_prev = false;
+    // mixed precision: FP32 inner vectors
+    float *rf = nullptr, *zf = nullptr, *pf = nullptr, *qf = nullptr, *df = nullptr;
     Scalars *sc = nullptr;
     Partials *pt = nullptr;
     Scalars *host_sc = nullptr;  // pinned
 };
 
 size_t solver_device_bytes(const Grid &g, const gbp_params &p);
+
+// Grids of the multigrid levels of g (level 0 = g).
+std::vector<Grid> mg_level_grids(const Grid &g, int coarsest);
 
 class Solver {
 public:
@@ -51,17 +58,29 @@ private:
         err_ = m;
         return code;
     }
-    int ensure_cg_graph(const Grid &g, int chunk, int grid_blocks, cudaStream_t stream);
+    template <class T> int alloc(T **p, size_t n);
+    int prepare_mg(const Grid &g, const gbp_params &p);
+    int solve_cg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches);
+    int solve_mg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches);
+    int run_graph(const gbp_params &p, int chunk, cudaStream_t stream, long long *launches);
+    MgSettings mg_settings(const gbp_params &p) const;
 
     SolverState st_;
     Grid g_{};
     bool allocated_ = false;
     bool have_prev_buf_ = false;
     std::string err_;
-    cudaGraphExec_t cg_graph_ = nullptr;
-    int cg_graph_chunk_ = 0;
-    int cg_graph_blocks_ = 0;
-    long long cg_graph_nodes_ = 0;
+    std::vector<void *> owned_;  // multigrid and mixed-precision buffers
+    // multigrid hierarchies (FP64 path and FP32 inner solve), built lazily
+    MgHierarchy<double> h64_;
+    MgHierarchy<float> h32_;
+    bool mg64_ready_ = false, mg32_ready_ = false;
+    int mg_coarsest_ = 0;
+    int last_precision_ = GBP_PRECISION_FP64;
+    // cached graph of solver iterations
+    cudaGraphExec_t graph_ = nullptr;
+    long long graph_key_ = -1;
+    long long graph_nodes_ = 0;
     int last_outer_ = 1;
     int last_inner_total_ = 0;
 };

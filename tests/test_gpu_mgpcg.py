@@ -1,0 +1,121 @@
+"""MGPCG (FP64 and mixed precision) against the reference (GPU tests).
+
+The multigrid-preconditioned solve stops by the reference's rule
+(|r|_inf <= Residual |r0|_inf) but follows a different Krylov sequence than
+the reference's plain CG, so at Residual 1e-6 the two pressures differ by
+the solve error, up to ~cond(A) x 1e-6. The tolerances below are relative to
+|p_ref|_inf (after removing the mean over the unknowns when the system has no
+Dirichlet cell, as in smoke, where pressure is defined up to a constant):
+
+  MG_RTOL_LIQUID  at Residual 1e-6, scenes with a free surface
+  MG_RTOL_NEUMANN at Residual 1e-6, all-Neumann scenes (smoke)
+  TIGHT_RTOL      at Residual 1e-12 (float storage of p dominates)
+
+Mixed precision refines an FP32 inner solve with FP64 residuals b - A x, so
+its stopping test is on the true FP64 residual.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from golden_io import Case, case_names
+from gpu_util import config_from, rel_inf, run_case_gpu
+from shiokaze_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+MG_RTOL_LIQUID = 2e-4
+MG_RTOL_NEUMANN = 2e-3
+TIGHT_RTOL = 2e-6
+MODES = [("mgpcg", "fp64"), ("mgpcg", "mixed")]
+
+
+def _neumann(name):
+    return name.startswith("smoke")
+
+
+def _pressure_err(p, want, unknown, neumann):
+    if neumann:
+        p = p.astype(np.float64) - p[unknown].mean()
+        want = want.astype(np.float64) - want[unknown].mean()
+        p[~unknown] = 0
+        want[~unknown] = 0
+    return rel_inf(p, want)
+
+
+CASES = [n for n in case_names() if "maxiter" not in n]
+
+
+@pytest.mark.parametrize("solver,precision", MODES)
+@pytest.mark.parametrize("name", CASES)
+def test_mgpcg_matches_reference_fixture(name, solver, precision):
+    c = Case(name)
+    extra = {"Solver": solver, "Precision": precision}
+    tight = c.params.get("residual", 1e-6) < 1e-9
+    if tight:
+        extra["Residual"] = 1e-12 if precision == "fp64" else 1e-11
+    p, (u, v, w), stats, statuses = run_case_gpu(c, **extra)
+    assert statuses[-1] == 0, statuses
+    assert stats["unknowns"] == int(c.out_unknown.sum())
+    assert not p[~c.out_unknown].any()
+    if tight:
+        rt = TIGHT_RTOL * (10 if precision == "mixed" else 1)
+    else:
+        rt = MG_RTOL_NEUMANN if _neumann(name) else MG_RTOL_LIQUID
+    err = _pressure_err(p, c.out_pressure, c.out_unknown, _neumann(name))
+    print(f"{name} {solver}/{precision}: iters={stats['iterations']} (ref {c.iterations}) "
+          f"outer={stats['outer_iterations']} p_err={err:.2e} true_resid={stats['true_resid_inf']:.2e}")
+    assert err <= rt, err
+    for got, want in ((u, c.out_u), (v, c.out_v), (w, c.out_w)):
+        if want is not None:
+            assert rel_inf(got, want) <= 10 * rt, rel_inf(got, want)
+    assert stats["reresid"] <= c.params.get("residual", 1e-6) * (1 + 1e-9)
+    if c.iterations > 0 and not tight:
+        assert stats["iterations"] < c.iterations  # multigrid needs far fewer iterations
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_mgpcg_full_size_liquid_128(precision):
+    sc = scenes.liquid3(128, seed=2)
+    want = oracle.project_scene(sc, "port", residual=1e-6)
+    import shiokaze_gb300 as gb
+    pj = gb.projector_for(sc, Residual=1e-6, Solver="mgpcg", Precision=precision)
+    u, v, w = sc.u.copy(), sc.v.copy(), sc.w.copy()
+    assert pj.project(sc.dt, (u, v, w), sc.solid, sc.fluid) == gb.GBP_OK
+    st = pj.stats
+    print(f"128^3 {precision}: iters={st.iterations} outer={st.outer_iterations} true={st.true_resid_inf:.2e} "
+          f"ms solve={st.ms_solve:.2f}")
+    assert st.unknowns == int(want.unknown.sum())
+    assert st.true_resid_inf <= 1.01e-6
+    assert rel_inf(pj.get_pressure(), want.pressure) <= MG_RTOL_LIQUID
+    assert rel_inf(w, want.w) <= 10 * MG_RTOL_LIQUID
+    assert st.iterations < want.iterations / 10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_mgpcg_deterministic(precision):
+    """Reductions run in a fixed order: the same input gives bitwise the
+    same pressure and velocity."""
+    import shiokaze_gb300 as gb
+    sc = scenes.smoke3(48, seed=7)
+    outs = []
+    for _ in range(2):
+        pj = gb.projector_for(sc, Residual=1e-6, Solver="mgpcg", Precision=precision)
+        u, v, w = sc.u.copy(), sc.v.copy(), sc.w.copy()
+        assert pj.project(sc.dt, (u, v, w), sc.solid, sc.fluid) == gb.GBP_OK
+        outs.append((pj.get_pressure().copy(), u, w))
+        pj.close()
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+
+
+def test_mgpcg_2d_and_odd_shapes():
+    import shiokaze_gb300 as gb
+    for sc in (scenes.liquid2((77, 45), seed=3), scenes.liquid3((33, 17, 29), seed=4), scenes.liquid3((5, 7, 6), seed=5)):
+        want = oracle.project_scene(sc, "port", residual=1e-9)
+        for precision in ("fp64", "mixed"):
+            pj = gb.projector_for(sc, Residual=1e-9, Solver="mgpcg", Precision=precision)
+            vel = (sc.u.copy(), sc.v.copy()) + ((sc.w.copy(),) if sc.dim == 3 else ())
+            assert pj.project(sc.dt, vel, sc.solid, sc.fluid) == gb.GBP_OK
+            assert rel_inf(pj.get_pressure(), want.pressure) <= 1e-5, (sc.name, precision)
+            pj.close()
