@@ -1,0 +1,95 @@
+// gbprojection2.cpp -- Shiokaze plugin module "gbprojection2": the GB300
+// pressure projection behind macproject2_interface
+// (include/shiokaze/projection/macproject2_interface.h), a drop-in for
+// "macpressuresolver2" (src/projection/macpressuresolver2.cpp). Selected with
+// Projection=gbprojection2. Dense read through operator(), gbp_project, and
+// write-back to the active faces, as in gbprojection3.cpp.
+#include <shiokaze/array/array2.h>
+#include <shiokaze/array/macarray2.h>
+#include <shiokaze/core/console.h>
+#include <shiokaze/projection/macproject2_interface.h>
+
+#include <vector>
+
+#include "gbprojection_common.h"
+
+SHKZ_USING_NAMESPACE
+
+class gbprojection2 : public macproject2_interface {
+protected:
+    LONG_NAME("GB300 Pressure Projection 2D")
+    ARGUMENT_NAME("GBProjection")
+
+    virtual void set_target_volume(double current_volume, double target_volume) override {
+        if (m_scene) gbprojection::check(gbp_scene_set_target_volume(m_scene, current_volume, target_volume), "set_target_volume");
+        m_current_volume = current_volume;
+        m_target_volume = target_volume;
+    }
+
+    virtual void project(double dt, macarray2<Real> &velocity, const array2<Real> &solid, const array2<Real> &fluid,
+                         double surface_tension, const std::vector<signed_rigidbody2_interface *> *) override {
+        const int nx = m_shape.w, ny = m_shape.h;
+        if (surface_tension) console::dump("gbprojection2: surface tension is not applied\n");
+        std::vector<float> s((size_t)(nx + 1) * (ny + 1)), f((size_t)nx * ny), p(f.size());
+        for (int j = 0; j <= ny; ++j)
+            for (int i = 0; i <= nx; ++i) s[i + (size_t)(nx + 1) * j] = solid(i, j);
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) f[i + (size_t)nx * j] = fluid(i, j);
+        std::vector<float> vel[2];
+        for (int d = 0; d < 2; ++d) {
+            const int fx = nx + (d == 0), fy = ny + (d == 1);
+            vel[d].resize((size_t)fx * fy);
+            for (int j = 0; j < fy; ++j)
+                for (int i = 0; i < fx; ++i) vel[d][i + (size_t)fx * j] = velocity[d](i, j);
+        }
+        if (!m_scene) {
+            gbprojection::check(gbp_create(m_device, &m_ctx), "gbp_create");
+            gbprojection::check(gbp_scene_create(m_ctx, 2, nx, ny, 1, m_dx, &m_scene), "gbp_scene_create");
+            if (m_target_volume) gbp_scene_set_target_volume(m_scene, m_current_volume, m_target_volume);
+        }
+        gbp_stats st;
+        int rc = gbp_project(m_scene, dt, s.data(), f.data(), vel[0].data(), vel[1].data(), nullptr, &m_params,
+                             p.data(), &st);
+        gbprojection::check(rc, "gbp_project");
+        m_pressure.clear();
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const float v = p[i + (size_t)nx * j];
+                if (v) m_pressure.set(i, j, v);
+            }
+        velocity.parallel_actives([&](int dim, int i, int j, auto &it, int tn) {
+            const int fx = nx + (dim == 0);
+            it.set(vel[dim][i + (size_t)fx * j]);
+        });
+    }
+
+    virtual void configure(configuration &config) override {
+        gbp_params_default(&m_params);
+        gbprojection::configure_params(config, m_params, m_device);
+    }
+    virtual void initialize(const shape2 &shape, double dx) override {
+        m_shape = shape;
+        m_dx = dx;
+    }
+    virtual void post_initialize() override { m_pressure.initialize(m_shape); }
+    virtual const array2<Real> *get_pressure() const override { return &m_pressure; }
+
+public:
+    virtual ~gbprojection2() {
+        if (m_scene) gbp_scene_destroy(m_scene);
+        if (m_ctx) gbp_destroy(m_ctx);
+    }
+
+private:
+    gbp_params m_params;
+    int m_device{0};
+    gbp_ctx *m_ctx{nullptr};
+    gbp_scene *m_scene{nullptr};
+    shape2 m_shape;
+    double m_dx{0.0};
+    double m_current_volume{0.0}, m_target_volume{0.0};
+    array2<Real> m_pressure{this};
+};
+
+extern "C" module *create_instance() { return new gbprojection2(); }
+extern "C" const char *license() { return "MIT"; }

@@ -1,0 +1,109 @@
+// gbprojection3.cpp -- Shiokaze plugin module "gbprojection3": the GB300
+// pressure projection behind macproject3_interface
+// (include/shiokaze/projection/macproject3_interface.h:38-99), a drop-in
+// for "macpressuresolver3" (src/projection/macpressuresolver3.cpp). Selected
+// with Projection=gbprojection3; compiled against the reference's headers
+// and linked to libgbp.so.
+//
+// The reference's arrays are sparse (tiled, narrow band); project() reads
+// them densely through operator() (which applies background/fill values),
+// calls gbp_project, and writes the projected velocity back to the faces
+// that were active, as the reference's velocity update iterates actives
+// (macpressuresolver3.cpp:252). Faces the reference would deactivate
+// (closed faces) are written as 0, which is the value they read back as.
+// Pressure is set on the cells with a nonzero pressure (the unknowns).
+#include <shiokaze/array/array3.h>
+#include <shiokaze/array/macarray3.h>
+#include <shiokaze/core/console.h>
+#include <shiokaze/projection/macproject3_interface.h>
+
+#include <vector>
+
+#include "gbprojection_common.h"
+
+SHKZ_USING_NAMESPACE
+
+class gbprojection3 : public macproject3_interface {
+protected:
+    LONG_NAME("GB300 Pressure Projection 3D")
+    ARGUMENT_NAME("GBProjection")
+
+    virtual void set_target_volume(double current_volume, double target_volume) override {
+        if (m_scene) gbprojection::check(gbp_scene_set_target_volume(m_scene, current_volume, target_volume), "set_target_volume");
+        m_current_volume = current_volume;
+        m_target_volume = target_volume;
+    }
+
+    virtual void project(double dt, macarray3<Real> &velocity, const array3<Real> &solid, const array3<Real> &fluid,
+                         double surface_tension, const std::vector<signed_rigidbody3_interface *> *) override {
+        const int nx = m_shape.w, ny = m_shape.h, nz = m_shape.d;
+        if (surface_tension) console::dump("gbprojection3: surface tension is not applied\n");
+        std::vector<float> s((size_t)(nx + 1) * (ny + 1) * (nz + 1)), f((size_t)nx * ny * nz), p(f.size());
+        for (int k = 0; k <= nz; ++k)
+            for (int j = 0; j <= ny; ++j)
+                for (int i = 0; i <= nx; ++i) s[i + (size_t)(nx + 1) * (j + (size_t)(ny + 1) * k)] = solid(i, j, k);
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) f[i + (size_t)nx * (j + (size_t)ny * k)] = fluid(i, j, k);
+        std::vector<float> vel[3];
+        for (int d = 0; d < 3; ++d) {
+            const int fx = nx + (d == 0), fy = ny + (d == 1), fz = nz + (d == 2);
+            vel[d].resize((size_t)fx * fy * fz);
+            for (int k = 0; k < fz; ++k)
+                for (int j = 0; j < fy; ++j)
+                    for (int i = 0; i < fx; ++i) vel[d][i + (size_t)fx * (j + (size_t)fy * k)] = velocity[d](i, j, k);
+        }
+        if (!m_scene) {
+            gbprojection::check(gbp_create(m_device, &m_ctx), "gbp_create");
+            gbprojection::check(gbp_scene_create(m_ctx, 3, nx, ny, nz, m_dx, &m_scene), "gbp_scene_create");
+            if (m_target_volume) gbp_scene_set_target_volume(m_scene, m_current_volume, m_target_volume);
+        }
+        gbp_stats st;
+        int rc = gbp_project(m_scene, dt, s.data(), f.data(), vel[0].data(), vel[1].data(), vel[2].data(), &m_params,
+                             p.data(), &st);
+        gbprojection::check(rc, "gbp_project");
+        console::dump("gbprojection3: %d iterations, Reresid=%e, %.3f ms\n", st.iterations, st.reresid, st.ms_total);
+        console::write(get_argument_name() + "_number_projection_iteration", st.iterations);
+        m_pressure.clear();
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const float v = p[i + (size_t)nx * (j + (size_t)ny * k)];
+                    if (v) m_pressure.set(i, j, k, v);
+                }
+        velocity.parallel_actives([&](int dim, int i, int j, int k, auto &it, int tn) {
+            const int fx = nx + (dim == 0), fy = ny + (dim == 1);
+            it.set(vel[dim][i + (size_t)fx * (j + (size_t)fy * k)]);
+        });
+    }
+
+    virtual void configure(configuration &config) override {
+        gbp_params_default(&m_params);
+        gbprojection::configure_params(config, m_params, m_device);
+    }
+    virtual void initialize(const shape3 &shape, double dx) override {
+        m_shape = shape;
+        m_dx = dx;
+    }
+    virtual void post_initialize() override { m_pressure.initialize(m_shape); }
+    virtual const array3<Real> *get_pressure() const override { return &m_pressure; }
+
+public:
+    virtual ~gbprojection3() {
+        if (m_scene) gbp_scene_destroy(m_scene);
+        if (m_ctx) gbp_destroy(m_ctx);
+    }
+
+private:
+    gbp_params m_params;
+    int m_device{0};
+    gbp_ctx *m_ctx{nullptr};
+    gbp_scene *m_scene{nullptr};
+    shape3 m_shape;
+    double m_dx{0.0};
+    double m_current_volume{0.0}, m_target_volume{0.0};
+    array3<Real> m_pressure{this};
+};
+
+extern "C" module *create_instance() { return new gbprojection3(); }
+extern "C" const char *license() { return "MIT"; }

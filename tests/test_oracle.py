@@ -66,3 +66,23 @@ def test_port_matches_live_reference(seed):
     assert np.array_equal(a.pressure, b.pressure)
     assert np.array_equal(a.w, b.w)
     assert a.iterations == b.iterations
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference oracle not built here")
+def test_plugin_module_loads_through_reference_loader(tmp_path):
+    """The drop-in: the reference's own module loader (src/core/module.cpp:
+    103-172) picks gbprojection3 / gbprojection2 by the Projection key,
+    creates, configures and initializes it. (project() needs a GPU.)"""
+    import subprocess
+    root = oracle.HERE.rsplit("/", 1)[0]
+    subprocess.check_call(["make", "-s", "-C", f"{root}/shiokaze_gb300/module", f"OUT={oracle.REF_DIR}"],
+                          stdout=subprocess.DEVNULL)
+    lib = oracle._ref_lib()
+    for dim in (3, 2):
+        log = str(tmp_path / f"load{dim}.log")
+        h = lib.ref_create(dim, 16, 16, 16, 1 / 16, f"Projection=gbprojection{dim} Solver=mgpcg".encode(),
+                           log.encode())
+        assert h
+        text = open(log).read()
+        assert f"gbprojection{dim}" in text
+        lib.ref_destroy(h)
