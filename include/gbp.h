@@ -165,6 +165,32 @@ int gbp_debug_assemble(gbp_scene *scene, double dt, const float *solid, const fl
 int gbp_bench_kernel(gbp_scene *scene, int which, int reps, void *stream, float *ms_per_launch,
                      double *bytes_per_launch);
 
+/* Allocation-free projection, for callers that cannot call cudaMalloc: a
+ * host whose device memory comes from its own allocator or a pool sized up
+ * front, a plugin in a process that forbids further device allocations, or
+ * a per-step path that must never reach the allocator. It is the plain FP64
+ * CG projection of gbp_project_device (the reference's solver), but keeps
+ * its scratch -- operator, CG vectors, reduction partials and scalars -- in
+ * one static device array of GBP_STATIC_SCRATCH_BYTES that every GPU loading
+ * the library holds until exit, and calls no cudaMalloc, cudaFree or
+ * allocating library routine. Inputs and outputs are the caller's DEVICE
+ * arrays, as for gbp_project_device; `stream` is a cudaStream_t (NULL = the
+ * legacy default stream) and the call returns once the work is done.
+ * At most GBP_STATIC_MAX_CELLS cells (larger grids return
+ * GBP_ERR_INVALID_ARGUMENT; gbp_strerror gives the reason); params->solver
+ * must be GBP_SOLVER_CG with GBP_PRECISION_FP64, and warm start and volume
+ * correction are not available (they need a scene's state). The first call
+ * on a device looks up the array's device address once (make that first
+ * call before any stream capture on that device). Every call shares the one
+ * array, which keeps the last call's contents: calls that overlap on the
+ * GPU race, so callers must serialise them. No counterpart in the reference,
+ * whose projection allocates on the host on every call. */
+#define GBP_STATIC_MAX_CELLS 32768
+#define GBP_STATIC_SCRATCH_BYTES (2400 * 1024)
+int gbp_project_device_static(int dim, int nx, int ny, int nz, double dx, double dt, const float *solid,
+                              const float *fluid, float *u, float *v, float *w, const gbp_params *params,
+                              float *pressure, gbp_stats *stats, void *stream);
+
 /* Number of kernel launches this context has issued (graph nodes count one
  * each). */
 long long gbp_launch_count(gbp_ctx *ctx);

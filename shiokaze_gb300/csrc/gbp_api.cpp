@@ -44,6 +44,11 @@ int fail(int code, const std::string &msg) {
 
 }  // namespace
 
+namespace gbp {
+// Message for gbp_strerror from code outside this file.
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace gbp
+
 struct gbp_ctx {
     int device = 0;
     int sm_count = 0;
