@@ -53,7 +53,7 @@ template <class F> __device__ __forceinline__ void for_each_cell(const Grid &g, 
     }
 }
 
-__global__ void __launch_bounds__(BLOCK_THREADS) cg_init_kernel(Grid g, Operator<double> A,
+__global__ void __launch_bounds__(BLOCK_THREADS, 6) cg_init_kernel(Grid g, Operator<double> A,
                                                                 const double *__restrict__ b,
                                                                 const double *__restrict__ prev, double *x, double *r,
                                                                 double *s, Scalars *sc, Partials *pt,
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) cg_init_kernel(Grid g, Operator
     }
 }
 
-__global__ void __launch_bounds__(BLOCK_THREADS) cg_spmv_kernel(Grid g, Operator<double> A,
+__global__ void __launch_bounds__(BLOCK_THREADS, 6) cg_spmv_kernel(Grid g, Operator<double> A,
                                                                 const double *__restrict__ s, double *z, Scalars *sc,
                                                                 Partials *pt) {
     if (stopped(sc)) return;
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) cg_spmv_kernel(Grid g, Operator
     }
 }
 
-__global__ void __launch_bounds__(BLOCK_THREADS) cg_update_kernel(Grid g, double *x, double *r,
+__global__ void __launch_bounds__(BLOCK_THREADS, 6) cg_update_kernel(Grid g, double *x, double *r,
                                                                   const double *__restrict__ s,
                                                                   const double *__restrict__ z, Scalars *sc,
                                                                   Partials *pt) {
@@ -175,14 +175,14 @@ __global__ void __launch_bounds__(BLOCK_THREADS) cg_update_kernel(Grid g, double
     }
 }
 
-__global__ void __launch_bounds__(BLOCK_THREADS) cg_direction_kernel(Grid g, const double *__restrict__ r,
+__global__ void __launch_bounds__(BLOCK_THREADS, 6) cg_direction_kernel(Grid g, const double *__restrict__ r,
                                                                      double *s, const Scalars *sc) {
     if (stopped(sc)) return;
     const double beta = sc->beta;
     for_each_cell(g, [&](int i, int j, int k, long long c) { s[c] = fma(beta, s[c], __ldg(r + c)); });
 }
 
-__global__ void __launch_bounds__(BLOCK_THREADS) true_residual_kernel(Grid g, Operator<double> A,
+__global__ void __launch_bounds__(BLOCK_THREADS, 6) true_residual_kernel(Grid g, Operator<double> A,
                                                                       const double *__restrict__ b,
                                                                       const double *__restrict__ x,
                                                                       const double *__restrict__ prev, Scalars *sc,

@@ -121,7 +121,7 @@ int gbp_create(int device, gbp_ctx **out) {
     cudaDeviceProp prop;
     GBP_CUDA(cudaGetDeviceProperties(&prop, device));
     c->sm_count = prop.multiProcessorCount;
-    c->grid_blocks = c->sm_count * 4;
+    c->grid_blocks = c->sm_count * 6;
     if (c->grid_blocks > MAX_GRID) c->grid_blocks = MAX_GRID;
     GBP_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     for (auto &e : c->ev) GBP_CUDA(cudaEventCreate(&e));
@@ -255,9 +255,10 @@ int project_device(gbp_scene *s, double dt, const float *solid, const float *flu
 
     GBP_CUDA(cudaEventRecord(c->ev[0], stream));
     GBP_CUDA(cudaMemsetAsync(st.sc, 0, sizeof(Scalars), stream));
-    GBP_CUDA(launch_assemble(g, dt, s->dx, sp, solid, fluid, u, v, w, st.diag, st.cx, st.cy, st.cz, st.b, st.sc,
-                             c->grid_blocks, stream));
-    c->launches += 1;
+    GBP_CUDA(launch_faces(g, dt, s->dx, sp, solid, fluid, u, v, w, st.faces, c->grid_blocks, stream));
+    GBP_CUDA(launch_assemble_faces(g, sp, fluid, st.faces, st.diag, st.cx, st.cy, st.cz, st.b, st.sc,
+                                   c->grid_blocks, stream));
+    c->launches += 2;
     GBP_CUDA(cudaEventRecord(c->ev[1], stream));
 
     long long launched = 0;
@@ -269,7 +270,7 @@ int project_device(gbp_scene *s, double dt, const float *solid, const float *flu
 
     GBP_CUDA(launch_pressure(g, st.diag, st.x, p.warm_start && st.have_prev ? st.prev : nullptr, pressure,
                              p.warm_start ? st.prev : nullptr, c->grid_blocks, stream));
-    GBP_CUDA(launch_velocity(g, dt, s->dx, sp, solid, fluid, pressure, u, v, w, st.sc, c->grid_blocks, stream));
+    GBP_CUDA(launch_velocity_faces(g, dt, s->dx, sp, pressure, st.faces, u, v, w, st.sc, c->grid_blocks, stream));
     c->launches += 2;
     if (p.warm_start) st.have_prev = true;
     GBP_CUDA(cudaEventRecord(c->ev[3], stream));
@@ -387,9 +388,11 @@ int gbp_debug_assemble(gbp_scene *s, double dt, const float *solid, const float 
     if (g.dim == 3) GBP_CUDA(cudaMemcpyAsync(s->d_w, w, 4 * n_face(g, 2), cudaMemcpyHostToDevice, str));
     SetupParams sp{p.eps_solid, p.eps_fluid, p.second_order_solid, p.second_order_fluid, 0.0};
     GBP_CUDA(cudaMemsetAsync(st.sc, 0, sizeof(Scalars), str));
-    GBP_CUDA(launch_assemble(g, dt, s->dx, sp, s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, st.diag, st.cx,
-                             st.cy, st.cz, st.b, st.sc, s->ctx->grid_blocks, str));
-    s->ctx->launches += 1;
+    GBP_CUDA(launch_faces(g, dt, s->dx, sp, s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, st.faces,
+                          s->ctx->grid_blocks, str));
+    GBP_CUDA(launch_assemble_faces(g, sp, s->d_fluid, st.faces, st.diag, st.cx, st.cy, st.cz, st.b, st.sc,
+                                   s->ctx->grid_blocks, str));
+    s->ctx->launches += 2;
     const size_t bytes = 8 * (size_t)g.ncell;
     GBP_CUDA(cudaMemcpyAsync(diag, st.diag, bytes, cudaMemcpyDeviceToHost, str));
     GBP_CUDA(cudaMemcpyAsync(cx, st.cx, bytes, cudaMemcpyDeviceToHost, str));

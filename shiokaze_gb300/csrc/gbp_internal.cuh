@@ -40,7 +40,9 @@ inline Grid make_grid(int dim, int nx, int ny, int nz) {
     g.nx = nx;
     g.ny = ny;
     g.nz = dim == 3 ? nz : 1;
-    g.tz = g.nz == 1 ? 1 : 4;
+    // deep tiles for big grids (more cells per block), thin ones for small
+    // grids so their tiles spread over all SMs
+    g.tz = (g.nz == 1 || (long long)nx * ny * g.nz <= (1LL << 21)) ? 1 : 4;
     g.ntx = (nx + TILE_X - 1) / TILE_X;
     g.nty = (ny + TILE_Y - 1) / TILE_Y;
     g.ntz = (g.nz + g.tz - 1) / g.tz;

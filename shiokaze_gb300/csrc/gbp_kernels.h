@@ -18,7 +18,26 @@ template <class T> struct Operator {
     const T *diag, *cx, *cy, *cz;  // cz == cy in 2D (never read)
 };
 
+// Per-face results of the face-first assembly, one array per face
+// direction, sized like that direction's face velocities.
+struct FaceArrays {
+    double *w[3];  // weight dt*area/(dx^2 rho) of open faces, -1 otherwise
+    double *q[3];  // area*u/dx (0 where area == 0)
+    float *rho[3]; // rho of open faces, -1 if only rho closes the face, 0 if area == 0
+};
+
 // ---- setup (setup_kernels.cu) ------------------------------------------------
+// Face-first path: faces, then cells; velocity update from the faces.
+cudaError_t launch_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
+                         const float *fluid, const float *u, const float *v, const float *w, FaceArrays fa,
+                         int grid_blocks, cudaStream_t stream);
+cudaError_t launch_assemble_faces(const Grid &g, const SetupParams &sp, const float *fluid, FaceArrays fa,
+                                  double *diag, double *cx, double *cy, double *cz, double *b, Scalars *sc,
+                                  int grid_blocks, cudaStream_t stream);
+cudaError_t launch_velocity_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *p,
+                                  FaceArrays fa, float *u, float *v, float *w, const Scalars *sc, int grid_blocks,
+                                  cudaStream_t stream);
+// Single-pass path (per cell, fractions recomputed per cell).
 cudaError_t launch_assemble(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
                             const float *fluid, const float *u, const float *v, const float *w, double *diag,
                             double *cx, double *cy, double *cz, double *b, Scalars *sc, int grid_blocks,

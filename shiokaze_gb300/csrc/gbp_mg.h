@@ -19,11 +19,38 @@ template <class T> struct MgLevel {
     T *b, *x;
 };
 
+// Levels from `tail` down run in one single-block kernel from shared memory
+// (tail == nlevels: no such levels); tail_smem is the bytes it needs.
+constexpr int MG_TAIL_THREADS = 1024;
+constexpr size_t MG_TAIL_SMEM_MAX = 200 * 1024;
+
 template <class T> struct MgHierarchy {
     int nlevels = 0;
+    int tail = 0;
+    size_t tail_smem = 0;
     bool fine_aliases_fp64 = false;  // level 0 operator is the FP64 assembly itself
     MgLevel<T> levels[MG_MAX_LEVELS];
 };
+
+// Raises the tail kernel's dynamic shared memory limit to `bytes`.
+template <class T> cudaError_t mg_tail_enable(size_t bytes);
+
+// First level (>= 1) from which every coarser level fits the single-block
+// kernel's shared memory, and the bytes needed.
+template <class T> void mg_plan_tail(MgHierarchy<T> &H) {
+    size_t bytes = 0;
+    int tail = H.nlevels;
+    for (int l = H.nlevels - 1; l >= 1; --l) {
+        // 7 arrays per level, plus an FP64 iterate of the coarsest level
+        const size_t need = bytes + 7 * sizeof(T) * (size_t)H.levels[l].g.ncell +
+                            (l == H.nlevels - 1 ? 16 + 8 * (size_t)H.levels[l].g.ncell : 0);
+        if (need > MG_TAIL_SMEM_MAX) break;
+        bytes = need;
+        tail = l;
+    }
+    H.tail = tail;
+    H.tail_smem = bytes;
+}
 
 struct MgSettings {
     int smooth;          // red-black sweeps before and after each coarse correction

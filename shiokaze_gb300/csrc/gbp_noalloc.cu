@@ -116,7 +116,7 @@ extern "C" int gbp_project_device_static(int dim, int nx, int ny, int nz, double
     double *x = vec[5], *r = vec[6], *s = vec[7], *z = vec[8];
     Partials *pt = reinterpret_cast<Partials *>(base + 9 * kVecBytes);
     Scalars *sc = reinterpret_cast<Scalars *>(base + 9 * kVecBytes + align256(sizeof(Partials)));
-    int grid_blocks = sms * 4;
+    int grid_blocks = sms * 6;
     if (grid_blocks > MAX_GRID) grid_blocks = MAX_GRID;
 
     // the scalars block (tickets, flags, counters) must start at zero

@@ -44,9 +44,14 @@ std::vector<Grid> mg_level_grids(const Grid &g, int coarsest) {
     return out;
 }
 
+static size_t face_count(const Grid &g, int d) {
+    return (size_t)(g.nx + (d == 0)) * (g.ny + (d == 1)) * (g.dim == 3 ? g.nz + (d == 2) : 1);
+}
+
 size_t solver_device_bytes(const Grid &g, const gbp_params &p) {
     const size_t cells = (size_t)g.ncell;
     size_t bytes = 8 * cells * (5 /*operator+b*/ + 4 /*x r s z*/ + (p.warm_start ? 1 : 0));
+    for (int d = 0; d < g.dim; ++d) bytes += 20 * face_count(g, d);  // face arrays
     if (p.solver == GBP_SOLVER_MGPCG) {
         bytes += 8 * cells;  // q
         const size_t s = p.precision == GBP_PRECISION_MIXED ? 4 : 8;
@@ -78,6 +83,12 @@ int Solver::prepare(const Grid &g, const gbp_params &p) {
         SOLVER_CUDA(cudaMemset(st_.sc, 0, sizeof(Scalars)));
         SOLVER_CUDA(cudaMalloc(&st_.pt, sizeof(Partials)));
         SOLVER_CUDA(cudaMallocHost(&st_.host_sc, sizeof(Scalars)));
+        for (int d = 0; d < 3; ++d) {
+            const size_t nf = d < g.dim ? face_count(g, d) : 1;
+            SOLVER_CUDA(cudaMalloc(&st_.faces.w[d], 8 * nf));
+            SOLVER_CUDA(cudaMalloc(&st_.faces.q[d], 8 * nf));
+            SOLVER_CUDA(cudaMalloc(&st_.faces.rho[d], 4 * nf));
+        }
         allocated_ = true;
     }
     if (p.warm_start && !have_prev_buf_) {
@@ -129,6 +140,8 @@ int Solver::prepare_mg(const Grid &g, const gbp_params &p) {
                 return rc;
             H.levels[l] = MgLevel<double>{lv[l], d, iv, x1, y1, lv[l].dim == 3 ? z1 : y1, b, x};
         }
+        mg_plan_tail(H);
+        if (H.tail < H.nlevels) SOLVER_CUDA(mg_tail_enable<double>(H.tail_smem));
         mg64_ready_ = true;
     }
     if (p.precision == GBP_PRECISION_MIXED && !mg32_ready_) {
@@ -152,6 +165,8 @@ int Solver::prepare_mg(const Grid &g, const gbp_params &p) {
             }
             H.levels[l] = MgLevel<float>{lv[l], d, iv, x1, y1, lv[l].dim == 3 ? z1 : y1, b, x};
         }
+        mg_plan_tail(H);
+        if (H.tail < H.nlevels) SOLVER_CUDA(mg_tail_enable<float>(H.tail_smem));
         mg32_ready_ = true;
     }
     return GBP_OK;
@@ -173,6 +188,11 @@ void Solver::release() {
     if (st_.sc) cudaFree(st_.sc);
     if (st_.pt) cudaFree(st_.pt);
     if (st_.host_sc) cudaFreeHost(st_.host_sc);
+    for (int d = 0; d < 3; ++d) {
+        if (st_.faces.w[d]) cudaFree(st_.faces.w[d]);
+        if (st_.faces.q[d]) cudaFree(st_.faces.q[d]);
+        if (st_.faces.rho[d]) cudaFree(st_.faces.rho[d]);
+    }
     st_ = SolverState();
     allocated_ = false;
     have_prev_buf_ = false;

@@ -26,6 +26,8 @@ struct SolverState {
     Scalars *sc = nullptr;
     Partials *pt = nullptr;
     Scalars *host_sc = nullptr;  // pinned
+    // per-face weights, fluxes and fractions of the face-first assembly
+    FaceArrays faces{};
 };
 
 size_t solver_device_bytes(const Grid &g, const gbp_params &p);

@@ -11,6 +11,7 @@
 // velocity update reads solid (4) + fluid (4) + pressure (4) + u,v,w (12)
 // and writes u,v,w (12) = 36 B.
 #include <cfloat>
+#include <cmath>
 
 #include "gbp_internal.cuh"
 #include "gbp_kernels.h"
@@ -73,7 +74,26 @@ __device__ double solid_area(double v0, double v1, double v2, double v3) {
 struct FaceParams {
     double eps_solid, eps_fluid;
     int second_order_solid, second_order_fluid;
+    // When dx is a power of two, 1/dx and 1/dx^2 are exact, and x/dx and
+    // x*(1/dx) are both the correctly rounded value of the same real number:
+    // multiplying gives the bit-identical result without an FP64 division.
+    int dx_pow2;
+    double inv_dx, inv_dx2;
+    double w_unit;  // dt*1/(dx*dx*1), the weight of a face with area = rho = 1 (host-evaluated)
 };
+
+// x / dx, bit-identical either way (see FaceParams::dx_pow2)
+__device__ __forceinline__ double div_dx(double x, double dx, const FaceParams &fp) {
+    return fp.dx_pow2 ? x * fp.inv_dx : x / dx;
+}
+
+// dt * area / (dx * dx * rho), as the reference evaluates it
+// (macpressuresolver3.cpp:185); with rho == 1, dx*dx*rho == dx*dx exactly.
+__device__ __forceinline__ double face_weight(double dt, double area, double rho, double dx, const FaceParams &fp) {
+    const double num = dt * area;
+    if (fp.dx_pow2 && rho == 1.0) return num * fp.inv_dx2;
+    return num / (dx * dx * rho);
+}
 
 // Open (non-solid) fraction of face (i,j,k) normal to d
 // (src/utility/macutility3.cpp:117-143; 2D macutility2.cpp:100-105).
@@ -87,8 +107,8 @@ __device__ float face_area(const Grid &g, const float *__restrict__ solid, int d
         area = 0.0;
     } else if (g.dim == 3) {
         const long long sx = g.nx + 1, sxy = sx * (g.ny + 1);
-        auto S = [&](int a, int b, int c) { return (double)__ldg(solid + a + sx * b + sxy * c); };
-        double q00, q10, q11, q01;
+        auto S = [&](int a, int b, int c) { return __ldg(solid + a + sx * b + sxy * c); };
+        float q00, q10, q11, q01;
         if (d == 0) {
             q00 = S(i, j, k); q10 = S(i, j + 1, k); q11 = S(i, j + 1, k + 1); q01 = S(i, j, k + 1);
         } else if (d == 1) {
@@ -96,7 +116,10 @@ __device__ float face_area(const Grid &g, const float *__restrict__ solid, int d
         } else {
             q00 = S(i, j, k); q10 = S(i + 1, j, k); q11 = S(i + 1, j + 1, k); q01 = S(i, j + 1, k);
         }
-        area = 1.0 - solid_area(q00, q10, q11, q01);
+        // uniform squares decided in float (the same comparisons as in double)
+        if (q00 >= 0.0f && q10 >= 0.0f && q11 >= 0.0f && q01 >= 0.0f) area = 1.0;
+        else if (q00 < 0.0f && q10 < 0.0f && q11 < 0.0f && q01 < 0.0f) area = 0.0;
+        else area = 1.0 - solid_area(q00, q10, q11, q01);
     } else {
         const long long sx = g.nx + 1;
         double s0 = __ldg(solid + i + sx * j);
@@ -121,9 +144,14 @@ __device__ float face_rho(const Grid &g, const float *__restrict__ fluid, int d,
         int a0 = min(max(i, 0), g.nx - 1), a1 = min(max(j, 0), g.ny - 1), a2 = min(max(k, 0), g.nz - 1);
         int b0 = min(max(i - (d == 0), 0), g.nx - 1), b1 = min(max(j - (d == 1), 0), g.ny - 1),
             b2 = min(max(k - (d == 2), 0), g.nz - 1);
-        double f0 = __ldg(fluid + a0 + (long long)g.nx * (a1 + (long long)g.ny * a2));
-        double f1 = __ldg(fluid + b0 + (long long)g.nx * (b1 + (long long)g.ny * b2));
-        double rho = fraction(f0, f1);
+        const float f0 = __ldg(fluid + a0 + (long long)g.nx * (a1 + (long long)g.ny * a2));
+        const float f1 = __ldg(fluid + b0 + (long long)g.nx * (b1 + (long long)g.ny * b2));
+        // Same sign (or a zero): fraction() returns 1 or 0. The double
+        // product of two floats never underflows to 0, so its sign test
+        // equals this float sign test.
+        double rho;
+        if (!((f0 < 0.0f && f1 > 0.0f) || (f0 > 0.0f && f1 < 0.0f))) rho = (f0 < 0.0f || f1 < 0.0f) ? 1.0 : 0.0;
+        else rho = fraction(f0, f1);
         if (rho && rho < fp.eps_fluid) rho = fp.eps_fluid;
         r = (float)rho;
     }
@@ -182,16 +210,16 @@ __global__ void __launch_bounds__(BLOCK_THREADS) assemble_kernel(
                     if (area) {
                         const double rho = face_rho(g, fluid, d, f[0], f[1], f[2], fp, 1);
                         if (rho) {
-                            const double value = dt * area / (dx * dx * rho);
+                            const double value = face_weight(dt, area, rho, dx, fp);
                             if (__ldg(fluid + cell_index(g, q[0], q[1], q[2])) < 0.0f) {
                                 unknown = true;
                                 if (plus) cpl[d] = value;
                             }
                             dg += value;
                         }
-                        if (g.dim == 3) rhs += -sgn * area * (double)uf / dx;
+                        if (g.dim == 3) rhs += div_dx(-sgn * area * (double)uf, dx, fp);
                     }
-                    if (g.dim == 2) rhs += -sgn * area * (double)uf / dx;
+                    if (g.dim == 2) rhs += div_dx(-sgn * area * (double)uf, dx, fp);
                 }
             }
             if (unknown) {
@@ -281,7 +309,9 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_kernel(Grid g, double 
                     const float pc = __ldg(p + cell_index(g, i, j, k));
                     const float pm = __ldg(p + cell_index(g, m[0], m[1], m[2]));
                     const float dp = pc - pm;
-                    const double val = dt * (double)dp / ((double)rho * dx);
+                    // rho * dx == dx exactly when rho == 1
+                    const double val = rho == 1.0f ? div_dx(dt * (double)dp, dx, fp)
+                                                   : dt * (double)dp / ((double)rho * dx);
                     out = vel[d][f] - (float)val;
                 }
             } else {
@@ -292,17 +322,228 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_kernel(Grid g, double 
     }
 }
 
+
+// ---- face-first assembly ----------------------------------------------------------
+//
+// Pass 1, one thread per node of the (nx+1)(ny+1)(nz+1) lattice, for the x-,
+// y- and z-face with that lower corner: the face's weight, flux and
+// fraction, computed once per face:
+//   fw  = dt*area/(dx*dx*rho) if the face is open (area > 0, rho > 0), else -1
+//   fq  = area*u/dx (0 if area == 0): the face's term of b is -fq on a
+//         cell's +d face and +fq on its -d face, exactly the reference's
+//         -sgn*area*u/dx since negation is exact
+//   frho = rho if open, -1 if area > 0 but rho == 0, 0 if area == 0
+// Pass 2, one thread per cell, sums them in the reference's face order
+// (+x, -x, +y, -y, +z, -z), so diag, couplings and b are bit-identical to
+// the single-pass assemble_kernel (and to the reference).
+__global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt, double dx, FaceParams fp,
+                                                              const float *__restrict__ solid,
+                                                              const float *__restrict__ fluid,
+                                                              const float *__restrict__ u,
+                                                              const float *__restrict__ v,
+                                                              const float *__restrict__ w, FaceArrays fa) {
+    const long long NX = g.nx + 1, NY = g.ny + 1, NZ = g.dim == 3 ? g.nz + 1 : 1;
+    const long long total = NX * NY * NZ;
+    const float *vel[3] = {u, v, w};
+    const int n[3] = {g.nx, g.ny, g.nz};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % NX);
+        const int j = (int)((t / NX) % NY);
+        const int k = (int)(t / (NX * NY));
+        const int pi[3] = {i, j, k};
+        for (int d = 0; d < g.dim; ++d) {
+            bool exists = true;
+            for (int e = 0; e < g.dim; ++e)
+                if (e != d && pi[e] >= n[e]) exists = false;
+            if (!exists) continue;
+            const long long f = face_index(g, d, i, j, k);
+            const float area = face_area(g, solid, d, i, j, k, fp);
+            const float rho = face_rho(g, fluid, d, i, j, k, fp, 1);
+            const bool open = area && rho;
+            fa.w[d][f] = !open ? -1.0 : (area == 1.0f && rho == 1.0f) ? fp.w_unit
+                                                                        : face_weight(dt, (double)area, (double)rho, dx, fp);
+            fa.q[d][f] = area ? div_dx((double)area * (double)__ldg(vel[d] + f), dx, fp) : 0.0;
+            fa.rho[d][f] = open ? rho : (area ? -1.0f : 0.0f);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK_THREADS) assemble_faces_kernel(
+    Grid g, double rhs_correct, const float *__restrict__ fluid, FaceArrays fa, double *__restrict__ diag,
+    double *__restrict__ cx, double *__restrict__ cy, double *__restrict__ cz, double *__restrict__ b, Scalars *sc) {
+    __shared__ unsigned long long sh_count[BLOCK_THREADS / 32];
+    const int tx = threadIdx.x & (TILE_X - 1), ty = threadIdx.x / TILE_X;
+    unsigned long long my_count = 0;
+    int my_fluid = 0;
+    double *cp[3] = {cx, cy, cz};
+    for (long long t = blockIdx.x; t < g.ntiles; t += gridDim.x) {
+        int i0, j0, k0;
+        tile_origin(g, t, i0, j0, k0);
+        const int i = i0 + tx, j = j0 + ty;
+        if (i >= g.nx || j >= g.ny) continue;
+        for (int kk = 0; kk < g.tz; ++kk) {
+            const int k = k0 + kk;
+            if (k >= g.nz) break;
+            const long long c = cell_index(g, i, j, k);
+            double dg = 0.0, rhs = 0.0, cpl[3] = {0.0, 0.0, 0.0};
+            bool unknown = false;
+            if (__ldg(fluid + c) < 0.0f) {
+                my_fluid = 1;
+                const int n[3] = {g.nx, g.ny, g.nz};
+                for (int nq = 0; nq < 2 * g.dim; ++nq) {
+                    const int d = nq >> 1;
+                    const bool plus = (nq & 1) == 0;
+                    int q[3] = {i, j, k};
+                    q[d] += plus ? 1 : -1;
+                    if (q[d] < 0 || q[d] >= n[d]) continue;
+                    int f[3] = {i, j, k};
+                    if (plus) f[d] += 1;
+                    const long long fi = face_index(g, d, f[0], f[1], f[2]);
+                    if (__ldg(fa.rho[d] + fi) > 0.0f) {  // open face
+                        const double wv = __ldg(fa.w[d] + fi);
+                        if (__ldg(fluid + cell_index(g, q[0], q[1], q[2])) < 0.0f) {
+                            unknown = true;
+                            if (plus) cpl[d] = wv;
+                        }
+                        dg += wv;
+                    }
+                    const double qv = __ldg(fa.q[d] + fi);
+                    rhs += plus ? -qv : qv;
+                }
+            }
+            if (unknown) {
+                my_count++;
+                if (rhs_correct) rhs += rhs_correct;
+            } else {
+                dg = 0.0;
+                rhs = 0.0;
+                cpl[0] = cpl[1] = cpl[2] = 0.0;
+            }
+            diag[c] = dg;
+            b[c] = rhs;
+            for (int d = 0; d < g.dim; ++d) cp[d][c] = cpl[d];
+        }
+    }
+    unsigned long long wsum = my_count;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wsum += __shfl_down_sync(0xffffffffu, wsum, o);
+    if ((threadIdx.x & 31) == 0) sh_count[threadIdx.x >> 5] = wsum;
+    int any_fluid = __syncthreads_or(my_fluid);
+    if (threadIdx.x == 0) {
+        unsigned long long s = 0;
+        for (int q = 0; q < BLOCK_THREADS / 32; ++q) s += sh_count[q];
+        if (s) atomicAdd(&sc->unknowns, s);
+        if (any_fluid) atomicOr(&sc->fluid_exists, 1);
+    }
+}
+
+// Velocity update from the stored face fractions (same rule as
+// velocity_kernel): open faces inside the domain get the pressure gradient,
+// every other face 0; with no fluid anywhere every face with area > 0 is open
+// with rho = 1 (macutility3.cpp:190-192).
+__global__ void __launch_bounds__(BLOCK_THREADS) velocity_faces_kernel(Grid g, double dt, double dx, FaceParams fp,
+                                                                       const float *__restrict__ p, FaceArrays fa,
+                                                                       float *__restrict__ u, float *__restrict__ v,
+                                                                       float *__restrict__ w,
+                                                                       const Scalars *__restrict__ sc) {
+    const int fluid_exists = sc->fluid_exists;
+    const long long NX = g.nx + 1, NY = g.ny + 1, NZ = g.dim == 3 ? g.nz + 1 : 1;
+    const long long total = NX * NY * NZ;
+    float *vel[3] = {u, v, w};
+    const int n[3] = {g.nx, g.ny, g.nz};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % NX);
+        const int j = (int)((t / NX) % NY);
+        const int k = (int)(t / (NX * NY));
+        const int pi[3] = {i, j, k};
+        for (int d = 0; d < g.dim; ++d) {
+            bool exists = true;
+            for (int e = 0; e < g.dim; ++e)
+                if (e != d && pi[e] >= n[e]) exists = false;
+            if (!exists) continue;
+            const long long f = face_index(g, d, i, j, k);
+            const float fr = __ldg(fa.rho[d] + f);
+            const bool open = fluid_exists ? fr > 0.0f : fr != 0.0f;
+            const float rho = fluid_exists ? fr : 1.0f;
+            float out = 0.0f;
+            if (open && !(pi[d] == 0 || pi[d] == n[d])) {
+                int m[3] = {i, j, k};
+                m[d] -= 1;
+                const float pc = __ldg(p + cell_index(g, i, j, k));
+                const float pm = __ldg(p + cell_index(g, m[0], m[1], m[2]));
+                const float dp = pc - pm;
+                const double val = rho == 1.0f ? div_dx(dt * (double)dp, dx, fp)
+                                               : dt * (double)dp / ((double)rho * dx);
+                out = vel[d][f] - (float)val;
+            }
+            vel[d][f] = out;
+        }
+    }
+}
+
+FaceParams face_params(const SetupParams &sp, double dx, double dt = 0.0) {
+    FaceParams fp{sp.eps_solid, sp.eps_fluid, sp.second_order_solid, sp.second_order_fluid, 0, 0.0, 0.0, 0.0};
+    int e = 0;
+    const double m = std::frexp(dx, &e);
+    if (m == 0.5 && e > -500 && e < 500) {  // dx == 2^(e-1)
+        fp.dx_pow2 = 1;
+        fp.inv_dx = std::ldexp(1.0, 1 - e);
+        fp.inv_dx2 = std::ldexp(1.0, 2 * (1 - e));
+    }
+    // the device's face_weight(dt, 1, 1, dx) evaluated here with the same
+    // IEEE operations (no additions, so no contraction can change it)
+    const double num = dt * 1.0;
+    volatile double denom = dx * dx;
+    fp.w_unit = fp.dx_pow2 ? num * fp.inv_dx2 : num / (denom * 1.0);
+    return fp;
+}
+
 }  // namespace
 
 cudaError_t launch_assemble(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
                             const float *fluid, const float *u, const float *v, const float *w, double *diag,
                             double *cx, double *cy, double *cz, double *b, Scalars *sc, int grid_blocks,
                             cudaStream_t stream) {
-    FaceParams fp{sp.eps_solid, sp.eps_fluid, sp.second_order_solid, sp.second_order_fluid};
+    const FaceParams fp = face_params(sp, dx);
     int blocks = (int)(g.ntiles < grid_blocks ? g.ntiles : grid_blocks);
     if (blocks < 1) blocks = 1;
     assemble_kernel<<<blocks, BLOCK_THREADS, 0, stream>>>(g, dt, dx, fp, sp.rhs_correct, solid, fluid, u, v, w, diag,
                                                           cx, cy, g.dim == 3 ? cz : cy, b, sc);
+    return cudaGetLastError();
+}
+
+static int node_blocks(const Grid &g, int grid_blocks) {
+    const long long total = (long long)(g.nx + 1) * (g.ny + 1) * (g.dim == 3 ? g.nz + 1 : 1);
+    const long long need = (total + BLOCK_THREADS - 1) / BLOCK_THREADS;
+    const long long b = need < grid_blocks ? need : grid_blocks;
+    return b < 1 ? 1 : (int)b;
+}
+
+cudaError_t launch_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
+                         const float *fluid, const float *u, const float *v, const float *w, FaceArrays fa,
+                         int grid_blocks, cudaStream_t stream) {
+    const FaceParams fp = face_params(sp, dx, dt);
+    faces_kernel<<<node_blocks(g, grid_blocks), BLOCK_THREADS, 0, stream>>>(g, dt, dx, fp, solid, fluid, u, v, w, fa);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_assemble_faces(const Grid &g, const SetupParams &sp, const float *fluid, FaceArrays fa,
+                                  double *diag, double *cx, double *cy, double *cz, double *b, Scalars *sc,
+                                  int grid_blocks, cudaStream_t stream) {
+    int blocks = (int)(g.ntiles < grid_blocks ? g.ntiles : grid_blocks);
+    if (blocks < 1) blocks = 1;
+    assemble_faces_kernel<<<blocks, BLOCK_THREADS, 0, stream>>>(g, sp.rhs_correct, fluid, fa, diag, cx, cy,
+                                                                g.dim == 3 ? cz : cy, b, sc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_velocity_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *p,
+                                  FaceArrays fa, float *u, float *v, float *w, const Scalars *sc, int grid_blocks,
+                                  cudaStream_t stream) {
+    const FaceParams fp = face_params(sp, dx);
+    velocity_faces_kernel<<<node_blocks(g, grid_blocks), BLOCK_THREADS, 0, stream>>>(g, dt, dx, fp, p, fa, u, v, w, sc);
     return cudaGetLastError();
 }
 
@@ -318,7 +559,7 @@ cudaError_t launch_pressure(const Grid &g, const double *diag, const double *x, 
 cudaError_t launch_velocity(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
                             const float *fluid, const float *p, float *u, float *v, float *w, const Scalars *sc,
                             int grid_blocks, cudaStream_t stream) {
-    FaceParams fp{sp.eps_solid, sp.eps_fluid, sp.second_order_solid, sp.second_order_fluid};
+    const FaceParams fp = face_params(sp, dx);
     long long total = (long long)(g.nx + 1) * (g.ny + 1) * (g.dim == 3 ? g.nz + 1 : 1);
     long long need = (total + BLOCK_THREADS - 1) / BLOCK_THREADS;
     int blocks = (int)(need < grid_blocks ? need : grid_blocks);
