@@ -133,6 +133,25 @@ int gbp_project(gbp_scene *scene, double dt, const float *solid, const float *fl
 int gbp_project_device(gbp_scene *scene, double dt, const float *solid, const float *fluid, float *u, float *v,
                        float *w, const gbp_params *params, float *pressure, gbp_stats *stats, void *stream);
 
+/* Batched projection: many independent scenes of uneven sizes solved
+ * together. Every kernel of the multigrid-preconditioned CG iteration runs
+ * once per iteration for the whole batch, over a work list of tiles of all
+ * scenes, and the iterations are replayed from one CUDA graph; each scene
+ * stops on its own stopping rule, and a scene's result does not depend on
+ * the other scenes in the batch (reductions are per scene, in a fixed
+ * order). Replaces a loop of macpressuresolver3::project calls over
+ * independent scenes. Scenes belong to `ctx`; the batch refers to them (it
+ * does not own them) and keeps their per-scene state (warm start, volume
+ * correction). params->solver must be GBP_SOLVER_MGPCG. */
+typedef struct gbp_batch gbp_batch;
+int gbp_batch_create(gbp_ctx *ctx, int count, gbp_scene *const *scenes, gbp_batch **out);
+void gbp_batch_destroy(gbp_batch *batch);
+/* DEVICE arrays, one per scene (dt per scene); stats may be NULL or hold
+ * `count` entries. Returns GBP_OK, or the first scene's non-OK status. */
+int gbp_batch_project_device(gbp_batch *batch, const double *dt, const float *const *solid,
+                             const float *const *fluid, float *const *u, float *const *v, float *const *w,
+                             const gbp_params *params, float *const *pressure, gbp_stats *stats, void *stream);
+
 /* Operator and right-hand side as assembled on the device, copied to host
  * arrays (each nx*ny*nz doubles): diagonal, coupling weight of each cell's
  * +x/+y/+z face (the negated off-diagonal, 0 unless both cells are

@@ -65,7 +65,8 @@ class GBPError(RuntimeError):
 _lib = None
 EXPORTED = ["gbp_params_default", "gbp_create", "gbp_destroy", "gbp_scene_create", "gbp_scene_destroy",
             "gbp_scene_device_bytes", "gbp_scene_set_target_volume", "gbp_project", "gbp_project_device",
-            "gbp_debug_assemble", "gbp_bench_kernel", "gbp_launch_count", "gbp_strerror"]
+            "gbp_debug_assemble", "gbp_bench_kernel", "gbp_launch_count", "gbp_strerror", "gbp_batch_create",
+            "gbp_batch_destroy", "gbp_batch_project_device"]
 
 
 def library_path() -> str:
@@ -104,6 +105,12 @@ def load_library():
                                        dp, dp]
     lib.gbp_bench_kernel.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, ctypes.POINTER(ctypes.c_float),
                                      ctypes.POINTER(ctypes.c_double)]
+    lib.gbp_batch_create.argtypes = [vp, ctypes.c_int, ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    lib.gbp_batch_destroy.argtypes = [vp]
+    lib.gbp_batch_destroy.restype = None
+    pp = ctypes.POINTER(vp)
+    lib.gbp_batch_project_device.argtypes = [vp, ctypes.POINTER(ctypes.c_double), pp, pp, pp, pp, pp,
+                                             ctypes.POINTER(Params), pp, ctypes.POINTER(Stats), vp]
     lib.gbp_launch_count.argtypes = [vp]
     lib.gbp_launch_count.restype = ctypes.c_longlong
     lib.gbp_strerror.argtypes = [ctypes.c_int]
@@ -305,6 +312,55 @@ class MacProject2(_MacProject):
 
     def __init__(self, nx, ny, dx, context: Context | None = None, **config):
         super().__init__(nx, ny, 1, dx, context, **config)
+
+
+class Batch:
+    """Many scenes projected together (gbp_batch_*): one launch per kernel
+    per iteration for all of them. Each projector keeps its own state (warm
+    start, volume correction); configuration comes from `config` and must
+    select Solver="mgpcg"."""
+
+    def __init__(self, projectors, context: Context | None = None, **config):
+        self.ctx = context or projectors[0].ctx
+        self.lib = self.ctx.lib
+        self.projectors = list(projectors)
+        self.config = dict(config)
+        self.config.setdefault("Solver", "mgpcg")
+        self.params = make_params(**self.config)
+        n = len(self.projectors)
+        arr = (ctypes.c_void_p * n)(*[pj.scene.value for pj in self.projectors])
+        self.handle = ctypes.c_void_p()
+        check(self.lib.gbp_batch_create(self.ctx.handle, n, arr, ctypes.byref(self.handle)))
+        self.stats = (Stats * n)()
+
+    def close(self):
+        if self.handle:
+            self.lib.gbp_batch_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def project(self, dts, velocities, solids, fluids, pressures, stream=None):
+        """Device (torch CUDA) arrays, one entry per scene; velocities are
+        tuples (u, v[, w]) updated in place; pressures are outputs."""
+        import torch
+        n = len(self.projectors)
+        V = ctypes.c_void_p
+
+        def ptrs(items):
+            return (V * n)(*[None if t is None else t.data_ptr() for t in items])
+        u = ptrs([vel[0] for vel in velocities])
+        v = ptrs([vel[1] for vel in velocities])
+        w = ptrs([vel[2] if len(vel) > 2 else None for vel in velocities])
+        dt = (ctypes.c_double * n)(*dts)
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        rc = self.lib.gbp_batch_project_device(self.handle, dt, ptrs(solids), ptrs(fluids), u, v, w,
+                                               ctypes.byref(self.params), ptrs(pressures), self.stats, V(st))
+        return check(rc, (GBP_OK, GBP_ERR_NOT_CONVERGED, GBP_ERR_NAN))
 
 
 def projector_for(scene, context: Context | None = None, **config):

@@ -18,6 +18,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "gbp_kernels.h"
 #include "gbp_solver.h"
@@ -348,6 +349,151 @@ int gbp_project(gbp_scene *s, double dt, const float *solid, const float *fluid,
     if (stats)
         stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return rc;
+}
+
+}  // extern "C"
+
+struct gbp_batch {
+    gbp_ctx *ctx = nullptr;
+    std::vector<gbp_scene *> scenes;
+    BatchRunner runner;
+    long long key = -1;
+};
+
+extern "C" {
+
+int gbp_batch_create(gbp_ctx *c, int count, gbp_scene *const *scenes, gbp_batch **out) {
+    if (!c || !out || count < 1 || !scenes) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_batch_create: bad argument");
+    *out = nullptr;
+    for (int i = 0; i < count; ++i)
+        if (!scenes[i] || scenes[i]->ctx != c)
+            return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_batch_create: scene missing or from another context");
+    auto *b = new (std::nothrow) gbp_batch();
+    if (!b) return fail(GBP_ERR_OUT_OF_MEMORY, "gbp_batch_create: host allocation");
+    b->ctx = c;
+    b->scenes.assign(scenes, scenes + count);
+    *out = b;
+    return GBP_OK;
+}
+
+void gbp_batch_destroy(gbp_batch *b) {
+    if (!b) return;
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    delete b;
+}
+
+int gbp_batch_project_device(gbp_batch *b, const double *dt, const float *const *solid, const float *const *fluid,
+                             float *const *u, float *const *v, float *const *w, const gbp_params *params,
+                             float *const *pressure, gbp_stats *stats, void *stream) {
+    if (!b || !dt || !solid || !fluid || !u || !v) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_batch_project_device: NULL");
+    auto t0 = std::chrono::steady_clock::now();
+    gbp_ctx *c = b->ctx;
+    gbp_params p;
+    gbp_params_default(&p);
+    if (params) p = *params;
+    int rc = validate(p);
+    if (rc) return rc;
+    if (p.solver != GBP_SOLVER_MGPCG) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_batch_project_device: MGPCG only");
+    GBP_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    const int n = (int)b->scenes.size();
+    for (int i = 0; i < n; ++i) {
+        const Grid &g = b->scenes[i]->g;
+        if (!solid[i] || !fluid[i] || !u[i] || !v[i] || (g.dim == 3 && (!w || !w[i])))
+            return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_batch_project_device: NULL array");
+    }
+    GBP_CUDA(cudaEventRecord(c->ev[0], st));
+    // per scene: assembly and multigrid setup
+    long long launched = 0;
+    bool warm_key = false;
+    for (int i = 0; i < n; ++i) {
+        gbp_scene *s = b->scenes[i];
+        const Grid &g = s->g;
+        rc = s->solver->prepare(g, p);
+        if (rc) return fail(rc, s->solver->error());
+        if (!pressure || !pressure[i]) {
+            rc = ensure_staging(s);
+            if (rc) return rc;
+        }
+        SolverState &ss = s->solver->state();
+        SetupParams sp{p.eps_solid, p.eps_fluid, p.second_order_solid, p.second_order_fluid, 0.0};
+        sp.rhs_correct = volume_correction(s, dt[i], p);
+        GBP_CUDA(cudaMemsetAsync(ss.sc, 0, sizeof(Scalars), st));
+        GBP_CUDA(launch_faces(g, dt[i], s->dx, sp, solid[i], fluid[i], u[i], v[i], g.dim == 3 ? w[i] : nullptr,
+                              ss.faces, c->grid_blocks, st));
+        GBP_CUDA(launch_assemble_faces(g, sp, fluid[i], ss.faces, ss.diag, ss.cx, ss.cy, ss.cz, ss.b, ss.sc,
+                                       c->grid_blocks, st));
+        launched += 2;
+        rc = s->solver->setup_mg(g, p, c->grid_blocks, st, &launched);
+        if (rc) return fail(rc, s->solver->error());
+        warm_key = warm_key || (p.warm_start && s->solver->has_prev());
+    }
+    GBP_CUDA(cudaEventRecord(c->ev[1], st));
+    // the batched solve
+    const bool mixed = p.precision == GBP_PRECISION_MIXED;
+    long long key = (mixed ? 1 : 0) | (p.warm_start ? 2 : 0) | ((long long)c->grid_blocks << 4) |
+                    ((long long)(p.mg_coarsest > 1 ? p.mg_coarsest : 4) << 24);
+    for (int i = 0; i < n; ++i) key = key * 31 + (b->scenes[i]->solver->has_prev() ? 1 : 0);
+    if (b->key != key) {
+        if (mixed) {
+            BatchPlan<float> plan;
+            for (gbp_scene *s : b->scenes) s->solver->add_to_plan<float>(plan, p);
+            rc = b->runner.build<float>(plan, c->grid_blocks);
+        } else {
+            BatchPlan<double> plan;
+            for (gbp_scene *s : b->scenes) s->solver->add_to_plan<double>(plan, p);
+            rc = b->runner.build<double>(plan, c->grid_blocks);
+        }
+        if (rc) return fail(rc, b->runner.error());
+        b->key = key;
+    }
+    rc = mixed ? b->runner.solve<float>(p, st, &launched) : b->runner.solve<double>(p, st, &launched);
+    if (rc) return fail(rc, b->runner.error());
+    GBP_CUDA(cudaEventRecord(c->ev[2], st));
+    // per scene: residual report, pressure, velocity
+    int first_bad = GBP_OK;
+    for (int i = 0; i < n; ++i) {
+        gbp_scene *s = b->scenes[i];
+        const Grid &g = s->g;
+        SolverState &ss = s->solver->state();
+        rc = s->solver->finish_batched(p, st);
+        if (rc) return fail(rc, s->solver->error());
+        int status = s->solver->complete(g, p, c->grid_blocks, st, &launched);
+        if (status != GBP_OK && status != GBP_ERR_NOT_CONVERGED && status != GBP_ERR_NAN)
+            return fail(status, s->solver->error());
+        if (status != GBP_OK && first_bad == GBP_OK) first_bad = status;
+        float *pout = pressure && pressure[i] ? pressure[i] : s->d_p;
+        SetupParams sp{p.eps_solid, p.eps_fluid, p.second_order_solid, p.second_order_fluid, 0.0};
+        GBP_CUDA(launch_pressure(g, ss.diag, ss.x, p.warm_start && ss.have_prev ? ss.prev : nullptr, pout,
+                                 p.warm_start ? ss.prev : nullptr, c->grid_blocks, st));
+        GBP_CUDA(launch_velocity_faces(g, dt[i], s->dx, sp, pout, ss.faces, u[i], v[i], g.dim == 3 ? w[i] : nullptr,
+                                       ss.sc, c->grid_blocks, st));
+        launched += 2;
+        if (p.warm_start) ss.have_prev = true;
+    }
+    GBP_CUDA(cudaEventRecord(c->ev[3], st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    c->launches += launched;
+    if (stats) {
+        float ms_a = 0, ms_s = 0, ms_u = 0;
+        cudaEventElapsedTime(&ms_a, c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&ms_s, c->ev[1], c->ev[2]);
+        cudaEventElapsedTime(&ms_u, c->ev[2], c->ev[3]);
+        const float total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        for (int i = 0; i < n; ++i) {
+            Scalars h;
+            GBP_CUDA(cudaMemcpy(&h, b->scenes[i]->solver->state().sc, sizeof(Scalars), cudaMemcpyDeviceToHost));
+            std::memset(&stats[i], 0, sizeof(gbp_stats));
+            b->scenes[i]->solver->fill_stats(h, &stats[i]);
+            stats[i].unknowns = (long long)h.unknowns;
+            stats[i].ms_assemble = ms_a;
+            stats[i].ms_solve = ms_s;
+            stats[i].ms_update = ms_u;
+            stats[i].ms_total = total;
+        }
+    }
+    return first_bad;
 }
 
 int gbp_bench_kernel(gbp_scene *s, int which, int reps, void *stream, float *ms_per_launch,

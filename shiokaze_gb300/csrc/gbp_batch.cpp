@@ -1,0 +1,253 @@
+// gbp_batch.cpp -- host side of the batched MGPCG (BatchRunner).
+//
+// build(): uploads the level table, the per-scene table, the tails and the
+// work lists of a plan. solve(): initial FP64 residual over every scene,
+// then replays a CUDA graph of `chunk` iterations (one launch per kernel per
+// iteration for the whole batch) and reads one counter -- the number of
+// scenes not done -- between replays.
+#include "gbp_batch.h"
+
+#include <algorithm>
+#include <cstring>
+#include <functional>
+
+namespace gbp {
+
+namespace {
+#define RUN_CUDA(call)                                                                                 \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess)                                                                         \
+            return fail(e_ == cudaErrorMemoryAllocation ? GBP_ERR_OUT_OF_MEMORY : GBP_ERR_CUDA,        \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                          \
+    } while (0)
+
+constexpr int kChunk = 4;
+constexpr int kInnerMax = 50;
+}  // namespace
+
+void BatchRunner::release() {
+    if (graph_) {
+        cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+    }
+    graph_key_ = -1;
+    for (void *p : owned_) cudaFree(p);
+    owned_.clear();
+    if (h_counters_) cudaFreeHost(h_counters_);
+    h_counters_ = nullptr;
+    d_levels_ = d_scenes_ = d_tails_ = nullptr;
+    d_pair_.clear();
+    d_restrict_.clear();
+    n_pair_.clear();
+    n_restrict_.clear();
+    d_fine_cells_ = d_fine_pairs_ = nullptr;
+    d_part_ = nullptr;
+    d_counters_ = nullptr;
+    bytes_ = 0;
+}
+
+template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blocks) {
+    release();
+    auto upload = [&](const void *src, size_t bytes, void **dst) -> int {
+        void *d = nullptr;
+        RUN_CUDA(cudaMalloc(&d, bytes ? bytes : 16));
+        owned_.push_back(d);
+        bytes_ += bytes;
+        if (bytes) RUN_CUDA(cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice));
+        *dst = d;
+        return GBP_OK;
+    };
+    int rc;
+    nscenes_ = plan.nscenes;
+    max_global_ = plan.max_global;
+    tail_smem_ = plan.tail_smem;
+    grid_blocks_ = grid_blocks;
+    mixed_ = sizeof(T) == 4;
+    if ((rc = upload(plan.levels.data(), plan.levels.size() * sizeof(BLevel<T>), &d_levels_))) return rc;
+    if ((rc = upload(plan.scenes.data(), plan.scenes.size() * sizeof(BScene<T>), &d_scenes_))) return rc;
+    if ((rc = upload(plan.tails.data(), plan.tails.size() * sizeof(BTail<T>), &d_tails_))) return rc;
+    size_t max_items = std::max(plan.fine_cells.size(), plan.fine_pairs.size());
+    for (int l = 0; l < plan.max_global; ++l) {
+        void *d;
+        if ((rc = upload(plan.pair[l].data(), plan.pair[l].size() * sizeof(BItem), &d))) return rc;
+        d_pair_.push_back(static_cast<BItem *>(d));
+        n_pair_.push_back((int)plan.pair[l].size());
+        if ((rc = upload(plan.restrict_[l].data(), plan.restrict_[l].size() * sizeof(BItem), &d))) return rc;
+        d_restrict_.push_back(static_cast<BItem *>(d));
+        n_restrict_.push_back((int)plan.restrict_[l].size());
+        max_items = std::max(max_items, plan.pair[l].size());
+    }
+    void *d;
+    if ((rc = upload(plan.fine_cells.data(), plan.fine_cells.size() * sizeof(BItem), &d))) return rc;
+    d_fine_cells_ = static_cast<BItem *>(d);
+    n_fine_cells_ = (int)plan.fine_cells.size();
+    if ((rc = upload(plan.fine_pairs.data(), plan.fine_pairs.size() * sizeof(BItem), &d))) return rc;
+    d_fine_pairs_ = static_cast<BItem *>(d);
+    n_fine_pairs_ = (int)plan.fine_pairs.size();
+    max_items_ = (int)max_items;
+    if ((rc = upload(nullptr, sizeof(double) * (max_items + 1), &d))) return rc;
+    d_part_ = static_cast<double *>(d);
+    if ((rc = upload(nullptr, sizeof(BatchCounters), &d))) return rc;
+    d_counters_ = static_cast<BatchCounters *>(d);
+    RUN_CUDA(cudaMallocHost(&h_counters_, sizeof(BatchCounters)));
+    if (tail_smem_ > 0) RUN_CUDA(b_tail_enable<T>(tail_smem_));
+    return GBP_OK;
+}
+
+static MgSettings settings_of(const gbp_params &p) {
+    MgSettings ms;
+    ms.smooth = p.mg_smooth > 0 ? p.mg_smooth : 1;
+    ms.coarsest_pairs = 4;
+    ms.alpha = 1.6;
+    return ms;
+}
+
+static int blocks_for(int items, int grid_blocks) { return std::max(1, std::min(items, grid_blocks)); }
+
+template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &p, cudaStream_t st, long long *nodes) {
+    const int gate = mixed_ ? 1 : 0;
+    const MgSettings ms = settings_of(p);
+    auto *lv = static_cast<const BLevel<T> *>(d_levels_);
+    auto *sc = static_cast<const BScene<T> *>(d_scenes_);
+    auto *tl = static_cast<const BTail<T> *>(d_tails_);
+    cudaError_t e = cudaSuccess;
+    auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, gate}; };
+    // descend
+    for (int l = 0; l < max_global_ && e == cudaSuccess; ++l) {
+        e = b_presmooth<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc);
+        ++*nodes;
+        for (int s = 1; s < ms.smooth && e == cudaSuccess; ++s) {
+            e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc, 0);
+            if (e == cudaSuccess) e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc, 1);
+            *nodes += 2;
+        }
+        if (e == cudaSuccess) e = b_restrict<T>(L(n_restrict_[l]), lv, d_restrict_[l], n_restrict_[l], sc);
+        ++*nodes;
+    }
+    if (e == cudaSuccess && tail_smem_ > 0) {
+        e = b_tail<T>(BLaunch{nscenes_, st, gate}, tl, nscenes_, sc, ms, tail_smem_);
+        ++*nodes;
+    }
+    // ascend
+    for (int l = max_global_ - 1; l >= 0 && e == cudaSuccess; --l) {
+        e = b_post_black<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc, T(ms.alpha));
+        ++*nodes;
+        for (int s = 1; s < ms.smooth && e == cudaSuccess; ++s) {
+            e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc, 0);
+            if (e == cudaSuccess) e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc, 1);
+            *nodes += 2;
+        }
+        if (e != cudaSuccess) break;
+        if (l > 0) e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc, 0);
+        else e = b_red_dot<T>(L(n_fine_pairs_), lv, d_fine_pairs_, n_fine_pairs_, sc, d_part_);
+        ++*nodes;
+    }
+    // CG on the fine level
+    if (e == cudaSuccess) e = b_direction<T>(L(n_fine_cells_), lv, d_fine_cells_, n_fine_cells_, sc);
+    if (e == cudaSuccess) e = b_spmv<T>(L(n_fine_cells_), lv, d_fine_cells_, n_fine_cells_, sc, d_part_);
+    if (e == cudaSuccess)
+        e = b_update<T>(L(n_fine_cells_), lv, d_fine_cells_, n_fine_cells_, sc, d_part_, mixed_ ? 1 : 0, d_counters_);
+    *nodes += 3;
+    if (mixed_ && e == cudaSuccess) {
+        const BLaunch L2{blocks_for(n_fine_cells_, grid_blocks_), st, 2};
+        e = b_refine_accumulate<T>(L2, lv, d_fine_cells_, n_fine_cells_, sc);
+        if (e == cudaSuccess)
+            e = b_refine_residual<T>(L2, lv, d_fine_cells_, n_fine_cells_, sc, d_part_, 0, p.residual,
+                                     p.max_iterations, inner_rel_, kInnerMax, d_counters_);
+        *nodes += 2;
+    }
+    return e;
+}
+
+template <class T> int BatchRunner::solve(const gbp_params &p, cudaStream_t st, long long *launches) {
+    inner_rel_ = p.inner_tolerance > 0 ? p.inner_tolerance : 1e-3;
+    auto *lv = static_cast<const BLevel<T> *>(d_levels_);
+    auto *sc = static_cast<const BScene<T> *>(d_scenes_);
+    h_counters_->remaining = nscenes_;
+    RUN_CUDA(cudaMemcpyAsync(d_counters_, h_counters_, sizeof(BatchCounters), cudaMemcpyHostToDevice, st));
+    // initial residual of every scene (also zeroes x64, sets thresholds)
+    RUN_CUDA(b_refine_residual<T>(BLaunch{blocks_for(n_fine_cells_, grid_blocks_), st, 0}, lv, d_fine_cells_,
+                                  n_fine_cells_, sc, d_part_, 1, p.residual, p.max_iterations, inner_rel_, kInnerMax,
+                                  d_counters_));
+    *launches += 1;
+    const long long key = ((long long)(p.mg_smooth > 0 ? p.mg_smooth : 1) << 40) ^
+                          (long long)(p.residual * 1e15) ^ ((long long)p.max_iterations << 8) ^
+                          (long long)(inner_rel_ * 1e12);
+    if (!graph_ || graph_key_ != key) {
+        if (graph_) cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+        cudaGraph_t graph;
+        long long nodes = 0;
+        RUN_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        for (int it = 0; it < kChunk && e == cudaSuccess; ++it) e = enqueue_iteration<T>(p, st, &nodes);
+        cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+        if (e != cudaSuccess || e2 != cudaSuccess)
+            return fail(GBP_ERR_CUDA, std::string("capturing batched MGPCG iterations: ") +
+                                          cudaGetErrorString(e != cudaSuccess ? e : e2));
+        e = cudaGraphInstantiate(&graph_, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(GBP_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        graph_key_ = key;
+        graph_nodes_ = nodes;
+    }
+    const long long max_chunks = (long long)p.max_iterations / kChunk + 64;
+    for (long long k = 0; k < max_chunks; ++k) {
+        RUN_CUDA(cudaMemcpyAsync(h_counters_, d_counters_, sizeof(BatchCounters), cudaMemcpyDeviceToHost, st));
+        RUN_CUDA(cudaStreamSynchronize(st));
+        if (h_counters_->remaining <= 0) return GBP_OK;
+        RUN_CUDA(cudaGraphLaunch(graph_, st));
+        *launches += graph_nodes_;
+    }
+    RUN_CUDA(cudaStreamSynchronize(st));
+    return GBP_OK;
+}
+
+template <class T> int BatchRunner::bench(int which, int reps, cudaStream_t st, float *ms) {
+    auto *lv = static_cast<const BLevel<T> *>(d_levels_);
+    auto *sc = static_cast<const BScene<T> *>(d_scenes_);
+    const MgSettings mset = settings_of(gbp_params{});
+    std::function<cudaError_t()> launch;
+    auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, 0}; };
+    switch (which) {
+    case 0: launch = [&]() { return b_presmooth<T>(L(n_pair_[0]), lv, d_pair_[0], n_pair_[0], sc); }; break;
+    case 1: launch = [&]() { return b_restrict<T>(L(n_restrict_[0]), lv, d_restrict_[0], n_restrict_[0], sc); }; break;
+    case 2:
+        launch = [&]() { return b_post_black<T>(L(n_pair_[0]), lv, d_pair_[0], n_pair_[0], sc, T(mset.alpha)); };
+        break;
+    case 3: launch = [&]() { return b_red_dot<T>(L(n_fine_pairs_), lv, d_fine_pairs_, n_fine_pairs_, sc, d_part_); }; break;
+    case 4: launch = [&]() { return b_direction<T>(L(n_fine_cells_), lv, d_fine_cells_, n_fine_cells_, sc); }; break;
+    case 5: launch = [&]() { return b_spmv<T>(L(n_fine_cells_), lv, d_fine_cells_, n_fine_cells_, sc, d_part_); }; break;
+    case 6:
+        launch = [&]() {
+            return b_update<T>(L(n_fine_cells_), lv, d_fine_cells_, n_fine_cells_, sc, d_part_, 0, d_counters_);
+        };
+        break;
+    default: return fail(GBP_ERR_INVALID_ARGUMENT, "bench: unknown kernel");
+    }
+    if (max_global_ < 1) return fail(GBP_ERR_INVALID_ARGUMENT, "bench: no multigrid level");
+    cudaEvent_t e0, e1;
+    RUN_CUDA(cudaEventCreate(&e0));
+    RUN_CUDA(cudaEventCreate(&e1));
+    RUN_CUDA(launch());
+    RUN_CUDA(cudaEventRecord(e0, st));
+    for (int i = 0; i < reps; ++i) RUN_CUDA(launch());
+    RUN_CUDA(cudaEventRecord(e1, st));
+    RUN_CUDA(cudaEventSynchronize(e1));
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / (reps > 0 ? reps : 1);
+    return GBP_OK;
+}
+
+template int BatchRunner::build<double>(const BatchPlan<double> &, int);
+template int BatchRunner::build<float>(const BatchPlan<float> &, int);
+template int BatchRunner::solve<double>(const gbp_params &, cudaStream_t, long long *);
+template int BatchRunner::solve<float>(const gbp_params &, cudaStream_t, long long *);
+template int BatchRunner::bench<double>(int, int, cudaStream_t, float *);
+template int BatchRunner::bench<float>(int, int, cudaStream_t, float *);
+
+}  // namespace gbp

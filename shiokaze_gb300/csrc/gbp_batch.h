@@ -1,0 +1,180 @@
+// gbp_batch.h -- batched MGPCG: one launch per kernel for many scenes.
+//
+// Every kernel of the multigrid-preconditioned CG iteration walks a work
+// list of items; an item is one tile of one level of one scene. A launch
+// therefore serves all scenes of a batch (of uneven sizes and depths) at
+// once, and a CUDA graph of a few iterations serves the whole batch.
+//
+// Reductions are per scene and deterministic: each item writes its tile's
+// partial, takes a ticket from its scene's counter, and the item that takes
+// the scene's last ticket sums that scene's partials in item order. A
+// scene's result therefore does not depend on which other scenes share the
+// batch (the serving test checks this), and a single-scene solve is a batch
+// of one.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "gbp.h"
+#include "gbp_internal.cuh"
+#include "gbp_kernels.h"
+#include "gbp_mg.h"
+
+namespace gbp {
+
+// One level of one scene as the batched kernels see it.
+template <class T> struct BLevel {
+    Grid g;
+    const T *diag, *inv, *cx, *cy, *cz;  // cz == cy in 2D
+    T *b, *x;
+    const T *xc;  // x of the next coarser level (post-smoothing)
+    T *bc;        // b of the next coarser level (restriction)
+    Grid gc;      // the next coarser grid
+    int scene;
+};
+
+// Per-scene state of the fine level.
+template <class T> struct BScene {
+    Grid g;
+    T *x, *r, *z, *p, *q;  // PCG vectors (x: the correction in FP64 mode, d in mixed mode)
+    // FP64 operator and refinement state
+    Operator<double> A;
+    const double *b, *prev;
+    double *x64, *r64;
+    Scalars *sc;
+    int levels;  // multigrid levels of the scene
+    int tail;    // first level of its shared-memory tail (== levels: none)
+};
+
+struct BItem {
+    int ref;    // level table index (or scene index for fine-level lists)
+    int tile;   // tile index in the kernel's tiling of that level
+    int begin;  // first item of this scene in the list
+    int count;  // items of this scene in the list
+};
+
+template <class T> struct BTail {
+    int nt;
+    MgLevel<T> lv[MG_MAX_LEVELS];
+};
+
+// Tilings: pair tiles (64 x 8 x tz) for the red-black kernels, cell tiles
+// (32 x 8 x tz) for the rest.
+inline long long pair_tiles(const Grid &g) { return (long long)((g.nx + 63) / 64) * g.nty * g.ntz; }
+inline long long cell_tiles(const Grid &g) { return g.ntiles; }
+
+struct BatchCounters {
+    int remaining;  // scenes not done
+    int pad[3];
+};
+
+// Device tables and work lists of one batch, built on the host.
+template <class T> struct BatchPlan {
+    int nscenes = 0;
+    int max_global = 0;                  // max over scenes of the tail level
+    std::vector<BLevel<T>> levels;       // all scenes' global levels
+    std::vector<BScene<T>> scenes;
+    std::vector<BTail<T>> tails;
+    size_t tail_smem = 0;
+    // item lists: pair[l], restrict[l] (coarse tiles of l+1), fine (cell tiles of level 0)
+    std::vector<std::vector<BItem>> pair, restrict_;
+    std::vector<BItem> fine_cells, fine_pairs;
+};
+
+class BatchRunner {
+public:
+    BatchRunner() = default;
+    ~BatchRunner() { release(); }
+    BatchRunner(const BatchRunner &) = delete;
+    BatchRunner &operator=(const BatchRunner &) = delete;
+
+    // Uploads the plan (tables, lists) and sizes the partials. T = double
+    // for the FP64 path, float for the inner solve of the mixed path.
+    template <class T> int build(const BatchPlan<T> &plan, int grid_blocks);
+    // Runs the solve after every scene's operator and hierarchy are set up:
+    // initial residual, then graph replays until every scene is done.
+    template <class T> int solve(const gbp_params &p, cudaStream_t stream, long long *launches);
+    // Times reps launches of one kernel of the iteration (benchmarking):
+    // 0 presmooth, 1 restrict, 2 post_black, 3 red_dot (fine level),
+    // 4 direction, 5 spmv, 6 update.
+    template <class T> int bench(int which, int reps, cudaStream_t stream, float *ms);
+    void release();
+    const char *error() const { return err_.c_str(); }
+    size_t device_bytes() const { return bytes_; }
+
+private:
+    int fail(int code, const std::string &m) {
+        err_ = m;
+        return code;
+    }
+    template <class T> cudaError_t enqueue_iteration(const gbp_params &p, cudaStream_t stream, long long *nodes);
+    std::string err_;
+    bool mixed_ = false;
+    int grid_blocks_ = 0;
+    int nscenes_ = 0;
+    int max_global_ = 0;
+    size_t tail_smem_ = 0;
+    size_t bytes_ = 0;
+    std::vector<void *> owned_;
+    // device copies
+    void *d_levels_ = nullptr, *d_scenes_ = nullptr, *d_tails_ = nullptr;
+    std::vector<BItem *> d_pair_, d_restrict_;
+    std::vector<int> n_pair_, n_restrict_;
+    BItem *d_fine_cells_ = nullptr, *d_fine_pairs_ = nullptr;
+    int n_fine_cells_ = 0, n_fine_pairs_ = 0;
+    double *d_part_ = nullptr;  // 3 x max items
+    int max_items_ = 0;
+    BatchCounters *d_counters_ = nullptr, *h_counters_ = nullptr;
+    cudaGraphExec_t graph_ = nullptr;
+    long long graph_key_ = -1;
+    long long graph_nodes_ = 0;
+    double inner_rel_ = 1e-3;
+};
+
+// Launch functions (batch_kernels.cu). `levels`, `scenes`, `items` are
+// device arrays.
+struct BLaunch {
+    int blocks;
+    cudaStream_t stream;
+    int gate;
+};
+
+template <class T>
+cudaError_t b_presmooth(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes);
+template <class T>
+cudaError_t b_sweep(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
+                    int color);
+template <class T>
+cudaError_t b_restrict(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+                       const BScene<T> *scenes);
+template <class T>
+cudaError_t b_post_black(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+                         const BScene<T> *scenes, T alpha);
+template <class T>
+cudaError_t b_red_dot(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
+                      double *part);
+template <class T>
+cudaError_t b_tail(const BLaunch &L, const BTail<T> *tails, int nscenes, const BScene<T> *scenes, MgSettings ms,
+                   size_t smem);
+template <class T> cudaError_t b_tail_enable(size_t bytes);
+template <class T>
+cudaError_t b_direction(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+                        const BScene<T> *scenes);
+template <class T>
+cudaError_t b_spmv(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
+                   double *part);
+template <class T>
+cudaError_t b_update(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
+                     double *part, int mode, BatchCounters *cnt);
+template <class T>
+cudaError_t b_refine_accumulate(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+                                const BScene<T> *scenes);
+template <class T>
+cudaError_t b_refine_residual(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+                              const BScene<T> *scenes, double *part, int initial, double residual, int max_iter,
+                              double inner_rel, int inner_max, BatchCounters *cnt);
+
+}  // namespace gbp

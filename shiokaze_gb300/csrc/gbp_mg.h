@@ -32,9 +32,6 @@ template <class T> struct MgHierarchy {
     MgLevel<T> levels[MG_MAX_LEVELS];
 };
 
-// Raises the tail kernel's dynamic shared memory limit to `bytes`.
-template <class T> cudaError_t mg_tail_enable(size_t bytes);
-
 // First level (>= 1) from which every coarser level fits the single-block
 // kernel's shared memory, and the bytes needed.
 template <class T> void mg_plan_tail(MgHierarchy<T> &H) {
@@ -63,36 +60,5 @@ struct MgSettings {
 template <class T>
 cudaError_t mg_setup(const Grid &g0, Operator<double> A, const MgHierarchy<T> &H, int grid_blocks,
                      cudaStream_t stream);
-
-// One preconditioned CG iteration: z = V-cycle(r) with rho' = z.r and beta;
-// p = z + beta p; q = A p; alpha; x += alpha p; r -= alpha q; stop test.
-// mode 0: the solve's stopping rule; mode 1: inner solve of the mixed path.
-template <class T>
-cudaError_t pcg_iteration(const MgHierarchy<T> &H, const MgSettings &ms, T *x, T *r, T *z, T *p, T *q, Scalars *sc,
-                          Partials *pt, int mode, int grid_blocks, cudaStream_t stream, long long *launches);
-
-// FP64 residual r = b - A (prev + x) (x may be NULL), r_f = (float) r, stop
-// test and the opening of the next inner solve. initial: sets the stopping
-// threshold from |r|_inf and zeroes zero_x; otherwise runs only after an
-// inner solve stopped.
-cudaError_t refine_residual(const Grid &g, Operator<double> A, const double *b, const double *prev, const double *x,
-                            double *r, float *rf, double *zero_x, Scalars *sc, Partials *pt, bool initial,
-                            double residual, int max_iter, double inner_rel, int inner_max, int grid_blocks,
-                            cudaStream_t stream);
-// x64 += (double) d after an inner solve stopped.
-cudaError_t refine_accumulate(const Grid &g, double *x, const float *d, const Scalars *sc, int grid_blocks,
-                              cudaStream_t stream);
-
-// One launch of a fine-level V-cycle kernel (0 presmooth, 1 sweep, 2
-// restrict, 3 post-smooth black, 4 red pass + dot), for benchmarking.
-template <class T>
-cudaError_t mg_bench_launch(const MgHierarchy<T> &H, int which, Scalars *sc, Partials *pt, int grid_blocks,
-                            cudaStream_t stream);
-
-// One launch of a CG kernel of the MGPCG loop (0 direction, 1 spmv,
-// 2 update), for benchmarking.
-template <class T>
-cudaError_t pcg_bench_launch(const MgHierarchy<T> &H, int which, T *x, T *r, T *z, T *p, T *q, Scalars *sc,
-                             Partials *pt, int grid_blocks, cudaStream_t stream);
 
 }  // namespace gbp

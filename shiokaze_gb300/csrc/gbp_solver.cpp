@@ -37,8 +37,8 @@ std::vector<Grid> mg_level_grids(const Grid &g, int coarsest) {
     while ((int)out.size() < MG_MAX_LEVELS) {
         const Grid &f = out.back();
         const int mx = std::max(f.nx, std::max(f.ny, f.nz));
-        if (mx <= coarsest && f.ncell <= MG_COARSEST_MAX) break;
-        if (mx <= 1) break;
+        // at least two levels (the fine level always runs the global kernels)
+        if (out.size() >= 2 && ((mx <= coarsest && f.ncell <= MG_COARSEST_MAX) || mx <= 1)) break;
         out.push_back(make_grid(f.dim, (f.nx + 1) / 2, (f.ny + 1) / 2, f.dim == 3 ? (f.nz + 1) / 2 : 1));
     }
     return out;
@@ -141,7 +141,6 @@ int Solver::prepare_mg(const Grid &g, const gbp_params &p) {
             H.levels[l] = MgLevel<double>{lv[l], d, iv, x1, y1, lv[l].dim == 3 ? z1 : y1, b, x};
         }
         mg_plan_tail(H);
-        if (H.tail < H.nlevels) SOLVER_CUDA(mg_tail_enable<double>(H.tail_smem));
         mg64_ready_ = true;
     }
     if (p.precision == GBP_PRECISION_MIXED && !mg32_ready_) {
@@ -166,7 +165,6 @@ int Solver::prepare_mg(const Grid &g, const gbp_params &p) {
             H.levels[l] = MgLevel<float>{lv[l], d, iv, x1, y1, lv[l].dim == 3 ? z1 : y1, b, x};
         }
         mg_plan_tail(H);
-        if (H.tail < H.nlevels) SOLVER_CUDA(mg_tail_enable<float>(H.tail_smem));
         mg32_ready_ = true;
     }
     return GBP_OK;
@@ -199,14 +197,6 @@ void Solver::release() {
     mg64_ready_ = mg32_ready_ = false;
 }
 
-MgSettings Solver::mg_settings(const gbp_params &p) const {
-    MgSettings ms;
-    ms.smooth = p.mg_smooth > 0 ? p.mg_smooth : 1;
-    ms.coarsest_pairs = 4;
-    ms.alpha = 1.6;
-    return ms;
-}
-
 // Replays the cached graph until the device reports done.
 int Solver::run_graph(const gbp_params &p, int chunk, cudaStream_t stream, long long *launches) {
     const long long max_chunks = (long long)p.max_iterations / chunk + 64;
@@ -227,6 +217,10 @@ int Solver::solve(const Grid &g, const gbp_params &p, int grid_blocks, cudaStrea
     int rc = p.solver == GBP_SOLVER_MGPCG ? solve_mg(g, p, grid_blocks, stream, launches)
                                           : solve_cg(g, p, grid_blocks, stream, launches);
     if (rc) return rc;
+    return complete(g, p, grid_blocks, stream, launches);
+}
+
+int Solver::complete(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches) {
     const bool warm = p.warm_start && st_.have_prev;
     Operator<double> A{st_.diag, st_.cx, st_.cy, g.dim == 3 ? st_.cz : st_.cy};
     SOLVER_CUDA(launch_true_residual(g, A, st_.b, st_.x, warm ? st_.prev : nullptr, st_.sc, st_.pt, grid_blocks,
@@ -270,58 +264,108 @@ int Solver::solve_cg(const Grid &g, const gbp_params &p, int grid_blocks, cudaSt
     return run_graph(p, chunk, stream, launches);
 }
 
-int Solver::solve_mg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches) {
-    const bool warm = p.warm_start && st_.have_prev;
-    const bool mixed = p.precision == GBP_PRECISION_MIXED;
+int Solver::setup_mg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches) {
     Operator<double> A{st_.diag, st_.cx, st_.cy, g.dim == 3 ? st_.cz : st_.cy};
-    const MgSettings ms = mg_settings(p);
-    // operator hierarchy of this system
-    if (mixed) SOLVER_CUDA(mg_setup<float>(g, A, h32_, grid_blocks, stream));
-    else SOLVER_CUDA(mg_setup<double>(g, A, h64_, grid_blocks, stream));
-    *launches += (mixed ? h32_.nlevels : h64_.nlevels);
-    // initial residual r = b - A prev, x = 0, stopping threshold
-    const double inner_rel = p.inner_tolerance > 0 ? p.inner_tolerance : 1e-3;
-    SOLVER_CUDA(refine_residual(g, A, st_.b, warm ? st_.prev : nullptr, nullptr, st_.r, mixed ? st_.rf : nullptr,
-                                st_.x, st_.sc, st_.pt, true, p.residual, p.max_iterations, inner_rel, 50,
-                                grid_blocks, stream));
-    *launches += 1;
-    const int chunk = 4;
-    // the mixed loop reads prev inside the graph: its presence is part of the key
-    const long long key = ((long long)chunk << 20) | ((long long)grid_blocks << 4) | (mixed ? 2 : 1) |
-                          (warm ? 8 : 0) | ((long long)ms.smooth << 40);
-    if (!graph_ || graph_key_ != key) {
-        if (graph_) cudaGraphExecDestroy(graph_);
-        graph_ = nullptr;
-        cudaGraph_t graph;
-        long long nodes = 0;
-        SOLVER_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = cudaSuccess;
-        for (int it = 0; it < chunk && e == cudaSuccess; ++it) {
-            if (mixed) {
-                e = pcg_iteration<float>(h32_, ms, st_.df, st_.rf, st_.zf, st_.pf, st_.qf, st_.sc, st_.pt, 1,
-                                         grid_blocks, stream, &nodes);
-                if (e == cudaSuccess) e = refine_accumulate(g, st_.x, st_.df, st_.sc, grid_blocks, stream);
-                if (e == cudaSuccess)
-                    e = refine_residual(g, A, st_.b, warm ? st_.prev : nullptr, st_.x, st_.r, st_.rf, nullptr,
-                                        st_.sc, st_.pt, false, p.residual, p.max_iterations, inner_rel, 50,
-                                        grid_blocks, stream);
-                nodes += 2;
-            } else {
-                e = pcg_iteration<double>(h64_, ms, st_.x, st_.r, st_.z, st_.s, st_.q, st_.sc, st_.pt, 0,
-                                          grid_blocks, stream, &nodes);
-            }
-        }
-        cudaError_t e2 = cudaStreamEndCapture(stream, &graph);
-        if (e != cudaSuccess || e2 != cudaSuccess)
-            return fail(GBP_ERR_CUDA, std::string("capturing MGPCG iterations: ") +
-                                          cudaGetErrorString(e != cudaSuccess ? e : e2));
-        e = cudaGraphInstantiate(&graph_, graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) return fail(GBP_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
-        graph_key_ = key;
-        graph_nodes_ = nodes;
+    if (p.precision == GBP_PRECISION_MIXED) {
+        SOLVER_CUDA(mg_setup<float>(g, A, h32_, grid_blocks, stream));
+        *launches += h32_.nlevels;
+    } else {
+        SOLVER_CUDA(mg_setup<double>(g, A, h64_, grid_blocks, stream));
+        *launches += h64_.nlevels;
     }
-    return run_graph(p, chunk, stream, launches);
+    return GBP_OK;
+}
+
+template <class T> void Solver::add_to_plan(BatchPlan<T> &plan, const gbp_params &p) const {
+    const MgHierarchy<T> &H = *reinterpret_cast<const MgHierarchy<T> *>(
+        sizeof(T) == 4 ? static_cast<const void *>(&h32_) : static_cast<const void *>(&h64_));
+    const int s = plan.nscenes++;
+    const bool warm = p.warm_start && st_.have_prev;
+    const int G = H.tail;  // levels [0, G) run the global kernels; [G, L) the tail
+    BScene<T> sc{};
+    sc.g = H.levels[0].g;
+    if (sizeof(T) == 4) {
+        sc.x = reinterpret_cast<T *>(st_.df);
+        sc.r = reinterpret_cast<T *>(st_.rf);
+        sc.z = reinterpret_cast<T *>(st_.zf);
+        sc.p = reinterpret_cast<T *>(st_.pf);
+        sc.q = reinterpret_cast<T *>(st_.qf);
+    } else {
+        sc.x = reinterpret_cast<T *>(st_.x);
+        sc.r = reinterpret_cast<T *>(st_.r);
+        sc.z = reinterpret_cast<T *>(st_.z);
+        sc.p = reinterpret_cast<T *>(st_.s);
+        sc.q = reinterpret_cast<T *>(st_.q);
+    }
+    sc.A = Operator<double>{st_.diag, st_.cx, st_.cy, sc.g.dim == 3 ? st_.cz : st_.cy};
+    sc.b = st_.b;
+    sc.prev = warm ? st_.prev : nullptr;
+    sc.x64 = st_.x;
+    sc.r64 = st_.r;
+    sc.sc = st_.sc;
+    sc.levels = H.nlevels;
+    sc.tail = G;
+    plan.scenes.push_back(sc);
+    if ((int)plan.pair.size() < G) {
+        plan.pair.resize(G);
+        plan.restrict_.resize(G);
+    }
+    plan.max_global = std::max(plan.max_global, G);
+    const int base = (int)plan.levels.size();
+    for (int l = 0; l < G; ++l) {
+        const MgLevel<T> &F = H.levels[l], &C = H.levels[l + 1];
+        plan.levels.push_back(BLevel<T>{F.g, F.diag, F.inv, F.cx, F.cy, F.cz, F.b, F.x, C.x, C.b, C.g, s});
+        auto add = [&](std::vector<BItem> &list, long long tiles) {
+            const int begin = (int)list.size();
+            for (long long t = 0; t < tiles; ++t) list.push_back(BItem{base + l, (int)t, begin, (int)tiles});
+        };
+        add(plan.pair[l], pair_tiles(F.g));
+        add(plan.restrict_[l], cell_tiles(C.g));
+        if (l == 0) {
+            add(plan.fine_cells, cell_tiles(F.g));
+            add(plan.fine_pairs, pair_tiles(F.g));
+        }
+    }
+    BTail<T> tail{};
+    tail.nt = H.nlevels - G;
+    for (int l = G; l < H.nlevels; ++l) tail.lv[l - G] = H.levels[l];
+    plan.tails.push_back(tail);
+    plan.tail_smem = std::max(plan.tail_smem, H.tail_smem);
+}
+
+template void Solver::add_to_plan<double>(BatchPlan<double> &, const gbp_params &) const;
+template void Solver::add_to_plan<float>(BatchPlan<float> &, const gbp_params &) const;
+
+int Solver::finish_batched(const gbp_params &p, cudaStream_t stream) {
+    SOLVER_CUDA(cudaMemcpyAsync(st_.host_sc, st_.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, stream));
+    SOLVER_CUDA(cudaStreamSynchronize(stream));
+    return GBP_OK;
+}
+
+int Solver::solve_mg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches) {
+    const bool mixed = p.precision == GBP_PRECISION_MIXED;
+    const bool warm = p.warm_start && st_.have_prev;
+    int rc = setup_mg(g, p, grid_blocks, stream, launches);
+    if (rc) return rc;
+    // a batch of one: the same kernels and reductions as a batched solve
+    const long long key = (mixed ? 1 : 0) | (warm ? 2 : 0) | ((long long)grid_blocks << 4) |
+                          ((long long)mg_coarsest_ << 24);
+    if (runner_key_ != key) {
+        if (mixed) {
+            BatchPlan<float> plan;
+            add_to_plan<float>(plan, p);
+            rc = runner_.build<float>(plan, grid_blocks);
+        } else {
+            BatchPlan<double> plan;
+            add_to_plan<double>(plan, p);
+            rc = runner_.build<double>(plan, grid_blocks);
+        }
+        if (rc) return fail(rc, runner_.error());
+        runner_key_ = key;
+    }
+    rc = mixed ? runner_.solve<float>(p, stream, launches) : runner_.solve<double>(p, stream, launches);
+    if (rc) return fail(rc, runner_.error());
+    return finish_batched(p, stream);
 }
 
 int Solver::bench_kernel(const Grid &g, int which, int reps, int grid_blocks, cudaStream_t stream, float *ms,
@@ -357,36 +401,22 @@ int Solver::bench_kernel(const Grid &g, int which, int reps, int grid_blocks, cu
         launch = [&]() { return launch_cg_direction(g, st_.r, st_.s, st_.sc, grid_blocks, stream); };
         break;
     case GBP_KERNEL_MG_PRESMOOTH:
-    case GBP_KERNEL_MG_SWEEP:
     case GBP_KERNEL_MG_RESTRICT:
     case GBP_KERNEL_MG_POST_BLACK:
-    case GBP_KERNEL_MG_RED_DOT: {
-        if (!(mixed ? mg32_ready_ : mg64_ready_)) return fail(GBP_ERR_INVALID_ARGUMENT, "bench_kernel: no multigrid yet");
-        const int k = which - GBP_KERNEL_MG_PRESMOOTH;
-        const double pc[] = {6.0, 7.0, 6.125, 7.125, 7.0};
-        per_cell = pc[k] * s;
-        if (mixed) launch = [&, k]() { return mg_bench_launch<float>(h32_, k, st_.sc, st_.pt, grid_blocks, stream); };
-        else launch = [&, k]() { return mg_bench_launch<double>(h64_, k, st_.sc, st_.pt, grid_blocks, stream); };
-        break;
-    }
+    case GBP_KERNEL_MG_RED_DOT:
     case GBP_KERNEL_PCG_DIRECTION:
     case GBP_KERNEL_PCG_SPMV:
     case GBP_KERNEL_PCG_UPDATE: {
-        if (!(mixed ? mg32_ready_ : mg64_ready_)) return fail(GBP_ERR_INVALID_ARGUMENT, "bench_kernel: no multigrid yet");
-        const int k = which - GBP_KERNEL_PCG_DIRECTION;
-        const double pc[] = {3.0, 6.0, 6.0};
+        if (runner_key_ < 0) return fail(GBP_ERR_INVALID_ARGUMENT, "bench_kernel: no multigrid solve yet");
+        static const int map[8] = {0, -1, 1, 2, 3, 4, 5, 6};
+        static const double pc[8] = {6.0, 7.0, 6.125, 7.125, 7.0, 3.0, 6.0, 6.0};
+        const int k = which - GBP_KERNEL_MG_PRESMOOTH;
         per_cell = pc[k] * s;
-        if (mixed)
-            launch = [&, k]() {
-                return pcg_bench_launch<float>(h32_, k, st_.df, st_.rf, st_.zf, st_.pf, st_.qf, st_.sc, st_.pt,
-                                               grid_blocks, stream);
-            };
-        else
-            launch = [&, k]() {
-                return pcg_bench_launch<double>(h64_, k, st_.x, st_.r, st_.z, st_.s, st_.q, st_.sc, st_.pt,
-                                                grid_blocks, stream);
-            };
-        break;
+        *bytes = per_cell * cells;
+        const int rk = map[k];
+        int rc = mixed ? runner_.bench<float>(rk, reps, stream, ms) : runner_.bench<double>(rk, reps, stream, ms);
+        if (rc) return fail(rc, runner_.error());
+        return GBP_OK;
     }
     default: return fail(GBP_ERR_INVALID_ARGUMENT, "bench_kernel: unknown kernel");
     }

@@ -8,6 +8,7 @@
 
 #include "gbp.h"
 #include "gbp_kernels.h"
+#include "gbp_batch.h"
 #include "gbp_mg.h"
 
 namespace gbp {
@@ -55,6 +56,17 @@ public:
     SolverState &state() { return st_; }
     const char *error() const { return err_.c_str(); }
 
+    // Batched MGPCG: per-scene setup (level-0 operator in T, Galerkin
+    // hierarchy), then this scene's entries of a batch plan.
+    int setup_mg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches);
+    template <class T> void add_to_plan(BatchPlan<T> &plan, const gbp_params &p) const;
+    // Reads this scene's scalars after a batched solve.
+    int finish_batched(const gbp_params &p, cudaStream_t stream);
+    // After the solve: FP64 true residual, iteration counts, status
+    // (GBP_OK / GBP_ERR_NOT_CONVERGED / GBP_ERR_NAN).
+    int complete(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches);
+    bool has_prev() const { return st_.have_prev; }
+
 private:
     int fail(int code, const std::string &m) {
         err_ = m;
@@ -65,7 +77,6 @@ private:
     int solve_cg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches);
     int solve_mg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches);
     int run_graph(const gbp_params &p, int chunk, cudaStream_t stream, long long *launches);
-    MgSettings mg_settings(const gbp_params &p) const;
 
     SolverState st_;
     Grid g_{};
@@ -85,6 +96,9 @@ private:
     long long graph_nodes_ = 0;
     int last_outer_ = 1;
     int last_inner_total_ = 0;
+    // batch of one for the scene's own MGPCG solves
+    BatchRunner runner_;
+    long long runner_key_ = -1;
 };
 
 }  // namespace gbp
