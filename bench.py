@@ -51,6 +51,9 @@ WORKLOADS = {
     "liquid3_128": dict(kind="liquid3", n=128, desc="3D liquid 128^3, solid sphere r=0.12, pool y<0.35 + drop r=0.18"),
     "smoke3_256": dict(kind="smoke3", n=256, desc="3D smoke 256^3, all fluid, solid cylinder r=0.1 along z"),
     "liquid2_128": dict(kind="liquid2", n=128, desc="2D liquid 128^2, pool y<0.3 + circle r=0.15"),
+    "served": dict(kind="served", n=0, desc="served stream: Poisson arrivals (seed 5, 8 requests/s), 70% liquid / 30% "
+                   "smoke, edge in {32,64,96,128,192,256}, 50 steps each, warm start, 150 GB HBM budget; "
+                   "--steps = number of requests"),
     "batch64_liquid3": dict(kind="batch", n=64, desc="64 independent 3D liquid scenes, edge log-uniform in "
                             "[32, 160], fluid fraction U[0.1, 0.6], one batched solve per step"),
 }
@@ -444,6 +447,55 @@ def run_gbp_batch(args):
         torch.distributed.destroy_process_group()
 
 
+def run_gbp_served(args):
+    """Continuous-batching server on a seeded Poisson request stream; the
+    same stream served with the mixed and the FP64 solver."""
+    import torch
+    from shiokaze_gb300.serving import ProjectionServer, poisson_requests
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    nreq = max(4, args.steps)
+    results = {}
+    sampler = ClockSampler(local)
+    for precision in ([args.precision] + ([] if args.no_compare else
+                                          ["fp64" if args.precision == "mixed" else "mixed"])):
+        warm = ProjectionServer(budget_bytes=150e9, precision=precision, device=local)
+        warm.serve(poisson_requests(3, 50.0, seed=99, edges=(32, 64), steps=3))  # JIT/graph warm-up
+        srv = ProjectionServer(budget_bytes=150e9, precision=precision, device=local)
+        reqs = poisson_requests(nreq, 8.0, seed=5, steps=50)
+        if precision == args.precision:
+            sampler.start()
+        torch.cuda.synchronize()
+        l0 = srv.ctx.launches()
+        done, out = srv.serve(reqs)
+        torch.cuda.synchronize()
+        out["gpu_launches"] = srv.ctx.launches() - l0
+        if precision == args.precision:
+            out["clocks"] = sampler.stop()
+        results[precision] = out
+    main = results[args.precision]
+    value = world * main["solves_per_s"]
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": "solves/s", "n_gpus": world, "steps": nreq,
+        "warmup": args.warmup, "ms_per_step": round(1000.0 / main["solves_per_s"], 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic (seeded Poisson request stream and scene generator)",
+        "config": {"workload": "served", "desc": WORKLOADS["served"]["desc"], "requests": nreq,
+                   "solver": "mgpcg", "precision": args.precision, "residual": 1e-6,
+                   "parallelism": f"replicas x{world}", "l2": "no flush: working set above the 129 MB L2"},
+        "latency_ms": main["step_latency_ms"],
+        "request_latency_s": main["request_latency_s"],
+        "serving": {k: main[k] for k in ("requests", "solves", "wall_s", "ticks", "mean_batch", "max_batch",
+                                         "batch_rebuilds", "peak_bytes", "admission_waits")},
+        "compare": {p: {"solves_per_s": round(r["solves_per_s"], 3), "step_latency_ms": r["step_latency_ms"]}
+                    for p, r in results.items() if p != args.precision},
+        "clocks": main.get("clocks"), "gpu_launches": int(main["gpu_launches"]),
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def run_reference(args):
     rank, world, local = dist_info()
     if rank != 0:
@@ -452,6 +504,8 @@ def run_reference(args):
     if WORKLOADS[args.workload]["kind"] == "batch":
         from shiokaze_gb300 import scenes as scn
         scene = min(scn.batch_liquid3(WORKLOADS[args.workload]["n"], seed=4), key=lambda sc: sc.cells)
+    elif WORKLOADS[args.workload]["kind"] == "served":
+        scene = make_scene("liquid3_128")
     else:
         scene = make_scene(args.workload)
     kind = "port"
@@ -515,6 +569,8 @@ def main():
         run_reference(args)
     elif WORKLOADS[args.workload]["kind"] == "batch":
         run_gbp_batch(args)
+    elif WORKLOADS[args.workload]["kind"] == "served":
+        run_gbp_served(args)
     else:
         run_gbp(args)
 

@@ -52,7 +52,7 @@ __device__ __forceinline__ double max_range(const double *part, int begin, int c
 }
 
 // cells (i, i+1) of the pair tile t: f(i, j, k, c, second)
-template <class F> __device__ __forceinline__ void pair_tile(const Grid &g, long long t, F f) {
+template <class F> __device__ __forceinline__ void pair_tile1(const Grid &g, long long t, F f) {
     const int px = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int ntx2 = (g.nx + 63) >> 6;
     const long long tx = t % ntx2, r = t / ntx2;
@@ -66,13 +66,21 @@ template <class F> __device__ __forceinline__ void pair_tile(const Grid &g, long
 }
 
 // cells of the cell tile t: f(i, j, k, c)
-template <class F> __device__ __forceinline__ void cell_tile(const Grid &g, long long t, F f) {
+template <class F> __device__ __forceinline__ void cell_tile1(const Grid &g, long long t, F f) {
     int i0, j0, k0;
     tile_origin(g, t, i0, j0, k0);
     const int i = i0 + (threadIdx.x & (TILE_X - 1)), j = j0 + threadIdx.x / TILE_X;
     if (i >= g.nx || j >= g.ny) return;
     const int kend = min(k0 + g.tz, g.nz);
     for (int k = k0; k < kend; ++k) f(i, j, k, cell_index(g, i, j, k));
+}
+
+// every tile of an item
+template <class F> __device__ __forceinline__ void pair_tile(const Grid &g, const BItem &it, F f) {
+    for (int t = 0; t < it.ntiles; ++t) pair_tile1(g, (long long)it.tile + t, f);
+}
+template <class F> __device__ __forceinline__ void cell_tile(const Grid &g, const BItem &it, F f) {
+    for (int t = 0; t < it.ntiles; ++t) cell_tile1(g, (long long)it.tile + t, f);
 }
 
 template <class T, class X>
@@ -91,18 +99,100 @@ __device__ __forceinline__ T nsum(const BLevel<T> &L, int i, int j, int k, long 
     return s;
 }
 
+
+// The level and scene of the current item, held in shared memory and
+// reloaded only when the item's level changes (each work list holds one
+// level per scene, so once per scene per block). Kernels then read the
+// descriptors from shared memory instead of chasing item -> level -> scene
+// pointers in global memory for every item.
+template <class T> struct ItemCtx {
+    BLevel<T> L;
+    BScene<T> S;
+    int skip;
+    double alpha, beta;
+    int overwrite;
+};
+
+template <class T>
+__device__ __forceinline__ void refresh(ItemCtx<T> &c, int &cur_ref, const BItem &it, const BLevel<T> *levels,
+                                        const BScene<T> *scenes, int gate) {
+    if (it.ref == cur_ref) return;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        c.L = levels[it.ref];
+        c.S = scenes[c.L.scene];
+        c.skip = gate < 0 ? 0 : gated(c.S.sc, gate);
+        c.alpha = c.S.sc->alpha;
+        c.beta = c.S.sc->beta;
+        c.overwrite = c.S.sc->first_update;
+    }
+    __syncthreads();
+    cur_ref = it.ref;
+}
+
+// Reduction over a work list with one partial per (block, scene): a block
+// walks its items (sorted by scene), accumulates a scene's cells in
+// `acc`, and flushes when the scene changes. The flush of block b for a
+// scene whose items occupy list positions [begin, begin+count) goes to slot
+// (b - begin) mod gridDim.x of that range; min(count, gridDim.x) blocks
+// flush per scene, and the one taking the scene's last ticket combines the
+// slots in slot order (deterministic for a given batch and grid).
+template <class T, class Acc, class Body, class Finish>
+__device__ __forceinline__ void reduce_items(const BItem *__restrict__ items, int n, double *part,
+                                             const BLevel<T> *levels, const BScene<T> *scenes, int gate,
+                                             ItemCtx<T> &ctx, Body body, Finish finish) {
+    __shared__ double sh[BLOCK_THREADS / 32];
+    int cur = -1;
+    BItem first{};
+    Acc acc;
+    acc.reset();
+    auto flush = [&]() {
+        const double v = acc.block(sh);
+        const int B = gridDim.x;
+        const int slot = (int)((((long long)blockIdx.x - first.begin) % B + B) % B);
+        if (threadIdx.x == 0) part[first.begin + slot] = v;
+        finish(first, min(first.count, B));
+    };
+    for (int w = blockIdx.x; w < n; w += gridDim.x) {
+        const BItem it = items[w];
+        if (it.ref != cur) {
+            // one level per scene in a list: a new level is a new scene
+            if (cur >= 0 && !ctx.skip) flush();
+            refresh(ctx, cur, it, levels, scenes, gate);
+            first = it;
+            acc.reset();
+        }
+        if (!ctx.skip) body(it, acc);
+    }
+    if (cur >= 0 && !ctx.skip) flush();
+}
+
+struct SumAcc {
+    double v;
+    __device__ void reset() { v = 0.0; }
+    __device__ double block(double *sh) { return block_sum(v, sh); }
+};
+struct MaxAcc {
+    double v;
+    __device__ void reset() { v = 0.0; }
+    __device__ double block(double *sh) { return block_max(v, sh); }
+};
+
 // ---- smoothing and transfers on the global-memory levels --------------------------
 
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) presmooth_kernel(const BLevel<T> *__restrict__ levels,
                                                                      const BItem *__restrict__ items, int n,
                                                                      const BScene<T> *__restrict__ scenes, int gate) {
+    __shared__ ItemCtx<T> ctx;
+    int cur = -1;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const BItem it = items[w];
-        const BLevel<T> &L = levels[it.ref];
-        if (gated(scenes[L.scene].sc, gate)) continue;
+        refresh(ctx, cur, it, levels, scenes, gate);
+        if (ctx.skip) continue;
+        const BLevel<T> &L = ctx.L;
         auto red_value = [&](long long m, int, int, int) { return __ldg(L.b + m) * __ldg(L.inv + m); };
-        pair_tile(L.g, it.tile, [&](int i, int j, int k, long long c, bool second) {
+        pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
             const bool a_red = ((i + j + k) & 1) == 0;
             for (int h = 0; h < (second ? 2 : 1); ++h) {
                 const long long cc = c + h;
@@ -120,12 +210,15 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) sweep_kernel(const BLevel<T>
                                                                  const BItem *__restrict__ items, int n,
                                                                  const BScene<T> *__restrict__ scenes, int gate,
                                                                  int color) {
+    __shared__ ItemCtx<T> ctx;
+    int cur = -1;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const BItem it = items[w];
-        const BLevel<T> &L = levels[it.ref];
-        if (gated(scenes[L.scene].sc, gate)) continue;
+        refresh(ctx, cur, it, levels, scenes, gate);
+        if (ctx.skip) continue;
+        const BLevel<T> &L = ctx.L;
         auto xval = [&](long long m, int, int, int) { return __ldg(L.x + m); };
-        pair_tile(L.g, it.tile, [&](int i, int j, int k, long long c, bool second) {
+        pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
             const int h = ((i + j + k) & 1) == color ? 0 : 1;
             if (h == 1 && !second) return;
             const long long cc = c + h;
@@ -139,13 +232,16 @@ template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) restrict_kernel(const BLevel<T> *__restrict__ levels,
                                                                     const BItem *__restrict__ items, int n,
                                                                     const BScene<T> *__restrict__ scenes, int gate) {
+    __shared__ ItemCtx<T> ctx;
+    int cur = -1;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const BItem it = items[w];
-        const BLevel<T> &L = levels[it.ref];
-        if (gated(scenes[L.scene].sc, gate)) continue;
+        refresh(ctx, cur, it, levels, scenes, gate);
+        if (ctx.skip) continue;
+        const BLevel<T> &L = ctx.L;
         const Grid &fg = L.g;
         auto xval = [&](long long m, int, int, int) { return __ldg(L.x + m); };
-        cell_tile(L.gc, it.tile, [&](int I, int J, int K, long long cc) {
+        cell_tile(L.gc, it, [&](int I, int J, int K, long long cc) {
             T sum = T(0);
             const int kmax = fg.dim == 3 ? 2 : 1;
             for (int c2 = 0; c2 < kmax; ++c2)
@@ -167,16 +263,19 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) post_black_kernel(const BLev
                                                                       const BItem *__restrict__ items, int n,
                                                                       const BScene<T> *__restrict__ scenes, int gate,
                                                                       T alpha) {
+    __shared__ ItemCtx<T> ctx;
+    int cur = -1;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const BItem it = items[w];
-        const BLevel<T> &L = levels[it.ref];
-        if (gated(scenes[L.scene].sc, gate)) continue;
+        refresh(ctx, cur, it, levels, scenes, gate);
+        if (ctx.skip) continue;
+        const BLevel<T> &L = ctx.L;
         const Grid &cg = L.gc;
         const bool d3 = L.g.dim == 3;
         auto corrected = [&](long long m, int ni, int nj, int nk) {
             return __ldg(L.x + m) + alpha * __ldg(L.xc + cell_index(cg, ni >> 1, nj >> 1, d3 ? (nk >> 1) : 0));
         };
-        pair_tile(L.g, it.tile, [&](int i, int j, int k, long long c, bool second) {
+        pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
             const int h = ((i + j + k) & 1) == 1 ? 0 : 1;
             if (h == 1 && !second) return;
             const long long cc = c + h;
@@ -186,55 +285,55 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) post_black_kernel(const BLev
 }
 
 // Last red pass of the fine level, with rho' = z . r (z = x, r = b there)
-// per scene; the scene's last item sets beta (0 for a new direction).
+// per scene; the scene's last flush sets beta (0 for a new direction).
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) red_dot_kernel(const BLevel<T> *__restrict__ levels,
+__global__ void __launch_bounds__(BLOCK_THREADS, 5) red_dot_kernel(const BLevel<T> *__restrict__ levels,
                                                                    const BItem *__restrict__ items, int n,
                                                                    const BScene<T> *__restrict__ scenes, int gate,
-                                                                   double *part) {
-    __shared__ double sh[BLOCK_THREADS / 32];
-    for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        const BItem it = items[w];
-        const BLevel<T> &L = levels[it.ref];
-        Scalars *sc = scenes[L.scene].sc;
-        if (gated(sc, gate)) continue;
-        double dot = 0.0;
-        auto xval = [&](long long m, int, int, int) { return __ldg(L.x + m); };
-        pair_tile(L.g, it.tile, [&](int i, int j, int k, long long c, bool second) {
-            const int hr = ((i + j + k) & 1) == 0 ? 0 : 1;
-            for (int h = 0; h < (second ? 2 : 1); ++h) {
-                const long long cc = c + h;
-                const T bv = __ldg(L.b + cc);
-                T xv;
-                if (h == hr) {
-                    xv = (bv + nsum(L, i + h, j, k, cc, xval)) * __ldg(L.inv + cc);
-                    L.x[cc] = xv;
-                } else {
-                    xv = L.x[cc];
+                                                                   double *part, const int *__restrict__ scene_of) {
+    __shared__ double shf[BLOCK_THREADS / 32];
+    __shared__ ItemCtx<T> ctx;
+    reduce_items<T, SumAcc>(
+        items, n, part, levels, scenes, gate, ctx,
+        [&](const BItem &it, SumAcc &acc) {
+            const BLevel<T> &L = ctx.L;
+            auto xval = [&](long long m, int, int, int) { return __ldg(L.x + m); };
+            pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
+                const int hr = ((i + j + k) & 1) == 0 ? 0 : 1;
+                for (int h = 0; h < (second ? 2 : 1); ++h) {
+                    const long long cc = c + h;
+                    const T bv = __ldg(L.b + cc);
+                    T xv;
+                    if (h == hr) {
+                        xv = (bv + nsum(L, i + h, j, k, cc, xval)) * __ldg(L.inv + cc);
+                        L.x[cc] = xv;
+                    } else {
+                        xv = L.x[cc];
+                    }
+                    acc.v = fma((double)xv, (double)bv, acc.v);
                 }
-                dot = fma((double)xv, (double)bv, dot);
+            });
+        },
+        [&](const BItem &it, int flushes) {
+            Scalars *sc = ctx.S.sc;
+            if (item_last(&sc->counter[SITE_DOT], flushes)) {
+                const double rho_new = sum_range(part, it.begin, flushes, shf);
+                if (threadIdx.x == 0) {
+                    if (sc->first) {
+                        sc->beta = 0.0;
+                        sc->first = 0;
+                    } else {
+                        sc->beta = rho_new / sc->rho;
+                    }
+                    sc->rho = rho_new;
+                    if (rho_new != rho_new) {
+                        sc->done = 1;
+                        sc->status = 3;
+                    }
+                    sc->counter[SITE_DOT] = 0;
+                }
             }
         });
-        const double bsum = block_sum(dot, sh);
-        if (threadIdx.x == 0) part[w] = bsum;
-        if (item_last(&sc->counter[SITE_DOT], it.count)) {
-            const double rho_new = sum_range(part, it.begin, it.count, sh);
-            if (threadIdx.x == 0) {
-                if (sc->first) {
-                    sc->beta = 0.0;
-                    sc->first = 0;
-                } else {
-                    sc->beta = rho_new / sc->rho;
-                }
-                sc->rho = rho_new;
-                if (rho_new != rho_new) {
-                    sc->done = 1;
-                    sc->status = 3;
-                }
-                sc->counter[SITE_DOT] = 0;
-            }
-        }
-    }
 }
 
 // ---- shared-memory tail, one block per scene -----------------------------------
@@ -401,112 +500,117 @@ template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) direction_kernel(const BLevel<T> *__restrict__ levels,
                                                                      const BItem *__restrict__ items, int n,
                                                                      const BScene<T> *__restrict__ scenes, int gate) {
+    __shared__ ItemCtx<T> ctx;
+    int cur = -1;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const BItem it = items[w];
-        const BLevel<T> &L = levels[it.ref];
-        const BScene<T> &S = scenes[L.scene];
-        if (gated(S.sc, gate)) continue;
-        const T beta = T(S.sc->beta);
-        if (beta == T(0)) cell_tile(L.g, it.tile, [&](int, int, int, long long c) { S.p[c] = S.z[c]; });
-        else cell_tile(L.g, it.tile, [&](int, int, int, long long c) { S.p[c] = S.z[c] + beta * S.p[c]; });
+        refresh(ctx, cur, it, levels, scenes, gate);
+        if (ctx.skip) continue;
+        const BLevel<T> &L = ctx.L;
+        const BScene<T> &S = ctx.S;
+        const T beta = T(ctx.beta);
+        if (beta == T(0)) cell_tile(L.g, it, [&](int, int, int, long long c) { S.p[c] = S.z[c]; });
+        else cell_tile(L.g, it, [&](int, int, int, long long c) { S.p[c] = S.z[c] + beta * S.p[c]; });
     }
 }
 
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) spmv_kernel(const BLevel<T> *__restrict__ levels,
+__global__ void __launch_bounds__(BLOCK_THREADS, 5) spmv_kernel(const BLevel<T> *__restrict__ levels,
                                                                 const BItem *__restrict__ items, int n,
                                                                 const BScene<T> *__restrict__ scenes, int gate,
-                                                                double *part) {
-    __shared__ double sh[BLOCK_THREADS / 32];
-    for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        const BItem it = items[w];
-        const BLevel<T> &L = levels[it.ref];
-        const BScene<T> &S = scenes[L.scene];
-        Scalars *sc = S.sc;
-        if (gated(sc, gate)) continue;
-        double dot = 0.0;
-        auto pval = [&](long long m, int, int, int) { return __ldg(S.p + m); };
-        cell_tile(L.g, it.tile, [&](int i, int j, int k, long long c) {
-            const T pc = __ldg(S.p + c);
-            const T qv = __ldg(L.diag + c) * pc - nsum(L, i, j, k, c, pval);
-            S.q[c] = qv;
-            dot = fma((double)pc, (double)qv, dot);
-        });
-        const double bsum = block_sum(dot, sh);
-        if (threadIdx.x == 0) part[w] = bsum;
-        if (item_last(&sc->counter[SITE_SPMV], it.count)) {
-            const double pq = sum_range(part, it.begin, it.count, sh);
-            if (threadIdx.x == 0) {
-                sc->pap = pq;
-                sc->alpha = sc->rho / pq;
-                sc->counter[SITE_SPMV] = 0;
+                                                                double *part, const int *__restrict__ scene_of) {
+    __shared__ double shf[BLOCK_THREADS / 32];
+    __shared__ ItemCtx<T> ctx;
+    reduce_items<T, SumAcc>(
+        items, n, part, levels, scenes, gate, ctx,
+        [&](const BItem &it, SumAcc &acc) {
+            const BLevel<T> &L = ctx.L;
+            const BScene<T> &S = ctx.S;
+            auto pval = [&](long long m, int, int, int) { return __ldg(S.p + m); };
+            cell_tile(L.g, it, [&](int i, int j, int k, long long c) {
+                const T pc = __ldg(S.p + c);
+                const T qv = __ldg(L.diag + c) * pc - nsum(L, i, j, k, c, pval);
+                S.q[c] = qv;
+                acc.v = fma((double)pc, (double)qv, acc.v);
+            });
+        },
+        [&](const BItem &it, int flushes) {
+            Scalars *sc = ctx.S.sc;
+            if (item_last(&sc->counter[SITE_SPMV], flushes)) {
+                const double pq = sum_range(part, it.begin, flushes, shf);
+                if (threadIdx.x == 0) {
+                    sc->pap = pq;
+                    sc->alpha = sc->rho / pq;
+                    sc->counter[SITE_SPMV] = 0;
+                }
             }
-        }
-    }
+        });
 }
 
 // x += alpha p (x = alpha p on the first update of a solve), r -= alpha q,
 // |r|_inf. mode 0: the solve's stopping rule; mode 1: inner solve.
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) update_kernel(const BLevel<T> *__restrict__ levels,
+__global__ void __launch_bounds__(BLOCK_THREADS, 5) update_kernel(const BLevel<T> *__restrict__ levels,
                                                                   const BItem *__restrict__ items, int n,
                                                                   const BScene<T> *__restrict__ scenes, int gate,
-                                                                  double *part, int mode, BatchCounters *cnt) {
-    __shared__ double sh[BLOCK_THREADS / 32];
-    for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        const BItem it = items[w];
-        const BLevel<T> &L = levels[it.ref];
-        const BScene<T> &S = scenes[L.scene];
-        Scalars *sc = S.sc;
-        if (gated(sc, gate)) continue;
-        const T alpha = T(sc->alpha);
-        const bool overwrite = sc->first_update != 0;
-        double mx = 0.0;
-        cell_tile(L.g, it.tile, [&](int, int, int, long long c) {
-            const T pc = S.p[c];
-            S.x[c] = overwrite ? alpha * pc : S.x[c] + alpha * pc;
-            const T rv = S.r[c] - alpha * S.q[c];
-            S.r[c] = rv;
-            mx = fmax(mx, fabs((double)rv));
-        });
-        const double bm = block_max(mx, sh);
-        if (threadIdx.x == 0) part[w] = bm;
-        if (item_last(&sc->counter[SITE_UPDATE], it.count)) {
-            const double res = max_range(part, it.begin, it.count, sh);
-            if (threadIdx.x == 0) {
-                sc->first_update = 0;
-                sc->iter += 1;
-                const bool bad = res != res || sc->alpha != sc->alpha;
-                int finished = 0;
-                if (mode == 0) {
-                    sc->res = res;
-                    if (bad) {
-                        sc->status = 3;
-                        finished = 1;
-                    } else if (res <= sc->tol) {
-                        sc->status = 1;
-                        finished = 1;
-                    } else if (sc->iter >= sc->max_iter) {
-                        sc->status = 2;
-                        finished = 1;
+                                                                  double *part, int mode, BatchCounters *cnt,
+                                                                  const int *__restrict__ scene_of) {
+    __shared__ double shf[BLOCK_THREADS / 32];
+    __shared__ ItemCtx<T> ctx;
+    reduce_items<T, MaxAcc>(
+        items, n, part, levels, scenes, gate, ctx,
+        [&](const BItem &it, MaxAcc &acc) {
+            const BLevel<T> &L = ctx.L;
+            const BScene<T> &S = ctx.S;
+            const T alpha = T(ctx.alpha);
+            const bool overwrite = ctx.overwrite != 0;
+            cell_tile(L.g, it, [&](int, int, int, long long c) {
+                const T pc = S.p[c];
+                S.x[c] = overwrite ? alpha * pc : S.x[c] + alpha * pc;
+                const T rv = S.r[c] - alpha * S.q[c];
+                S.r[c] = rv;
+                acc.v = fmax(acc.v, fabs((double)rv));
+            });
+        },
+        [&](const BItem &it, int flushes) {
+            Scalars *sc = ctx.S.sc;
+            if (item_last(&sc->counter[SITE_UPDATE], flushes)) {
+                const double res = max_range(part, it.begin, flushes, shf);
+                if (threadIdx.x == 0) {
+                    sc->first_update = 0;
+                    sc->iter += 1;
+                    const bool bad = res != res || sc->alpha != sc->alpha;
+                    int finished = 0;
+                    if (mode == 0) {
+                        sc->res = res;
+                        if (bad) {
+                            sc->status = 3;
+                            finished = 1;
+                        } else if (res <= sc->tol) {
+                            sc->status = 1;
+                            finished = 1;
+                        } else if (sc->iter >= sc->max_iter) {
+                            sc->status = 2;
+                            finished = 1;
+                        }
+                    } else {
+                        sc->inner_iter += 1;
+                        if (bad) {
+                            sc->status = 3;
+                            finished = 1;
+                        } else if (res <= sc->inner_tol || sc->inner_iter >= sc->inner_max ||
+                                   sc->iter >= sc->max_iter) {
+                            sc->inner_done = 1;
+                        }
                     }
-                } else {
-                    sc->inner_iter += 1;
-                    if (bad) {
-                        sc->status = 3;
-                        finished = 1;
-                    } else if (res <= sc->inner_tol || sc->inner_iter >= sc->inner_max || sc->iter >= sc->max_iter) {
-                        sc->inner_done = 1;
+                    if (finished) {
+                        sc->done = 1;
+                        atomicSub(&cnt->remaining, 1);
                     }
+                    sc->counter[SITE_UPDATE] = 0;
                 }
-                if (finished) {
-                    sc->done = 1;
-                    atomicSub(&cnt->remaining, 1);
-                }
-                sc->counter[SITE_UPDATE] = 0;
             }
-        }
-    }
+        });
 }
 
 // ---- mixed precision: FP64 refinement -------------------------------------------------
@@ -515,98 +619,101 @@ template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) refine_accumulate_kernel(const BLevel<T> *__restrict__ levels,
                                                                              const BItem *__restrict__ items, int n,
                                                                              const BScene<T> *__restrict__ scenes) {
+    __shared__ ItemCtx<T> ctx;
+    int cur = -1;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const BItem it = items[w];
-        const BLevel<T> &L = levels[it.ref];
-        const BScene<T> &S = scenes[L.scene];
-        if (gated(S.sc, 2)) continue;
-        cell_tile(L.g, it.tile, [&](int, int, int, long long c) { S.x64[c] += (double)S.x[c]; });
+        refresh(ctx, cur, it, levels, scenes, 2);
+        if (ctx.skip) continue;
+        const BLevel<T> &L = ctx.L;
+        const BScene<T> &S = ctx.S;
+        cell_tile(L.g, it, [&](int, int, int, long long c) { S.x64[c] += (double)S.x[c]; });
     }
 }
 
 // r64 = b - A64 (prev + x64) (x64 absent: initial), r_T = r64, |r64|_inf;
-// the scene's last item applies the stopping rule and opens the next inner
+// the scene's last flush applies the stopping rule and opens the next inner
 // solve. initial: sets the threshold, zeroes x64.
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) refine_residual_kernel(
+__global__ void __launch_bounds__(BLOCK_THREADS, 5) refine_residual_kernel(
     const BLevel<T> *__restrict__ levels, const BItem *__restrict__ items, int n,
     const BScene<T> *__restrict__ scenes, double *part, int initial, double residual, int max_iter,
-    double inner_rel, int inner_max, BatchCounters *cnt) {
-    __shared__ double sh[BLOCK_THREADS / 32];
-    for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        const BItem it = items[w];
-        const BLevel<T> &L = levels[it.ref];
-        const BScene<T> &S = scenes[L.scene];
-        Scalars *sc = S.sc;
-        if (!initial && gated(sc, 2)) continue;
-        const Grid &g = L.g;
-        const long long sy = g.nx, sz = (long long)g.nx * g.ny;
-        const Operator<double> &A = S.A;
-        auto X = [&](long long c) {
-            double v = initial ? 0.0 : S.x64[c];
-            if (S.prev) v += S.prev[c];
-            return v;
-        };
-        double mx = 0.0;
-        cell_tile(g, it.tile, [&](int i, int j, int k, long long c) {
-            double acc = A.diag[c] * X(c);
-            if (i > 0) acc -= A.cx[c - 1] * X(c - 1);
-            if (i + 1 < g.nx) acc -= A.cx[c] * X(c + 1);
-            if (j > 0) acc -= A.cy[c - sy] * X(c - sy);
-            if (j + 1 < g.ny) acc -= A.cy[c] * X(c + sy);
-            if (g.dim == 3) {
-                if (k > 0) acc -= A.cz[c - sz] * X(c - sz);
-                if (k + 1 < g.nz) acc -= A.cz[c] * X(c + sz);
+    double inner_rel, int inner_max, BatchCounters *cnt, const int *__restrict__ scene_of) {
+    __shared__ double shf[BLOCK_THREADS / 32];
+    __shared__ ItemCtx<T> ctx;
+    reduce_items<T, MaxAcc>(
+        items, n, part, levels, scenes, initial ? -1 : 2, ctx,
+        [&](const BItem &it, MaxAcc &acc) {
+            const BLevel<T> &L = ctx.L;
+            const BScene<T> &S = ctx.S;
+            const Grid &g = L.g;
+            const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+            const Operator<double> &A = S.A;
+            auto X = [&](long long c) {
+                double v = initial ? 0.0 : S.x64[c];
+                if (S.prev) v += S.prev[c];
+                return v;
+            };
+            cell_tile(g, it, [&](int i, int j, int k, long long c) {
+                double a = A.diag[c] * X(c);
+                if (i > 0) a -= A.cx[c - 1] * X(c - 1);
+                if (i + 1 < g.nx) a -= A.cx[c] * X(c + 1);
+                if (j > 0) a -= A.cy[c - sy] * X(c - sy);
+                if (j + 1 < g.ny) a -= A.cy[c] * X(c + sy);
+                if (g.dim == 3) {
+                    if (k > 0) a -= A.cz[c - sz] * X(c - sz);
+                    if (k + 1 < g.nz) a -= A.cz[c] * X(c + sz);
+                }
+                const double rv = S.b[c] - a;
+                S.r64[c] = rv;
+                S.r[c] = T(rv);
+                acc.v = fmax(acc.v, fabs(rv));
+            });
+            if (initial) cell_tile(g, it, [&](int, int, int, long long c) { S.x64[c] = 0.0; });
+        },
+        [&](const BItem &it, int flushes) {
+            Scalars *sc = ctx.S.sc;
+            if (item_last(&sc->counter[SITE_REFINE], flushes)) {
+                const double res = max_range(part, it.begin, flushes, shf);
+                if (threadIdx.x == 0) {
+                    if (initial) {
+                        const double tolf = residual < 1e-30 ? 1e-30 : residual;
+                        sc->res0 = res;
+                        sc->tol = tolf * res;
+                        sc->iter = 0;
+                        sc->outer_iter = 0;
+                        sc->max_iter = max_iter;
+                        sc->inner_max = inner_max;
+                        sc->status = 0;
+                        sc->done = 0;
+                    } else {
+                        sc->outer_iter += 1;
+                    }
+                    sc->res = res;
+                    int finished = 1;
+                    if (res != res) {
+                        sc->status = 3;
+                    } else if (res <= sc->tol) {
+                        sc->status = 1;
+                    } else if (sc->iter >= sc->max_iter) {
+                        sc->status = 2;
+                    } else {
+                        finished = 0;
+                        sc->inner_done = 0;
+                        sc->inner_iter = 0;
+                        sc->first = 1;
+                        sc->first_update = 1;
+                        sc->inner_res0 = res;
+                        sc->inner_tol = inner_rel * res;
+                    }
+                    if (finished) {
+                        sc->done = 1;
+                        atomicSub(&cnt->remaining, 1);
+                    }
+                    sc->counter[SITE_REFINE] = 0;
+                }
             }
-            const double rv = S.b[c] - acc;
-            S.r64[c] = rv;
-            S.r[c] = T(rv);
-            mx = fmax(mx, fabs(rv));
         });
-        if (initial) cell_tile(g, it.tile, [&](int, int, int, long long c) { S.x64[c] = 0.0; });
-        const double bm = block_max(mx, sh);
-        if (threadIdx.x == 0) part[w] = bm;
-        if (item_last(&sc->counter[SITE_REFINE], it.count)) {
-            const double res = max_range(part, it.begin, it.count, sh);
-            if (threadIdx.x == 0) {
-                if (initial) {
-                    const double tolf = residual < 1e-30 ? 1e-30 : residual;
-                    sc->res0 = res;
-                    sc->tol = tolf * res;
-                    sc->iter = 0;
-                    sc->outer_iter = 0;
-                    sc->max_iter = max_iter;
-                    sc->inner_max = inner_max;
-                    sc->status = 0;
-                    sc->done = 0;
-                } else {
-                    sc->outer_iter += 1;
-                }
-                sc->res = res;
-                int finished = 1;
-                if (res != res) {
-                    sc->status = 3;
-                } else if (res <= sc->tol) {
-                    sc->status = 1;
-                } else if (sc->iter >= sc->max_iter) {
-                    sc->status = 2;
-                } else {
-                    finished = 0;
-                    sc->inner_done = 0;
-                    sc->inner_iter = 0;
-                    sc->first = 1;
-                    sc->first_update = 1;
-                    sc->inner_res0 = res;
-                    sc->inner_tol = inner_rel * res;
-                }
-                if (finished) {
-                    sc->done = 1;
-                    atomicSub(&cnt->remaining, 1);
-                }
-                sc->counter[SITE_REFINE] = 0;
-            }
-        }
-    }
 }
 
 }  // namespace
@@ -638,7 +745,7 @@ cudaError_t b_post_black(const BLaunch &L, const BLevel<T> *levels, const BItem 
 template <class T>
 cudaError_t b_red_dot(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
                       double *part) {
-    red_dot_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate, part);
+    red_dot_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate, part, L.scene_of);
     return cudaGetLastError();
 }
 template <class T>
@@ -659,13 +766,14 @@ cudaError_t b_direction(const BLaunch &L, const BLevel<T> *levels, const BItem *
 template <class T>
 cudaError_t b_spmv(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
                    double *part) {
-    spmv_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate, part);
+    spmv_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate, part, L.scene_of);
     return cudaGetLastError();
 }
 template <class T>
 cudaError_t b_update(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
                      double *part, int mode, BatchCounters *cnt) {
-    update_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate, part, mode, cnt);
+    update_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate, part, mode, cnt,
+                                                               L.scene_of);
     return cudaGetLastError();
 }
 template <class T>
@@ -678,8 +786,8 @@ template <class T>
 cudaError_t b_refine_residual(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
                               const BScene<T> *scenes, double *part, int initial, double residual, int max_iter,
                               double inner_rel, int inner_max, BatchCounters *cnt) {
-    refine_residual_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, part, initial,
-                                                                       residual, max_iter, inner_rel, inner_max, cnt);
+    refine_residual_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(
+        levels, items, n, scenes, part, initial, residual, max_iter, inner_rel, inner_max, cnt, L.scene_of);
     return cudaGetLastError();
 }
 

@@ -37,6 +37,7 @@ void BatchRunner::release() {
     if (h_counters_) cudaFreeHost(h_counters_);
     h_counters_ = nullptr;
     d_levels_ = d_scenes_ = d_tails_ = nullptr;
+    d_scene_of_ = nullptr;
     d_pair_.clear();
     d_restrict_.clear();
     n_pair_.clear();
@@ -54,7 +55,8 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
         RUN_CUDA(cudaMalloc(&d, bytes ? bytes : 16));
         owned_.push_back(d);
         bytes_ += bytes;
-        if (bytes) RUN_CUDA(cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice));
+        if (bytes && src) RUN_CUDA(cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice));
+        else if (bytes) RUN_CUDA(cudaMemset(d, 0, bytes));
         *dst = d;
         return GBP_OK;
     };
@@ -66,6 +68,11 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
     mixed_ = sizeof(T) == 4;
     if ((rc = upload(plan.levels.data(), plan.levels.size() * sizeof(BLevel<T>), &d_levels_))) return rc;
     if ((rc = upload(plan.scenes.data(), plan.scenes.size() * sizeof(BScene<T>), &d_scenes_))) return rc;
+    {
+        void *d;
+        if ((rc = upload(plan.scene_of.data(), plan.scene_of.size() * sizeof(int), &d))) return rc;
+        d_scene_of_ = static_cast<int *>(d);
+    }
     if ((rc = upload(plan.tails.data(), plan.tails.size() * sizeof(BTail<T>), &d_tails_))) return rc;
     size_t max_items = std::max(plan.fine_cells.size(), plan.fine_pairs.size());
     for (int l = 0; l < plan.max_global; ++l) {
@@ -112,7 +119,7 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
     auto *sc = static_cast<const BScene<T> *>(d_scenes_);
     auto *tl = static_cast<const BTail<T> *>(d_tails_);
     cudaError_t e = cudaSuccess;
-    auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, gate}; };
+    auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, gate, d_scene_of_}; };
     // descend
     for (int l = 0; l < max_global_ && e == cudaSuccess; ++l) {
         e = b_presmooth<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc);
@@ -126,7 +133,7 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
         ++*nodes;
     }
     if (e == cudaSuccess && tail_smem_ > 0) {
-        e = b_tail<T>(BLaunch{nscenes_, st, gate}, tl, nscenes_, sc, ms, tail_smem_);
+        e = b_tail<T>(BLaunch{nscenes_, st, gate, d_scene_of_}, tl, nscenes_, sc, ms, tail_smem_);
         ++*nodes;
     }
     // ascend
@@ -150,7 +157,7 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
         e = b_update<T>(L(n_fine_cells_), lv, d_fine_cells_, n_fine_cells_, sc, d_part_, mixed_ ? 1 : 0, d_counters_);
     *nodes += 3;
     if (mixed_ && e == cudaSuccess) {
-        const BLaunch L2{blocks_for(n_fine_cells_, grid_blocks_), st, 2};
+        const BLaunch L2{blocks_for(n_fine_cells_, grid_blocks_), st, 2, d_scene_of_};
         e = b_refine_accumulate<T>(L2, lv, d_fine_cells_, n_fine_cells_, sc);
         if (e == cudaSuccess)
             e = b_refine_residual<T>(L2, lv, d_fine_cells_, n_fine_cells_, sc, d_part_, 0, p.residual,
@@ -167,7 +174,8 @@ template <class T> int BatchRunner::solve(const gbp_params &p, cudaStream_t st, 
     h_counters_->remaining = nscenes_;
     RUN_CUDA(cudaMemcpyAsync(d_counters_, h_counters_, sizeof(BatchCounters), cudaMemcpyHostToDevice, st));
     // initial residual of every scene (also zeroes x64, sets thresholds)
-    RUN_CUDA(b_refine_residual<T>(BLaunch{blocks_for(n_fine_cells_, grid_blocks_), st, 0}, lv, d_fine_cells_,
+    RUN_CUDA(b_refine_residual<T>(BLaunch{blocks_for(n_fine_cells_, grid_blocks_), st, 0, d_scene_of_}, lv,
+                                  d_fine_cells_,
                                   n_fine_cells_, sc, d_part_, 1, p.residual, p.max_iterations, inner_rel_, kInnerMax,
                                   d_counters_));
     *launches += 1;
@@ -209,7 +217,7 @@ template <class T> int BatchRunner::bench(int which, int reps, cudaStream_t st, 
     auto *sc = static_cast<const BScene<T> *>(d_scenes_);
     const MgSettings mset = settings_of(gbp_params{});
     std::function<cudaError_t()> launch;
-    auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, 0}; };
+    auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, 0, d_scene_of_}; };
     switch (which) {
     case 0: launch = [&]() { return b_presmooth<T>(L(n_pair_[0]), lv, d_pair_[0], n_pair_[0], sc); }; break;
     case 1: launch = [&]() { return b_restrict<T>(L(n_restrict_[0]), lv, d_restrict_[0], n_restrict_[0], sc); }; break;

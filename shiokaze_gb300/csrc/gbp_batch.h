@@ -50,11 +50,16 @@ template <class T> struct BScene {
 };
 
 struct BItem {
-    int ref;    // level table index (or scene index for fine-level lists)
-    int tile;   // tile index in the kernel's tiling of that level
-    int begin;  // first item of this scene in the list
-    int count;  // items of this scene in the list
+    int ref;     // level table index
+    int tile;    // first tile (in the kernel's tiling of that level)
+    int ntiles;  // consecutive tiles of the item
+    int begin;   // first item of this scene in the list
+    int count;   // items of this scene in the list
 };
+
+// Tiles per item (items are the unit of load balance; reductions are per
+// block, so small items cost little).
+constexpr int BITEM_CELLS = 512;
 
 template <class T> struct BTail {
     int nt;
@@ -76,6 +81,7 @@ template <class T> struct BatchPlan {
     int nscenes = 0;
     int max_global = 0;                  // max over scenes of the tail level
     std::vector<BLevel<T>> levels;       // all scenes' global levels
+    std::vector<int> scene_of;           // scene of each level entry
     std::vector<BScene<T>> scenes;
     std::vector<BTail<T>> tails;
     size_t tail_smem = 0;
@@ -121,6 +127,7 @@ private:
     std::vector<void *> owned_;
     // device copies
     void *d_levels_ = nullptr, *d_scenes_ = nullptr, *d_tails_ = nullptr;
+    int *d_scene_of_ = nullptr;
     std::vector<BItem *> d_pair_, d_restrict_;
     std::vector<int> n_pair_, n_restrict_;
     BItem *d_fine_cells_ = nullptr, *d_fine_pairs_ = nullptr;
@@ -140,6 +147,7 @@ struct BLaunch {
     int blocks;
     cudaStream_t stream;
     int gate;
+    const int *scene_of;  // scene of each level-table entry (reductions)
 };
 
 template <class T>
