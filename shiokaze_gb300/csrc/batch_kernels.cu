@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) post_black_kernel(const BLev
 // Last red pass of the fine level, with rho' = z . r (z = x, r = b there)
 // per scene; the scene's last flush sets beta (0 for a new direction).
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 5) red_dot_kernel(const BLevel<T> *__restrict__ levels,
+__global__ void __launch_bounds__(BLOCK_THREADS, 6) red_dot_kernel(const BLevel<T> *__restrict__ levels,
                                                                    const BItem *__restrict__ items, int n,
                                                                    const BScene<T> *__restrict__ scenes, int gate,
                                                                    double *part, const int *__restrict__ scene_of) {
@@ -515,7 +515,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) direction_kernel(const BLeve
 }
 
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 5) spmv_kernel(const BLevel<T> *__restrict__ levels,
+__global__ void __launch_bounds__(BLOCK_THREADS, 6) spmv_kernel(const BLevel<T> *__restrict__ levels,
                                                                 const BItem *__restrict__ items, int n,
                                                                 const BScene<T> *__restrict__ scenes, int gate,
                                                                 double *part, const int *__restrict__ scene_of) {
@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 5) spmv_kernel(const BLevel<T> 
 // x += alpha p (x = alpha p on the first update of a solve), r -= alpha q,
 // |r|_inf. mode 0: the solve's stopping rule; mode 1: inner solve.
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 5) update_kernel(const BLevel<T> *__restrict__ levels,
+__global__ void __launch_bounds__(BLOCK_THREADS, 6) update_kernel(const BLevel<T> *__restrict__ levels,
                                                                   const BItem *__restrict__ items, int n,
                                                                   const BScene<T> *__restrict__ scenes, int gate,
                                                                   double *part, int mode, BatchCounters *cnt,
@@ -635,7 +635,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) refine_accumulate_kernel(con
 // the scene's last flush applies the stopping rule and opens the next inner
 // solve. initial: sets the threshold, zeroes x64.
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 5) refine_residual_kernel(
+__global__ void __launch_bounds__(BLOCK_THREADS, 6) refine_residual_kernel(
     const BLevel<T> *__restrict__ levels, const BItem *__restrict__ items, int n,
     const BScene<T> *__restrict__ scenes, double *part, int initial, double residual, int max_iter,
     double inner_rel, int inner_max, BatchCounters *cnt, const int *__restrict__ scene_of) {

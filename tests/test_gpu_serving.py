@@ -30,8 +30,9 @@ def _rel(a, b, neumann):
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_served_results_equal_alone(precision):
     from shiokaze_gb300.serving import ProjectionServer, Request, simulate_alone
-    reqs = [Request(0, 0.00, "liquid", 24, 5, 11), Request(1, 0.02, "smoke", 16, 4, 12),
-            Request(2, 0.03, "liquid", 32, 6, 13), Request(3, 0.25, "liquid", 20, 3, 14)]
+    # three requests arrive together (they must share ticks), one later
+    reqs = [Request(0, 0.0, "liquid", 24, 5, 11), Request(1, 0.0, "smoke", 16, 4, 12),
+            Request(2, 0.0, "liquid", 32, 6, 13), Request(3, 0.2, "liquid", 20, 3, 14)]
     final = {}
 
     def rec(rid, step, p, vel):
