@@ -138,7 +138,7 @@ __device__ __forceinline__ void refresh(ItemCtx<T> &c, int &cur_ref, const BItem
 // flush per scene, and the one taking the scene's last ticket combines the
 // slots in slot order (deterministic for a given batch and grid).
 template <class T, class Acc, class Body, class Finish>
-__device__ __forceinline__ void reduce_items(const BItem *__restrict__ items, int n, double *part,
+__device__ __forceinline__ void reduce_items(const BSeg *__restrict__ segs, int nseg, int n, double *part,
                                              const BLevel<T> *levels, const BScene<T> *scenes, int gate,
                                              ItemCtx<T> &ctx, Body body, Finish finish) {
     __shared__ double sh[BLOCK_THREADS / 32];
@@ -153,8 +153,9 @@ __device__ __forceinline__ void reduce_items(const BItem *__restrict__ items, in
         if (threadIdx.x == 0) part[first.begin + slot] = v;
         finish(first, min(first.count, B));
     };
+    int sgc = 0;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        const BItem it = items[w];
+        const BItem it = item_at(segs, nseg, w, sgc);
         if (it.ref != cur) {
             // one level per scene in a list: a new level is a new scene
             if (cur >= 0 && !ctx.skip) flush();
@@ -182,12 +183,13 @@ struct MaxAcc {
 
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) presmooth_kernel(const BLevel<T> *__restrict__ levels,
-                                                                     const BItem *__restrict__ items, int n,
+                                                                     const BSeg *__restrict__ segs, int nseg, int n,
                                                                      const BScene<T> *__restrict__ scenes, int gate) {
     __shared__ ItemCtx<T> ctx;
     int cur = -1;
+    int sgc = 0;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        const BItem it = items[w];
+        const BItem it = item_at(segs, nseg, w, sgc);
         refresh(ctx, cur, it, levels, scenes, gate);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
@@ -207,13 +209,14 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) presmooth_kernel(const BLeve
 
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) sweep_kernel(const BLevel<T> *__restrict__ levels,
-                                                                 const BItem *__restrict__ items, int n,
+                                                                 const BSeg *__restrict__ segs, int nseg, int n,
                                                                  const BScene<T> *__restrict__ scenes, int gate,
                                                                  int color) {
     __shared__ ItemCtx<T> ctx;
     int cur = -1;
+    int sgc = 0;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        const BItem it = items[w];
+        const BItem it = item_at(segs, nseg, w, sgc);
         refresh(ctx, cur, it, levels, scenes, gate);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
@@ -230,12 +233,13 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) sweep_kernel(const BLevel<T>
 // items are cell tiles of the coarse grid gc
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) restrict_kernel(const BLevel<T> *__restrict__ levels,
-                                                                    const BItem *__restrict__ items, int n,
+                                                                    const BSeg *__restrict__ segs, int nseg, int n,
                                                                     const BScene<T> *__restrict__ scenes, int gate) {
     __shared__ ItemCtx<T> ctx;
     int cur = -1;
+    int sgc = 0;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        const BItem it = items[w];
+        const BItem it = item_at(segs, nseg, w, sgc);
         refresh(ctx, cur, it, levels, scenes, gate);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
@@ -260,13 +264,14 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) restrict_kernel(const BLevel
 
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) post_black_kernel(const BLevel<T> *__restrict__ levels,
-                                                                      const BItem *__restrict__ items, int n,
+                                                                      const BSeg *__restrict__ segs, int nseg, int n,
                                                                       const BScene<T> *__restrict__ scenes, int gate,
                                                                       T alpha) {
     __shared__ ItemCtx<T> ctx;
     int cur = -1;
+    int sgc = 0;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        const BItem it = items[w];
+        const BItem it = item_at(segs, nseg, w, sgc);
         refresh(ctx, cur, it, levels, scenes, gate);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
@@ -288,13 +293,13 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) post_black_kernel(const BLev
 // per scene; the scene's last flush sets beta (0 for a new direction).
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) red_dot_kernel(const BLevel<T> *__restrict__ levels,
-                                                                   const BItem *__restrict__ items, int n,
+                                                                   const BSeg *__restrict__ segs, int nseg, int n,
                                                                    const BScene<T> *__restrict__ scenes, int gate,
                                                                    double *part, const int *__restrict__ scene_of) {
     __shared__ double shf[BLOCK_THREADS / 32];
     __shared__ ItemCtx<T> ctx;
     reduce_items<T, SumAcc>(
-        items, n, part, levels, scenes, gate, ctx,
+        segs, nseg, n, part, levels, scenes, gate, ctx,
         [&](const BItem &it, SumAcc &acc) {
             const BLevel<T> &L = ctx.L;
             auto xval = [&](long long m, int, int, int) { return __ldg(L.x + m); };
@@ -498,12 +503,13 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
 
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) direction_kernel(const BLevel<T> *__restrict__ levels,
-                                                                     const BItem *__restrict__ items, int n,
+                                                                     const BSeg *__restrict__ segs, int nseg, int n,
                                                                      const BScene<T> *__restrict__ scenes, int gate) {
     __shared__ ItemCtx<T> ctx;
     int cur = -1;
+    int sgc = 0;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        const BItem it = items[w];
+        const BItem it = item_at(segs, nseg, w, sgc);
         refresh(ctx, cur, it, levels, scenes, gate);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
@@ -516,13 +522,13 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) direction_kernel(const BLeve
 
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) spmv_kernel(const BLevel<T> *__restrict__ levels,
-                                                                const BItem *__restrict__ items, int n,
+                                                                const BSeg *__restrict__ segs, int nseg, int n,
                                                                 const BScene<T> *__restrict__ scenes, int gate,
                                                                 double *part, const int *__restrict__ scene_of) {
     __shared__ double shf[BLOCK_THREADS / 32];
     __shared__ ItemCtx<T> ctx;
     reduce_items<T, SumAcc>(
-        items, n, part, levels, scenes, gate, ctx,
+        segs, nseg, n, part, levels, scenes, gate, ctx,
         [&](const BItem &it, SumAcc &acc) {
             const BLevel<T> &L = ctx.L;
             const BScene<T> &S = ctx.S;
@@ -551,14 +557,14 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) spmv_kernel(const BLevel<T> 
 // |r|_inf. mode 0: the solve's stopping rule; mode 1: inner solve.
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) update_kernel(const BLevel<T> *__restrict__ levels,
-                                                                  const BItem *__restrict__ items, int n,
+                                                                  const BSeg *__restrict__ segs, int nseg, int n,
                                                                   const BScene<T> *__restrict__ scenes, int gate,
                                                                   double *part, int mode, BatchCounters *cnt,
                                                                   const int *__restrict__ scene_of) {
     __shared__ double shf[BLOCK_THREADS / 32];
     __shared__ ItemCtx<T> ctx;
     reduce_items<T, MaxAcc>(
-        items, n, part, levels, scenes, gate, ctx,
+        segs, nseg, n, part, levels, scenes, gate, ctx,
         [&](const BItem &it, MaxAcc &acc) {
             const BLevel<T> &L = ctx.L;
             const BScene<T> &S = ctx.S;
@@ -617,12 +623,13 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) update_kernel(const BLevel<T
 
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) refine_accumulate_kernel(const BLevel<T> *__restrict__ levels,
-                                                                             const BItem *__restrict__ items, int n,
+                                                                             const BSeg *__restrict__ segs, int nseg, int n,
                                                                              const BScene<T> *__restrict__ scenes) {
     __shared__ ItemCtx<T> ctx;
     int cur = -1;
+    int sgc = 0;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        const BItem it = items[w];
+        const BItem it = item_at(segs, nseg, w, sgc);
         refresh(ctx, cur, it, levels, scenes, 2);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
@@ -636,13 +643,13 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) refine_accumulate_kernel(con
 // solve. initial: sets the threshold, zeroes x64.
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) refine_residual_kernel(
-    const BLevel<T> *__restrict__ levels, const BItem *__restrict__ items, int n,
+    const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
     const BScene<T> *__restrict__ scenes, double *part, int initial, double residual, int max_iter,
     double inner_rel, int inner_max, BatchCounters *cnt, const int *__restrict__ scene_of) {
     __shared__ double shf[BLOCK_THREADS / 32];
     __shared__ ItemCtx<T> ctx;
     reduce_items<T, MaxAcc>(
-        items, n, part, levels, scenes, initial ? -1 : 2, ctx,
+        segs, nseg, n, part, levels, scenes, initial ? -1 : 2, ctx,
         [&](const BItem &it, MaxAcc &acc) {
             const BLevel<T> &L = ctx.L;
             const BScene<T> &S = ctx.S;
@@ -719,33 +726,33 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) refine_residual_kernel(
 }  // namespace
 
 template <class T>
-cudaError_t b_presmooth(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+cudaError_t b_presmooth(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                         const BScene<T> *scenes) {
-    presmooth_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate);
+    presmooth_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate);
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_sweep(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
+cudaError_t b_sweep(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
                     int color) {
-    sweep_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate, color);
+    sweep_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, color);
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_restrict(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+cudaError_t b_restrict(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                        const BScene<T> *scenes) {
-    restrict_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate);
+    restrict_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate);
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_post_black(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+cudaError_t b_post_black(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                          const BScene<T> *scenes, T alpha) {
-    post_black_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate, alpha);
+    post_black_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, alpha);
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_red_dot(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
+cudaError_t b_red_dot(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
                       double *part) {
-    red_dot_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate, part, L.scene_of);
+    red_dot_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, part, L.scene_of);
     return cudaGetLastError();
 }
 template <class T>
@@ -758,57 +765,57 @@ template <class T> cudaError_t b_tail_enable(size_t bytes) {
     return cudaFuncSetAttribute(tail_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 template <class T>
-cudaError_t b_direction(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+cudaError_t b_direction(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                         const BScene<T> *scenes) {
-    direction_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate);
+    direction_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate);
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_spmv(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
+cudaError_t b_spmv(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
                    double *part) {
-    spmv_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate, part, L.scene_of);
+    spmv_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, part, L.scene_of);
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_update(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
+cudaError_t b_update(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
                      double *part, int mode, BatchCounters *cnt) {
-    update_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes, L.gate, part, mode, cnt,
+    update_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, part, mode, cnt,
                                                                L.scene_of);
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_refine_accumulate(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+cudaError_t b_refine_accumulate(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                                 const BScene<T> *scenes) {
-    refine_accumulate_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, items, n, scenes);
+    refine_accumulate_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes);
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_refine_residual(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+cudaError_t b_refine_residual(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                               const BScene<T> *scenes, double *part, int initial, double residual, int max_iter,
                               double inner_rel, int inner_max, BatchCounters *cnt) {
     refine_residual_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(
-        levels, items, n, scenes, part, initial, residual, max_iter, inner_rel, inner_max, cnt, L.scene_of);
+        levels, segs, nseg, n, scenes, part, initial, residual, max_iter, inner_rel, inner_max, cnt, L.scene_of);
     return cudaGetLastError();
 }
 
 #define GBP_BATCH_INSTANTIATE(T)                                                                                   \
-    template cudaError_t b_presmooth<T>(const BLaunch &, const BLevel<T> *, const BItem *, int, const BScene<T> *); \
-    template cudaError_t b_sweep<T>(const BLaunch &, const BLevel<T> *, const BItem *, int, const BScene<T> *, int); \
-    template cudaError_t b_restrict<T>(const BLaunch &, const BLevel<T> *, const BItem *, int, const BScene<T> *);  \
-    template cudaError_t b_post_black<T>(const BLaunch &, const BLevel<T> *, const BItem *, int, const BScene<T> *, \
+    template cudaError_t b_presmooth<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *); \
+    template cudaError_t b_sweep<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *, int); \
+    template cudaError_t b_restrict<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *);  \
+    template cudaError_t b_post_black<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *, \
                                          T);                                                                       \
-    template cudaError_t b_red_dot<T>(const BLaunch &, const BLevel<T> *, const BItem *, int, const BScene<T> *,    \
+    template cudaError_t b_red_dot<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *,    \
                                       double *);                                                                   \
     template cudaError_t b_tail<T>(const BLaunch &, const BTail<T> *, int, const BScene<T> *, MgSettings, size_t);  \
     template cudaError_t b_tail_enable<T>(size_t);                                                                 \
-    template cudaError_t b_direction<T>(const BLaunch &, const BLevel<T> *, const BItem *, int, const BScene<T> *); \
-    template cudaError_t b_spmv<T>(const BLaunch &, const BLevel<T> *, const BItem *, int, const BScene<T> *,       \
+    template cudaError_t b_direction<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *); \
+    template cudaError_t b_spmv<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *,       \
                                    double *);                                                                      \
-    template cudaError_t b_update<T>(const BLaunch &, const BLevel<T> *, const BItem *, int, const BScene<T> *,     \
+    template cudaError_t b_update<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *,     \
                                      double *, int, BatchCounters *);                                              \
-    template cudaError_t b_refine_accumulate<T>(const BLaunch &, const BLevel<T> *, const BItem *, int,           \
+    template cudaError_t b_refine_accumulate<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,           \
                                                 const BScene<T> *);                                                \
-    template cudaError_t b_refine_residual<T>(const BLaunch &, const BLevel<T> *, const BItem *, int,             \
+    template cudaError_t b_refine_residual<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,             \
                                               const BScene<T> *, double *, int, double, int, double, int,          \
                                               BatchCounters *);
 

@@ -42,6 +42,8 @@ void BatchRunner::release() {
     d_restrict_.clear();
     n_pair_.clear();
     n_restrict_.clear();
+    s_pair_.clear();
+    s_restrict_.clear();
     d_fine_cells_ = d_fine_pairs_ = nullptr;
     d_part_ = nullptr;
     d_counters_ = nullptr;
@@ -74,24 +76,30 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
         d_scene_of_ = static_cast<int *>(d);
     }
     if ((rc = upload(plan.tails.data(), plan.tails.size() * sizeof(BTail<T>), &d_tails_))) return rc;
-    size_t max_items = std::max(plan.fine_cells.size(), plan.fine_pairs.size());
-    for (int l = 0; l < plan.max_global; ++l) {
+    size_t max_items = (size_t)std::max(plan.n_fine_cells, plan.n_fine_pairs);
+    auto segs = [&](const std::vector<BSeg> &list, BSeg **dst, int *nseg) -> int {
         void *d;
-        if ((rc = upload(plan.pair[l].data(), plan.pair[l].size() * sizeof(BItem), &d))) return rc;
-        d_pair_.push_back(static_cast<BItem *>(d));
-        n_pair_.push_back((int)plan.pair[l].size());
-        if ((rc = upload(plan.restrict_[l].data(), plan.restrict_[l].size() * sizeof(BItem), &d))) return rc;
-        d_restrict_.push_back(static_cast<BItem *>(d));
-        n_restrict_.push_back((int)plan.restrict_[l].size());
-        max_items = std::max(max_items, plan.pair[l].size());
+        int rc2 = upload(list.data(), list.size() * sizeof(BSeg), &d);
+        *dst = static_cast<BSeg *>(d);
+        *nseg = (int)list.size();
+        return rc2;
+    };
+    d_pair_.assign(plan.max_global, nullptr);
+    d_restrict_.assign(plan.max_global, nullptr);
+    s_pair_.assign(plan.max_global, 0);
+    s_restrict_.assign(plan.max_global, 0);
+    n_pair_.assign(plan.n_pair.begin(), plan.n_pair.begin() + plan.max_global);
+    n_restrict_.assign(plan.n_restrict.begin(), plan.n_restrict.begin() + plan.max_global);
+    for (int l = 0; l < plan.max_global; ++l) {
+        if ((rc = segs(plan.pair[l], &d_pair_[l], &s_pair_[l]))) return rc;
+        if ((rc = segs(plan.restrict_[l], &d_restrict_[l], &s_restrict_[l]))) return rc;
+        max_items = std::max(max_items, (size_t)plan.n_pair[l]);
     }
+    if ((rc = segs(plan.fine_cells, &d_fine_cells_, &s_fine_cells_))) return rc;
+    n_fine_cells_ = plan.n_fine_cells;
+    if ((rc = segs(plan.fine_pairs, &d_fine_pairs_, &s_fine_pairs_))) return rc;
+    n_fine_pairs_ = plan.n_fine_pairs;
     void *d;
-    if ((rc = upload(plan.fine_cells.data(), plan.fine_cells.size() * sizeof(BItem), &d))) return rc;
-    d_fine_cells_ = static_cast<BItem *>(d);
-    n_fine_cells_ = (int)plan.fine_cells.size();
-    if ((rc = upload(plan.fine_pairs.data(), plan.fine_pairs.size() * sizeof(BItem), &d))) return rc;
-    d_fine_pairs_ = static_cast<BItem *>(d);
-    n_fine_pairs_ = (int)plan.fine_pairs.size();
     max_items_ = (int)max_items;
     if ((rc = upload(nullptr, sizeof(double) * (max_items + 1), &d))) return rc;
     d_part_ = static_cast<double *>(d);
@@ -122,14 +130,14 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
     auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, gate, d_scene_of_}; };
     // descend
     for (int l = 0; l < max_global_ && e == cudaSuccess; ++l) {
-        e = b_presmooth<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc);
+        e = b_presmooth<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc);
         ++*nodes;
         for (int s = 1; s < ms.smooth && e == cudaSuccess; ++s) {
-            e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc, 0);
-            if (e == cudaSuccess) e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc, 1);
+            e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, 0);
+            if (e == cudaSuccess) e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, 1);
             *nodes += 2;
         }
-        if (e == cudaSuccess) e = b_restrict<T>(L(n_restrict_[l]), lv, d_restrict_[l], n_restrict_[l], sc);
+        if (e == cudaSuccess) e = b_restrict<T>(L(n_restrict_[l]), lv, d_restrict_[l], s_restrict_[l], n_restrict_[l], sc);
         ++*nodes;
     }
     if (e == cudaSuccess && tail_smem_ > 0) {
@@ -138,29 +146,29 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
     }
     // ascend
     for (int l = max_global_ - 1; l >= 0 && e == cudaSuccess; --l) {
-        e = b_post_black<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc, T(ms.alpha));
+        e = b_post_black<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, T(ms.alpha));
         ++*nodes;
         for (int s = 1; s < ms.smooth && e == cudaSuccess; ++s) {
-            e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc, 0);
-            if (e == cudaSuccess) e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc, 1);
+            e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, 0);
+            if (e == cudaSuccess) e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, 1);
             *nodes += 2;
         }
         if (e != cudaSuccess) break;
-        if (l > 0) e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], n_pair_[l], sc, 0);
-        else e = b_red_dot<T>(L(n_fine_pairs_), lv, d_fine_pairs_, n_fine_pairs_, sc, d_part_);
+        if (l > 0) e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, 0);
+        else e = b_red_dot<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_);
         ++*nodes;
     }
     // CG on the fine level
-    if (e == cudaSuccess) e = b_direction<T>(L(n_fine_cells_), lv, d_fine_cells_, n_fine_cells_, sc);
-    if (e == cudaSuccess) e = b_spmv<T>(L(n_fine_cells_), lv, d_fine_cells_, n_fine_cells_, sc, d_part_);
+    if (e == cudaSuccess) e = b_direction<T>(L(n_fine_cells_), lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc);
+    if (e == cudaSuccess) e = b_spmv<T>(L(n_fine_cells_), lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc, d_part_);
     if (e == cudaSuccess)
-        e = b_update<T>(L(n_fine_cells_), lv, d_fine_cells_, n_fine_cells_, sc, d_part_, mixed_ ? 1 : 0, d_counters_);
+        e = b_update<T>(L(n_fine_cells_), lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc, d_part_, mixed_ ? 1 : 0, d_counters_);
     *nodes += 3;
     if (mixed_ && e == cudaSuccess) {
         const BLaunch L2{blocks_for(n_fine_cells_, grid_blocks_), st, 2, d_scene_of_};
-        e = b_refine_accumulate<T>(L2, lv, d_fine_cells_, n_fine_cells_, sc);
+        e = b_refine_accumulate<T>(L2, lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc);
         if (e == cudaSuccess)
-            e = b_refine_residual<T>(L2, lv, d_fine_cells_, n_fine_cells_, sc, d_part_, 0, p.residual,
+            e = b_refine_residual<T>(L2, lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc, d_part_, 0, p.residual,
                                      p.max_iterations, inner_rel_, kInnerMax, d_counters_);
         *nodes += 2;
     }
@@ -175,8 +183,7 @@ template <class T> int BatchRunner::solve(const gbp_params &p, cudaStream_t st, 
     RUN_CUDA(cudaMemcpyAsync(d_counters_, h_counters_, sizeof(BatchCounters), cudaMemcpyHostToDevice, st));
     // initial residual of every scene (also zeroes x64, sets thresholds)
     RUN_CUDA(b_refine_residual<T>(BLaunch{blocks_for(n_fine_cells_, grid_blocks_), st, 0, d_scene_of_}, lv,
-                                  d_fine_cells_,
-                                  n_fine_cells_, sc, d_part_, 1, p.residual, p.max_iterations, inner_rel_, kInnerMax,
+                                  d_fine_cells_, s_fine_cells_, n_fine_cells_, sc, d_part_, 1, p.residual, p.max_iterations, inner_rel_, kInnerMax,
                                   d_counters_));
     *launches += 1;
     const long long key = ((long long)(p.mg_smooth > 0 ? p.mg_smooth : 1) << 40) ^
@@ -219,17 +226,17 @@ template <class T> int BatchRunner::bench(int which, int reps, cudaStream_t st, 
     std::function<cudaError_t()> launch;
     auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, 0, d_scene_of_}; };
     switch (which) {
-    case 0: launch = [&]() { return b_presmooth<T>(L(n_pair_[0]), lv, d_pair_[0], n_pair_[0], sc); }; break;
-    case 1: launch = [&]() { return b_restrict<T>(L(n_restrict_[0]), lv, d_restrict_[0], n_restrict_[0], sc); }; break;
+    case 0: launch = [&]() { return b_presmooth<T>(L(n_pair_[0]), lv, d_pair_[0], s_pair_[0], n_pair_[0], sc); }; break;
+    case 1: launch = [&]() { return b_restrict<T>(L(n_restrict_[0]), lv, d_restrict_[0], s_restrict_[0], n_restrict_[0], sc); }; break;
     case 2:
-        launch = [&]() { return b_post_black<T>(L(n_pair_[0]), lv, d_pair_[0], n_pair_[0], sc, T(mset.alpha)); };
+        launch = [&]() { return b_post_black<T>(L(n_pair_[0]), lv, d_pair_[0], s_pair_[0], n_pair_[0], sc, T(mset.alpha)); };
         break;
-    case 3: launch = [&]() { return b_red_dot<T>(L(n_fine_pairs_), lv, d_fine_pairs_, n_fine_pairs_, sc, d_part_); }; break;
-    case 4: launch = [&]() { return b_direction<T>(L(n_fine_cells_), lv, d_fine_cells_, n_fine_cells_, sc); }; break;
-    case 5: launch = [&]() { return b_spmv<T>(L(n_fine_cells_), lv, d_fine_cells_, n_fine_cells_, sc, d_part_); }; break;
+    case 3: launch = [&]() { return b_red_dot<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_); }; break;
+    case 4: launch = [&]() { return b_direction<T>(L(n_fine_cells_), lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc); }; break;
+    case 5: launch = [&]() { return b_spmv<T>(L(n_fine_cells_), lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc, d_part_); }; break;
     case 6:
         launch = [&]() {
-            return b_update<T>(L(n_fine_cells_), lv, d_fine_cells_, n_fine_cells_, sc, d_part_, 0, d_counters_);
+            return b_update<T>(L(n_fine_cells_), lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc, d_part_, 0, d_counters_);
         };
         break;
     default: return fail(GBP_ERR_INVALID_ARGUMENT, "bench: unknown kernel");

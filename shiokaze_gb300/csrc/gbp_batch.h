@@ -61,6 +61,28 @@ struct BItem {
 // block, so small items cost little).
 constexpr int BITEM_CELLS = 512;
 
+// A work list is the concatenation of one segment per scene: items
+// [begin, begin+count) of the list are tiles [k*m, k*m+m) of level `ref`.
+// Kernels derive each item from its index, with no per-item load.
+struct BSeg {
+    int ref;
+    int begin;
+    int count;
+    int m;       // tiles per item
+    int ntiles;  // tiles of the level in this tiling
+};
+
+// Item w of a segment list; `seg` is the caller's cursor (items are visited
+// in increasing order, so it only moves forward).
+__host__ __device__ inline BItem item_at(const BSeg *segs, int nseg, int w, int &seg) {
+    while (seg + 1 < nseg && w >= segs[seg + 1].begin) ++seg;
+    const BSeg &s = segs[seg];
+    const int k = w - s.begin;
+    const int t = k * s.m;
+    const int nt = s.ntiles - t < s.m ? s.ntiles - t : s.m;
+    return BItem{s.ref, t, nt, s.begin, s.count};
+}
+
 template <class T> struct BTail {
     int nt;
     MgLevel<T> lv[MG_MAX_LEVELS];
@@ -85,9 +107,12 @@ template <class T> struct BatchPlan {
     std::vector<BScene<T>> scenes;
     std::vector<BTail<T>> tails;
     size_t tail_smem = 0;
-    // item lists: pair[l], restrict[l] (coarse tiles of l+1), fine (cell tiles of level 0)
-    std::vector<std::vector<BItem>> pair, restrict_;
-    std::vector<BItem> fine_cells, fine_pairs;
+    // work lists as segments: pair[l], restrict[l] (coarse tiles of l+1),
+    // fine (tiles of level 0), with their item counts
+    std::vector<std::vector<BSeg>> pair, restrict_;
+    std::vector<BSeg> fine_cells, fine_pairs;
+    std::vector<int> n_pair, n_restrict;
+    int n_fine_cells = 0, n_fine_pairs = 0;
 };
 
 class BatchRunner {
@@ -128,10 +153,10 @@ private:
     // device copies
     void *d_levels_ = nullptr, *d_scenes_ = nullptr, *d_tails_ = nullptr;
     int *d_scene_of_ = nullptr;
-    std::vector<BItem *> d_pair_, d_restrict_;
-    std::vector<int> n_pair_, n_restrict_;
-    BItem *d_fine_cells_ = nullptr, *d_fine_pairs_ = nullptr;
-    int n_fine_cells_ = 0, n_fine_pairs_ = 0;
+    std::vector<BSeg *> d_pair_, d_restrict_;
+    std::vector<int> n_pair_, n_restrict_, s_pair_, s_restrict_;  // items, segments
+    BSeg *d_fine_cells_ = nullptr, *d_fine_pairs_ = nullptr;
+    int n_fine_cells_ = 0, n_fine_pairs_ = 0, s_fine_cells_ = 0, s_fine_pairs_ = 0;
     double *d_part_ = nullptr;  // 3 x max items
     int max_items_ = 0;
     BatchCounters *d_counters_ = nullptr, *h_counters_ = nullptr;
@@ -151,37 +176,37 @@ struct BLaunch {
 };
 
 template <class T>
-cudaError_t b_presmooth(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes);
+cudaError_t b_presmooth(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes);
 template <class T>
-cudaError_t b_sweep(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
+cudaError_t b_sweep(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
                     int color);
 template <class T>
-cudaError_t b_restrict(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+cudaError_t b_restrict(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                        const BScene<T> *scenes);
 template <class T>
-cudaError_t b_post_black(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+cudaError_t b_post_black(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                          const BScene<T> *scenes, T alpha);
 template <class T>
-cudaError_t b_red_dot(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
+cudaError_t b_red_dot(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
                       double *part);
 template <class T>
 cudaError_t b_tail(const BLaunch &L, const BTail<T> *tails, int nscenes, const BScene<T> *scenes, MgSettings ms,
                    size_t smem);
 template <class T> cudaError_t b_tail_enable(size_t bytes);
 template <class T>
-cudaError_t b_direction(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+cudaError_t b_direction(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                         const BScene<T> *scenes);
 template <class T>
-cudaError_t b_spmv(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
+cudaError_t b_spmv(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
                    double *part);
 template <class T>
-cudaError_t b_update(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n, const BScene<T> *scenes,
+cudaError_t b_update(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
                      double *part, int mode, BatchCounters *cnt);
 template <class T>
-cudaError_t b_refine_accumulate(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+cudaError_t b_refine_accumulate(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                                 const BScene<T> *scenes);
 template <class T>
-cudaError_t b_refine_residual(const BLaunch &L, const BLevel<T> *levels, const BItem *items, int n,
+cudaError_t b_refine_residual(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                               const BScene<T> *scenes, double *part, int initial, double residual, int max_iter,
                               double inner_rel, int inner_max, BatchCounters *cnt);
 

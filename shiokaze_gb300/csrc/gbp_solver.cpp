@@ -309,6 +309,8 @@ template <class T> void Solver::add_to_plan(BatchPlan<T> &plan, const gbp_params
     if ((int)plan.pair.size() < G) {
         plan.pair.resize(G);
         plan.restrict_.resize(G);
+        plan.n_pair.resize(G, 0);
+        plan.n_restrict.resize(G, 0);
     }
     plan.max_global = std::max(plan.max_global, G);
     const int base = (int)plan.levels.size();
@@ -316,19 +318,18 @@ template <class T> void Solver::add_to_plan(BatchPlan<T> &plan, const gbp_params
         const MgLevel<T> &F = H.levels[l], &C = H.levels[l + 1];
         plan.levels.push_back(BLevel<T>{F.g, F.diag, F.inv, F.cx, F.cy, F.cz, F.b, F.x, C.x, C.b, C.g, s});
         plan.scene_of.push_back(s);
-        auto add = [&](std::vector<BItem> &list, long long tiles, long long cells_per_tile) {
-            const int begin = (int)list.size();
-            const long long m = std::max(1LL, BITEM_CELLS / cells_per_tile);
+        auto add = [&](std::vector<BSeg> &list, int &items, long long tiles, long long cells_per_tile) {
+            const int m = (int)std::max(1LL, BITEM_CELLS / cells_per_tile);
             const int count = (int)((tiles + m - 1) / m);
-            for (long long t = 0; t < tiles; t += m)
-                list.push_back(BItem{base + l, (int)t, (int)std::min(m, tiles - t), begin, count});
+            list.push_back(BSeg{base + l, items, count, m, (int)tiles});
+            items += count;
         };
-        add(plan.pair[l], pair_tiles(F.g), 64LL * TILE_Y * F.g.tz);
+        add(plan.pair[l], plan.n_pair[l], pair_tiles(F.g), 64LL * TILE_Y * F.g.tz);
         // a restriction item's work is its 8x as many fine cells
-        add(plan.restrict_[l], cell_tiles(C.g), 8LL * TILE_X * TILE_Y * C.g.tz);
+        add(plan.restrict_[l], plan.n_restrict[l], cell_tiles(C.g), 8LL * TILE_X * TILE_Y * C.g.tz);
         if (l == 0) {
-            add(plan.fine_cells, cell_tiles(F.g), (long long)TILE_X * TILE_Y * F.g.tz);
-            add(plan.fine_pairs, pair_tiles(F.g), 64LL * TILE_Y * F.g.tz);
+            add(plan.fine_cells, plan.n_fine_cells, cell_tiles(F.g), (long long)TILE_X * TILE_Y * F.g.tz);
+            add(plan.fine_pairs, plan.n_fine_pairs, pair_tiles(F.g), 64LL * TILE_Y * F.g.tz);
         }
     }
     BTail<T> tail{};
