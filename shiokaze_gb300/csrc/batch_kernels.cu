@@ -1,17 +1,25 @@
 // batch_kernels.cu -- the MGPCG iteration over a work list of (level, tile)
 // items spanning every scene of a batch (see gbp_batch.h).
 //
-// The arithmetic is that of the single-level kernels it generalises: red
-// (i+j+k even) / black Gauss-Seidel on pair tiles (each thread owns the two
-// x-adjacent cells of a row, one of each colour), Galerkin restriction by
-// summing the 8 children's residuals, post-smoothing black (reading the red
-// neighbours with their parent's correction added) then red, a shared-memory
-// tail per scene for the small levels, and CG with FP64 dot products.
+// Red (i+j+k even) / black Gauss-Seidel, Galerkin restriction by summing the
+// 8 children's residuals, post-smoothing black (reading the red neighbours
+// with their parent's correction added) then red, a shared-memory tail per
+// scene for the small levels, and CG with FP64-accumulated dot products.
+//
+// Every kernel walks pair tiles (64 x 8 x tz cells): a thread owns the two
+// x-adjacent cells (i, i+1) of a row, i even, one of each colour. On levels
+// with an even row length and suitably aligned arrays (the host checks both
+// and sets BLevel::vec) the pair and its y/z neighbour pairs move as one
+// 8-byte (FP32) or 16-byte (FP64) access; elsewhere as two scalar accesses.
+// The arithmetic, including the order of every sum, is the same either way.
+//
 // Algorithmic DRAM bytes per fine cell (s = sizeof(T)): presmooth 6 s,
 // sweep 7 s, restrict 6 s + s/8, post_black 7 s + s/8, red_dot 7 s,
 // direction 3 s, spmv 6 s, update 6 s, refine_accumulate 12 B (d f32 read,
 // x64 read+write), refine_residual 8+32+8+8+4 = 60 B (x64, operator, b, r64
 // write, r_f write).
+#include <type_traits>
+
 #include "gbp_batch.h"
 
 namespace gbp {
@@ -25,6 +33,12 @@ __device__ __forceinline__ bool gated(const Scalars *sc, int gate) {
     if (gate == 1) return v->inner_done != 0;
     if (gate == 2) return v->inner_done == 0;
     return false;
+}
+
+// Every scene of the batch is done (the rest of a graph chunk after the
+// last scene stopped): a launch returns at once.
+__device__ __forceinline__ bool batch_idle(const BatchCounters *cnt) {
+    return cnt != nullptr && *(const volatile int *)&cnt->remaining <= 0;
 }
 
 // Ticket of one item of a scene; true in every thread of the block whose
@@ -51,54 +65,127 @@ __device__ __forceinline__ double max_range(const double *part, int begin, int c
     return block_max(v, sh);
 }
 
-// cells (i, i+1) of the pair tile t: f(i, j, k, c, second)
-template <class F> __device__ __forceinline__ void pair_tile1(const Grid &g, long long t, F f) {
+// ---- pairs -----------------------------------------------------------------------
+
+// Values of the cells (i, i+1) of a pair.
+template <class T> struct Pair {
+    T a, b;
+};
+template <class T> struct Vec2;
+template <> struct Vec2<float> {
+    using type = float2;
+};
+template <> struct Vec2<double> {
+    using type = double2;
+};
+
+// Read-only pair load: one 2-wide load when V (c even, array aligned), else
+// the cells one by one (the second only if it exists).
+template <class T, bool V> __device__ __forceinline__ Pair<T> ld2(const T *p, long long c, bool second) {
+    if constexpr (V) {
+        const typename Vec2<T>::type v = __ldg(reinterpret_cast<const typename Vec2<T>::type *>(p + c));
+        return Pair<T>{v.x, v.y};
+    } else {
+        return Pair<T>{__ldg(p + c), second ? __ldg(p + c + 1) : T(0)};
+    }
+}
+template <class T, bool V> __device__ __forceinline__ void st2(T *p, long long c, Pair<T> v, bool second) {
+    if constexpr (V) {
+        typename Vec2<T>::type w;
+        w.x = v.a;
+        w.y = v.b;
+        *reinterpret_cast<typename Vec2<T>::type *>(p + c) = w;
+    } else {
+        p[c] = v.a;
+        if (second) p[c + 1] = v.b;
+    }
+}
+
+// The pair tile t of grid g: f(i, j, k, c, second) for each of the thread's
+// tz pairs, c = index of cell i, second = (i+1 < nx).
+template <class F> __device__ __forceinline__ void pair_tile1(const Grid &g, unsigned t, F f) {
     const int px = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int ntx2 = (g.nx + 63) >> 6;
-    const long long tx = t % ntx2, r = t / ntx2;
-    const int i = (int)tx * 64 + 2 * px;
-    const int j = (int)(r % g.nty) * TILE_Y + ty;
-    const int k0 = (int)(r / g.nty) * g.tz;
+    const unsigned r = fdiv(t, g.ftx2);
+    const unsigned tk = fdiv(r, g.fty);
+    const int i = (int)(t - r * g.ftx2.d) * 64 + 2 * px;
+    const int j = (int)(r - tk * (unsigned)g.nty) * TILE_Y + ty;
+    const int k0 = (int)tk * g.tz;
     if (i >= g.nx || j >= g.ny) return;
     const int kend = min(k0 + g.tz, g.nz);
     const bool second = i + 1 < g.nx;
-    for (int k = k0; k < kend; ++k) f(i, j, k, cell_index(g, i, j, k), second);
+    const long long sz = (long long)g.nx * g.ny;
+    long long c = cell_index(g, i, j, k0);
+    for (int k = k0; k < kend; ++k, c += sz) f(i, j, k, c, second);
 }
 
-// cells of the cell tile t: f(i, j, k, c)
-template <class F> __device__ __forceinline__ void cell_tile1(const Grid &g, long long t, F f) {
+// cells of the cell tile t (32 x 8 x tz, one cell per thread and plane)
+template <class F> __device__ __forceinline__ void cell_tile1(const Grid &g, unsigned t, F f) {
     int i0, j0, k0;
     tile_origin(g, t, i0, j0, k0);
     const int i = i0 + (threadIdx.x & (TILE_X - 1)), j = j0 + threadIdx.x / TILE_X;
     if (i >= g.nx || j >= g.ny) return;
     const int kend = min(k0 + g.tz, g.nz);
-    for (int k = k0; k < kend; ++k) f(i, j, k, cell_index(g, i, j, k));
+    const long long sz = (long long)g.nx * g.ny;
+    long long c = cell_index(g, i, j, k0);
+    for (int k = k0; k < kend; ++k, c += sz) f(i, j, k, c);
 }
 
-// every tile of an item
 template <class F> __device__ __forceinline__ void pair_tile(const Grid &g, const BItem &it, F f) {
-    for (int t = 0; t < it.ntiles; ++t) pair_tile1(g, (long long)it.tile + t, f);
+    for (int t = 0; t < it.ntiles; ++t) pair_tile1(g, (unsigned)(it.tile + t), f);
 }
 template <class F> __device__ __forceinline__ void cell_tile(const Grid &g, const BItem &it, F f) {
-    for (int t = 0; t < it.ntiles; ++t) cell_tile1(g, (long long)it.tile + t, f);
+    for (int t = 0; t < it.ntiles; ++t) cell_tile1(g, (unsigned)(it.tile + t), f);
 }
 
-template <class T, class X>
-__device__ __forceinline__ T nsum(const BLevel<T> &L, int i, int j, int k, long long c, X xat) {
-    const Grid &g = L.g;
+// Runs body(std::true_type) on vector levels, body(std::false_type) elsewhere.
+template <class B> __device__ __forceinline__ void with_vec(int vec, B body) {
+    if (vec) body(std::true_type{});
+    else body(std::false_type{});
+}
+
+// Neighbour sums of the pair (i, i+1) at c = index of cell i:
+//   s.a = sum over the neighbours f of cell i of c_f v_f, s.b for cell i+1,
+// in the order -x, +x, -y, +y, -z, +z. W selects the sums wanted: 0 (s.a),
+// 1 (s.b) or 2 (both); the other's arithmetic and single-cell loads are
+// dead code. `own` holds the pair's own values (each cell is the other's x
+// neighbour); nb2(c', j', k', second) gives the neighbour pair at c' (row
+// j', plane k'; its second cell exists exactly when the pair's does),
+// nb1(c', i') one cell of the same row outside the pair.
+template <class T, bool V, int W, class NB2, class NB1>
+__device__ __forceinline__ Pair<T> pair_nsum(const Grid &g, const T *cx, const T *cy, const T *cz, int i, int j, int k,
+                                              long long c, bool second, Pair<T> own, NB2 nb2, NB1 nb1) {
+    constexpr bool A = W != 1, B = W != 0;
     const long long sy = g.nx, sz = (long long)g.nx * g.ny;
-    T s = T(0);
-    if (i > 0) s += __ldg(L.cx + c - 1) * xat(c - 1, i - 1, j, k);
-    if (i + 1 < g.nx) s += __ldg(L.cx + c) * xat(c + 1, i + 1, j, k);
-    if (j > 0) s += __ldg(L.cy + c - sy) * xat(c - sy, i, j - 1, k);
-    if (j + 1 < g.ny) s += __ldg(L.cy + c) * xat(c + sy, i, j + 1, k);
+    Pair<T> s{T(0), T(0)};
+    const Pair<T> cxp = ld2<T, V>(cx, c, second);  // faces (i|i+1), (i+1|i+2)
+    if (A && i > 0) s.a += __ldg(cx + c - 1) * nb1(c - 1, i - 1);
+    if (second) {
+        if (A) s.a += cxp.a * own.b;
+        if (B) s.b += cxp.a * own.a;
+        if (B && i + 2 < g.nx) s.b += cxp.b * nb1(c + 2, i + 2);
+    }
+    auto add = [&](const Pair<T> &w, const Pair<T> &v) {
+        if (A) s.a += w.a * v.a;
+        if (B) s.b += w.b * v.b;
+    };
+    if (j > 0) add(ld2<T, V>(cy, c - sy, second), nb2(c - sy, j - 1, k, second));
+    if (j + 1 < g.ny) add(ld2<T, V>(cy, c, second), nb2(c + sy, j + 1, k, second));
     if (g.dim == 3) {
-        if (k > 0) s += __ldg(L.cz + c - sz) * xat(c - sz, i, j, k - 1);
-        if (k + 1 < g.nz) s += __ldg(L.cz + c) * xat(c + sz, i, j, k + 1);
+        if (k > 0) add(ld2<T, V>(cz, c - sz, second), nb2(c - sz, j, k - 1, second));
+        if (k + 1 < g.nz) add(ld2<T, V>(cz, c, second), nb2(c + sz, j, k + 1, second));
     }
     return s;
 }
 
+// The neighbour sum of one cell h (0: i, 1: i+1) of the pair. h is uniform
+// across a warp (a warp holds one row of pairs, i even, so the colour of
+// cell i is that of j + k), so the branch does not diverge.
+template <class T, bool V, class NB2, class NB1>
+__device__ __forceinline__ T pair_nsum1(int h, const Grid &g, const T *cx, const T *cy, const T *cz, int i, int j,
+                                        int k, long long c, bool second, Pair<T> own, NB2 nb2, NB1 nb1) {
+    if (h == 0) return pair_nsum<T, V, 0>(g, cx, cy, cz, i, j, k, c, second, own, nb2, nb1).a;
+    return pair_nsum<T, V, 1>(g, cx, cy, cz, i, j, k, c, second, own, nb2, nb1).b;
+}
 
 // The level and scene of the current item, held in shared memory and
 // reloaded only when the item's level changes (each work list holds one
@@ -168,23 +255,54 @@ __device__ __forceinline__ void reduce_items(const BSeg *__restrict__ segs, int 
     if (cur >= 0 && !ctx.skip) flush();
 }
 
-struct SumAcc {
+// Per-thread partials of the reductions. FP64 path: FP64 FMA per term.
+// FP32 path: each product is split exactly by an FMA (a*b = p + e) and the
+// terms are summed in float-float (TwoSum, renormalised after every term,
+// about 46 significant bits); a partial is converted to FP64 once, when its
+// block flushes, and partials add across threads and blocks in FP64. The
+// FP32 path then issues no FP64 instruction per cell (the FP64 pipe of this
+// GPU runs at a small fraction of its FP32 rate). It assumes |a b| stays
+// inside the FP32 range, as the FP32 inner solve does for its vectors.
+template <class T> struct DotAcc;
+template <> struct DotAcc<double> {
     double v;
     __device__ void reset() { v = 0.0; }
+    __device__ void add(double a, double b) { v = fma(a, b, v); }
     __device__ double block(double *sh) { return block_sum(v, sh); }
 };
-struct MaxAcc {
-    double v;
-    __device__ void reset() { v = 0.0; }
-    __device__ double block(double *sh) { return block_max(v, sh); }
+template <> struct DotAcc<float> {
+    float hi, lo;
+    __device__ void reset() { hi = lo = 0.0f; }
+    __device__ void add(float a, float b) {
+        const float p = __fmul_rn(a, b);
+        const float e = __fmaf_rn(a, b, -p);
+        const float s = __fadd_rn(hi, p);
+        const float bb = __fsub_rn(s, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+        const float t = __fadd_rn(lo, __fadd_rn(err, e));
+        hi = __fadd_rn(s, t);
+        lo = __fsub_rn(t, __fsub_rn(hi, s));
+    }
+    __device__ double block(double *sh) { return block_sum((double)hi + (double)lo, sh); }
+};
+// max |x|: exact in either type; FP32 converts once per flush. NaN terms
+// are ignored here (fmax), as before; NaN is caught through alpha.
+template <class T> struct MaxAcc {
+    T v;
+    __device__ void reset() { v = T(0); }
+    __device__ void add(T x) { v = fmax(v, fabs(x)); }
+    __device__ double block(double *sh) { return block_max((double)v, sh); }
 };
 
 // ---- smoothing and transfers on the global-memory levels --------------------------
 
+// First pre-smoothing pass from x = 0: red x = b / diag, then black from the
+// red neighbours (computed on the fly as b inv), both written.
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) presmooth_kernel(const BLevel<T> *__restrict__ levels,
-                                                                     const BSeg *__restrict__ segs, int nseg, int n,
-                                                                     const BScene<T> *__restrict__ scenes, int gate) {
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    presmooth_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                     const BScene<T> *__restrict__ scenes, int gate, const BatchCounters *live) {
+    if (batch_idle(live)) return;
     __shared__ ItemCtx<T> ctx;
     int cur = -1;
     int sgc = 0;
@@ -193,25 +311,39 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) presmooth_kernel(const BLeve
         refresh(ctx, cur, it, levels, scenes, gate);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
-        auto red_value = [&](long long m, int, int, int) { return __ldg(L.b + m) * __ldg(L.inv + m); };
-        pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
-            const bool a_red = ((i + j + k) & 1) == 0;
-            for (int h = 0; h < (second ? 2 : 1); ++h) {
-                const long long cc = c + h;
-                T xv;
-                if ((h == 0) == a_red) xv = __ldg(L.b + cc) * __ldg(L.inv + cc);
-                else xv = (__ldg(L.b + cc) + nsum(L, i + h, j, k, cc, red_value)) * __ldg(L.inv + cc);
-                L.x[cc] = xv;
-            }
+        with_vec(L.vec, [&](auto vt) {
+            constexpr bool V = decltype(vt)::value;
+            auto nb2 = [&](long long m, int, int, bool sec) {
+                const Pair<T> bb = ld2<T, V>(L.b, m, sec), ii = ld2<T, V>(L.inv, m, sec);
+                return Pair<T>{bb.a * ii.a, bb.b * ii.b};
+            };
+            auto nb1 = [&](long long m, int) { return __ldg(L.b + m) * __ldg(L.inv + m); };
+            pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
+                const bool a_red = ((i + j + k) & 1) == 0;
+                const Pair<T> b2 = ld2<T, V>(L.b, c, second), iv = ld2<T, V>(L.inv, c, second);
+                const Pair<T> red{b2.a * iv.a, b2.b * iv.b};
+                Pair<T> out = red;
+                if (a_red) {
+                    if (second)
+                        out.b = (b2.b + pair_nsum1<T, V>(1, L.g, L.cx, L.cy, L.cz, i, j, k, c, second, red, nb2, nb1)) *
+                                iv.b;
+                } else {
+                    out.a = (b2.a + pair_nsum1<T, V>(0, L.g, L.cx, L.cy, L.cz, i, j, k, c, second, red, nb2, nb1)) *
+                            iv.a;
+                }
+                st2<T, V>(L.x, c, out, second);
+            });
         });
     }
 }
 
+// One colour of a Gauss-Seidel sweep (extra smoothing sweeps, and the final
+// red pass of the post-smoothing on coarse levels).
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) sweep_kernel(const BLevel<T> *__restrict__ levels,
-                                                                 const BSeg *__restrict__ segs, int nseg, int n,
-                                                                 const BScene<T> *__restrict__ scenes, int gate,
-                                                                 int color) {
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    sweep_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                 const BScene<T> *__restrict__ scenes, int gate, int color, const BatchCounters *live) {
+    if (batch_idle(live)) return;
     __shared__ ItemCtx<T> ctx;
     int cur = -1;
     int sgc = 0;
@@ -220,21 +352,30 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) sweep_kernel(const BLevel<T>
         refresh(ctx, cur, it, levels, scenes, gate);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
-        auto xval = [&](long long m, int, int, int) { return __ldg(L.x + m); };
-        pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
-            const int h = ((i + j + k) & 1) == color ? 0 : 1;
-            if (h == 1 && !second) return;
-            const long long cc = c + h;
-            L.x[cc] = (__ldg(L.b + cc) + nsum(L, i + h, j, k, cc, xval)) * __ldg(L.inv + cc);
+        with_vec(L.vec, [&](auto vt) {
+            constexpr bool V = decltype(vt)::value;
+            auto nb2 = [&](long long m, int, int, bool sec) { return ld2<T, V>(L.x, m, sec); };
+            auto nb1 = [&](long long m, int) { return __ldg(L.x + m); };
+            pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
+                const int h = ((i + j + k) & 1) == color ? 0 : 1;
+                if (h == 1 && !second) return;
+                const Pair<T> x2 = ld2<T, V>(L.x, c, second);
+                const T sh = pair_nsum1<T, V>(h, L.g, L.cx, L.cy, L.cz, i, j, k, c, second, x2, nb2, nb1);
+                const long long ch = c + h;
+                L.x[ch] = (__ldg(L.b + ch) + sh) * __ldg(L.inv + ch);
+            });
         });
     }
 }
 
-// items are cell tiles of the coarse grid gc
+// Items are cell tiles of the coarse grid gc; a thread sums the residuals
+// b - A x of the (up to) 8 children of its coarse cell, child pairs
+// (2I, 2I+1) in order of (z, y).
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) restrict_kernel(const BLevel<T> *__restrict__ levels,
-                                                                    const BSeg *__restrict__ segs, int nseg, int n,
-                                                                    const BScene<T> *__restrict__ scenes, int gate) {
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    restrict_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                    const BScene<T> *__restrict__ scenes, int gate, const BatchCounters *live) {
+    if (batch_idle(live)) return;
     __shared__ ItemCtx<T> ctx;
     int cur = -1;
     int sgc = 0;
@@ -243,30 +384,41 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) restrict_kernel(const BLevel
         refresh(ctx, cur, it, levels, scenes, gate);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
-        const Grid &fg = L.g;
-        auto xval = [&](long long m, int, int, int) { return __ldg(L.x + m); };
-        cell_tile(L.gc, it, [&](int I, int J, int K, long long cc) {
-            T sum = T(0);
-            const int kmax = fg.dim == 3 ? 2 : 1;
-            for (int c2 = 0; c2 < kmax; ++c2)
-                for (int b2 = 0; b2 < 2; ++b2)
-                    for (int a2 = 0; a2 < 2; ++a2) {
-                        const int i = 2 * I + a2, j = 2 * J + b2, k = 2 * K + c2;
-                        if (i >= fg.nx || j >= fg.ny || k >= fg.nz) continue;
+        with_vec(L.vec, [&](auto vt) {
+            constexpr bool V = decltype(vt)::value;
+            const Grid &fg = L.g;
+            auto nb2 = [&](long long m, int, int, bool sec) { return ld2<T, V>(L.x, m, sec); };
+            auto nb1 = [&](long long m, int) { return __ldg(L.x + m); };
+            cell_tile(L.gc, it, [&](int I, int J, int K, long long cc) {
+                T sum = T(0);
+                const int kmax = fg.dim == 3 ? 2 : 1;
+                const int i = 2 * I;
+                const bool second = i + 1 < fg.nx;
+                for (int c2 = 0; c2 < kmax; ++c2)
+                    for (int b2 = 0; b2 < 2; ++b2) {
+                        const int j = 2 * J + b2, k = 2 * K + c2;
+                        if (j >= fg.ny || k >= fg.nz) continue;
                         const long long f = cell_index(fg, i, j, k);
-                        const T s = nsum(L, i, j, k, f, xval);
-                        sum += __ldg(L.b + f) - (__ldg(L.diag + f) * __ldg(L.x + f) - s);
+                        const Pair<T> x2 = ld2<T, V>(L.x, f, second);
+                        const Pair<T> s = pair_nsum<T, V, 2>(fg, L.cx, L.cy, L.cz, i, j, k, f, second, x2, nb2, nb1);
+                        const Pair<T> bb = ld2<T, V>(L.b, f, second), dd = ld2<T, V>(L.diag, f, second);
+                        sum += bb.a - (dd.a * x2.a - s.a);
+                        if (second) sum += bb.b - (dd.b * x2.b - s.b);
                     }
-            L.bc[cc] = sum;
+                L.bc[cc] = sum;
+            });
         });
     }
 }
 
+// Prolongation fused with the black half of the post-smoothing: black cells
+// from their red neighbours plus alpha times the neighbour's parent value.
+// The two cells of a pair (i even) share their parent.
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) post_black_kernel(const BLevel<T> *__restrict__ levels,
-                                                                      const BSeg *__restrict__ segs, int nseg, int n,
-                                                                      const BScene<T> *__restrict__ scenes, int gate,
-                                                                      T alpha) {
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    post_black_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                      const BScene<T> *__restrict__ scenes, int gate, T alpha, const BatchCounters *live) {
+    if (batch_idle(live)) return;
     __shared__ ItemCtx<T> ctx;
     int cur = -1;
     int sgc = 0;
@@ -275,16 +427,33 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) post_black_kernel(const BLev
         refresh(ctx, cur, it, levels, scenes, gate);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
-        const Grid &cg = L.gc;
-        const bool d3 = L.g.dim == 3;
-        auto corrected = [&](long long m, int ni, int nj, int nk) {
-            return __ldg(L.x + m) + alpha * __ldg(L.xc + cell_index(cg, ni >> 1, nj >> 1, d3 ? (nk >> 1) : 0));
-        };
-        pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
-            const int h = ((i + j + k) & 1) == 1 ? 0 : 1;
-            if (h == 1 && !second) return;
-            const long long cc = c + h;
-            L.x[cc] = (__ldg(L.b + cc) + nsum(L, i + h, j, k, cc, corrected)) * __ldg(L.inv + cc);
+        with_vec(L.vec, [&](auto vt) {
+            constexpr bool V = decltype(vt)::value;
+            const Grid &cg = L.gc;
+            const bool d3 = L.g.dim == 3;
+            const long long csy = cg.nx, csz = (long long)cg.nx * cg.ny;
+            pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
+                const int h = ((i + j + k) & 1) == 1 ? 0 : 1;
+                if (h == 1 && !second) return;
+                // parent of the pair and of its neighbours: the same coarse
+                // cell unless the neighbour crosses a parent boundary
+                const long long P = cell_index(cg, i >> 1, j >> 1, d3 ? (k >> 1) : 0);
+                const T pc = __ldg(L.xc + P);
+                auto nb2 = [&](long long m, int jj, int kk, bool sec) {
+                    const Pair<T> v = ld2<T, V>(L.x, m, sec);
+                    const int dj = (jj >> 1) - (j >> 1), dk = d3 ? (kk >> 1) - (k >> 1) : 0;
+                    const T q = (dj | dk) == 0 ? pc : __ldg(L.xc + P + dj * csy + dk * csz);
+                    return Pair<T>{v.a + alpha * q, v.b + alpha * q};
+                };
+                auto nb1 = [&](long long m, int ii) {
+                    return __ldg(L.x + m) + alpha * __ldg(L.xc + P + ((ii >> 1) - (i >> 1)));
+                };
+                const Pair<T> x2 = ld2<T, V>(L.x, c, second);
+                const Pair<T> own{x2.a + alpha * pc, x2.b + alpha * pc};
+                const T sh = pair_nsum1<T, V>(h, L.g, L.cx, L.cy, L.cz, i, j, k, c, second, own, nb2, nb1);
+                const long long ch = c + h;
+                L.x[ch] = (__ldg(L.b + ch) + sh) * __ldg(L.inv + ch);
+            });
         });
     }
 }
@@ -292,31 +461,36 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) post_black_kernel(const BLev
 // Last red pass of the fine level, with rho' = z . r (z = x, r = b there)
 // per scene; the scene's last flush sets beta (0 for a new direction).
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) red_dot_kernel(const BLevel<T> *__restrict__ levels,
-                                                                   const BSeg *__restrict__ segs, int nseg, int n,
-                                                                   const BScene<T> *__restrict__ scenes, int gate,
-                                                                   double *part, const int *__restrict__ scene_of) {
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    red_dot_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                   const BScene<T> *__restrict__ scenes, int gate, double *part, const int *__restrict__ scene_of,
+                   const BatchCounters *live) {
+    if (batch_idle(live)) return;
     __shared__ double shf[BLOCK_THREADS / 32];
     __shared__ ItemCtx<T> ctx;
-    reduce_items<T, SumAcc>(
+    reduce_items<T, DotAcc<T>>(
         segs, nseg, n, part, levels, scenes, gate, ctx,
-        [&](const BItem &it, SumAcc &acc) {
+        [&](const BItem &it, DotAcc<T> &acc) {
             const BLevel<T> &L = ctx.L;
-            auto xval = [&](long long m, int, int, int) { return __ldg(L.x + m); };
-            pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
-                const int hr = ((i + j + k) & 1) == 0 ? 0 : 1;
-                for (int h = 0; h < (second ? 2 : 1); ++h) {
-                    const long long cc = c + h;
-                    const T bv = __ldg(L.b + cc);
-                    T xv;
-                    if (h == hr) {
-                        xv = (bv + nsum(L, i + h, j, k, cc, xval)) * __ldg(L.inv + cc);
-                        L.x[cc] = xv;
-                    } else {
-                        xv = L.x[cc];
+            with_vec(L.vec, [&](auto vt) {
+                constexpr bool V = decltype(vt)::value;
+                auto nb2 = [&](long long m, int, int, bool sec) { return ld2<T, V>(L.x, m, sec); };
+                auto nb1 = [&](long long m, int) { return __ldg(L.x + m); };
+                pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
+                    const int hr = ((i + j + k) & 1) == 0 ? 0 : 1;
+                    const Pair<T> x2 = ld2<T, V>(L.x, c, second), b2 = ld2<T, V>(L.b, c, second);
+                    Pair<T> out = x2;
+                    if (hr == 0 || second) {
+                        const T sh = pair_nsum1<T, V>(hr, L.g, L.cx, L.cy, L.cz, i, j, k, c, second, x2, nb2, nb1);
+                        const long long ch = c + hr;
+                        const T xv = ((hr ? b2.b : b2.a) + sh) * __ldg(L.inv + ch);
+                        if (hr) out.b = xv;
+                        else out.a = xv;
+                        L.x[ch] = xv;
                     }
-                    acc.v = fma((double)xv, (double)bv, acc.v);
-                }
+                    acc.add(out.a, b2.a);
+                    if (second) acc.add(out.b, b2.b);
+                });
             });
         },
         [&](const BItem &it, int flushes) {
@@ -343,8 +517,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) red_dot_kernel(const BLevel<
 
 // ---- shared-memory tail, one block per scene -----------------------------------
 
+// A tail level in shared memory; descriptors live in shared memory too (one
+// copy per block, read as broadcasts).
 template <class T> struct SLevel {
     int nx, ny, nz, dim, n;
+    FastDiv fx, fxy;  // nx and nx ny, to split cell indices
     T *b, *x, *inv, *diag, *cx, *cy, *cz;
 };
 
@@ -365,7 +542,8 @@ __device__ __forceinline__ T snb(const SLevel<T> &L, int i, int j, int k, int c,
 
 template <class T, class F> __device__ __forceinline__ void s_for_each(const SLevel<T> &L, F f) {
     for (int c = threadIdx.x; c < L.n; c += blockDim.x) {
-        const int i = c % L.nx, t = c / L.nx, j = t % L.ny, k = t / L.ny;
+        const int t = (int)fdiv((unsigned)c, L.fx), k = (int)fdiv((unsigned)c, L.fxy);
+        const int i = c - t * L.nx, j = t - k * L.ny;
         f(i, j, k, c);
     }
     __syncthreads();
@@ -373,39 +551,47 @@ template <class T, class F> __device__ __forceinline__ void s_for_each(const SLe
 
 // The V-cycle of the levels lv[0..nt) from shared memory: b of lv[0] in,
 // x of lv[0] out, same smoother, transfers and coarsest solve (FP64
-// symmetric sweep pairs) as the global levels.
+// symmetric sweep pairs, with the coarsest operator and right-hand side
+// held in FP64) as the global levels.
 template <class T>
 __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *__restrict__ tails,
                                                                const BScene<T> *__restrict__ scenes, int gate,
-                                                               MgSettings ms) {
+                                                               MgSettings ms, const BatchCounters *live) {
+    if (batch_idle(live)) return;
     const int s = blockIdx.x;
     const BTail<T> &A = tails[s];
     if (A.nt <= 0) return;
     if (gated(scenes[s].sc, gate)) return;
     extern __shared__ __align__(16) unsigned char tail_smem[];
-    SLevel<T> S[MG_MAX_LEVELS];
-    size_t off = 0;
-    T *base = reinterpret_cast<T *>(tail_smem);
-    for (int l = 0; l < A.nt; ++l) {
-        const Grid &g = A.lv[l].g;
-        SLevel<T> &L = S[l];
-        L.nx = g.nx;
-        L.ny = g.ny;
-        L.nz = g.nz;
-        L.dim = g.dim;
-        L.n = (int)g.ncell;
-        T **arr[7] = {&L.b, &L.x, &L.inv, &L.diag, &L.cx, &L.cy, &L.cz};
-        for (int a = 0; a < 7; ++a) {
-            *arr[a] = base + off;
-            off += (size_t)L.n;
+    __shared__ SLevel<T> S[MG_MAX_LEVELS];
+    __shared__ double *cd[6];  // coarsest: x, b, inv, cx, cy, cz in FP64
+    if (threadIdx.x == 0) {
+        size_t off = 0;
+        T *base = reinterpret_cast<T *>(tail_smem);
+        for (int l = 0; l < A.nt; ++l) {
+            const Grid &g = A.lv[l].g;
+            SLevel<T> &L = S[l];
+            L.nx = g.nx;
+            L.ny = g.ny;
+            L.nz = g.nz;
+            L.dim = g.dim;
+            L.n = (int)g.ncell;
+            L.fx = make_fastdiv((unsigned)g.nx);
+            L.fxy = make_fastdiv((unsigned)(g.nx * g.ny));
+            T **arr[7] = {&L.b, &L.x, &L.inv, &L.diag, &L.cx, &L.cy, &L.cz};
+            for (int a = 0; a < 7; ++a) {
+                *arr[a] = base + off;
+                off += (size_t)L.n;
+            }
         }
+        size_t off_bytes = (off * sizeof(T) + 15) / 16 * 16;
+        const int nc = (int)A.lv[A.nt - 1].g.ncell;
+        for (int a = 0; a < 6; ++a) cd[a] = reinterpret_cast<double *>(tail_smem + off_bytes) + (size_t)a * nc;
     }
-    size_t off_bytes = off * sizeof(T);
-    off_bytes = (off_bytes + 15) / 16 * 16;
-    double *xc = reinterpret_cast<double *>(tail_smem + off_bytes);
+    __syncthreads();
     for (int l = 0; l < A.nt; ++l) {
         const MgLevel<T> &G = A.lv[l];
-        SLevel<T> &L = S[l];
+        const SLevel<T> &L = S[l];
         for (int c = threadIdx.x; c < L.n; c += blockDim.x) {
             L.inv[c] = G.inv[c];
             L.diag[c] = G.diag[c];
@@ -450,24 +636,32 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
     }
     {
         const SLevel<T> &L = S[A.nt - 1];
-        for (int c = threadIdx.x; c < L.n; c += blockDim.x) xc[c] = 0.0;
+        double *xc = cd[0], *bd = cd[1], *ivd = cd[2], *cxd = cd[3], *cyd = cd[4], *czd = cd[5];
+        for (int c = threadIdx.x; c < L.n; c += blockDim.x) {
+            xc[c] = 0.0;
+            bd[c] = (double)L.b[c];
+            ivd[c] = (double)L.inv[c];
+            cxd[c] = (double)L.cx[c];
+            cyd[c] = (double)L.cy[c];
+            czd[c] = (double)L.cz[c];
+        }
         __syncthreads();
+        const int sy = L.nx, sz = L.nx * L.ny;
         for (int p = 0; p < ms.coarsest_pairs; ++p) {
             const int order[4] = {0, 1, 1, 0};
             for (int q = 0; q < 4; ++q)
                 s_for_each(L, [&](int i, int j, int k, int c) {
                     if (((i + j + k) & 1) != order[q]) return;
-                    const int sy = L.nx, sz = L.nx * L.ny;
                     double acc = 0.0;
-                    if (i > 0) acc += (double)L.cx[c - 1] * xc[c - 1];
-                    if (i + 1 < L.nx) acc += (double)L.cx[c] * xc[c + 1];
-                    if (j > 0) acc += (double)L.cy[c - sy] * xc[c - sy];
-                    if (j + 1 < L.ny) acc += (double)L.cy[c] * xc[c + sy];
+                    if (i > 0) acc += cxd[c - 1] * xc[c - 1];
+                    if (i + 1 < L.nx) acc += cxd[c] * xc[c + 1];
+                    if (j > 0) acc += cyd[c - sy] * xc[c - sy];
+                    if (j + 1 < L.ny) acc += cyd[c] * xc[c + sy];
                     if (L.dim == 3) {
-                        if (k > 0) acc += (double)L.cz[c - sz] * xc[c - sz];
-                        if (k + 1 < L.nz) acc += (double)L.cz[c] * xc[c + sz];
+                        if (k > 0) acc += czd[c - sz] * xc[c - sz];
+                        if (k + 1 < L.nz) acc += czd[c] * xc[c + sz];
                     }
-                    xc[c] = ((double)L.b[c] + acc) * (double)L.inv[c];
+                    xc[c] = (bd[c] + acc) * ivd[c];
                 });
         }
         for (int c = threadIdx.x; c < L.n; c += blockDim.x) L.x[c] = T(xc[c]);
@@ -479,7 +673,8 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
         s_for_each(L, [&](int i, int j, int k, int c) {
             if (((i + j + k) & 1) != 1) return;
             L.x[c] = (L.b[c] + snb(L, i, j, k, c, [&](int m) {
-                         const int mi = m % L.nx, t = m / L.nx, mj = t % L.ny, mk = t / L.ny;
+                         const int mt = (int)fdiv((unsigned)m, L.fx), mk = (int)fdiv((unsigned)m, L.fxy);
+                         const int mi = m - mt * L.nx, mj = mt - mk * L.ny;
                          return L.x[m] +
                                 alpha * C.x[(mi >> 1) + C.nx * ((mj >> 1) + C.ny * (L.dim == 3 ? (mk >> 1) : 0))];
                      })) * L.inv[c];
@@ -502,9 +697,10 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
 // ---- CG on the fine level -----------------------------------------------------------
 
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) direction_kernel(const BLevel<T> *__restrict__ levels,
-                                                                     const BSeg *__restrict__ segs, int nseg, int n,
-                                                                     const BScene<T> *__restrict__ scenes, int gate) {
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    direction_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                     const BScene<T> *__restrict__ scenes, int gate, const BatchCounters *live) {
+    if (batch_idle(live)) return;
     __shared__ ItemCtx<T> ctx;
     int cur = -1;
     int sgc = 0;
@@ -515,29 +711,48 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) direction_kernel(const BLeve
         const BLevel<T> &L = ctx.L;
         const BScene<T> &S = ctx.S;
         const T beta = T(ctx.beta);
-        if (beta == T(0)) cell_tile(L.g, it, [&](int, int, int, long long c) { S.p[c] = S.z[c]; });
-        else cell_tile(L.g, it, [&](int, int, int, long long c) { S.p[c] = S.z[c] + beta * S.p[c]; });
+        with_vec(L.vec, [&](auto vt) {
+            constexpr bool V = decltype(vt)::value;
+            pair_tile(L.g, it, [&](int, int, int, long long c, bool second) {
+                const Pair<T> z2 = ld2<T, V>(S.z, c, second);
+                Pair<T> p2;
+                if (beta == T(0)) {
+                    p2 = z2;
+                } else {
+                    const Pair<T> o = ld2<T, V>(S.p, c, second);
+                    p2 = Pair<T>{z2.a + beta * o.a, z2.b + beta * o.b};
+                }
+                st2<T, V>(S.p, c, p2, second);
+            });
+        });
     }
 }
 
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) spmv_kernel(const BLevel<T> *__restrict__ levels,
-                                                                const BSeg *__restrict__ segs, int nseg, int n,
-                                                                const BScene<T> *__restrict__ scenes, int gate,
-                                                                double *part, const int *__restrict__ scene_of) {
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    spmv_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                const BScene<T> *__restrict__ scenes, int gate, double *part, const int *__restrict__ scene_of,
+                const BatchCounters *live) {
+    if (batch_idle(live)) return;
     __shared__ double shf[BLOCK_THREADS / 32];
     __shared__ ItemCtx<T> ctx;
-    reduce_items<T, SumAcc>(
+    reduce_items<T, DotAcc<T>>(
         segs, nseg, n, part, levels, scenes, gate, ctx,
-        [&](const BItem &it, SumAcc &acc) {
+        [&](const BItem &it, DotAcc<T> &acc) {
             const BLevel<T> &L = ctx.L;
             const BScene<T> &S = ctx.S;
-            auto pval = [&](long long m, int, int, int) { return __ldg(S.p + m); };
-            cell_tile(L.g, it, [&](int i, int j, int k, long long c) {
-                const T pc = __ldg(S.p + c);
-                const T qv = __ldg(L.diag + c) * pc - nsum(L, i, j, k, c, pval);
-                S.q[c] = qv;
-                acc.v = fma((double)pc, (double)qv, acc.v);
+            with_vec(L.vec, [&](auto vt) {
+                constexpr bool V = decltype(vt)::value;
+                auto nb2 = [&](long long m, int, int, bool sec) { return ld2<T, V>(S.p, m, sec); };
+                auto nb1 = [&](long long m, int) { return __ldg(S.p + m); };
+                pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
+                    const Pair<T> p2 = ld2<T, V>(S.p, c, second), d2 = ld2<T, V>(L.diag, c, second);
+                    const Pair<T> s = pair_nsum<T, V, 2>(L.g, L.cx, L.cy, L.cz, i, j, k, c, second, p2, nb2, nb1);
+                    const Pair<T> q2{d2.a * p2.a - s.a, d2.b * p2.b - s.b};
+                    st2<T, V>(S.q, c, q2, second);
+                    acc.add(p2.a, q2.a);
+                    if (second) acc.add(p2.b, q2.b);
+                });
             });
         },
         [&](const BItem &it, int flushes) {
@@ -556,26 +771,38 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) spmv_kernel(const BLevel<T> 
 // x += alpha p (x = alpha p on the first update of a solve), r -= alpha q,
 // |r|_inf. mode 0: the solve's stopping rule; mode 1: inner solve.
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) update_kernel(const BLevel<T> *__restrict__ levels,
-                                                                  const BSeg *__restrict__ segs, int nseg, int n,
-                                                                  const BScene<T> *__restrict__ scenes, int gate,
-                                                                  double *part, int mode, BatchCounters *cnt,
-                                                                  const int *__restrict__ scene_of) {
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    update_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                  const BScene<T> *__restrict__ scenes, int gate, double *part, int mode, BatchCounters *cnt,
+                  const int *__restrict__ scene_of) {
+    if (batch_idle(cnt)) return;
     __shared__ double shf[BLOCK_THREADS / 32];
     __shared__ ItemCtx<T> ctx;
-    reduce_items<T, MaxAcc>(
+    reduce_items<T, MaxAcc<T>>(
         segs, nseg, n, part, levels, scenes, gate, ctx,
-        [&](const BItem &it, MaxAcc &acc) {
+        [&](const BItem &it, MaxAcc<T> &acc) {
             const BLevel<T> &L = ctx.L;
             const BScene<T> &S = ctx.S;
             const T alpha = T(ctx.alpha);
             const bool overwrite = ctx.overwrite != 0;
-            cell_tile(L.g, it, [&](int, int, int, long long c) {
-                const T pc = S.p[c];
-                S.x[c] = overwrite ? alpha * pc : S.x[c] + alpha * pc;
-                const T rv = S.r[c] - alpha * S.q[c];
-                S.r[c] = rv;
-                acc.v = fmax(acc.v, fabs((double)rv));
+            with_vec(L.vec, [&](auto vt) {
+                constexpr bool V = decltype(vt)::value;
+                pair_tile(L.g, it, [&](int, int, int, long long c, bool second) {
+                    const Pair<T> p2 = ld2<T, V>(S.p, c, second), q2 = ld2<T, V>(S.q, c, second);
+                    const Pair<T> r2 = ld2<T, V>(S.r, c, second);
+                    Pair<T> x2;
+                    if (overwrite) {
+                        x2 = Pair<T>{alpha * p2.a, alpha * p2.b};
+                    } else {
+                        const Pair<T> o = ld2<T, V>(S.x, c, second);
+                        x2 = Pair<T>{o.a + alpha * p2.a, o.b + alpha * p2.b};
+                    }
+                    const Pair<T> rn{r2.a - alpha * q2.a, r2.b - alpha * q2.b};
+                    st2<T, V>(S.x, c, x2, second);
+                    st2<T, V>(S.r, c, rn, second);
+                    acc.add(rn.a);
+                    if (second) acc.add(rn.b);
+                });
             });
         },
         [&](const BItem &it, int flushes) {
@@ -607,6 +834,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) update_kernel(const BLevel<T
                         } else if (res <= sc->inner_tol || sc->inner_iter >= sc->inner_max ||
                                    sc->iter >= sc->max_iter) {
                             sc->inner_done = 1;
+                            atomicAdd(&cnt->refine, 1);
                         }
                     }
                     if (finished) {
@@ -622,9 +850,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) update_kernel(const BLevel<T
 // ---- mixed precision: FP64 refinement -------------------------------------------------
 
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) refine_accumulate_kernel(const BLevel<T> *__restrict__ levels,
-                                                                             const BSeg *__restrict__ segs, int nseg, int n,
-                                                                             const BScene<T> *__restrict__ scenes) {
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    refine_accumulate_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                             const BScene<T> *__restrict__ scenes, const BatchCounters *cnt) {
+    // no scene has finished an inner solve in this iteration
+    if (*(const volatile int *)&cnt->refine <= 0) return;
     __shared__ ItemCtx<T> ctx;
     int cur = -1;
     int sgc = 0;
@@ -634,49 +864,96 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) refine_accumulate_kernel(con
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
         const BScene<T> &S = ctx.S;
-        cell_tile(L.g, it, [&](int, int, int, long long c) { S.x64[c] += (double)S.x[c]; });
+        with_vec(L.vec, [&](auto vt) {
+            constexpr bool V = decltype(vt)::value;
+            pair_tile(L.g, it, [&](int, int, int, long long c, bool second) {
+                const Pair<T> d2 = ld2<T, V>(S.x, c, second);
+                const Pair<double> o = ld2<double, V>(S.x64, c, second);
+                st2<double, V>(S.x64, c, Pair<double>{o.a + (double)d2.a, o.b + (double)d2.b}, second);
+            });
+        });
     }
 }
 
 // r64 = b - A64 (prev + x64) (x64 absent: initial), r_T = r64, |r64|_inf;
 // the scene's last flush applies the stopping rule and opens the next inner
-// solve. initial: sets the threshold, zeroes x64.
+// solve. initial: sets the threshold, zeroes x64. Each cell's residual is
+// accumulated as diag X minus the neighbour terms one by one (-x, +x, -y,
+// +y, -z, +z), in FP64.
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 6) refine_residual_kernel(
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_residual_kernel(
     const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
     const BScene<T> *__restrict__ scenes, double *part, int initial, double residual, int max_iter,
     double inner_rel, int inner_max, BatchCounters *cnt, const int *__restrict__ scene_of) {
+    if (!initial && *(const volatile int *)&cnt->refine <= 0) return;
     __shared__ double shf[BLOCK_THREADS / 32];
     __shared__ ItemCtx<T> ctx;
-    reduce_items<T, MaxAcc>(
+    reduce_items<T, MaxAcc<double>>(
         segs, nseg, n, part, levels, scenes, initial ? -1 : 2, ctx,
-        [&](const BItem &it, MaxAcc &acc) {
+        [&](const BItem &it, MaxAcc<double> &acc) {
             const BLevel<T> &L = ctx.L;
             const BScene<T> &S = ctx.S;
             const Grid &g = L.g;
             const long long sy = g.nx, sz = (long long)g.nx * g.ny;
             const Operator<double> &A = S.A;
-            auto X = [&](long long c) {
-                double v = initial ? 0.0 : S.x64[c];
-                if (S.prev) v += S.prev[c];
-                return v;
-            };
-            cell_tile(g, it, [&](int i, int j, int k, long long c) {
-                double a = A.diag[c] * X(c);
-                if (i > 0) a -= A.cx[c - 1] * X(c - 1);
-                if (i + 1 < g.nx) a -= A.cx[c] * X(c + 1);
-                if (j > 0) a -= A.cy[c - sy] * X(c - sy);
-                if (j + 1 < g.ny) a -= A.cy[c] * X(c + sy);
-                if (g.dim == 3) {
-                    if (k > 0) a -= A.cz[c - sz] * X(c - sz);
-                    if (k + 1 < g.nz) a -= A.cz[c] * X(c + sz);
-                }
-                const double rv = S.b[c] - a;
-                S.r64[c] = rv;
-                S.r[c] = T(rv);
-                acc.v = fmax(acc.v, fabs(rv));
+            with_vec(L.vec, [&](auto vt) {
+                constexpr bool V = decltype(vt)::value;
+                auto X2 = [&](long long m, bool sec) {
+                    Pair<double> v{0.0, 0.0};
+                    if (!initial) v = ld2<double, V>(S.x64, m, sec);
+                    if (S.prev) {
+                        const Pair<double> pv = ld2<double, V>(S.prev, m, sec);
+                        v.a += pv.a;
+                        v.b += pv.b;
+                    }
+                    return v;
+                };
+                auto X1 = [&](long long m) {
+                    double v = initial ? 0.0 : __ldg(S.x64 + m);
+                    if (S.prev) v += __ldg(S.prev + m);
+                    return v;
+                };
+                pair_tile(g, it, [&](int i, int j, int k, long long c, bool second) {
+                    const Pair<double> xc = X2(c, second), dg = ld2<double, V>(A.diag, c, second);
+                    const Pair<double> cxp = ld2<double, V>(A.cx, c, second);
+                    double a0 = dg.a * xc.a, a1 = dg.b * xc.b;
+                    if (i > 0) a0 -= __ldg(A.cx + c - 1) * X1(c - 1);
+                    if (second) {
+                        a0 -= cxp.a * xc.b;
+                        a1 -= cxp.a * xc.a;
+                        if (i + 2 < g.nx) a1 -= cxp.b * X1(c + 2);
+                    }
+                    if (j > 0) {
+                        const Pair<double> w = ld2<double, V>(A.cy, c - sy, second), v = X2(c - sy, second);
+                        a0 -= w.a * v.a;
+                        a1 -= w.b * v.b;
+                    }
+                    if (j + 1 < g.ny) {
+                        const Pair<double> w = ld2<double, V>(A.cy, c, second), v = X2(c + sy, second);
+                        a0 -= w.a * v.a;
+                        a1 -= w.b * v.b;
+                    }
+                    if (g.dim == 3) {
+                        if (k > 0) {
+                            const Pair<double> w = ld2<double, V>(A.cz, c - sz, second), v = X2(c - sz, second);
+                            a0 -= w.a * v.a;
+                            a1 -= w.b * v.b;
+                        }
+                        if (k + 1 < g.nz) {
+                            const Pair<double> w = ld2<double, V>(A.cz, c, second), v = X2(c + sz, second);
+                            a0 -= w.a * v.a;
+                            a1 -= w.b * v.b;
+                        }
+                    }
+                    const Pair<double> bb = ld2<double, V>(S.b, c, second);
+                    const Pair<double> rv{bb.a - a0, bb.b - a1};
+                    st2<double, V>(S.r64, c, rv, second);
+                    st2<T, V>(S.r, c, Pair<T>{T(rv.a), T(rv.b)}, second);
+                    acc.add(rv.a);
+                    if (second) acc.add(rv.b);
+                    if (initial) st2<double, V>(S.x64, c, Pair<double>{0.0, 0.0}, second);
+                });
             });
-            if (initial) cell_tile(g, it, [&](int, int, int, long long c) { S.x64[c] = 0.0; });
         },
         [&](const BItem &it, int flushes) {
             Scalars *sc = ctx.S.sc;
@@ -695,6 +972,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) refine_residual_kernel(
                         sc->done = 0;
                     } else {
                         sc->outer_iter += 1;
+                        atomicSub(&cnt->refine, 1);
                     }
                     sc->res = res;
                     int finished = 1;
@@ -728,37 +1006,39 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) refine_residual_kernel(
 template <class T>
 cudaError_t b_presmooth(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                         const BScene<T> *scenes) {
-    presmooth_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate);
+    presmooth_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, L.cnt);
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_sweep(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
-                    int color) {
-    sweep_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, color);
+cudaError_t b_sweep(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
+                    const BScene<T> *scenes, int color) {
+    sweep_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, color, L.cnt);
     return cudaGetLastError();
 }
 template <class T>
 cudaError_t b_restrict(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                        const BScene<T> *scenes) {
-    restrict_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate);
+    restrict_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, L.cnt);
     return cudaGetLastError();
 }
 template <class T>
 cudaError_t b_post_black(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                          const BScene<T> *scenes, T alpha) {
-    post_black_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, alpha);
+    post_black_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, alpha,
+                                                                   L.cnt);
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_red_dot(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
-                      double *part) {
-    red_dot_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, part, L.scene_of);
+cudaError_t b_red_dot(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
+                      const BScene<T> *scenes, double *part) {
+    red_dot_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, part,
+                                                                L.scene_of, L.cnt);
     return cudaGetLastError();
 }
 template <class T>
 cudaError_t b_tail(const BLaunch &L, const BTail<T> *tails, int nscenes, const BScene<T> *scenes, MgSettings ms,
                    size_t smem) {
-    tail_kernel<T><<<nscenes, MG_TAIL_THREADS, smem, L.stream>>>(tails, scenes, L.gate, ms);
+    tail_kernel<T><<<nscenes, MG_TAIL_THREADS, smem, L.stream>>>(tails, scenes, L.gate, ms, L.cnt);
     return cudaGetLastError();
 }
 template <class T> cudaError_t b_tail_enable(size_t bytes) {
@@ -767,18 +1047,19 @@ template <class T> cudaError_t b_tail_enable(size_t bytes) {
 template <class T>
 cudaError_t b_direction(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                         const BScene<T> *scenes) {
-    direction_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate);
+    direction_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, L.cnt);
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_spmv(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
-                   double *part) {
-    spmv_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, part, L.scene_of);
+cudaError_t b_spmv(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
+                   const BScene<T> *scenes, double *part) {
+    spmv_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, part, L.scene_of,
+                                                             L.cnt);
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_update(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
-                     double *part, int mode, BatchCounters *cnt) {
+cudaError_t b_update(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
+                     const BScene<T> *scenes, double *part, int mode, BatchCounters *cnt) {
     update_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, part, mode, cnt,
                                                                L.scene_of);
     return cudaGetLastError();
@@ -786,7 +1067,7 @@ cudaError_t b_update(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs
 template <class T>
 cudaError_t b_refine_accumulate(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                                 const BScene<T> *scenes) {
-    refine_accumulate_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes);
+    refine_accumulate_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.cnt);
     return cudaGetLastError();
 }
 template <class T>
@@ -798,25 +1079,29 @@ cudaError_t b_refine_residual(const BLaunch &L, const BLevel<T> *levels, const B
     return cudaGetLastError();
 }
 
-#define GBP_BATCH_INSTANTIATE(T)                                                                                   \
-    template cudaError_t b_presmooth<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *); \
-    template cudaError_t b_sweep<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *, int); \
-    template cudaError_t b_restrict<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *);  \
-    template cudaError_t b_post_black<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *, \
-                                         T);                                                                       \
-    template cudaError_t b_red_dot<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *,    \
-                                      double *);                                                                   \
-    template cudaError_t b_tail<T>(const BLaunch &, const BTail<T> *, int, const BScene<T> *, MgSettings, size_t);  \
-    template cudaError_t b_tail_enable<T>(size_t);                                                                 \
-    template cudaError_t b_direction<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *); \
-    template cudaError_t b_spmv<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *,       \
-                                   double *);                                                                      \
-    template cudaError_t b_update<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *,     \
-                                     double *, int, BatchCounters *);                                              \
-    template cudaError_t b_refine_accumulate<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,           \
-                                                const BScene<T> *);                                                \
-    template cudaError_t b_refine_residual<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,             \
-                                              const BScene<T> *, double *, int, double, int, double, int,          \
+#define GBP_BATCH_INSTANTIATE(T)                                                                                     \
+    template cudaError_t b_presmooth<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,                 \
+                                        const BScene<T> *);                                                          \
+    template cudaError_t b_sweep<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *,  \
+                                    int);                                                                            \
+    template cudaError_t b_restrict<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,                  \
+                                       const BScene<T> *);                                                           \
+    template cudaError_t b_post_black<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,                \
+                                         const BScene<T> *, T);                                                      \
+    template cudaError_t b_red_dot<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,                   \
+                                      const BScene<T> *, double *);                                                  \
+    template cudaError_t b_tail<T>(const BLaunch &, const BTail<T> *, int, const BScene<T> *, MgSettings, size_t);    \
+    template cudaError_t b_tail_enable<T>(size_t);                                                                   \
+    template cudaError_t b_direction<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,                 \
+                                        const BScene<T> *);                                                          \
+    template cudaError_t b_spmv<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *,   \
+                                   double *);                                                                        \
+    template cudaError_t b_update<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *, \
+                                     double *, int, BatchCounters *);                                                \
+    template cudaError_t b_refine_accumulate<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,         \
+                                                const BScene<T> *);                                                  \
+    template cudaError_t b_refine_residual<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,           \
+                                              const BScene<T> *, double *, int, double, int, double, int,            \
                                               BatchCounters *);
 
 GBP_BATCH_INSTANTIATE(double)

@@ -44,7 +44,7 @@ void BatchRunner::release() {
     n_restrict_.clear();
     s_pair_.clear();
     s_restrict_.clear();
-    d_fine_cells_ = d_fine_pairs_ = nullptr;
+    d_fine_pairs_ = nullptr;
     d_part_ = nullptr;
     d_counters_ = nullptr;
     bytes_ = 0;
@@ -66,7 +66,13 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
     nscenes_ = plan.nscenes;
     max_global_ = plan.max_global;
     tail_smem_ = plan.tail_smem;
-    grid_blocks_ = grid_blocks;
+    {
+        int dev = 0, sms = 0;
+        RUN_CUDA(cudaGetDevice(&dev));
+        RUN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        grid_blocks_ = std::min(MAX_GRID, std::max(1, sms * BatchOcc<T>::blocks));
+        (void)grid_blocks;
+    }
     mixed_ = sizeof(T) == 4;
     if ((rc = upload(plan.levels.data(), plan.levels.size() * sizeof(BLevel<T>), &d_levels_))) return rc;
     if ((rc = upload(plan.scenes.data(), plan.scenes.size() * sizeof(BScene<T>), &d_scenes_))) return rc;
@@ -76,7 +82,7 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
         d_scene_of_ = static_cast<int *>(d);
     }
     if ((rc = upload(plan.tails.data(), plan.tails.size() * sizeof(BTail<T>), &d_tails_))) return rc;
-    size_t max_items = (size_t)std::max(plan.n_fine_cells, plan.n_fine_pairs);
+    size_t max_items = (size_t)plan.n_fine_pairs;
     auto segs = [&](const std::vector<BSeg> &list, BSeg **dst, int *nseg) -> int {
         void *d;
         int rc2 = upload(list.data(), list.size() * sizeof(BSeg), &d);
@@ -95,8 +101,6 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
         if ((rc = segs(plan.restrict_[l], &d_restrict_[l], &s_restrict_[l]))) return rc;
         max_items = std::max(max_items, (size_t)plan.n_pair[l]);
     }
-    if ((rc = segs(plan.fine_cells, &d_fine_cells_, &s_fine_cells_))) return rc;
-    n_fine_cells_ = plan.n_fine_cells;
     if ((rc = segs(plan.fine_pairs, &d_fine_pairs_, &s_fine_pairs_))) return rc;
     n_fine_pairs_ = plan.n_fine_pairs;
     void *d;
@@ -127,7 +131,7 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
     auto *sc = static_cast<const BScene<T> *>(d_scenes_);
     auto *tl = static_cast<const BTail<T> *>(d_tails_);
     cudaError_t e = cudaSuccess;
-    auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, gate, d_scene_of_}; };
+    auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, gate, d_scene_of_, d_counters_}; };
     // descend
     for (int l = 0; l < max_global_ && e == cudaSuccess; ++l) {
         e = b_presmooth<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc);
@@ -141,7 +145,7 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
         ++*nodes;
     }
     if (e == cudaSuccess && tail_smem_ > 0) {
-        e = b_tail<T>(BLaunch{nscenes_, st, gate, d_scene_of_}, tl, nscenes_, sc, ms, tail_smem_);
+        e = b_tail<T>(BLaunch{nscenes_, st, gate, d_scene_of_, d_counters_}, tl, nscenes_, sc, ms, tail_smem_);
         ++*nodes;
     }
     // ascend
@@ -159,16 +163,16 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
         ++*nodes;
     }
     // CG on the fine level
-    if (e == cudaSuccess) e = b_direction<T>(L(n_fine_cells_), lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc);
-    if (e == cudaSuccess) e = b_spmv<T>(L(n_fine_cells_), lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc, d_part_);
+    if (e == cudaSuccess) e = b_direction<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc);
+    if (e == cudaSuccess) e = b_spmv<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_);
     if (e == cudaSuccess)
-        e = b_update<T>(L(n_fine_cells_), lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc, d_part_, mixed_ ? 1 : 0, d_counters_);
+        e = b_update<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_, mixed_ ? 1 : 0, d_counters_);
     *nodes += 3;
     if (mixed_ && e == cudaSuccess) {
-        const BLaunch L2{blocks_for(n_fine_cells_, grid_blocks_), st, 2, d_scene_of_};
-        e = b_refine_accumulate<T>(L2, lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc);
+        const BLaunch L2{blocks_for(n_fine_pairs_, grid_blocks_), st, 2, d_scene_of_, d_counters_};
+        e = b_refine_accumulate<T>(L2, lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc);
         if (e == cudaSuccess)
-            e = b_refine_residual<T>(L2, lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc, d_part_, 0, p.residual,
+            e = b_refine_residual<T>(L2, lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_, 0, p.residual,
                                      p.max_iterations, inner_rel_, kInnerMax, d_counters_);
         *nodes += 2;
     }
@@ -180,10 +184,11 @@ template <class T> int BatchRunner::solve(const gbp_params &p, cudaStream_t st, 
     auto *lv = static_cast<const BLevel<T> *>(d_levels_);
     auto *sc = static_cast<const BScene<T> *>(d_scenes_);
     h_counters_->remaining = nscenes_;
+    h_counters_->refine = 0;
     RUN_CUDA(cudaMemcpyAsync(d_counters_, h_counters_, sizeof(BatchCounters), cudaMemcpyHostToDevice, st));
     // initial residual of every scene (also zeroes x64, sets thresholds)
-    RUN_CUDA(b_refine_residual<T>(BLaunch{blocks_for(n_fine_cells_, grid_blocks_), st, 0, d_scene_of_}, lv,
-                                  d_fine_cells_, s_fine_cells_, n_fine_cells_, sc, d_part_, 1, p.residual, p.max_iterations, inner_rel_, kInnerMax,
+    RUN_CUDA(b_refine_residual<T>(BLaunch{blocks_for(n_fine_pairs_, grid_blocks_), st, 0, d_scene_of_, d_counters_}, lv,
+                                  d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_, 1, p.residual, p.max_iterations, inner_rel_, kInnerMax,
                                   d_counters_));
     *launches += 1;
     const long long key = ((long long)(p.mg_smooth > 0 ? p.mg_smooth : 1) << 40) ^
@@ -224,7 +229,7 @@ template <class T> int BatchRunner::bench(int which, int reps, cudaStream_t st, 
     auto *sc = static_cast<const BScene<T> *>(d_scenes_);
     const MgSettings mset = settings_of(gbp_params{});
     std::function<cudaError_t()> launch;
-    auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, 0, d_scene_of_}; };
+    auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, 0, d_scene_of_, d_counters_}; };
     switch (which) {
     case 0: launch = [&]() { return b_presmooth<T>(L(n_pair_[0]), lv, d_pair_[0], s_pair_[0], n_pair_[0], sc); }; break;
     case 1: launch = [&]() { return b_restrict<T>(L(n_restrict_[0]), lv, d_restrict_[0], s_restrict_[0], n_restrict_[0], sc); }; break;
@@ -232,16 +237,20 @@ template <class T> int BatchRunner::bench(int which, int reps, cudaStream_t st, 
         launch = [&]() { return b_post_black<T>(L(n_pair_[0]), lv, d_pair_[0], s_pair_[0], n_pair_[0], sc, T(mset.alpha)); };
         break;
     case 3: launch = [&]() { return b_red_dot<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_); }; break;
-    case 4: launch = [&]() { return b_direction<T>(L(n_fine_cells_), lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc); }; break;
-    case 5: launch = [&]() { return b_spmv<T>(L(n_fine_cells_), lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc, d_part_); }; break;
+    case 4: launch = [&]() { return b_direction<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc); }; break;
+    case 5: launch = [&]() { return b_spmv<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_); }; break;
     case 6:
         launch = [&]() {
-            return b_update<T>(L(n_fine_cells_), lv, d_fine_cells_, s_fine_cells_, n_fine_cells_, sc, d_part_, 0, d_counters_);
+            return b_update<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_, 0, d_counters_);
         };
         break;
     default: return fail(GBP_ERR_INVALID_ARGUMENT, "bench: unknown kernel");
     }
     if (max_global_ < 1) return fail(GBP_ERR_INVALID_ARGUMENT, "bench: no multigrid level");
+    // a live batch, so that no launch takes the idle exit
+    h_counters_->remaining = nscenes_;
+    h_counters_->refine = 0;
+    RUN_CUDA(cudaMemcpyAsync(d_counters_, h_counters_, sizeof(BatchCounters), cudaMemcpyHostToDevice, st));
     cudaEvent_t e0, e1;
     RUN_CUDA(cudaEventCreate(&e0));
     RUN_CUDA(cudaEventCreate(&e1));

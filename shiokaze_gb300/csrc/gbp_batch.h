@@ -34,6 +34,9 @@ template <class T> struct BLevel {
     T *bc;        // b of the next coarser level (restriction)
     Grid gc;      // the next coarser grid
     int scene;
+    // pairs of this level (and, on level 0, of the scene's vectors) move as
+    // 2-wide accesses: nx even and every such array 2-element aligned
+    int vec;
 };
 
 // Per-scene state of the fine level.
@@ -55,6 +58,19 @@ struct BItem {
     int ntiles;  // consecutive tiles of the item
     int begin;   // first item of this scene in the list
     int count;   // items of this scene in the list
+};
+
+// Resident blocks of BLOCK_THREADS per SM that the batched kernels of type
+// T are compiled for (their launch bounds) and launched with (grid = SMs x
+// this). The FP32 kernels move pairs of cells and want registers (48 a
+// thread at 5 blocks); the FP64 kernels are bound by the FP64 pipe and want
+// warps to hide its latency.
+template <class T> struct BatchOcc;
+template <> struct BatchOcc<float> {
+    static constexpr int blocks = 5;
+};
+template <> struct BatchOcc<double> {
+    static constexpr int blocks = 4;
 };
 
 // Tiles per item (items are the unit of load balance; reductions are per
@@ -95,7 +111,8 @@ inline long long cell_tiles(const Grid &g) { return g.ntiles; }
 
 struct BatchCounters {
     int remaining;  // scenes not done
-    int pad[3];
+    int refine;     // scenes whose inner solve ended, awaiting refinement
+    int pad[2];
 };
 
 // Device tables and work lists of one batch, built on the host.
@@ -107,12 +124,13 @@ template <class T> struct BatchPlan {
     std::vector<BScene<T>> scenes;
     std::vector<BTail<T>> tails;
     size_t tail_smem = 0;
-    // work lists as segments: pair[l], restrict[l] (coarse tiles of l+1),
-    // fine (tiles of level 0), with their item counts
+    // work lists as segments: pair[l] (pair tiles of level l), restrict[l]
+    // (cell tiles of level l+1), fine (pair tiles of level 0), with their
+    // item counts
     std::vector<std::vector<BSeg>> pair, restrict_;
-    std::vector<BSeg> fine_cells, fine_pairs;
+    std::vector<BSeg> fine_pairs;
     std::vector<int> n_pair, n_restrict;
-    int n_fine_cells = 0, n_fine_pairs = 0;
+    int n_fine_pairs = 0;
 };
 
 class BatchRunner {
@@ -155,8 +173,8 @@ private:
     int *d_scene_of_ = nullptr;
     std::vector<BSeg *> d_pair_, d_restrict_;
     std::vector<int> n_pair_, n_restrict_, s_pair_, s_restrict_;  // items, segments
-    BSeg *d_fine_cells_ = nullptr, *d_fine_pairs_ = nullptr;
-    int n_fine_cells_ = 0, n_fine_pairs_ = 0, s_fine_cells_ = 0, s_fine_pairs_ = 0;
+    BSeg *d_fine_pairs_ = nullptr;
+    int n_fine_pairs_ = 0, s_fine_pairs_ = 0;
     double *d_part_ = nullptr;  // 3 x max items
     int max_items_ = 0;
     BatchCounters *d_counters_ = nullptr, *h_counters_ = nullptr;
@@ -173,6 +191,7 @@ struct BLaunch {
     cudaStream_t stream;
     int gate;
     const int *scene_of;  // scene of each level-table entry (reductions)
+    BatchCounters *cnt;   // batch counters (idle and refinement checks)
 };
 
 template <class T>

@@ -25,6 +25,35 @@ constexpr int TILE_Y = 8;
 constexpr int BLOCK_THREADS = TILE_X * TILE_Y;  // 256
 constexpr int MAX_GRID = 152 * 8;               // partial-array capacity
 
+// Exact unsigned division by a divisor fixed at run time: one multiply-high,
+// an add and two shifts instead of a division routine (Granlund and
+// Montgomery, "Division by invariant integers using multiplication",
+// PLDI 1994, fig. 4.1). Exact for every 32-bit dividend and divisor >= 1.
+struct FastDiv {
+    unsigned d, m;
+    int s1, s2;
+};
+
+__host__ __device__ inline FastDiv make_fastdiv(unsigned d) {
+    FastDiv f;
+    f.d = d;
+    int l = 0;
+    while ((1ull << l) < d) ++l;  // l = ceil(log2 d)
+    f.m = (unsigned)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    f.s1 = l < 1 ? l : 1;
+    f.s2 = l > 1 ? l - 1 : 0;
+    return f;
+}
+
+__host__ __device__ __forceinline__ unsigned fdiv(unsigned n, const FastDiv &f) {
+#ifdef __CUDA_ARCH__
+    const unsigned t1 = __umulhi(f.m, n);
+#else
+    const unsigned t1 = (unsigned)(((unsigned long long)f.m * n) >> 32);
+#endif
+    return (t1 + ((n - t1) >> f.s1)) >> f.s2;
+}
+
 struct Grid {
     int nx, ny, nz;   // cells (nz == 1 in 2D)
     int dim;          // 2 or 3
@@ -32,6 +61,9 @@ struct Grid {
     int ntx, nty, ntz;
     long long ntiles;
     long long ncell;
+    // divisors of the tile decompositions: ntx (32-wide cell tiles), ntx2
+    // (64-wide pair tiles), nty
+    FastDiv ftx, ftx2, fty;
 };
 
 inline Grid make_grid(int dim, int nx, int ny, int nz) {
@@ -48,6 +80,9 @@ inline Grid make_grid(int dim, int nx, int ny, int nz) {
     g.ntz = (g.nz + g.tz - 1) / g.tz;
     g.ntiles = (long long)g.ntx * g.nty * g.ntz;
     g.ncell = (long long)nx * ny * g.nz;
+    g.ftx = make_fastdiv((unsigned)g.ntx);
+    g.ftx2 = make_fastdiv((unsigned)((nx + 63) / 64));
+    g.fty = make_fastdiv((unsigned)g.nty);
     return g;
 }
 
@@ -94,13 +129,13 @@ __device__ __forceinline__ long long cell_index(const Grid &g, int i, int j, int
     return (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * k);
 }
 
+// Tiles are numbered x fastest, then y, then z (tile counts fit 32 bits).
 __device__ __forceinline__ void tile_origin(const Grid &g, long long t, int &i0, int &j0, int &k0) {
-    long long tx = t % g.ntx;
-    long long r = t / g.ntx;
-    long long ty = r % g.nty;
-    long long tk = r / g.nty;
-    i0 = (int)tx * TILE_X;
-    j0 = (int)ty * TILE_Y;
+    const unsigned tt = (unsigned)t;
+    const unsigned r = fdiv(tt, g.ftx);
+    const unsigned tk = fdiv(r, g.fty);
+    i0 = (int)(tt - r * (unsigned)g.ntx) * TILE_X;
+    j0 = (int)(r - tk * (unsigned)g.nty) * TILE_Y;
     k0 = (int)tk * g.tz;
 }
 

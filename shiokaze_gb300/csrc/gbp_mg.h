@@ -38,9 +38,10 @@ template <class T> void mg_plan_tail(MgHierarchy<T> &H) {
     size_t bytes = 0;
     int tail = H.nlevels;
     for (int l = H.nlevels - 1; l >= 1; --l) {
-        // 7 arrays per level, plus an FP64 iterate of the coarsest level
+        // 7 arrays per level, plus on the coarsest level its FP64 iterate,
+        // right-hand side, inverse diagonal and couplings
         const size_t need = bytes + 7 * sizeof(T) * (size_t)H.levels[l].g.ncell +
-                            (l == H.nlevels - 1 ? 16 + 8 * (size_t)H.levels[l].g.ncell : 0);
+                            (l == H.nlevels - 1 ? 16 + 6 * 8 * (size_t)H.levels[l].g.ncell : 0);
         if (need > MG_TAIL_SMEM_MAX) break;
         bytes = need;
         tail = l;

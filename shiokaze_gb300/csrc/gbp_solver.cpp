@@ -14,6 +14,8 @@
 //                              r64 = b - A64 x64 (outer stop)] x chunk
 #include "gbp_solver.h"
 
+#include <cstdint>
+
 #include <algorithm>
 #include <cstring>
 #include <functional>
@@ -316,7 +318,24 @@ template <class T> void Solver::add_to_plan(BatchPlan<T> &plan, const gbp_params
     const int base = (int)plan.levels.size();
     for (int l = 0; l < G; ++l) {
         const MgLevel<T> &F = H.levels[l], &C = H.levels[l + 1];
-        plan.levels.push_back(BLevel<T>{F.g, F.diag, F.inv, F.cx, F.cy, F.cz, F.b, F.x, C.x, C.b, C.g, s});
+        // 2-wide accesses need an even row length and 2-element alignment of
+        // every array that moves in pairs (on level 0 also the scene's
+        // vectors and FP64 operator and refinement arrays)
+        auto al = [](const void *ptr, size_t bytes) { return ptr == nullptr || (uintptr_t)ptr % bytes == 0; };
+        bool vec = F.g.nx % 2 == 0;
+        for (const void *ptr : {(const void *)F.diag, (const void *)F.inv, (const void *)F.cx, (const void *)F.cy,
+                                (const void *)F.cz, (const void *)F.b, (const void *)F.x})
+            vec = vec && al(ptr, 2 * sizeof(T));
+        if (l == 0) {
+            for (const void *ptr : {(const void *)sc.x, (const void *)sc.r, (const void *)sc.z, (const void *)sc.p,
+                                    (const void *)sc.q})
+                vec = vec && al(ptr, 2 * sizeof(T));
+            for (const void *ptr : {(const void *)sc.A.diag, (const void *)sc.A.cx, (const void *)sc.A.cy,
+                                    (const void *)sc.A.cz, (const void *)sc.b, (const void *)sc.prev,
+                                    (const void *)sc.x64, (const void *)sc.r64})
+                vec = vec && al(ptr, 2 * sizeof(double));
+        }
+        plan.levels.push_back(BLevel<T>{F.g, F.diag, F.inv, F.cx, F.cy, F.cz, F.b, F.x, C.x, C.b, C.g, s, vec ? 1 : 0});
         plan.scene_of.push_back(s);
         auto add = [&](std::vector<BSeg> &list, int &items, long long tiles, long long cells_per_tile) {
             const int m = (int)std::max(1LL, BITEM_CELLS / cells_per_tile);
@@ -327,10 +346,7 @@ template <class T> void Solver::add_to_plan(BatchPlan<T> &plan, const gbp_params
         add(plan.pair[l], plan.n_pair[l], pair_tiles(F.g), 64LL * TILE_Y * F.g.tz);
         // a restriction item's work is its 8x as many fine cells
         add(plan.restrict_[l], plan.n_restrict[l], cell_tiles(C.g), 8LL * TILE_X * TILE_Y * C.g.tz);
-        if (l == 0) {
-            add(plan.fine_cells, plan.n_fine_cells, cell_tiles(F.g), (long long)TILE_X * TILE_Y * F.g.tz);
-            add(plan.fine_pairs, plan.n_fine_pairs, pair_tiles(F.g), 64LL * TILE_Y * F.g.tz);
-        }
+        if (l == 0) add(plan.fine_pairs, plan.n_fine_pairs, pair_tiles(F.g), 64LL * TILE_Y * F.g.tz);
     }
     BTail<T> tail{};
     tail.nt = H.nlevels - G;
