@@ -234,10 +234,9 @@ __device__ __forceinline__ void reduce_items(const BSeg *__restrict__ segs, int 
     Acc acc;
     acc.reset();
     auto flush = [&]() {
-        const double v = acc.block(sh);
         const int B = gridDim.x;
         const int slot = (int)((((long long)blockIdx.x - first.begin) % B + B) % B);
-        if (threadIdx.x == 0) part[first.begin + slot] = v;
+        acc.store(sh, part, first.begin + slot, n);
         finish(first, min(first.count, B));
     };
     int sgc = 0;
@@ -263,12 +262,18 @@ __device__ __forceinline__ void reduce_items(const BSeg *__restrict__ segs, int 
 // FP32 path then issues no FP64 instruction per cell (the FP64 pipe of this
 // GPU runs at a small fraction of its FP32 rate). It assumes |a b| stays
 // inside the FP32 range, as the FP32 inner solve does for its vectors.
+// store() publishes the block's partial(s) at slot idx of the list's
+// partials (a second partial, if any, at n + idx).
 template <class T> struct DotAcc;
 template <> struct DotAcc<double> {
     double v;
     __device__ void reset() { v = 0.0; }
     __device__ void add(double a, double b) { v = fma(a, b, v); }
     __device__ double block(double *sh) { return block_sum(v, sh); }
+    __device__ void store(double *sh, double *part, int idx, int) {
+        const double b = block(sh);
+        if (threadIdx.x == 0) part[idx] = b;
+    }
 };
 template <> struct DotAcc<float> {
     float hi, lo;
@@ -284,6 +289,10 @@ template <> struct DotAcc<float> {
         lo = __fsub_rn(t, __fsub_rn(hi, s));
     }
     __device__ double block(double *sh) { return block_sum((double)hi + (double)lo, sh); }
+    __device__ void store(double *sh, double *part, int idx, int) {
+        const double b = block(sh);
+        if (threadIdx.x == 0) part[idx] = b;
+    }
 };
 // max |x|: exact in either type; FP32 converts once per flush. NaN terms
 // are ignored here (fmax), as before; NaN is caught through alpha.
@@ -292,6 +301,28 @@ template <class T> struct MaxAcc {
     __device__ void reset() { v = T(0); }
     __device__ void add(T x) { v = fmax(v, fabs(x)); }
     __device__ double block(double *sh) { return block_max((double)v, sh); }
+    __device__ void store(double *sh, double *part, int idx, int) {
+        const double b = block(sh);
+        if (threadIdx.x == 0) part[idx] = b;
+    }
+};
+// max |x| and sum x^2 in FP64 (the refinement residual); partials at idx
+// and n + idx.
+struct MaxSumAcc {
+    double m, s;
+    __device__ void reset() { m = s = 0.0; }
+    __device__ void add(double x) {
+        m = fmax(m, fabs(x));
+        s = fma(x, x, s);
+    }
+    __device__ void store(double *sh, double *part, int idx, int n) {
+        const double bm = block_max(m, sh);
+        const double bs = block_sum(s, sh);
+        if (threadIdx.x == 0) {
+            part[idx] = bm;
+            part[n + idx] = bs;
+        }
+    }
 };
 
 // ---- smoothing and transfers on the global-memory levels --------------------------
@@ -875,11 +906,13 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
     }
 }
 
-// r64 = b - A64 (prev + x64) (x64 absent: initial), r_T = r64, |r64|_inf;
-// the scene's last flush applies the stopping rule and opens the next inner
-// solve. initial: sets the threshold, zeroes x64. Each cell's residual is
-// accumulated as diag X minus the neighbour terms one by one (-x, +x, -y,
-// +y, -z, +z), in FP64.
+// r64 = b - A64 (prev + x64) (x64 absent: initial), r_T = r64, |r64|_inf
+// and |r64|_2; the scene's last flush applies the stopping rule and opens
+// the next inner solve. initial: sets the threshold, zeroes x64, and keeps
+// |b - A prev|_2 (with no warm start that is b itself, and the stencil is
+// skipped). The last pass's norms are the true residual of the returned
+// solution. Each cell's residual is accumulated as diag X minus the
+// neighbour terms one by one (-x, +x, -y, +y, -z, +z), in FP64.
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_residual_kernel(
     const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
@@ -888,9 +921,9 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_res
     if (!initial && *(const volatile int *)&cnt->refine <= 0) return;
     __shared__ double shf[BLOCK_THREADS / 32];
     __shared__ ItemCtx<T> ctx;
-    reduce_items<T, MaxAcc<double>>(
+    reduce_items<T, MaxSumAcc>(
         segs, nseg, n, part, levels, scenes, initial ? -1 : 2, ctx,
-        [&](const BItem &it, MaxAcc<double> &acc) {
+        [&](const BItem &it, MaxSumAcc &acc) {
             const BLevel<T> &L = ctx.L;
             const BScene<T> &S = ctx.S;
             const Grid &g = L.g;
@@ -913,7 +946,17 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_res
                     if (S.prev) v += __ldg(S.prev + m);
                     return v;
                 };
+                const bool zero_x = initial && S.prev == nullptr;  // r = b exactly
                 pair_tile(g, it, [&](int i, int j, int k, long long c, bool second) {
+                    if (zero_x) {
+                        const Pair<double> rv = ld2<double, V>(S.b, c, second);
+                        st2<double, V>(S.r64, c, rv, second);
+                        st2<T, V>(S.r, c, Pair<T>{T(rv.a), T(rv.b)}, second);
+                        acc.add(rv.a);
+                        if (second) acc.add(rv.b);
+                        st2<double, V>(S.x64, c, Pair<double>{0.0, 0.0}, second);
+                        return;
+                    }
                     const Pair<double> xc = X2(c, second), dg = ld2<double, V>(A.diag, c, second);
                     const Pair<double> cxp = ld2<double, V>(A.cx, c, second);
                     double a0 = dg.a * xc.a, a1 = dg.b * xc.b;
@@ -959,7 +1002,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_res
             Scalars *sc = ctx.S.sc;
             if (item_last(&sc->counter[SITE_REFINE], flushes)) {
                 const double res = max_range(part, it.begin, flushes, shf);
+                const double ss = sum_range(part + n, it.begin, flushes, shf);
                 if (threadIdx.x == 0) {
+                    sc->aux[0] = res;
+                    sc->aux[1] = sqrt(ss);
+                    if (initial) sc->aux[2] = sqrt(ss);
                     if (initial) {
                         const double tolf = residual < 1e-30 ? 1e-30 : residual;
                         sc->res0 = res;

@@ -105,7 +105,8 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
     n_fine_pairs_ = plan.n_fine_pairs;
     void *d;
     max_items_ = (int)max_items;
-    if ((rc = upload(nullptr, sizeof(double) * (max_items + 1), &d))) return rc;
+    // two partials per item (the refinement keeps a max and a sum)
+    if ((rc = upload(nullptr, sizeof(double) * 2 * (max_items + 1), &d))) return rc;
     d_part_ = static_cast<double *>(d);
     if ((rc = upload(nullptr, sizeof(BatchCounters), &d))) return rc;
     d_counters_ = static_cast<BatchCounters *>(d);

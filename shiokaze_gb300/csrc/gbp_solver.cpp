@@ -224,10 +224,17 @@ int Solver::solve(const Grid &g, const gbp_params &p, int grid_blocks, cudaStrea
 
 int Solver::complete(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches) {
     const bool warm = p.warm_start && st_.have_prev;
-    Operator<double> A{st_.diag, st_.cx, st_.cy, g.dim == 3 ? st_.cz : st_.cy};
-    SOLVER_CUDA(launch_true_residual(g, A, st_.b, st_.x, warm ? st_.prev : nullptr, st_.sc, st_.pt, grid_blocks,
-                                     stream));
-    *launches += 1;
+    // A mixed MGPCG solve that stopped on its FP64 refinement check has the
+    // true residual of its solution already (that check computes it); every
+    // other solve gets a separate FP64 pass.
+    const bool have_true = p.solver == GBP_SOLVER_MGPCG && p.precision == GBP_PRECISION_MIXED &&
+                           (st_.host_sc->status == 1 || st_.host_sc->status == 2);
+    if (!have_true) {
+        Operator<double> A{st_.diag, st_.cx, st_.cy, g.dim == 3 ? st_.cz : st_.cy};
+        SOLVER_CUDA(launch_true_residual(g, A, st_.b, st_.x, warm ? st_.prev : nullptr, st_.sc, st_.pt, grid_blocks,
+                                         stream));
+        *launches += 1;
+    }
     last_inner_total_ = st_.host_sc->iter;
     last_outer_ = p.precision == GBP_PRECISION_MIXED ? st_.host_sc->outer_iter : 1;
     last_precision_ = p.precision;
