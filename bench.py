@@ -290,9 +290,8 @@ def run_gbp(args):
     # roofline: the path's fine-level kernels timed alone, each launched once
     # per iteration; the slowest is the dominant one
     if args.solver == "mgpcg":
-        kernels = {10: "mg_presmooth_kernel", 12: "mg_restrict_kernel", 13: "mg_post_black_kernel",
-                   14: "mg_red_dot_kernel", 15: "pcg_direction_kernel", 16: "pcg_spmv_kernel",
-                   17: "pcg_update_kernel"}
+        kernels = {10: "presmooth_kernel", 12: "restrict_kernel", 13: "post_black_kernel",
+                   14: "red_dot_kernel", 15: "direction_kernel", 16: "spmv_kernel", 17: "update_kernel"}
     else:
         kernels = {0: "cg_spmv_kernel", 1: "cg_update_kernel", 2: "cg_direction_kernel"}
     timed = {}

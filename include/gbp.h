@@ -137,9 +137,9 @@ int gbp_project_device(gbp_scene *scene, double dt, const float *solid, const fl
  * together. Every kernel of the multigrid-preconditioned CG iteration runs
  * once per iteration for the whole batch, over a work list of tiles of all
  * scenes, and the iterations are replayed from one CUDA graph; each scene
- * stops on its own stopping rule, and a scene's result does not depend on
- * the other scenes in the batch (reductions are per scene, in a fixed
- * order). Replaces a loop of macpressuresolver3::project calls over
+ * stops on its own stopping rule, and its reductions are its own (per
+ * scene, in a fixed order for a given batch): its result matches its
+ * single-scene solve up to the grouping of its dot-product partials. Replaces a loop of macpressuresolver3::project calls over
  * independent scenes. Scenes belong to `ctx`; the batch refers to them (it
  * does not own them) and keeps their per-scene state (warm start, volume
  * correction). params->solver must be GBP_SOLVER_MGPCG. */

@@ -42,6 +42,7 @@ class Request:
     edge: int
     steps: int = 50
     seed: int = 0
+    scene: object = None    # the request's input arrays (made by make_scene if absent)
 
 
 @dataclass
@@ -76,6 +77,8 @@ def poisson_requests(n: int, rate: float, seed: int = 5, edges=(32, 64, 96, 128,
 
 
 def make_scene(req: Request):
+    if req.scene is not None:
+        return req.scene
     if req.kind == "liquid":
         return scn.liquid3(req.edge, seed=req.seed)
     return scn.smoke3(req.edge, seed=req.seed)
@@ -188,7 +191,11 @@ class ProjectionServer:
     # ---- the request loop ------------------------------------------------------------
     def serve(self, requests: list[Request], time_scale: float = 1.0):
         """Runs until every request is done; arrivals are replayed in real
-        time (scaled). Returns per-request records and the server stats."""
+        time (scaled). A request's input arrays exist when it arrives: the
+        synthetic ones are made before the clock starts. Returns per-request
+        records and the server stats."""
+        for r in requests:
+            r.scene = make_scene(r)
         pending = [(r.arrival * time_scale, r.rid, r) for r in requests]
         heapq.heapify(pending)
         waiting: list[Request] = []
