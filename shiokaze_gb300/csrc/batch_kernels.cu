@@ -330,11 +330,8 @@ struct MaxSumAcc {
 // First pre-smoothing pass from x = 0: red x = b / diag, then black from the
 // red neighbours (computed on the fly as b inv), both written.
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
-    presmooth_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
-                     const BScene<T> *__restrict__ scenes, int gate, const BatchCounters *live) {
-    if (batch_idle(live)) return;
-    __shared__ ItemCtx<T> ctx;
+__device__ __forceinline__ void presmooth_items(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg,
+        int n, const BScene<T> *__restrict__ scenes, int gate, ItemCtx<T> &ctx) {
     int cur = -1;
     int sgc = 0;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
@@ -368,14 +365,20 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
     }
 }
 
+template <class T>
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    presmooth_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                  const BScene<T> *__restrict__ scenes, int gate, const BatchCounters *live) {
+    if (batch_idle(live)) return;
+    __shared__ ItemCtx<T> ctx;
+    presmooth_items<T>(levels, segs, nseg, n, scenes, gate, ctx);
+}
+
 // One colour of a Gauss-Seidel sweep (extra smoothing sweeps, and the final
 // red pass of the post-smoothing on coarse levels).
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
-    sweep_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
-                 const BScene<T> *__restrict__ scenes, int gate, int color, const BatchCounters *live) {
-    if (batch_idle(live)) return;
-    __shared__ ItemCtx<T> ctx;
+__device__ __forceinline__ void sweep_items(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg,
+        int n, const BScene<T> *__restrict__ scenes, int gate, int color, ItemCtx<T> &ctx) {
     int cur = -1;
     int sgc = 0;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
@@ -399,15 +402,21 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
     }
 }
 
+template <class T>
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    sweep_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                  const BScene<T> *__restrict__ scenes, int gate, int color, const BatchCounters *live) {
+    if (batch_idle(live)) return;
+    __shared__ ItemCtx<T> ctx;
+    sweep_items<T>(levels, segs, nseg, n, scenes, gate, color, ctx);
+}
+
 // Items are cell tiles of the coarse grid gc; a thread sums the residuals
 // b - A x of the (up to) 8 children of its coarse cell, child pairs
 // (2I, 2I+1) in order of (z, y).
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
-    restrict_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
-                    const BScene<T> *__restrict__ scenes, int gate, const BatchCounters *live) {
-    if (batch_idle(live)) return;
-    __shared__ ItemCtx<T> ctx;
+__device__ __forceinline__ void restrict_items(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg,
+        int n, const BScene<T> *__restrict__ scenes, int gate, ItemCtx<T> &ctx) {
     int cur = -1;
     int sgc = 0;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
@@ -442,15 +451,21 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
     }
 }
 
+template <class T>
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    restrict_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                  const BScene<T> *__restrict__ scenes, int gate, const BatchCounters *live) {
+    if (batch_idle(live)) return;
+    __shared__ ItemCtx<T> ctx;
+    restrict_items<T>(levels, segs, nseg, n, scenes, gate, ctx);
+}
+
 // Prolongation fused with the black half of the post-smoothing: black cells
 // from their red neighbours plus alpha times the neighbour's parent value.
 // The two cells of a pair (i even) share their parent.
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
-    post_black_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
-                      const BScene<T> *__restrict__ scenes, int gate, T alpha, const BatchCounters *live) {
-    if (batch_idle(live)) return;
-    __shared__ ItemCtx<T> ctx;
+__device__ __forceinline__ void post_black_items(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg,
+        int n, const BScene<T> *__restrict__ scenes, int gate, T alpha, ItemCtx<T> &ctx) {
     int cur = -1;
     int sgc = 0;
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
@@ -486,6 +501,94 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
                 L.x[ch] = (__ldg(L.b + ch) + sh) * __ldg(L.inv + ch);
             });
         });
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    post_black_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                  const BScene<T> *__restrict__ scenes, int gate, T alpha, const BatchCounters *live) {
+    if (batch_idle(live)) return;
+    __shared__ ItemCtx<T> ctx;
+    post_black_items<T>(levels, segs, nseg, n, scenes, gate, alpha, ctx);
+}
+
+// ---- coarse levels in two cooperative launches -------------------------------------
+
+// Grid-wide barrier of a cooperative launch (every block resident): arrivals
+// counted on cnt->bar_count, release by a bump of cnt->bar_gen, which each
+// block reads before it arrives. The wait is bounded (about a second); a
+// block whose wait runs out records cnt->bar_err and leaves the kernel, the
+// others run out the same way, and the host reports the error.
+__device__ __forceinline__ bool grid_barrier(BatchCounters *cnt) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = &cnt->bar_gen;
+        const unsigned g = *gen;
+        __threadfence();
+        int good = 1;
+        if (atomicAdd(&cnt->bar_count, 1u) == gridDim.x - 1) {
+            cnt->bar_count = 0;
+            __threadfence();
+            atomicAdd(&cnt->bar_gen, 1u);
+        } else {
+            for (int it = 0; *gen == g; ++it) {
+                if (it > (1 << 24)) {
+                    good = 0;
+                    atomicExch(&cnt->bar_err, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Levels first..last top-down: presmooth, extra sweeps, restriction. The
+// idle test at the start reads a counter no block changes during the
+// launch, so either every block returns there or none does.
+template <class T>
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    coarse_descend_kernel(const BLevel<T> *__restrict__ levels, const CoarseLists cl,
+                          const BScene<T> *__restrict__ scenes, int gate, MgSettings ms, BatchCounters *cnt) {
+    if (batch_idle(cnt)) return;
+    __shared__ ItemCtx<T> ctx;
+    for (int l = cl.first; l <= cl.last; ++l) {
+        presmooth_items<T>(levels, cl.pair[l], cl.pair_seg[l], cl.pair_n[l], scenes, gate, ctx);
+        if (!grid_barrier(cnt)) return;
+        for (int sw = 1; sw < ms.smooth; ++sw)
+            for (int color = 0; color < 2; ++color) {
+                sweep_items<T>(levels, cl.pair[l], cl.pair_seg[l], cl.pair_n[l], scenes, gate, color, ctx);
+                if (!grid_barrier(cnt)) return;
+            }
+        restrict_items<T>(levels, cl.restr[l], cl.restr_seg[l], cl.restr_n[l], scenes, gate, ctx);
+        if (l < cl.last && !grid_barrier(cnt)) return;
+    }
+}
+
+// Levels last..first bottom-up: prolongation with the black sweep, extra
+// sweeps, the red sweep.
+template <class T>
+__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+    coarse_ascend_kernel(const BLevel<T> *__restrict__ levels, const CoarseLists cl,
+                         const BScene<T> *__restrict__ scenes, int gate, MgSettings ms, T alpha, BatchCounters *cnt) {
+    if (batch_idle(cnt)) return;
+    __shared__ ItemCtx<T> ctx;
+    for (int l = cl.last; l >= cl.first; --l) {
+        post_black_items<T>(levels, cl.pair[l], cl.pair_seg[l], cl.pair_n[l], scenes, gate, alpha, ctx);
+        if (!grid_barrier(cnt)) return;
+        for (int sw = 1; sw < ms.smooth; ++sw)
+            for (int color = 0; color < 2; ++color) {
+                sweep_items<T>(levels, cl.pair[l], cl.pair_seg[l], cl.pair_n[l], scenes, gate, color, ctx);
+                if (!grid_barrier(cnt)) return;
+            }
+        sweep_items<T>(levels, cl.pair[l], cl.pair_seg[l], cl.pair_n[l], scenes, gate, 0, ctx);
+        if (l > cl.first && !grid_barrier(cnt)) return;
     }
 }
 
@@ -552,34 +655,54 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
 // copy per block, read as broadcasts).
 template <class T> struct SLevel {
     int nx, ny, nz, dim, n;
-    FastDiv fx, fxy;  // nx and nx ny, to split cell indices
+    int hx;             // pair slots per row, (nx + 1) / 2
+    FastDiv fhx, fhxy;  // hx and hx ny, to split pair-slot indices
     T *b, *x, *inv, *diag, *cx, *cy, *cz;
 };
 
+// Neighbour sum of cell (i, j, k) = c, in the order -x, +x, -y, +y, -z,
+// +z; xat(m, i', j', k') is the value at neighbour m = (i', j', k').
 template <class T, class X>
 __device__ __forceinline__ T snb(const SLevel<T> &L, int i, int j, int k, int c, X xat) {
     const int sy = L.nx, sz = L.nx * L.ny;
     T s = T(0);
-    if (i > 0) s += L.cx[c - 1] * xat(c - 1);
-    if (i + 1 < L.nx) s += L.cx[c] * xat(c + 1);
-    if (j > 0) s += L.cy[c - sy] * xat(c - sy);
-    if (j + 1 < L.ny) s += L.cy[c] * xat(c + sy);
+    if (i > 0) s += L.cx[c - 1] * xat(c - 1, i - 1, j, k);
+    if (i + 1 < L.nx) s += L.cx[c] * xat(c + 1, i + 1, j, k);
+    if (j > 0) s += L.cy[c - sy] * xat(c - sy, i, j - 1, k);
+    if (j + 1 < L.ny) s += L.cy[c] * xat(c + sy, i, j + 1, k);
     if (L.dim == 3) {
-        if (k > 0) s += L.cz[c - sz] * xat(c - sz);
-        if (k + 1 < L.nz) s += L.cz[c] * xat(c + sz);
+        if (k > 0) s += L.cz[c - sz] * xat(c - sz, i, j, k - 1);
+        if (k + 1 < L.nz) s += L.cz[c] * xat(c + sz, i, j, k + 1);
     }
     return s;
 }
 
-template <class T, class F> __device__ __forceinline__ void s_for_each(const SLevel<T> &L, F f) {
-    for (int c = threadIdx.x; c < L.n; c += blockDim.x) {
-        const int t = (int)fdiv((unsigned)c, L.fx), k = (int)fdiv((unsigned)c, L.fxy);
-        const int i = c - t * L.nx, j = t - k * L.ny;
-        f(i, j, k, c);
+// Thread mapping of the tail: pair slots (2 ip, j, k), ip < hx. A pass that
+// updates one colour gives each thread the slot's cell of that colour
+// (i = 2 ip + ((j + k + color) & 1)), so no thread idles on the other
+// colour; a pass over every cell gives it both cells of the slot.
+template <class T, class F> __device__ __forceinline__ void s_for_color(const SLevel<T> &L, int color, F f) {
+    const int slots = L.hx * L.ny * L.nz;
+    for (int p = threadIdx.x; p < slots; p += blockDim.x) {
+        const int t = (int)fdiv((unsigned)p, L.fhx), k = (int)fdiv((unsigned)p, L.fhxy);
+        const int j = t - k * L.ny;
+        const int i = 2 * (p - t * L.hx) + ((j + k + color) & 1);
+        if (i < L.nx) f(i, j, k, i + L.nx * (j + L.ny * k));
     }
     __syncthreads();
 }
-
+template <class T, class F> __device__ __forceinline__ void s_for_cells(const SLevel<T> &L, F f) {
+    const int slots = L.hx * L.ny * L.nz;
+    for (int p = threadIdx.x; p < slots; p += blockDim.x) {
+        const int t = (int)fdiv((unsigned)p, L.fhx), k = (int)fdiv((unsigned)p, L.fhxy);
+        const int j = t - k * L.ny;
+        const int i = 2 * (p - t * L.hx);
+        const int c = i + L.nx * (j + L.ny * k);
+        f(i, j, k, c);
+        if (i + 1 < L.nx) f(i + 1, j, k, c + 1);
+    }
+    __syncthreads();
+}
 // The V-cycle of the levels lv[0..nt) from shared memory: b of lv[0] in,
 // x of lv[0] out, same smoother, transfers and coarsest solve (FP64
 // symmetric sweep pairs, with the coarsest operator and right-hand side
@@ -607,8 +730,9 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
             L.nz = g.nz;
             L.dim = g.dim;
             L.n = (int)g.ncell;
-            L.fx = make_fastdiv((unsigned)g.nx);
-            L.fxy = make_fastdiv((unsigned)(g.nx * g.ny));
+            L.hx = (g.nx + 1) / 2;
+            L.fhx = make_fastdiv((unsigned)L.hx);
+            L.fhxy = make_fastdiv((unsigned)(L.hx * g.ny));
             T **arr[7] = {&L.b, &L.x, &L.inv, &L.diag, &L.cx, &L.cy, &L.cz};
             for (int a = 0; a < 7; ++a) {
                 *arr[a] = base + off;
@@ -636,22 +760,22 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
     const T alpha = T(ms.alpha);
     for (int l = 0; l + 1 < A.nt; ++l) {
         const SLevel<T> &L = S[l];
-        s_for_each(L, [&](int i, int j, int k, int c) {
+        s_for_cells(L, [&](int i, int j, int k, int c) {
             const T inv = L.inv[c];
             if (((i + j + k) & 1) == 0) {
                 L.x[c] = L.b[c] * inv;
             } else {
-                L.x[c] = (L.b[c] + snb(L, i, j, k, c, [&](int m) { return L.b[m] * L.inv[m]; })) * inv;
+                L.x[c] = (L.b[c] + snb(L, i, j, k, c, [&](int m, int, int, int) { return L.b[m] * L.inv[m]; })) *
+                         inv;
             }
         });
         for (int sw = 1; sw < ms.smooth; ++sw)
             for (int color = 0; color < 2; ++color)
-                s_for_each(L, [&](int i, int j, int k, int c) {
-                    if (((i + j + k) & 1) != color) return;
-                    L.x[c] = (L.b[c] + snb(L, i, j, k, c, [&](int m) { return L.x[m]; })) * L.inv[c];
+                s_for_color(L, color, [&](int i, int j, int k, int c) {
+                    L.x[c] = (L.b[c] + snb(L, i, j, k, c, [&](int m, int, int, int) { return L.x[m]; })) * L.inv[c];
                 });
         const SLevel<T> &C = S[l + 1];
-        s_for_each(C, [&](int I, int J, int K, int cc) {
+        s_for_cells(C, [&](int I, int J, int K, int cc) {
             T sum = T(0);
             const int kmax = L.dim == 3 ? 2 : 1;
             for (int c2 = 0; c2 < kmax; ++c2)
@@ -660,7 +784,8 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
                         const int i = 2 * I + a2, j = 2 * J + b2, k = 2 * K + c2;
                         if (i >= L.nx || j >= L.ny || k >= L.nz) continue;
                         const int f = i + L.nx * (j + L.ny * k);
-                        sum += L.b[f] - (L.diag[f] * L.x[f] - snb(L, i, j, k, f, [&](int m) { return L.x[m]; }));
+                        sum += L.b[f] -
+                               (L.diag[f] * L.x[f] - snb(L, i, j, k, f, [&](int m, int, int, int) { return L.x[m]; }));
                     }
             C.b[cc] = sum;
         });
@@ -681,8 +806,7 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
         for (int p = 0; p < ms.coarsest_pairs; ++p) {
             const int order[4] = {0, 1, 1, 0};
             for (int q = 0; q < 4; ++q)
-                s_for_each(L, [&](int i, int j, int k, int c) {
-                    if (((i + j + k) & 1) != order[q]) return;
+                s_for_color(L, order[q], [&](int i, int j, int k, int c) {
                     double acc = 0.0;
                     if (i > 0) acc += cxd[c - 1] * xc[c - 1];
                     if (i + 1 < L.nx) acc += cxd[c] * xc[c + 1];
@@ -701,24 +825,19 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
     for (int l = A.nt - 2; l >= 0; --l) {
         const SLevel<T> &L = S[l];
         const SLevel<T> &C = S[l + 1];
-        s_for_each(L, [&](int i, int j, int k, int c) {
-            if (((i + j + k) & 1) != 1) return;
-            L.x[c] = (L.b[c] + snb(L, i, j, k, c, [&](int m) {
-                         const int mt = (int)fdiv((unsigned)m, L.fx), mk = (int)fdiv((unsigned)m, L.fxy);
-                         const int mi = m - mt * L.nx, mj = mt - mk * L.ny;
-                         return L.x[m] +
-                                alpha * C.x[(mi >> 1) + C.nx * ((mj >> 1) + C.ny * (L.dim == 3 ? (mk >> 1) : 0))];
+        const bool d3 = L.dim == 3;
+        s_for_color(L, 1, [&](int i, int j, int k, int c) {
+            L.x[c] = (L.b[c] + snb(L, i, j, k, c, [&](int m, int mi, int mj, int mk) {
+                         return L.x[m] + alpha * C.x[(mi >> 1) + C.nx * ((mj >> 1) + C.ny * (d3 ? (mk >> 1) : 0))];
                      })) * L.inv[c];
         });
         for (int sw = 1; sw < ms.smooth; ++sw)
             for (int color = 0; color < 2; ++color)
-                s_for_each(L, [&](int i, int j, int k, int c) {
-                    if (((i + j + k) & 1) != color) return;
-                    L.x[c] = (L.b[c] + snb(L, i, j, k, c, [&](int m) { return L.x[m]; })) * L.inv[c];
+                s_for_color(L, color, [&](int i, int j, int k, int c) {
+                    L.x[c] = (L.b[c] + snb(L, i, j, k, c, [&](int m, int, int, int) { return L.x[m]; })) * L.inv[c];
                 });
-        s_for_each(L, [&](int i, int j, int k, int c) {
-            if (((i + j + k) & 1) != 0) return;
-            L.x[c] = (L.b[c] + snb(L, i, j, k, c, [&](int m) { return L.x[m]; })) * L.inv[c];
+        s_for_color(L, 0, [&](int i, int j, int k, int c) {
+            L.x[c] = (L.b[c] + snb(L, i, j, k, c, [&](int m, int, int, int) { return L.x[m]; })) * L.inv[c];
         });
     }
     const SLevel<T> &L0 = S[0];
@@ -1092,6 +1211,42 @@ template <class T> cudaError_t b_tail_enable(size_t bytes) {
     return cudaFuncSetAttribute(tail_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 template <class T>
+cudaError_t b_coarse_descend(const BLaunch &L, const BLevel<T> *levels, const CoarseLists &cl,
+                             const BScene<T> *scenes, MgSettings ms) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)L.blocks);
+    cfg.blockDim = dim3(BLOCK_THREADS);
+    cfg.stream = L.stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, coarse_descend_kernel<T>, levels, cl, scenes, L.gate, ms, L.cnt);
+}
+template <class T>
+cudaError_t b_coarse_ascend(const BLaunch &L, const BLevel<T> *levels, const CoarseLists &cl,
+                            const BScene<T> *scenes, MgSettings ms, T alpha) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)L.blocks);
+    cfg.blockDim = dim3(BLOCK_THREADS);
+    cfg.stream = L.stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, coarse_ascend_kernel<T>, levels, cl, scenes, L.gate, ms, alpha, L.cnt);
+}
+// resident blocks of the two cooperative kernels on `sms` SMs (the smaller)
+template <class T> int b_coarse_capacity(int sms) {
+    int a = 0, b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, coarse_descend_kernel<T>, BLOCK_THREADS, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, coarse_ascend_kernel<T>, BLOCK_THREADS, 0) != cudaSuccess)
+        return 0;
+    return sms * (a < b ? a : b);
+}
+template <class T>
 cudaError_t b_direction(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                         const BScene<T> *scenes) {
     direction_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, L.cnt);
@@ -1139,6 +1294,11 @@ cudaError_t b_refine_residual(const BLaunch &L, const BLevel<T> *levels, const B
                                       const BScene<T> *, double *);                                                  \
     template cudaError_t b_tail<T>(const BLaunch &, const BTail<T> *, int, const BScene<T> *, MgSettings, size_t);    \
     template cudaError_t b_tail_enable<T>(size_t);                                                                   \
+    template cudaError_t b_coarse_descend<T>(const BLaunch &, const BLevel<T> *, const CoarseLists &,                 \
+                                             const BScene<T> *, MgSettings);                                         \
+    template cudaError_t b_coarse_ascend<T>(const BLaunch &, const BLevel<T> *, const CoarseLists &,                  \
+                                            const BScene<T> *, MgSettings, T);                                       \
+    template int b_coarse_capacity<T>(int);                                                                          \
     template cudaError_t b_direction<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,                 \
                                         const BScene<T> *);                                                          \
     template cudaError_t b_spmv<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *,   \

@@ -103,6 +103,30 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
     }
     if ((rc = segs(plan.fine_pairs, &d_fine_pairs_, &s_fine_pairs_))) return rc;
     n_fine_pairs_ = plan.n_fine_pairs;
+    // coarse global levels 1..max_global-1: one cooperative launch per
+    // V-cycle half, on at most as many blocks as stay resident
+    coarse_ = CoarseLists{};
+    coarse_blocks_ = 0;
+    if (plan.max_global > 1) {
+        coarse_.first = 1;
+        coarse_.last = plan.max_global - 1;
+        int most = 1;
+        for (int l = 1; l < plan.max_global; ++l) {
+            coarse_.pair[l] = d_pair_[l];
+            coarse_.pair_seg[l] = s_pair_[l];
+            coarse_.pair_n[l] = n_pair_[l];
+            coarse_.restr[l] = d_restrict_[l];
+            coarse_.restr_seg[l] = s_restrict_[l];
+            coarse_.restr_n[l] = n_restrict_[l];
+            most = std::max(most, std::max(n_pair_[l], n_restrict_[l]));
+        }
+        int dev = 0, sms = 0;
+        RUN_CUDA(cudaGetDevice(&dev));
+        RUN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const int cap = b_coarse_capacity<T>(sms);
+        if (cap < 1) return fail(GBP_ERR_CUDA, "coarse-level kernels: no resident block");
+        coarse_blocks_ = std::min(cap, most);
+    }
     void *d;
     max_items_ = (int)max_items;
     // two partials per item (the refinement keeps a max and a sum)
@@ -133,8 +157,9 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
     auto *tl = static_cast<const BTail<T> *>(d_tails_);
     cudaError_t e = cudaSuccess;
     auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, gate, d_scene_of_, d_counters_}; };
-    // descend
-    for (int l = 0; l < max_global_ && e == cudaSuccess; ++l) {
+    // descend: the fine level, then the coarse global levels in one launch
+    if (max_global_ > 0) {
+        const int l = 0;
         e = b_presmooth<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc);
         ++*nodes;
         for (int s = 1; s < ms.smooth && e == cudaSuccess; ++s) {
@@ -145,12 +170,22 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
         if (e == cudaSuccess) e = b_restrict<T>(L(n_restrict_[l]), lv, d_restrict_[l], s_restrict_[l], n_restrict_[l], sc);
         ++*nodes;
     }
+    if (e == cudaSuccess && max_global_ > 1) {
+        e = b_coarse_descend<T>(BLaunch{coarse_blocks_, st, gate, d_scene_of_, d_counters_}, lv, coarse_, sc, ms);
+        ++*nodes;
+    }
     if (e == cudaSuccess && tail_smem_ > 0) {
         e = b_tail<T>(BLaunch{nscenes_, st, gate, d_scene_of_, d_counters_}, tl, nscenes_, sc, ms, tail_smem_);
         ++*nodes;
     }
-    // ascend
-    for (int l = max_global_ - 1; l >= 0 && e == cudaSuccess; --l) {
+    // ascend: the coarse global levels in one launch, then the fine level
+    if (e == cudaSuccess && max_global_ > 1) {
+        e = b_coarse_ascend<T>(BLaunch{coarse_blocks_, st, gate, d_scene_of_, d_counters_}, lv, coarse_, sc, ms,
+                               T(ms.alpha));
+        ++*nodes;
+    }
+    if (e == cudaSuccess && max_global_ > 0) {
+        const int l = 0;
         e = b_post_black<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, T(ms.alpha));
         ++*nodes;
         for (int s = 1; s < ms.smooth && e == cudaSuccess; ++s) {
@@ -158,9 +193,7 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
             if (e == cudaSuccess) e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, 1);
             *nodes += 2;
         }
-        if (e != cudaSuccess) break;
-        if (l > 0) e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, 0);
-        else e = b_red_dot<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_);
+        if (e == cudaSuccess) e = b_red_dot<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_);
         ++*nodes;
     }
     // CG on the fine level
@@ -184,8 +217,8 @@ template <class T> int BatchRunner::solve(const gbp_params &p, cudaStream_t st, 
     inner_rel_ = p.inner_tolerance > 0 ? p.inner_tolerance : 1e-3;
     auto *lv = static_cast<const BLevel<T> *>(d_levels_);
     auto *sc = static_cast<const BScene<T> *>(d_scenes_);
+    std::memset(h_counters_, 0, sizeof(BatchCounters));
     h_counters_->remaining = nscenes_;
-    h_counters_->refine = 0;
     RUN_CUDA(cudaMemcpyAsync(d_counters_, h_counters_, sizeof(BatchCounters), cudaMemcpyHostToDevice, st));
     // initial residual of every scene (also zeroes x64, sets thresholds)
     RUN_CUDA(b_refine_residual<T>(BLaunch{blocks_for(n_fine_pairs_, grid_blocks_), st, 0, d_scene_of_, d_counters_}, lv,
@@ -217,6 +250,8 @@ template <class T> int BatchRunner::solve(const gbp_params &p, cudaStream_t st, 
     for (long long k = 0; k < max_chunks; ++k) {
         RUN_CUDA(cudaMemcpyAsync(h_counters_, d_counters_, sizeof(BatchCounters), cudaMemcpyDeviceToHost, st));
         RUN_CUDA(cudaStreamSynchronize(st));
+        if (h_counters_->bar_err)
+            return fail(GBP_ERR_CUDA, "coarse-level kernels: a grid barrier wait ran out (solve abandoned)");
         if (h_counters_->remaining <= 0) return GBP_OK;
         RUN_CUDA(cudaGraphLaunch(graph_, st));
         *launches += graph_nodes_;
@@ -249,8 +284,8 @@ template <class T> int BatchRunner::bench(int which, int reps, cudaStream_t st, 
     }
     if (max_global_ < 1) return fail(GBP_ERR_INVALID_ARGUMENT, "bench: no multigrid level");
     // a live batch, so that no launch takes the idle exit
+    std::memset(h_counters_, 0, sizeof(BatchCounters));
     h_counters_->remaining = nscenes_;
-    h_counters_->refine = 0;
     RUN_CUDA(cudaMemcpyAsync(d_counters_, h_counters_, sizeof(BatchCounters), cudaMemcpyHostToDevice, st));
     cudaEvent_t e0, e1;
     RUN_CUDA(cudaEventCreate(&e0));

@@ -110,9 +110,22 @@ inline long long pair_tiles(const Grid &g) { return (long long)((g.nx + 63) / 64
 inline long long cell_tiles(const Grid &g) { return g.ntiles; }
 
 struct BatchCounters {
-    int remaining;  // scenes not done
-    int refine;     // scenes whose inner solve ended, awaiting refinement
-    int pad[2];
+    int remaining;        // scenes not done
+    int refine;           // scenes whose inner solve ended, awaiting refinement
+    unsigned bar_count;   // grid barrier of the coarse-level kernels: arrivals
+    unsigned bar_gen;     // ... and generation
+    int bar_err;          // a barrier wait ran out (the solve is abandoned)
+    int pad[3];
+};
+
+// Work lists of the global coarse levels [first, last] (first >= 1), run by
+// one cooperative launch per V-cycle half.
+struct CoarseLists {
+    int first, last;
+    const BSeg *pair[MG_MAX_LEVELS];
+    int pair_seg[MG_MAX_LEVELS], pair_n[MG_MAX_LEVELS];
+    const BSeg *restr[MG_MAX_LEVELS];
+    int restr_seg[MG_MAX_LEVELS], restr_n[MG_MAX_LEVELS];
 };
 
 // Device tables and work lists of one batch, built on the host.
@@ -178,6 +191,8 @@ private:
     double *d_part_ = nullptr;  // 3 x max items
     int max_items_ = 0;
     BatchCounters *d_counters_ = nullptr, *h_counters_ = nullptr;
+    CoarseLists coarse_{};
+    int coarse_blocks_ = 0;
     cudaGraphExec_t graph_ = nullptr;
     long long graph_key_ = -1;
     long long graph_nodes_ = 0;
@@ -212,6 +227,17 @@ template <class T>
 cudaError_t b_tail(const BLaunch &L, const BTail<T> *tails, int nscenes, const BScene<T> *scenes, MgSettings ms,
                    size_t smem);
 template <class T> cudaError_t b_tail_enable(size_t bytes);
+// The coarse levels' descent (presmooth, sweeps, restrict per level) and
+// ascent (post_black, sweeps, red sweep per level) as cooperative launches
+// with grid barriers between passes; L.blocks must not exceed
+// b_coarse_capacity (every block resident).
+template <class T>
+cudaError_t b_coarse_descend(const BLaunch &L, const BLevel<T> *levels, const CoarseLists &cl,
+                             const BScene<T> *scenes, MgSettings ms);
+template <class T>
+cudaError_t b_coarse_ascend(const BLaunch &L, const BLevel<T> *levels, const CoarseLists &cl,
+                            const BScene<T> *scenes, MgSettings ms, T alpha);
+template <class T> int b_coarse_capacity(int sms);
 template <class T>
 cudaError_t b_direction(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                         const BScene<T> *scenes);
