@@ -84,6 +84,8 @@ typedef struct gbp_params {
     int mg_coarsest;        /* coarsen while any edge exceeds this (default 8) */
     double inner_tolerance; /* MIXED: relative residual of each inner solve (default 1e-3) */
     int iterations_per_sync;/* CG iterations between host checks of convergence (default 16) */
+    double surface_tension; /* the surface_tension argument of macproject3_interface::project
+                               (macpressuresolver3.cpp:85-115); 0 (default) leaves the velocity as is */
 } gbp_params;
 
 typedef struct gbp_stats {

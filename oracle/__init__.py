@@ -57,7 +57,7 @@ class _Params(ctypes.Structure):
     _fields_ = [("residual", ctypes.c_double), ("max_iterations", ctypes.c_int), ("warm_start", ctypes.c_int),
                 ("eps_fluid", ctypes.c_double), ("eps_solid", ctypes.c_double),
                 ("second_order_fluid", ctypes.c_int), ("second_order_solid", ctypes.c_int),
-                ("gain", ctypes.c_double)]
+                ("gain", ctypes.c_double), ("surface_tension", ctypes.c_double)]
 
 
 class _Stats(ctypes.Structure):
@@ -111,9 +111,9 @@ def _port_lib():
 
 
 def make_params(residual=1e-6, max_iterations=30000, warm_start=False, eps_fluid=1e-2, eps_solid=1e-2,
-                second_order_fluid=True, second_order_solid=True, gain=1.0):
+                second_order_fluid=True, second_order_solid=True, gain=1.0, surface_tension=0.0):
     return _Params(residual, max_iterations, int(warm_start), eps_fluid, eps_solid, int(second_order_fluid),
-                   int(second_order_solid), gain)
+                   int(second_order_solid), gain, surface_tension)
 
 
 class PortProjector:
@@ -176,7 +176,7 @@ def _ref_lib():
         lib.ref_destroy.argtypes = [ctypes.c_void_p]
         lib.ref_project.restype = ctypes.c_double
         lib.ref_project.argtypes = [ctypes.c_void_p, ctypes.c_double, fp, ctypes.c_int, ctypes.c_float, fp,
-                                    ctypes.c_int, ctypes.c_float, fp, fp, fp, fp,
+                                    ctypes.c_int, ctypes.c_float, fp, fp, fp, ctypes.c_double, fp,
                                     ctypes.POINTER(ctypes.c_ubyte), ctypes.c_char_p]
         lib.ref_levelset_roundtrip.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp,
                                                ctypes.c_int, ctypes.c_float, fp]
@@ -191,8 +191,10 @@ class RefProjector:
     """The reference's own macpressuresolver{2,3}, loaded by name."""
 
     def __init__(self, dim, nx, ny, nz, dx, residual=1e-6, max_iterations=30000, warm_start=False, eps_fluid=1e-2,
-                 eps_solid=1e-2, second_order_fluid=True, second_order_solid=True, gain=1.0, threads=None):
+                 eps_solid=1e-2, second_order_fluid=True, second_order_solid=True, gain=1.0, surface_tension=0.0,
+                 threads=None):
         self.lib = _ref_lib()
+        self.surface_tension = float(surface_tension)  # project()'s argument, not a configuration key
         self.dim, self.nx, self.ny, self.nz, self.dx = dim, nx, ny, (nz if dim == 3 else 1), dx
         kv = (f"Residual={residual!r} MaxIterations={max_iterations} WarmStart={'Yes' if warm_start else 'No'} "
               f"EpsFluid={eps_fluid!r} EpsSolid={eps_solid!r} "
@@ -224,8 +226,8 @@ class RefProjector:
         act = np.zeros(fluid.shape, np.uint8)
         open(self._log, "w").close()
         ms = self.lib.ref_project(self.ctx, dt, _ptr(solid), solid_mode, band, _ptr(fluid), fluid_mode, band,
-                                  _ptr(u), _ptr(v), _ptr(w), _ptr(p), _ptr(act, ctypes.c_ubyte),
-                                  self._log.encode())
+                                  _ptr(u), _ptr(v), _ptr(w), self.surface_tension, _ptr(p),
+                                  _ptr(act, ctypes.c_ubyte), self._log.encode())
         with open(self._log, errors="replace") as f:
             log = f.read()
         m = _ITER_RE.findall(log)

@@ -48,6 +48,7 @@ typedef struct {
     int second_order_fluid; /* SecondOrderAccurateFluid */
     int second_order_solid; /* SecondOrderAccurateSolid */
     double gain;            /* Gain (volume correction) */
+    double surface_tension; /* project()'s surface_tension argument (macpressuresolver3.cpp:85-115) */
 } oracle_params;
 
 typedef struct {
@@ -220,6 +221,62 @@ static float rho2(const oracle_ctx *c, const float *fluid, int fluid_exists, int
     }
     if (!prm->second_order_fluid && r) r = 1.0f;
     return r;
+}
+
+/* Curvature of a cell for the surface-tension term (macpressuresolver3.cpp:
+ * 93-101, macpressuresolver2.cpp:79-88): the level set at the clamped
+ * neighbours summed in float (-x, +x, -y, +y[, -z, +z]), minus 6 (4) times the
+ * cell's value in double, over dx^2, stored as float. */
+static float st_curvature(const oracle_ctx *c, const float *fluid, int i, int j, int k) {
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+#define ST_F(a, b, q)                                                                              \
+    fluid[(size_t)((a) < 0 ? 0 : (a) >= nx ? nx - 1 : (a)) +                                       \
+          (size_t)nx * ((size_t)((b) < 0 ? 0 : (b) >= ny ? ny - 1 : (b)) +                         \
+                        (size_t)ny * (size_t)((q) < 0 ? 0 : (q) >= nz ? nz - 1 : (q)))]
+    float s = ST_F(i - 1, j, k) + ST_F(i + 1, j, k);
+    s = s + ST_F(i, j - 1, k);
+    s = s + ST_F(i, j + 1, k);
+    double value;
+    if (c->dim == 3) {
+        s = s + ST_F(i, j, k - 1);
+        s = s + ST_F(i, j, k + 1);
+        value = ((double)s - 6.0 * (double)ST_F(i, j, k)) / (c->dx * c->dx);
+    } else {
+        value = ((double)s - 4.0 * (double)ST_F(i, j, k)) / (c->dx * c->dx);
+    }
+#undef ST_F
+    return (float)value;
+}
+
+/* Surface tension (macpressuresolver3.cpp:103-113, macpressuresolver2.cpp:
+ * 90-103), in place on the face velocities: every face with 0 < rho < 1 gets
+ * -sgn dt/(dx rho) kappa (theta c+ + (1-theta) c-) added, the increment
+ * rounded to float and added in float (array3.h:987-994). */
+static void apply_surface_tension(const oracle_ctx *c, const float *fluid, float *const R[3], float *vel[3],
+                                  double dt, double kappa) {
+    const int nx = c->nx, ny = c->ny, nz = c->nz, dim = c->dim;
+    for (int d = 0; d < dim; ++d) {
+        const int fx = nx + (d == 0), fy = ny + (d == 1), fz = dim == 3 ? nz + (d == 2) : 1;
+        for (int k = 0; k < fz; ++k)
+            for (int j = 0; j < fy; ++j)
+                for (int i = 0; i < fx; ++i) {
+                    const size_t f = (size_t)i + (size_t)fx * ((size_t)j + (size_t)fy * (size_t)k);
+                    const double rho = R[d][f];
+                    if (!(rho && rho < 1.0)) continue;
+                    const int a0 = i >= nx ? nx - 1 : i, a1 = j >= ny ? ny - 1 : j, a2 = k >= nz ? nz - 1 : k;
+                    int b0 = i - (d == 0), b1 = j - (d == 1), b2 = k - (d == 2);
+                    b0 = b0 < 0 ? 0 : b0 >= nx ? nx - 1 : b0;
+                    b1 = b1 < 0 ? 0 : b1 >= ny ? ny - 1 : b1;
+                    b2 = b2 < 0 ? 0 : b2 >= nz ? nz - 1 : b2;
+                    const float fa = fluid[(size_t)a0 + (size_t)nx * ((size_t)a1 + (size_t)ny * (size_t)a2)];
+                    const double sgn = fa < 0.0 ? -1.0 : 1.0;
+                    const double theta = sgn < 0 ? 1.0 - rho : rho;
+                    const double face_c = theta * (double)st_curvature(c, fluid, a0, a1, a2) +
+                                          (1.0 - theta) * (double)st_curvature(c, fluid, b0, b1, b2);
+                    const float inc = (float)(-sgn * dt / (c->dx * rho) * kappa * face_c);
+                    vel[d][f] = vel[d][f] + inc;
+                }
+    }
 }
 
 /* Face fraction arrays for every face: areas[d], rhos[d] sized as the face
@@ -402,6 +459,10 @@ int oracle_project(oracle_ctx *c, double dt, const float *solid, const float *fl
         R[d] = (float *)calloc(nf[d], sizeof(float));
     }
     oracle_face_fractions(c, solid, fluid, prm, A[0], A[1], A[2], R[0], R[1], R[2]);
+    if (prm->surface_tension != 0.0) {
+        float *vel_st[3] = {u, v, w};
+        apply_surface_tension(c, fluid, R, vel_st, dt, prm->surface_tension);
+    }
     int fluid_exists = 0;
     for (size_t n = 0; n < ncell; ++n)
         if (fluid[n] < 0.0f) { fluid_exists = 1; break; }
@@ -587,6 +648,15 @@ int oracle_assemble(oracle_ctx *c, double dt, const float *solid, const float *f
     long long *index = index_out ? index_out : (long long *)malloc(sizeof(long long) * ncell);
     label_cells(c, fluid, A, R, index);
     const float *vel[3] = {u, v, w};
+    float *vel_st[3] = {NULL, NULL, NULL};
+    if (prm->surface_tension != 0.0) {
+        for (int d = 0; d < dim; ++d) {
+            vel_st[d] = (float *)malloc(nf[d] * sizeof(float));
+            memcpy(vel_st[d], vel[d], nf[d] * sizeof(float));
+        }
+        apply_surface_tension(c, fluid, R, vel_st, dt, prm->surface_tension);
+        for (int d = 0; d < dim; ++d) vel[d] = vel_st[d];
+    }
     double *cp[3] = {cpx, cpy, cpz};
     for (size_t cn = 0; cn < ncell; ++cn) {
         diag[cn] = 0.0;
@@ -625,6 +695,7 @@ int oracle_assemble(oracle_ctx *c, double dt, const float *solid, const float *f
     for (int d = 0; d < 3; ++d) {
         free(A[d]);
         free(R[d]);
+        free(vel_st[d]);
     }
     return 0;
 }

@@ -166,10 +166,11 @@ void ref_destroy(void *hp) { delete static_cast<harness *>(hp); }
  *   pressure: cells (out), active: cells, 1 where pressure is active (out).
  * solid_mode/fluid_mode: 0 = narrow-band level set of half-width band,
  * 1 = constant array (value = first element).
+ * surface_tension: project()'s own argument (0 = none).
  * Returns wall-clock milliseconds of project(). */
 double ref_project(void *hp, double dt, const float *solid, int solid_mode, float solid_band,
                    const float *fluid, int fluid_mode, float fluid_band, float *u, float *v, float *w,
-                   float *pressure, unsigned char *active, const char *log_path) {
+                   double surface_tension, float *pressure, unsigned char *active, const char *log_path) {
     auto *h = static_cast<harness *>(hp);
     const int nx = h->nx, ny = h->ny, nz = h->nz;
     double ms = 0.0;
@@ -190,7 +191,7 @@ double ref_project(void *hp, double dt, const float *solid, int solid_mode, floa
         }
         with_stdout_to(log_path, [&]() {
             auto t0 = std::chrono::steady_clock::now();
-            (*h->proj3)->project(dt, vel, solid_a, fluid_a);
+            (*h->proj3)->project(dt, vel, solid_a, fluid_a, surface_tension);
             auto t1 = std::chrono::steady_clock::now();
             ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
         });
@@ -225,7 +226,7 @@ double ref_project(void *hp, double dt, const float *solid, int solid_mode, floa
         }
         with_stdout_to(log_path, [&]() {
             auto t0 = std::chrono::steady_clock::now();
-            (*h->proj2)->project(dt, vel, solid_a, fluid_a);
+            (*h->proj2)->project(dt, vel, solid_a, fluid_a, surface_tension);
             auto t1 = std::chrono::steady_clock::now();
             ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
         });

@@ -13,7 +13,9 @@ Configuration keys are the reference's (``Residual``, ``MaxIterations``,
 ``WarmStart``, ``EpsFluid``, ``EpsSolid``, ``SecondOrderAccurateFluid``,
 ``SecondOrderAccurateSolid``, ``Gain``) plus this module's own
 (``Solver`` = "cg" | "mgpcg", ``Precision`` = "fp64" | "mixed",
-``MGSmooth``, ``MGCoarsest``, ``InnerTolerance``, ``IterationsPerSync``).
+``MGSmooth``, ``MGCoarsest``, ``InnerTolerance``, ``IterationsPerSync``), and
+``SurfaceTension``, the value the reference passes as project()'s
+surface_tension argument.
 
 Arrays may be numpy arrays (host; copied in and out by the call) or torch
 CUDA tensors (device; used in place). There is no CPU fallback: without the
@@ -42,7 +44,7 @@ class Params(ctypes.Structure):
                 ("second_order_fluid", ctypes.c_int), ("second_order_solid", ctypes.c_int),
                 ("gain", ctypes.c_double), ("solver", ctypes.c_int), ("precision", ctypes.c_int),
                 ("mg_smooth", ctypes.c_int), ("mg_coarsest", ctypes.c_int), ("inner_tolerance", ctypes.c_double),
-                ("iterations_per_sync", ctypes.c_int)]
+                ("iterations_per_sync", ctypes.c_int), ("surface_tension", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -131,6 +133,7 @@ _KEYMAP = {
     "SecondOrderAccurateFluid": ("second_order_fluid", int), "SecondOrderAccurateSolid": ("second_order_solid", int),
     "Gain": ("gain", float), "MGSmooth": ("mg_smooth", int), "MGCoarsest": ("mg_coarsest", int),
     "InnerTolerance": ("inner_tolerance", float), "IterationsPerSync": ("iterations_per_sync", int),
+    "SurfaceTension": ("surface_tension", float),
 }
 
 

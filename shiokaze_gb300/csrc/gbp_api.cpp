@@ -90,6 +90,7 @@ void gbp_params_default(gbp_params *p) {
     p->mg_coarsest = 8;
     p->inner_tolerance = 1e-3;
     p->iterations_per_sync = 16;
+    p->surface_tension = 0.0;
 }
 
 const char *gbp_strerror(int status) {
@@ -256,6 +257,10 @@ int project_device(gbp_scene *s, double dt, const float *solid, const float *flu
 
     GBP_CUDA(cudaEventRecord(c->ev[0], stream));
     GBP_CUDA(cudaMemsetAsync(st.sc, 0, sizeof(Scalars), stream));
+    if (p.surface_tension != 0.0) {
+        GBP_CUDA(launch_surface_tension(g, dt, s->dx, sp, p.surface_tension, fluid, u, v, w, c->grid_blocks, stream));
+        c->launches += 1;
+    }
     GBP_CUDA(launch_faces(g, dt, s->dx, sp, solid, fluid, u, v, w, st.faces, c->grid_blocks, stream));
     GBP_CUDA(launch_assemble_faces(g, sp, fluid, st.faces, st.diag, st.cx, st.cy, st.cz, st.b, st.sc,
                                    c->grid_blocks, stream));
@@ -420,6 +425,11 @@ int gbp_batch_project_device(gbp_batch *b, const double *dt, const float *const 
         SetupParams sp{p.eps_solid, p.eps_fluid, p.second_order_solid, p.second_order_fluid, 0.0};
         sp.rhs_correct = volume_correction(s, dt[i], p);
         GBP_CUDA(cudaMemsetAsync(ss.sc, 0, sizeof(Scalars), st));
+        if (p.surface_tension != 0.0) {
+            GBP_CUDA(launch_surface_tension(g, dt[i], s->dx, sp, p.surface_tension, fluid[i], u[i], v[i],
+                                            g.dim == 3 ? w[i] : nullptr, c->grid_blocks, st));
+            launched += 1;
+        }
         GBP_CUDA(launch_faces(g, dt[i], s->dx, sp, solid[i], fluid[i], u[i], v[i], g.dim == 3 ? w[i] : nullptr,
                               ss.faces, c->grid_blocks, st));
         GBP_CUDA(launch_assemble_faces(g, sp, fluid[i], ss.faces, ss.diag, ss.cx, ss.cy, ss.cz, ss.b, ss.sc,
@@ -534,6 +544,9 @@ int gbp_debug_assemble(gbp_scene *s, double dt, const float *solid, const float 
     if (g.dim == 3) GBP_CUDA(cudaMemcpyAsync(s->d_w, w, 4 * n_face(g, 2), cudaMemcpyHostToDevice, str));
     SetupParams sp{p.eps_solid, p.eps_fluid, p.second_order_solid, p.second_order_fluid, 0.0};
     GBP_CUDA(cudaMemsetAsync(st.sc, 0, sizeof(Scalars), str));
+    if (p.surface_tension != 0.0)
+        GBP_CUDA(launch_surface_tension(g, dt, s->dx, sp, p.surface_tension, s->d_fluid, s->d_u, s->d_v, s->d_w,
+                                        s->ctx->grid_blocks, str));
     GBP_CUDA(launch_faces(g, dt, s->dx, sp, s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, st.faces,
                           s->ctx->grid_blocks, str));
     GBP_CUDA(launch_assemble_faces(g, sp, s->d_fluid, st.faces, st.diag, st.cx, st.cy, st.cz, st.b, st.sc,

@@ -28,6 +28,10 @@ struct FaceArrays {
 
 // ---- setup (setup_kernels.cu) ------------------------------------------------
 // Face-first path: faces, then cells; velocity update from the faces.
+// Surface-tension increment of the face velocities, in place (kappa != 0).
+cudaError_t launch_surface_tension(const Grid &g, double dt, double dx, const SetupParams &sp, double kappa,
+                                   const float *fluid, float *u, float *v, float *w, int grid_blocks,
+                                   cudaStream_t stream);
 cudaError_t launch_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
                          const float *fluid, const float *u, const float *v, const float *w, FaceArrays fa,
                          int grid_blocks, cudaStream_t stream);

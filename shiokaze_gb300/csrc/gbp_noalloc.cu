@@ -122,6 +122,8 @@ extern "C" int gbp_project_device_static(int dim, int nx, int ny, int nz, double
     // the scalars block (tickets, flags, counters) must start at zero
     NOALLOC_CUDA(cudaMemsetAsync(sc, 0, sizeof(Scalars), st));
     SetupParams sp{p.eps_solid, p.eps_fluid, p.second_order_solid, p.second_order_fluid, 0.0};
+    if (p.surface_tension != 0.0)
+        NOALLOC_CUDA(launch_surface_tension(g, dt, dx, sp, p.surface_tension, fluid, u, v, w, grid_blocks, st));
     NOALLOC_CUDA(launch_assemble(g, dt, dx, sp, solid, fluid, u, v, w, diag, cx, cy, cz, b, sc, grid_blocks, st));
     Operator<double> A{diag, cx, cy, dim == 3 ? cz : cy};
     NOALLOC_CUDA(launch_cg_init(g, A, b, nullptr, x, r, s, sc, pt, p.residual, p.max_iterations, grid_blocks, st));

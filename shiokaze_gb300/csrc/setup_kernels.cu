@@ -164,6 +164,74 @@ __device__ __forceinline__ long long face_index(const Grid &g, int d, int i, int
     return i + fx * (j + fy * (long long)k);
 }
 
+// Curvature of cell (i, j, k) as the surface-tension term computes it
+// (macpressuresolver3.cpp:93-101, macpressuresolver2.cpp:79-88): the level
+// set at the clamped neighbours summed in float in the order -x, +x, -y,
+// +y[, -z, +z], then minus 6 (4 in 2D) times the cell's value in double,
+// over dx^2, rounded to float as the reference stores it.
+__device__ float st_curvature(const Grid &g, const float *__restrict__ fluid, int i, int j, int k, double dx) {
+    auto F = [&](int a, int b, int c) {
+        a = min(max(a, 0), g.nx - 1);
+        b = min(max(b, 0), g.ny - 1);
+        c = min(max(c, 0), g.nz - 1);
+        return __ldg(fluid + a + (long long)g.nx * (b + (long long)g.ny * c));
+    };
+    float s = F(i - 1, j, k) + F(i + 1, j, k);
+    s = s + F(i, j - 1, k);
+    s = s + F(i, j + 1, k);
+    double value;
+    if (g.dim == 3) {
+        s = s + F(i, j, k - 1);
+        s = s + F(i, j, k + 1);
+        value = ((double)s - 6.0 * (double)F(i, j, k)) / (dx * dx);
+    } else {
+        value = ((double)s - 4.0 * (double)F(i, j, k)) / (dx * dx);
+    }
+    return (float)value;
+}
+
+// Surface tension (macpressuresolver3.cpp:85-115, macpressuresolver2.cpp:
+// 76-105), in place on the face velocities before anything reads them:
+// every face with 0 < rho < 1 gets -sgn dt/(dx rho) kappa face_c added, sgn
+// the sign of the level set on the face's + side, theta = rho (1 - rho for
+// sgn < 0) and face_c = theta c+ + (1 - theta) c- from the curvatures of the
+// two cells; the increment is rounded to float and added in float, as the
+// reference's iterator increment does.
+__global__ void __launch_bounds__(BLOCK_THREADS) surface_tension_kernel(Grid g, double dt, double dx, double kappa,
+                                                                        FaceParams fp, const float *__restrict__ fluid,
+                                                                        float *u, float *v, float *w) {
+    const long long NX = g.nx + 1, NY = g.ny + 1, NZ = g.dim == 3 ? g.nz + 1 : 1;
+    const long long total = NX * NY * NZ;
+    float *vel[3] = {u, v, w};
+    const int n[3] = {g.nx, g.ny, g.nz};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % NX);
+        const int j = (int)((t / NX) % NY);
+        const int k = (int)(t / (NX * NY));
+        const int pi[3] = {i, j, k};
+        for (int d = 0; d < g.dim; ++d) {
+            bool exists = true;
+            for (int e = 0; e < g.dim; ++e)
+                if (e != d && pi[e] >= n[e]) exists = false;
+            if (!exists) continue;
+            const double rho = face_rho(g, fluid, d, i, j, k, fp, 1);
+            if (!(rho && rho < 1.0)) continue;
+            const int a0 = min(max(i, 0), g.nx - 1), a1 = min(max(j, 0), g.ny - 1), a2 = min(max(k, 0), g.nz - 1);
+            const int b0 = min(max(i - (d == 0), 0), g.nx - 1), b1 = min(max(j - (d == 1), 0), g.ny - 1),
+                      b2 = min(max(k - (d == 2), 0), g.nz - 1);
+            const float fa = __ldg(fluid + a0 + (long long)g.nx * (a1 + (long long)g.ny * a2));
+            const double sgn = fa < 0.0 ? -1.0 : 1.0;
+            const double theta = sgn < 0 ? 1.0 - rho : rho;
+            const double face_c = theta * (double)st_curvature(g, fluid, a0, a1, a2, dx) +
+                                  (1.0 - theta) * (double)st_curvature(g, fluid, b0, b1, b2, dx);
+            const float inc = (float)(-sgn * dt / (dx * rho) * kappa * face_c);
+            const long long f = face_index(g, d, i, j, k);
+            vel[d][f] = vel[d][f] + inc;
+        }
+    }
+}
+
 // One thread per cell: labels the cell, assembles its row of the operator
 // and its right-hand side (macpressuresolver3.cpp:121-199,
 // macpressuresolver2.cpp:111-179). A cell is an unknown iff it is fluid and
@@ -519,6 +587,15 @@ static int node_blocks(const Grid &g, int grid_blocks) {
     const long long need = (total + BLOCK_THREADS - 1) / BLOCK_THREADS;
     const long long b = need < grid_blocks ? need : grid_blocks;
     return b < 1 ? 1 : (int)b;
+}
+
+cudaError_t launch_surface_tension(const Grid &g, double dt, double dx, const SetupParams &sp, double kappa,
+                                   const float *fluid, float *u, float *v, float *w, int grid_blocks,
+                                   cudaStream_t stream) {
+    const FaceParams fp = face_params(sp, dx, dt);
+    surface_tension_kernel<<<node_blocks(g, grid_blocks), BLOCK_THREADS, 0, stream>>>(g, dt, dx, kappa, fp, fluid, u, v,
+                                                                                       w);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,

@@ -29,7 +29,7 @@ protected:
     virtual void project(double dt, macarray2<Real> &velocity, const array2<Real> &solid, const array2<Real> &fluid,
                          double surface_tension, const std::vector<signed_rigidbody2_interface *> *) override {
         const int nx = m_shape.w, ny = m_shape.h;
-        if (surface_tension) console::dump("gbprojection2: surface tension is not applied\n");
+        m_params.surface_tension = surface_tension;
         std::vector<float> s((size_t)(nx + 1) * (ny + 1)), f((size_t)nx * ny), p(f.size());
         for (int j = 0; j <= ny; ++j)
             for (int i = 0; i <= nx; ++i) s[i + (size_t)(nx + 1) * j] = solid(i, j);

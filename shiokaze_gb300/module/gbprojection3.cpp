@@ -37,7 +37,7 @@ protected:
     virtual void project(double dt, macarray3<Real> &velocity, const array3<Real> &solid, const array3<Real> &fluid,
                          double surface_tension, const std::vector<signed_rigidbody3_interface *> *) override {
         const int nx = m_shape.w, ny = m_shape.h, nz = m_shape.d;
-        if (surface_tension) console::dump("gbprojection3: surface tension is not applied\n");
+        m_params.surface_tension = surface_tension;
         std::vector<float> s((size_t)(nx + 1) * (ny + 1) * (nz + 1)), f((size_t)nx * ny * nz), p(f.size());
         for (int k = 0; k <= nz; ++k)
             for (int j = 0; j <= ny; ++j)

@@ -71,6 +71,8 @@ CASES = {
     "liquid2_32": (lambda: scenes.liquid2(32, seed=1), {}, 1),
     "liquid2_40x24": (lambda: scenes.liquid2((40, 24), seed=9), {}, 1),
     "isolated3": (isolated_cells3, {}, 1),
+    "liquid3_16_tension": (lambda: scenes.liquid3(16, seed=21), {"surface_tension": 0.05}, 1),
+    "liquid2_32_tension": (lambda: scenes.liquid2(32, seed=22), {"surface_tension": 0.02}, 1),
     # No case without fluid: the reference then assembles an empty system and
     # pcg_solver.h:62-63 takes abs_max of an empty vector, which crashes.
     "accuracy3_16": (lambda: scenes.accuracy3(16, 0.25)[0], {"residual": 1e-18, "eps_fluid": 1e-18}, 1),

@@ -6,7 +6,8 @@ from golden_io import Case
 
 CONFIG_KEYS = {"residual": "Residual", "max_iterations": "MaxIterations", "warm_start": "WarmStart",
                "eps_fluid": "EpsFluid", "eps_solid": "EpsSolid", "second_order_fluid": "SecondOrderAccurateFluid",
-               "second_order_solid": "SecondOrderAccurateSolid", "gain": "Gain"}
+               "second_order_solid": "SecondOrderAccurateSolid", "gain": "Gain",
+               "surface_tension": "SurfaceTension"}
 
 
 def config_from(params: dict, **extra):
