@@ -174,6 +174,7 @@ def _ref_lib():
         lib.ref_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                    ctypes.c_char_p, ctypes.c_char_p]
         lib.ref_destroy.argtypes = [ctypes.c_void_p]
+        lib.ref_set_target_volume.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
         lib.ref_project.restype = ctypes.c_double
         lib.ref_project.argtypes = [ctypes.c_void_p, ctypes.c_double, fp, ctypes.c_int, ctypes.c_float, fp,
                                     ctypes.c_int, ctypes.c_float, fp, fp, fp, ctypes.c_double, fp,
@@ -215,6 +216,9 @@ class RefProjector:
                 pass
 
     __del__ = close
+
+    def set_target_volume(self, current, target):
+        self.lib.ref_set_target_volume(self.ctx, current, target)
 
     def project(self, dt, solid, fluid, u, v, w=None, solid_mode=0, fluid_mode=0, band=None) -> Result:
         if band is None:

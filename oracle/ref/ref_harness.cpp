@@ -160,6 +160,15 @@ void *ref_create(int dim, int nx, int ny, int nz, double dx, const char *kv, con
 
 void ref_destroy(void *hp) { delete static_cast<harness *>(hp); }
 
+/* macproject{2,3}_interface::set_target_volume (macpressuresolver3.cpp:45-48):
+ * the volumes the next project() corrects towards (macpressuresolver3.cpp:
+ * 204-217). */
+void ref_set_target_volume(void *hp, double current_volume, double target_volume) {
+    auto *h = static_cast<harness *>(hp);
+    if (h->dim == 3) (*h->proj3)->set_target_volume(current_volume, target_volume);
+    else (*h->proj2)->set_target_volume(current_volume, target_volume);
+}
+
 /* One projection. Arrays are dense, x fastest:
  *   solid: nodal (nx+1)(ny+1)(nz+1), fluid: cells nx*ny*nz,
  *   u: (nx+1)*ny*nz, v: nx*(ny+1)*nz, w: nx*ny*(nz+1)   (in/out),

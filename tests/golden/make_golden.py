@@ -73,6 +73,10 @@ CASES = {
     "isolated3": (isolated_cells3, {}, 1),
     "liquid3_16_tension": (lambda: scenes.liquid3(16, seed=21), {"surface_tension": 0.05}, 1),
     "liquid2_32_tension": (lambda: scenes.liquid2(32, seed=22), {"surface_tension": 0.02}, 1),
+    # volume correction: (current, target) volumes set before each step; two
+    # steps so that the controller's integral term carries over
+    "liquid3_12_volume": (lambda: scenes.liquid3(12, seed=23),
+                          {"gain": 1.0, "volume": [[0.30, 0.32], [0.31, 0.32]]}, 2),
     # No case without fluid: the reference then assembles an empty system and
     # pcg_solver.h:62-63 takes abs_max of an empty vector, which crashes.
     "accuracy3_16": (lambda: scenes.accuracy3(16, 0.25)[0], {"residual": 1e-18, "eps_fluid": 1e-18}, 1),
@@ -97,6 +101,8 @@ def check_realizable(sc):
 def make_case(name, factory, params, steps):
     sc = factory()
     check_realizable(sc)
+    params = dict(params)
+    volume = params.pop("volume", None)
     pj = oracle.RefProjector(sc.dim, sc.nx, sc.ny, sc.nz, sc.dx, **params)
     rng = np.random.default_rng(1000 + len(name))
     u, v, w = sc.u, sc.v, sc.w
@@ -104,6 +110,8 @@ def make_case(name, factory, params, steps):
     res = None
     for s in range(steps):
         inputs.append((u, v, w))
+        if volume is not None:
+            pj.set_target_volume(*volume[s])
         res = pj.project(sc.dt, sc.solid, sc.fluid, u, v, w, sc.solid_mode, sc.fluid_mode, sc.band)
         if s + 1 < steps:
             u, v, w = next_velocity(res, sc, rng)
@@ -112,6 +120,8 @@ def make_case(name, factory, params, steps):
                solid=sc.solid, fluid=sc.fluid, solid_mode=sc.solid_mode, fluid_mode=sc.fluid_mode, band=sc.band,
                steps=steps, out_pressure=res.pressure, out_u=res.u, out_v=res.v, out_unknown=res.unknown,
                iterations=res.iterations, reresid=res.reresid)
+    if volume is not None:
+        out["volume"] = np.array(volume, np.float64)
     for s, (uu, vv, ww) in enumerate(inputs):
         out[f"u{s}"] = uu
         out[f"v{s}"] = vv

@@ -33,3 +33,5 @@ class Case:
         self.out_unknown = d["out_unknown"].astype(bool)
         self.iterations = int(d["iterations"])
         self.reresid = float(d["reresid"])
+        # (current, target) volumes set before each step, if the case has them
+        self.volume = d["volume"] if "volume" in d else None

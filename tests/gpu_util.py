@@ -26,6 +26,8 @@ def run_case_gpu(c: Case, **extra):
     for s in range(c.steps):
         u, v, w = (None if a is None else a.copy() for a in c.inputs[s])
         vel = (u, v, w) if c.dim == 3 else (u, v)
+        if c.volume is not None:
+            pj.set_target_volume(*c.volume[s])
         statuses.append(pj.project(c.dt, vel, c.solid, c.fluid))
         out = (u, v, w)
     p = pj.get_pressure().copy()

@@ -20,6 +20,8 @@ def test_port_matches_reference_fixture(name):
     res = None
     for s in range(c.steps):
         u, v, w = c.inputs[s]
+        if c.volume is not None:
+            pj.set_target_volume(*c.volume[s])
         res = pj.project(c.dt, c.solid, c.fluid, u, v, w)
     pj.close()
     assert np.array_equal(res.unknown, c.out_unknown)
