@@ -86,6 +86,10 @@ typedef struct gbp_params {
     int iterations_per_sync;/* CG iterations between host checks of convergence (default 16) */
     double surface_tension; /* the surface_tension argument of macproject3_interface::project
                                (macpressuresolver3.cpp:85-115); 0 (default) leaves the velocity as is */
+    int tma_staging;        /* MGPCG MIXED: nonzero runs the fine level's four stencil passes with their
+                               tiles staged in shared memory by TMA where the grid allows it (3D, more than
+                               2^21 cells, nx % 8 == 0); 0 (default) uses the direct-load kernels, which
+                               compute every cell alike and measure faster over a whole solve on GB300 */
 } gbp_params;
 
 typedef struct gbp_stats {
@@ -101,6 +105,7 @@ typedef struct gbp_stats {
     float ms_solve;         /* device time, the linear solve */
     float ms_update;        /* device time, velocity update + pressure write */
     float ms_total;         /* host wall time of the call */
+    int tma_staged;         /* the fine level ran the TMA-staged kernels (see gbp_params.tma_staging) */
 } gbp_stats;
 
 /* Fills *p with the reference's defaults (and CG / FP64). */

@@ -13,7 +13,8 @@ Configuration keys are the reference's (``Residual``, ``MaxIterations``,
 ``WarmStart``, ``EpsFluid``, ``EpsSolid``, ``SecondOrderAccurateFluid``,
 ``SecondOrderAccurateSolid``, ``Gain``) plus this module's own
 (``Solver`` = "cg" | "mgpcg", ``Precision`` = "fp64" | "mixed",
-``MGSmooth``, ``MGCoarsest``, ``InnerTolerance``, ``IterationsPerSync``), and
+``MGSmooth``, ``MGCoarsest``, ``InnerTolerance``, ``IterationsPerSync``,
+``TMAStaging``), and
 ``SurfaceTension``, the value the reference passes as project()'s
 surface_tension argument.
 
@@ -44,7 +45,8 @@ class Params(ctypes.Structure):
                 ("second_order_fluid", ctypes.c_int), ("second_order_solid", ctypes.c_int),
                 ("gain", ctypes.c_double), ("solver", ctypes.c_int), ("precision", ctypes.c_int),
                 ("mg_smooth", ctypes.c_int), ("mg_coarsest", ctypes.c_int), ("inner_tolerance", ctypes.c_double),
-                ("iterations_per_sync", ctypes.c_int), ("surface_tension", ctypes.c_double)]
+                ("iterations_per_sync", ctypes.c_int), ("surface_tension", ctypes.c_double),
+                ("tma_staging", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -52,7 +54,7 @@ class Stats(ctypes.Structure):
                 ("reresid", ctypes.c_double), ("true_resid_inf", ctypes.c_double),
                 ("true_resid_l2", ctypes.c_double), ("b_inf", ctypes.c_double), ("unknowns", ctypes.c_longlong),
                 ("ms_assemble", ctypes.c_float), ("ms_solve", ctypes.c_float), ("ms_update", ctypes.c_float),
-                ("ms_total", ctypes.c_float)]
+                ("ms_total", ctypes.c_float), ("tma_staged", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -133,7 +135,7 @@ _KEYMAP = {
     "SecondOrderAccurateFluid": ("second_order_fluid", int), "SecondOrderAccurateSolid": ("second_order_solid", int),
     "Gain": ("gain", float), "MGSmooth": ("mg_smooth", int), "MGCoarsest": ("mg_coarsest", int),
     "InnerTolerance": ("inner_tolerance", float), "IterationsPerSync": ("iterations_per_sync", int),
-    "SurfaceTension": ("surface_tension", float),
+    "SurfaceTension": ("surface_tension", float), "TMAStaging": ("tma_staging", int),
 }
 
 

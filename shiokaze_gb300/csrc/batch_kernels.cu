@@ -1167,6 +1167,345 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_res
         });
 }
 
+// ---- TMA-staged fine-level kernels (FP32) ---------------------------------------------
+
+constexpr int ST_HX = ST_TX + 8, ST_HY = ST_TY + 2, ST_HZ = ST_TZ + 2;
+constexpr int ST_HALO = ST_HX * ST_HY * ST_HZ;       // floats of a HALO box
+constexpr int ST_OWN = ST_TX * ST_TY * ST_TZ;        // OWN
+constexpr int ST_CXN = ST_HX * ST_TY * ST_TZ;        // CX
+constexpr int ST_CYN = ST_TX * (ST_TY + 1) * ST_TZ;  // CY
+constexpr int ST_CZN = ST_TX * ST_TY * (ST_TZ + 1);  // CZ
+constexpr int ST_XCX = 40, ST_XCY = 6, ST_XCZ = 4;
+constexpr int ST_XCN = ST_XCX * ST_XCY * ST_XCZ;      // XC
+static_assert(ST_HALO % 32 == 0 && ST_OWN % 32 == 0 && ST_CXN % 32 == 0 && ST_CYN % 32 == 0 && ST_CZN % 32 == 0 &&
+                  ST_XCN % 32 == 0,
+              "every box starts on a 128-byte boundary");
+
+// Box layout of one stage of each kind, in floats: {map, offset, size}.
+struct StageBox {
+    int map, off, n;
+};
+template <int KIND> struct StageLayout;
+template <> struct StageLayout<STAGE_PRESMOOTH> {
+    static constexpr int nbox = 5;
+    __host__ __device__ static constexpr StageBox box(int q) {
+        return q == 0   ? StageBox{SM_B_HALO, 0, ST_HALO}
+               : q == 1 ? StageBox{SM_INV_HALO, ST_HALO, ST_HALO}
+               : q == 2 ? StageBox{SM_CX, 2 * ST_HALO, ST_CXN}
+               : q == 3 ? StageBox{SM_CY, 2 * ST_HALO + ST_CXN, ST_CYN}
+                        : StageBox{SM_CZ, 2 * ST_HALO + ST_CXN + ST_CYN, ST_CZN};
+    }
+    static constexpr int floats = 2 * ST_HALO + ST_CXN + ST_CYN + ST_CZN;
+};
+template <> struct StageLayout<STAGE_POST_BLACK> {
+    static constexpr int nbox = 7;
+    __host__ __device__ static constexpr StageBox box(int q) {
+        return q == 0   ? StageBox{SM_X_HALO, 0, ST_HALO}
+               : q == 1 ? StageBox{SM_B_OWN, ST_HALO, ST_OWN}
+               : q == 2 ? StageBox{SM_INV_OWN, ST_HALO + ST_OWN, ST_OWN}
+               : q == 3 ? StageBox{SM_CX, ST_HALO + 2 * ST_OWN, ST_CXN}
+               : q == 4 ? StageBox{SM_CY, ST_HALO + 2 * ST_OWN + ST_CXN, ST_CYN}
+               : q == 5 ? StageBox{SM_CZ, ST_HALO + 2 * ST_OWN + ST_CXN + ST_CYN, ST_CZN}
+                        : StageBox{SM_XC, ST_HALO + 2 * ST_OWN + ST_CXN + ST_CYN + ST_CZN, ST_XCN};
+    }
+    static constexpr int floats = ST_HALO + 2 * ST_OWN + ST_CXN + ST_CYN + ST_CZN + ST_XCN;
+};
+template <> struct StageLayout<STAGE_RED_DOT> {
+    static constexpr int nbox = 6;
+    __host__ __device__ static constexpr StageBox box(int q) {
+        return q == 0   ? StageBox{SM_X_HALO, 0, ST_HALO}
+               : q == 1 ? StageBox{SM_B_OWN, ST_HALO, ST_OWN}
+               : q == 2 ? StageBox{SM_INV_OWN, ST_HALO + ST_OWN, ST_OWN}
+               : q == 3 ? StageBox{SM_CX, ST_HALO + 2 * ST_OWN, ST_CXN}
+               : q == 4 ? StageBox{SM_CY, ST_HALO + 2 * ST_OWN + ST_CXN, ST_CYN}
+                        : StageBox{SM_CZ, ST_HALO + 2 * ST_OWN + ST_CXN + ST_CYN, ST_CZN};
+    }
+    static constexpr int floats = ST_HALO + 2 * ST_OWN + ST_CXN + ST_CYN + ST_CZN;
+};
+template <> struct StageLayout<STAGE_SPMV> {
+    static constexpr int nbox = 5;
+    __host__ __device__ static constexpr StageBox box(int q) {
+        return q == 0   ? StageBox{SM_P_HALO, 0, ST_HALO}
+               : q == 1 ? StageBox{SM_DIAG_OWN, ST_HALO, ST_OWN}
+               : q == 2 ? StageBox{SM_CX, ST_HALO + ST_OWN, ST_CXN}
+               : q == 3 ? StageBox{SM_CY, ST_HALO + ST_OWN + ST_CXN, ST_CYN}
+                        : StageBox{SM_CZ, ST_HALO + ST_OWN + ST_CXN + ST_CYN, ST_CZN};
+    }
+    static constexpr int floats = ST_HALO + ST_OWN + ST_CXN + ST_CYN + ST_CZN;
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *b) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(b)));
+}
+__device__ __forceinline__ void mbar_expect(unsigned long long *b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+// Bounded wait for the phase of the given parity (about a second at most).
+__device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity) {
+    for (int it = 0; it < (1 << 22); ++it) {
+        unsigned done;
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.b32 %0, 1, 0, p; }"
+                     : "=r"(done)
+                     : "r"(smem_u32(b)), "r"(parity)
+                     : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void tma_box(float *dst, const CUtensorMap *map, int x, int y, int z,
+                                        unsigned long long *b) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(b))
+        : "memory");
+}
+
+// Neighbour sum of cell h (0: i, 1: i+1) of a pair from the staged boxes, in
+// the order -x, +x, -y, +y, -z, +z (the arithmetic of pair_nsum): hc is cell
+// i's index in a HALO box, cxi / cyi / czi in the CX / CY / CZ boxes, `own`
+// the pair's values, val(m, d) the value at HALO index m reached in
+// direction d (0..5 for -x, +x, -y, +y, -z, +z). The pair's second cell
+// always exists (staged levels have nx % 8 == 0).
+template <class VF>
+__device__ __forceinline__ float staged_nsum(int h, const Grid &g, int i, int j, int k, int hc, int cxi, int cyi,
+                                             int czi, const float *scx, const float *scy, const float *scz,
+                                             Pair<float> own, VF val) {
+    float s = 0.0f;
+    if (h == 0) {
+        if (i > 0) s += scx[cxi - 1] * val(hc - 1, 0);
+        s += scx[cxi] * own.b;
+    } else {
+        s += scx[cxi] * own.a;
+        if (i + 2 < g.nx) s += scx[cxi + 1] * val(hc + 2, 1);
+    }
+    const int hh = hc + h;
+    if (j > 0) s += scy[cyi + h - ST_TX] * val(hh - ST_HX, 2);
+    if (j + 1 < g.ny) s += scy[cyi + h] * val(hh + ST_HX, 3);
+    if (k > 0) s += scz[czi + h - ST_TX * ST_TY] * val(hh - ST_HX * ST_HY, 4);
+    if (k + 1 < g.nz) s += scz[czi + h] * val(hh + ST_HX * ST_HY, 5);
+    return s;
+}
+
+// One launch over the staged fine levels of a batch: blocks walk their items
+// (one 64 x 8 x 4 tile each) as the other kernels do, with the tiles of the
+// next two items in flight: thread 0 issues an item's boxes into a stage
+// when the item two back has been consumed, every thread waits on the
+// stage's mbarrier (bounded), computes from shared memory, and writes its
+// results to global memory. Reductions (red_dot, spmv) flush per scene as
+// reduce_items does. A wait that runs out records cnt->bar_err = 2 and the
+// block leaves after letting its other copy land (bounded); the host then
+// abandons the solve.
+template <int KIND>
+__global__ void __launch_bounds__(BLOCK_THREADS, 1)
+    staged_kernel(const BLevel<float> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
+                  const BScene<float> *__restrict__ scenes, int gate, double *part, float alpha, BatchCounters *cnt) {
+    using LY = StageLayout<KIND>;
+    constexpr bool REDUCE = KIND == STAGE_RED_DOT || KIND == STAGE_SPMV;
+    constexpr int STAGE_FLOATS = LY::floats;
+    if (batch_idle(cnt)) return;
+    extern __shared__ unsigned char st_smem[];
+    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ int valid[2];
+    __shared__ ItemCtx<float> ctx;
+    __shared__ double shf[BLOCK_THREADS / 32];
+    float *stage0 = reinterpret_cast<float *>(st_smem + ((128u - (smem_u32(st_smem) & 127u)) & 127u));
+    const int tid = threadIdx.x, G = gridDim.x;
+    if (tid == 0) {
+        mbar_init(&bar[0]);
+        mbar_init(&bar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    int issue_seg = 0;
+    // thread 0: the boxes of item w into stage s (if its scene is not gated)
+    auto issue = [&](int s, int w) {
+        const BItem it = item_at(segs, nseg, w, issue_seg);
+        const BLevel<float> &L = levels[it.ref];
+        const int ok = gate < 0 ? 1 : !gated(scenes[L.scene].sc, gate);
+        valid[s] = ok;
+        if (!ok) return;
+        const Grid &g = L.g;
+        const unsigned t = (unsigned)it.tile;
+        const unsigned r = fdiv(t, g.ftx2);
+        const unsigned tk = fdiv(r, g.fty);
+        const int x0 = (int)(t - r * g.ftx2.d) * ST_TX, y0 = (int)(r - tk * (unsigned)g.nty) * ST_TY,
+                  z0 = (int)tk * ST_TZ;
+        float *dst = stage0 + (size_t)s * STAGE_FLOATS;
+        mbar_expect(&bar[s], (unsigned)(LY::floats * 4));
+#pragma unroll
+        for (int q = 0; q < LY::nbox; ++q) {
+            const StageBox bx = LY::box(q);
+            int x = x0, y = y0, z = z0;
+            if (bx.map == SM_XC) {
+                x = x0 / 2 - 4;
+                y = y0 / 2 - 1;
+                z = z0 / 2 - 1;
+            } else if (bx.map <= SM_P_HALO) {
+                x = x0 - 4;
+                y = y0 - 1;
+                z = z0 - 1;
+            } else if (bx.map == SM_CX) {
+                x = x0 - 4;
+            } else if (bx.map == SM_CY) {
+                y = y0 - 1;
+            } else if (bx.map == SM_CZ) {
+                z = z0 - 1;
+            }
+            tma_box(dst + bx.off, L.tmap + bx.map, x, y, z, &bar[s]);
+        }
+    };
+    if (tid == 0) {
+        if (blockIdx.x < n) issue(0, blockIdx.x);
+        if (blockIdx.x + G < n) issue(1, blockIdx.x + G);
+    }
+    __syncthreads();
+    unsigned phase = 0u;
+    int cur = -1, sgc = 0;
+    BItem first{};
+    DotAcc<float> acc;
+    acc.reset();
+    auto flush = [&]() {
+        const int slot = (int)((((long long)blockIdx.x - first.begin) % G + G) % G);
+        acc.store(shf, part, first.begin + slot, n);
+        const int flushes = min(first.count, G);
+        Scalars *sc = ctx.S.sc;
+        if constexpr (KIND == STAGE_RED_DOT) {
+            if (item_last(&sc->counter[SITE_DOT], flushes)) {
+                const double rho_new = sum_range(part, first.begin, flushes, shf);
+                if (threadIdx.x == 0) {
+                    if (sc->first) {
+                        sc->beta = 0.0;
+                        sc->first = 0;
+                    } else {
+                        sc->beta = rho_new / sc->rho;
+                    }
+                    sc->rho = rho_new;
+                    if (rho_new != rho_new) {
+                        sc->done = 1;
+                        sc->status = 3;
+                    }
+                    sc->counter[SITE_DOT] = 0;
+                }
+            }
+        } else if constexpr (KIND == STAGE_SPMV) {
+            if (item_last(&sc->counter[SITE_SPMV], flushes)) {
+                const double pq = sum_range(part, first.begin, flushes, shf);
+                if (threadIdx.x == 0) {
+                    sc->pap = pq;
+                    sc->alpha = sc->rho / pq;
+                    sc->counter[SITE_SPMV] = 0;
+                }
+            }
+        }
+    };
+    for (int nn = 0, w = blockIdx.x; w < n; ++nn, w += G) {
+        const int s = nn & 1;
+        const BItem it = item_at(segs, nseg, w, sgc);
+        if (it.ref != cur) {
+            if (REDUCE && cur >= 0 && !ctx.skip) flush();
+            refresh(ctx, cur, it, levels, scenes, gate);
+            first = it;
+            acc.reset();
+        }
+        if (valid[s]) {
+            const bool ok = mbar_wait(&bar[s], (phase >> s) & 1u);
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicExch(&cnt->bar_err, 2);
+                    if (w + G < n && valid[s ^ 1]) mbar_wait(&bar[s ^ 1], (phase >> (s ^ 1)) & 1u);
+                }
+                return;
+            }
+            phase ^= 1u << s;
+            const BLevel<float> &L = ctx.L;
+            const Grid &g = L.g;
+            const float *st = stage0 + (size_t)s * STAGE_FLOATS;
+            const unsigned t = (unsigned)it.tile;
+            const unsigned r = fdiv(t, g.ftx2);
+            const unsigned tk = fdiv(r, g.fty);
+            const int x0 = (int)(t - r * g.ftx2.d) * ST_TX, y0 = (int)(r - tk * (unsigned)g.nty) * ST_TY,
+                      z0 = (int)tk * ST_TZ;
+            const int px = tid & 31, qy = tid >> 5;
+            const int i = x0 + 2 * px, j = y0 + qy;
+            if (i < g.nx && j < g.ny) {
+                const float *scx = st + LY::box((KIND == STAGE_PRESMOOTH || KIND == STAGE_SPMV) ? 2 : 3).off;
+                const float *scy = scx + ST_CXN, *scz = scy + ST_CYN;
+                for (int kk = 0; kk < ST_TZ; ++kk) {
+                    const int k = z0 + kk;
+                    if (k >= g.nz) break;
+                    const int hc = (2 * px + 4) + ST_HX * ((qy + 1) + ST_HY * (kk + 1));
+                    const int oc = 2 * px + ST_TX * (qy + ST_TY * kk);
+                    const int cxi = (2 * px + 4) + ST_HX * (qy + ST_TY * kk);
+                    const int cyi = 2 * px + ST_TX * ((qy + 1) + (ST_TY + 1) * kk);
+                    const int czi = 2 * px + ST_TX * (qy + ST_TY * (kk + 1));
+                    const long long c = cell_index(g, i, j, k);
+                    if constexpr (KIND == STAGE_PRESMOOTH) {
+                        const float *sb = st, *si = st + ST_HALO;
+                        const Pair<float> b2{sb[hc], sb[hc + 1]}, iv{si[hc], si[hc + 1]};
+                        const Pair<float> red{b2.a * iv.a, b2.b * iv.b};
+                        auto val = [&](int m, int) { return sb[m] * si[m]; };
+                        Pair<float> out = red;
+                        if (((i + j + k) & 1) == 0)
+                            out.b = (b2.b + staged_nsum(1, g, i, j, k, hc, cxi, cyi, czi, scx, scy, scz, red, val)) *
+                                    iv.b;
+                        else
+                            out.a = (b2.a + staged_nsum(0, g, i, j, k, hc, cxi, cyi, czi, scx, scy, scz, red, val)) *
+                                    iv.a;
+                        st2<float, true>(L.x, c, out, true);
+                    } else if constexpr (KIND == STAGE_POST_BLACK) {
+                        const float *sx = st, *sb = st + ST_HALO, *si = sb + ST_OWN, *sxc = scz + ST_CZN;
+                        const int h = ((i + j + k) & 1) == 1 ? 0 : 1;
+                        // parents in the XC box: own, and the steps to the
+                        // parents of the -x, +x, -y, +y, -z, +z neighbours
+                        const int P = (px + 4) + ST_XCX * (((qy >> 1) + 1) + ST_XCY * ((kk >> 1) + 1));
+                        const int step[6] = {-1, 1, (j & 1) ? 0 : -ST_XCX, (j & 1) ? ST_XCX : 0,
+                                             (k & 1) ? 0 : -ST_XCX * ST_XCY, (k & 1) ? ST_XCX * ST_XCY : 0};
+                        const float pc = sxc[P];
+                        auto val = [&](int m, int d) {
+                            const float q = (d >= 2 && step[d] == 0) ? pc : sxc[P + step[d]];
+                            return sx[m] + alpha * q;
+                        };
+                        const Pair<float> own{sx[hc] + alpha * pc, sx[hc + 1] + alpha * pc};
+                        const float sh = staged_nsum(h, g, i, j, k, hc, cxi, cyi, czi, scx, scy, scz, own, val);
+                        L.x[c + h] = (sb[oc + h] + sh) * si[oc + h];
+                    } else if constexpr (KIND == STAGE_RED_DOT) {
+                        const float *sx = st, *sb = st + ST_HALO, *si = sb + ST_OWN;
+                        const int hr = ((i + j + k) & 1) == 0 ? 0 : 1;
+                        const Pair<float> x2{sx[hc], sx[hc + 1]}, b2{sb[oc], sb[oc + 1]};
+                        auto val = [&](int m, int) { return sx[m]; };
+                        const float sh = staged_nsum(hr, g, i, j, k, hc, cxi, cyi, czi, scx, scy, scz, x2, val);
+                        const float xv = ((hr ? b2.b : b2.a) + sh) * si[oc + hr];
+                        Pair<float> out = x2;
+                        if (hr) out.b = xv;
+                        else out.a = xv;
+                        L.x[c + hr] = xv;
+                        acc.add(out.a, b2.a);
+                        acc.add(out.b, b2.b);
+                    } else {
+                        const float *sp = st, *sd = st + ST_HALO;
+                        const Pair<float> p2{sp[hc], sp[hc + 1]}, d2{sd[oc], sd[oc + 1]};
+                        auto val = [&](int m, int) { return sp[m]; };
+                        const float sa = staged_nsum(0, g, i, j, k, hc, cxi, cyi, czi, scx, scy, scz, p2, val);
+                        const float sb2 = staged_nsum(1, g, i, j, k, hc, cxi, cyi, czi, scx, scy, scz, p2, val);
+                        const Pair<float> q2{d2.a * p2.a - sa, d2.b * p2.b - sb2};
+                        st2<float, true>(ctx.S.q, c, q2, true);
+                        acc.add(p2.a, q2.a);
+                        acc.add(p2.b, q2.b);
+                    }
+                }
+            }
+        }
+        __syncthreads();  // stage s consumed by every thread
+        if (tid == 0 && w + 2 * G < n) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(s, w + 2 * G);
+        }
+    }
+    if (REDUCE && cur >= 0 && !ctx.skip) flush();
+}
+
 }  // namespace
 
 template <class T>
@@ -1246,6 +1585,53 @@ template <class T> int b_coarse_capacity(int sms) {
         return 0;
     return sms * (a < b ? a : b);
 }
+size_t stage_bytes(int kind) {
+    switch (kind) {
+    case STAGE_PRESMOOTH: return sizeof(float) * StageLayout<STAGE_PRESMOOTH>::floats;
+    case STAGE_POST_BLACK: return sizeof(float) * StageLayout<STAGE_POST_BLACK>::floats;
+    case STAGE_RED_DOT: return sizeof(float) * StageLayout<STAGE_RED_DOT>::floats;
+    default: return sizeof(float) * StageLayout<STAGE_SPMV>::floats;
+    }
+}
+// two stages and 128 bytes to align them
+static size_t staged_smem(int kind) { return 2 * stage_bytes(kind) + 128; }
+cudaError_t b_staged_enable() {
+    cudaError_t e = cudaFuncSetAttribute(staged_kernel<STAGE_PRESMOOTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)staged_smem(STAGE_PRESMOOTH));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(staged_kernel<STAGE_POST_BLACK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)staged_smem(STAGE_POST_BLACK));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(staged_kernel<STAGE_RED_DOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)staged_smem(STAGE_RED_DOT));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(staged_kernel<STAGE_SPMV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)staged_smem(STAGE_SPMV));
+    return e;
+}
+cudaError_t b_staged(int kind, const BLaunch &L, const BLevel<float> *levels, const BSeg *segs, int nseg, int n,
+                     const BScene<float> *scenes, double *part, float alpha) {
+    const size_t sm = staged_smem(kind);
+    switch (kind) {
+    case STAGE_PRESMOOTH:
+        staged_kernel<STAGE_PRESMOOTH><<<L.blocks, BLOCK_THREADS, sm, L.stream>>>(levels, segs, nseg, n, scenes, L.gate,
+                                                                                  part, alpha, L.cnt);
+        break;
+    case STAGE_POST_BLACK:
+        staged_kernel<STAGE_POST_BLACK><<<L.blocks, BLOCK_THREADS, sm, L.stream>>>(levels, segs, nseg, n, scenes,
+                                                                                   L.gate, part, alpha, L.cnt);
+        break;
+    case STAGE_RED_DOT:
+        staged_kernel<STAGE_RED_DOT><<<L.blocks, BLOCK_THREADS, sm, L.stream>>>(levels, segs, nseg, n, scenes, L.gate,
+                                                                                part, alpha, L.cnt);
+        break;
+    default:
+        staged_kernel<STAGE_SPMV><<<L.blocks, BLOCK_THREADS, sm, L.stream>>>(levels, segs, nseg, n, scenes, L.gate,
+                                                                             part, alpha, L.cnt);
+    }
+    return cudaGetLastError();
+}
+
 template <class T>
 cudaError_t b_direction(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                         const BScene<T> *scenes) {

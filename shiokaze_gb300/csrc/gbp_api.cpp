@@ -91,6 +91,7 @@ void gbp_params_default(gbp_params *p) {
     p->inner_tolerance = 1e-3;
     p->iterations_per_sync = 16;
     p->surface_tension = 0.0;
+    p->tma_staging = 0;
 }
 
 const char *gbp_strerror(int status) {
@@ -287,6 +288,7 @@ int project_device(gbp_scene *s, double dt, const float *solid, const float *flu
         GBP_CUDA(cudaMemcpy(&h, st.sc, sizeof(Scalars), cudaMemcpyDeviceToHost));
         s->solver->fill_stats(h, stats);
         stats->unknowns = (long long)h.unknowns;
+        stats->tma_staged = p.solver == GBP_SOLVER_MGPCG && s->solver->staged() ? 1 : 0;
         cudaEventElapsedTime(&stats->ms_assemble, c->ev[0], c->ev[1]);
         cudaEventElapsedTime(&stats->ms_solve, c->ev[1], c->ev[2]);
         cudaEventElapsedTime(&stats->ms_update, c->ev[2], c->ev[3]);
@@ -442,18 +444,18 @@ int gbp_batch_project_device(gbp_batch *b, const double *dt, const float *const 
     GBP_CUDA(cudaEventRecord(c->ev[1], st));
     // the batched solve
     const bool mixed = p.precision == GBP_PRECISION_MIXED;
-    long long key = (mixed ? 1 : 0) | (p.warm_start ? 2 : 0) | ((long long)c->grid_blocks << 4) |
-                    ((long long)(p.mg_coarsest > 1 ? p.mg_coarsest : 4) << 24);
+    long long key = (mixed ? 1 : 0) | (p.warm_start ? 2 : 0) | (p.tma_staging ? 4 : 0) |
+                    ((long long)c->grid_blocks << 4) | ((long long)(p.mg_coarsest > 1 ? p.mg_coarsest : 4) << 24);
     for (int i = 0; i < n; ++i) key = key * 31 + (b->scenes[i]->solver->has_prev() ? 1 : 0);
     if (b->key != key) {
         if (mixed) {
             BatchPlan<float> plan;
             for (gbp_scene *s : b->scenes) s->solver->add_to_plan<float>(plan, p);
-            rc = b->runner.build<float>(plan, c->grid_blocks);
+            rc = b->runner.build<float>(plan, c->grid_blocks, p.tma_staging, st);
         } else {
             BatchPlan<double> plan;
             for (gbp_scene *s : b->scenes) s->solver->add_to_plan<double>(plan, p);
-            rc = b->runner.build<double>(plan, c->grid_blocks);
+            rc = b->runner.build<double>(plan, c->grid_blocks, 0, st);
         }
         if (rc) return fail(rc, b->runner.error());
         b->key = key;
@@ -497,6 +499,7 @@ int gbp_batch_project_device(gbp_batch *b, const double *dt, const float *const 
             std::memset(&stats[i], 0, sizeof(gbp_stats));
             b->scenes[i]->solver->fill_stats(h, &stats[i]);
             stats[i].unknowns = (long long)h.unknowns;
+            stats[i].tma_staged = b->runner.scene_staged(i) ? 1 : 0;
             stats[i].ms_assemble = ms_a;
             stats[i].ms_solve = ms_s;
             stats[i].ms_update = ms_u;

@@ -7,7 +7,10 @@
 // scenes not done -- between replays.
 #include "gbp_batch.h"
 
+#include <cudaTypedefs.h>
+
 #include <algorithm>
+#include <cstdint>
 #include <cstring>
 #include <functional>
 
@@ -24,6 +27,63 @@ namespace {
 
 constexpr int kChunk = 4;
 constexpr int kInnerMax = 50;
+
+int blocks_for(int items, int grid_blocks) { return std::max(1, std::min(items, grid_blocks)); }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); null if the driver does not provide it.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// A 3D FP32 tensor map over an nx x ny x nz array with the given box.
+bool encode_map(CUtensorMap *m, const float *ptr, int nx, int ny, int nz, unsigned bx, unsigned by, unsigned bz) {
+    auto enc = tensor_map_encoder();
+    if (!enc || !ptr) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+    cuuint64_t strides[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
+    cuuint32_t box[3] = {bx, by, bz};
+    cuuint32_t es[3] = {1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(ptr), dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The STAGE_MAPS maps of a fine FP32 level, or false if the level does not
+// qualify: 3D, 4-plane tiles (one tile per item), nx a multiple of 8 (rows
+// of the level and of its coarse grid are multiples of 16 bytes, every box
+// x start a multiple of 4 floats), every array 16-byte aligned.
+bool stage_maps(const BLevel<float> &L, const BScene<float> &S, CUtensorMap *m) {
+    const Grid &g = L.g, &c = L.gc;
+    if (g.dim != 3 || g.tz != ST_TZ || g.nx % 8 != 0 || !L.vec || c.nx % 4 != 0) return false;
+    for (const void *p : {(const void *)L.b, (const void *)L.inv, (const void *)L.x, (const void *)L.cx,
+                          (const void *)L.cy, (const void *)L.cz, (const void *)L.diag, (const void *)L.xc,
+                          (const void *)S.p, (const void *)S.q})
+        if (!p || (uintptr_t)p % 16 != 0) return false;
+    const unsigned HX = ST_TX + 8, HY = ST_TY + 2, HZ = ST_TZ + 2;
+    return encode_map(&m[SM_B_HALO], L.b, g.nx, g.ny, g.nz, HX, HY, HZ) &&
+           encode_map(&m[SM_INV_HALO], L.inv, g.nx, g.ny, g.nz, HX, HY, HZ) &&
+           encode_map(&m[SM_X_HALO], L.x, g.nx, g.ny, g.nz, HX, HY, HZ) &&
+           encode_map(&m[SM_P_HALO], S.p, g.nx, g.ny, g.nz, HX, HY, HZ) &&
+           encode_map(&m[SM_CX], L.cx, g.nx, g.ny, g.nz, HX, ST_TY, ST_TZ) &&
+           encode_map(&m[SM_CY], L.cy, g.nx, g.ny, g.nz, ST_TX, ST_TY + 1, ST_TZ) &&
+           encode_map(&m[SM_CZ], L.cz, g.nx, g.ny, g.nz, ST_TX, ST_TY, ST_TZ + 1) &&
+           encode_map(&m[SM_B_OWN], L.b, g.nx, g.ny, g.nz, ST_TX, ST_TY, ST_TZ) &&
+           encode_map(&m[SM_INV_OWN], L.inv, g.nx, g.ny, g.nz, ST_TX, ST_TY, ST_TZ) &&
+           encode_map(&m[SM_DIAG_OWN], L.diag, g.nx, g.ny, g.nz, ST_TX, ST_TY, ST_TZ) &&
+           encode_map(&m[SM_XC], L.xc, c.nx, c.ny, c.nz, 40, 6, 4);
+}
 }  // namespace
 
 void BatchRunner::release() {
@@ -45,13 +105,18 @@ void BatchRunner::release() {
     s_pair_.clear();
     s_restrict_.clear();
     d_fine_pairs_ = nullptr;
+    d_fine_staged_ = d_fine_plain_ = nullptr;
+    n_fine_staged_ = s_fine_staged_ = n_fine_plain_ = s_fine_plain_ = 0;
+    d_tmaps_ = nullptr;
+    staged_scene_.clear();
     d_part_ = nullptr;
     d_counters_ = nullptr;
     bytes_ = 0;
 }
 
-template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blocks) {
+template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blocks, int staging, cudaStream_t stream) {
     release();
+    stage_mask_ = 0;
     auto upload = [&](const void *src, size_t bytes, void **dst) -> int {
         void *d = nullptr;
         RUN_CUDA(cudaMalloc(&d, bytes ? bytes : 16));
@@ -74,7 +139,33 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
         (void)grid_blocks;
     }
     mixed_ = sizeof(T) == 4;
-    if ((rc = upload(plan.levels.data(), plan.levels.size() * sizeof(BLevel<T>), &d_levels_))) return rc;
+    sms_ = std::max(1, grid_blocks_ / BatchOcc<T>::blocks);
+    // staged fine levels: their tensor maps, in one device array
+    std::vector<BLevel<T>> levels = plan.levels;
+    std::vector<int> staged_at(levels.size(), -1);
+    staged_scene_.assign(plan.nscenes, 0);
+    if constexpr (sizeof(T) == 4) {
+        if (staging) {
+            std::vector<CUtensorMap> maps;
+            for (int s = 0; s < plan.nscenes && s < (int)plan.fine_ref.size(); ++s) {
+                const int ref = plan.fine_ref[s];
+                CUtensorMap m[STAGE_MAPS];
+                if (!stage_maps(levels[ref], plan.scenes[s], m)) continue;
+                staged_at[ref] = (int)maps.size();
+                staged_scene_[s] = 1;
+                maps.insert(maps.end(), m, m + STAGE_MAPS);
+            }
+            if (!maps.empty()) {
+                void *d;
+                if ((rc = upload(maps.data(), maps.size() * sizeof(CUtensorMap), &d))) return rc;
+                d_tmaps_ = static_cast<CUtensorMap *>(d);
+                for (size_t r = 0; r < levels.size(); ++r)
+                    if (staged_at[r] >= 0) levels[r].tmap = d_tmaps_ + staged_at[r];
+                RUN_CUDA(b_staged_enable());
+            }
+        }
+    }
+    if ((rc = upload(levels.data(), levels.size() * sizeof(BLevel<T>), &d_levels_))) return rc;
     if ((rc = upload(plan.scenes.data(), plan.scenes.size() * sizeof(BScene<T>), &d_scenes_))) return rc;
     {
         void *d;
@@ -103,6 +194,27 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
     }
     if ((rc = segs(plan.fine_pairs, &d_fine_pairs_, &s_fine_pairs_))) return rc;
     n_fine_pairs_ = plan.n_fine_pairs;
+    // the fine list split into staged and plain segments (item positions
+    // renumbered within each)
+    {
+        std::vector<BSeg> staged, plain;
+        int ns = 0, np = 0;
+        for (BSeg sg : plan.fine_pairs) {
+            if (staged_at[sg.ref] >= 0) {
+                sg.begin = ns;
+                ns += sg.count;
+                staged.push_back(sg);
+            } else {
+                sg.begin = np;
+                np += sg.count;
+                plain.push_back(sg);
+            }
+        }
+        if ((rc = segs(staged, &d_fine_staged_, &s_fine_staged_))) return rc;
+        if ((rc = segs(plain, &d_fine_plain_, &s_fine_plain_))) return rc;
+        n_fine_staged_ = ns;
+        n_fine_plain_ = np;
+    }
     // coarse global levels 1..max_global-1: one cooperative launch per
     // V-cycle half, on at most as many blocks as stay resident
     coarse_ = CoarseLists{};
@@ -136,6 +248,7 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
     d_counters_ = static_cast<BatchCounters *>(d);
     RUN_CUDA(cudaMallocHost(&h_counters_, sizeof(BatchCounters)));
     if (tail_smem_ > 0) RUN_CUDA(b_tail_enable<T>(tail_smem_));
+    if (n_fine_staged_ > 0) stage_mask_ = (1 << STAGE_KINDS) - 1;
     return GBP_OK;
 }
 
@@ -147,7 +260,34 @@ static MgSettings settings_of(const gbp_params &p) {
     return ms;
 }
 
-static int blocks_for(int items, int grid_blocks) { return std::max(1, std::min(items, grid_blocks)); }
+// One pass over the fine levels: the staged ones in one launch, the others
+// with the direct-load kernel.
+template <class T> cudaError_t BatchRunner::fine_pass(int kind, const gbp_params &p, cudaStream_t st, int gate) {
+    const MgSettings ms = settings_of(p);
+    auto *lv = static_cast<const BLevel<T> *>(d_levels_);
+    auto *sc = static_cast<const BScene<T> *>(d_scenes_);
+    cudaError_t e = cudaSuccess;
+    // the plain pass covers every fine level unless this pass runs staged
+    const BSeg *segs = d_fine_pairs_;
+    int nseg = s_fine_pairs_, n = n_fine_pairs_;
+    if constexpr (sizeof(T) == 4) {
+        if (n_fine_staged_ > 0 && (stage_mask_ >> kind & 1)) {
+            e = b_staged(kind, BLaunch{std::min(n_fine_staged_, sms_), st, gate, d_scene_of_, d_counters_}, lv,
+                         d_fine_staged_, s_fine_staged_, n_fine_staged_, sc, d_part_, (float)ms.alpha);
+            segs = d_fine_plain_;
+            nseg = s_fine_plain_;
+            n = n_fine_plain_;
+        }
+    }
+    if (e != cudaSuccess || n == 0) return e;
+    const BLaunch L{blocks_for(n, grid_blocks_), st, gate, d_scene_of_, d_counters_};
+    switch (kind) {
+    case STAGE_PRESMOOTH: return b_presmooth<T>(L, lv, segs, nseg, n, sc);
+    case STAGE_POST_BLACK: return b_post_black<T>(L, lv, segs, nseg, n, sc, T(ms.alpha));
+    case STAGE_RED_DOT: return b_red_dot<T>(L, lv, segs, nseg, n, sc, d_part_);
+    default: return b_spmv<T>(L, lv, segs, nseg, n, sc, d_part_);
+    }
+}
 
 template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &p, cudaStream_t st, long long *nodes) {
     const int gate = mixed_ ? 1 : 0;
@@ -160,7 +300,7 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
     // descend: the fine level, then the coarse global levels in one launch
     if (max_global_ > 0) {
         const int l = 0;
-        e = b_presmooth<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc);
+        e = fine_pass<T>(STAGE_PRESMOOTH, p, st, gate);
         ++*nodes;
         for (int s = 1; s < ms.smooth && e == cudaSuccess; ++s) {
             e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, 0);
@@ -186,19 +326,19 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
     }
     if (e == cudaSuccess && max_global_ > 0) {
         const int l = 0;
-        e = b_post_black<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, T(ms.alpha));
+        e = fine_pass<T>(STAGE_POST_BLACK, p, st, gate);
         ++*nodes;
         for (int s = 1; s < ms.smooth && e == cudaSuccess; ++s) {
             e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, 0);
             if (e == cudaSuccess) e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, 1);
             *nodes += 2;
         }
-        if (e == cudaSuccess) e = b_red_dot<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_);
+        if (e == cudaSuccess) e = fine_pass<T>(STAGE_RED_DOT, p, st, gate);
         ++*nodes;
     }
     // CG on the fine level
     if (e == cudaSuccess) e = b_direction<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc);
-    if (e == cudaSuccess) e = b_spmv<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_);
+    if (e == cudaSuccess) e = fine_pass<T>(STAGE_SPMV, p, st, gate);
     if (e == cudaSuccess)
         e = b_update<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_, mixed_ ? 1 : 0, d_counters_);
     *nodes += 3;
@@ -251,7 +391,9 @@ template <class T> int BatchRunner::solve(const gbp_params &p, cudaStream_t st, 
         RUN_CUDA(cudaMemcpyAsync(h_counters_, d_counters_, sizeof(BatchCounters), cudaMemcpyDeviceToHost, st));
         RUN_CUDA(cudaStreamSynchronize(st));
         if (h_counters_->bar_err)
-            return fail(GBP_ERR_CUDA, "coarse-level kernels: a grid barrier wait ran out (solve abandoned)");
+            return fail(GBP_ERR_CUDA, h_counters_->bar_err == 2
+                                          ? "staged fine-level kernels: a tile wait ran out (solve abandoned)"
+                                          : "coarse-level kernels: a grid barrier wait ran out (solve abandoned)");
         if (h_counters_->remaining <= 0) return GBP_OK;
         RUN_CUDA(cudaGraphLaunch(graph_, st));
         *launches += graph_nodes_;
@@ -267,14 +409,14 @@ template <class T> int BatchRunner::bench(int which, int reps, cudaStream_t st, 
     std::function<cudaError_t()> launch;
     auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, 0, d_scene_of_, d_counters_}; };
     switch (which) {
-    case 0: launch = [&]() { return b_presmooth<T>(L(n_pair_[0]), lv, d_pair_[0], s_pair_[0], n_pair_[0], sc); }; break;
+    case 0: launch = [&]() { return fine_pass<T>(STAGE_PRESMOOTH, gbp_params{}, st, 0); }; break;
     case 1: launch = [&]() { return b_restrict<T>(L(n_restrict_[0]), lv, d_restrict_[0], s_restrict_[0], n_restrict_[0], sc); }; break;
     case 2:
-        launch = [&]() { return b_post_black<T>(L(n_pair_[0]), lv, d_pair_[0], s_pair_[0], n_pair_[0], sc, T(mset.alpha)); };
+        launch = [&]() { return fine_pass<T>(STAGE_POST_BLACK, gbp_params{}, st, 0); };
         break;
-    case 3: launch = [&]() { return b_red_dot<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_); }; break;
+    case 3: launch = [&]() { return fine_pass<T>(STAGE_RED_DOT, gbp_params{}, st, 0); }; break;
     case 4: launch = [&]() { return b_direction<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc); }; break;
-    case 5: launch = [&]() { return b_spmv<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_); }; break;
+    case 5: launch = [&]() { return fine_pass<T>(STAGE_SPMV, gbp_params{}, st, 0); }; break;
     case 6:
         launch = [&]() {
             return b_update<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_, 0, d_counters_);
@@ -303,8 +445,8 @@ template <class T> int BatchRunner::bench(int which, int reps, cudaStream_t st, 
     return GBP_OK;
 }
 
-template int BatchRunner::build<double>(const BatchPlan<double> &, int);
-template int BatchRunner::build<float>(const BatchPlan<float> &, int);
+template int BatchRunner::build<double>(const BatchPlan<double> &, int, int, cudaStream_t);
+template int BatchRunner::build<float>(const BatchPlan<float> &, int, int, cudaStream_t);
 template int BatchRunner::solve<double>(const gbp_params &, cudaStream_t, long long *);
 template int BatchRunner::solve<float>(const gbp_params &, cudaStream_t, long long *);
 template int BatchRunner::bench<double>(int, int, cudaStream_t, float *);

@@ -13,6 +13,7 @@
 // of one.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -37,7 +38,26 @@ template <class T> struct BLevel {
     // pairs of this level (and, on level 0, of the scene's vectors) move as
     // 2-wide accesses: nx even and every such array 2-element aligned
     int vec;
+    // TMA descriptors of a staged fine level (STAGE_MAPS of them), or null
+    const CUtensorMap *tmap;
 };
+
+// Staged fine-level kernels: a pair tile of 64 x 8 x 4 cells and the halo
+// its stencil reads are copied into shared memory by TMA
+// (cp.async.bulk.tensor) two tiles ahead of the compute. The boxes around a
+// tile at (x0, y0, z0): HALO 72 x 10 x 6 from (x0-4, y0-1, z0-1) (x starts
+// on a 16-byte boundary, hence 4 columns left), OWN 64 x 8 x 4 from the
+// tile, CX 72 x 8 x 4 from (x0-4, y0, z0), CY 64 x 9 x 4 from (x0, y0-1, z0),
+// CZ 64 x 8 x 5 from (x0, y0, z0-1), and XC 40 x 6 x 4 of the coarse grid
+// from (x0/2-4, y0/2-1, z0/2-1) (the parents of the tile and its halo).
+enum StageMap {
+    SM_B_HALO, SM_INV_HALO, SM_X_HALO, SM_P_HALO, SM_CX, SM_CY, SM_CZ,
+    SM_B_OWN, SM_INV_OWN, SM_DIAG_OWN, SM_XC, STAGE_MAPS
+};
+enum StageKind { STAGE_PRESMOOTH, STAGE_POST_BLACK, STAGE_RED_DOT, STAGE_SPMV, STAGE_KINDS };
+constexpr int ST_TX = 64, ST_TY = 8, ST_TZ = 4;
+// shared-memory bytes of one stage of each kind (two stages per block)
+size_t stage_bytes(int kind);
 
 // Per-scene state of the fine level.
 template <class T> struct BScene {
@@ -144,6 +164,7 @@ template <class T> struct BatchPlan {
     std::vector<BSeg> fine_pairs;
     std::vector<int> n_pair, n_restrict;
     int n_fine_pairs = 0;
+    std::vector<int> fine_ref;           // level entry of each scene's fine level
 };
 
 class BatchRunner {
@@ -155,7 +176,9 @@ public:
 
     // Uploads the plan (tables, lists) and sizes the partials. T = double
     // for the FP64 path, float for the inner solve of the mixed path.
-    template <class T> int build(const BatchPlan<T> &plan, int grid_blocks);
+    // staging (gbp_params.tma_staging): nonzero stages the FP32 fine levels
+    // that qualify (the four stencil passes run TMA-staged there).
+    template <class T> int build(const BatchPlan<T> &plan, int grid_blocks, int staging, cudaStream_t stream);
     // Runs the solve after every scene's operator and hierarchy are set up:
     // initial residual, then graph replays until every scene is done.
     template <class T> int solve(const gbp_params &p, cudaStream_t stream, long long *launches);
@@ -166,6 +189,11 @@ public:
     void release();
     const char *error() const { return err_.c_str(); }
     size_t device_bytes() const { return bytes_; }
+    // whether scene s's fine level runs TMA-staged kernels (any of the passes)
+    bool scene_staged(int s) const {
+        return stage_mask_ && s >= 0 && s < (int)staged_scene_.size() && staged_scene_[s];
+    }
+    int stage_mask() const { return stage_mask_; }
 
 private:
     int fail(int code, const std::string &m) {
@@ -193,6 +221,15 @@ private:
     BatchCounters *d_counters_ = nullptr, *h_counters_ = nullptr;
     CoarseLists coarse_{};
     int coarse_blocks_ = 0;
+    // fine levels split by staging: TMA-staged (FP32 levels that qualify) and
+    // plain; each a segment list over pair tiles of level 0
+    BSeg *d_fine_staged_ = nullptr, *d_fine_plain_ = nullptr;
+    int n_fine_staged_ = 0, s_fine_staged_ = 0, n_fine_plain_ = 0, s_fine_plain_ = 0;
+    CUtensorMap *d_tmaps_ = nullptr;
+    std::vector<char> staged_scene_;
+    int stage_mask_ = 0;  // bit k: pass k (StageKind) runs staged
+    int sms_ = 0;
+    template <class T> cudaError_t fine_pass(int kind, const gbp_params &p, cudaStream_t st, int gate);
     cudaGraphExec_t graph_ = nullptr;
     long long graph_key_ = -1;
     long long graph_nodes_ = 0;
@@ -238,6 +275,11 @@ template <class T>
 cudaError_t b_coarse_ascend(const BLaunch &L, const BLevel<T> *levels, const CoarseLists &cl,
                             const BScene<T> *scenes, MgSettings ms, T alpha);
 template <class T> int b_coarse_capacity(int sms);
+// One staged fine-level pass (FP32) over the items of `segs`: presmooth,
+// post_black (alpha), red_dot or spmv (partials in `part`). L.blocks <= SMs.
+cudaError_t b_staged(int kind, const BLaunch &L, const BLevel<float> *levels, const BSeg *segs, int nseg, int n,
+                     const BScene<float> *scenes, double *part, float alpha);
+cudaError_t b_staged_enable();
 template <class T>
 cudaError_t b_direction(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                         const BScene<T> *scenes);

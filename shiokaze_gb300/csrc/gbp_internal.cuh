@@ -62,8 +62,9 @@ struct Grid {
     long long ntiles;
     long long ncell;
     // divisors of the tile decompositions: ntx (32-wide cell tiles), ntx2
-    // (64-wide pair tiles), nty
+    // (64-wide pair tiles), nty; and of the node grid: nx+1, (nx+1)(ny+1)
     FastDiv ftx, ftx2, fty;
+    FastDiv fn1, fn2;
 };
 
 inline Grid make_grid(int dim, int nx, int ny, int nz) {
@@ -83,6 +84,8 @@ inline Grid make_grid(int dim, int nx, int ny, int nz) {
     g.ftx = make_fastdiv((unsigned)g.ntx);
     g.ftx2 = make_fastdiv((unsigned)((nx + 63) / 64));
     g.fty = make_fastdiv((unsigned)g.nty);
+    g.fn1 = make_fastdiv((unsigned)(nx + 1));
+    g.fn2 = make_fastdiv((unsigned)((nx + 1) * (ny + 1)));
     return g;
 }
 
@@ -127,6 +130,17 @@ struct Partials {
 
 __device__ __forceinline__ long long cell_index(const Grid &g, int i, int j, int k) {
     return (long long)i + (long long)g.nx * ((long long)j + (long long)g.ny * k);
+}
+
+// Coordinates of node t of the (nx+1)(ny+1)(nz+1) node grid, x fastest
+// (node counts fit 32 bits).
+__device__ __forceinline__ void node_coords(const Grid &g, long long t, int &i, int &j, int &k) {
+    const unsigned tt = (unsigned)t;
+    const unsigned q = fdiv(tt, g.fn1);
+    const unsigned kk = fdiv(tt, g.fn2);
+    i = (int)(tt - q * g.fn1.d);
+    j = (int)(q - kk * (unsigned)(g.ny + 1));
+    k = (int)kk;
 }
 
 // Tiles are numbered x fastest, then y, then z (tile counts fit 32 bits).

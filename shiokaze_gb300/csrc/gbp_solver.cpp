@@ -342,7 +342,9 @@ template <class T> void Solver::add_to_plan(BatchPlan<T> &plan, const gbp_params
                                     (const void *)sc.x64, (const void *)sc.r64})
                 vec = vec && al(ptr, 2 * sizeof(double));
         }
-        plan.levels.push_back(BLevel<T>{F.g, F.diag, F.inv, F.cx, F.cy, F.cz, F.b, F.x, C.x, C.b, C.g, s, vec ? 1 : 0});
+        if (l == 0) plan.fine_ref.push_back((int)plan.levels.size());
+        plan.levels.push_back(
+            BLevel<T>{F.g, F.diag, F.inv, F.cx, F.cy, F.cz, F.b, F.x, C.x, C.b, C.g, s, vec ? 1 : 0, nullptr});
         plan.scene_of.push_back(s);
         auto add = [&](std::vector<BSeg> &list, int &items, long long tiles, long long cells_per_tile) {
             const int m = (int)std::max(1LL, BITEM_CELLS / cells_per_tile);
@@ -377,17 +379,17 @@ int Solver::solve_mg(const Grid &g, const gbp_params &p, int grid_blocks, cudaSt
     int rc = setup_mg(g, p, grid_blocks, stream, launches);
     if (rc) return rc;
     // a batch of one: the same kernels and reductions as a batched solve
-    const long long key = (mixed ? 1 : 0) | (warm ? 2 : 0) | ((long long)grid_blocks << 4) |
-                          ((long long)mg_coarsest_ << 24);
+    const long long key = (mixed ? 1 : 0) | (warm ? 2 : 0) | (p.tma_staging ? 4 : 0) |
+                          ((long long)grid_blocks << 4) | ((long long)mg_coarsest_ << 24);
     if (runner_key_ != key) {
         if (mixed) {
             BatchPlan<float> plan;
             add_to_plan<float>(plan, p);
-            rc = runner_.build<float>(plan, grid_blocks);
+            rc = runner_.build<float>(plan, grid_blocks, p.tma_staging, stream);
         } else {
             BatchPlan<double> plan;
             add_to_plan<double>(plan, p);
-            rc = runner_.build<double>(plan, grid_blocks);
+            rc = runner_.build<double>(plan, grid_blocks, 0, stream);
         }
         if (rc) return fail(rc, runner_.error());
         runner_key_ = key;

@@ -66,6 +66,8 @@ public:
     // (GBP_OK / GBP_ERR_NOT_CONVERGED / GBP_ERR_NAN).
     int complete(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches);
     bool has_prev() const { return st_.have_prev; }
+    // the last single-scene MGPCG solve ran the TMA-staged fine kernels
+    bool staged() const { return runner_key_ >= 0 && runner_.scene_staged(0); }
 
 private:
     int fail(int code, const std::string &m) {

@@ -206,9 +206,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS) surface_tension_kernel(Grid g, 
     const int n[3] = {g.nx, g.ny, g.nz};
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % NX);
-        const int j = (int)((t / NX) % NY);
-        const int k = (int)(t / (NX * NY));
+        int i, j, k;
+        node_coords(g, t, i, j, k);
         const int pi[3] = {i, j, k};
         for (int d = 0; d < g.dim; ++d) {
             bool exists = true;
@@ -354,9 +353,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_kernel(Grid g, double 
     const int n[3] = {g.nx, g.ny, g.nz};
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % NX);
-        const int j = (int)((t / NX) % NY);
-        const int k = (int)(t / (NX * NY));
+        int i, j, k;
+        node_coords(g, t, i, j, k);
         const int pi[3] = {i, j, k};
         for (int d = 0; d < g.dim; ++d) {
             // face (i,j,k) of dimension d exists if the other indices are cells
@@ -416,9 +414,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt,
     const int n[3] = {g.nx, g.ny, g.nz};
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % NX);
-        const int j = (int)((t / NX) % NY);
-        const int k = (int)(t / (NX * NY));
+        int i, j, k;
+        node_coords(g, t, i, j, k);
         const int pi[3] = {i, j, k};
         for (int d = 0; d < g.dim; ++d) {
             bool exists = true;
@@ -522,9 +519,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_faces_kernel(Grid g, d
     const int n[3] = {g.nx, g.ny, g.nz};
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % NX);
-        const int j = (int)((t / NX) % NY);
-        const int k = (int)(t / (NX * NY));
+        int i, j, k;
+        node_coords(g, t, i, j, k);
         const int pi[3] = {i, j, k};
         for (int d = 0; d < g.dim; ++d) {
             bool exists = true;
