@@ -365,8 +365,8 @@ __device__ __forceinline__ void presmooth_items(const BLevel<T> *__restrict__ le
     }
 }
 
-template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+template <class T, int OCC>
+__global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     presmooth_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
                   const BScene<T> *__restrict__ scenes, int gate, const BatchCounters *live) {
     if (batch_idle(live)) return;
@@ -402,8 +402,8 @@ __device__ __forceinline__ void sweep_items(const BLevel<T> *__restrict__ levels
     }
 }
 
-template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+template <class T, int OCC>
+__global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     sweep_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
                   const BScene<T> *__restrict__ scenes, int gate, int color, const BatchCounters *live) {
     if (batch_idle(live)) return;
@@ -451,8 +451,8 @@ __device__ __forceinline__ void restrict_items(const BLevel<T> *__restrict__ lev
     }
 }
 
-template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+template <class T, int OCC>
+__global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     restrict_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
                   const BScene<T> *__restrict__ scenes, int gate, const BatchCounters *live) {
     if (batch_idle(live)) return;
@@ -504,8 +504,8 @@ __device__ __forceinline__ void post_black_items(const BLevel<T> *__restrict__ l
     }
 }
 
-template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+template <class T, int OCC>
+__global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     post_black_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
                   const BScene<T> *__restrict__ scenes, int gate, T alpha, const BatchCounters *live) {
     if (batch_idle(live)) return;
@@ -594,8 +594,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
 
 // Last red pass of the fine level, with rho' = z . r (z = x, r = b there)
 // per scene; the scene's last flush sets beta (0 for a new direction).
-template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+template <class T, int OCC>
+__global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     red_dot_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
                    const BScene<T> *__restrict__ scenes, int gate, double *part, const int *__restrict__ scene_of,
                    const BatchCounters *live) {
@@ -846,8 +846,8 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
 
 // ---- CG on the fine level -----------------------------------------------------------
 
-template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+template <class T, int OCC>
+__global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     direction_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
                      const BScene<T> *__restrict__ scenes, int gate, const BatchCounters *live) {
     if (batch_idle(live)) return;
@@ -878,8 +878,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
     }
 }
 
-template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+template <class T, int OCC>
+__global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     spmv_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
                 const BScene<T> *__restrict__ scenes, int gate, double *part, const int *__restrict__ scene_of,
                 const BatchCounters *live) {
@@ -920,8 +920,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
 
 // x += alpha p (x = alpha p on the first update of a solve), r -= alpha q,
 // |r|_inf. mode 0: the solve's stopping rule; mode 1: inner solve.
-template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+template <class T, int OCC>
+__global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     update_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
                   const BScene<T> *__restrict__ scenes, int gate, double *part, int mode, BatchCounters *cnt,
                   const int *__restrict__ scene_of) {
@@ -1508,36 +1508,48 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 1)
 
 }  // namespace
 
+// Launches kernel<T, OCC> with OCC = L.occ, one of the occupancy variants
+// the kernels are compiled for (blocks of 256 threads per SM); 0 selects the
+// precision's default.
+#define OCC_DISPATCH(L, kernel, T, ARGS)                                                  \
+    do {                                                                                  \
+        switch ((L).occ ? (L).occ : BatchOcc<T>::blocks) {                                \
+        case 4: kernel<T, 4><<<(L).blocks, BLOCK_THREADS, 0, (L).stream>>> ARGS; break;   \
+        case 6: kernel<T, 6><<<(L).blocks, BLOCK_THREADS, 0, (L).stream>>> ARGS; break;   \
+        default: kernel<T, 5><<<(L).blocks, BLOCK_THREADS, 0, (L).stream>>> ARGS; break;  \
+        }                                                                                 \
+    } while (0)
+
 template <class T>
 cudaError_t b_presmooth(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                         const BScene<T> *scenes) {
-    presmooth_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, L.cnt);
+    OCC_DISPATCH(L, presmooth_kernel, T, (levels, segs, nseg, n, scenes, L.gate, L.cnt));
     return cudaGetLastError();
 }
 template <class T>
 cudaError_t b_sweep(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                     const BScene<T> *scenes, int color) {
-    sweep_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, color, L.cnt);
+    OCC_DISPATCH(L, sweep_kernel, T, (levels, segs, nseg, n, scenes, L.gate, color, L.cnt));
     return cudaGetLastError();
 }
 template <class T>
 cudaError_t b_restrict(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                        const BScene<T> *scenes) {
-    restrict_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, L.cnt);
+    OCC_DISPATCH(L, restrict_kernel, T, (levels, segs, nseg, n, scenes, L.gate, L.cnt));
     return cudaGetLastError();
 }
 template <class T>
 cudaError_t b_post_black(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                          const BScene<T> *scenes, T alpha) {
-    post_black_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, alpha,
-                                                                   L.cnt);
+    OCC_DISPATCH(L, post_black_kernel, T, (levels, segs, nseg, n, scenes, L.gate, alpha,
+                                                                   L.cnt));
     return cudaGetLastError();
 }
 template <class T>
 cudaError_t b_red_dot(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                       const BScene<T> *scenes, double *part) {
-    red_dot_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, part,
-                                                                L.scene_of, L.cnt);
+    OCC_DISPATCH(L, red_dot_kernel, T, (levels, segs, nseg, n, scenes, L.gate, part,
+                                                                L.scene_of, L.cnt));
     return cudaGetLastError();
 }
 template <class T>
@@ -1635,21 +1647,21 @@ cudaError_t b_staged(int kind, const BLaunch &L, const BLevel<float> *levels, co
 template <class T>
 cudaError_t b_direction(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                         const BScene<T> *scenes) {
-    direction_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, L.cnt);
+    OCC_DISPATCH(L, direction_kernel, T, (levels, segs, nseg, n, scenes, L.gate, L.cnt));
     return cudaGetLastError();
 }
 template <class T>
 cudaError_t b_spmv(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                    const BScene<T> *scenes, double *part) {
-    spmv_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, part, L.scene_of,
-                                                             L.cnt);
+    OCC_DISPATCH(L, spmv_kernel, T, (levels, segs, nseg, n, scenes, L.gate, part, L.scene_of,
+                                                             L.cnt));
     return cudaGetLastError();
 }
 template <class T>
 cudaError_t b_update(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                      const BScene<T> *scenes, double *part, int mode, BatchCounters *cnt) {
-    update_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.gate, part, mode, cnt,
-                                                               L.scene_of);
+    OCC_DISPATCH(L, update_kernel, T, (levels, segs, nseg, n, scenes, L.gate, part, mode, cnt,
+                                                               L.scene_of));
     return cudaGetLastError();
 }
 template <class T>

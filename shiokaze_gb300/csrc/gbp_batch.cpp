@@ -11,8 +11,11 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cmath>
 #include <cstring>
 #include <functional>
+#include <map>
+#include <mutex>
 
 namespace gbp {
 
@@ -117,6 +120,7 @@ void BatchRunner::release() {
 template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blocks, int staging, cudaStream_t stream) {
     release();
     stage_mask_ = 0;
+    for (int &o : occ_) o = 0;
     auto upload = [&](const void *src, size_t bytes, void **dst) -> int {
         void *d = nullptr;
         RUN_CUDA(cudaMalloc(&d, bytes ? bytes : 16));
@@ -249,6 +253,99 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
     RUN_CUDA(cudaMallocHost(&h_counters_, sizeof(BatchCounters)));
     if (tail_smem_ > 0) RUN_CUDA(b_tail_enable<T>(tail_smem_));
     if (n_fine_staged_ > 0) stage_mask_ = (1 << STAGE_KINDS) - 1;
+    // occupancy variants, tuned per precision and half-octave of fine cells
+    long long cells = 0;
+    for (const BScene<T> &sc : plan.scenes) cells += sc.g.ncell;
+    const int bucket = cells > 0 ? (int)std::lround(2.0 * std::log2((double)cells)) : 0;
+    const std::string key = std::string(sizeof(T) == 4 ? "f" : "d") + std::to_string(bucket) +
+                            (stage_mask_ ? "s" : "") + "/" + std::to_string(plan.nscenes > 1 ? 2 : 1);
+    if ((rc = tune_occupancy<T>(stream, key))) return rc;
+    return GBP_OK;
+}
+
+template <class T> BLaunch BatchRunner::launch_for(int bk, int items, cudaStream_t st, int gate) const {
+    const int occ = bk >= 0 ? occ_[bk] : 0;
+    const int per_sm = occ ? occ : BatchOcc<T>::blocks;
+    return BLaunch{blocks_for(items, std::min(MAX_GRID, sms_ * per_sm)), st, gate, d_scene_of_, d_counters_, occ};
+}
+
+// The autotuner of occupancy: the fine-level kernels are compiled for 4, 5
+// and 6 resident blocks of 256 threads per SM (more registers per thread, or
+// more warps to hide latency); the best choice moves with the problem size
+// (at 128^3 most run best with 4, at 256^3 red_dot and spmv with 6). For each
+// tuned kernel this times the three variants on the batch's own work lists
+// (one untimed launch, then the median of three, CUDA events on the solve's
+// stream) and keeps the fastest. The launches run ungated on the scenes'
+// arrays before the solve fills them: values do not change the work, every
+// array they write is rewritten by the solve before it is read, and the
+// solve resets the scalars and counters they touch. Choices are kept per
+// precision and half-octave of the batch's fine cells.
+template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::string &key) {
+    static std::mutex mu;
+    static std::map<std::string, std::vector<int>> cache;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) {
+            for (int k = 0; k < BK_TUNED; ++k) occ_[k] = it->second[k];
+            return GBP_OK;
+        }
+    }
+    if (max_global_ < 1) return GBP_OK;
+    std::memset(h_counters_, 0, sizeof(BatchCounters));
+    h_counters_->remaining = nscenes_;
+    RUN_CUDA(cudaMemcpyAsync(d_counters_, h_counters_, sizeof(BatchCounters), cudaMemcpyHostToDevice, st));
+    cudaEvent_t e0, e1;
+    RUN_CUDA(cudaEventCreate(&e0));
+    RUN_CUDA(cudaEventCreate(&e1));
+    auto *lv = static_cast<const BLevel<T> *>(d_levels_);
+    auto *sc = static_cast<const BScene<T> *>(d_scenes_);
+    const gbp_params p{};
+    cudaError_t err = cudaSuccess;
+    auto pass = [&](int k) -> cudaError_t {
+        switch (k) {
+        case BK_PRESMOOTH: return fine_pass<T>(STAGE_PRESMOOTH, p, st, -1);
+        case BK_RESTRICT:
+            return b_restrict<T>(launch_for<T>(BK_RESTRICT, n_restrict_[0], st, -1), lv, d_restrict_[0],
+                                 s_restrict_[0], n_restrict_[0], sc);
+        case BK_POST_BLACK: return fine_pass<T>(STAGE_POST_BLACK, p, st, -1);
+        case BK_RED_DOT: return fine_pass<T>(STAGE_RED_DOT, p, st, -1);
+        case BK_DIRECTION:
+            return b_direction<T>(launch_for<T>(BK_DIRECTION, n_fine_pairs_, st, -1), lv, d_fine_pairs_,
+                                  s_fine_pairs_, n_fine_pairs_, sc);
+        default: return fine_pass<T>(STAGE_SPMV, p, st, -1);
+        }
+    };
+    const int variants[3] = {4, 5, 6};
+    for (int k = 0; k < BK_TUNED && err == cudaSuccess; ++k) {
+        float best = 0.f;
+        int pick = 0;
+        for (int v : variants) {
+            occ_[k] = v;
+            float t[3] = {0.f, 0.f, 0.f};
+            err = pass(k);
+            for (int r = 0; r < 3 && err == cudaSuccess; ++r) {
+                err = cudaEventRecord(e0, st);
+                if (err == cudaSuccess) err = pass(k);
+                if (err == cudaSuccess) err = cudaEventRecord(e1, st);
+                if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+                if (err == cudaSuccess) err = cudaEventElapsedTime(&t[r], e0, e1);
+            }
+            if (err != cudaSuccess) break;
+            std::sort(t, t + 3);
+            if (!pick || t[1] < best) {
+                best = t[1];
+                pick = v;
+            }
+        }
+        occ_[k] = pick;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (err != cudaSuccess)
+        return fail(GBP_ERR_CUDA, std::string("tuning kernel occupancy: ") + cudaGetErrorString(err));
+    std::lock_guard<std::mutex> lock(mu);
+    cache[key] = std::vector<int>(occ_, occ_ + BK_TUNED);
     return GBP_OK;
 }
 
@@ -280,7 +377,11 @@ template <class T> cudaError_t BatchRunner::fine_pass(int kind, const gbp_params
         }
     }
     if (e != cudaSuccess || n == 0) return e;
-    const BLaunch L{blocks_for(n, grid_blocks_), st, gate, d_scene_of_, d_counters_};
+    const int bk = kind == STAGE_PRESMOOTH ? BK_PRESMOOTH
+                   : kind == STAGE_POST_BLACK ? BK_POST_BLACK
+                   : kind == STAGE_RED_DOT ? BK_RED_DOT
+                                           : BK_SPMV;
+    const BLaunch L = launch_for<T>(bk, n, st, gate);
     switch (kind) {
     case STAGE_PRESMOOTH: return b_presmooth<T>(L, lv, segs, nseg, n, sc);
     case STAGE_POST_BLACK: return b_post_black<T>(L, lv, segs, nseg, n, sc, T(ms.alpha));
@@ -307,7 +408,9 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
             if (e == cudaSuccess) e = b_sweep<T>(L(n_pair_[l]), lv, d_pair_[l], s_pair_[l], n_pair_[l], sc, 1);
             *nodes += 2;
         }
-        if (e == cudaSuccess) e = b_restrict<T>(L(n_restrict_[l]), lv, d_restrict_[l], s_restrict_[l], n_restrict_[l], sc);
+        if (e == cudaSuccess)
+            e = b_restrict<T>(launch_for<T>(BK_RESTRICT, n_restrict_[l], st, gate), lv, d_restrict_[l],
+                              s_restrict_[l], n_restrict_[l], sc);
         ++*nodes;
     }
     if (e == cudaSuccess && max_global_ > 1) {
@@ -337,7 +440,9 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
         ++*nodes;
     }
     // CG on the fine level
-    if (e == cudaSuccess) e = b_direction<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc);
+    if (e == cudaSuccess)
+        e = b_direction<T>(launch_for<T>(BK_DIRECTION, n_fine_pairs_, st, gate), lv, d_fine_pairs_, s_fine_pairs_,
+                           n_fine_pairs_, sc);
     if (e == cudaSuccess) e = fine_pass<T>(STAGE_SPMV, p, st, gate);
     if (e == cudaSuccess)
         e = b_update<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_, mixed_ ? 1 : 0, d_counters_);
@@ -410,12 +515,22 @@ template <class T> int BatchRunner::bench(int which, int reps, cudaStream_t st, 
     auto L = [&](int items) { return BLaunch{blocks_for(items, grid_blocks_), st, 0, d_scene_of_, d_counters_}; };
     switch (which) {
     case 0: launch = [&]() { return fine_pass<T>(STAGE_PRESMOOTH, gbp_params{}, st, 0); }; break;
-    case 1: launch = [&]() { return b_restrict<T>(L(n_restrict_[0]), lv, d_restrict_[0], s_restrict_[0], n_restrict_[0], sc); }; break;
+    case 1:
+        launch = [&]() {
+            return b_restrict<T>(launch_for<T>(BK_RESTRICT, n_restrict_[0], st, 0), lv, d_restrict_[0],
+                                 s_restrict_[0], n_restrict_[0], sc);
+        };
+        break;
     case 2:
         launch = [&]() { return fine_pass<T>(STAGE_POST_BLACK, gbp_params{}, st, 0); };
         break;
     case 3: launch = [&]() { return fine_pass<T>(STAGE_RED_DOT, gbp_params{}, st, 0); }; break;
-    case 4: launch = [&]() { return b_direction<T>(L(n_fine_pairs_), lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc); }; break;
+    case 4:
+        launch = [&]() {
+            return b_direction<T>(launch_for<T>(BK_DIRECTION, n_fine_pairs_, st, 0), lv, d_fine_pairs_,
+                                  s_fine_pairs_, n_fine_pairs_, sc);
+        };
+        break;
     case 5: launch = [&]() { return fine_pass<T>(STAGE_SPMV, gbp_params{}, st, 0); }; break;
     case 6:
         launch = [&]() {

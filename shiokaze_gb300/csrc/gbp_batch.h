@@ -167,6 +167,19 @@ template <class T> struct BatchPlan {
     std::vector<int> fine_ref;           // level entry of each scene's fine level
 };
 
+// A launch of a batched kernel.
+struct BLaunch {
+    int blocks;
+    cudaStream_t stream;
+    int gate;
+    const int *scene_of;  // scene of each level-table entry (reductions)
+    BatchCounters *cnt;   // batch counters (idle and refinement checks)
+    int occ;              // occupancy variant (4, 5 or 6 blocks per SM); 0: the precision's default
+};
+
+// Fine-level kernels whose occupancy variant the autotuner picks per batch.
+enum BatchKernel { BK_PRESMOOTH, BK_RESTRICT, BK_POST_BLACK, BK_RED_DOT, BK_DIRECTION, BK_SPMV, BK_TUNED };
+
 class BatchRunner {
 public:
     BatchRunner() = default;
@@ -228,6 +241,14 @@ private:
     CUtensorMap *d_tmaps_ = nullptr;
     std::vector<char> staged_scene_;
     int stage_mask_ = 0;  // bit k: pass k (StageKind) runs staged
+    int occ_[BK_TUNED] = {};  // occupancy variant per tuned kernel (0: default)
+    // a launch of tuned kernel bk (or -1: untuned) over `items` items
+    template <class T> BLaunch launch_for(int bk, int items, cudaStream_t st, int gate) const;
+    template <class T> int tune_occupancy(cudaStream_t st, const std::string &key);
+public:
+    // the chosen occupancy variant of tuned kernel bk (blocks of 256 threads per SM)
+    template <class T> int occupancy(int bk) const { return occ_[bk] ? occ_[bk] : BatchOcc<T>::blocks; }
+private:
     int sms_ = 0;
     template <class T> cudaError_t fine_pass(int kind, const gbp_params &p, cudaStream_t st, int gate);
     cudaGraphExec_t graph_ = nullptr;
@@ -236,16 +257,10 @@ private:
     double inner_rel_ = 1e-3;
 };
 
-// Launch functions (batch_kernels.cu). `levels`, `scenes`, `items` are
-// device arrays.
-struct BLaunch {
-    int blocks;
-    cudaStream_t stream;
-    int gate;
-    const int *scene_of;  // scene of each level-table entry (reductions)
-    BatchCounters *cnt;   // batch counters (idle and refinement checks)
-};
 
+
+// Launch functions (batch_kernels.cu). `levels`, `scenes` and `segs` are
+// device arrays.
 template <class T>
 cudaError_t b_presmooth(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes);
 template <class T>
