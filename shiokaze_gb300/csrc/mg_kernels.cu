@@ -52,6 +52,14 @@ __device__ __forceinline__ bool gated(const Scalars *sc, int gate) {
     return false;
 }
 
+// 1/d in the level's type: FP64 division for the FP64 hierarchy; for the
+// FP32 one the correctly rounded FP32 reciprocal of the rounded diagonal
+// (no FP64 division, whose pipe is scarce on this GPU; the preconditioner
+// only needs a consistent value).
+template <class T> __device__ __forceinline__ T recip(double d);
+template <> __device__ __forceinline__ double recip<double>(double d) { return 1.0 / d; }
+template <> __device__ __forceinline__ float recip<float>(double d) { return __frcp_rn((float)d); }
+
 template <class F> __device__ __forceinline__ void for_each_cell(const Grid &g, F f) {
     const int tx = threadIdx.x & (TILE_X - 1), ty = threadIdx.x / TILE_X;
     for (long long t = blockIdx.x; t < g.ntiles; t += gridDim.x) {
@@ -89,7 +97,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) mg_fine_setup_kernel(Grid g,
                                                                       T *cx, T *cy, T *cz, bool copy) {
     for_each_cell(g, [&](int i, int j, int k, long long c) {
         const double d = A.diag[c];
-        inv[c] = d > 0.0 ? T(1.0 / d) : T(0);
+        inv[c] = d > 0.0 ? recip<T>(d) : T(0);
         if (copy) {
             diag[c] = T(d);
             cx[c] = T(A.cx[c]);
@@ -130,7 +138,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) mg_coarsen_kernel(MgLevel<T>
         // dropped from the coarse problem: it is a floating Neumann pocket
         const bool active = d > 1e-12 * (ex + ey + ez + 1e-300);
         cdiag[cc] = T(active ? d : 0.0);
-        cinv[cc] = active ? T(1.0 / d) : T(0);
+        cinv[cc] = active ? recip<T>(d) : T(0);
         ccx[cc] = T(ex);
         ccy[cc] = T(ey);
         if (fg.dim == 3) ccz[cc] = T(ez);

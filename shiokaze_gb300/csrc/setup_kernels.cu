@@ -80,7 +80,35 @@ struct FaceParams {
     int dx_pow2;
     double inv_dx, inv_dx2;
     double w_unit;  // dt*1/(dx*dx*1), the weight of a face with area = rho = 1 (host-evaluated)
+    int inv_dx_exp;  // 1/dx = 2^inv_dx_exp when dx_pow2
+    double dt_inv_dx;  // dt * (1/dx), exact when dx_pow2
+    // eps_solid <= 1 (eps_fluid <= 1): a fraction of exactly 0 or 1 is never
+    // clamped, so uniform faces skip the FP64 clamp and conversion
+    int eps_solid_le1, eps_fluid_le1;
 };
+
+// (double)u * 2^e for a float u, built from u's bits with integer
+// instructions (exact: the product of a float and a power of two is a
+// double with u's mantissa and a shifted exponent). ok = false for
+// subnormal, infinite and NaN u, and for exponents out of range; the
+// caller then takes the FP64 path.
+__device__ __forceinline__ double scaled_to_double(float u, int e, bool &ok) {
+    const unsigned b = __float_as_uint(u);
+    const unsigned ex = (b >> 23) & 0xffu, man = b & 0x7fffffu;
+    const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
+    ok = true;
+    if (ex == 0u) {
+        if (man == 0u) return __longlong_as_double((long long)sign);  // +-0
+        ok = false;
+        return 0.0;
+    }
+    const int de = (int)ex + (1023 - 127) + e;
+    if (ex == 0xffu || de <= 0 || de >= 2047) {
+        ok = false;
+        return 0.0;
+    }
+    return __longlong_as_double((long long)(sign | ((unsigned long long)de << 52) | ((unsigned long long)man << 29)));
+}
 
 // x / dx, bit-identical either way (see FaceParams::dx_pow2)
 __device__ __forceinline__ double div_dx(double x, double dx, const FaceParams &fp) {
@@ -104,7 +132,7 @@ __device__ float face_area(const Grid &g, const float *__restrict__ solid, int d
     const int n[3] = {g.nx, g.ny, g.nz};
     double area;
     if (p[d] == 0 || p[d] == n[d]) {
-        area = 0.0;
+        return 0.0f;  // 0 is never clamped, and the first-order override keeps it
     } else if (g.dim == 3) {
         const long long sx = g.nx + 1, sxy = sx * (g.ny + 1);
         auto S = [&](int a, int b, int c) { return __ldg(solid + a + sx * b + sxy * c); };
@@ -116,10 +144,16 @@ __device__ float face_area(const Grid &g, const float *__restrict__ solid, int d
         } else {
             q00 = S(i, j, k); q10 = S(i + 1, j, k); q11 = S(i + 1, j + 1, k); q01 = S(i, j + 1, k);
         }
-        // uniform squares decided in float (the same comparisons as in double)
-        if (q00 >= 0.0f && q10 >= 0.0f && q11 >= 0.0f && q01 >= 0.0f) area = 1.0;
-        else if (q00 < 0.0f && q10 < 0.0f && q11 < 0.0f && q01 < 0.0f) area = 0.0;
-        else area = 1.0 - solid_area(q00, q10, q11, q01);
+        // uniform squares decided in float (the same comparisons as in double);
+        // their fraction (1 or 0) is final unless eps_solid exceeds 1
+        if (q00 >= 0.0f && q10 >= 0.0f && q11 >= 0.0f && q01 >= 0.0f) {
+            if (fp.eps_solid_le1) return 1.0f;
+            area = 1.0;
+        } else if (q00 < 0.0f && q10 < 0.0f && q11 < 0.0f && q01 < 0.0f) {
+            return 0.0f;
+        } else {
+            area = 1.0 - solid_area(q00, q10, q11, q01);
+        }
     } else {
         const long long sx = g.nx + 1;
         double s0 = __ldg(solid + i + sx * j);
@@ -150,8 +184,18 @@ __device__ float face_rho(const Grid &g, const float *__restrict__ fluid, int d,
         // product of two floats never underflows to 0, so its sign test
         // equals this float sign test.
         double rho;
-        if (!((f0 < 0.0f && f1 > 0.0f) || (f0 > 0.0f && f1 < 0.0f))) rho = (f0 < 0.0f || f1 < 0.0f) ? 1.0 : 0.0;
-        else rho = fraction(f0, f1);
+        if (!((f0 < 0.0f && f1 > 0.0f) || (f0 > 0.0f && f1 < 0.0f))) {
+            // 1 or 0, final unless eps_fluid exceeds 1
+            const bool wet = f0 < 0.0f || f1 < 0.0f;
+            if (!wet || fp.eps_fluid_le1) {
+                r = wet ? 1.0f : 0.0f;
+                if (!fp.second_order_fluid && r) r = 1.0f;
+                return r;
+            }
+            rho = 1.0;
+        } else {
+            rho = fraction(f0, f1);
+        }
         if (rho && rho < fp.eps_fluid) rho = fp.eps_fluid;
         r = (float)rho;
     }
@@ -428,7 +472,12 @@ __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt,
             const bool open = area && rho;
             fa.w[d][f] = !open ? -1.0 : (area == 1.0f && rho == 1.0f) ? fp.w_unit
                                                                         : face_weight(dt, (double)area, (double)rho, dx, fp);
-            fa.q[d][f] = area ? div_dx((double)area * (double)__ldg(vel[d] + f), dx, fp) : 0.0;
+            const float uf = __ldg(vel[d] + f);
+            double q = 0.0;
+            bool fast = false;
+            if (area == 1.0f && fp.dx_pow2) q = scaled_to_double(uf, fp.inv_dx_exp, fast);  // (1 * u) / dx, exactly
+            if (!fast) q = area ? div_dx((double)area * (double)uf, dx, fp) : 0.0;
+            fa.q[d][f] = q;
             fa.rho[d][f] = open ? rho : (area ? -1.0f : 0.0f);
         }
     }
@@ -538,8 +587,16 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_faces_kernel(Grid g, d
                 const float pc = __ldg(p + cell_index(g, i, j, k));
                 const float pm = __ldg(p + cell_index(g, m[0], m[1], m[2]));
                 const float dp = pc - pm;
-                const double val = rho == 1.0f ? div_dx(dt * (double)dp, dx, fp)
-                                               : dt * (double)dp / ((double)rho * dx);
+                double val;
+                if (rho == 1.0f && fp.dx_pow2) {
+                    // (dt dp) / dx with dx = 2^-e: the scaling commutes with the
+                    // rounding of the product, so (dt 2^e) dp is the same double
+                    bool ok;
+                    const double dpd = scaled_to_double(dp, 0, ok);
+                    val = fp.dt_inv_dx * (ok ? dpd : (double)dp);
+                } else {
+                    val = rho == 1.0f ? div_dx(dt * (double)dp, dx, fp) : dt * (double)dp / ((double)rho * dx);
+                }
                 out = vel[d][f] - (float)val;
             }
             vel[d][f] = out;
@@ -547,13 +604,18 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_faces_kernel(Grid g, d
     }
 }
 
-FaceParams face_params(const SetupParams &sp, double dx, double dt = 0.0) {
-    FaceParams fp{sp.eps_solid, sp.eps_fluid, sp.second_order_solid, sp.second_order_fluid, 0, 0.0, 0.0, 0.0};
+FaceParams face_params(const SetupParams &sp, double dx, double dt) {
+    FaceParams fp{sp.eps_solid, sp.eps_fluid, sp.second_order_solid, sp.second_order_fluid, 0, 0.0, 0.0, 0.0, 0, 0.0,
+                  0, 0};
+    fp.eps_solid_le1 = sp.eps_solid <= 1.0;
+    fp.eps_fluid_le1 = sp.eps_fluid <= 1.0;
     int e = 0;
     const double m = std::frexp(dx, &e);
     if (m == 0.5 && e > -500 && e < 500) {  // dx == 2^(e-1)
         fp.dx_pow2 = 1;
         fp.inv_dx = std::ldexp(1.0, 1 - e);
+        fp.inv_dx_exp = 1 - e;
+        fp.dt_inv_dx = dt * fp.inv_dx;  // a power-of-two scaling: exact
         fp.inv_dx2 = std::ldexp(1.0, 2 * (1 - e));
     }
     // the device's face_weight(dt, 1, 1, dx) evaluated here with the same
@@ -570,7 +632,7 @@ cudaError_t launch_assemble(const Grid &g, double dt, double dx, const SetupPara
                             const float *fluid, const float *u, const float *v, const float *w, double *diag,
                             double *cx, double *cy, double *cz, double *b, Scalars *sc, int grid_blocks,
                             cudaStream_t stream) {
-    const FaceParams fp = face_params(sp, dx);
+    const FaceParams fp = face_params(sp, dx, dt);
     int blocks = (int)(g.ntiles < grid_blocks ? g.ntiles : grid_blocks);
     if (blocks < 1) blocks = 1;
     assemble_kernel<<<blocks, BLOCK_THREADS, 0, stream>>>(g, dt, dx, fp, sp.rhs_correct, solid, fluid, u, v, w, diag,
@@ -615,7 +677,7 @@ cudaError_t launch_assemble_faces(const Grid &g, const SetupParams &sp, const fl
 cudaError_t launch_velocity_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *p,
                                   FaceArrays fa, float *u, float *v, float *w, const Scalars *sc, int grid_blocks,
                                   cudaStream_t stream) {
-    const FaceParams fp = face_params(sp, dx);
+    const FaceParams fp = face_params(sp, dx, dt);
     velocity_faces_kernel<<<node_blocks(g, grid_blocks), BLOCK_THREADS, 0, stream>>>(g, dt, dx, fp, p, fa, u, v, w, sc);
     return cudaGetLastError();
 }
@@ -632,7 +694,7 @@ cudaError_t launch_pressure(const Grid &g, const double *diag, const double *x, 
 cudaError_t launch_velocity(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
                             const float *fluid, const float *p, float *u, float *v, float *w, const Scalars *sc,
                             int grid_blocks, cudaStream_t stream) {
-    const FaceParams fp = face_params(sp, dx);
+    const FaceParams fp = face_params(sp, dx, dt);
     long long total = (long long)(g.nx + 1) * (g.ny + 1) * (g.dim == 3 ? g.nz + 1 : 1);
     long long need = (total + BLOCK_THREADS - 1) / BLOCK_THREADS;
     int blocks = (int)(need < grid_blocks ? need : grid_blocks);

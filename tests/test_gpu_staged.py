@@ -1,9 +1,9 @@
 """TMA-staged fine-level kernels (FP32 MGPCG) against the direct-load kernels.
 
-A fine level is staged when it is 3D with 4-plane tiles (more than 2^21
-cells) and nx is a multiple of 8; TMAStaging=1 stages every pass there
-(the default, 1, keeps each pass in whichever form measures faster). The staged kernels compute each cell with
-the same arithmetic as the direct-load ones; a solve differs only through
+A fine level is staged (TMAStaging=1; the default, 0, uses the direct-load
+kernels) when it is 3D with 4-plane tiles (more than 2^21 cells) and nx is
+a multiple of 8. The staged kernels compute each cell with the same
+arithmetic as the direct-load ones; a solve differs only through
 the grouping of its dot-product partials (the staged launch runs one block
 per SM), so the two solves agree to the last digits and take the same
 number of iterations.
