@@ -79,6 +79,53 @@ def dist_info():
     return rank, world, local
 
 
+class Ranks:
+    """The ranks of one bench run, one process per GPU (torchrun env).
+
+    Each rank projects its own replica of the workload: the projection has
+    no exchange step between GPUs, so no collective touches the data path.
+    The timed region is bracketed by barriers on every rank, the job's time
+    is the slowest rank's (all_reduce MAX) and the job's rate is the units
+    all ranks processed over that time. backend "nccl" runs on the GPUs;
+    "gloo" runs the same logic on CPU processes."""
+
+    def __init__(self, backend="nccl", device=None):
+        self.rank, self.world, self.local = dist_info()
+        self.backend = backend
+        self.device = device
+        if self.world > 1:
+            import torch.distributed as dist
+            if backend == "nccl":
+                dist.init_process_group("nccl", device_id=device)
+            else:
+                dist.init_process_group(backend)
+
+    def barrier(self):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max_ms(self, ms):
+        """The slowest rank's time; every rank must call it."""
+        if self.world <= 1:
+            return float(ms)
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(ms)], dtype=torch.float64,
+                         device=self.device if self.backend == "nccl" else "cpu")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def rate(self, units_per_rank, ms):
+        """Whole-job units/s: all ranks' units over the slowest rank's time."""
+        return self.world * units_per_rank / (self.max_ms(ms) / 1000.0)
+
+    def close(self):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
 class ClockSampler:
     """Samples SM clocks and throttle reasons with nvidia-smi while running."""
 
@@ -166,7 +213,7 @@ def cpu_baseline(scene, solver_desc):
             "seconds_per_solve": dt, "iterations": r.iterations}
 
 
-def _measure(gb, torch, pj, ctx, scene, dev_arrays, stream, steps, warmup, sampler=None):
+def _measure(gb, torch, pj, ctx, scene, dev_arrays, stream, steps, warmup, ranks, sampler=None):
     """Times `steps` projections (after `warmup`) with CUDA events on the
     projection's stream; the velocity is reset from a device copy first."""
     solid, fluid, comps, comps0, p = dev_arrays
@@ -183,9 +230,7 @@ def _measure(gb, torch, pj, ctx, scene, dev_arrays, stream, steps, warmup, sampl
         for _ in range(warmup):
             step()
     torch.cuda.synchronize()
-    _, world, _ = dist_info()
-    if world > 1:
-        torch.distributed.barrier()
+    ranks.barrier()
     if sampler:
         sampler.start()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
@@ -197,8 +242,7 @@ def _measure(gb, torch, pj, ctx, scene, dev_arrays, stream, steps, warmup, sampl
             step()
             ev[k + 1].record(stream)
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    ranks.barrier()
     clocks = sampler.stop() if sampler else None
     per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
     return {"total_ms": ev[0].elapsed_time(ev[-1]), "per_step": per_step, "launches": ctx.launches() - l0,
@@ -210,9 +254,7 @@ def run_gbp(args):
     import shiokaze_gb300 as gb
 
     rank, world, local = dist_info()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ranks = Ranks("nccl", torch.device("cuda", local))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     scene = make_scene(args.workload)
@@ -232,14 +274,10 @@ def run_gbp(args):
 
     cfg = dict(Residual=1e-6, Solver=args.solver, Precision=args.precision)
     pj = gb.projector_for(scene, ctx, **cfg)
-    main = _measure(gb, torch, pj, ctx, scene, arrays, stream, args.steps, args.warmup, ClockSampler(local))
+    main = _measure(gb, torch, pj, ctx, scene, arrays, stream, args.steps, args.warmup, ranks, ClockSampler(local))
     stats = main["stats"]
-    total_ms = main["total_ms"]
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps / (total_ms / 1000.0)
+    total_ms = ranks.max_ms(main["total_ms"])
+    value = ranks.rate(args.steps, total_ms)
 
     # the other GPU paths on the same scene, for comparison (fewer steps)
     compare = {}
@@ -249,7 +287,7 @@ def run_gbp(args):
                 continue
             other = gb.projector_for(scene, ctx, Residual=1e-6, Solver=solver, Precision=precision)
             nsteps = 3 if solver == "cg" else max(3, args.steps // 2)
-            m = _measure(gb, torch, other, ctx, scene, arrays, stream, nsteps, 3)
+            m = _measure(gb, torch, other, ctx, scene, arrays, stream, nsteps, 3, ranks)
             ms = m["total_ms"] / nsteps
             compare[f"{solver}_{precision}"] = {
                 "solves_per_s": round(1000.0 / ms, 3), "ms_per_step": round(ms, 4),
@@ -280,12 +318,8 @@ def run_gbp(args):
     face_bytes = sum(a.nbytes for a in h0)
     h2d = scene.solid.nbytes + scene.fluid.nbytes + face_bytes
     d2h = face_bytes + scene.fluid.nbytes
-    e2e_total = sum(e2e_times)
-    if world > 1:
-        t = torch.tensor([e2e_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = world * len(e2e_times) / e2e_total
+    ranks.barrier()
+    e2e_value = ranks.rate(len(e2e_times), 1000.0 * sum(e2e_times))
 
     # roofline: the path's fine-level kernels timed alone, each launched once
     # per iteration; the slowest is the dominant one
@@ -340,8 +374,7 @@ def run_gbp(args):
         out["cpu_baseline"] = cpu_baseline(scene, args.solver)
     if rank == 0:
         print(json.dumps(out), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    ranks.close()
 
 
 def run_gbp_batch(args):
@@ -351,9 +384,7 @@ def run_gbp_batch(args):
     from shiokaze_gb300 import scenes as scn
 
     rank, world, local = dist_info()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ranks = Ranks("nccl", torch.device("cuda", local))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     scs = scn.batch_liquid3(WORKLOADS[args.workload]["n"], seed=4)
@@ -388,6 +419,7 @@ def run_gbp_batch(args):
             for _ in range(warmup):
                 step()
         torch.cuda.synchronize()
+        ranks.barrier()
         if sampler:
             sampler.start()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
@@ -398,14 +430,15 @@ def run_gbp_batch(args):
                 step()
                 ev[k + 1].record(stream)
         torch.cuda.synchronize()
+        ranks.barrier()
         clocks = sampler.stop() if sampler else None
         per = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
-        return ev[0].elapsed_time(ev[-1]), per, ctx.launches() - l0, clocks
+        return ranks.max_ms(ev[0].elapsed_time(ev[-1])), per, ctx.launches() - l0, clocks
 
     pjs, batch = make(args.precision)
     total_ms, per, launches, clocks = measure(batch, args.steps, args.warmup, ClockSampler(local))
     iters = [batch.stats[i].iterations for i in range(len(scs))]
-    value = world * len(scs) * args.steps / (total_ms / 1000.0)
+    value = ranks.rate(len(scs) * args.steps, total_ms)
     compare = {}
     if not args.no_compare:
         other = "fp64" if args.precision == "mixed" else "mixed"
@@ -442,8 +475,7 @@ def run_gbp_batch(args):
     }
     if rank == 0:
         print(json.dumps(out), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    ranks.close()
 
 
 def run_gbp_served(args):
@@ -453,6 +485,7 @@ def run_gbp_served(args):
     from shiokaze_gb300.serving import ProjectionServer, poisson_requests
 
     rank, world, local = dist_info()
+    ranks = Ranks("nccl", torch.device("cuda", local))
     torch.cuda.set_device(local)
     nreq = max(4, args.steps)
     results = {}
@@ -466,15 +499,17 @@ def run_gbp_served(args):
         if precision == args.precision:
             sampler.start()
         torch.cuda.synchronize()
+        ranks.barrier()
         l0 = srv.ctx.launches()
         done, out = srv.serve(reqs)
         torch.cuda.synchronize()
+        ranks.barrier()
         out["gpu_launches"] = srv.ctx.launches() - l0
         if precision == args.precision:
             out["clocks"] = sampler.stop()
         results[precision] = out
     main = results[args.precision]
-    value = world * main["solves_per_s"]
+    value = ranks.rate(main["solves"], 1000.0 * main["wall_s"])
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": "solves/s", "n_gpus": world, "steps": nreq,
         "warmup": args.warmup, "ms_per_step": round(1000.0 / main["solves_per_s"], 4), "higher_is_better": True,
@@ -493,6 +528,7 @@ def run_gbp_served(args):
     }
     if rank == 0:
         print(json.dumps(out), flush=True)
+    ranks.close()
 
 
 def run_reference(args):
