@@ -90,6 +90,10 @@ typedef struct gbp_params {
                                tiles staged in shared memory by TMA where the grid allows it (3D, more than
                                2^21 cells, nx % 8 == 0); 0 (default) uses the direct-load kernels, which
                                compute every cell alike and measure faster over a whole solve on GB300 */
+    int tile_classes;       /* MGPCG: nonzero (default) lets the multigrid and CG kernels use the tile classes of
+                               each level: in the FP32 kernels a tile whose couplings all share one value reads
+                               that value instead of the coupling arrays, and a tile with no unknown writes zeros
+                               without loading; the results equal those with 0, which reads every array */
 } gbp_params;
 
 typedef struct gbp_stats {

@@ -14,7 +14,7 @@ Configuration keys are the reference's (``Residual``, ``MaxIterations``,
 ``SecondOrderAccurateSolid``, ``Gain``) plus this module's own
 (``Solver`` = "cg" | "mgpcg", ``Precision`` = "fp64" | "mixed",
 ``MGSmooth``, ``MGCoarsest``, ``InnerTolerance``, ``IterationsPerSync``,
-``TMAStaging``), and
+``TMAStaging``, ``TileClasses``), and
 ``SurfaceTension``, the value the reference passes as project()'s
 surface_tension argument.
 
@@ -46,7 +46,7 @@ class Params(ctypes.Structure):
                 ("gain", ctypes.c_double), ("solver", ctypes.c_int), ("precision", ctypes.c_int),
                 ("mg_smooth", ctypes.c_int), ("mg_coarsest", ctypes.c_int), ("inner_tolerance", ctypes.c_double),
                 ("iterations_per_sync", ctypes.c_int), ("surface_tension", ctypes.c_double),
-                ("tma_staging", ctypes.c_int)]
+                ("tma_staging", ctypes.c_int), ("tile_classes", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -136,6 +136,7 @@ _KEYMAP = {
     "Gain": ("gain", float), "MGSmooth": ("mg_smooth", int), "MGCoarsest": ("mg_coarsest", int),
     "InnerTolerance": ("inner_tolerance", float), "IterationsPerSync": ("iterations_per_sync", int),
     "SurfaceTension": ("surface_tension", float), "TMAStaging": ("tma_staging", int),
+    "TileClasses": ("tile_classes", int),
 }
 
 

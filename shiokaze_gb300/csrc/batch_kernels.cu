@@ -142,6 +142,63 @@ template <class B> __device__ __forceinline__ void with_vec(int vec, B body) {
     if (vec) body(std::true_type{});
     else body(std::false_type{});
 }
+// body(V, U) with V as in with_vec and U = uniform couplings (tile class
+// >= 0): each combination is its own straight-line code, so no load waits
+// behind a branch on the class.
+template <class B> __device__ __forceinline__ void with_vu(int vec, bool uni, B body) {
+    if (vec) {
+        if (uni) body(std::true_type{}, std::true_type{});
+        else body(std::true_type{}, std::false_type{});
+    } else {
+        if (uni) body(std::false_type{}, std::true_type{});
+        else body(std::false_type{}, std::false_type{});
+    }
+}
+
+// The couplings a stencil reads: the level's arrays, or (u >= 0) the one
+// value that every coupling of the current tile has (its tile class).
+template <class T> struct Cpl {
+    const T *cx, *cy, *cz;
+    T u;
+};
+
+// The class of an item's tile (TILE_MIXED for items of several tiles, or
+// without classes).
+template <class T> __device__ __forceinline__ T item_class(const T *cls, const BItem &it) {
+    return (cls != nullptr && it.ntiles == 1) ? __ldg(cls + it.tile) : T(TILE_MIXED);
+}
+// Class tests on the bit pattern (integer compares: no FP64 instruction,
+// which this GPU issues at a small fraction of its FP32 rate).
+__device__ __forceinline__ long long class_bits(double u) { return __double_as_longlong(u); }
+__device__ __forceinline__ long long class_bits(float u) { return __float_as_int(u); }
+template <class T> __device__ __forceinline__ bool tile_empty(T u) { return class_bits(u) == class_bits(T(TILE_EMPTY)); }
+// Uniform tiles take the coupling-free path in FP32 only: the FP64 kernels
+// are bound by the FP64 pipe, not by loads, and measure faster reading the
+// couplings (empty tiles are skipped in both).
+template <class T> __device__ __forceinline__ bool tile_uniform(T u) {
+    return sizeof(T) == 4 && class_bits(u) >= 0;
+}
+
+// The class of item w of a list (TILE_MIXED past the end), with R the
+// restriction tiling. Kernels load the class of the block's next item
+// (w + G) while item w runs, so no stencil load waits on a class; `seg` is
+// a copy of the caller's segment cursor.
+template <class T, bool R>
+__device__ __forceinline__ T class_at(const BLevel<T> *levels, const BSeg *segs, int nseg, int n, int w, int seg) {
+    if (w >= n) return T(TILE_MIXED);
+    const BItem it = item_at(segs, nseg, w, seg);
+    return item_class(R ? levels[it.ref].tcr : levels[it.ref].tcp, it);
+}
+// The same for the block's next item, with the current item's level `ref`
+// and class array (from the shared descriptors), used when the next item
+// is of the same level (the common case: one global load instead of two).
+template <class T, bool R>
+__device__ __forceinline__ T class_next(const BLevel<T> *levels, const BSeg *segs, int nseg, int n, int w, int seg,
+                                        int ref, const T *cls) {
+    if (w >= n) return T(TILE_MIXED);
+    const BItem it = item_at(segs, nseg, w, seg);
+    return item_class(it.ref == ref ? cls : (R ? levels[it.ref].tcr : levels[it.ref].tcp), it);
+}
 
 // Neighbour sums of the pair (i, i+1) at c = index of cell i:
 //   s.a = sum over the neighbours f of cell i of c_f v_f, s.b for cell i+1,
@@ -150,29 +207,39 @@ template <class B> __device__ __forceinline__ void with_vec(int vec, B body) {
 // dead code. `own` holds the pair's own values (each cell is the other's x
 // neighbour); nb2(c', j', k', second) gives the neighbour pair at c' (row
 // j', plane k'; its second cell exists exactly when the pair's does),
-// nb1(c', i') one cell of the same row outside the pair.
-template <class T, bool V, int W, class NB2, class NB1>
-__device__ __forceinline__ Pair<T> pair_nsum(const Grid &g, const T *cx, const T *cy, const T *cz, int i, int j, int k,
-                                              long long c, bool second, Pair<T> own, NB2 nb2, NB1 nb1) {
+// nb1(c', i') one cell of the same row outside the pair. U: the tile's
+// couplings all equal w.u, which replaces the coupling loads (the same
+// products in the same order).
+template <class T, bool V, bool U, int W, class NB2, class NB1>
+__device__ __forceinline__ Pair<T> pair_nsum(const Grid &g, const Cpl<T> &w, int i, int j, int k, long long c,
+                                              bool second, Pair<T> own, NB2 nb2, NB1 nb1) {
     constexpr bool A = W != 1, B = W != 0;
     const long long sy = g.nx, sz = (long long)g.nx * g.ny;
     Pair<T> s{T(0), T(0)};
-    const Pair<T> cxp = ld2<T, V>(cx, c, second);  // faces (i|i+1), (i+1|i+2)
-    if (A && i > 0) s.a += __ldg(cx + c - 1) * nb1(c - 1, i - 1);
+    auto cw2 = [&](const T *a, long long m) {
+        if constexpr (U) return Pair<T>{w.u, w.u};
+        else return ld2<T, V>(a, m, second);
+    };
+    auto cw1 = [&](const T *a, long long m) {
+        if constexpr (U) return w.u;
+        else return __ldg(a + m);
+    };
+    const Pair<T> cxp = cw2(w.cx, c);  // faces (i|i+1), (i+1|i+2)
+    if (A && i > 0) s.a += cw1(w.cx, c - 1) * nb1(c - 1, i - 1);
     if (second) {
         if (A) s.a += cxp.a * own.b;
         if (B) s.b += cxp.a * own.a;
         if (B && i + 2 < g.nx) s.b += cxp.b * nb1(c + 2, i + 2);
     }
-    auto add = [&](const Pair<T> &w, const Pair<T> &v) {
-        if (A) s.a += w.a * v.a;
-        if (B) s.b += w.b * v.b;
+    auto add = [&](const Pair<T> &cw, const Pair<T> &v) {
+        if (A) s.a += cw.a * v.a;
+        if (B) s.b += cw.b * v.b;
     };
-    if (j > 0) add(ld2<T, V>(cy, c - sy, second), nb2(c - sy, j - 1, k, second));
-    if (j + 1 < g.ny) add(ld2<T, V>(cy, c, second), nb2(c + sy, j + 1, k, second));
+    if (j > 0) add(cw2(w.cy, c - sy), nb2(c - sy, j - 1, k, second));
+    if (j + 1 < g.ny) add(cw2(w.cy, c), nb2(c + sy, j + 1, k, second));
     if (g.dim == 3) {
-        if (k > 0) add(ld2<T, V>(cz, c - sz, second), nb2(c - sz, j, k - 1, second));
-        if (k + 1 < g.nz) add(ld2<T, V>(cz, c, second), nb2(c + sz, j, k + 1, second));
+        if (k > 0) add(cw2(w.cz, c - sz), nb2(c - sz, j, k - 1, second));
+        if (k + 1 < g.nz) add(cw2(w.cz, c), nb2(c + sz, j, k + 1, second));
     }
     return s;
 }
@@ -180,11 +247,11 @@ __device__ __forceinline__ Pair<T> pair_nsum(const Grid &g, const T *cx, const T
 // The neighbour sum of one cell h (0: i, 1: i+1) of the pair. h is uniform
 // across a warp (a warp holds one row of pairs, i even, so the colour of
 // cell i is that of j + k), so the branch does not diverge.
-template <class T, bool V, class NB2, class NB1>
-__device__ __forceinline__ T pair_nsum1(int h, const Grid &g, const T *cx, const T *cy, const T *cz, int i, int j,
-                                        int k, long long c, bool second, Pair<T> own, NB2 nb2, NB1 nb1) {
-    if (h == 0) return pair_nsum<T, V, 0>(g, cx, cy, cz, i, j, k, c, second, own, nb2, nb1).a;
-    return pair_nsum<T, V, 1>(g, cx, cy, cz, i, j, k, c, second, own, nb2, nb1).b;
+template <class T, bool V, bool U, class NB2, class NB1>
+__device__ __forceinline__ T pair_nsum1(int h, const Grid &g, const Cpl<T> &w, int i, int j, int k, long long c,
+                                        bool second, Pair<T> own, NB2 nb2, NB1 nb1) {
+    if (h == 0) return pair_nsum<T, V, U, 0>(g, w, i, j, k, c, second, own, nb2, nb1).a;
+    return pair_nsum<T, V, U, 1>(g, w, i, j, k, c, second, own, nb2, nb1).b;
 }
 
 // The level and scene of the current item, held in shared memory and
@@ -224,7 +291,7 @@ __device__ __forceinline__ void refresh(ItemCtx<T> &c, int &cur_ref, const BItem
 // (b - begin) mod gridDim.x of that range; min(count, gridDim.x) blocks
 // flush per scene, and the one taking the scene's last ticket combines the
 // slots in slot order (deterministic for a given batch and grid).
-template <class T, class Acc, class Body, class Finish>
+template <class T, class Acc, bool CLASSES = true, class Body, class Finish>
 __device__ __forceinline__ void reduce_items(const BSeg *__restrict__ segs, int nseg, int n, double *part,
                                              const BLevel<T> *levels, const BScene<T> *scenes, int gate,
                                              ItemCtx<T> &ctx, Body body, Finish finish) {
@@ -240,8 +307,10 @@ __device__ __forceinline__ void reduce_items(const BSeg *__restrict__ segs, int 
         finish(first, min(first.count, B));
     };
     int sgc = 0;
+    T cls_next = CLASSES ? class_at<T, false>(levels, segs, nseg, n, blockIdx.x, 0) : T(TILE_MIXED);
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const BItem it = item_at(segs, nseg, w, sgc);
+        const T cls = cls_next;
         if (it.ref != cur) {
             // one level per scene in a list: a new level is a new scene
             if (cur >= 0 && !ctx.skip) flush();
@@ -249,7 +318,8 @@ __device__ __forceinline__ void reduce_items(const BSeg *__restrict__ segs, int 
             first = it;
             acc.reset();
         }
-        if (!ctx.skip) body(it, acc);
+        if (CLASSES) cls_next = class_next<T, false>(levels, segs, nseg, n, w + gridDim.x, sgc, it.ref, ctx.L.tcp);
+        if (!ctx.skip) body(it, acc, cls);
     }
     if (cur >= 0 && !ctx.skip) flush();
 }
@@ -334,13 +404,24 @@ __device__ __forceinline__ void presmooth_items(const BLevel<T> *__restrict__ le
         int n, const BScene<T> *__restrict__ scenes, int gate, ItemCtx<T> &ctx) {
     int cur = -1;
     int sgc = 0;
+    T cls_next = class_at<T, false>(levels, segs, nseg, n, blockIdx.x, 0);
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const BItem it = item_at(segs, nseg, w, sgc);
+        const T cls = cls_next;
         refresh(ctx, cur, it, levels, scenes, gate);
+        cls_next = class_next<T, false>(levels, segs, nseg, n, w + gridDim.x, sgc, it.ref, ctx.L.tcp);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
-        with_vec(L.vec, [&](auto vt) {
+        const Cpl<T> cw{L.cx, L.cy, L.cz, cls};
+        with_vu(L.vec, tile_uniform(cw.u), [&](auto vt, auto ut) {
             constexpr bool V = decltype(vt)::value;
+            constexpr bool U = decltype(ut)::value;
+            if (tile_empty(cw.u)) {  // no unknown: x = 0
+                pair_tile(L.g, it, [&](int, int, int, long long c, bool second) {
+                    st2<T, V>(L.x, c, Pair<T>{T(0), T(0)}, second);
+                });
+                return;
+            }
             auto nb2 = [&](long long m, int, int, bool sec) {
                 const Pair<T> bb = ld2<T, V>(L.b, m, sec), ii = ld2<T, V>(L.inv, m, sec);
                 return Pair<T>{bb.a * ii.a, bb.b * ii.b};
@@ -353,10 +434,10 @@ __device__ __forceinline__ void presmooth_items(const BLevel<T> *__restrict__ le
                 Pair<T> out = red;
                 if (a_red) {
                     if (second)
-                        out.b = (b2.b + pair_nsum1<T, V>(1, L.g, L.cx, L.cy, L.cz, i, j, k, c, second, red, nb2, nb1)) *
+                        out.b = (b2.b + pair_nsum1<T, V, U>(1, L.g, cw, i, j, k, c, second, red, nb2, nb1)) *
                                 iv.b;
                 } else {
-                    out.a = (b2.a + pair_nsum1<T, V>(0, L.g, L.cx, L.cy, L.cz, i, j, k, c, second, red, nb2, nb1)) *
+                    out.a = (b2.a + pair_nsum1<T, V, U>(0, L.g, cw, i, j, k, c, second, red, nb2, nb1)) *
                             iv.a;
                 }
                 st2<T, V>(L.x, c, out, second);
@@ -381,20 +462,26 @@ __device__ __forceinline__ void sweep_items(const BLevel<T> *__restrict__ levels
         int n, const BScene<T> *__restrict__ scenes, int gate, int color, ItemCtx<T> &ctx) {
     int cur = -1;
     int sgc = 0;
+    T cls_next = class_at<T, false>(levels, segs, nseg, n, blockIdx.x, 0);
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const BItem it = item_at(segs, nseg, w, sgc);
+        const T cls = cls_next;
         refresh(ctx, cur, it, levels, scenes, gate);
+        cls_next = class_next<T, false>(levels, segs, nseg, n, w + gridDim.x, sgc, it.ref, ctx.L.tcp);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
-        with_vec(L.vec, [&](auto vt) {
+        const Cpl<T> cw{L.cx, L.cy, L.cz, cls};
+        if (tile_empty(cw.u)) continue;  // x stays 0 (written by the presmoothing)
+        with_vu(L.vec, tile_uniform(cw.u), [&](auto vt, auto ut) {
             constexpr bool V = decltype(vt)::value;
+            constexpr bool U = decltype(ut)::value;
             auto nb2 = [&](long long m, int, int, bool sec) { return ld2<T, V>(L.x, m, sec); };
             auto nb1 = [&](long long m, int) { return __ldg(L.x + m); };
             pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
                 const int h = ((i + j + k) & 1) == color ? 0 : 1;
                 if (h == 1 && !second) return;
                 const Pair<T> x2 = ld2<T, V>(L.x, c, second);
-                const T sh = pair_nsum1<T, V>(h, L.g, L.cx, L.cy, L.cz, i, j, k, c, second, x2, nb2, nb1);
+                const T sh = pair_nsum1<T, V, U>(h, L.g, cw, i, j, k, c, second, x2, nb2, nb1);
                 const long long ch = c + h;
                 L.x[ch] = (__ldg(L.b + ch) + sh) * __ldg(L.inv + ch);
             });
@@ -419,13 +506,22 @@ __device__ __forceinline__ void restrict_items(const BLevel<T> *__restrict__ lev
         int n, const BScene<T> *__restrict__ scenes, int gate, ItemCtx<T> &ctx) {
     int cur = -1;
     int sgc = 0;
+    T cls_next = class_at<T, true>(levels, segs, nseg, n, blockIdx.x, 0);
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const BItem it = item_at(segs, nseg, w, sgc);
+        const T cls = cls_next;
         refresh(ctx, cur, it, levels, scenes, gate);
+        cls_next = class_next<T, true>(levels, segs, nseg, n, w + gridDim.x, sgc, it.ref, ctx.L.tcr);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
-        with_vec(L.vec, [&](auto vt) {
+        const Cpl<T> cw{L.cx, L.cy, L.cz, cls};
+        if (tile_empty(cw.u)) {  // no unknown among the children: b_c = 0
+            cell_tile(L.gc, it, [&](int, int, int, long long cc) { L.bc[cc] = T(0); });
+            continue;
+        }
+        with_vu(L.vec, tile_uniform(cw.u), [&](auto vt, auto ut) {
             constexpr bool V = decltype(vt)::value;
+            constexpr bool U = decltype(ut)::value;
             const Grid &fg = L.g;
             auto nb2 = [&](long long m, int, int, bool sec) { return ld2<T, V>(L.x, m, sec); };
             auto nb1 = [&](long long m, int) { return __ldg(L.x + m); };
@@ -440,7 +536,7 @@ __device__ __forceinline__ void restrict_items(const BLevel<T> *__restrict__ lev
                         if (j >= fg.ny || k >= fg.nz) continue;
                         const long long f = cell_index(fg, i, j, k);
                         const Pair<T> x2 = ld2<T, V>(L.x, f, second);
-                        const Pair<T> s = pair_nsum<T, V, 2>(fg, L.cx, L.cy, L.cz, i, j, k, f, second, x2, nb2, nb1);
+                        const Pair<T> s = pair_nsum<T, V, U, 2>(fg, cw, i, j, k, f, second, x2, nb2, nb1);
                         const Pair<T> bb = ld2<T, V>(L.b, f, second), dd = ld2<T, V>(L.diag, f, second);
                         sum += bb.a - (dd.a * x2.a - s.a);
                         if (second) sum += bb.b - (dd.b * x2.b - s.b);
@@ -468,13 +564,19 @@ __device__ __forceinline__ void post_black_items(const BLevel<T> *__restrict__ l
         int n, const BScene<T> *__restrict__ scenes, int gate, T alpha, ItemCtx<T> &ctx) {
     int cur = -1;
     int sgc = 0;
+    T cls_next = class_at<T, false>(levels, segs, nseg, n, blockIdx.x, 0);
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const BItem it = item_at(segs, nseg, w, sgc);
+        const T cls = cls_next;
         refresh(ctx, cur, it, levels, scenes, gate);
+        cls_next = class_next<T, false>(levels, segs, nseg, n, w + gridDim.x, sgc, it.ref, ctx.L.tcp);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
-        with_vec(L.vec, [&](auto vt) {
+        const Cpl<T> cw{L.cx, L.cy, L.cz, cls};
+        if (tile_empty(cw.u)) continue;  // x stays 0 (written by the presmoothing)
+        with_vu(L.vec, tile_uniform(cw.u), [&](auto vt, auto ut) {
             constexpr bool V = decltype(vt)::value;
+            constexpr bool U = decltype(ut)::value;
             const Grid &cg = L.gc;
             const bool d3 = L.g.dim == 3;
             const long long csy = cg.nx, csz = (long long)cg.nx * cg.ny;
@@ -496,7 +598,7 @@ __device__ __forceinline__ void post_black_items(const BLevel<T> *__restrict__ l
                 };
                 const Pair<T> x2 = ld2<T, V>(L.x, c, second);
                 const Pair<T> own{x2.a + alpha * pc, x2.b + alpha * pc};
-                const T sh = pair_nsum1<T, V>(h, L.g, L.cx, L.cy, L.cz, i, j, k, c, second, own, nb2, nb1);
+                const T sh = pair_nsum1<T, V, U>(h, L.g, cw, i, j, k, c, second, own, nb2, nb1);
                 const long long ch = c + h;
                 L.x[ch] = (__ldg(L.b + ch) + sh) * __ldg(L.inv + ch);
             });
@@ -604,10 +706,13 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     __shared__ ItemCtx<T> ctx;
     reduce_items<T, DotAcc<T>>(
         segs, nseg, n, part, levels, scenes, gate, ctx,
-        [&](const BItem &it, DotAcc<T> &acc) {
+        [&](const BItem &it, DotAcc<T> &acc, T cls) {
             const BLevel<T> &L = ctx.L;
-            with_vec(L.vec, [&](auto vt) {
+            const Cpl<T> cw{L.cx, L.cy, L.cz, cls};
+            if (tile_empty(cw.u)) return;  // z = 0 there: nothing to write or add
+            with_vu(L.vec, tile_uniform(cw.u), [&](auto vt, auto ut) {
                 constexpr bool V = decltype(vt)::value;
+                constexpr bool U = decltype(ut)::value;
                 auto nb2 = [&](long long m, int, int, bool sec) { return ld2<T, V>(L.x, m, sec); };
                 auto nb1 = [&](long long m, int) { return __ldg(L.x + m); };
                 pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
@@ -615,7 +720,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
                     const Pair<T> x2 = ld2<T, V>(L.x, c, second), b2 = ld2<T, V>(L.b, c, second);
                     Pair<T> out = x2;
                     if (hr == 0 || second) {
-                        const T sh = pair_nsum1<T, V>(hr, L.g, L.cx, L.cy, L.cz, i, j, k, c, second, x2, nb2, nb1);
+                        const T sh = pair_nsum1<T, V, U>(hr, L.g, cw, i, j, k, c, second, x2, nb2, nb1);
                         const long long ch = c + hr;
                         const T xv = ((hr ? b2.b : b2.a) + sh) * __ldg(L.inv + ch);
                         if (hr) out.b = xv;
@@ -854,15 +959,28 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     __shared__ ItemCtx<T> ctx;
     int cur = -1;
     int sgc = 0;
+    T cls_next = class_at<T, false>(levels, segs, nseg, n, blockIdx.x, 0);
     for (int w = blockIdx.x; w < n; w += gridDim.x) {
         const BItem it = item_at(segs, nseg, w, sgc);
+        const T cls = cls_next;
         refresh(ctx, cur, it, levels, scenes, gate);
+        cls_next = class_next<T, false>(levels, segs, nseg, n, w + gridDim.x, sgc, it.ref, ctx.L.tcp);
         if (ctx.skip) continue;
         const BLevel<T> &L = ctx.L;
         const BScene<T> &S = ctx.S;
         const T beta = T(ctx.beta);
+        const bool empty = tile_empty(cls);
+        // no unknown: p = 0, written when a direction starts (beta = 0) and
+        // unchanged after that
+        if (empty && beta != T(0)) continue;
         with_vec(L.vec, [&](auto vt) {
             constexpr bool V = decltype(vt)::value;
+            if (empty) {
+                pair_tile(L.g, it, [&](int, int, int, long long c, bool second) {
+                    st2<T, V>(S.p, c, Pair<T>{T(0), T(0)}, second);
+                });
+                return;
+            }
             pair_tile(L.g, it, [&](int, int, int, long long c, bool second) {
                 const Pair<T> z2 = ld2<T, V>(S.z, c, second);
                 Pair<T> p2;
@@ -888,16 +1006,21 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     __shared__ ItemCtx<T> ctx;
     reduce_items<T, DotAcc<T>>(
         segs, nseg, n, part, levels, scenes, gate, ctx,
-        [&](const BItem &it, DotAcc<T> &acc) {
+        [&](const BItem &it, DotAcc<T> &acc, T cls) {
             const BLevel<T> &L = ctx.L;
             const BScene<T> &S = ctx.S;
-            with_vec(L.vec, [&](auto vt) {
+            const Cpl<T> cw{L.cx, L.cy, L.cz, cls};
+            // no unknown: q = A p = 0 there, and q is read nowhere else (the
+            // update skips such tiles too)
+            if (tile_empty(cw.u)) return;
+            with_vu(L.vec, tile_uniform(cw.u), [&](auto vt, auto ut) {
                 constexpr bool V = decltype(vt)::value;
+                constexpr bool U = decltype(ut)::value;
                 auto nb2 = [&](long long m, int, int, bool sec) { return ld2<T, V>(S.p, m, sec); };
                 auto nb1 = [&](long long m, int) { return __ldg(S.p + m); };
                 pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
                     const Pair<T> p2 = ld2<T, V>(S.p, c, second), d2 = ld2<T, V>(L.diag, c, second);
-                    const Pair<T> s = pair_nsum<T, V, 2>(L.g, L.cx, L.cy, L.cz, i, j, k, c, second, p2, nb2, nb1);
+                    const Pair<T> s = pair_nsum<T, V, U, 2>(L.g, cw, i, j, k, c, second, p2, nb2, nb1);
                     const Pair<T> q2{d2.a * p2.a - s.a, d2.b * p2.b - s.b};
                     st2<T, V>(S.q, c, q2, second);
                     acc.add(p2.a, q2.a);
@@ -930,13 +1053,23 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     __shared__ ItemCtx<T> ctx;
     reduce_items<T, MaxAcc<T>>(
         segs, nseg, n, part, levels, scenes, gate, ctx,
-        [&](const BItem &it, MaxAcc<T> &acc) {
+        [&](const BItem &it, MaxAcc<T> &acc, T cls) {
             const BLevel<T> &L = ctx.L;
             const BScene<T> &S = ctx.S;
             const T alpha = T(ctx.alpha);
             const bool overwrite = ctx.overwrite != 0;
+            // no unknown: p = q = r = 0 there; x = 0 is written by the
+            // solve's first update and unchanged after that
+            const bool empty = tile_empty(cls);
+            if (empty && !overwrite) return;
             with_vec(L.vec, [&](auto vt) {
                 constexpr bool V = decltype(vt)::value;
+                if (empty) {
+                    pair_tile(L.g, it, [&](int, int, int, long long c, bool second) {
+                        st2<T, V>(S.x, c, Pair<T>{T(0), T(0)}, second);
+                    });
+                    return;
+                }
                 pair_tile(L.g, it, [&](int, int, int, long long c, bool second) {
                     const Pair<T> p2 = ld2<T, V>(S.p, c, second), q2 = ld2<T, V>(S.q, c, second);
                     const Pair<T> r2 = ld2<T, V>(S.r, c, second);
@@ -1040,9 +1173,9 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_res
     if (!initial && *(const volatile int *)&cnt->refine <= 0) return;
     __shared__ double shf[BLOCK_THREADS / 32];
     __shared__ ItemCtx<T> ctx;
-    reduce_items<T, MaxSumAcc>(
+    reduce_items<T, MaxSumAcc, false>(
         segs, nseg, n, part, levels, scenes, initial ? -1 : 2, ctx,
-        [&](const BItem &it, MaxSumAcc &acc) {
+        [&](const BItem &it, MaxSumAcc &acc, T) {
             const BLevel<T> &L = ctx.L;
             const BScene<T> &S = ctx.S;
             const Grid &g = L.g;

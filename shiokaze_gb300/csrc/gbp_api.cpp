@@ -92,6 +92,7 @@ void gbp_params_default(gbp_params *p) {
     p->iterations_per_sync = 16;
     p->surface_tension = 0.0;
     p->tma_staging = 0;
+    p->tile_classes = 1;
 }
 
 const char *gbp_strerror(int status) {
@@ -444,7 +445,7 @@ int gbp_batch_project_device(gbp_batch *b, const double *dt, const float *const 
     GBP_CUDA(cudaEventRecord(c->ev[1], st));
     // the batched solve
     const bool mixed = p.precision == GBP_PRECISION_MIXED;
-    long long key = (mixed ? 1 : 0) | (p.warm_start ? 2 : 0) | (p.tma_staging ? 4 : 0) |
+    long long key = (mixed ? 1 : 0) | (p.warm_start ? 2 : 0) | (p.tma_staging ? 4 : 0) | (p.tile_classes ? 0 : 8) |
                     ((long long)c->grid_blocks << 4) | ((long long)(p.mg_coarsest > 1 ? p.mg_coarsest : 4) << 24);
     for (int i = 0; i < n; ++i) key = key * 31 + (b->scenes[i]->solver->has_prev() ? 1 : 0);
     if (b->key != key) {

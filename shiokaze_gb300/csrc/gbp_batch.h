@@ -40,6 +40,8 @@ template <class T> struct BLevel {
     int vec;
     // TMA descriptors of a staged fine level (STAGE_MAPS of them), or null
     const CUtensorMap *tmap;
+    // tile classes (MgLevel::tcp, tcr), or null: every tile reads its arrays
+    const T *tcp, *tcr;
 };
 
 // Staged fine-level kernels: a pair tile of 64 x 8 x 4 cells and the halo

@@ -17,7 +17,21 @@ template <class T> struct MgLevel {
     Grid g;
     const T *diag, *inv, *cx, *cy, *cz;  // cz == cy in 2D (never read)
     T *b, *x;
+    // tile classes (mg_setup): one per pair tile of g (64 x 8 x tz cells,
+    // the smoothing and CG items) and one per cell tile of the next coarser
+    // grid (its 64 x 16 x 2tz fine cells, the restriction items); null on
+    // the coarsest level
+    T *tcp, *tcr;
 };
+
+// A tile class is the common value u >= 0 of every coupling that the
+// stencils of the tile's cells read (each in-grid face of each cell), so the
+// kernels use u instead of loading cx, cy, cz; TILE_MIXED if those
+// couplings differ; TILE_EMPTY if they are all 0 and no cell of the tile
+// has a nonzero diagonal (no unknown: every vector is 0 there). Couplings
+// are never negative, so the two markers cannot be taken for a value.
+constexpr double TILE_MIXED = -1.0;
+constexpr double TILE_EMPTY = -2.0;
 
 // Levels from `tail` down run in one single-block kernel from shared memory
 // (tail == nlevels: no such levels); tail_smem is the bytes it needs.

@@ -61,6 +61,9 @@ size_t solver_device_bytes(const Grid &g, const gbp_params &p) {
         // level 0: inverse diagonal (+ operator copy and 5 vectors in FP32)
         bytes += s * cells * (p.precision == GBP_PRECISION_MIXED ? 10 : 1);
         for (size_t l = 1; l < lv.size(); ++l) bytes += s * (size_t)lv[l].ncell * 7;
+        // tile classes (a value per tile; rounded up to whole allocations)
+        for (size_t l = 0; l + 1 < lv.size(); ++l)
+            bytes += s * (size_t)(((lv[l].nx + 63) / 64) * (long long)lv[l].nty * lv[l].ntz + lv[l + 1].ntiles) + 1024;
     }
     return bytes;
 }
@@ -70,6 +73,18 @@ template <class T> int Solver::alloc(T **p, size_t n) {
     SOLVER_CUDA(cudaMalloc(&d, sizeof(T) * (n ? n : 1)));
     owned_.push_back(d);
     *p = static_cast<T *>(d);
+    return GBP_OK;
+}
+
+// Tile-class arrays of every level that has a coarser one: one value per
+// pair tile of the level and per cell tile of the coarser grid.
+template <class T> int Solver::alloc_classes(MgHierarchy<T> &H) {
+    for (int l = 0; l + 1 < H.nlevels; ++l) {
+        MgLevel<T> &F = H.levels[l];
+        const Grid &C = H.levels[l + 1].g;
+        int rc = alloc(&F.tcp, (size_t)(((F.g.nx + 63) / 64) * (long long)F.g.nty * F.g.ntz));
+        if (rc || (rc = alloc(&F.tcr, (size_t)C.ntiles))) return rc;
+    }
     return GBP_OK;
 }
 
@@ -142,6 +157,7 @@ int Solver::prepare_mg(const Grid &g, const gbp_params &p) {
                 return rc;
             H.levels[l] = MgLevel<double>{lv[l], d, iv, x1, y1, lv[l].dim == 3 ? z1 : y1, b, x};
         }
+        if ((rc = alloc_classes(H))) return rc;
         mg_plan_tail(H);
         mg64_ready_ = true;
     }
@@ -166,6 +182,7 @@ int Solver::prepare_mg(const Grid &g, const gbp_params &p) {
             }
             H.levels[l] = MgLevel<float>{lv[l], d, iv, x1, y1, lv[l].dim == 3 ? z1 : y1, b, x};
         }
+        if ((rc = alloc_classes(H))) return rc;
         mg_plan_tail(H);
         mg32_ready_ = true;
     }
@@ -344,7 +361,8 @@ template <class T> void Solver::add_to_plan(BatchPlan<T> &plan, const gbp_params
         }
         if (l == 0) plan.fine_ref.push_back((int)plan.levels.size());
         plan.levels.push_back(
-            BLevel<T>{F.g, F.diag, F.inv, F.cx, F.cy, F.cz, F.b, F.x, C.x, C.b, C.g, s, vec ? 1 : 0, nullptr});
+            BLevel<T>{F.g, F.diag, F.inv, F.cx, F.cy, F.cz, F.b, F.x, C.x, C.b, C.g, s, vec ? 1 : 0, nullptr,
+                      p.tile_classes ? F.tcp : nullptr, p.tile_classes ? F.tcr : nullptr});
         plan.scene_of.push_back(s);
         auto add = [&](std::vector<BSeg> &list, int &items, long long tiles, long long cells_per_tile) {
             const int m = (int)std::max(1LL, BITEM_CELLS / cells_per_tile);
@@ -379,7 +397,7 @@ int Solver::solve_mg(const Grid &g, const gbp_params &p, int grid_blocks, cudaSt
     int rc = setup_mg(g, p, grid_blocks, stream, launches);
     if (rc) return rc;
     // a batch of one: the same kernels and reductions as a batched solve
-    const long long key = (mixed ? 1 : 0) | (warm ? 2 : 0) | (p.tma_staging ? 4 : 0) |
+    const long long key = (mixed ? 1 : 0) | (warm ? 2 : 0) | (p.tma_staging ? 4 : 0) | (p.tile_classes ? 0 : 8) |
                           ((long long)grid_blocks << 4) | ((long long)mg_coarsest_ << 24);
     if (runner_key_ != key) {
         if (mixed) {

@@ -75,6 +75,7 @@ private:
         return code;
     }
     template <class T> int alloc(T **p, size_t n);
+    template <class T> int alloc_classes(MgHierarchy<T> &H);
     int prepare_mg(const Grid &g, const gbp_params &p);
     int solve_cg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches);
     int solve_mg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches);

@@ -34,6 +34,8 @@
 //   direction        read z, p; write p                               3 s
 //   spmv             read p, diag, cx, cy, cz; write q                6 s
 //   update           read x, p, r, q; write x, r                      6 s
+#include <algorithm>
+
 #include "gbp_internal.cuh"
 #include "gbp_kernels.h"
 #include "gbp_mg.h"
@@ -145,6 +147,105 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) mg_coarsen_kernel(MgLevel<T>
     });
 }
 
+// Tile classes of level L (TILE_MIXED / TILE_EMPTY / the common coupling).
+// mode 0: box b is pair tile b of L.g (64 x 8 x tz cells); mode 1: box b
+// holds the fine cells of cell tile b of the coarser grid gc (64 x 16 x
+// 2 tz_c, a restriction item). A cell contributes its diagonal and the
+// coupling of each face whose neighbour is inside the grid, the ones the
+// stencils read. Values are compared through their bit patterns (integer
+// min and max: no FP64 instruction, and "uniform" means bitwise equal).
+template <class T> struct Bits;
+template <> struct Bits<float> {
+    using U = unsigned;
+    static __device__ U of(float v) { return __float_as_uint(v); }
+    static __device__ float value(U u) { return __uint_as_float(u); }
+};
+template <> struct Bits<double> {
+    using U = unsigned long long;
+    static __device__ U of(double v) { return (U)__double_as_longlong(v); }
+    static __device__ double value(U u) { return __longlong_as_double((long long)u); }
+};
+
+template <class T>
+__global__ void __launch_bounds__(BLOCK_THREADS) mg_classify_kernel(MgLevel<T> L, Grid gc, int mode, T *out,
+                                                                    long long nbox) {
+    using U = typename Bits<T>::U;
+    __shared__ U slo[BLOCK_THREADS / 32], shi[BLOCK_THREADS / 32];
+    __shared__ int sany[BLOCK_THREADS / 32];
+    const Grid &g = L.g;
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    // box extents: 64 x by x bz, by = 8 or 16 (log2 yb)
+    const int yb = mode == 0 ? 3 : 4;
+    const int bz = mode == 0 ? g.tz : (g.dim == 3 ? 2 * gc.tz : 1);
+    const int nb = (64 << yb) * bz;
+    for (long long b = blockIdx.x; b < nbox; b += gridDim.x) {
+        int i0, j0, k0;
+        if (mode == 0) {
+            const long long ntx2 = (g.nx + 63) / 64;
+            const long long r = b / ntx2;
+            i0 = (int)(b - r * ntx2) * 64;
+            j0 = (int)(r % g.nty) * TILE_Y;
+            k0 = (int)(r / g.nty) * g.tz;
+        } else {
+            int I0, J0, K0;
+            tile_origin(gc, b, I0, J0, K0);
+            i0 = 2 * I0;
+            j0 = 2 * J0;
+            k0 = g.dim == 3 ? 2 * K0 : 0;
+        }
+        U lo = ~U(0), hi = 0;
+        int any = 0;
+        for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+            const int i = i0 + (q & 63), j = j0 + ((q >> 6) & ((1 << yb) - 1)), k = k0 + (q >> (6 + yb));
+            if (i >= g.nx || j >= g.ny || k >= g.nz) continue;
+            const long long c = cell_index(g, i, j, k);
+            any |= (Bits<T>::of(L.diag[c]) << 1) != 0;  // diag != 0 (either sign of 0)
+            auto see = [&](T v) {
+                const U u = Bits<T>::of(v);
+                lo = u < lo ? u : lo;
+                hi = u > hi ? u : hi;
+            };
+            if (i > 0) see(L.cx[c - 1]);
+            if (i + 1 < g.nx) see(L.cx[c]);
+            if (j > 0) see(L.cy[c - sy]);
+            if (j + 1 < g.ny) see(L.cy[c]);
+            if (g.dim == 3) {
+                if (k > 0) see(L.cz[c - sz]);
+                if (k + 1 < g.nz) see(L.cz[c]);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const U l2 = __shfl_xor_sync(0xffffffffu, lo, o), h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+            lo = l2 < lo ? l2 : lo;
+            hi = h2 > hi ? h2 : hi;
+            any |= __shfl_xor_sync(0xffffffffu, any, o);
+        }
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        if (lane == 0) {
+            slo[wid] = lo;
+            shi[wid] = hi;
+            sany[wid] = any;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < BLOCK_THREADS / 32; ++w) {
+                lo = slo[w] < lo ? slo[w] : lo;
+                hi = shi[w] > hi ? shi[w] : hi;
+                any |= sany[w];
+            }
+            // (lo > hi: no face in the box)
+            T cls = T(TILE_MIXED);
+            if (!any && lo == 0 && hi == 0) cls = T(TILE_EMPTY);
+            else if (lo == hi) cls = Bits<T>::value(lo);
+            // a common value that is not a coupling (negative, NaN) is no class
+            if (!(cls >= T(0)) && cls != T(TILE_EMPTY)) cls = T(TILE_MIXED);
+            out[b] = cls;
+        }
+        __syncthreads();
+    }
+}
+
 template <class T> int nblocks(const Grid &g, int grid_blocks) {
     long long b = g.ntiles < grid_blocks ? g.ntiles : grid_blocks;
     return b < 1 ? 1 : (int)b;
@@ -165,6 +266,16 @@ cudaError_t mg_setup(const Grid &g0, Operator<double> A, const MgHierarchy<T> &H
         mg_coarsen_kernel<T><<<nblocks<T>(C.g, grid_blocks), BLOCK_THREADS, 0, stream>>>(
             F, C, const_cast<T *>(C.diag), const_cast<T *>(C.inv), const_cast<T *>(C.cx), const_cast<T *>(C.cy),
             const_cast<T *>(C.cz));
+    }
+    // tile classes of the levels the global-memory kernels run
+    for (int l = 0; l < H.tail && l + 1 < H.nlevels; ++l) {
+        const MgLevel<T> &F = H.levels[l], &C = H.levels[l + 1];
+        if (!F.tcp || !F.tcr) continue;
+        const long long np = (long long)((F.g.nx + 63) / 64) * F.g.nty * F.g.ntz, nr = C.g.ntiles;
+        mg_classify_kernel<T><<<(int)std::min<long long>(np, grid_blocks), BLOCK_THREADS, 0, stream>>>(
+            F, C.g, 0, F.tcp, np);
+        mg_classify_kernel<T><<<(int)std::min<long long>(nr, grid_blocks), BLOCK_THREADS, 0, stream>>>(
+            F, C.g, 1, F.tcr, nr);
     }
     return cudaGetLastError();
 }
