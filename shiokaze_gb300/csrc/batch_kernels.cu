@@ -137,6 +137,31 @@ template <class F> __device__ __forceinline__ void cell_tile(const Grid &g, cons
     for (int t = 0; t < it.ntiles; ++t) cell_tile1(g, (unsigned)(it.tile + t), f);
 }
 
+// A one-tile item whose tile has all 4 planes: fz(i, j, k0, c0) once per
+// thread for its whole column of 4 pairs (the gather-first kernels, which
+// issue every load of the column before the arithmetic); otherwise f per
+// plane as pair_tile.
+template <class FZ, class F>
+__device__ __forceinline__ void pair_tile_z4(const Grid &g, const BItem &it, FZ fz, F f) {
+    if (it.ntiles != 1 || g.tz != 4) {
+        pair_tile(g, it, f);
+        return;
+    }
+    const unsigned t = (unsigned)it.tile;
+    const int px = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const unsigned r = fdiv(t, g.ftx2);
+    const unsigned tk = fdiv(r, g.fty);
+    const int i = (int)(t - r * g.ftx2.d) * 64 + 2 * px;
+    const int j = (int)(r - tk * (unsigned)g.nty) * TILE_Y + ty;
+    const int k0 = (int)tk * 4;
+    if (k0 + 4 > g.nz) {
+        pair_tile1(g, t, f);
+        return;
+    }
+    if (i >= g.nx || j >= g.ny) return;
+    fz(i, j, k0, cell_index(g, i, j, k0));
+}
+
 // Runs body(std::true_type) on vector levels, body(std::false_type) elsewhere.
 template <class B> __device__ __forceinline__ void with_vec(int vec, B body) {
     if (vec) body(std::true_type{});
@@ -397,9 +422,79 @@ struct MaxSumAcc {
 
 // ---- smoothing and transfers on the global-memory levels --------------------------
 
+// First pre-smoothing pass over a gather-first column (the form of
+// spmv_col4): red cells x = b inv, black cells from their red neighbours'
+// b inv, with the products and sums of the plane-by-plane form. The black
+// cell of each pair is cell i+1 where i + j + k is even, else cell i; only
+// that side of each neighbour pair is read.
+template <class T>
+__device__ __forceinline__ void presmooth_col4(const Grid &g, T u, T *x, const T *b, const T *inv, int i, int j,
+                                               int k0, long long c0) {
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    Pair<T> bo[4], io[4];
+    T yb[4][2], yi[4][2], xb[4], xi[4];
+    const int h0 = ((i + j + k0) & 1) ^ 1;  // black side of plane k0 (alternates with z)
+    T zb[2] = {T(0), T(0)}, zi[2] = {T(0), T(0)};
+    if (k0 > 0) {
+        zb[0] = __ldg(b + c0 - sz + h0);
+        zi[0] = __ldg(inv + c0 - sz + h0);
+    }
+    if (k0 + 4 < g.nz) {
+        zb[1] = __ldg(b + c0 + 4 * sz + (h0 ^ 1));
+        zi[1] = __ldg(inv + c0 + 4 * sz + (h0 ^ 1));
+    }
+#pragma unroll
+    for (int z = 0; z < 4; ++z) {
+        const long long c = c0 + z * sz;
+        const int h = h0 ^ (z & 1);
+        bo[z] = ld2<T, true>(b, c, true);
+        io[z] = ld2<T, true>(inv, c, true);
+        yb[z][0] = yi[z][0] = yb[z][1] = yi[z][1] = T(0);
+        if (j > 0) {
+            yb[z][0] = __ldg(b + c - sy + h);
+            yi[z][0] = __ldg(inv + c - sy + h);
+        }
+        if (j + 1 < g.ny) {
+            yb[z][1] = __ldg(b + c + sy + h);
+            yi[z][1] = __ldg(inv + c + sy + h);
+        }
+        const long long xc = h == 0 ? c - 1 : c + 2;
+        const bool xin = h == 0 ? i > 0 : i + 2 < g.nx;
+        xb[z] = xin ? __ldg(b + xc) : T(0);
+        xi[z] = xin ? __ldg(inv + xc) : T(0);
+    }
+#pragma unroll
+    for (int z = 0; z < 4; ++z) {
+        const int k = k0 + z;
+        const int h = h0 ^ (z & 1);
+        const Pair<T> red{bo[z].a * io[z].a, bo[z].b * io[z].b};
+        // the black side's z neighbours (red): the same side of the planes around
+        const T zm = z == 0 ? zb[0] * zi[0] : (h ? bo[z - 1].b * io[z - 1].b : bo[z - 1].a * io[z - 1].a);
+        const T zp = z == 3 ? zb[1] * zi[1] : (h ? bo[z + 1].b * io[z + 1].b : bo[z + 1].a * io[z + 1].a);
+        T s = T(0);
+        if (h == 0) {
+            if (i > 0) s += u * (xb[z] * xi[z]);
+            s += u * red.b;
+        } else {
+            s += u * red.a;
+            if (i + 2 < g.nx) s += u * (xb[z] * xi[z]);
+        }
+        if (j > 0) s += u * (yb[z][0] * yi[z][0]);
+        if (j + 1 < g.ny) s += u * (yb[z][1] * yi[z][1]);
+        if (k > 0) s += u * zm;
+        if (k + 1 < g.nz) s += u * zp;
+        Pair<T> out = red;
+        if (h) out.b = (bo[z].b + s) * io[z].b;
+        else out.a = (bo[z].a + s) * io[z].a;
+        st2<T, true>(x, c0 + z * sz, out, true);
+    }
+}
+
 // First pre-smoothing pass from x = 0: red x = b / diag, then black from the
 // red neighbours (computed on the fly as b inv), both written.
-template <class T>
+// COL: use presmooth_col4 where it applies (the cooperative coarse kernels,
+// whose levels seldom have 4-plane tiles, leave it out to save registers).
+template <class T, bool COL>
 __device__ __forceinline__ void presmooth_items(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg,
         int n, const BScene<T> *__restrict__ scenes, int gate, ItemCtx<T> &ctx) {
     int cur = -1;
@@ -427,7 +522,7 @@ __device__ __forceinline__ void presmooth_items(const BLevel<T> *__restrict__ le
                 return Pair<T>{bb.a * ii.a, bb.b * ii.b};
             };
             auto nb1 = [&](long long m, int) { return __ldg(L.b + m) * __ldg(L.inv + m); };
-            pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
+            auto plane = [&](int i, int j, int k, long long c, bool second) {
                 const bool a_red = ((i + j + k) & 1) == 0;
                 const Pair<T> b2 = ld2<T, V>(L.b, c, second), iv = ld2<T, V>(L.inv, c, second);
                 const Pair<T> red{b2.a * iv.a, b2.b * iv.b};
@@ -441,7 +536,13 @@ __device__ __forceinline__ void presmooth_items(const BLevel<T> *__restrict__ le
                             iv.a;
                 }
                 st2<T, V>(L.x, c, out, second);
-            });
+            };
+            if constexpr (COL && U && V)
+                pair_tile_z4(L.g, it, [&](int i, int j, int k0, long long c0) {
+                    presmooth_col4<T>(L.g, cw.u, L.x, L.b, L.inv, i, j, k0, c0);
+                }, plane);
+            else
+                pair_tile(L.g, it, plane);
         });
     }
 }
@@ -452,7 +553,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
                   const BScene<T> *__restrict__ scenes, int gate, const BatchCounters *live) {
     if (batch_idle(live)) return;
     __shared__ ItemCtx<T> ctx;
-    presmooth_items<T>(levels, segs, nseg, n, scenes, gate, ctx);
+    presmooth_items<T, true>(levels, segs, nseg, n, scenes, gate, ctx);
 }
 
 // One colour of a Gauss-Seidel sweep (extra smoothing sweeps, and the final
@@ -661,7 +762,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
     if (batch_idle(cnt)) return;
     __shared__ ItemCtx<T> ctx;
     for (int l = cl.first; l <= cl.last; ++l) {
-        presmooth_items<T>(levels, cl.pair[l], cl.pair_seg[l], cl.pair_n[l], scenes, gate, ctx);
+        presmooth_items<T, false>(levels, cl.pair[l], cl.pair_seg[l], cl.pair_n[l], scenes, gate, ctx);
         if (!grid_barrier(cnt)) return;
         for (int sw = 1; sw < ms.smooth; ++sw)
             for (int color = 0; color < 2; ++color) {
@@ -694,6 +795,135 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
     }
 }
 
+// Gather-first columns: one thread's 4 pairs (i, i+1) x rows j x planes
+// k0..k0+3 of a uniform tile (coupling u) on a vector level (nx even, so
+// every pair is whole). Every load of the column is issued before the
+// arithmetic: the planes' own pairs k0-1..k0+4 (whose neighbours in z are
+// each other), the +-y pairs and the +-x cells. The plane-by-plane form
+// cannot hoist them, as its stores could alias the next plane's loads.
+// Products, their order (that of pair_nsum: -x, +x, -y, +y, -z, +z) and the
+// dot-product terms are those of the plane-by-plane form, so the results
+// are bitwise the same.
+template <class T> struct Col4 {
+    Pair<T> z[6];        // own pairs of planes k0-1 .. k0+4 (0 outside the grid)
+    Pair<T> ym[4], yp[4];  // rows j-1, j+1
+};
+template <class T>
+__device__ __forceinline__ void load_col4(Col4<T> &q, const T *v, const Grid &g, int j, int k0, long long c0) {
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const Pair<T> zero{T(0), T(0)};
+    q.z[0] = k0 > 0 ? ld2<T, true>(v, c0 - sz, true) : zero;
+    q.z[5] = k0 + 4 < g.nz ? ld2<T, true>(v, c0 + 4 * sz, true) : zero;
+#pragma unroll
+    for (int z = 0; z < 4; ++z) {
+        const long long c = c0 + z * sz;
+        q.z[z + 1] = ld2<T, true>(v, c, true);
+        q.ym[z] = j > 0 ? ld2<T, true>(v, c - sy, true) : zero;
+        q.yp[z] = j + 1 < g.ny ? ld2<T, true>(v, c + sy, true) : zero;
+    }
+}
+
+// q = A p and p . q over a column (spmv)
+template <class T>
+__device__ __forceinline__ void spmv_col4(const Grid &g, T u, const T *p, const T *diag, T *qv, int i, int j, int k0,
+                                          long long c0, DotAcc<T> &acc) {
+    const long long sz = (long long)g.nx * g.ny;
+    Col4<T> P;
+    load_col4(P, p, g, j, k0, c0);
+    T xm[4], xp[4];
+    Pair<T> dv[4];
+#pragma unroll
+    for (int z = 0; z < 4; ++z) {
+        const long long c = c0 + z * sz;
+        xm[z] = i > 0 ? __ldg(p + c - 1) : T(0);
+        xp[z] = i + 2 < g.nx ? __ldg(p + c + 2) : T(0);
+        dv[z] = ld2<T, true>(diag, c, true);
+    }
+#pragma unroll
+    for (int z = 0; z < 4; ++z) {
+        const int k = k0 + z;
+        const Pair<T> own = P.z[z + 1];
+        Pair<T> s{T(0), T(0)};
+        if (i > 0) s.a += u * xm[z];
+        s.a += u * own.b;
+        s.b += u * own.a;
+        if (i + 2 < g.nx) s.b += u * xp[z];
+        if (j > 0) {
+            s.a += u * P.ym[z].a;
+            s.b += u * P.ym[z].b;
+        }
+        if (j + 1 < g.ny) {
+            s.a += u * P.yp[z].a;
+            s.b += u * P.yp[z].b;
+        }
+        if (k > 0) {
+            s.a += u * P.z[z].a;
+            s.b += u * P.z[z].b;
+        }
+        if (k + 1 < g.nz) {
+            s.a += u * P.z[z + 2].a;
+            s.b += u * P.z[z + 2].b;
+        }
+        const Pair<T> q2{dv[z].a * own.a - s.a, dv[z].b * own.b - s.b};
+        st2<T, true>(qv, c0 + z * sz, q2, true);
+        acc.add(own.a, q2.a);
+        acc.add(own.b, q2.b);
+    }
+}
+
+// red half-sweep of x (b = r) and z . r over a column (red_dot): the red
+// cell of each pair is cell i where i + j + k is even, else cell i+1; its
+// neighbours are black and not written here
+template <class T>
+__device__ __forceinline__ void red_dot_col4(const Grid &g, T u, T *x, const T *b, const T *inv, int i, int j,
+                                             int k0, long long c0, DotAcc<T> &acc) {
+    // only the red cell's side of each neighbour pair is read: single cells
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    Pair<T> own[4], bv[4];
+    T xs[4], iv[4], ym[4], yp[4];
+    const int h0 = (i + j + k0) & 1;  // red side of plane k0 (alternates with z)
+    const T zlo = k0 > 0 ? __ldg(x + c0 - sz + h0) : T(0);
+    const T zhi = k0 + 4 < g.nz ? __ldg(x + c0 + 4 * sz + (h0 ^ 1)) : T(0);
+#pragma unroll
+    for (int z = 0; z < 4; ++z) {
+        const long long c = c0 + z * sz;
+        const int hr = h0 ^ (z & 1);
+        own[z] = ld2<T, true>(x, c, true);
+        ym[z] = j > 0 ? __ldg(x + c - sy + hr) : T(0);
+        yp[z] = j + 1 < g.ny ? __ldg(x + c + sy + hr) : T(0);
+        xs[z] = hr == 0 ? (i > 0 ? __ldg(x + c - 1) : T(0)) : (i + 2 < g.nx ? __ldg(x + c + 2) : T(0));
+        iv[z] = __ldg(inv + c + hr);
+        bv[z] = ld2<T, true>(b, c, true);
+    }
+#pragma unroll
+    for (int z = 0; z < 4; ++z) {
+        const int k = k0 + z;
+        const int hr = h0 ^ (z & 1);
+        // the red side's z neighbours: the same side of the planes around
+        const T zm = z == 0 ? zlo : (hr ? own[z - 1].b : own[z - 1].a);
+        const T zp = z == 3 ? zhi : (hr ? own[z + 1].b : own[z + 1].a);
+        T s = T(0);
+        if (hr == 0) {
+            if (i > 0) s += u * xs[z];
+            s += u * own[z].b;
+        } else {
+            s += u * own[z].a;
+            if (i + 2 < g.nx) s += u * xs[z];
+        }
+        if (j > 0) s += u * ym[z];
+        if (j + 1 < g.ny) s += u * yp[z];
+        if (k > 0) s += u * zm;
+        if (k + 1 < g.nz) s += u * zp;
+        const T xv = ((hr ? bv[z].b : bv[z].a) + s) * iv[z];
+        Pair<T> out = own[z];
+        if (hr) out.b = xv;
+        else out.a = xv;
+        x[c0 + z * sz + hr] = xv;
+        acc.add(out.a, bv[z].a);
+        acc.add(out.b, bv[z].b);
+    }
+}
+
 // Last red pass of the fine level, with rho' = z . r (z = x, r = b there)
 // per scene; the scene's last flush sets beta (0 for a new direction).
 template <class T, int OCC>
@@ -715,7 +945,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
                 constexpr bool U = decltype(ut)::value;
                 auto nb2 = [&](long long m, int, int, bool sec) { return ld2<T, V>(L.x, m, sec); };
                 auto nb1 = [&](long long m, int) { return __ldg(L.x + m); };
-                pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
+                auto plane = [&](int i, int j, int k, long long c, bool second) {
                     const int hr = ((i + j + k) & 1) == 0 ? 0 : 1;
                     const Pair<T> x2 = ld2<T, V>(L.x, c, second), b2 = ld2<T, V>(L.b, c, second);
                     Pair<T> out = x2;
@@ -729,7 +959,13 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
                     }
                     acc.add(out.a, b2.a);
                     if (second) acc.add(out.b, b2.b);
-                });
+                };
+                if constexpr (U && V)
+                    pair_tile_z4(L.g, it, [&](int i, int j, int k0, long long c0) {
+                        red_dot_col4<T>(L.g, cw.u, L.x, L.b, L.inv, i, j, k0, c0, acc);
+                    }, plane);
+                else
+                    pair_tile(L.g, it, plane);
             });
         },
         [&](const BItem &it, int flushes) {
@@ -1018,14 +1254,20 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
                 constexpr bool U = decltype(ut)::value;
                 auto nb2 = [&](long long m, int, int, bool sec) { return ld2<T, V>(S.p, m, sec); };
                 auto nb1 = [&](long long m, int) { return __ldg(S.p + m); };
-                pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
+                auto plane = [&](int i, int j, int k, long long c, bool second) {
                     const Pair<T> p2 = ld2<T, V>(S.p, c, second), d2 = ld2<T, V>(L.diag, c, second);
                     const Pair<T> s = pair_nsum<T, V, U, 2>(L.g, cw, i, j, k, c, second, p2, nb2, nb1);
                     const Pair<T> q2{d2.a * p2.a - s.a, d2.b * p2.b - s.b};
                     st2<T, V>(S.q, c, q2, second);
                     acc.add(p2.a, q2.a);
                     if (second) acc.add(p2.b, q2.b);
-                });
+                };
+                if constexpr (U && V)
+                    pair_tile_z4(L.g, it, [&](int i, int j, int k0, long long c0) {
+                        spmv_col4<T>(L.g, cw.u, S.p, L.diag, S.q, i, j, k0, c0, acc);
+                    }, plane);
+                else
+                    pair_tile(L.g, it, plane);
             });
         },
         [&](const BItem &it, int flushes) {

@@ -2,7 +2,9 @@
 every coupling array (TileClasses=0).
 
 In the FP32 kernels a tile whose stencils read only couplings of one value
-u uses u instead of the arrays (the same products in the same order); in
+u uses u instead of the arrays (the same products in the same order; on
+4-plane tiles of grids over 2^21 cells, with every load of a thread's
+column issued first); in
 both precisions a tile with no unknown writes zeros without loading, or
 is skipped where its values are already 0. The solves must therefore
 agree exactly: the same iteration counts and the same pressure and
@@ -26,7 +28,7 @@ def _solve(sc, **cfg):
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 @pytest.mark.parametrize("kind,shape", [("liquid3", 96), ("smoke3", (80, 64, 72)), ("liquid3", 160),
-                                        ("liquid2", 200)])
+                                        ("smoke3", (136, 128, 128)), ("liquid2", 200)])
 def test_tile_classes_change_nothing(kind, shape, precision):
     import shiokaze_gb300 as gb
     from shiokaze_gb300 import scenes
