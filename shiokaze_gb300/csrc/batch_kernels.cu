@@ -79,6 +79,15 @@ template <> struct Vec2<double> {
     using type = double2;
 };
 
+// v + alpha q as one fused multiply-add, written out so that every form of
+// the prolongation (plane by plane, gather-first, staged) rounds alike
+// whatever the compiler shares between them.
+__device__ __forceinline__ float prolong(float v, float alpha, float q) { return __fmaf_rn(alpha, q, v); }
+__device__ __forceinline__ double prolong(double v, double alpha, double q) { return __fma_rn(alpha, q, v); }
+// s + c v, fused, for the same reason (every neighbour sum of the stencils)
+__device__ __forceinline__ float fmadd(float s, float c, float v) { return __fmaf_rn(c, v, s); }
+__device__ __forceinline__ double fmadd(double s, double c, double v) { return __fma_rn(c, v, s); }
+
 // Read-only pair load: one 2-wide load when V (c even, array aligned), else
 // the cells one by one (the second only if it exists).
 template <class T, bool V> __device__ __forceinline__ Pair<T> ld2(const T *p, long long c, bool second) {
@@ -250,15 +259,15 @@ __device__ __forceinline__ Pair<T> pair_nsum(const Grid &g, const Cpl<T> &w, int
         else return __ldg(a + m);
     };
     const Pair<T> cxp = cw2(w.cx, c);  // faces (i|i+1), (i+1|i+2)
-    if (A && i > 0) s.a += cw1(w.cx, c - 1) * nb1(c - 1, i - 1);
+    if (A && i > 0) s.a = fmadd(s.a, cw1(w.cx, c - 1), nb1(c - 1, i - 1));
     if (second) {
-        if (A) s.a += cxp.a * own.b;
-        if (B) s.b += cxp.a * own.a;
-        if (B && i + 2 < g.nx) s.b += cxp.b * nb1(c + 2, i + 2);
+        if (A) s.a = fmadd(s.a, cxp.a, own.b);
+        if (B) s.b = fmadd(s.b, cxp.a, own.a);
+        if (B && i + 2 < g.nx) s.b = fmadd(s.b, cxp.b, nb1(c + 2, i + 2));
     }
     auto add = [&](const Pair<T> &cw, const Pair<T> &v) {
-        if (A) s.a += cw.a * v.a;
-        if (B) s.b += cw.b * v.b;
+        if (A) s.a = fmadd(s.a, cw.a, v.a);
+        if (B) s.b = fmadd(s.b, cw.b, v.b);
     };
     if (j > 0) add(cw2(w.cy, c - sy), nb2(c - sy, j - 1, k, second));
     if (j + 1 < g.ny) add(cw2(w.cy, c), nb2(c + sy, j + 1, k, second));
@@ -473,16 +482,16 @@ __device__ __forceinline__ void presmooth_col4(const Grid &g, T u, T *x, const T
         const T zp = z == 3 ? zb[1] * zi[1] : (h ? bo[z + 1].b * io[z + 1].b : bo[z + 1].a * io[z + 1].a);
         T s = T(0);
         if (h == 0) {
-            if (i > 0) s += u * (xb[z] * xi[z]);
-            s += u * red.b;
+            if (i > 0) s = fmadd(s, u, (xb[z] * xi[z]));
+            s = fmadd(s, u, red.b);
         } else {
-            s += u * red.a;
-            if (i + 2 < g.nx) s += u * (xb[z] * xi[z]);
+            s = fmadd(s, u, red.a);
+            if (i + 2 < g.nx) s = fmadd(s, u, (xb[z] * xi[z]));
         }
-        if (j > 0) s += u * (yb[z][0] * yi[z][0]);
-        if (j + 1 < g.ny) s += u * (yb[z][1] * yi[z][1]);
-        if (k > 0) s += u * zm;
-        if (k + 1 < g.nz) s += u * zp;
+        if (j > 0) s = fmadd(s, u, (yb[z][0] * yi[z][0]));
+        if (j + 1 < g.ny) s = fmadd(s, u, (yb[z][1] * yi[z][1]));
+        if (k > 0) s = fmadd(s, u, zm);
+        if (k + 1 < g.nz) s = fmadd(s, u, zp);
         Pair<T> out = red;
         if (h) out.b = (bo[z].b + s) * io[z].b;
         else out.a = (bo[z].a + s) * io[z].a;
@@ -547,13 +556,13 @@ __device__ __forceinline__ void presmooth_items(const BLevel<T> *__restrict__ le
     }
 }
 
-template <class T, int OCC>
+template <class T, int OCC, bool COL>
 __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     presmooth_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
                   const BScene<T> *__restrict__ scenes, int gate, const BatchCounters *live) {
     if (batch_idle(live)) return;
     __shared__ ItemCtx<T> ctx;
-    presmooth_items<T, true>(levels, segs, nseg, n, scenes, gate, ctx);
+    presmooth_items<T, COL>(levels, segs, nseg, n, scenes, gate, ctx);
 }
 
 // One colour of a Gauss-Seidel sweep (extra smoothing sweeps, and the final
@@ -657,10 +666,78 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     restrict_items<T>(levels, segs, nseg, n, scenes, gate, ctx);
 }
 
+// Prolongation and black half-sweep over a gather-first column (the form
+// of spmv_col4; 3D, k0 even, so planes k0, k0+1 share the parent plane
+// k0/2 and k0+2, k0+3 the next one). The black cell of each pair is cell i
+// where i + j + k is odd, else cell i+1; its red neighbours are read with
+// alpha times their own parent added, with the products and sums of the
+// plane-by-plane form.
+template <class T>
+__device__ __forceinline__ void post_black_col4(const Grid &g, const Grid &cg, T u, T alpha, T *x, const T *b,
+                                                const T *inv, const T *xc, int i, int j, int k0, long long c0) {
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const long long csy = cg.nx, csz = (long long)cg.nx * cg.ny;
+    const long long P0 = cell_index(cg, i >> 1, j >> 1, k0 >> 1);
+    const int h0 = ((i + j + k0) & 1) == 1 ? 0 : 1;  // black side of plane k0 (alternates with z)
+    // parents: own (two parent planes), across z, across y, across x
+    const T pc0 = __ldg(xc + P0), pc1 = __ldg(xc + P0 + csz);
+    const T pzl = k0 > 0 ? __ldg(xc + P0 - csz) : T(0);
+    const T pzh = k0 + 4 < g.nz ? __ldg(xc + P0 + 2 * csz) : T(0);
+    // row j's neighbour in the other parent row: j - 1 for even j, j + 1 for odd j
+    const bool yodd = (j & 1) != 0;
+    const bool ycross = yodd ? j + 1 < g.ny : j > 0;
+    const long long pyo = yodd ? csy : -csy;
+    const T py0 = ycross ? __ldg(xc + P0 + pyo) : T(0), py1 = ycross ? __ldg(xc + P0 + csz + pyo) : T(0);
+    const T pxm0 = i > 0 ? __ldg(xc + P0 - 1) : T(0), pxm1 = i > 0 ? __ldg(xc + P0 + csz - 1) : T(0);
+    const T pxp0 = i + 2 < g.nx ? __ldg(xc + P0 + 1) : T(0), pxp1 = i + 2 < g.nx ? __ldg(xc + P0 + csz + 1) : T(0);
+    Pair<T> own[4];
+    T ym[4], yp[4], xs[4], bb[4], iv[4];
+    const T zlo = k0 > 0 ? __ldg(x + c0 - sz + h0) : T(0);
+    const T zhi = k0 + 4 < g.nz ? __ldg(x + c0 + 4 * sz + (h0 ^ 1)) : T(0);
+#pragma unroll
+    for (int z = 0; z < 4; ++z) {
+        const long long c = c0 + z * sz;
+        const int h = h0 ^ (z & 1);
+        own[z] = ld2<T, true>(x, c, true);
+        ym[z] = j > 0 ? __ldg(x + c - sy + h) : T(0);
+        yp[z] = j + 1 < g.ny ? __ldg(x + c + sy + h) : T(0);
+        xs[z] = h == 0 ? (i > 0 ? __ldg(x + c - 1) : T(0)) : (i + 2 < g.nx ? __ldg(x + c + 2) : T(0));
+        bb[z] = __ldg(b + c + h);
+        iv[z] = __ldg(inv + c + h);
+    }
+#pragma unroll
+    for (int z = 0; z < 4; ++z) {
+        const int k = k0 + z;
+        const int h = h0 ^ (z & 1);
+        const T pc = z < 2 ? pc0 : pc1;
+        const Pair<T> o{prolong(own[z].a, alpha, pc), prolong(own[z].b, alpha, pc)};
+        // the black side's y and z neighbours with their parents
+        const T qym = yodd ? pc : (z < 2 ? py0 : py1);
+        const T qyp = yodd ? (z < 2 ? py0 : py1) : pc;
+        const T qzm = (z & 1) ? pc : (z == 0 ? pzl : pc0);
+        const T qzp = (z & 1) ? (z == 1 ? pc1 : pzh) : pc;
+        const T vzm = z == 0 ? zlo : (h ? own[z - 1].b : own[z - 1].a);
+        const T vzp = z == 3 ? zhi : (h ? own[z + 1].b : own[z + 1].a);
+        T s = T(0);
+        if (h == 0) {
+            if (i > 0) s = fmadd(s, u, prolong(xs[z], alpha, z < 2 ? pxm0 : pxm1));
+            s = fmadd(s, u, o.b);
+        } else {
+            s = fmadd(s, u, o.a);
+            if (i + 2 < g.nx) s = fmadd(s, u, prolong(xs[z], alpha, z < 2 ? pxp0 : pxp1));
+        }
+        if (j > 0) s = fmadd(s, u, prolong(ym[z], alpha, qym));
+        if (j + 1 < g.ny) s = fmadd(s, u, prolong(yp[z], alpha, qyp));
+        if (k > 0) s = fmadd(s, u, prolong(vzm, alpha, qzm));
+        if (k + 1 < g.nz) s = fmadd(s, u, prolong(vzp, alpha, qzp));
+        x[c0 + z * sz + h] = (bb[z] + s) * iv[z];
+    }
+}
+
 // Prolongation fused with the black half of the post-smoothing: black cells
 // from their red neighbours plus alpha times the neighbour's parent value.
 // The two cells of a pair (i even) share their parent.
-template <class T>
+template <class T, bool COL>
 __device__ __forceinline__ void post_black_items(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg,
         int n, const BScene<T> *__restrict__ scenes, int gate, T alpha, ItemCtx<T> &ctx) {
     int cur = -1;
@@ -681,7 +758,7 @@ __device__ __forceinline__ void post_black_items(const BLevel<T> *__restrict__ l
             const Grid &cg = L.gc;
             const bool d3 = L.g.dim == 3;
             const long long csy = cg.nx, csz = (long long)cg.nx * cg.ny;
-            pair_tile(L.g, it, [&](int i, int j, int k, long long c, bool second) {
+            auto plane = [&](int i, int j, int k, long long c, bool second) {
                 const int h = ((i + j + k) & 1) == 1 ? 0 : 1;
                 if (h == 1 && !second) return;
                 // parent of the pair and of its neighbours: the same coarse
@@ -692,28 +769,34 @@ __device__ __forceinline__ void post_black_items(const BLevel<T> *__restrict__ l
                     const Pair<T> v = ld2<T, V>(L.x, m, sec);
                     const int dj = (jj >> 1) - (j >> 1), dk = d3 ? (kk >> 1) - (k >> 1) : 0;
                     const T q = (dj | dk) == 0 ? pc : __ldg(L.xc + P + dj * csy + dk * csz);
-                    return Pair<T>{v.a + alpha * q, v.b + alpha * q};
+                    return Pair<T>{prolong(v.a, alpha, q), prolong(v.b, alpha, q)};
                 };
                 auto nb1 = [&](long long m, int ii) {
-                    return __ldg(L.x + m) + alpha * __ldg(L.xc + P + ((ii >> 1) - (i >> 1)));
+                    return prolong(__ldg(L.x + m), alpha, __ldg(L.xc + P + ((ii >> 1) - (i >> 1))));
                 };
                 const Pair<T> x2 = ld2<T, V>(L.x, c, second);
-                const Pair<T> own{x2.a + alpha * pc, x2.b + alpha * pc};
+                const Pair<T> own{prolong(x2.a, alpha, pc), prolong(x2.b, alpha, pc)};
                 const T sh = pair_nsum1<T, V, U>(h, L.g, cw, i, j, k, c, second, own, nb2, nb1);
                 const long long ch = c + h;
                 L.x[ch] = (__ldg(L.b + ch) + sh) * __ldg(L.inv + ch);
-            });
+            };
+            if constexpr (COL && U && V)
+                pair_tile_z4(L.g, it, [&](int i, int j, int k0, long long c0) {
+                    post_black_col4<T>(L.g, cg, cw.u, alpha, L.x, L.b, L.inv, L.xc, i, j, k0, c0);
+                }, plane);
+            else
+                pair_tile(L.g, it, plane);
         });
     }
 }
 
-template <class T, int OCC>
+template <class T, int OCC, bool COL>
 __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     post_black_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
                   const BScene<T> *__restrict__ scenes, int gate, T alpha, const BatchCounters *live) {
     if (batch_idle(live)) return;
     __shared__ ItemCtx<T> ctx;
-    post_black_items<T>(levels, segs, nseg, n, scenes, gate, alpha, ctx);
+    post_black_items<T, COL>(levels, segs, nseg, n, scenes, gate, alpha, ctx);
 }
 
 // ---- coarse levels in two cooperative launches -------------------------------------
@@ -783,7 +866,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
     if (batch_idle(cnt)) return;
     __shared__ ItemCtx<T> ctx;
     for (int l = cl.last; l >= cl.first; --l) {
-        post_black_items<T>(levels, cl.pair[l], cl.pair_seg[l], cl.pair_n[l], scenes, gate, alpha, ctx);
+        post_black_items<T, false>(levels, cl.pair[l], cl.pair_seg[l], cl.pair_n[l], scenes, gate, alpha, ctx);
         if (!grid_barrier(cnt)) return;
         for (int sw = 1; sw < ms.smooth; ++sw)
             for (int color = 0; color < 2; ++color) {
@@ -844,25 +927,25 @@ __device__ __forceinline__ void spmv_col4(const Grid &g, T u, const T *p, const 
         const int k = k0 + z;
         const Pair<T> own = P.z[z + 1];
         Pair<T> s{T(0), T(0)};
-        if (i > 0) s.a += u * xm[z];
-        s.a += u * own.b;
-        s.b += u * own.a;
-        if (i + 2 < g.nx) s.b += u * xp[z];
+        if (i > 0) s.a = fmadd(s.a, u, xm[z]);
+        s.a = fmadd(s.a, u, own.b);
+        s.b = fmadd(s.b, u, own.a);
+        if (i + 2 < g.nx) s.b = fmadd(s.b, u, xp[z]);
         if (j > 0) {
-            s.a += u * P.ym[z].a;
-            s.b += u * P.ym[z].b;
+            s.a = fmadd(s.a, u, P.ym[z].a);
+            s.b = fmadd(s.b, u, P.ym[z].b);
         }
         if (j + 1 < g.ny) {
-            s.a += u * P.yp[z].a;
-            s.b += u * P.yp[z].b;
+            s.a = fmadd(s.a, u, P.yp[z].a);
+            s.b = fmadd(s.b, u, P.yp[z].b);
         }
         if (k > 0) {
-            s.a += u * P.z[z].a;
-            s.b += u * P.z[z].b;
+            s.a = fmadd(s.a, u, P.z[z].a);
+            s.b = fmadd(s.b, u, P.z[z].b);
         }
         if (k + 1 < g.nz) {
-            s.a += u * P.z[z + 2].a;
-            s.b += u * P.z[z + 2].b;
+            s.a = fmadd(s.a, u, P.z[z + 2].a);
+            s.b = fmadd(s.b, u, P.z[z + 2].b);
         }
         const Pair<T> q2{dv[z].a * own.a - s.a, dv[z].b * own.b - s.b};
         st2<T, true>(qv, c0 + z * sz, q2, true);
@@ -904,16 +987,16 @@ __device__ __forceinline__ void red_dot_col4(const Grid &g, T u, T *x, const T *
         const T zp = z == 3 ? zhi : (hr ? own[z + 1].b : own[z + 1].a);
         T s = T(0);
         if (hr == 0) {
-            if (i > 0) s += u * xs[z];
-            s += u * own[z].b;
+            if (i > 0) s = fmadd(s, u, xs[z]);
+            s = fmadd(s, u, own[z].b);
         } else {
-            s += u * own[z].a;
-            if (i + 2 < g.nx) s += u * xs[z];
+            s = fmadd(s, u, own[z].a);
+            if (i + 2 < g.nx) s = fmadd(s, u, xs[z]);
         }
-        if (j > 0) s += u * ym[z];
-        if (j + 1 < g.ny) s += u * yp[z];
-        if (k > 0) s += u * zm;
-        if (k + 1 < g.nz) s += u * zp;
+        if (j > 0) s = fmadd(s, u, ym[z]);
+        if (j + 1 < g.ny) s = fmadd(s, u, yp[z]);
+        if (k > 0) s = fmadd(s, u, zm);
+        if (k + 1 < g.nz) s = fmadd(s, u, zp);
         const T xv = ((hr ? bv[z].b : bv[z].a) + s) * iv[z];
         Pair<T> out = own[z];
         if (hr) out.b = xv;
@@ -926,7 +1009,7 @@ __device__ __forceinline__ void red_dot_col4(const Grid &g, T u, T *x, const T *
 
 // Last red pass of the fine level, with rho' = z . r (z = x, r = b there)
 // per scene; the scene's last flush sets beta (0 for a new direction).
-template <class T, int OCC>
+template <class T, int OCC, bool COL>
 __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     red_dot_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
                    const BScene<T> *__restrict__ scenes, int gate, double *part, const int *__restrict__ scene_of,
@@ -960,7 +1043,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
                     acc.add(out.a, b2.a);
                     if (second) acc.add(out.b, b2.b);
                 };
-                if constexpr (U && V)
+                if constexpr (COL && U && V)
                     pair_tile_z4(L.g, it, [&](int i, int j, int k0, long long c0) {
                         red_dot_col4<T>(L.g, cw.u, L.x, L.b, L.inv, i, j, k0, c0, acc);
                     }, plane);
@@ -1232,7 +1315,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     }
 }
 
-template <class T, int OCC>
+template <class T, int OCC, bool COL>
 __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     spmv_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
                 const BScene<T> *__restrict__ scenes, int gate, double *part, const int *__restrict__ scene_of,
@@ -1262,7 +1345,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
                     acc.add(p2.a, q2.a);
                     if (second) acc.add(p2.b, q2.b);
                 };
-                if constexpr (U && V)
+                if constexpr (COL && U && V)
                     pair_tile_z4(L.g, it, [&](int i, int j, int k0, long long c0) {
                         spmv_col4<T>(L.g, cw.u, S.p, L.diag, S.q, i, j, k0, c0, acc);
                     }, plane);
@@ -1840,9 +1923,9 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 1)
                         const float pc = sxc[P];
                         auto val = [&](int m, int d) {
                             const float q = (d >= 2 && step[d] == 0) ? pc : sxc[P + step[d]];
-                            return sx[m] + alpha * q;
+                            return prolong(sx[m], alpha, q);
                         };
-                        const Pair<float> own{sx[hc] + alpha * pc, sx[hc + 1] + alpha * pc};
+                        const Pair<float> own{prolong(sx[hc], alpha, pc), prolong(sx[hc + 1], alpha, pc)};
                         const float sh = staged_nsum(h, g, i, j, k, hc, cxi, cyi, czi, scx, scy, scz, own, val);
                         L.x[c + h] = (sb[oc + h] + sh) * si[oc + h];
                     } else if constexpr (KIND == STAGE_RED_DOT) {
@@ -1894,11 +1977,26 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 1)
         default: kernel<T, 5><<<(L).blocks, BLOCK_THREADS, 0, (L).stream>>> ARGS; break;  \
         }                                                                                 \
     } while (0)
+// The same for the kernels with a gather-first column form: COL when the
+// list holds 4-plane tiles ((L).col), else the plane-by-plane kernel alone.
+#define OCC_COL_DISPATCH(L, kernel, T, ARGS)                                                     \
+    do {                                                                                         \
+        const int occ_ = (L).occ ? (L).occ : BatchOcc<T>::blocks;                                \
+        if ((L).col) {                                                                           \
+            if (occ_ == 4) kernel<T, 4, true><<<(L).blocks, BLOCK_THREADS, 0, (L).stream>>> ARGS;       \
+            else if (occ_ == 6) kernel<T, 6, true><<<(L).blocks, BLOCK_THREADS, 0, (L).stream>>> ARGS;  \
+            else kernel<T, 5, true><<<(L).blocks, BLOCK_THREADS, 0, (L).stream>>> ARGS;                 \
+        } else {                                                                                 \
+            if (occ_ == 4) kernel<T, 4, false><<<(L).blocks, BLOCK_THREADS, 0, (L).stream>>> ARGS;      \
+            else if (occ_ == 6) kernel<T, 6, false><<<(L).blocks, BLOCK_THREADS, 0, (L).stream>>> ARGS; \
+            else kernel<T, 5, false><<<(L).blocks, BLOCK_THREADS, 0, (L).stream>>> ARGS;                \
+        }                                                                                        \
+    } while (0)
 
 template <class T>
 cudaError_t b_presmooth(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                         const BScene<T> *scenes) {
-    OCC_DISPATCH(L, presmooth_kernel, T, (levels, segs, nseg, n, scenes, L.gate, L.cnt));
+    OCC_COL_DISPATCH(L, presmooth_kernel, T, (levels, segs, nseg, n, scenes, L.gate, L.cnt));
     return cudaGetLastError();
 }
 template <class T>
@@ -1916,14 +2014,14 @@ cudaError_t b_restrict(const BLaunch &L, const BLevel<T> *levels, const BSeg *se
 template <class T>
 cudaError_t b_post_black(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                          const BScene<T> *scenes, T alpha) {
-    OCC_DISPATCH(L, post_black_kernel, T, (levels, segs, nseg, n, scenes, L.gate, alpha,
+    OCC_COL_DISPATCH(L, post_black_kernel, T, (levels, segs, nseg, n, scenes, L.gate, alpha,
                                                                    L.cnt));
     return cudaGetLastError();
 }
 template <class T>
 cudaError_t b_red_dot(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                       const BScene<T> *scenes, double *part) {
-    OCC_DISPATCH(L, red_dot_kernel, T, (levels, segs, nseg, n, scenes, L.gate, part,
+    OCC_COL_DISPATCH(L, red_dot_kernel, T, (levels, segs, nseg, n, scenes, L.gate, part,
                                                                 L.scene_of, L.cnt));
     return cudaGetLastError();
 }
@@ -2028,7 +2126,7 @@ cudaError_t b_direction(const BLaunch &L, const BLevel<T> *levels, const BSeg *s
 template <class T>
 cudaError_t b_spmv(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                    const BScene<T> *scenes, double *part) {
-    OCC_DISPATCH(L, spmv_kernel, T, (levels, segs, nseg, n, scenes, L.gate, part, L.scene_of,
+    OCC_COL_DISPATCH(L, spmv_kernel, T, (levels, segs, nseg, n, scenes, L.gate, part, L.scene_of,
                                                              L.cnt));
     return cudaGetLastError();
 }

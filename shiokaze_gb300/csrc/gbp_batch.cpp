@@ -144,6 +144,12 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
     }
     mixed_ = sizeof(T) == 4;
     sms_ = std::max(1, grid_blocks_ / BatchOcc<T>::blocks);
+    // the gather-first column kernels (FP32 uniform tiles of 4 planes on
+    // vector levels) are launched only for lists that hold such tiles
+    fine_col_ = false;
+    if (sizeof(T) == 4)
+        for (int ref : plan.fine_ref)
+            if (plan.levels[ref].g.tz == 4 && plan.levels[ref].vec && plan.levels[ref].tcp) fine_col_ = true;
     // staged fine levels: their tensor maps, in one device array
     std::vector<BLevel<T>> levels = plan.levels;
     std::vector<int> staged_at(levels.size(), -1);
@@ -266,7 +272,9 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
 template <class T> BLaunch BatchRunner::launch_for(int bk, int items, cudaStream_t st, int gate) const {
     const int occ = bk >= 0 ? occ_[bk] : 0;
     const int per_sm = occ ? occ : BatchOcc<T>::blocks;
-    return BLaunch{blocks_for(items, std::min(MAX_GRID, sms_ * per_sm)), st, gate, d_scene_of_, d_counters_, occ};
+    const bool col = fine_col_ && (bk == BK_PRESMOOTH || bk == BK_POST_BLACK || bk == BK_RED_DOT || bk == BK_SPMV);
+    return BLaunch{blocks_for(items, std::min(MAX_GRID, sms_ * per_sm)), st, gate, d_scene_of_, d_counters_, occ,
+                   col ? 1 : 0};
 }
 
 // The autotuner of occupancy: the fine-level kernels are compiled for 4, 5

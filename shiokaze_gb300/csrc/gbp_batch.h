@@ -177,6 +177,7 @@ struct BLaunch {
     const int *scene_of;  // scene of each level-table entry (reductions)
     BatchCounters *cnt;   // batch counters (idle and refinement checks)
     int occ;              // occupancy variant (4, 5 or 6 blocks per SM); 0: the precision's default
+    int col;              // the list has 4-plane tiles: launch the gather-first column kernels
 };
 
 // Fine-level kernels whose occupancy variant the autotuner picks per batch.
@@ -244,6 +245,7 @@ private:
     std::vector<char> staged_scene_;
     int stage_mask_ = 0;  // bit k: pass k (StageKind) runs staged
     int occ_[BK_TUNED] = {};  // occupancy variant per tuned kernel (0: default)
+    bool fine_col_ = false;    // some scene's fine level has 4-plane tiles of pairs (FP32)
     // a launch of tuned kernel bk (or -1: untuned) over `items` items
     template <class T> BLaunch launch_for(int bk, int items, cudaStream_t st, int gate) const;
     template <class T> int tune_occupancy(cudaStream_t st, const std::string &key);
