@@ -277,6 +277,14 @@ template <class T> BLaunch BatchRunner::launch_for(int bk, int items, cudaStream
                    col ? 1 : 0};
 }
 
+static MgSettings settings_of(const gbp_params &p) {
+    MgSettings ms;
+    ms.smooth = p.mg_smooth > 0 ? p.mg_smooth : 1;
+    ms.coarsest_pairs = 4;
+    ms.alpha = 1.6;
+    return ms;
+}
+
 // The autotuner of occupancy: the fine-level kernels are compiled for 4, 5
 // and 6 resident blocks of 256 threads per SM (more registers per thread, or
 // more warps to hide latency); the best choice moves with the problem size
@@ -287,7 +295,10 @@ template <class T> BLaunch BatchRunner::launch_for(int bk, int items, cudaStream
 // arrays before the solve fills them: values do not change the work, every
 // array they write is rewritten by the solve before it is read, and the
 // solve resets the scalars and counters they touch. Choices are kept per
-// precision and half-octave of the batch's fine cells.
+// precision and half-octave of the batch's fine cells. The same timing
+// picks the grid of the cooperative coarse-level kernels (2, 3 or 4 blocks
+// per SM, or all that stay resident): fewer blocks make each grid-wide
+// barrier cheaper, more hide the loads of the larger coarse levels.
 template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::string &key) {
     static std::mutex mu;
     static std::map<std::string, std::vector<int>> cache;
@@ -296,6 +307,7 @@ template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::s
         auto it = cache.find(key);
         if (it != cache.end()) {
             for (int k = 0; k < BK_TUNED; ++k) occ_[k] = it->second[k];
+            coarse_blocks_ = std::min(coarse_blocks_, it->second[BK_TUNED]);
             return GBP_OK;
         }
     }
@@ -348,21 +360,54 @@ template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::s
         }
         occ_[k] = pick;
     }
+    if (err == cudaSuccess && coarse_blocks_ > 0) {
+        const MgSettings ms = settings_of(p);
+        const int full = coarse_blocks_;
+        float best = 0.f;
+        int pick = full;
+        for (int f : {2, 3, 4, 0}) {
+            const int nb = f ? std::min(full, sms_ * f) : full;
+            if (f && nb >= full) continue;
+            auto run = [&]() {
+                cudaError_t e = b_coarse_descend<T>(BLaunch{nb, st, -1, d_scene_of_, d_counters_}, lv, coarse_, sc, ms);
+                if (e == cudaSuccess)
+                    e = b_coarse_ascend<T>(BLaunch{nb, st, -1, d_scene_of_, d_counters_}, lv, coarse_, sc, ms,
+                                           T(ms.alpha));
+                return e;
+            };
+            float t[3] = {0.f, 0.f, 0.f};
+            err = run();
+            for (int r = 0; r < 3 && err == cudaSuccess; ++r) {
+                err = cudaEventRecord(e0, st);
+                if (err == cudaSuccess) err = run();
+                if (err == cudaSuccess) err = cudaEventRecord(e1, st);
+                if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+                if (err == cudaSuccess) err = cudaEventElapsedTime(&t[r], e0, e1);
+            }
+            if (err != cudaSuccess) break;
+            std::sort(t, t + 3);
+            if (best == 0.f || t[1] < best) {
+                best = t[1];
+                pick = nb;
+            }
+        }
+        coarse_blocks_ = pick;
+        if (err == cudaSuccess) {
+            // a barrier that ran out of its wait is an error here as in a solve
+            RUN_CUDA(cudaMemcpyAsync(h_counters_, d_counters_, sizeof(BatchCounters), cudaMemcpyDeviceToHost, st));
+            RUN_CUDA(cudaStreamSynchronize(st));
+            if (h_counters_->bar_err) err = cudaErrorLaunchTimeout;
+        }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (err != cudaSuccess)
         return fail(GBP_ERR_CUDA, std::string("tuning kernel occupancy: ") + cudaGetErrorString(err));
     std::lock_guard<std::mutex> lock(mu);
-    cache[key] = std::vector<int>(occ_, occ_ + BK_TUNED);
+    std::vector<int> choice(occ_, occ_ + BK_TUNED);
+    choice.push_back(coarse_blocks_);
+    cache[key] = choice;
     return GBP_OK;
-}
-
-static MgSettings settings_of(const gbp_params &p) {
-    MgSettings ms;
-    ms.smooth = p.mg_smooth > 0 ? p.mg_smooth : 1;
-    ms.coarsest_pairs = 4;
-    ms.alpha = 1.6;
-    return ms;
 }
 
 // One pass over the fine levels: the staged ones in one launch, the others
