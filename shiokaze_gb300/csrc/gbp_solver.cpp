@@ -417,6 +417,46 @@ int Solver::solve_mg(const Grid &g, const gbp_params &p, int grid_blocks, cudaSt
     return finish_batched(p, stream);
 }
 
+namespace {
+// Fine cells of level 0 by tile class, for the byte counts of the
+// multigrid kernels: [0] over the pair tiles (tcp), [1] over the
+// restriction tiles (tcr); classes mixed, uniform, empty. Without classes
+// every cell counts as mixed.
+template <class T> void class_cells(const MgHierarchy<T> &H, double out[2][3]) {
+    for (int a = 0; a < 2; ++a) out[a][0] = out[a][1] = out[a][2] = 0.0;
+    const MgLevel<T> &F = H.levels[0];
+    const Grid &g = F.g;
+    if (H.nlevels < 2 || !F.tcp || !F.tcr) {
+        out[0][0] = out[1][0] = (double)g.ncell;
+        return;
+    }
+    const Grid &C = H.levels[1].g;
+    const long long ntx2 = (g.nx + 63) / 64, np = ntx2 * g.nty * g.ntz, nr = C.ntiles;
+    std::vector<T> cp((size_t)np), cr((size_t)nr);
+    if (cudaMemcpy(cp.data(), F.tcp, sizeof(T) * np, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(cr.data(), F.tcr, sizeof(T) * nr, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        out[0][0] = out[1][0] = (double)g.ncell;
+        return;
+    }
+    auto cls = [](T v) { return v == T(TILE_EMPTY) ? 2 : (v >= T(0) && sizeof(T) == 4 ? 1 : 0); };
+    for (long long t = 0; t < np; ++t) {
+        const long long tx = t % ntx2, r = t / ntx2, ty = r % g.nty, tk = r / g.nty;
+        const double n = (double)std::min<long long>(64, g.nx - 64 * tx) * std::min<long long>(TILE_Y, g.ny - TILE_Y * ty) *
+                         std::min<long long>(g.tz, g.nz - g.tz * tk);
+        out[0][cls(cp[(size_t)t])] += n;
+    }
+    for (long long t = 0; t < nr; ++t) {
+        const long long tx = t % C.ntx, r = t / C.ntx, ty = r % C.nty, tk = r / C.nty;
+        const long long i0 = 2 * TILE_X * tx, j0 = 2 * TILE_Y * ty, k0 = g.dim == 3 ? 2LL * C.tz * tk : 0;
+        const long long bz = g.dim == 3 ? 2LL * C.tz : 1;
+        const double n = (double)std::max(0LL, std::min<long long>(2 * TILE_X, g.nx - i0)) *
+                         std::max(0LL, std::min<long long>(2 * TILE_Y, g.ny - j0)) *
+                         std::max(0LL, std::min<long long>(bz, g.nz - k0));
+        out[1][cls(cr[(size_t)t])] += n;
+    }
+}
+}  // namespace
+
 int Solver::bench_kernel(const Grid &g, int which, int reps, int grid_blocks, cudaStream_t stream, float *ms,
                          double *bytes) {
     if (!allocated_) return fail(GBP_ERR_INVALID_ARGUMENT, "bench_kernel: scene has not been projected yet");
@@ -458,10 +498,18 @@ int Solver::bench_kernel(const Grid &g, int which, int reps, int grid_blocks, cu
     case GBP_KERNEL_PCG_UPDATE: {
         if (runner_key_ < 0) return fail(GBP_ERR_INVALID_ARGUMENT, "bench_kernel: no multigrid solve yet");
         static const int map[8] = {0, -1, 1, 2, 3, 4, 5, 6};
-        static const double pc[8] = {6.0, 7.0, 6.125, 7.125, 7.0, 3.0, 6.0, 6.0};
+        // compulsory bytes per fine cell in units of the word size, for
+        // tiles of mixed couplings / uniform couplings (no coupling loads;
+        // FP32 only) / no unknown (zeros written or nothing)
+        static const double pc[8][3] = {{6.0, 3.0, 1.0},     {7.0, 4.0, 0.0},   {6.125, 3.125, 0.125},
+                                        {7.125, 4.125, 0.0}, {7.0, 4.0, 0.0},   {3.0, 3.0, 0.0},
+                                        {6.0, 3.0, 0.0},     {6.0, 6.0, 0.0}};
         const int k = which - GBP_KERNEL_MG_PRESMOOTH;
-        per_cell = pc[k] * s;
-        *bytes = per_cell * cells;
+        double cc[2][3];
+        if (mixed) class_cells(h32_, cc);
+        else class_cells(h64_, cc);
+        const int a = which == GBP_KERNEL_MG_RESTRICT ? 1 : 0;
+        *bytes = s * (pc[k][0] * cc[a][0] + pc[k][1] * cc[a][1] + pc[k][2] * cc[a][2]);
         const int rk = map[k];
         int rc = mixed ? runner_.bench<float>(rk, reps, stream, ms) : runner_.bench<double>(rk, reps, stream, ms);
         if (rc) return fail(rc, runner_.error());

@@ -40,6 +40,12 @@ inline void configure_params(shiokaze_v1::configuration &config, gbp_params &p, 
     config.get_integer("MGSmooth", p.mg_smooth, "Red-black sweeps per multigrid level");
     config.get_integer("MGCoarsest", p.mg_coarsest, "Coarsest multigrid edge");
     config.get_double("InnerTolerance", p.inner_tolerance, "Relative residual of each mixed-precision inner solve");
+    config.get_integer("IterationsPerSync", p.iterations_per_sync, "CG iterations between host convergence checks");
+    bool staging = p.tma_staging != 0, classes = p.tile_classes != 0;
+    config.get_bool("TMAStaging", staging, "Stage the FP32 fine-level stencils in shared memory by TMA");
+    config.get_bool("TileClasses", classes, "Use per-tile coupling classes in the multigrid kernels");
+    p.tma_staging = staging;
+    p.tile_classes = classes;
     config.get_integer("Device", device, "CUDA device");
     p.residual = residual;
     p.max_iterations = (int)max_iter;
