@@ -307,7 +307,9 @@ template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::s
         auto it = cache.find(key);
         if (it != cache.end()) {
             for (int k = 0; k < BK_TUNED; ++k) occ_[k] = it->second[k];
-            coarse_blocks_ = std::min(coarse_blocks_, it->second[BK_TUNED]);
+            // blocks per SM of the cooperative grid (0: all that stay resident)
+            const int f = it->second[BK_TUNED];
+            if (f > 0) coarse_blocks_ = std::min(coarse_blocks_, sms_ * f);
             return GBP_OK;
         }
     }
@@ -360,11 +362,13 @@ template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::s
         }
         occ_[k] = pick;
     }
+    int coarse_per_sm = 0;  // the cooperative grid's blocks per SM, 0: all resident (kept per key)
     if (err == cudaSuccess && coarse_blocks_ > 0) {
         const MgSettings ms = settings_of(p);
         const int full = coarse_blocks_;
         float best = 0.f;
         int pick = full;
+        coarse_per_sm = 0;
         for (int f : {2, 3, 4, 0}) {
             const int nb = f ? std::min(full, sms_ * f) : full;
             if (f && nb >= full) continue;
@@ -389,6 +393,7 @@ template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::s
             if (best == 0.f || t[1] < best) {
                 best = t[1];
                 pick = nb;
+                coarse_per_sm = f;
             }
         }
         coarse_blocks_ = pick;
@@ -405,7 +410,7 @@ template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::s
         return fail(GBP_ERR_CUDA, std::string("tuning kernel occupancy: ") + cudaGetErrorString(err));
     std::lock_guard<std::mutex> lock(mu);
     std::vector<int> choice(occ_, occ_ + BK_TUNED);
-    choice.push_back(coarse_blocks_);
+    choice.push_back(coarse_per_sm);
     cache[key] = choice;
     return GBP_OK;
 }

@@ -123,6 +123,26 @@ __device__ __forceinline__ double face_weight(double dt, double area, double rho
     return num / (dx * dx * rho);
 }
 
+// face_area of an interior 3D face from its four corner levels (q00, q10,
+// q11, q01 in the corner order of face_area).
+__device__ __forceinline__ float area3(float q00, float q10, float q11, float q01, const FaceParams &fp) {
+    double area;
+    // uniform squares decided in float (the same comparisons as in double);
+    // their fraction (1 or 0) is final unless eps_solid exceeds 1
+    if (q00 >= 0.0f && q10 >= 0.0f && q11 >= 0.0f && q01 >= 0.0f) {
+        if (fp.eps_solid_le1) return 1.0f;
+        area = 1.0;
+    } else if (q00 < 0.0f && q10 < 0.0f && q11 < 0.0f && q01 < 0.0f) {
+        return 0.0f;
+    } else {
+        area = 1.0 - solid_area(q00, q10, q11, q01);
+    }
+    if (area && area < fp.eps_solid) area = fp.eps_solid;
+    float a = (float)area;
+    if (!fp.second_order_solid && a) a = 1.0f;  // macpressuresolver3.cpp:76-80
+    return a;
+}
+
 // Open (non-solid) fraction of face (i,j,k) normal to d
 // (src/utility/macutility3.cpp:117-143; 2D macutility2.cpp:100-105).
 // Domain-boundary faces read 0; their value never reaches the outputs.
@@ -144,16 +164,7 @@ __device__ float face_area(const Grid &g, const float *__restrict__ solid, int d
         } else {
             q00 = S(i, j, k); q10 = S(i + 1, j, k); q11 = S(i + 1, j + 1, k); q01 = S(i, j + 1, k);
         }
-        // uniform squares decided in float (the same comparisons as in double);
-        // their fraction (1 or 0) is final unless eps_solid exceeds 1
-        if (q00 >= 0.0f && q10 >= 0.0f && q11 >= 0.0f && q01 >= 0.0f) {
-            if (fp.eps_solid_le1) return 1.0f;
-            area = 1.0;
-        } else if (q00 < 0.0f && q10 < 0.0f && q11 < 0.0f && q01 < 0.0f) {
-            return 0.0f;
-        } else {
-            area = 1.0 - solid_area(q00, q10, q11, q01);
-        }
+        return area3(q00, q10, q11, q01, fp);
     } else {
         const long long sx = g.nx + 1;
         double s0 = __ldg(solid + i + sx * j);
@@ -164,6 +175,30 @@ __device__ float face_area(const Grid &g, const float *__restrict__ solid, int d
     float a = (float)area;
     if (!fp.second_order_solid && a) a = 1.0f;  // macpressuresolver3.cpp:76-80
     return a;
+}
+
+// face_rho of a face between cells of levels f0 and f1, with fluid present.
+__device__ __forceinline__ float rho_of(float f0, float f1, const FaceParams &fp) {
+    // Same sign (or a zero): fraction() returns 1 or 0. The double product
+    // of two floats never underflows to 0, so its sign test equals this
+    // float sign test.
+    double rho;
+    if (!((f0 < 0.0f && f1 > 0.0f) || (f0 > 0.0f && f1 < 0.0f))) {
+        // 1 or 0, final unless eps_fluid exceeds 1
+        const bool wet = f0 < 0.0f || f1 < 0.0f;
+        if (!wet || fp.eps_fluid_le1) {
+            float r = wet ? 1.0f : 0.0f;
+            if (!fp.second_order_fluid && r) r = 1.0f;
+            return r;
+        }
+        rho = 1.0;
+    } else {
+        rho = fraction(f0, f1);
+    }
+    if (rho && rho < fp.eps_fluid) rho = fp.eps_fluid;
+    float r = (float)rho;
+    if (!fp.second_order_fluid && r) r = 1.0f;  // macpressuresolver3.cpp:70-74
+    return r;
 }
 
 // Liquid fraction of face (i,j,k) normal to d, between the clamped cells
@@ -180,24 +215,7 @@ __device__ float face_rho(const Grid &g, const float *__restrict__ fluid, int d,
             b2 = min(max(k - (d == 2), 0), g.nz - 1);
         const float f0 = __ldg(fluid + a0 + (long long)g.nx * (a1 + (long long)g.ny * a2));
         const float f1 = __ldg(fluid + b0 + (long long)g.nx * (b1 + (long long)g.ny * b2));
-        // Same sign (or a zero): fraction() returns 1 or 0. The double
-        // product of two floats never underflows to 0, so its sign test
-        // equals this float sign test.
-        double rho;
-        if (!((f0 < 0.0f && f1 > 0.0f) || (f0 > 0.0f && f1 < 0.0f))) {
-            // 1 or 0, final unless eps_fluid exceeds 1
-            const bool wet = f0 < 0.0f || f1 < 0.0f;
-            if (!wet || fp.eps_fluid_le1) {
-                r = wet ? 1.0f : 0.0f;
-                if (!fp.second_order_fluid && r) r = 1.0f;
-                return r;
-            }
-            rho = 1.0;
-        } else {
-            rho = fraction(f0, f1);
-        }
-        if (rho && rho < fp.eps_fluid) rho = fp.eps_fluid;
-        r = (float)rho;
+        return rho_of(f0, f1, fp);
     }
     if (!fp.second_order_fluid && r) r = 1.0f;  // macpressuresolver3.cpp:70-74
     return r;
@@ -456,10 +474,60 @@ __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt,
     const long long total = NX * NY * NZ;
     const float *vel[3] = {u, v, w};
     const int n[3] = {g.nx, g.ny, g.nz};
+    // One face's outputs from its fractions and velocity.
+    auto emit = [&](int d, long long f, float area, float rho, float uf) {
+        const bool open = area && rho;
+        fa.w[d][f] = !open ? -1.0 : (area == 1.0f && rho == 1.0f) ? fp.w_unit
+                                                                    : face_weight(dt, (double)area, (double)rho, dx, fp);
+        double q = 0.0;
+        bool fast = false;
+        if (area == 1.0f && fp.dx_pow2) q = scaled_to_double(uf, fp.inv_dx_exp, fast);  // (1 * u) / dx, exactly
+        if (!fast) q = area ? div_dx((double)area * (double)uf, dx, fp) : 0.0;
+        fa.q[d][f] = q;
+        fa.rho[d][f] = open ? rho : (area ? -1.0f : 0.0f);
+    };
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         node_coords(g, t, i, j, k);
+        if (g.dim == 3) {
+            // The node's three faces with every load issued first (the
+            // per-face form waits for each face's loads in turn: its stores
+            // could alias the next face's inputs). A face exists when its
+            // other two indices are cells; its area comes from its corners
+            // unless it lies on the domain boundary (area 0).
+            const bool ci = i < g.nx, cj = j < g.ny, ck = k < g.nz;
+            const bool ex[3] = {cj && ck, ci && ck, ci && cj};
+            const bool in[3] = {ex[0] && i > 0 && ci, ex[1] && j > 0 && cj, ex[2] && k > 0 && ck};
+            const long long sx = NX, sxy = NX * NY;
+            const float *s0 = solid + i + sx * j + sxy * k;
+            const float S000 = (in[0] || in[1] || in[2]) ? __ldg(s0) : 0.0f;
+            const float S010 = (in[0] || in[2]) ? __ldg(s0 + sx) : 0.0f;
+            const float S001 = (in[0] || in[1]) ? __ldg(s0 + sxy) : 0.0f;
+            const float S011 = in[0] ? __ldg(s0 + sx + sxy) : 0.0f;
+            const float S100 = (in[1] || in[2]) ? __ldg(s0 + 1) : 0.0f;
+            const float S101 = in[1] ? __ldg(s0 + 1 + sxy) : 0.0f;
+            const float S110 = in[2] ? __ldg(s0 + 1 + sx) : 0.0f;
+            // the face's cells, clamped as face_rho clamps them
+            const int a0 = min(i, g.nx - 1), a1 = min(j, g.ny - 1), a2 = min(k, g.nz - 1);
+            const long long ca = cell_index(g, a0, a1, a2);
+            const bool any = ex[0] || ex[1] || ex[2];
+            const float fA = any ? __ldg(fluid + ca) : 0.0f;
+            const float fB0 = ex[0] ? __ldg(fluid + cell_index(g, min(max(i - 1, 0), g.nx - 1), a1, a2)) : 0.0f;
+            const float fB1 = ex[1] ? __ldg(fluid + cell_index(g, a0, min(max(j - 1, 0), g.ny - 1), a2)) : 0.0f;
+            const float fB2 = ex[2] ? __ldg(fluid + cell_index(g, a0, a1, min(max(k - 1, 0), g.nz - 1))) : 0.0f;
+            long long f[3];
+            float uf[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                f[d] = face_index(g, d, i, j, k);
+                uf[d] = ex[d] ? __ldg(vel[d] + f[d]) : 0.0f;
+            }
+            if (ex[0]) emit(0, f[0], in[0] ? area3(S000, S010, S011, S001, fp) : 0.0f, rho_of(fA, fB0, fp), uf[0]);
+            if (ex[1]) emit(1, f[1], in[1] ? area3(S000, S100, S101, S001, fp) : 0.0f, rho_of(fA, fB1, fp), uf[1]);
+            if (ex[2]) emit(2, f[2], in[2] ? area3(S000, S100, S110, S010, fp) : 0.0f, rho_of(fA, fB2, fp), uf[2]);
+            continue;
+        }
         const int pi[3] = {i, j, k};
         for (int d = 0; d < g.dim; ++d) {
             bool exists = true;
@@ -467,18 +535,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt,
                 if (e != d && pi[e] >= n[e]) exists = false;
             if (!exists) continue;
             const long long f = face_index(g, d, i, j, k);
-            const float area = face_area(g, solid, d, i, j, k, fp);
-            const float rho = face_rho(g, fluid, d, i, j, k, fp, 1);
-            const bool open = area && rho;
-            fa.w[d][f] = !open ? -1.0 : (area == 1.0f && rho == 1.0f) ? fp.w_unit
-                                                                        : face_weight(dt, (double)area, (double)rho, dx, fp);
-            const float uf = __ldg(vel[d] + f);
-            double q = 0.0;
-            bool fast = false;
-            if (area == 1.0f && fp.dx_pow2) q = scaled_to_double(uf, fp.inv_dx_exp, fast);  // (1 * u) / dx, exactly
-            if (!fast) q = area ? div_dx((double)area * (double)uf, dx, fp) : 0.0;
-            fa.q[d][f] = q;
-            fa.rho[d][f] = open ? rho : (area ? -1.0f : 0.0f);
+            emit(d, f, face_area(g, solid, d, i, j, k, fp), face_rho(g, fluid, d, i, j, k, fp, 1), __ldg(vel[d] + f));
         }
     }
 }
@@ -502,28 +559,44 @@ __global__ void __launch_bounds__(BLOCK_THREADS) assemble_faces_kernel(
             const long long c = cell_index(g, i, j, k);
             double dg = 0.0, rhs = 0.0, cpl[3] = {0.0, 0.0, 0.0};
             bool unknown = false;
-            if (__ldg(fluid + c) < 0.0f) {
+            // every load of the cell's row first (its own level, and per face
+            // in the order +x, -x, +y, -y, +z, -z: fraction, weight, flux and
+            // the neighbour's level), then the row in that order
+            const int n[3] = {g.nx, g.ny, g.nz};
+            const float fc = __ldg(fluid + c);
+            float fr[6], fq[6];
+            double wv[6], qv[6];
+            bool has[6];
+#pragma unroll
+            for (int nq = 0; nq < 6; ++nq) {
+                const int d = nq >> 1;
+                const bool plus = (nq & 1) == 0;
+                int q[3] = {i, j, k};
+                q[d] += plus ? 1 : -1;
+                has[nq] = d < g.dim && q[d] >= 0 && q[d] < n[d];
+                int f[3] = {i, j, k};
+                if (plus) f[d] += 1;
+                const long long fi = has[nq] ? face_index(g, d, f[0], f[1], f[2]) : 0;
+                fr[nq] = has[nq] ? __ldg(fa.rho[d] + fi) : 0.0f;
+                wv[nq] = has[nq] ? __ldg(fa.w[d] + fi) : 0.0;
+                qv[nq] = has[nq] ? __ldg(fa.q[d] + fi) : 0.0;
+                fq[nq] = has[nq] ? __ldg(fluid + cell_index(g, q[0], q[1], q[2])) : 0.0f;
+            }
+            if (fc < 0.0f) {
                 my_fluid = 1;
-                const int n[3] = {g.nx, g.ny, g.nz};
-                for (int nq = 0; nq < 2 * g.dim; ++nq) {
+#pragma unroll
+                for (int nq = 0; nq < 6; ++nq) {
+                    if (!has[nq]) continue;
                     const int d = nq >> 1;
                     const bool plus = (nq & 1) == 0;
-                    int q[3] = {i, j, k};
-                    q[d] += plus ? 1 : -1;
-                    if (q[d] < 0 || q[d] >= n[d]) continue;
-                    int f[3] = {i, j, k};
-                    if (plus) f[d] += 1;
-                    const long long fi = face_index(g, d, f[0], f[1], f[2]);
-                    if (__ldg(fa.rho[d] + fi) > 0.0f) {  // open face
-                        const double wv = __ldg(fa.w[d] + fi);
-                        if (__ldg(fluid + cell_index(g, q[0], q[1], q[2])) < 0.0f) {
+                    if (fr[nq] > 0.0f) {  // open face
+                        if (fq[nq] < 0.0f) {
                             unknown = true;
-                            if (plus) cpl[d] = wv;
+                            if (plus) cpl[d] = wv[nq];
                         }
-                        dg += wv;
+                        dg += wv[nq];
                     }
-                    const double qv = __ldg(fa.q[d] + fi);
-                    rhs += plus ? -qv : qv;
+                    rhs += plus ? -qv[nq] : qv[nq];
                 }
             }
             if (unknown) {
@@ -566,41 +639,45 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_faces_kernel(Grid g, d
     const long long total = NX * NY * NZ;
     float *vel[3] = {u, v, w};
     const int n[3] = {g.nx, g.ny, g.nz};
+    // the new velocity of one face from its stored fraction (fr), the
+    // pressures on its two sides and its velocity; interior: not on the
+    // domain boundary
+    auto update = [&](float fr, bool interior, float pc, float pm, float uf) {
+        const bool open = fluid_exists ? fr > 0.0f : fr != 0.0f;
+        const float rho = fluid_exists ? fr : 1.0f;
+        if (!open || !interior) return 0.0f;
+        const float dp = pc - pm;
+        // rho * dx == dx exactly when rho == 1
+        const double val = rho == 1.0f ? div_dx(dt * (double)dp, dx, fp) : dt * (double)dp / ((double)rho * dx);
+        return uf - (float)val;
+    };
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         node_coords(g, t, i, j, k);
         const int pi[3] = {i, j, k};
-        for (int d = 0; d < g.dim; ++d) {
-            bool exists = true;
+        bool ex[3], in[3];
+        long long f[3];
+        float fr[3], pm[3], uf[3];
+        bool any_in = false;
+        // every load of the node's faces first, then the updates (the
+        // per-face form waits for each face's loads in turn)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            ex[d] = d < g.dim;
             for (int e = 0; e < g.dim; ++e)
-                if (e != d && pi[e] >= n[e]) exists = false;
-            if (!exists) continue;
-            const long long f = face_index(g, d, i, j, k);
-            const float fr = __ldg(fa.rho[d] + f);
-            const bool open = fluid_exists ? fr > 0.0f : fr != 0.0f;
-            const float rho = fluid_exists ? fr : 1.0f;
-            float out = 0.0f;
-            if (open && !(pi[d] == 0 || pi[d] == n[d])) {
-                int m[3] = {i, j, k};
-                m[d] -= 1;
-                const float pc = __ldg(p + cell_index(g, i, j, k));
-                const float pm = __ldg(p + cell_index(g, m[0], m[1], m[2]));
-                const float dp = pc - pm;
-                double val;
-                if (rho == 1.0f && fp.dx_pow2) {
-                    // (dt dp) / dx with dx = 2^-e: the scaling commutes with the
-                    // rounding of the product, so (dt 2^e) dp is the same double
-                    bool ok;
-                    const double dpd = scaled_to_double(dp, 0, ok);
-                    val = fp.dt_inv_dx * (ok ? dpd : (double)dp);
-                } else {
-                    val = rho == 1.0f ? div_dx(dt * (double)dp, dx, fp) : dt * (double)dp / ((double)rho * dx);
-                }
-                out = vel[d][f] - (float)val;
-            }
-            vel[d][f] = out;
+                if (e != d && pi[e] >= n[e]) ex[d] = false;
+            in[d] = ex[d] && pi[d] > 0 && pi[d] < n[d];
+            any_in = any_in || in[d];
+            f[d] = ex[d] ? face_index(g, d, i, j, k) : 0;
+            fr[d] = ex[d] ? __ldg(fa.rho[d] + f[d]) : 0.0f;
+            uf[d] = in[d] ? vel[d][f[d]] : 0.0f;
+            pm[d] = in[d] ? __ldg(p + cell_index(g, i - (d == 0), j - (d == 1), k - (d == 2))) : 0.0f;
         }
+        const float pc = any_in ? __ldg(p + cell_index(g, i, j, k)) : 0.0f;
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            if (ex[d]) vel[d][f[d]] = update(fr[d], in[d], pc, pm[d], uf[d]);
     }
 }
 
