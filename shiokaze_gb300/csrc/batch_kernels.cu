@@ -1127,10 +1127,15 @@ template <class T, class F> __device__ __forceinline__ void s_for_cells(const SL
     }
     __syncthreads();
 }
-// The V-cycle of the levels lv[0..nt) from shared memory: b of lv[0] in,
-// x of lv[0] out, same smoother, transfers and coarsest solve (FP64
+// The V-cycle of the levels lv[0..nt) in one block per scene: b of lv[0]
+// in, x of lv[0] out, same smoother, transfers and coarsest solve (FP64
 // symmetric sweep pairs, with the coarsest operator and right-hand side
-// held in FP64) as the global levels.
+// held in FP64) as the global levels. The levels (a few hundred KB at
+// most) are read and written in place in global memory, where the block's
+// L1 holds them between passes; __syncthreads orders a pass's writes
+// before the next pass's reads within the block. (A copy into shared memory
+// needs a carveout of the SM's L1 different from every other kernel's, and
+// the switch costs more than the copy saves.)
 template <class T>
 __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *__restrict__ tails,
                                                                const BScene<T> *__restrict__ scenes, int gate,
@@ -1140,14 +1145,12 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
     const BTail<T> &A = tails[s];
     if (A.nt <= 0) return;
     if (gated(scenes[s].sc, gate)) return;
-    extern __shared__ __align__(16) unsigned char tail_smem[];
     __shared__ SLevel<T> S[MG_MAX_LEVELS];
     __shared__ double *cd[6];  // coarsest: x, b, inv, cx, cy, cz in FP64
     if (threadIdx.x == 0) {
-        size_t off = 0;
-        T *base = reinterpret_cast<T *>(tail_smem);
         for (int l = 0; l < A.nt; ++l) {
-            const Grid &g = A.lv[l].g;
+            const MgLevel<T> &G = A.lv[l];
+            const Grid &g = G.g;
             SLevel<T> &L = S[l];
             L.nx = g.nx;
             L.ny = g.ny;
@@ -1157,28 +1160,15 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
             L.hx = (g.nx + 1) / 2;
             L.fhx = make_fastdiv((unsigned)L.hx);
             L.fhxy = make_fastdiv((unsigned)(L.hx * g.ny));
-            T **arr[7] = {&L.b, &L.x, &L.inv, &L.diag, &L.cx, &L.cy, &L.cz};
-            for (int a = 0; a < 7; ++a) {
-                *arr[a] = base + off;
-                off += (size_t)L.n;
-            }
+            L.b = G.b;
+            L.x = G.x;
+            L.inv = const_cast<T *>(G.inv);
+            L.diag = const_cast<T *>(G.diag);
+            L.cx = const_cast<T *>(G.cx);
+            L.cy = const_cast<T *>(G.cy);
+            L.cz = const_cast<T *>(G.cz);  // == cy in 2D, never read there
         }
-        size_t off_bytes = (off * sizeof(T) + 15) / 16 * 16;
-        const int nc = (int)A.lv[A.nt - 1].g.ncell;
-        for (int a = 0; a < 6; ++a) cd[a] = reinterpret_cast<double *>(tail_smem + off_bytes) + (size_t)a * nc;
-    }
-    __syncthreads();
-    for (int l = 0; l < A.nt; ++l) {
-        const MgLevel<T> &G = A.lv[l];
-        const SLevel<T> &L = S[l];
-        for (int c = threadIdx.x; c < L.n; c += blockDim.x) {
-            L.inv[c] = G.inv[c];
-            L.diag[c] = G.diag[c];
-            L.cx[c] = G.cx[c];
-            L.cy[c] = G.cy[c];
-            L.cz[c] = L.dim == 3 ? G.cz[c] : T(0);
-            if (l == 0) L.b[c] = G.b[c];
-        }
+        for (int a = 0; a < 6; ++a) cd[a] = A.c64 + (size_t)a * MG_COARSEST_MAX;
     }
     __syncthreads();
     const T alpha = T(ms.alpha);
@@ -1264,8 +1254,6 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
             L.x[c] = (L.b[c] + snb(L, i, j, k, c, [&](int m, int, int, int) { return L.x[m]; })) * L.inv[c];
         });
     }
-    const SLevel<T> &L0 = S[0];
-    for (int c = threadIdx.x; c < L0.n; c += blockDim.x) A.lv[0].x[c] = L0.x[c];
 }
 
 // ---- CG on the fine level -----------------------------------------------------------
@@ -2028,7 +2016,8 @@ cudaError_t b_red_dot(const BLaunch &L, const BLevel<T> *levels, const BSeg *seg
 template <class T>
 cudaError_t b_tail(const BLaunch &L, const BTail<T> *tails, int nscenes, const BScene<T> *scenes, MgSettings ms,
                    size_t smem) {
-    tail_kernel<T><<<nscenes, MG_TAIL_THREADS, smem, L.stream>>>(tails, scenes, L.gate, ms, L.cnt);
+    (void)smem;
+    tail_kernel<T><<<nscenes, MG_TAIL_THREADS, 0, L.stream>>>(tails, scenes, L.gate, ms, L.cnt);
     return cudaGetLastError();
 }
 template <class T> cudaError_t b_tail_enable(size_t bytes) {

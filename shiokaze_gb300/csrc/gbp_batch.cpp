@@ -182,7 +182,15 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
         if ((rc = upload(plan.scene_of.data(), plan.scene_of.size() * sizeof(int), &d))) return rc;
         d_scene_of_ = static_cast<int *>(d);
     }
-    if ((rc = upload(plan.tails.data(), plan.tails.size() * sizeof(BTail<T>), &d_tails_))) return rc;
+    {
+        // FP64 scratch of each scene's coarsest level, then the tail table
+        void *d;
+        const size_t per = 6 * (size_t)MG_COARSEST_MAX;
+        if ((rc = upload(nullptr, sizeof(double) * per * std::max<size_t>(1, plan.tails.size()), &d))) return rc;
+        std::vector<BTail<T>> tails = plan.tails;
+        for (size_t s = 0; s < tails.size(); ++s) tails[s].c64 = static_cast<double *>(d) + s * per;
+        if ((rc = upload(tails.data(), tails.size() * sizeof(BTail<T>), &d_tails_))) return rc;
+    }
     size_t max_items = (size_t)plan.n_fine_pairs;
     auto segs = [&](const std::vector<BSeg> &list, BSeg **dst, int *nseg) -> int {
         void *d;
@@ -257,7 +265,6 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
     if ((rc = upload(nullptr, sizeof(BatchCounters), &d))) return rc;
     d_counters_ = static_cast<BatchCounters *>(d);
     RUN_CUDA(cudaMallocHost(&h_counters_, sizeof(BatchCounters)));
-    if (tail_smem_ > 0) RUN_CUDA(b_tail_enable<T>(tail_smem_));
     if (n_fine_staged_ > 0) stage_mask_ = (1 << STAGE_KINDS) - 1;
     // occupancy variants, tuned per precision and half-octave of fine cells
     long long cells = 0;

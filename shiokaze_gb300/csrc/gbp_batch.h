@@ -124,6 +124,9 @@ __host__ __device__ inline BItem item_at(const BSeg *segs, int nseg, int w, int 
 template <class T> struct BTail {
     int nt;
     MgLevel<T> lv[MG_MAX_LEVELS];
+    // the coarsest level in FP64 (x, b, inv, cx, cy, cz; MG_COARSEST_MAX
+    // each), scratch of the batch runner
+    double *c64;
 };
 
 // Tilings: pair tiles (64 x 8 x tz) for the red-black kernels, cell tiles
