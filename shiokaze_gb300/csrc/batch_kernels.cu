@@ -1288,17 +1288,36 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
                 });
                 return;
             }
-            pair_tile(L.g, it, [&](int, int, int, long long c, bool second) {
+            const bool fresh = beta == T(0);
+            auto plane = [&](int, int, int, long long c, bool second) {
                 const Pair<T> z2 = ld2<T, V>(S.z, c, second);
                 Pair<T> p2;
-                if (beta == T(0)) {
+                if (fresh) {
                     p2 = z2;
                 } else {
                     const Pair<T> o = ld2<T, V>(S.p, c, second);
-                    p2 = Pair<T>{z2.a + beta * o.a, z2.b + beta * o.b};
+                    p2 = Pair<T>{fmadd(z2.a, beta, o.a), fmadd(z2.b, beta, o.b)};
                 }
                 st2<T, V>(S.p, c, p2, second);
-            });
+            };
+            if constexpr (V)
+                // the column's loads first (see pair_tile_z4)
+                pair_tile_z4(L.g, it, [&](int, int, int, long long c0) {
+                    const long long sz = (long long)L.g.nx * L.g.ny;
+                    Pair<T> z2[4], o[4];
+#pragma unroll
+                    for (int z = 0; z < 4; ++z) {
+                        z2[z] = ld2<T, true>(S.z, c0 + z * sz, true);
+                        o[z] = fresh ? Pair<T>{T(0), T(0)} : ld2<T, true>(S.p, c0 + z * sz, true);
+                    }
+#pragma unroll
+                    for (int z = 0; z < 4; ++z)
+                        st2<T, true>(S.p, c0 + z * sz,
+                                     fresh ? z2[z] : Pair<T>{fmadd(z2[z].a, beta, o[z].a), fmadd(z2[z].b, beta, o[z].b)},
+                                     true);
+                }, plane);
+            else
+                pair_tile(L.g, it, plane);
         });
     }
 }
@@ -1383,7 +1402,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
                     });
                     return;
                 }
-                pair_tile(L.g, it, [&](int, int, int, long long c, bool second) {
+                auto plane = [&](int, int, int, long long c, bool second) {
                     const Pair<T> p2 = ld2<T, V>(S.p, c, second), q2 = ld2<T, V>(S.q, c, second);
                     const Pair<T> r2 = ld2<T, V>(S.r, c, second);
                     Pair<T> x2;
@@ -1391,14 +1410,42 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
                         x2 = Pair<T>{alpha * p2.a, alpha * p2.b};
                     } else {
                         const Pair<T> o = ld2<T, V>(S.x, c, second);
-                        x2 = Pair<T>{o.a + alpha * p2.a, o.b + alpha * p2.b};
+                        x2 = Pair<T>{fmadd(o.a, alpha, p2.a), fmadd(o.b, alpha, p2.b)};
                     }
-                    const Pair<T> rn{r2.a - alpha * q2.a, r2.b - alpha * q2.b};
+                    const Pair<T> rn{fmadd(r2.a, -alpha, q2.a), fmadd(r2.b, -alpha, q2.b)};
                     st2<T, V>(S.x, c, x2, second);
                     st2<T, V>(S.r, c, rn, second);
                     acc.add(rn.a);
                     if (second) acc.add(rn.b);
-                });
+                };
+                if constexpr (V)
+                    // the column's loads first (see pair_tile_z4)
+                    pair_tile_z4(L.g, it, [&](int, int, int, long long c0) {
+                        const long long sz = (long long)L.g.nx * L.g.ny;
+                        Pair<T> p2[4], q2[4], r2[4], o[4];
+#pragma unroll
+                        for (int z = 0; z < 4; ++z) {
+                            const long long c = c0 + z * sz;
+                            p2[z] = ld2<T, true>(S.p, c, true);
+                            q2[z] = ld2<T, true>(S.q, c, true);
+                            r2[z] = ld2<T, true>(S.r, c, true);
+                            o[z] = overwrite ? Pair<T>{T(0), T(0)} : ld2<T, true>(S.x, c, true);
+                        }
+#pragma unroll
+                        for (int z = 0; z < 4; ++z) {
+                            const long long c = c0 + z * sz;
+                            const Pair<T> x2 = overwrite ? Pair<T>{alpha * p2[z].a, alpha * p2[z].b}
+                                                         : Pair<T>{fmadd(o[z].a, alpha, p2[z].a),
+                                                                   fmadd(o[z].b, alpha, p2[z].b)};
+                            const Pair<T> rn{fmadd(r2[z].a, -alpha, q2[z].a), fmadd(r2[z].b, -alpha, q2[z].b)};
+                            st2<T, true>(S.x, c, x2, true);
+                            st2<T, true>(S.r, c, rn, true);
+                            acc.add(rn.a);
+                            acc.add(rn.b);
+                        }
+                    }, plane);
+                else
+                    pair_tile(L.g, it, plane);
             });
         },
         [&](const BItem &it, int flushes) {
