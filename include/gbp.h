@@ -87,7 +87,7 @@ typedef struct gbp_params {
     double surface_tension; /* the surface_tension argument of macproject3_interface::project
                                (macpressuresolver3.cpp:85-115); 0 (default) leaves the velocity as is */
     int tma_staging;        /* MGPCG MIXED: nonzero runs the fine level's four stencil passes with their
-                               tiles staged in shared memory by TMA where the grid allows it (3D, more than
+                               tiles staged in shared memory by TMA where the grid allows it (3D, at least
                                2^21 cells, nx % 8 == 0); 0 (default) uses the direct-load kernels, which
                                compute every cell alike and measure faster over a whole solve on GB300 */
     int tile_classes;       /* MGPCG: nonzero (default) lets the multigrid and CG kernels use the tile classes of

@@ -67,15 +67,20 @@ struct Grid {
     FastDiv fn1, fn2;
 };
 
-inline Grid make_grid(int dim, int nx, int ny, int nz) {
+// deep_min: the fewest cells for tiles 4 planes deep. Deep tiles give a
+// block more cells and the gather-first column kernels their 4 planes;
+// thin ones spread small grids over all SMs. A scene's fine grid takes deep
+// tiles from 2^21 cells (128^3), coarse levels only above (their 2^21-cell
+// level, under a 256^3 grid, balances better in thin tiles).
+constexpr long long DEEP_MIN_FINE = 1LL << 21;
+constexpr long long DEEP_MIN_COARSE = (1LL << 21) + 1;
+inline Grid make_grid(int dim, int nx, int ny, int nz, long long deep_min = DEEP_MIN_FINE) {
     Grid g;
     g.dim = dim;
     g.nx = nx;
     g.ny = ny;
     g.nz = dim == 3 ? nz : 1;
-    // deep tiles for big grids (more cells per block), thin ones for small
-    // grids so their tiles spread over all SMs
-    g.tz = (g.nz == 1 || (long long)nx * ny * g.nz <= (1LL << 21)) ? 1 : 4;
+    g.tz = (g.nz == 1 || (long long)nx * ny * g.nz < deep_min) ? 1 : 4;
     g.ntx = (nx + TILE_X - 1) / TILE_X;
     g.nty = (ny + TILE_Y - 1) / TILE_Y;
     g.ntz = (g.nz + g.tz - 1) / g.tz;

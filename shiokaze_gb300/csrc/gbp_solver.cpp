@@ -41,7 +41,8 @@ std::vector<Grid> mg_level_grids(const Grid &g, int coarsest) {
         const int mx = std::max(f.nx, std::max(f.ny, f.nz));
         // at least two levels (the fine level always runs the global kernels)
         if (out.size() >= 2 && ((mx <= coarsest && f.ncell <= MG_COARSEST_MAX) || mx <= 1)) break;
-        out.push_back(make_grid(f.dim, (f.nx + 1) / 2, (f.ny + 1) / 2, f.dim == 3 ? (f.nz + 1) / 2 : 1));
+        out.push_back(make_grid(f.dim, (f.nx + 1) / 2, (f.ny + 1) / 2, f.dim == 3 ? (f.nz + 1) / 2 : 1,
+                                DEEP_MIN_COARSE));
     }
     return out;
 }

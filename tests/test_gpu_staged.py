@@ -1,7 +1,7 @@
 """TMA-staged fine-level kernels (FP32 MGPCG) against the direct-load kernels.
 
 A fine level is staged (TMAStaging=1; the default, 0, uses the direct-load
-kernels) when it is 3D with 4-plane tiles (more than 2^21 cells) and nx is
+kernels) when it is 3D with 4-plane tiles (2^21 cells or more) and nx is
 a multiple of 8. The staged kernels compute each cell with the same
 arithmetic as the direct-load ones; a solve differs only through
 the grouping of its dot-product partials (the staged launch runs one block

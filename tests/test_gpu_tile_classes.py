@@ -3,7 +3,7 @@ every coupling array (TileClasses=0).
 
 In the FP32 kernels a tile whose stencils read only couplings of one value
 u uses u instead of the arrays (the same products in the same order; on
-4-plane tiles of grids over 2^21 cells, with every load of a thread's
+4-plane tiles (fine grids of 2^21 cells or more), with every load of a thread's
 column issued first); in
 both precisions a tile with no unknown writes zeros without loading, or
 is skipped where its values are already 0. The solves must therefore
