@@ -1217,21 +1217,39 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) tail_kernel(const BTail<T> *_
         }
         __syncthreads();
         const int sy = L.nx, sz = L.nx * L.ny;
-        for (int p = 0; p < ms.coarsest_pairs; ++p) {
-            const int order[4] = {0, 1, 1, 0};
-            for (int q = 0; q < 4; ++q)
-                s_for_color(L, order[q], [&](int i, int j, int k, int c) {
-                    double acc = 0.0;
-                    if (i > 0) acc += cxd[c - 1] * xc[c - 1];
-                    if (i + 1 < L.nx) acc += cxd[c] * xc[c + 1];
-                    if (j > 0) acc += cyd[c - sy] * xc[c - sy];
-                    if (j + 1 < L.ny) acc += cyd[c] * xc[c + sy];
-                    if (L.dim == 3) {
-                        if (k > 0) acc += czd[c - sz] * xc[c - sz];
-                        if (k + 1 < L.nz) acc += czd[c] * xc[c + sz];
+        auto relax = [&](int i, int j, int k, int c) {
+            double acc = 0.0;
+            if (i > 0) acc += cxd[c - 1] * xc[c - 1];
+            if (i + 1 < L.nx) acc += cxd[c] * xc[c + 1];
+            if (j > 0) acc += cyd[c - sy] * xc[c - sy];
+            if (j + 1 < L.ny) acc += cyd[c] * xc[c + sy];
+            if (L.dim == 3) {
+                if (k > 0) acc += czd[c - sz] * xc[c - sz];
+                if (k + 1 < L.nz) acc += czd[c] * xc[c + sz];
+            }
+            xc[c] = (bd[c] + acc) * ivd[c];
+        };
+        const int order[4] = {0, 1, 1, 0};
+        const int slots = L.hx * L.ny * L.nz;
+        if (slots <= 32) {
+            // a coarsest level of one warp's slots (4^3 and below): the
+            // warp sweeps it alone, with warp barriers between half-sweeps,
+            // so it can afford more sweep pairs
+            if (threadIdx.x < 32) {
+                const int p = threadIdx.x;
+                const int t = (int)fdiv((unsigned)p, L.fhx), k = (int)fdiv((unsigned)p, L.fhxy);
+                const int j = t - k * L.ny;
+                for (int pr = 0; pr < ms.coarsest_pairs_warp; ++pr)
+                    for (int q = 0; q < 4; ++q) {
+                        const int i = 2 * (p - t * L.hx) + ((j + k + order[q]) & 1);
+                        if (p < slots && i < L.nx) relax(i, j, k, i + L.nx * (j + L.ny * k));
+                        __syncwarp();
                     }
-                    xc[c] = (bd[c] + acc) * ivd[c];
-                });
+            }
+            __syncthreads();
+        } else {
+            for (int p = 0; p < ms.coarsest_pairs; ++p)
+                for (int q = 0; q < 4; ++q) s_for_color(L, order[q], relax);
         }
         for (int c = threadIdx.x; c < L.n; c += blockDim.x) L.x[c] = T(xc[c]);
         __syncthreads();

@@ -87,7 +87,7 @@ void gbp_params_default(gbp_params *p) {
     p->solver = GBP_SOLVER_CG;
     p->precision = GBP_PRECISION_FP64;
     p->mg_smooth = 1;
-    p->mg_coarsest = 8;
+    p->mg_coarsest = 4;
     p->inner_tolerance = 1e-3;
     p->iterations_per_sync = 16;
     p->surface_tension = 0.0;

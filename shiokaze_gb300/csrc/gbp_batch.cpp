@@ -288,6 +288,7 @@ static MgSettings settings_of(const gbp_params &p) {
     MgSettings ms;
     ms.smooth = p.mg_smooth > 0 ? p.mg_smooth : 1;
     ms.coarsest_pairs = 4;
+    ms.coarsest_pairs_warp = 8;
     ms.alpha = 1.6;
     return ms;
 }

@@ -67,6 +67,7 @@ template <class T> void mg_plan_tail(MgHierarchy<T> &H) {
 struct MgSettings {
     int smooth;          // red-black sweeps before and after each coarse correction
     int coarsest_pairs;  // symmetric sweep pairs on the coarsest level
+    int coarsest_pairs_warp;  // the same when the coarsest level fits one warp's slots
     double alpha;        // scale of the coarse-grid correction
 };
 
