@@ -112,8 +112,31 @@ typedef struct gbp_stats {
     int tma_staged;         /* the fine level ran the TMA-staged kernels (see gbp_params.tma_staging) */
 } gbp_stats;
 
+/* Result of gbp_csr_cg. */
+typedef struct gbp_csr_stats {
+    int iterations;         /* CG iterations, as pcg_solver.h:283-293 counts them */
+    int converged;          /* stopping rule met (or b == 0) */
+    double reresid;         /* |r|_inf / |b|_inf at exit: the residual the reference's pcg module returns */
+    float ms_solve;         /* device time of the iterations */
+    float ms_total;         /* host wall time of the call, copies included */
+} gbp_csr_stats;
+
 /* Fills *p with the reference's defaults (and CG / FP64). */
 void gbp_params_default(gbp_params *p);
+
+/* Solves A x = b on the GPU for a symmetric positive (semi)definite matrix
+ * of n rows in compressed rows (host arrays: rowstart[0..n], rowstart[0] = 0;
+ * column indices cols[rowstart[r]..rowstart[r+1]) in [0, n) and values vals
+ * alike; duplicate entries of a row add up), with the reference's LinSolver
+ * "pcg" (src/linsolver/pcg.cpp:44-74; local/include/pcgsolver/pcg_solver.h:
+ * 246-295): plain CG from x = 0 in FP64 until |r|_inf <= residual |b|_inf
+ * or max_iterations. x (n values) receives the solution (the last iterate
+ * if not converged). Returns GBP_OK, GBP_ERR_NOT_CONVERGED, GBP_ERR_NAN
+ * (breakdown) or an argument / CUDA error; stats may be NULL. The matrix
+ * and vectors are copied to the device on every call; the context keeps the
+ * device arrays between calls of up to the same sizes. */
+int gbp_csr_cg(gbp_ctx *ctx, long long n, const long long *rowstart, const long long *cols, const double *vals,
+               const double *b, double *x, double residual, int max_iterations, gbp_csr_stats *stats);
 
 /* Context on CUDA device `device`: stream, events, graph cache. */
 int gbp_create(int device, gbp_ctx **out);

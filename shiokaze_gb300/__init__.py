@@ -60,6 +60,14 @@ class Stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class CsrStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("reresid", ctypes.c_double),
+                ("ms_solve", ctypes.c_float), ("ms_total", ctypes.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class GBPError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"gbp error {code}: {msg}")
@@ -115,6 +123,9 @@ def load_library():
     pp = ctypes.POINTER(vp)
     lib.gbp_batch_project_device.argtypes = [vp, ctypes.POINTER(ctypes.c_double), pp, pp, pp, pp, pp,
                                              ctypes.POINTER(Params), pp, ctypes.POINTER(Stats), vp]
+    lp = ctypes.POINTER(ctypes.c_longlong)
+    lib.gbp_csr_cg.argtypes = [vp, ctypes.c_longlong, lp, lp, dp, dp, dp, ctypes.c_double, ctypes.c_int,
+                               ctypes.POINTER(CsrStats)]
     lib.gbp_launch_count.argtypes = [vp]
     lib.gbp_launch_count.restype = ctypes.c_longlong
     lib.gbp_strerror.argtypes = [ctypes.c_int]
@@ -190,6 +201,30 @@ def default_context() -> Context:
     if _default_ctx is None:
         _default_ctx = Context(0)
     return _default_ctx
+
+
+def csr_cg(indptr, indices, data, b, residual=1e-4, max_iterations=30000, context: Context | None = None):
+    """Solves A x = b for A in compressed rows (indptr, indices, data: the
+    row pointers, column indices and values of a symmetric positive
+    (semi)definite matrix) with the reference's LinSolver "pcg" algorithm
+    (plain FP64 CG from x = 0, stop at |r|_inf <= residual |b|_inf) on the
+    GPU. Returns (x, status, stats)."""
+    ctx = context or default_context()
+    lib = ctx.lib
+    ip = np.ascontiguousarray(indptr, dtype=np.int64)
+    ix = np.ascontiguousarray(indices, dtype=np.int64)
+    va = np.ascontiguousarray(data, dtype=np.float64)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    n = bb.shape[0]
+    assert ip.shape[0] == n + 1, "indptr must have n + 1 entries"
+    x = np.zeros(n, np.float64)
+    st = CsrStats()
+    lp = ctypes.POINTER(ctypes.c_longlong)
+    dpp = ctypes.POINTER(ctypes.c_double)
+    rc = lib.gbp_csr_cg(ctx.handle, n, ip.ctypes.data_as(lp), ix.ctypes.data_as(lp), va.ctypes.data_as(dpp),
+                        bb.ctypes.data_as(dpp), x.ctypes.data_as(dpp), residual, max_iterations, ctypes.byref(st))
+    check(rc, (GBP_OK, GBP_ERR_NOT_CONVERGED, GBP_ERR_NAN))
+    return x, rc, st.as_dict()
 
 
 def _host_f32(a):

@@ -20,6 +20,7 @@
 #include <string>
 #include <vector>
 
+#include "csr_solver.h"
 #include "gbp_kernels.h"
 #include "gbp_solver.h"
 
@@ -57,6 +58,7 @@ struct gbp_ctx {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     long long launches = 0;
+    CsrWork csr;  // device arrays of gbp_csr_cg
 };
 
 struct gbp_scene {
@@ -136,6 +138,7 @@ int gbp_create(int device, gbp_ctx **out) {
 void gbp_destroy(gbp_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
+    csr_release(c->csr);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -143,6 +146,58 @@ void gbp_destroy(gbp_ctx *c) {
 }
 
 long long gbp_launch_count(gbp_ctx *c) { return c ? c->launches : 0; }
+
+int gbp_csr_cg(gbp_ctx *c, long long n, const long long *rowstart, const long long *cols, const double *vals,
+               const double *b, double *x, double residual, int max_iterations, gbp_csr_stats *stats) {
+    const auto t0 = std::chrono::steady_clock::now();
+    if (!c || n < 0 || (n > 0 && (!rowstart || !b || !x)))
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_csr_cg: bad argument");
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (n == 0) {
+        if (stats) stats->converged = 1;
+        return GBP_OK;
+    }
+    // the structure is checked on the host: no index reaches the device
+    // unless it lies inside the arrays
+    if (rowstart[0] != 0) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_csr_cg: rowstart[0] != 0");
+    for (long long r = 0; r < n; ++r)
+        if (rowstart[r + 1] < rowstart[r]) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_csr_cg: rowstart decreases");
+    const long long nnz = rowstart[n];
+    if (nnz > 0 && (!cols || !vals)) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_csr_cg: NULL cols or vals");
+    for (long long e = 0; e < nnz; ++e)
+        if (cols[e] < 0 || cols[e] >= n) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_csr_cg: column out of range");
+    if (n > (1LL << 40) || nnz > (1LL << 40)) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_csr_cg: too large");
+    GBP_CUDA(cudaSetDevice(c->device));
+    GBP_CUDA(csr_reserve(c->csr, n, nnz > 0 ? nnz : 1));
+    CsrWork &w = c->csr;
+    cudaStream_t st = c->stream;
+    GBP_CUDA(cudaMemcpyAsync(w.rowstart, rowstart, sizeof(long long) * (size_t)(n + 1), cudaMemcpyHostToDevice, st));
+    if (nnz > 0) {
+        GBP_CUDA(cudaMemcpyAsync(w.cols, cols, sizeof(long long) * (size_t)nnz, cudaMemcpyHostToDevice, st));
+        GBP_CUDA(cudaMemcpyAsync(w.vals, vals, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, st));
+    }
+    GBP_CUDA(cudaMemcpyAsync(w.b, b, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaEventRecord(c->ev[0], st));
+    long long launches = 0;
+    GBP_CUDA(csr_cg_run(w, n, residual, max_iterations, c->grid_blocks, st, &launches));
+    GBP_CUDA(cudaEventRecord(c->ev[1], st));
+    GBP_CUDA(cudaMemcpyAsync(x, w.x, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    c->launches += launches;
+    const Scalars &h = *w.host_sc;
+    if (stats) {
+        stats->iterations = h.iter;
+        stats->converged = h.status == 1;
+        stats->reresid = h.res0 > 0.0 ? h.res / h.res0 : 0.0;  // pcg_solver.h:284, :294
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+        stats->ms_solve = ms;
+        stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    if (h.status == 3) return fail(GBP_ERR_NAN, "gbp_csr_cg: breakdown (NaN or zero curvature)");
+    if (h.status != 1) return fail(GBP_ERR_NOT_CONVERGED, "gbp_csr_cg: not converged");
+    return GBP_OK;
+}
 
 size_t gbp_scene_device_bytes(int dim, int nx, int ny, int nz, const gbp_params *params) {
     gbp_params p;

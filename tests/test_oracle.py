@@ -88,3 +88,22 @@ def test_plugin_module_loads_through_reference_loader(tmp_path):
         text = open(log).read()
         assert f"gbprojection{dim}" in text
         lib.ref_destroy(h)
+
+
+def test_linsolver_module_loads_through_reference_loader(tmp_path):
+    """The LinSolver drop-in: macpressuresolver3 / 2 create their linear
+    solver through the reference's loader by the LinSolver key
+    (include/shiokaze/linsolver/RCMatrix_solver.h:40); LinSolver=gbpcg loads
+    the GPU solver module in place of pcg. (solve() needs a GPU.)"""
+    import subprocess
+    root = oracle.HERE.rsplit("/", 1)[0]
+    subprocess.check_call(["make", "-s", "-C", f"{root}/shiokaze_gb300/module", f"OUT={oracle.REF_DIR}"],
+                          stdout=subprocess.DEVNULL)
+    lib = oracle._ref_lib()
+    for dim in (3, 2):
+        log = str(tmp_path / f"lin{dim}.log")
+        h = lib.ref_create(dim, 16, 16, 16, 1 / 16, b"LinSolver=gbpcg Residual=1e-6", log.encode())
+        assert h
+        text = open(log).read()
+        assert "gbpcg" in text and "pcg.so" not in text.replace("gbpcg.so", "")
+        lib.ref_destroy(h)
