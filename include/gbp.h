@@ -125,7 +125,7 @@ typedef struct gbp_csr_stats {
 void gbp_params_default(gbp_params *p);
 
 /* Solves A x = b on the GPU for a symmetric positive (semi)definite matrix
- * of n rows in compressed rows (host arrays: rowstart[0..n], rowstart[0] = 0;
+ * of n < 2^31 rows in compressed rows (host arrays: rowstart[0..n], rowstart[0] = 0;
  * column indices cols[rowstart[r]..rowstart[r+1]) in [0, n) and values vals
  * alike; duplicate entries of a row add up), with the reference's LinSolver
  * "pcg" (src/linsolver/pcg.cpp:44-74; local/include/pcgsolver/pcg_solver.h:

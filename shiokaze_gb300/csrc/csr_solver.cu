@@ -6,9 +6,9 @@
 // a CUDA graph may hold more iterations than are needed.
 //
 // Algorithmic DRAM bytes per iteration: spmv reads the row pointers (8 per
-// row), columns and values (16 per entry) and s (8 per entry, most from
-// cache; counted once per row), writes z (8 per row); update 48 and
-// direction 24 per row.
+// row), columns and values (12 per entry: 32-bit columns) and s (8 per
+// entry, mostly from cache; counted once per row), writes z (8 per row);
+// update 48 and direction 24 per row.
 #include "csr_solver.h"
 
 namespace gbp {
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) csr_init_kernel(long long n, co
 // z = A s, s.z, alpha = rho / s.z (pcg_solver.h:276-277); each row's entries
 // are summed in their stored order.
 __global__ void __launch_bounds__(BLOCK_THREADS) csr_spmv_kernel(long long n, const long long *__restrict__ rowstart,
-                                                                 const long long *__restrict__ cols,
+                                                                 const int *__restrict__ cols,
                                                                  const double *__restrict__ vals,
                                                                  const double *__restrict__ s, double *z, Scalars *sc,
                                                                  Partials *pt) {
@@ -198,7 +198,7 @@ cudaError_t csr_reserve(CsrWork &w, long long n, long long nnz) {
         w.cols = nullptr;
         w.vals = nullptr;
         w.nnz_cap = 0;
-        if ((e = cudaMalloc(&w.cols, sizeof(long long) * (size_t)nnz)) != cudaSuccess) return e;
+        if ((e = cudaMalloc(&w.cols, sizeof(int) * (size_t)nnz)) != cudaSuccess) return e;
         if ((e = cudaMalloc(&w.vals, sizeof(double) * (size_t)nnz)) != cudaSuccess) return e;
         w.nnz_cap = nnz;
         if (w.graph) cudaGraphExecDestroy(w.graph);

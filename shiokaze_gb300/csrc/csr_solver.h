@@ -16,7 +16,8 @@ namespace gbp {
 // Device arrays of one solve, grown on demand and kept between calls.
 struct CsrWork {
     long long n_cap = 0, nnz_cap = 0;
-    long long *rowstart = nullptr, *cols = nullptr;
+    long long *rowstart = nullptr;
+    int *cols = nullptr;  // column indices (32-bit: the host checks n < 2^31)
     double *vals = nullptr, *b = nullptr, *x = nullptr, *r = nullptr, *s = nullptr, *z = nullptr;
     Scalars *sc = nullptr, *host_sc = nullptr;
     Partials *pt = nullptr;

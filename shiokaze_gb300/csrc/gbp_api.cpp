@@ -164,16 +164,20 @@ int gbp_csr_cg(gbp_ctx *c, long long n, const long long *rowstart, const long lo
         if (rowstart[r + 1] < rowstart[r]) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_csr_cg: rowstart decreases");
     const long long nnz = rowstart[n];
     if (nnz > 0 && (!cols || !vals)) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_csr_cg: NULL cols or vals");
-    for (long long e = 0; e < nnz; ++e)
+    if (n >= (1LL << 31) || nnz > (1LL << 40)) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_csr_cg: too large");
+    // checked and narrowed to the device's 32-bit column indices in one pass
+    std::vector<int> cols32((size_t)(nnz > 0 ? nnz : 1));
+    for (long long e = 0; e < nnz; ++e) {
         if (cols[e] < 0 || cols[e] >= n) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_csr_cg: column out of range");
-    if (n > (1LL << 40) || nnz > (1LL << 40)) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_csr_cg: too large");
+        cols32[(size_t)e] = (int)cols[e];
+    }
     GBP_CUDA(cudaSetDevice(c->device));
     GBP_CUDA(csr_reserve(c->csr, n, nnz > 0 ? nnz : 1));
     CsrWork &w = c->csr;
     cudaStream_t st = c->stream;
     GBP_CUDA(cudaMemcpyAsync(w.rowstart, rowstart, sizeof(long long) * (size_t)(n + 1), cudaMemcpyHostToDevice, st));
     if (nnz > 0) {
-        GBP_CUDA(cudaMemcpyAsync(w.cols, cols, sizeof(long long) * (size_t)nnz, cudaMemcpyHostToDevice, st));
+        GBP_CUDA(cudaMemcpyAsync(w.cols, cols32.data(), sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, st));
         GBP_CUDA(cudaMemcpyAsync(w.vals, vals, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, st));
     }
     GBP_CUDA(cudaMemcpyAsync(w.b, b, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, st));
