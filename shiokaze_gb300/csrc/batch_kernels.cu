@@ -410,18 +410,27 @@ template <class T> struct MaxAcc {
         if (threadIdx.x == 0) part[idx] = b;
     }
 };
-// max |x| and sum x^2 in FP64 (the refinement residual); partials at idx
-// and n + idx.
-struct MaxSumAcc {
-    double m, s;
-    __device__ void reset() { m = s = 0.0; }
-    __device__ void add(double x) {
-        m = fmax(m, fabs(x));
-        s = fma(x, x, s);
+// The refinement residual's norms (partials at idx and n + idx): max |x|
+// of the FP64 residual, exact, taken on the bit patterns (integer compares:
+// no FP64 instruction; a NaN outranks every number, so it reaches the
+// stopping rule), and the sum of squares of its T copy with the dot
+// product's accumulation (float-float for T = float), which only reports
+// the L2 norm.
+template <class T> struct MaxSumAcc {
+    unsigned long long m;
+    DotAcc<T> s;
+    __device__ void reset() {
+        m = 0ull;
+        s.reset();
+    }
+    __device__ void add(double x, T xt) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+        m = b > m ? b : m;
+        s.add(xt, xt);
     }
     __device__ void store(double *sh, double *part, int idx, int n) {
-        const double bm = block_max(m, sh);
-        const double bs = block_sum(s, sh);
+        const double bm = block_max(__longlong_as_double((long long)m), sh);
+        const double bs = s.block(sh);
         if (threadIdx.x == 0) {
             part[idx] = bm;
             part[n + idx] = bs;
@@ -1551,16 +1560,28 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_res
     if (!initial && *(const volatile int *)&cnt->refine <= 0) return;
     __shared__ double shf[BLOCK_THREADS / 32];
     __shared__ ItemCtx<T> ctx;
-    reduce_items<T, MaxSumAcc, false>(
+    reduce_items<T, MaxSumAcc<T>>(
         segs, nseg, n, part, levels, scenes, initial ? -1 : 2, ctx,
-        [&](const BItem &it, MaxSumAcc &acc, T) {
+        [&](const BItem &it, MaxSumAcc<T> &acc, T cls) {
             const BLevel<T> &L = ctx.L;
             const BScene<T> &S = ctx.S;
             const Grid &g = L.g;
             const long long sy = g.nx, sz = (long long)g.nx * g.ny;
             const Operator<double> &A = S.A;
+            // no unknown: b = 0 and every row of A is 0 there, so r = 0,
+            // written by the initial pass (with x64 = 0) and unchanged after
+            const bool empty = tile_empty(cls);
+            if (empty && !initial) return;
             with_vec(L.vec, [&](auto vt) {
                 constexpr bool V = decltype(vt)::value;
+                if (empty) {
+                    pair_tile(g, it, [&](int, int, int, long long c, bool second) {
+                        st2<double, V>(S.r64, c, Pair<double>{0.0, 0.0}, second);
+                        st2<T, V>(S.r, c, Pair<T>{T(0), T(0)}, second);
+                        st2<double, V>(S.x64, c, Pair<double>{0.0, 0.0}, second);
+                    });
+                    return;
+                }
                 auto X2 = [&](long long m, bool sec) {
                     Pair<double> v{0.0, 0.0};
                     if (!initial) v = ld2<double, V>(S.x64, m, sec);
@@ -1580,10 +1601,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_res
                 pair_tile(g, it, [&](int i, int j, int k, long long c, bool second) {
                     if (zero_x) {
                         const Pair<double> rv = ld2<double, V>(S.b, c, second);
+                        const Pair<T> rt{T(rv.a), T(rv.b)};
                         st2<double, V>(S.r64, c, rv, second);
-                        st2<T, V>(S.r, c, Pair<T>{T(rv.a), T(rv.b)}, second);
-                        acc.add(rv.a);
-                        if (second) acc.add(rv.b);
+                        st2<T, V>(S.r, c, rt, second);
+                        acc.add(rv.a, rt.a);
+                        if (second) acc.add(rv.b, rt.b);
                         st2<double, V>(S.x64, c, Pair<double>{0.0, 0.0}, second);
                         return;
                     }
@@ -1620,10 +1642,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_res
                     }
                     const Pair<double> bb = ld2<double, V>(S.b, c, second);
                     const Pair<double> rv{bb.a - a0, bb.b - a1};
+                    const Pair<T> rt{T(rv.a), T(rv.b)};
                     st2<double, V>(S.r64, c, rv, second);
-                    st2<T, V>(S.r, c, Pair<T>{T(rv.a), T(rv.b)}, second);
-                    acc.add(rv.a);
-                    if (second) acc.add(rv.b);
+                    st2<T, V>(S.r, c, rt, second);
+                    acc.add(rv.a, rt.a);
+                    if (second) acc.add(rv.b, rt.b);
                     if (initial) st2<double, V>(S.x64, c, Pair<double>{0.0, 0.0}, second);
                 });
             });
