@@ -2102,14 +2102,9 @@ cudaError_t b_red_dot(const BLaunch &L, const BLevel<T> *levels, const BSeg *seg
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_tail(const BLaunch &L, const BTail<T> *tails, int nscenes, const BScene<T> *scenes, MgSettings ms,
-                   size_t smem) {
-    (void)smem;
+cudaError_t b_tail(const BLaunch &L, const BTail<T> *tails, int nscenes, const BScene<T> *scenes, MgSettings ms) {
     tail_kernel<T><<<nscenes, MG_TAIL_THREADS, 0, L.stream>>>(tails, scenes, L.gate, ms, L.cnt);
     return cudaGetLastError();
-}
-template <class T> cudaError_t b_tail_enable(size_t bytes) {
-    return cudaFuncSetAttribute(tail_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 template <class T>
 cudaError_t b_coarse_descend(const BLaunch &L, const BLevel<T> *levels, const CoarseLists &cl,
@@ -2240,8 +2235,7 @@ cudaError_t b_refine_residual(const BLaunch &L, const BLevel<T> *levels, const B
                                          const BScene<T> *, T);                                                      \
     template cudaError_t b_red_dot<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,                   \
                                       const BScene<T> *, double *);                                                  \
-    template cudaError_t b_tail<T>(const BLaunch &, const BTail<T> *, int, const BScene<T> *, MgSettings, size_t);    \
-    template cudaError_t b_tail_enable<T>(size_t);                                                                   \
+    template cudaError_t b_tail<T>(const BLaunch &, const BTail<T> *, int, const BScene<T> *, MgSettings);            \
     template cudaError_t b_coarse_descend<T>(const BLaunch &, const BLevel<T> *, const CoarseLists &,                 \
                                              const BScene<T> *, MgSettings);                                         \
     template cudaError_t b_coarse_ascend<T>(const BLaunch &, const BLevel<T> *, const CoarseLists &,                  \

@@ -134,7 +134,7 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
     int rc;
     nscenes_ = plan.nscenes;
     max_global_ = plan.max_global;
-    tail_smem_ = plan.tail_smem;
+    tail_bytes_ = plan.tail_bytes;
     {
         int dev = 0, sms = 0;
         RUN_CUDA(cudaGetDevice(&dev));
@@ -483,8 +483,8 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
         e = b_coarse_descend<T>(BLaunch{coarse_blocks_, st, gate, d_scene_of_, d_counters_}, lv, coarse_, sc, ms);
         ++*nodes;
     }
-    if (e == cudaSuccess && tail_smem_ > 0) {
-        e = b_tail<T>(BLaunch{nscenes_, st, gate, d_scene_of_, d_counters_}, tl, nscenes_, sc, ms, tail_smem_);
+    if (e == cudaSuccess && tail_bytes_ > 0) {
+        e = b_tail<T>(BLaunch{nscenes_, st, gate, d_scene_of_, d_counters_}, tl, nscenes_, sc, ms);
         ++*nodes;
     }
     // ascend: the coarse global levels in one launch, then the fine level

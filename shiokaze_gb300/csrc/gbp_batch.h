@@ -161,7 +161,7 @@ template <class T> struct BatchPlan {
     std::vector<int> scene_of;           // scene of each level entry
     std::vector<BScene<T>> scenes;
     std::vector<BTail<T>> tails;
-    size_t tail_smem = 0;
+    size_t tail_bytes = 0;
     // work lists as segments: pair[l] (pair tiles of level l), restrict[l]
     // (cell tiles of level l+1), fine (pair tiles of level 0), with their
     // item counts
@@ -225,7 +225,7 @@ private:
     int grid_blocks_ = 0;
     int nscenes_ = 0;
     int max_global_ = 0;
-    size_t tail_smem_ = 0;
+    size_t tail_bytes_ = 0;
     size_t bytes_ = 0;
     std::vector<void *> owned_;
     // device copies
@@ -283,9 +283,7 @@ template <class T>
 cudaError_t b_red_dot(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
                       double *part);
 template <class T>
-cudaError_t b_tail(const BLaunch &L, const BTail<T> *tails, int nscenes, const BScene<T> *scenes, MgSettings ms,
-                   size_t smem);
-template <class T> cudaError_t b_tail_enable(size_t bytes);
+cudaError_t b_tail(const BLaunch &L, const BTail<T> *tails, int nscenes, const BScene<T> *scenes, MgSettings ms);
 // The coarse levels' descent (presmooth, sweeps, restrict per level) and
 // ascent (post_black, sweeps, red sweep per level) as cooperative launches
 // with grid barriers between passes; L.blocks must not exceed

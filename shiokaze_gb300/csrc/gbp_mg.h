@@ -33,15 +33,18 @@ template <class T> struct MgLevel {
 constexpr double TILE_MIXED = -1.0;
 constexpr double TILE_EMPTY = -2.0;
 
-// Levels from `tail` down run in one single-block kernel from shared memory
-// (tail == nlevels: no such levels); tail_smem is the bytes it needs.
+// Levels from `tail` down run in one single-block kernel per scene, in
+// place in global memory (tail == nlevels: no such levels): the coarsest
+// levels whose 7 arrays take at most MG_TAIL_BYTES_MAX, small enough that
+// one block's passes beat grid-wide barriers. tail_bytes is their
+// footprint (nonzero exactly when there is a tail).
 constexpr int MG_TAIL_THREADS = 1024;
-constexpr size_t MG_TAIL_SMEM_MAX = 200 * 1024;
+constexpr size_t MG_TAIL_BYTES_MAX = 200 * 1024;
 
 template <class T> struct MgHierarchy {
     int nlevels = 0;
     int tail = 0;
-    size_t tail_smem = 0;
+    size_t tail_bytes = 0;
     bool fine_aliases_fp64 = false;  // level 0 operator is the FP64 assembly itself
     MgLevel<T> levels[MG_MAX_LEVELS];
 };
@@ -56,12 +59,12 @@ template <class T> void mg_plan_tail(MgHierarchy<T> &H) {
         // right-hand side, inverse diagonal and couplings
         const size_t need = bytes + 7 * sizeof(T) * (size_t)H.levels[l].g.ncell +
                             (l == H.nlevels - 1 ? 16 + 6 * 8 * (size_t)H.levels[l].g.ncell : 0);
-        if (need > MG_TAIL_SMEM_MAX) break;
+        if (need > MG_TAIL_BYTES_MAX) break;
         bytes = need;
         tail = l;
     }
     H.tail = tail;
-    H.tail_smem = bytes;
+    H.tail_bytes = bytes;
 }
 
 struct MgSettings {

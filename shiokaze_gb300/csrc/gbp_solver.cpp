@@ -380,7 +380,7 @@ template <class T> void Solver::add_to_plan(BatchPlan<T> &plan, const gbp_params
     tail.nt = H.nlevels - G;
     for (int l = G; l < H.nlevels; ++l) tail.lv[l - G] = H.levels[l];
     plan.tails.push_back(tail);
-    plan.tail_smem = std::max(plan.tail_smem, H.tail_smem);
+    plan.tail_bytes = std::max(plan.tail_bytes, H.tail_bytes);
 }
 
 template void Solver::add_to_plan<double>(BatchPlan<double> &, const gbp_params &) const;
