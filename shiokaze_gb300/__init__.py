@@ -140,14 +140,27 @@ def check(rc: int, allow=(GBP_OK,)):
     return rc
 
 
+def _flag(val) -> int:
+    """A boolean key's value: bool, int, or the strings yes/no, true/false, 1/0."""
+    if isinstance(val, str):
+        low = val.strip().lower()
+        if low in ("yes", "true", "1"):
+            return 1
+        if low in ("no", "false", "0"):
+            return 0
+        raise ValueError(f"not a boolean value: {val!r}")
+    return 1 if val else 0
+
+
 _KEYMAP = {
-    "Residual": ("residual", float), "MaxIterations": ("max_iterations", int), "WarmStart": ("warm_start", int),
+    "Residual": ("residual", float), "MaxIterations": ("max_iterations", int), "WarmStart": ("warm_start", _flag),
     "EpsFluid": ("eps_fluid", float), "EpsSolid": ("eps_solid", float),
-    "SecondOrderAccurateFluid": ("second_order_fluid", int), "SecondOrderAccurateSolid": ("second_order_solid", int),
+    "SecondOrderAccurateFluid": ("second_order_fluid", _flag),
+    "SecondOrderAccurateSolid": ("second_order_solid", _flag),
     "Gain": ("gain", float), "MGSmooth": ("mg_smooth", int), "MGCoarsest": ("mg_coarsest", int),
     "InnerTolerance": ("inner_tolerance", float), "IterationsPerSync": ("iterations_per_sync", int),
-    "SurfaceTension": ("surface_tension", float), "TMAStaging": ("tma_staging", int),
-    "TileClasses": ("tile_classes", int),
+    "SurfaceTension": ("surface_tension", float), "TMAStaging": ("tma_staging", _flag),
+    "TileClasses": ("tile_classes", _flag),
 }
 
 
@@ -162,8 +175,6 @@ def make_params(**keys) -> Params:
             p.precision = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED}[str(val).lower()]
         elif k in _KEYMAP:
             name, conv = _KEYMAP[k]
-            if conv is int and isinstance(val, str):
-                val = val.lower() in ("yes", "true", "1")
             setattr(p, name, conv(val))
         else:
             raise KeyError(f"unknown configuration key {k}")

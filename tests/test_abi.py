@@ -57,6 +57,14 @@ def test_config_keys(lib):
     assert p.solver == gb.SOLVER_MGPCG and p.precision == gb.PRECISION_MIXED
     with pytest.raises(KeyError):
         gb.make_params(NoSuchKey=1)
+    # values read from a configuration file arrive as strings: integer keys
+    # parse as numbers, boolean keys as yes/no
+    p = gb.make_params(MGSmooth="2", MGCoarsest="8", MaxIterations="500", TileClasses="No",
+                       SecondOrderAccurateFluid="false", TMAStaging=True)
+    assert p.mg_smooth == 2 and p.mg_coarsest == 8 and p.max_iterations == 500
+    assert p.tile_classes == 0 and p.second_order_fluid == 0 and p.tma_staging == 1
+    with pytest.raises(ValueError):
+        gb.make_params(WarmStart="maybe")
 
 
 def test_strerror_and_bytes(lib):

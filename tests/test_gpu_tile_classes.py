@@ -28,7 +28,8 @@ def _solve(sc, **cfg):
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 @pytest.mark.parametrize("kind,shape", [("liquid3", 96), ("smoke3", (80, 64, 72)), ("liquid3", 160),
-                                        ("smoke3", (136, 128, 128)), ("liquid2", 200)])
+                                        ("smoke3", (136, 128, 128)), ("liquid3", (129, 130, 127)),
+                                        ("liquid2", 200)])
 def test_tile_classes_change_nothing(kind, shape, precision):
     import shiokaze_gb300 as gb
     from shiokaze_gb300 import scenes
