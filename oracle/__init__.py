@@ -181,8 +181,30 @@ def _ref_lib():
                                     ctypes.POINTER(ctypes.c_ubyte), ctypes.c_char_p]
         lib.ref_levelset_roundtrip.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp,
                                                ctypes.c_int, ctypes.c_float, fp]
+        dp = ctypes.POINTER(ctypes.c_double)
+        lib.ref_densify_compare.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, ctypes.c_int,
+                                            ctypes.c_float, ctypes.c_int, fp, fp, dp, dp]
         _ref = lib
     return _ref
+
+
+def ref_densify_compare(values: np.ndarray, mode: int, band: float, reps: int = 1):
+    """The plugin modules' dense copy of a reference array (gbarray_adapter.h)
+    and a read of every cell through the reference's operator(), for an array
+    built from `values` (z, y, x or y, x; x fastest) as a narrow-band level set
+    (mode 0), a constant (mode 1) or a partly active velocity component with
+    background `band` (mode 2). Returns (adapter, lookup, ms_adapter,
+    ms_lookup), the times the best of `reps`."""
+    lib = _ref_lib()
+    v = np.ascontiguousarray(values, dtype=np.float32)
+    dim = v.ndim
+    sx, sy, sz = (v.shape[2], v.shape[1], v.shape[0]) if dim == 3 else (v.shape[1], v.shape[0], 1)
+    fp = ctypes.POINTER(ctypes.c_float)
+    a, b = np.empty_like(v), np.empty_like(v)
+    ma, ml = ctypes.c_double(), ctypes.c_double()
+    lib.ref_densify_compare(dim, sx, sy, sz, v.ctypes.data_as(fp), mode, band, reps, a.ctypes.data_as(fp),
+                            b.ctypes.data_as(fp), ctypes.byref(ma), ctypes.byref(ml))
+    return a, b, ma.value, ml.value
 
 
 _ITER_RE = re.compile(r"Took (\d+) iterations, Reresid=([0-9][0-9.eE+\-]*[0-9]|nan|inf)")

@@ -28,6 +28,10 @@
 #include <shiokaze/core/configuration.h>
 #include <shiokaze/core/configurable.h>
 #include <shiokaze/projection/macproject2_interface.h>
+
+#include <chrono>
+
+#include "gbarray_adapter.h"
 #include <shiokaze/projection/macproject3_interface.h>
 
 #include <chrono>
@@ -273,6 +277,66 @@ void ref_levelset_roundtrip(int dim, int sx, int sy, int sz, const float *in, in
         fill_levelset2(a, s, in, mode, band);
         for (int j = 0; j < sy; ++j)
             for (int i = 0; i < sx; ++i) out[i + (size_t)sx * j] = a(i, j);
+    }
+}
+
+/* The plugin modules' dense copy (shiokaze_gb300/module/gbarray_adapter.h)
+ * against a read of every cell through operator(), on an array built from
+ * `in` by fill_levelset{2,3} (mode 0 narrow band + flood fill, mode 1
+ * constant) or, mode 2, as a velocity component: background `band`, cells
+ * with |v| < band active, no fill. Writes both copies and their times
+ * (best of `reps`). */
+void ref_densify_compare(int dim, int sx, int sy, int sz, const float *in, int mode, float band, int reps,
+                         float *out_adapter, float *out_lookup, double *ms_adapter, double *ms_lookup) {
+    if (!g_config_ready) install_global_config("");
+    using clock = std::chrono::steady_clock;
+    auto best = [&](auto &&fn) {
+        double b = 1e300;
+        for (int r = 0; r < (reps > 0 ? reps : 1); ++r) {
+            const auto t0 = clock::now();
+            fn();
+            b = std::min(b, std::chrono::duration<double, std::milli>(clock::now() - t0).count());
+        }
+        return b;
+    };
+    if (dim == 3) {
+        array3<Real> a;
+        shape3 s(sx, sy, sz);
+        if (mode == 2) {
+            a.initialize(s, band);
+            for (int k = 0; k < sz; ++k)
+                for (int j = 0; j < sy; ++j)
+                    for (int i = 0; i < sx; ++i) {
+                        const float x = in[i + (size_t)sx * (j + (size_t)sy * k)];
+                        if (std::abs(x) < band) a.set(i, j, k, x);
+                    }
+        } else {
+            fill_levelset3(a, s, in, mode, band);
+        }
+        *ms_adapter = best([&] { gbarray::densify_passes(a, out_adapter); });
+        *ms_lookup = best([&] {
+            for (int k = 0; k < sz; ++k)
+                for (int j = 0; j < sy; ++j)
+                    for (int i = 0; i < sx; ++i) out_lookup[i + (size_t)sx * (j + (size_t)sy * k)] = a(i, j, k);
+        });
+    } else {
+        array2<Real> a;
+        shape2 s(sx, sy);
+        if (mode == 2) {
+            a.initialize(s, band);
+            for (int j = 0; j < sy; ++j)
+                for (int i = 0; i < sx; ++i) {
+                    const float x = in[i + (size_t)sx * j];
+                    if (std::abs(x) < band) a.set(i, j, x);
+                }
+        } else {
+            fill_levelset2(a, s, in, mode, band);
+        }
+        *ms_adapter = best([&] { gbarray::densify_passes(a, out_adapter); });
+        *ms_lookup = best([&] {
+            for (int j = 0; j < sy; ++j)
+                for (int i = 0; i < sx; ++i) out_lookup[i + (size_t)sx * j] = a(i, j);
+        });
     }
 }
 

@@ -2,8 +2,9 @@
 // pressure projection behind macproject2_interface
 // (include/shiokaze/projection/macproject2_interface.h), a drop-in for
 // "macpressuresolver2" (src/projection/macpressuresolver2.cpp). Selected with
-// Projection=gbprojection2. Dense read through operator(), gbp_project, and
-// write-back to the active faces, as in gbprojection3.cpp.
+// Projection=gbprojection2. Dense copy with operator()'s values
+// (gbarray_adapter.h), gbp_project, and write-back to the active faces, as
+// in gbprojection3.cpp.
 #include <shiokaze/array/array2.h>
 #include <shiokaze/array/macarray2.h>
 #include <shiokaze/core/console.h>
@@ -11,6 +12,7 @@
 
 #include <vector>
 
+#include "gbarray_adapter.h"
 #include "gbprojection_common.h"
 
 SHKZ_USING_NAMESPACE
@@ -31,16 +33,16 @@ protected:
         const int nx = m_shape.w, ny = m_shape.h;
         m_params.surface_tension = surface_tension;
         std::vector<float> s((size_t)(nx + 1) * (ny + 1)), f((size_t)nx * ny), p(f.size());
-        for (int j = 0; j <= ny; ++j)
-            for (int i = 0; i <= nx; ++i) s[i + (size_t)(nx + 1) * j] = solid(i, j);
-        for (int j = 0; j < ny; ++j)
-            for (int i = 0; i < nx; ++i) f[i + (size_t)nx * j] = fluid(i, j);
+        expect_shape(solid.shape(), nx + 1, ny + 1, "solid");
+        expect_shape(fluid.shape(), nx, ny, "fluid");
+        gbarray::densify(solid, s.data());
+        gbarray::densify(fluid, f.data());
         std::vector<float> vel[2];
         for (int d = 0; d < 2; ++d) {
             const int fx = nx + (d == 0), fy = ny + (d == 1);
+            expect_shape(velocity[d].shape(), fx, fy, "velocity");
             vel[d].resize((size_t)fx * fy);
-            for (int j = 0; j < fy; ++j)
-                for (int i = 0; i < fx; ++i) vel[d][i + (size_t)fx * j] = velocity[d](i, j);
+            gbarray::densify(velocity[d], vel[d].data());
         }
         if (!m_scene) {
             gbprojection::check(gbp_create(m_device, &m_ctx), "gbp_create");
@@ -61,6 +63,13 @@ protected:
             const int fx = nx + (dim == 0);
             it.set(vel[dim][i + (size_t)fx * j]);
         });
+    }
+
+    static void expect_shape(const shape2 &s, int w, int h, const char *what) {
+        if ((int)s.w != w || (int)s.h != h) {
+            std::fprintf(stderr, "gbprojection2: %s array is %ux%u, expected %dx%d\n", what, s.w, s.h, w, h);
+            std::exit(-1);
+        }
     }
 
     virtual void configure(configuration &config) override {

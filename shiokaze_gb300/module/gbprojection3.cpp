@@ -5,9 +5,10 @@
 // with Projection=gbprojection3; compiled against the reference's headers
 // and linked to libgbp.so.
 //
-// The reference's arrays are sparse (tiled, narrow band); project() reads
-// them densely through operator() (which applies background/fill values),
-// calls gbp_project, and writes the projected velocity back to the faces
+// The reference's arrays are sparse (tiled, narrow band); project() copies
+// them to dense arrays with exactly operator()'s values (background, fill
+// and active values; gbarray_adapter.h, one pass over the filled and active
+// cells instead of one lookup per cell), calls gbp_project, and writes the projected velocity back to the faces
 // that were active, as the reference's velocity update iterates actives
 // (macpressuresolver3.cpp:252). Faces the reference would deactivate
 // (closed faces) are written as 0, which is the value they read back as.
@@ -19,6 +20,7 @@
 
 #include <vector>
 
+#include "gbarray_adapter.h"
 #include "gbprojection_common.h"
 
 SHKZ_USING_NAMESPACE
@@ -39,19 +41,16 @@ protected:
         const int nx = m_shape.w, ny = m_shape.h, nz = m_shape.d;
         m_params.surface_tension = surface_tension;
         std::vector<float> s((size_t)(nx + 1) * (ny + 1) * (nz + 1)), f((size_t)nx * ny * nz), p(f.size());
-        for (int k = 0; k <= nz; ++k)
-            for (int j = 0; j <= ny; ++j)
-                for (int i = 0; i <= nx; ++i) s[i + (size_t)(nx + 1) * (j + (size_t)(ny + 1) * k)] = solid(i, j, k);
-        for (int k = 0; k < nz; ++k)
-            for (int j = 0; j < ny; ++j)
-                for (int i = 0; i < nx; ++i) f[i + (size_t)nx * (j + (size_t)ny * k)] = fluid(i, j, k);
+        expect_shape(solid.shape(), nx + 1, ny + 1, nz + 1, "solid");
+        expect_shape(fluid.shape(), nx, ny, nz, "fluid");
+        gbarray::densify(solid, s.data());
+        gbarray::densify(fluid, f.data());
         std::vector<float> vel[3];
         for (int d = 0; d < 3; ++d) {
             const int fx = nx + (d == 0), fy = ny + (d == 1), fz = nz + (d == 2);
+            expect_shape(velocity[d].shape(), fx, fy, fz, "velocity");
             vel[d].resize((size_t)fx * fy * fz);
-            for (int k = 0; k < fz; ++k)
-                for (int j = 0; j < fy; ++j)
-                    for (int i = 0; i < fx; ++i) vel[d][i + (size_t)fx * (j + (size_t)fy * k)] = velocity[d](i, j, k);
+            gbarray::densify(velocity[d], vel[d].data());
         }
         if (!m_scene) {
             gbprojection::check(gbp_create(m_device, &m_ctx), "gbp_create");
@@ -75,6 +74,15 @@ protected:
             const int fx = nx + (dim == 0), fy = ny + (dim == 1);
             it.set(vel[dim][i + (size_t)fx * (j + (size_t)fy * k)]);
         });
+    }
+
+    // the reference indexes these arrays by the simulation's shape and
+    // exits on a mismatch in its debug builds (array3.h bound checks)
+    static void expect_shape(const shape3 &s, int w, int h, int d, const char *what) {
+        if ((int)s.w != w || (int)s.h != h || (int)s.d != d) {
+            std::fprintf(stderr, "gbprojection3: %s array is %ux%ux%u, expected %dx%dx%d\n", what, s.w, s.h, s.d, w, h, d);
+            std::exit(-1);
+        }
     }
 
     virtual void configure(configuration &config) override {

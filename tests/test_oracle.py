@@ -107,3 +107,25 @@ def test_linsolver_module_loads_through_reference_loader(tmp_path):
         text = open(log).read()
         assert "gbpcg" in text and "pcg.so" not in text.replace("gbpcg.so", "")
         lib.ref_destroy(h)
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference oracle not built here")
+@pytest.mark.parametrize("kind,n", [("liquid3", 48), ("liquid3", (40, 33, 37)), ("smoke3", 40), ("liquid2", 160),
+                                    ("liquid2", (150, 97))])
+def test_module_densify_matches_operator_reads(kind, n):
+    """The plugin modules' dense copy of the reference's tiled arrays
+    (shiokaze_gb300/module/gbarray_adapter.h: background, then the filled
+    cells, then the active cells) equals reading every cell through the
+    reference's operator() (include/shiokaze/array/array3.h:796-800), bit
+    for bit: narrow-band level sets with flood-filled tiles, a constant
+    array, and a partly active velocity component over a background."""
+    sc = getattr(scenes, kind)(n, seed=5)
+    vel_band = float(np.quantile(np.abs(sc.u), 0.4))
+    for arr, mode, band in ((sc.solid, sc.solid_mode, sc.band), (sc.fluid, sc.fluid_mode, sc.band),
+                            (sc.u, 2, vel_band), (sc.v, 2, vel_band)):
+        a, b, _, _ = oracle.ref_densify_compare(arr, mode, band)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    # the narrow band leaves filled and background cells on both sides
+    if kind.startswith("liquid"):
+        a, _, _, _ = oracle.ref_densify_compare(sc.fluid, 0, sc.band)
+        assert (a == -np.float32(sc.band)).any() and (a == np.float32(sc.band)).any()
