@@ -20,6 +20,7 @@ import os
 import re
 import subprocess
 import tempfile
+import time
 from dataclasses import dataclass
 
 import numpy as np
@@ -32,9 +33,9 @@ DEFAULT_REFERENCE = "/root/reference"
 
 
 def build_port(force: bool = False) -> str:
-    src = os.path.join(HERE, "gbp_oracle.c")
-    if force or not os.path.exists(PORT_SO) or os.path.getmtime(PORT_SO) < os.path.getmtime(src):
-        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", PORT_SO, "-lm"])
+    srcs = [os.path.join(HERE, f) for f in ("gbp_oracle.c", "advect_oracle.c")]
+    if force or not os.path.exists(PORT_SO) or os.path.getmtime(PORT_SO) < max(map(os.path.getmtime, srcs)):
+        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", *srcs, "-o", PORT_SO, "-lm"])
     return PORT_SO
 
 
@@ -106,6 +107,9 @@ def _port_lib():
                                         ctypes.POINTER(_Params), dp, dp, dp, dp, dp, lp]
         lib.oracle_face_fractions.argtypes = [ctypes.c_void_p, fp, fp, ctypes.POINTER(_Params), fp, fp, fp, fp, fp,
                                               fp]
+        lib.oracle_advect3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_int, ctypes.c_int, fp, fp, fp, fp, fp, ctypes.POINTER(ctypes.c_ubyte),
+                                       ctypes.c_float]
         _port = lib
     return _port
 
@@ -182,6 +186,10 @@ def _ref_lib():
         lib.ref_levelset_roundtrip.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp,
                                                ctypes.c_int, ctypes.c_float, fp]
         dp = ctypes.POINTER(ctypes.c_double)
+        lib.ref_advect3.restype = ctypes.c_double
+        lib.ref_advect3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_char_p, fp, fp, fp, fp, ctypes.c_int, ctypes.c_float, fp,
+                                    ctypes.POINTER(ctypes.c_ubyte), ctypes.c_float, ctypes.c_char_p]
         lib.ref_densify_compare.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, ctypes.c_int,
                                             ctypes.c_float, ctypes.c_int, fp, fp, dp, dp]
         _ref = lib
@@ -205,6 +213,60 @@ def ref_densify_compare(values: np.ndarray, mode: int, band: float, reps: int = 
     lib.ref_densify_compare(dim, sx, sy, sz, v.ctypes.data_as(fp), mode, band, reps, a.ctypes.data_as(fp),
                             b.ctypes.data_as(fp), ctypes.byref(ma), ctypes.byref(ml))
     return a, b, ma.value, ml.value
+
+
+def advect3(u, v, w, fluid, dx, dt, q=None, q_mask=None, q_bg=0.0, maccormack=True, trim_narrowband=1,
+            impl="port", fluid_mode=0, band=0.0):
+    """macsmoke3's advection step (the scalar q, if given, by the velocity,
+    then the velocity by itself) on dense 3D arrays (z, y, x), by the C
+    restatement (impl "port") or the reference's own module ("reference";
+    fluid_mode / band say how it builds its fluid array). Returns (u, v, w,
+    q, ms) as new arrays."""
+    if impl == "reference":
+        return ref_advect3(u, v, w, fluid, fluid_mode, band, dx, dt, q=q, q_mask=q_mask, q_bg=q_bg,
+                           maccormack=maccormack, trim_narrowband=trim_narrowband)
+    lib = _port_lib()
+    fp = ctypes.POINTER(ctypes.c_float)
+    nz, ny, nx = fluid.shape
+    uo, vo, wo = (np.array(a, dtype=np.float32, order="C") for a in (u, v, w))
+    fl = np.ascontiguousarray(fluid, dtype=np.float32)
+    qo = None if q is None else np.array(q, dtype=np.float32, order="C")
+    qm = None if q_mask is None else np.ascontiguousarray(q_mask, dtype=np.uint8)
+    t0 = time.perf_counter()
+    rc = lib.oracle_advect3(nx, ny, nz, dx, dt, int(maccormack), int(trim_narrowband), uo.ctypes.data_as(fp),
+                            vo.ctypes.data_as(fp), wo.ctypes.data_as(fp), fl.ctypes.data_as(fp),
+                            None if qo is None else qo.ctypes.data_as(fp),
+                            None if qm is None else qm.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), q_bg)
+    ms = 1000.0 * (time.perf_counter() - t0)
+    if rc:
+        raise ValueError("oracle_advect3: grid too small")
+    return uo, vo, wo, qo, ms
+
+
+def ref_advect3(u, v, w, fluid, fluid_mode, band, dx, dt, q=None, q_mask=None, q_bg=0.0, maccormack=True,
+                trim_narrowband=1):
+    """The reference's own macadvection3 on dense 3D arrays (arrays z, y, x;
+    every velocity face active): the scalar q (if given; active where q_mask,
+    all if None) advected by the velocity, then the velocity by itself, as
+    macsmoke3::idle does. Returns (u, v, w, q, ms) as new arrays."""
+    lib = _ref_lib()
+    fp = ctypes.POINTER(ctypes.c_float)
+    nz, ny, nx = fluid.shape
+    uo, vo, wo = (np.array(a, dtype=np.float32, order="C") for a in (u, v, w))
+    fl = np.ascontiguousarray(fluid, dtype=np.float32)
+    qo = None if q is None else np.array(q, dtype=np.float32, order="C")
+    qm = None if q_mask is None else np.ascontiguousarray(q_mask, dtype=np.uint8)
+    kv = f"MacCormack={'Yes' if maccormack else 'No'} TrimNarrowBand={int(trim_narrowband)}"
+    log = tempfile.NamedTemporaryFile(prefix="ref_advect_", suffix=".log", delete=False).name
+    try:
+        ms = lib.ref_advect3(nx, ny, nz, dx, dt, kv.encode(), uo.ctypes.data_as(fp), vo.ctypes.data_as(fp),
+                             wo.ctypes.data_as(fp), fl.ctypes.data_as(fp), fluid_mode, band,
+                             None if qo is None else qo.ctypes.data_as(fp),
+                             None if qm is None else qm.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), q_bg,
+                             log.encode())
+    finally:
+        os.unlink(log)
+    return uo, vo, wo, qo, ms
 
 
 _ITER_RE = re.compile(r"Took (\d+) iterations, Reresid=([0-9][0-9.eE+\-]*[0-9]|nan|inf)")

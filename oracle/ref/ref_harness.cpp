@@ -28,8 +28,7 @@
 #include <shiokaze/core/configuration.h>
 #include <shiokaze/core/configurable.h>
 #include <shiokaze/projection/macproject2_interface.h>
-
-#include <chrono>
+#include <shiokaze/advection/macadvection3_interface.h>
 
 #include "gbarray_adapter.h"
 #include <shiokaze/projection/macproject3_interface.h>
@@ -338,6 +337,73 @@ void ref_densify_compare(int dim, int sx, int sy, int sz, const float *in, int m
                 for (int i = 0; i < sx; ++i) out_lookup[i + (size_t)sx * j] = a(i, j);
         });
     }
+}
+
+/* The reference's macadvection3 (src/advection/macadvection3.cpp), loaded
+ * by name, on dense 3D arrays, in macsmoke3::idle's order
+ * (src/smoke/macsmoke3.cpp:270-281): the scalar (if q is given) advected by
+ * the velocity, then the velocity by itself. kv: the module's keys
+ * (MacCormack, WENO, TrimNarrowBand). u, v, w: every face active (the smoke
+ * scene's velocity, macsmoke3.cpp:115), in/out. fluid: level set built as
+ * in ref_project. q: cells, in/out, background q_bg; the cells with
+ * q_mask[c] != 0 are active (all if q_mask is NULL). Outputs are read
+ * through operator(). Returns wall-clock milliseconds of the two calls. */
+double ref_advect3(int nx, int ny, int nz, double dx, double dt, const char *kv, float *u, float *v, float *w,
+                   const float *fluid, int fluid_mode, float fluid_band, float *q, const unsigned char *q_mask,
+                   float q_bg, const char *log_path) {
+    configuration &config = install_global_config(kv);
+    shape3 s(nx, ny, nz);
+    double dxv = dx, ms = 0.0;
+    with_stdout_to(log_path, [&]() {
+        macadvection3_driver adv("macadvection3");
+        adv.set_environment("shape", &s);
+        adv.set_environment("dx", &dxv);
+        adv.setup_now(config);
+        array3<Real> fluid_a;
+        fill_levelset3(fluid_a, s, fluid, fluid_mode, fluid_band);
+        // the advected velocity and macsmoke3's copy of it (the second
+        // argument, which advect_vector does not read)
+        macarray3<Real> vel(s), save(s);
+        vel.activate_all();
+        save.activate_all();
+        float *comp[3] = {u, v, w};
+        for (int d = 0; d < 3; ++d) {
+            const shape3 fs = s.face(d);
+            for (int k = 0; k < (int)fs.d; ++k)
+                for (int j = 0; j < (int)fs.h; ++j)
+                    for (int i = 0; i < (int)fs.w; ++i) {
+                        const float x = comp[d][i + (size_t)fs.w * (j + (size_t)fs.h * k)];
+                        vel[d].set(i, j, k, x);
+                        save[d].set(i, j, k, x);
+                    }
+        }
+        array3<Real> qa;
+        if (q) {
+            qa.initialize(s, q_bg);
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j)
+                    for (int i = 0; i < nx; ++i) {
+                        const size_t n = i + (size_t)nx * (j + (size_t)ny * k);
+                        if (!q_mask || q_mask[n]) qa.set(i, j, k, q[n]);
+                    }
+        }
+        auto t0 = std::chrono::steady_clock::now();
+        if (q) adv->advect_scalar(qa, vel, fluid_a, dt, "density");
+        adv->advect_vector(vel, save, fluid_a, dt, "velocity");
+        ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        for (int d = 0; d < 3; ++d) {
+            const shape3 fs = s.face(d);
+            for (int k = 0; k < (int)fs.d; ++k)
+                for (int j = 0; j < (int)fs.h; ++j)
+                    for (int i = 0; i < (int)fs.w; ++i)
+                        comp[d][i + (size_t)fs.w * (j + (size_t)fs.h * k)] = vel[d](i, j, k);
+        }
+        if (q)
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j)
+                    for (int i = 0; i < nx; ++i) q[i + (size_t)nx * (j + (size_t)ny * k)] = qa(i, j, k);
+    });
+    return ms;
 }
 
 }  // extern "C"
