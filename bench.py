@@ -56,7 +56,11 @@ WORKLOADS = {
                    "--steps = number of requests"),
     "batch64_liquid3": dict(kind="batch", n=64, desc="64 independent 3D liquid scenes, edge log-uniform in "
                             "[32, 160], fluid fraction U[0.1, 0.6], one batched solve per step"),
+    "advect_smoke3_256": dict(kind="advect", n=256, desc="MAC advection of the 3D smoke scene 256^3 (macsmoke3's "
+                              "step: density U[0,1) by the velocity, then the velocity by itself; MacCormack, "
+                              "bilinear, TrimNarrowBand 1); --steps = chained advection steps"),
 }
+ADVECT_METRIC = "3D MAC advection steps/s (MacCormack, density + velocity)"
 METRIC = "3D pressure solves/s at 1e-6 resid"
 L2_BYTES = 129 * 2 ** 20
 REFERENCE_BUDGET_S = 150.0
@@ -552,6 +556,185 @@ def run_gbp_served(args):
     ranks.close()
 
 
+def advect_scene(name):
+    """The smoke scene of an advection workload and its density field."""
+    from shiokaze_gb300 import scenes
+    scene = scenes.smoke3(WORKLOADS[name]["n"], seed=3)
+    density = np.random.default_rng(6).random(scene.fluid.shape, dtype=np.float32)
+    return scene, density
+
+
+def advect_bytes(scene):
+    """Algorithmic DRAM bytes of one MacCormack step (density + velocity):
+    per cell 32 B in each scalar pass (the density, the three velocity
+    components' faces counted once, the fluid level set, the forward value
+    and limiter record); per face 17.3 B forward (the component, the level
+    set shared by three faces, the forward value and the 8-byte limiter
+    record) and 20 B backward (forward value, record, input, result)."""
+    cells = scene.cells
+    faces = scene.u.size + scene.v.size + scene.w.size
+    return 64.0 * cells + (4 + 4 / 3 + 12 + 20) * faces
+
+
+def run_gbp_advect(args):
+    import torch
+    import shiokaze_gb300 as gb
+
+    rank, world, local = dist_info()
+    ranks = Ranks("nccl", torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    scene, density = advect_scene(args.workload)
+    ctx = gb.Context(local)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+
+    def dev_t(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+    u, v, w, fluid, q = (dev_t(a) for a in (scene.u, scene.v, scene.w, scene.fluid, density))
+    torch.cuda.synchronize()
+    adv = gb.MacAdvection3(scene.nx, scene.ny, scene.nz, scene.dx, context=ctx)
+
+    def step():
+        adv.advect_step((u, v, w), fluid, scene.dt, scalar=q, stream=sh)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ranks.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    l0 = ctx.launches()
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for k in range(args.steps):
+        step()
+        ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    launches = ctx.launches() - l0
+    per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = ranks.max_ms(ev[0].elapsed_time(ev[-1]))
+    value = ranks.rate(args.steps, total_ms)
+
+    # end to end through the host-array call, pinned host buffers
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float32, pin_memory=True)
+        t.numpy()[...] = a
+        return t
+    hu, hv, hw, hf, hq = (pinned(a) for a in (scene.u, scene.v, scene.w, scene.fluid, density))
+    e2e_times = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        adv.advect_step((hu.numpy(), hv.numpy(), hw.numpy()), hf.numpy(), scene.dt, scalar=hq.numpy())
+        t1 = time.perf_counter()
+        if k >= args.warmup:
+            e2e_times.append(t1 - t0)
+    face_bytes = scene.u.nbytes + scene.v.nbytes + scene.w.nbytes
+    h2d = face_bytes + scene.fluid.nbytes + density.nbytes
+    d2h = face_bytes + density.nbytes
+    ranks.barrier()
+    e2e_value = ranks.rate(len(e2e_times), 1000.0 * sum(e2e_times))
+
+    # the two halves of the step timed alone with CUDA events: the face
+    # passes (velocity forward + backward) dominate, the cell passes carry
+    # the density
+    def timed(fn, reps=10):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+    face_ms = timed(lambda: adv.advect_vector((u, v, w), (u, v, w), fluid, scene.dt, stream=sh))
+    cell_ms = timed(lambda: adv.advect_scalar(q, (u, v, w), fluid, scene.dt, stream=sh))
+    faces = scene.u.size + scene.v.size + scene.w.size
+    face_bytes_alg = (4 + 4 / 3 + 12 + 20) * faces
+    cell_bytes_alg = 64.0 * scene.cells
+
+    ms_step = total_ms / args.steps
+    nbytes = advect_bytes(scene)
+    peak, peak_kind = measured_peak_gbs()
+    achieved = face_bytes_alg / (face_ms * 1e-3) / 1e9
+    out = {
+        "metric": ADVECT_METRIC, "value": round(value, 3), "unit": "steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 storage, f64 traces (the reference's)",
+        "data": "synthetic (seeded smoke scene: velocity N(0,1) faces, density U[0,1))",
+        "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]["desc"],
+                   "grid": [scene.nx, scene.ny, scene.nz], "parallelism": f"replicas x{world}",
+                   "l2": "no flush: inputs and scratch (~1.1 GB) above the 129 MB L2"},
+        "latency_ms": {"p50": round(float(np.percentile(per_step, 50)), 4),
+                       "p99": round(float(np.percentile(per_step, 99)), 4)},
+        "cell_updates_per_s": round(scene.cells / (ms_step * 1e-3), 1),
+        "e2e": {"value": round(e2e_value, 3), "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "kernel": "adv_face_forward + adv_face_backward (velocity passes)",
+                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": committed_traffic(args.workload, "face_passes"), "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": face_bytes_alg, "ms_per_launch": round(face_ms, 5),
+                     "limiter": "FP64 pipe: the reference's double-precision traces and trilinear weights",
+                     "kernels": {"face_passes": {"ms": round(face_ms, 5),
+                                                 "GBps": round(face_bytes_alg / (face_ms * 1e-3) / 1e9, 1)},
+                                 "cell_passes": {"ms": round(cell_ms, 5),
+                                                 "GBps": round(cell_bytes_alg / (cell_ms * 1e-3) / 1e9, 1)}},
+                     "step_GBps": round(nbytes / (ms_step * 1e-3) / 1e9, 1)},
+        "clocks": clocks,
+        "gpu_launches": int(launches),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle
+        t0 = time.perf_counter()
+        oracle.advect3(scene.u, scene.v, scene.w, scene.fluid, scene.dx, scene.dt, q=density)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(1.0 / dt, 5), "unit": "steps/s", "cores": 1, "kind": "port",
+                               "sample": f"one full advection step of the same scene by the oracle's C "
+                                         f"restatement of the reference's macadvection3, single thread, "
+                                         f"{dt:.1f} s"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    ranks.close()
+
+
+def run_reference_advect(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return
+    import oracle
+    scene, density = advect_scene(args.workload)
+    kind = "reference" if oracle.reference_available() else "port"
+    times = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.advect3(scene.u, scene.v, scene.w, scene.fluid, scene.dx, scene.dt, q=density, impl=kind,
+                       fluid_mode=scene.fluid_mode, band=scene.band)
+        times.append(time.perf_counter() - t0)
+        if sum(times) > REFERENCE_BUDGET_S:
+            break
+    value = len(times) / sum(times)
+    what = ("the reference's macadvection3 built from its sources (its own threads)" if kind == "reference"
+            else "the oracle's C restatement of the reference's macadvection3, single thread (the reference's "
+                 "own build is not on this host)")
+    out = {
+        "metric": ADVECT_METRIC, "value": round(value, 5), "unit": "steps/s", "n_gpus": world, "steps": len(times),
+        "warmup": args.warmup, "ms_per_step": round(1000 * sum(times) / len(times), 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 storage, f64 traces", "impl": "reference",
+        "data": "synthetic (seeded smoke scene: velocity N(0,1) faces, density U[0,1))",
+        "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]["desc"],
+                   "grid": [scene.nx, scene.ny, scene.nz]},
+        "cpu_baseline": {"value": round(value, 5), "unit": "steps/s",
+                         "cores": (os.cpu_count() or 1) if kind == "reference" else 1, "kind": kind,
+                         "sample": f"{len(times)} full advection steps of the workload by {what}"},
+        "e2e": {"value": round(value, 5), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
 def run_reference(args):
     rank, world, local = dist_info()
     if rank != 0:
@@ -621,12 +804,16 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gbp":
         args.warmup = 3
-    if args.impl == "reference":
+    if args.impl == "reference" and WORKLOADS[args.workload]["kind"] == "advect":
+        run_reference_advect(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif WORKLOADS[args.workload]["kind"] == "batch":
         run_gbp_batch(args)
     elif WORKLOADS[args.workload]["kind"] == "served":
         run_gbp_served(args)
+    elif WORKLOADS[args.workload]["kind"] == "advect":
+        run_gbp_advect(args)
     else:
         run_gbp(args)
 

@@ -244,6 +244,36 @@ int gbp_project_device_static(int dim, int nx, int ny, int nz, double dx, double
                               const float *fluid, float *u, float *v, float *w, const gbp_params *params,
                               float *pressure, gbp_stats *stats, void *stream);
 
+/* MAC advection, the neighbouring step of the projection in a smoke time
+ * step: replaces the reference's advection module
+ *   macadvection3_interface::advect_scalar / advect_vector
+ *     include/shiokaze/advection/macadvection3_interface.h:52-72
+ *   as implemented by src/advection/macadvection3.cpp:38-54 (advect_cell
+ *   :234-282, advect_u :136-180) with bilinear interpolation (WENO off),
+ * called in macsmoke3::idle's order (src/smoke/macsmoke3.cpp:270-281): the
+ * cell scalar q, if not NULL, is carried by u, v, w; then, if
+ * advect_velocity, u, v, w are carried by themselves. Results equal the
+ * reference's bit for bit. Every face of the velocity is active (a smoke
+ * velocity); q is active where q_mask is nonzero (all cells if q_mask is
+ * NULL) and reads q_bg elsewhere, where it is also written as q_bg.
+ * fluid is the cell level set that decides the narrow band in which the
+ * MacCormack limiter falls back to the forward value. Arrays are dense, x
+ * fastest, shapes as for gbp_project; at least 2 cells per edge. */
+typedef struct gbp_advect_params {
+    int maccormack;      /* "MacCormack" key: 1 (default) MacCormack, 0 one semi-Lagrangian pass */
+    int trim_narrowband; /* "TrimNarrowBand" key (default 1) */
+    int advect_velocity; /* 1 (default): also advect u, v, w by themselves */
+} gbp_advect_params;
+void gbp_advect_params_default(gbp_advect_params *p);
+/* DEVICE arrays, on `stream` (NULL = the context's stream, ordered after the
+ * legacy default stream); returns when the step has finished. */
+int gbp_advect3_device(gbp_ctx *ctx, int nx, int ny, int nz, double dx, double dt, const gbp_advect_params *params,
+                       float *u, float *v, float *w, const float *fluid, float *q, const unsigned char *q_mask,
+                       float q_bg, void *stream);
+/* HOST arrays, copied in and out on the context's stream. */
+int gbp_advect3(gbp_ctx *ctx, int nx, int ny, int nz, double dx, double dt, const gbp_advect_params *params, float *u,
+                float *v, float *w, const float *fluid, float *q, const unsigned char *q_mask, float q_bg);
+
 /* Number of kernel launches this context has issued (graph nodes count one
  * each). */
 long long gbp_launch_count(gbp_ctx *ctx);

@@ -1,0 +1,44 @@
+// advect.h -- the MAC advection step on the GPU: the engine behind
+// gbp_advect3 / gbp_advect3_device, the drop-in for the reference's
+// macadvection3 module (src/advection/macadvection3.cpp: advect_scalar
+// :38-45 and advect_vector :47-54 with bilinear interpolation) in the order
+// macsmoke3::idle calls them (src/smoke/macsmoke3.cpp:270-281): a scalar
+// carried by the velocity, then the velocity carried by itself.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "advect_core.cuh"
+
+namespace gbp {
+
+// Device scratch of the advection step, grown on demand and kept between
+// calls: the forward values and the limiter's bounds of the faces and cells.
+struct AdvectWork {
+    long long face_cap = 0, cell_cap = 0;
+    float *v0 = nullptr;   // forward velocity, the three face arrays back to back
+    gba::MinMax *vmm = nullptr;  // limiter record per face
+    float *q0 = nullptr;   // forward scalar
+    gba::MinMax *qmm = nullptr;  // limiter record per cell
+};
+
+cudaError_t advect_reserve(AdvectWork &w, long long faces, long long cells);
+void advect_release(AdvectWork &w);
+
+struct AdvectArgs {
+    int nx, ny, nz;
+    double dx, dt;
+    int maccormack;       // MacCormack (the reference's default) or one semi-Lagrangian pass
+    int trim_narrowband;  // TrimNarrowBand: bands of the fluid level set kept first order
+    float *u, *v, *w;     // device face velocities, in/out
+    const float *fluid;   // device cell level set
+    float *q;             // device cell scalar, in/out (may be NULL: velocity only)
+    const unsigned char *q_mask;  // active cells of q (NULL: all)
+    float q_bg;           // the value q reads off its active cells
+    int velocity;         // also carry u, v, w by themselves (advect_vector)
+};
+
+// Enqueues the step on `stream`; *launches counts kernel launches.
+cudaError_t advect_run(AdvectWork &w, const AdvectArgs &a, cudaStream_t stream, long long *launches);
+
+}  // namespace gbp

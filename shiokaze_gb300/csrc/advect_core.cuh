@@ -1,0 +1,382 @@
+// advect_core.cuh -- per-face and per-cell arithmetic of the MAC advection
+// step (MacCormack or semi-Lagrangian, trilinear interpolation), shared by
+// the kernels in advect_kernels.cu.
+//
+// It follows src/advection/macadvection3.cpp (WENO off, the module's
+// default) with the reference's types, so that every result rounds as the
+// reference's scalar C++ does (the including translation unit is compiled
+// with --fmad=false):
+//   face trace   (i,j,k) - dt*u/dx with u a float vector: dt*u and /dx are
+//                each rounded to float, the difference taken in double
+//                (advect_semiLagrangian_u, :82-89)
+//   min/max      the same trace in double, the eight interpolation corners'
+//                min/max from DBL_MAX / DBL_MIN, and the narrow-band test
+//                on the fluid level set at the traced face position
+//                (:97-131)
+//   cell trace   (i,j,k) - dt*u/dx in double (:188-203); min/max from
+//                FLT_MAX / FLT_MIN (:212-227)
+//   correction   0.5*(float)(in - backward), clamped to [min, max] outside
+//                the narrow band (:150-167, :256-269)
+//   interpolation include/shiokaze/array/array_interpolator3.h:50-104:
+//                clamp to the array, corner weights as products of the three
+//                axis weights, skip zero weights, accumulate in float with
+//                double products
+//   full vectors  include/shiokaze/array/macarray3.h:305-371: the other two
+//                components at a face as the mean of four clamped faces
+//                (double sum / 4), at a cell as 0.5*(lo + hi) faces
+// Every face of the velocity is active (the smoke scene's velocity,
+// src/smoke/macsmoke3.cpp:115); a scalar's inactive cells read its
+// background value.
+#pragma once
+
+#include <cfloat>
+
+#ifdef __CUDACC__
+#define GBA_HD __host__ __device__ __forceinline__
+#else
+#define GBA_HD inline
+#endif
+
+namespace gba {
+
+struct Shape {
+    int w, h, d;
+};
+
+struct Dims {
+    int nx, ny, nz;
+    double dx;      // grid spacing
+    double inv_dx;  // 1/dx; used only when dx is a power of two (then exact)
+    float inv_dx_f;
+    int pow2;       // dx is a power of two: divisions by dx are exact multiplications
+    double limit;   // -dx * TrimNarrowBand
+};
+
+GBA_HD Shape face_shape(const Dims &g, int dim) {
+    return Shape{g.nx + (dim == 0), g.ny + (dim == 1), g.nz + (dim == 2)};
+}
+
+GBA_HD long long at(const Shape &s, int i, int j, int k) {
+    return (long long)i + (long long)s.w * ((long long)j + (long long)s.h * k);
+}
+
+// std::min / std::max with the reference's argument order
+GBA_HD double smin(double a, double b) { return (b < a) ? b : a; }
+GBA_HD double smax(double a, double b) { return (a < b) ? b : a; }
+
+// corner of the interpolation cell and the three axis positions
+// (array_interpolator3::interpolate_coef, array_interpolator3.h:50-73)
+struct Corner {
+    int i, j, k;
+    double x, y, z;
+};
+
+GBA_HD Corner corner(const Shape &s, double px, double py, double pz) {
+    Corner c;
+    c.x = smax(0.0, smin(s.w - 1., px));
+    c.y = smax(0.0, smin(s.h - 1., py));
+    c.z = smax(0.0, smin(s.d - 1., pz));
+    c.i = (int)smin(c.x, s.w - 2.);
+    c.j = (int)smin(c.y, s.h - 2.);
+    c.k = (int)smin(c.z, s.d - 2.);
+    return c;
+}
+
+// array_interpolator3::interpolate<float> (:86-104) of a dense float array;
+// Read(x) returns the array's value at a flat index.
+template <class Read>
+GBA_HD float interp(const Shape &s, double px, double py, double pz, Read read) {
+    const Corner c = corner(s, px, py, pz);
+    const double ax0 = c.i + 1 - c.x, ax1 = c.x - c.i;
+    const double ay0 = c.j + 1 - c.y, ay1 = c.y - c.j;
+    const double az0 = c.k + 1 - c.z, az1 = c.z - c.k;
+    // coef[n] = az * ax * ay, multiplied left to right as the reference does
+    const double zx00 = az0 * ax0, zx01 = az0 * ax1, zx10 = az1 * ax0, zx11 = az1 * ax1;
+    const double coef[8] = {zx00 * ay0, zx01 * ay0, zx00 * ay1, zx01 * ay1,
+                            zx10 * ay0, zx11 * ay0, zx10 * ay1, zx11 * ay1};
+    const long long base = at(s, c.i, c.j, c.k);
+    const long long sy = s.w, sz = (long long)s.w * s.h;
+    const long long off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
+    float value = 0.0f;
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+        if (coef[n]) value = (float)((double)value + (double)read(base + off[n]) * coef[n]);
+    return value;
+}
+
+// min and max of the eight corners' values (the MacCormack limiter's
+// bounds), starting from `lo0` and `hi0`
+template <class Read>
+GBA_HD void corner_minmax(const Shape &s, double px, double py, double pz, double lo0, double hi0, Read read,
+                          float &lo, float &hi) {
+    const Corner c = corner(s, px, py, pz);
+    const long long base = at(s, c.i, c.j, c.k);
+    const long long sy = s.w, sz = (long long)s.w * s.h;
+    const long long off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
+    double l = lo0, h = hi0;
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+        const double v = read(base + off[n]);
+        l = smin(l, v);
+        h = smax(h, v);
+    }
+    lo = (float)l;
+    hi = (float)h;
+}
+
+// the full velocity at face (i,j,k) of component `dim` (macarray3.h:350-371):
+// its own component, and each other component as the mean of the four faces
+// around it, indices clamped to that component's shape
+GBA_HD void face_full(const Dims &g, const float *const comp[3], int dim, int i, int j, int k, float u[3]) {
+    const int pi[3] = {i - (dim == 0), j - (dim == 1), k - (dim == 2)};
+#pragma unroll
+    for (int ud = 0; ud < 3; ++ud) {
+        if (ud == dim) {
+            u[ud] = comp[ud][at(face_shape(g, ud), i, j, k)];
+            continue;
+        }
+        const Shape s = face_shape(g, ud);
+        double sum = 0.0;
+#pragma unroll
+        for (int ii = 0; ii < 2; ++ii)
+#pragma unroll
+            for (int jj = 0; jj < 2; ++jj) {
+                int q[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) q[c] = pi[c] + ii * (dim == c) + jj * (ud == c);
+                // shape3::clamp (include/shiokaze/math/shape.h:790-797)
+                q[0] = q[0] < 0 ? 0 : (q[0] > s.w - 1 ? s.w - 1 : q[0]);
+                q[1] = q[1] < 0 ? 0 : (q[1] > s.h - 1 ? s.h - 1 : q[1]);
+                q[2] = q[2] < 0 ? 0 : (q[2] > s.d - 1 ? s.d - 1 : q[2]);
+                sum += comp[ud][at(s, q[0], q[1], q[2])];
+            }
+        u[ud] = (float)(sum / 4.0);
+    }
+}
+
+// the full velocity at cell (i,j,k) (macarray3.h:305-343)
+GBA_HD void cell_full(const Dims &g, const float *const comp[3], int i, int j, int k, float u[3]) {
+#pragma unroll
+    for (int dim = 0; dim < 3; ++dim) {
+        const Shape s = face_shape(g, dim);
+        double value = 0.0;
+        value += comp[dim][at(s, i, j, k)];
+        value += comp[dim][at(s, i + (dim == 0), j + (dim == 1), k + (dim == 2))];
+        u[dim] = (float)(0.5 * value);
+    }
+}
+
+// dt*u/dx of one float velocity component as the float vector arithmetic
+// forms it: (float)(u*dt), then (float)(t/dx)
+GBA_HD float trace_f(const Dims &g, float u, double dt) {
+    const float t = (float)((double)u * dt);
+    return g.pow2 ? t * g.inv_dx_f : (float)((double)t / g.dx);
+}
+
+// u*dt/dx in double
+GBA_HD double trace_d(const Dims &g, double u, double dt) {
+    return g.pow2 ? (u * dt) * g.inv_dx : (u * dt) / g.dx;
+}
+
+// the MacCormack limiter's record for one face or cell: within the narrow
+// band (take the forward value) or the [lo, hi] clamp bounds. `within` is
+// kept as a NaN in lo: lo is a min over values starting from a finite bound,
+// and a NaN never wins std::min's comparison, so lo is never NaN otherwise.
+struct alignas(8) MinMax {
+    float lo, hi;
+};
+
+GBA_HD bool mm_within(const MinMax &m) { return m.lo != m.lo; }
+
+// the final MacCormack value (macadvection3.cpp:150-167, :256-269)
+GBA_HD float maccormack(const MinMax &m, float in, float fwd, float bwd) {
+    if (mm_within(m)) return fwd;
+    const double lo = m.lo, hi = m.hi, x0 = fwd;
+    const double corr = 0.5 * (double)(float)(in - bwd);
+    if (x0 + corr < lo) return (float)lo;
+    if (x0 + corr > hi) return (float)hi;
+    return (float)(x0 + corr);
+}
+
+GBA_HD float nan_mark() {
+    union {
+        unsigned u;
+        float f;
+    } b{0x7fc00000u};
+    return b.f;
+}
+
+struct Idx {
+    int i, j, k;
+};
+
+GBA_HD Idx decode(const Shape &s, unsigned f) {
+    const unsigned t = f / (unsigned)s.w;
+    return Idx{(int)(f - t * (unsigned)s.w), (int)(t % (unsigned)s.h), (int)(t / (unsigned)s.h)};
+}
+
+GBA_HD unsigned count(const Shape &s) { return (unsigned)s.w * (unsigned)s.h * (unsigned)s.d; }
+
+// Arguments of the four passes. Face scratch (v0, vmm) holds the three
+// components back to back at offsets 0, off1, off2.
+struct StepArgs {
+    Dims g;
+    double dt;
+    float *u, *v, *w;  // velocity, in/out
+    const float *fluid;
+    float *q;  // scalar, in/out
+    const unsigned char *mask;
+    float bg;
+    float *v0;
+    MinMax *vmm;
+    long long off1, off2;
+    float *q0;
+    MinMax *qmm;
+};
+
+// forward semi-Lagrangian pass at face f of component dim
+// (advect_semiLagrangian_u, macadvection3.cpp:70-134): the forward value
+// and, for MacCormack, the limiter record
+template <bool MAC>
+GBA_HD void face_forward(const StepArgs &a, int dim, unsigned f) {
+    const Dims &g = a.g;
+    const Shape fs = face_shape(g, dim);
+    if (f >= count(fs)) return;
+    const Idx x = decode(fs, f);
+    const int ip[3] = {x.i, x.j, x.k};
+    const float *const comp[3] = {a.u, a.v, a.w};
+    const float *src = dim == 0 ? a.u : (dim == 1 ? a.v : a.w);
+    const long long o = dim == 0 ? 0 : (dim == 1 ? a.off1 : a.off2);
+    auto rd = [src](long long n) { return src[n]; };
+    float uf[3];
+    face_full(g, comp, dim, x.i, x.j, x.k, uf);
+    const bool moving = uf[0] != 0.0f || uf[1] != 0.0f || uf[2] != 0.0f;
+    float out;
+    if (moving) {
+        double p[3];
+        for (int c = 0; c < 3; ++c) p[c] = (double)ip[c] - (double)trace_f(g, uf[c], a.dt);
+        out = interp(fs, p[0], p[1], p[2], rd);
+    } else {
+        out = src[f];
+    }
+    a.v0[o + f] = out;
+    if (!MAC) return;
+    MinMax m;
+    double fp[3];
+    if (moving) {
+        double p[3];
+        for (int c = 0; c < 3; ++c) {
+            const double disp = trace_d(g, (double)uf[c], a.dt);
+            p[c] = (double)ip[c] - disp;
+            fp[c] = (ip[c] + 0.5 * (dim != c)) - disp;
+        }
+        corner_minmax(fs, p[0], p[1], p[2], DBL_MAX, DBL_MIN, rd, m.lo, m.hi);
+    } else {
+        for (int c = 0; c < 3; ++c) fp[c] = ip[c] + 0.5 * (dim != c);
+        m.lo = m.hi = src[f];
+    }
+    const Shape cs{g.nx, g.ny, g.nz};
+    const float *fl = a.fluid;
+    const bool within =
+        (double)interp(cs, fp[0] - 0.5, fp[1] - 0.5, fp[2] - 0.5, [fl](long long n) { return fl[n]; }) > g.limit;
+    if (within) m.lo = nan_mark();
+    a.vmm[o + f] = m;
+}
+
+// backward pass from the forward values (advect_semiLagrangian_u with -dt)
+// and the limited MacCormack correction (macadvection3.cpp:150-167), written
+// over the input face (the only read of the input in this pass)
+GBA_HD void face_backward(const StepArgs &a, int dim, unsigned f) {
+    const Dims &g = a.g;
+    const Shape fs = face_shape(g, dim);
+    if (f >= count(fs)) return;
+    const Idx x = decode(fs, f);
+    const int ip[3] = {x.i, x.j, x.k};
+    const float *const comp[3] = {a.v0, a.v0 + a.off1, a.v0 + a.off2};
+    const float *src = dim == 0 ? comp[0] : (dim == 1 ? comp[1] : comp[2]);
+    float *io = dim == 0 ? a.u : (dim == 1 ? a.v : a.w);
+    const long long o = dim == 0 ? 0 : (dim == 1 ? a.off1 : a.off2);
+    float uf[3];
+    face_full(g, comp, dim, x.i, x.j, x.k, uf);
+    const bool moving = uf[0] != 0.0f || uf[1] != 0.0f || uf[2] != 0.0f;
+    float bwd;
+    if (moving) {
+        double p[3];
+        for (int c = 0; c < 3; ++c) p[c] = (double)ip[c] - (double)trace_f(g, uf[c], -a.dt);
+        bwd = interp(fs, p[0], p[1], p[2], [src](long long n) { return src[n]; });
+    } else {
+        bwd = src[f];
+    }
+    io[f] = maccormack(a.vmm[o + f], io[f], src[f], bwd);
+}
+
+// forward semi-Lagrangian pass at cell c (advect_semiLagrangian_cell,
+// macadvection3.cpp:182-232); inactive cells take the background
+template <bool MAC>
+GBA_HD void cell_forward(const StepArgs &a, unsigned c) {
+    const Dims &g = a.g;
+    const Shape cs{g.nx, g.ny, g.nz};
+    if (c >= count(cs)) return;
+    const unsigned char *mask = a.mask;
+    const float bg = a.bg;
+    if (mask && !mask[c]) {
+        a.q0[c] = bg;
+        return;
+    }
+    const Idx x = decode(cs, c);
+    const int ip[3] = {x.i, x.j, x.k};
+    const float *const comp[3] = {a.u, a.v, a.w};
+    const float *q = a.q;
+    auto rq = [q, mask, bg](long long n) { return (mask && !mask[n]) ? bg : q[n]; };
+    float uc[3];
+    cell_full(g, comp, x.i, x.j, x.k, uc);
+    const bool moving = uc[0] != 0.0f || uc[1] != 0.0f || uc[2] != 0.0f;
+    double p[3] = {0.0, 0.0, 0.0};
+    if (moving)
+        for (int d = 0; d < 3; ++d) p[d] = (double)ip[d] - trace_d(g, (double)uc[d], a.dt);
+    const float qc = q[c];
+    a.q0[c] = moving ? interp(cs, p[0], p[1], p[2], rq) : qc;
+    if (!MAC) return;
+    MinMax m;
+    bool within;
+    const float *fl = a.fluid;
+    if (moving) {
+        corner_minmax(cs, p[0], p[1], p[2], (double)FLT_MAX, (double)FLT_MIN, rq, m.lo, m.hi);
+        within = (double)interp(cs, p[0], p[1], p[2], [fl](long long n) { return fl[n]; }) > g.limit;
+    } else {
+        m.lo = m.hi = qc;
+        within = (double)fl[c] > g.limit;
+    }
+    if (within) m.lo = nan_mark();
+    a.qmm[c] = m;
+}
+
+// backward pass and limited correction at cell c (macadvection3.cpp:
+// 256-269), written over the input scalar (its only read in this pass)
+GBA_HD void cell_backward(const StepArgs &a, unsigned c) {
+    const Dims &g = a.g;
+    const Shape cs{g.nx, g.ny, g.nz};
+    if (c >= count(cs)) return;
+    if (a.mask && !a.mask[c]) {
+        a.q[c] = a.bg;
+        return;
+    }
+    const Idx x = decode(cs, c);
+    const int ip[3] = {x.i, x.j, x.k};
+    const float *const comp[3] = {a.u, a.v, a.w};
+    float uc[3];
+    cell_full(g, comp, x.i, x.j, x.k, uc);
+    const bool moving = uc[0] != 0.0f || uc[1] != 0.0f || uc[2] != 0.0f;
+    const float *q0 = a.q0;
+    float bwd;
+    if (moving) {
+        double p[3];
+        for (int d = 0; d < 3; ++d) p[d] = (double)ip[d] - trace_d(g, (double)uc[d], -a.dt);
+        bwd = interp(cs, p[0], p[1], p[2], [q0](long long n) { return q0[n]; });
+    } else {
+        bwd = q0[c];
+    }
+    a.q[c] = maccormack(a.qmm[c], a.q[c], q0[c], bwd);
+}
+
+}  // namespace gba

@@ -1,0 +1,166 @@
+// advect_kernels.cu -- MacCormack / semi-Lagrangian advection of a cell
+// scalar and of the MAC velocity on dense device grids (see advect.h and
+// advect_core.cuh). Compiled with --fmad=false: every result equals the
+// reference's scalar C++ bit for bit.
+//
+// A MacCormack step is four launches: scalar forward (forward value and the
+// limiter's record per cell), scalar backward (+ the limited correction,
+// written in place), velocity forward, velocity backward (in place). The
+// backward kernels read the step's input only at their own face or cell, so
+// writing the result over it is safe; the forward kernels read neighbours
+// and write scratch. One semi-Lagrangian pass is the forward kernel and a
+// copy back.
+//
+// One thread per face (blockIdx.y = component) or cell. Algorithmic DRAM
+// bytes per face of a MacCormack velocity step: forward reads u (4; the
+// neighbours come from cache) and writes the forward value and the limiter
+// record (4 + 8), backward reads them and the input (16) and writes the
+// result (4): 32 B. Cell scalar: the same 32 B plus the fluid level set read
+// twice (8) and, on the cell passes, the 3 velocity components' two faces
+// (counted once, 12). The arithmetic is the reference's: trilinear weights
+// and sums in FP64 on every trace (three per face, two per cell), which on
+// this GPU's FP64 pipe, not DRAM, bounds the kernels.
+#include <cfloat>
+#include <cmath>
+
+#include "advect.h"
+#include "advect_core.cuh"
+
+namespace gbp {
+namespace {
+
+using gba::Dims;
+using gba::StepArgs;
+
+constexpr int ADV_THREADS = 256;
+
+// one thread per face, blockIdx.y = component
+template <bool MAC>
+__global__ void __launch_bounds__(ADV_THREADS) adv_face_forward(StepArgs a) {
+    gba::face_forward<MAC>(a, (int)blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(ADV_THREADS) adv_face_backward(StepArgs a) {
+    gba::face_backward(a, (int)blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// one thread per cell
+template <bool MAC>
+__global__ void __launch_bounds__(ADV_THREADS) adv_cell_forward(StepArgs a) {
+    gba::cell_forward<MAC>(a, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(ADV_THREADS) adv_cell_backward(StepArgs a) {
+    gba::cell_backward(a, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+Dims make_dims(const AdvectArgs &a) {
+    Dims g{};
+    g.nx = a.nx;
+    g.ny = a.ny;
+    g.nz = a.nz;
+    g.dx = a.dx;
+    int e = 0;
+    const double m = std::frexp(a.dx, &e);
+    const double inv = 1.0 / a.dx;
+    g.pow2 = (m == 0.5 && std::isfinite(inv) && (double)(float)inv == inv) ? 1 : 0;
+    g.inv_dx = inv;
+    g.inv_dx_f = (float)inv;
+    g.limit = -a.dx * (double)a.trim_narrowband;
+    return g;
+}
+
+unsigned blocks_for(long long n) { return (unsigned)((n + ADV_THREADS - 1) / ADV_THREADS); }
+
+}  // namespace
+
+cudaError_t advect_reserve(AdvectWork &w, long long faces, long long cells) {
+    if (faces > w.face_cap) {
+        cudaFree(w.v0);
+        cudaFree(w.vmm);
+        w.v0 = nullptr;
+        w.vmm = nullptr;
+        w.face_cap = 0;
+        cudaError_t e = cudaMalloc(&w.v0, sizeof(float) * (size_t)faces);
+        if (e == cudaSuccess) e = cudaMalloc(&w.vmm, sizeof(gba::MinMax) * (size_t)faces);
+        if (e != cudaSuccess) return e;
+        w.face_cap = faces;
+    }
+    if (cells > w.cell_cap) {
+        cudaFree(w.q0);
+        cudaFree(w.qmm);
+        w.q0 = nullptr;
+        w.qmm = nullptr;
+        w.cell_cap = 0;
+        cudaError_t e = cudaMalloc(&w.q0, sizeof(float) * (size_t)cells);
+        if (e == cudaSuccess) e = cudaMalloc(&w.qmm, sizeof(gba::MinMax) * (size_t)cells);
+        if (e != cudaSuccess) return e;
+        w.cell_cap = cells;
+    }
+    return cudaSuccess;
+}
+
+void advect_release(AdvectWork &w) {
+    cudaFree(w.v0);
+    cudaFree(w.vmm);
+    cudaFree(w.q0);
+    cudaFree(w.qmm);
+    w = AdvectWork{};
+}
+
+cudaError_t advect_run(AdvectWork &w, const AdvectArgs &a, cudaStream_t st, long long *launches) {
+    const long long cells = (long long)a.nx * a.ny * a.nz;
+    const long long nf0 = (long long)(a.nx + 1) * a.ny * a.nz, nf1 = (long long)a.nx * (a.ny + 1) * a.nz,
+                    nf2 = (long long)a.nx * a.ny * (a.nz + 1);
+    long long nfmax = nf0 > nf1 ? nf0 : nf1;
+    if (nf2 > nfmax) nfmax = nf2;
+    cudaError_t e = advect_reserve(w, a.velocity ? nf0 + nf1 + nf2 : 0, a.q ? cells : 0);
+    if (e != cudaSuccess) return e;
+    StepArgs s{};
+    s.g = make_dims(a);
+    s.dt = a.dt;
+    s.u = a.u;
+    s.v = a.v;
+    s.w = a.w;
+    s.fluid = a.fluid;
+    s.q = a.q;
+    s.mask = a.q_mask;
+    s.bg = a.q_bg;
+    s.v0 = w.v0;
+    s.vmm = w.vmm;
+    s.off1 = nf0;
+    s.off2 = nf0 + nf1;
+    s.q0 = w.q0;
+    s.qmm = w.qmm;
+    if (a.q) {
+        if (a.maccormack) {
+            adv_cell_forward<true><<<blocks_for(cells), ADV_THREADS, 0, st>>>(s);
+            adv_cell_backward<<<blocks_for(cells), ADV_THREADS, 0, st>>>(s);
+            *launches += 2;
+        } else {
+            adv_cell_forward<false><<<blocks_for(cells), ADV_THREADS, 0, st>>>(s);
+            *launches += 1;
+            e = cudaMemcpyAsync(a.q, w.q0, sizeof(float) * (size_t)cells, cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) return e;
+        }
+    }
+    if (!a.velocity) return cudaGetLastError();
+    const dim3 fgrid(blocks_for(nfmax), 3);
+    if (a.maccormack) {
+        adv_face_forward<true><<<fgrid, ADV_THREADS, 0, st>>>(s);
+        adv_face_backward<<<fgrid, ADV_THREADS, 0, st>>>(s);
+        *launches += 2;
+    } else {
+        adv_face_forward<false><<<fgrid, ADV_THREADS, 0, st>>>(s);
+        *launches += 1;
+        float *dst[3] = {a.u, a.v, a.w};
+        const long long n[3] = {nf0, nf1, nf2}, o[3] = {0, s.off1, s.off2};
+        for (int d = 0; d < 3; ++d) {
+            e = cudaMemcpyAsync(dst[d], w.v0 + o[d], sizeof(float) * (size_t)n[d], cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) return e;
+        }
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace gbp

@@ -20,6 +20,7 @@
 #include <string>
 #include <vector>
 
+#include "advect.h"
 #include "csr_solver.h"
 #include "gbp_kernels.h"
 #include "gbp_solver.h"
@@ -59,6 +60,10 @@ struct gbp_ctx {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     long long launches = 0;
     CsrWork csr;  // device arrays of gbp_csr_cg
+    AdvectWork adv;  // device scratch of gbp_advect3*
+    // staging of the host-array advection call, grown on demand
+    float *adv_stage = nullptr;
+    long long adv_stage_floats = 0;
 };
 
 struct gbp_scene {
@@ -139,6 +144,8 @@ void gbp_destroy(gbp_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->device);
     csr_release(c->csr);
+    advect_release(c->adv);
+    if (c->adv_stage) cudaFree(c->adv_stage);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -622,6 +629,126 @@ int gbp_debug_assemble(gbp_scene *s, double dt, const float *solid, const float 
     if (g.dim == 3) GBP_CUDA(cudaMemcpyAsync(cz, st.cz, bytes, cudaMemcpyDeviceToHost, str));
     GBP_CUDA(cudaMemcpyAsync(b, st.b, bytes, cudaMemcpyDeviceToHost, str));
     GBP_CUDA(cudaStreamSynchronize(str));
+    return GBP_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// MAC advection (macadvection3, src/advection/macadvection3.cpp)
+
+namespace {
+
+int advect_check(const char *who, gbp_ctx *c, int nx, int ny, int nz, double dx, double dt,
+                 const gbp_advect_params *params, const float *u, const float *v, const float *w,
+                 const float *fluid, const float *q, gbp_advect_params *out) {
+    if (!c) return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": NULL context");
+    gbp_advect_params_default(out);
+    if (params) *out = *params;
+    if (nx < 2 || ny < 2 || nz < 2)
+        return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": every grid edge must be at least 2 cells");
+    if ((long long)(nx + 1) * ny * nz >= (1LL << 31) || (long long)nx * (ny + 1) * nz >= (1LL << 31) ||
+        (long long)nx * ny * (nz + 1) >= (1LL << 31))
+        return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": 2^31 faces or more in one component");
+    if (!(dx > 0.0) || !std::isfinite(dx) || !std::isfinite(dt))
+        return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": dx must be positive and finite, dt finite");
+    if (out->trim_narrowband < 0)
+        return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": trim_narrowband must be >= 0");
+    if (!fluid || !u || !v || !w) return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": NULL array");
+    if (!out->advect_velocity && !q)
+        return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": nothing to advect (no scalar, velocity off)");
+    return GBP_OK;
+}
+
+AdvectArgs advect_args(int nx, int ny, int nz, double dx, double dt, const gbp_advect_params &p, float *u, float *v,
+                       float *w, const float *fluid, float *q, const unsigned char *q_mask, float q_bg) {
+    AdvectArgs a{};
+    a.nx = nx;
+    a.ny = ny;
+    a.nz = nz;
+    a.dx = dx;
+    a.dt = dt;
+    a.maccormack = p.maccormack ? 1 : 0;
+    a.trim_narrowband = p.trim_narrowband;
+    a.u = u;
+    a.v = v;
+    a.w = w;
+    a.fluid = fluid;
+    a.q = q;
+    a.q_mask = q_mask;
+    a.q_bg = q_bg;
+    a.velocity = p.advect_velocity ? 1 : 0;
+    return a;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gbp_advect_params_default(gbp_advect_params *p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->maccormack = 1;
+    p->trim_narrowband = 1;
+    p->advect_velocity = 1;
+}
+
+int gbp_advect3_device(gbp_ctx *c, int nx, int ny, int nz, double dx, double dt, const gbp_advect_params *params,
+                       float *u, float *v, float *w, const float *fluid, float *q, const unsigned char *q_mask,
+                       float q_bg, void *stream) {
+    gbp_advect_params p;
+    int rc = advect_check("gbp_advect3_device", c, nx, ny, nz, dx, dt, params, u, v, w, fluid, q, &p);
+    if (rc) return rc;
+    GBP_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    if (!stream) {
+        GBP_CUDA(cudaEventRecord(c->ev[0], cudaStreamLegacy));
+        GBP_CUDA(cudaStreamWaitEvent(st, c->ev[0], 0));
+    }
+    long long launched = 0;
+    GBP_CUDA(advect_run(c->adv, advect_args(nx, ny, nz, dx, dt, p, u, v, w, fluid, q, q_mask, q_bg), st, &launched));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    c->launches += launched;
+    return GBP_OK;
+}
+
+int gbp_advect3(gbp_ctx *c, int nx, int ny, int nz, double dx, double dt, const gbp_advect_params *params, float *u,
+                float *v, float *w, const float *fluid, float *q, const unsigned char *q_mask, float q_bg) {
+    gbp_advect_params p;
+    int rc = advect_check("gbp_advect3", c, nx, ny, nz, dx, dt, params, u, v, w, fluid, q, &p);
+    if (rc) return rc;
+    GBP_CUDA(cudaSetDevice(c->device));
+    const size_t cells = (size_t)nx * ny * nz;
+    const size_t nf[3] = {(size_t)(nx + 1) * ny * nz, (size_t)nx * (ny + 1) * nz, (size_t)nx * ny * (nz + 1)};
+    const size_t mask_floats = q && q_mask ? (cells + 3) / 4 : 0;
+    const long long need = (long long)(nf[0] + nf[1] + nf[2] + cells + (q ? cells : 0) + mask_floats);
+    if (need > c->adv_stage_floats) {
+        if (c->adv_stage) cudaFree(c->adv_stage);
+        c->adv_stage = nullptr;
+        c->adv_stage_floats = 0;
+        GBP_CUDA(cudaMalloc(&c->adv_stage, sizeof(float) * (size_t)need));
+        c->adv_stage_floats = need;
+    }
+    float *du = c->adv_stage, *dv = du + nf[0], *dw = dv + nf[1], *df = dw + nf[2];
+    float *dq = q ? df + cells : nullptr;
+    unsigned char *dm = mask_floats ? (unsigned char *)(df + 2 * cells) : nullptr;
+    cudaStream_t st = c->stream;
+    GBP_CUDA(cudaMemcpyAsync(du, u, 4 * nf[0], cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(dv, v, 4 * nf[1], cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(dw, w, 4 * nf[2], cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(df, fluid, 4 * cells, cudaMemcpyHostToDevice, st));
+    if (dq) GBP_CUDA(cudaMemcpyAsync(dq, q, 4 * cells, cudaMemcpyHostToDevice, st));
+    if (dm) GBP_CUDA(cudaMemcpyAsync(dm, q_mask, cells, cudaMemcpyHostToDevice, st));
+    long long launched = 0;
+    GBP_CUDA(advect_run(c->adv, advect_args(nx, ny, nz, dx, dt, p, du, dv, dw, df, dq, dm, q_bg), st, &launched));
+    if (p.advect_velocity) {
+        GBP_CUDA(cudaMemcpyAsync(u, du, 4 * nf[0], cudaMemcpyDeviceToHost, st));
+        GBP_CUDA(cudaMemcpyAsync(v, dv, 4 * nf[1], cudaMemcpyDeviceToHost, st));
+        GBP_CUDA(cudaMemcpyAsync(w, dw, 4 * nf[2], cudaMemcpyDeviceToHost, st));
+    }
+    if (dq) GBP_CUDA(cudaMemcpyAsync(q, dq, 4 * cells, cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    c->launches += launched;
     return GBP_OK;
 }
 

@@ -81,3 +81,10 @@ def test_create_without_device_fails_cleanly(lib):
     h = ctypes.c_void_p()
     rc = lib.gbp_create(0, ctypes.byref(h))
     assert rc == 6 and not h  # GBP_ERR_NO_DEVICE
+
+
+def test_advect_params_default_matches_reference_defaults(lib):
+    p = gb.AdvectParams()
+    lib.gbp_advect_params_default(ctypes.byref(p))
+    # src/advection/macadvection3.cpp:284-288: MacCormack on, TrimNarrowBand 1
+    assert p.maccormack == 1 and p.trim_narrowband == 1 and p.advect_velocity == 1
