@@ -186,6 +186,8 @@ def _ref_lib():
         lib.ref_levelset_roundtrip.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp,
                                                ctypes.c_int, ctypes.c_float, fp]
         dp = ctypes.POINTER(ctypes.c_double)
+        lib.ref_advect_load.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_char_p,
+                                        ctypes.c_char_p]
         lib.ref_advect3.restype = ctypes.c_double
         lib.ref_advect3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_char_p, fp, fp, fp, fp, ctypes.c_int, ctypes.c_float, fp,
@@ -244,11 +246,13 @@ def advect3(u, v, w, fluid, dx, dt, q=None, q_mask=None, q_bg=0.0, maccormack=Tr
 
 
 def ref_advect3(u, v, w, fluid, fluid_mode, band, dx, dt, q=None, q_mask=None, q_bg=0.0, maccormack=True,
-                trim_narrowband=1):
+                trim_narrowband=1, extra_kv=""):
     """The reference's own macadvection3 on dense 3D arrays (arrays z, y, x;
     every velocity face active): the scalar q (if given; active where q_mask,
     all if None) advected by the velocity, then the velocity by itself, as
-    macsmoke3::idle does. Returns (u, v, w, q, ms) as new arrays."""
+    macsmoke3::idle does. extra_kv adds configuration (Advection=<module>
+    loads another module through the reference's loader). Returns (u, v, w,
+    q, ms) as new arrays."""
     lib = _ref_lib()
     fp = ctypes.POINTER(ctypes.c_float)
     nz, ny, nx = fluid.shape
@@ -256,7 +260,7 @@ def ref_advect3(u, v, w, fluid, fluid_mode, band, dx, dt, q=None, q_mask=None, q
     fl = np.ascontiguousarray(fluid, dtype=np.float32)
     qo = None if q is None else np.array(q, dtype=np.float32, order="C")
     qm = None if q_mask is None else np.ascontiguousarray(q_mask, dtype=np.uint8)
-    kv = f"MacCormack={'Yes' if maccormack else 'No'} TrimNarrowBand={int(trim_narrowband)}"
+    kv = f"MacCormack={'Yes' if maccormack else 'No'} TrimNarrowBand={int(trim_narrowband)} {extra_kv}".strip()
     log = tempfile.NamedTemporaryFile(prefix="ref_advect_", suffix=".log", delete=False).name
     try:
         ms = lib.ref_advect3(nx, ny, nz, dx, dt, kv.encode(), uo.ctypes.data_as(fp), vo.ctypes.data_as(fp),

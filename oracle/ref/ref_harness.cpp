@@ -406,4 +406,21 @@ double ref_advect3(int nx, int ny, int nz, double dx, double dt, const char *kv,
     return ms;
 }
 
+/* Loads, configures and initializes the advection module the
+ * configuration names (Advection=<name>, default macadvection3) through the
+ * reference's loader, without calling it; returns 1. For checking that a
+ * replacement module loads in place of macadvection3. */
+int ref_advect_load(int nx, int ny, int nz, double dx, const char *kv, const char *log_path) {
+    configuration &config = install_global_config(kv);
+    shape3 s(nx, ny, nz);
+    double dxv = dx;
+    with_stdout_to(log_path, [&]() {
+        macadvection3_driver adv("macadvection3");
+        adv.set_environment("shape", &s);
+        adv.set_environment("dx", &dxv);
+        adv.setup_now(config);
+    });
+    return 1;
+}
+
 }  // extern "C"

@@ -30,6 +30,7 @@
 #pragma once
 
 #include <cfloat>
+#include <cmath>
 
 #ifdef __CUDACC__
 #define GBA_HD __host__ __device__ __forceinline__
@@ -105,23 +106,73 @@ GBA_HD float interp(const Shape &s, double px, double py, double pz, Read read) 
 }
 
 // min and max of the eight corners' values (the MacCormack limiter's
-// bounds), starting from `lo0` and `hi0`
+// bounds), starting from `lo0` and `hi0`. The reference compares in double
+// from DBL_MAX / DBL_MIN (faces) or FLT_MAX / FLT_MIN (cells); the same
+// comparisons on the floats themselves give the same answers (a float's
+// double image is exact and ordered alike), and the double start values are
+// replaced by floats with the same outcome: DBL_MAX by +inf (only +inf and
+// NaN fail `v < start`, and DBL_MAX rounds to +inf in the end), DBL_MIN by
+// +0 (`DBL_MIN < v` holds for a float v exactly when `0 < v`, and DBL_MIN
+// rounds to +0). So the whole search runs on FP32, bit-exact.
 template <class Read>
-GBA_HD void corner_minmax(const Shape &s, double px, double py, double pz, double lo0, double hi0, Read read,
+GBA_HD void corner_minmax(const Shape &s, double px, double py, double pz, float lo0, float hi0, Read read,
                           float &lo, float &hi) {
     const Corner c = corner(s, px, py, pz);
     const long long base = at(s, c.i, c.j, c.k);
     const long long sy = s.w, sz = (long long)s.w * s.h;
     const long long off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
-    double l = lo0, h = hi0;
+    float l = lo0, h = hi0;
 #pragma unroll
     for (int n = 0; n < 8; ++n) {
-        const double v = read(base + off[n]);
-        l = smin(l, v);
-        h = smax(h, v);
+        const float v = read(base + off[n]);
+        l = (v < l) ? v : l;
+        h = (h < v) ? v : h;
     }
-    lo = (float)l;
-    hi = (float)h;
+    lo = l;
+    hi = h;
+}
+
+// interp(s, p, a) > limit, the narrow-band test. The eight corners' range
+// [mn, mx] usually decides it: the weights are nonnegative and sum to 1
+// within 16 double ulps, and each of the eight float accumulations of
+// interp rounds by at most 2^-24 of a partial sum bounded by M = max|a|,
+// so the interpolant lies in [mn - d, mx + d] for d = 2^-20 M + 1e-38
+// (twice the bound, plus the subnormal spacing eight times over). When
+// the limit falls inside that band, or a value is not finite, the
+// interpolant itself is compared; either way the answer is the reference's.
+GBA_HD bool above_limit(const Shape &s, double px, double py, double pz, const float *a, double limit) {
+    const Corner c = corner(s, px, py, pz);
+    const long long base = at(s, c.i, c.j, c.k);
+    const long long sy = s.w, sz = (long long)s.w * s.h;
+    const long long off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
+    float v[8];
+#pragma unroll
+    for (int n = 0; n < 8; ++n) v[n] = a[base + off[n]];
+    float mn = v[0], mx = v[0], sum = v[0];
+#pragma unroll
+    for (int n = 1; n < 8; ++n) {
+        mn = v[n] < mn ? v[n] : mn;
+        mx = mx < v[n] ? v[n] : mx;
+        sum += v[n];
+    }
+    if (sum - sum == 0.0f) {  // every value finite (a NaN or an infinity makes this false)
+        const float am = (-mn < mx) ? mx : -mn;
+        const double d = (double)am * 9.5367431640625e-07 + 1e-38;
+        if ((double)mx + d <= limit) return false;
+        if ((double)mn - d > limit) return true;
+    }
+    // the interpolant, as interp forms it (same corner, weights and order)
+    const double ax0 = c.i + 1 - c.x, ax1 = c.x - c.i;
+    const double ay0 = c.j + 1 - c.y, ay1 = c.y - c.j;
+    const double az0 = c.k + 1 - c.z, az1 = c.z - c.k;
+    const double zx00 = az0 * ax0, zx01 = az0 * ax1, zx10 = az1 * ax0, zx11 = az1 * ax1;
+    const double coef[8] = {zx00 * ay0, zx01 * ay0, zx00 * ay1, zx01 * ay1,
+                            zx10 * ay0, zx11 * ay0, zx10 * ay1, zx11 * ay1};
+    float value = 0.0f;
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+        if (coef[n]) value = (float)((double)value + (double)v[n] * coef[n]);
+    return (double)value > limit;
 }
 
 // the full velocity at face (i,j,k) of component `dim` (macarray3.h:350-371):
@@ -270,15 +321,14 @@ GBA_HD void face_forward(const StepArgs &a, int dim, unsigned f) {
             p[c] = (double)ip[c] - disp;
             fp[c] = (ip[c] + 0.5 * (dim != c)) - disp;
         }
-        corner_minmax(fs, p[0], p[1], p[2], DBL_MAX, DBL_MIN, rd, m.lo, m.hi);
+        corner_minmax(fs, p[0], p[1], p[2], INFINITY, 0.0f, rd, m.lo, m.hi);  // DBL_MAX, DBL_MIN
     } else {
         for (int c = 0; c < 3; ++c) fp[c] = ip[c] + 0.5 * (dim != c);
         m.lo = m.hi = src[f];
     }
     const Shape cs{g.nx, g.ny, g.nz};
     const float *fl = a.fluid;
-    const bool within =
-        (double)interp(cs, fp[0] - 0.5, fp[1] - 0.5, fp[2] - 0.5, [fl](long long n) { return fl[n]; }) > g.limit;
+    const bool within = above_limit(cs, fp[0] - 0.5, fp[1] - 0.5, fp[2] - 0.5, fl, g.limit);
     if (within) m.lo = nan_mark();
     a.vmm[o + f] = m;
 }
@@ -341,8 +391,8 @@ GBA_HD void cell_forward(const StepArgs &a, unsigned c) {
     bool within;
     const float *fl = a.fluid;
     if (moving) {
-        corner_minmax(cs, p[0], p[1], p[2], (double)FLT_MAX, (double)FLT_MIN, rq, m.lo, m.hi);
-        within = (double)interp(cs, p[0], p[1], p[2], [fl](long long n) { return fl[n]; }) > g.limit;
+        corner_minmax(cs, p[0], p[1], p[2], FLT_MAX, FLT_MIN, rq, m.lo, m.hi);
+        within = above_limit(cs, p[0], p[1], p[2], fl, g.limit);
     } else {
         m.lo = m.hi = qc;
         within = (double)fl[c] > g.limit;

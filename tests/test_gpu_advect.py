@@ -32,6 +32,16 @@ def bits_equal(a, b):
     return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
+def bits_equal_nan(a, b):
+    """Bit-equal except that any NaN equals any NaN: the GPU writes the
+    canonical NaN where a CPU propagates an input NaN's payload."""
+    a, b = np.asarray(a), np.asarray(b)
+    if a.shape != b.shape or not np.array_equal(np.isnan(a), np.isnan(b)):
+        return False
+    keep = ~np.isnan(a)
+    return np.array_equal(a.view(np.uint32)[keep], b.view(np.uint32)[keep])
+
+
 def gpu_step(u, v, w, fluid, dx, dt, q=None, q_mask=None, q_bg=0.0, maccormack=True, trim_narrowband=1):
     nz, ny, nx = fluid.shape
     adv = gb.MacAdvection3(nx, ny, nz, dx, MacCormack=maccormack, TrimNarrowBand=trim_narrowband)
@@ -75,6 +85,33 @@ def test_advect_matches_oracle_random(seed):
     got = gpu_step(*args, **kw)
     for a, b in zip(got, want[:4]):
         assert bits_equal(a, b)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_narrow_band_test_near_its_limit(seed):
+    """Level sets within a hair of the trimming limit, and non-finite
+    values: the kernels decide most narrow-band tests from the corners'
+    range and must agree with the interpolant wherever it is close."""
+    rng = np.random.default_rng(100 + seed)
+    n = tuple(int(x) for x in rng.integers(2, 14, 3))
+    sc = scenes.smoke3(n, seed=seed, sigma=float(rng.uniform(0.5, 3.0)))
+    trim = int(rng.integers(0, 3))
+    limit = -sc.dx * trim
+    scale = float(10.0 ** rng.uniform(-12, -3)) * sc.dx
+    fluid = (limit + rng.normal(0, 1, sc.fluid.shape) * scale).astype(np.float32)
+    if seed % 3 == 0:
+        fluid.flat[rng.integers(0, fluid.size, 3)] = [np.nan, np.inf, -np.inf]
+    if seed % 4 == 1:
+        fluid[...] = np.float32(limit)
+    q = rng.normal(0, 1, sc.fluid.shape).astype(np.float32)
+    if seed % 4 == 2:
+        q.flat[rng.integers(0, q.size, 2)] = [np.inf, np.nan]
+    u, v, w = (a * np.float32(rng.uniform(0.5, 20)) for a in (sc.u, sc.v, sc.w))
+    kw = dict(q=q, q_mask=None, q_bg=0.0, maccormack=True, trim_narrowband=trim)
+    want = oracle.advect3(u, v, w, fluid, sc.dx, sc.dt, **kw)
+    got = gpu_step(u, v, w, fluid, sc.dx, sc.dt, **kw)
+    for a, b in zip(got, want[:4]):
+        assert bits_equal_nan(a, b)
 
 
 def test_scalar_and_vector_calls_equal_the_step():

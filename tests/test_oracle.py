@@ -129,3 +129,92 @@ def test_module_densify_matches_operator_reads(kind, n):
     if kind.startswith("liquid"):
         a, _, _, _ = oracle.ref_densify_compare(sc.fluid, 0, sc.band)
         assert (a == -np.float32(sc.band)).any() and (a == np.float32(sc.band)).any()
+
+
+def test_advection_module_loads_through_reference_loader(tmp_path):
+    """The advection drop-in: the reference's loader picks gbadvection3 by
+    the Advection key (macadvection3_interface.h:39) in place of
+    macadvection3, configures (MacCormack, TrimNarrowBand) and initializes
+    it. (Advecting needs a GPU.)"""
+    import subprocess
+    if not oracle.reference_available():
+        pytest.skip("reference oracle not built here")
+    root = oracle.HERE.rsplit("/", 1)[0]
+    subprocess.check_call(["make", "-s", "-C", f"{root}/shiokaze_gb300/module", f"OUT={oracle.REF_DIR}"],
+                          stdout=subprocess.DEVNULL)
+    lib = oracle._ref_lib()
+    log = str(tmp_path / "adv.log")
+    assert lib.ref_advect_load(16, 16, 16, 1 / 16, b"Advection=gbadvection3 MacCormack=Yes TrimNarrowBand=2",
+                               log.encode()) == 1
+    text = open(log).read()
+    assert "gbadvection3.so" in text and "macadvection3.so" not in text
+
+
+def advect_module_cases():
+    for seed in (41, 42, 43, 44):
+        rng = np.random.default_rng(seed)
+        n = tuple(int(x) for x in rng.integers(6, 20, 3))
+        sc = (scenes.liquid3(n, seed=seed, pool=float(rng.uniform(0.2, 0.5))) if seed % 2
+              else scenes.smoke3(n, seed=seed, sigma=float(rng.uniform(0.5, 4.0))))
+        m = (rng.random(sc.fluid.shape) > 0.4).astype(np.uint8) if seed != 42 else None
+        q = rng.random(sc.fluid.shape, dtype=np.float32)
+        if m is not None:
+            q = np.where(m != 0, q, np.float32(0.25)).astype(np.float32)
+        kw = dict(q=q, q_mask=m, q_bg=0.25 if m is not None else 0.0, maccormack=seed != 43,
+                  trim_narrowband=int(rng.integers(0, 3)))
+        yield seed, sc, kw
+
+
+# runs in a process of its own: the reference's loader, which unloads its
+# modules at exit, faults at exit when a second advection module (even one
+# that does nothing) was loaded after macadvection3 had run in the process
+ADVECT_MODULE_RUN = r"""
+import sys
+import numpy as np
+import oracle
+sys.path.insert(0, "tests")
+from test_oracle import advect_module_cases
+out = {}
+for seed, sc, kw in advect_module_cases():
+    r = oracle.ref_advect3(sc.u, sc.v, sc.w, sc.fluid, sc.fluid_mode, sc.band, sc.dx, sc.dt,
+                           extra_kv="Advection=gbadvection3stub", **kw)
+    for name, a in zip("uvwq", r[:4]):
+        out[f"{seed}_{name}"] = a
+np.savez(sys.argv[1], **out)
+"""
+
+
+def test_advection_module_boundary_matches_reference_module(tmp_path):
+    """The gbadvection3 module's boundary on the CPU: linked against a
+    stand-in for libgbp that runs the oracle (tests/module_stub), loaded by
+    the reference's own loader in place of macadvection3 on the reference's
+    own tiled arrays (narrow-band liquid level sets, masked densities, every
+    velocity face active), it gives the reference module's results bit for
+    bit: the dense copies, the active mask, dt and the write-back are right."""
+    import os
+    import shutil
+    import subprocess
+    import sys
+    if not oracle.reference_available():
+        pytest.skip("reference oracle not built here")
+    root = oracle.HERE.rsplit("/", 1)[0]
+    oracle.build_port()
+    stub = tmp_path / "libgbp.so"
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-I", f"{root}/include",
+                           f"{root}/tests/module_stub/gbp_oracle_stub.c", "-o", str(stub), oracle.PORT_SO,
+                           f"-Wl,-rpath,{oracle.HERE}"])
+    subprocess.check_call(["make", "-s", "-B", "-C", f"{root}/shiokaze_gb300/module", f"OUT={tmp_path}",
+                           f"LDFLAGS=-shared -L{tmp_path} -lgbp -Wl,-rpath,{tmp_path}",
+                           f"{tmp_path}/libshiokaze_gbadvection3.so"], stdout=subprocess.DEVNULL)
+    shutil.copy(tmp_path / "libshiokaze_gbadvection3.so", os.path.join(oracle.REF_DIR,
+                                                                      "libshiokaze_gbadvection3stub.so"))
+    out = tmp_path / "module.npz"
+    r = subprocess.run([sys.executable, "-c", ADVECT_MODULE_RUN, str(out)], cwd=root, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    got = dict(np.load(out))
+    for seed, sc, kw in advect_module_cases():
+        want = oracle.ref_advect3(sc.u, sc.v, sc.w, sc.fluid, sc.fluid_mode, sc.band, sc.dx, sc.dt, **kw)
+        for name, a in zip("uvwq", want[:4]):
+            b = got[f"{seed}_{name}"]
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (seed, name)
