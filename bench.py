@@ -652,6 +652,10 @@ def run_gbp_advect(args):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / reps
     face_ms = timed(lambda: adv.advect_vector((u, v, w), (u, v, w), fluid, scene.dt, stream=sh))
+    # the solid constraint that follows the projection (macutility3::constrain_velocity)
+    solid = dev_t(scene.solid)
+    util = gb.MacUtility3(scene.nx, scene.ny, scene.nz, scene.dx, context=ctx)
+    constrain_ms = timed(lambda: util.constrain_velocity(solid, (u, v, w), stream=sh))
     cell_ms = timed(lambda: adv.advect_scalar(q, (u, v, w), fluid, scene.dt, stream=sh))
     faces = scene.u.size + scene.v.size + scene.w.size
     face_bytes_alg = (4 + 4 / 3 + 12 + 20) * faces
@@ -684,6 +688,7 @@ def run_gbp_advect(args):
                                  "cell_passes": {"ms": round(cell_ms, 5),
                                                  "GBps": round(cell_bytes_alg / (cell_ms * 1e-3) / 1e9, 1)}},
                      "step_GBps": round(nbytes / (ms_step * 1e-3) / 1e9, 1)},
+        "constrain_velocity_ms": round(constrain_ms, 4),
         "clocks": clocks,
         "gpu_launches": int(launches),
     }

@@ -274,6 +274,28 @@ int gbp_advect3_device(gbp_ctx *ctx, int nx, int ny, int nz, double dx, double d
 int gbp_advect3(gbp_ctx *ctx, int nx, int ny, int nz, double dx, double dt, const gbp_advect_params *params, float *u,
                 float *v, float *w, const float *fluid, float *q, const unsigned char *q_mask, float q_bg);
 
+/* Solid constraint of the velocity, the step after the projection in the
+ * liquid and smoke solvers (src/liquid/macliquid3.cpp:316,
+ * src/smoke/macsmoke3.cpp:294): replaces
+ *   macutility3_interface::constrain_velocity(solid, velocity)
+ *     include/shiokaze/utility/macutility3_interface.h
+ *   as implemented by src/utility/macutility3.cpp:61-86.
+ * If the nodal solid level set has a negative value, every active face
+ * inside the solid (interpolated solid < 0) loses the velocity's component
+ * into the solid (the saved velocity, interpolated at the face, minus its
+ * projection on the solid gradient, when that projection is negative), and
+ * faces on the domain walls keep no outflow. Results equal the reference's
+ * bit for bit. solid is nodal (nx+1)(ny+1)(nz+1); u, v, w in/out, holding
+ * the velocity's background (0) on inactive faces; mu, mv, mw mark the
+ * active faces (NULL: all). The reference tests for a negative solid value
+ * over the solid array's active values; this call over all values (the
+ * same answer for a narrow-band level set). */
+int gbp_constrain_velocity3_device(gbp_ctx *ctx, int nx, int ny, int nz, double dx, const float *solid, float *u,
+                                   float *v, float *w, const unsigned char *mu, const unsigned char *mv,
+                                   const unsigned char *mw, void *stream);
+int gbp_constrain_velocity3(gbp_ctx *ctx, int nx, int ny, int nz, double dx, const float *solid, float *u, float *v,
+                            float *w, const unsigned char *mu, const unsigned char *mv, const unsigned char *mw);
+
 /* Number of kernel launches this context has issued (graph nodes count one
  * each). */
 long long gbp_launch_count(gbp_ctx *ctx);

@@ -110,6 +110,9 @@ def _port_lib():
         lib.oracle_advect3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                        ctypes.c_int, ctypes.c_int, fp, fp, fp, fp, fp, ctypes.POINTER(ctypes.c_ubyte),
                                        ctypes.c_float]
+        u8 = ctypes.POINTER(ctypes.c_ubyte)
+        lib.oracle_constrain_velocity3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, fp, fp,
+                                                   fp, fp, u8, u8, u8]
         _port = lib
     return _port
 
@@ -192,6 +195,9 @@ def _ref_lib():
         lib.ref_advect3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_char_p, fp, fp, fp, fp, ctypes.c_int, ctypes.c_float, fp,
                                     ctypes.POINTER(ctypes.c_ubyte), ctypes.c_float, ctypes.c_char_p]
+        u8 = ctypes.POINTER(ctypes.c_ubyte)
+        lib.ref_constrain3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_char_p,
+                                       fp, ctypes.c_int, ctypes.c_float, fp, fp, fp, u8, u8, u8, ctypes.c_char_p]
         lib.ref_densify_compare.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, ctypes.c_int,
                                             ctypes.c_float, ctypes.c_int, fp, fp, dp, dp]
         _ref = lib
@@ -243,6 +249,39 @@ def advect3(u, v, w, fluid, dx, dt, q=None, q_mask=None, q_bg=0.0, maccormack=Tr
     if rc:
         raise ValueError("oracle_advect3: grid too small")
     return uo, vo, wo, qo, ms
+
+
+def _u8p(m):
+    return None if m is None else m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte))
+
+
+def constrain3(solid, u, v, w, dx, masks=(None, None, None), impl="port", solid_mode=0, band=0.0):
+    """macutility3::constrain_velocity (src/utility/macutility3.cpp:61-86)
+    on dense 3D arrays (z, y, x): solid nodal, u, v, w faces (holding the
+    velocity's background, 0, on inactive faces), updated where the
+    component's mask is nonzero (all faces for None). By the C restatement
+    ("port") or the reference's own macutility3 ("reference"; solid_mode /
+    band say how it builds its solid array). Returns new (u, v, w)."""
+    fp = ctypes.POINTER(ctypes.c_float)
+    nz, ny, nx = (d - 1 for d in solid.shape)
+    uo, vo, wo = (np.array(a, dtype=np.float32, order="C") for a in (u, v, w))
+    sl = np.ascontiguousarray(solid, dtype=np.float32)
+    ms = [None if m is None else np.ascontiguousarray(m, dtype=np.uint8) for m in masks]
+    if impl == "reference":
+        lib = _ref_lib()
+        log = tempfile.NamedTemporaryFile(prefix="ref_constrain_", suffix=".log", delete=False).name
+        try:
+            lib.ref_constrain3(nx, ny, nz, dx, b"", sl.ctypes.data_as(fp), solid_mode, band, uo.ctypes.data_as(fp),
+                               vo.ctypes.data_as(fp), wo.ctypes.data_as(fp), *[_u8p(m) for m in ms], log.encode())
+        finally:
+            os.unlink(log)
+    else:
+        rc = _port_lib().oracle_constrain_velocity3(nx, ny, nz, dx, sl.ctypes.data_as(fp), uo.ctypes.data_as(fp),
+                                                    vo.ctypes.data_as(fp), wo.ctypes.data_as(fp),
+                                                    *[_u8p(m) for m in ms])
+        if rc:
+            raise ValueError("oracle_constrain_velocity3: grid too small")
+    return uo, vo, wo
 
 
 def ref_advect3(u, v, w, fluid, fluid_mode, band, dx, dt, q=None, q_mask=None, q_bg=0.0, maccormack=True,

@@ -359,3 +359,115 @@ int oracle_advect3(int nx, int ny, int nz, double dx, double dt, int maccormack,
     advect_u(vel, nx, ny, nz, dx, dt, maccormack, trim, fluid);
     return 0;
 }
+
+/* ------------------------------------------------------------------------
+ * macutility3::constrain_velocity (src/utility/macutility3.cpp:61-86): the
+ * velocity's normal component into the solid removed at faces inside it,
+ * and outflow through the domain's walls set to 0. */
+
+/* array_derivative3::derivative (include/shiokaze/array/array_derivative3.h:
+ * 51-95, 107-116): the trilinear gradient in index space, every corner
+ * included, accumulated in float with double products */
+static void derivative(const float *a, shp3 s, const double p[3], float out[3]) {
+    const double x = smax(0.0, smin(s.w - 1., p[0]));
+    const double y = smax(0.0, smin(s.h - 1., p[1]));
+    const double z = smax(0.0, smin(s.d - 1., p[2]));
+    const int i = (int)smin(x, s.w - 2.);
+    const int j = (int)smin(y, s.h - 2.);
+    const int k = (int)smin(z, s.d - 2.);
+    double c[3][8];
+    c[0][0] = -(k + 1 - z) * (j + 1 - y);
+    c[0][1] = (k + 1 - z) * (j + 1 - y);
+    c[0][2] = -(k + 1 - z) * (y - j);
+    c[0][3] = (k + 1 - z) * (y - j);
+    c[0][4] = -(z - k) * (j + 1 - y);
+    c[0][5] = (z - k) * (j + 1 - y);
+    c[0][6] = -(z - k) * (y - j);
+    c[0][7] = (z - k) * (y - j);
+    c[1][0] = -(k + 1 - z) * (i + 1 - x);
+    c[1][1] = -(k + 1 - z) * (x - i);
+    c[1][2] = (k + 1 - z) * (i + 1 - x);
+    c[1][3] = (k + 1 - z) * (x - i);
+    c[1][4] = -(z - k) * (i + 1 - x);
+    c[1][5] = -(z - k) * (x - i);
+    c[1][6] = (z - k) * (i + 1 - x);
+    c[1][7] = (z - k) * (x - i);
+    c[2][0] = -(i + 1 - x) * (j + 1 - y);
+    c[2][1] = -(x - i) * (j + 1 - y);
+    c[2][2] = -(i + 1 - x) * (y - j);
+    c[2][3] = -(x - i) * (y - j);
+    c[2][4] = (i + 1 - x) * (j + 1 - y);
+    c[2][5] = (x - i) * (j + 1 - y);
+    c[2][6] = (i + 1 - x) * (y - j);
+    c[2][7] = (x - i) * (y - j);
+    for (int d = 0; d < 3; ++d) {
+        float r = 0.0f;
+        for (int n = 0; n < 8; ++n)
+            r = (float)((double)r + c[d][n] * (double)a[at(s, i + (n & 1), j + ((n >> 1) & 1), k + ((n >> 2) & 1))]);
+        out[d] = r;
+    }
+}
+
+/* u, v, w dense (operator() values: inactive faces hold the background),
+ * updated on the faces whose mask is nonzero (every face if a mask is NULL).
+ * solid is nodal (nx+1)(ny+1)(nz+1). The reference tests
+ * levelset_exist(solid) (array_utility3.h:112-122) over the array's active
+ * values; here over every value. It runs its face loop three times (the
+ * `for( int dim : DIMS3 )` around parallel_actives, :68); so does this. */
+int oracle_constrain_velocity3(int nx, int ny, int nz, double dx, const float *solid, float *u, float *v, float *w,
+                               const unsigned char *mu, const unsigned char *mv, const unsigned char *mw) {
+    if (nx < 2 || ny < 2 || nz < 2) return 1;
+    const shp3 ns = {nx + 1, ny + 1, nz + 1};
+    const long long nn = (long long)ns.w * ns.h * ns.d;
+    int exists = 0;
+    for (long long n = 0; n < nn && !exists; ++n) exists = solid[n] < 0.0;
+    if (!exists) return 0;
+    float *comp[3] = {u, v, w}, *save[3];
+    const unsigned char *mask[3] = {mu, mv, mw};
+    for (int d = 0; d < 3; ++d) {
+        const shp3 fs = face_shape(nx, ny, nz, d);
+        const long long nf = (long long)fs.w * fs.h * fs.d;
+        save[d] = (float *)malloc(sizeof(float) * nf);
+        memcpy(save[d], comp[d], sizeof(float) * nf);
+    }
+    const int shape[3] = {nx, ny, nz};
+    for (int rep = 0; rep < 3; ++rep)
+        for (int dim = 0; dim < 3; ++dim) {
+            const shp3 fs = face_shape(nx, ny, nz, dim);
+            for (int k = 0; k < fs.d; ++k)
+                for (int j = 0; j < fs.h; ++j)
+                    for (int i = 0; i < fs.w; ++i) {
+                        const long long f = at(fs, i, j, k);
+                        if (mask[dim] && !mask[dim][f]) continue;
+                        const int ip[3] = {i, j, k};
+                        double p[3];
+                        for (int c = 0; c < 3; ++c) p[c] = ip[c] + 0.5 * (dim != c);
+                        float val = comp[dim][f];
+                        if ((double)interp(solid, ns, p) < 0.0) {
+                            float dr[3];
+                            derivative(solid, ns, p, dr);
+                            double nrm[3];
+                            for (int c = 0; c < 3; ++c) nrm[c] = (double)dr[c] / dx;
+                            double n2 = 0.0;
+                            for (int c = 0; c < 3; ++c) n2 += nrm[c] * nrm[c];
+                            if (n2) {
+                                /* macarray_interpolator3::interpolate (macarray_interpolator3.h:49-56) */
+                                double uu[3];
+                                for (int c = 0; c < 3; ++c) {
+                                    double pos[3];
+                                    for (int e = 0; e < 3; ++e) pos[e] = p[e] - 0.5 * (c != e);
+                                    uu[c] = interp(save[c], face_shape(nx, ny, nz, c), pos);
+                                }
+                                double dot = 0.0;
+                                for (int c = 0; c < 3; ++c) dot += uu[c] * nrm[c];
+                                if (dot < 0.0) val = (float)(uu[dim] - nrm[dim] * dot);
+                            }
+                        }
+                        if (ip[dim] == 0 && val < 0.0) val = 0.0f;
+                        if (ip[dim] == shape[dim] && val > 0.0) val = 0.0f;
+                        comp[dim][f] = val;
+                    }
+        }
+    for (int d = 0; d < 3; ++d) free(save[d]);
+    return 0;
+}

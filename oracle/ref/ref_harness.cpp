@@ -29,6 +29,7 @@
 #include <shiokaze/core/configurable.h>
 #include <shiokaze/projection/macproject2_interface.h>
 #include <shiokaze/advection/macadvection3_interface.h>
+#include <shiokaze/utility/macutility3_interface.h>
 
 #include "gbarray_adapter.h"
 #include <shiokaze/projection/macproject3_interface.h>
@@ -419,6 +420,50 @@ int ref_advect_load(int nx, int ny, int nz, double dx, const char *kv, const cha
         adv.set_environment("shape", &s);
         adv.set_environment("dx", &dxv);
         adv.setup_now(config);
+    });
+    return 1;
+}
+
+/* The reference's macutility3::constrain_velocity
+ * (src/utility/macutility3.cpp:61-86), loaded by name, on dense 3D arrays:
+ * solid is the nodal level set (built as in ref_project from solid_mode /
+ * solid_band), u, v, w the face velocities (in/out), active where the
+ * component's mask is nonzero (every face if the mask is NULL; inactive
+ * faces read 0, the velocity's background). Outputs are read through
+ * operator(). Returns 1. */
+int ref_constrain3(int nx, int ny, int nz, double dx, const char *kv, const float *solid, int solid_mode,
+                   float solid_band, float *u, float *v, float *w, const unsigned char *mu, const unsigned char *mv,
+                   const unsigned char *mw, const char *log_path) {
+    configuration &config = install_global_config(kv);
+    shape3 s(nx, ny, nz);
+    double dxv = dx;
+    with_stdout_to(log_path, [&]() {
+        macutility3_driver util("macutility3");
+        util.set_environment("shape", &s);
+        util.set_environment("dx", &dxv);
+        util.setup_now(config);
+        array3<Real> solid_a;
+        fill_levelset3(solid_a, s.nodal(), solid, solid_mode, solid_band);
+        macarray3<Real> vel(s);
+        float *comp[3] = {u, v, w};
+        const unsigned char *mask[3] = {mu, mv, mw};
+        for (int d = 0; d < 3; ++d) {
+            const shape3 fs = s.face(d);
+            for (int k = 0; k < (int)fs.d; ++k)
+                for (int j = 0; j < (int)fs.h; ++j)
+                    for (int i = 0; i < (int)fs.w; ++i) {
+                        const size_t n = i + (size_t)fs.w * (j + (size_t)fs.h * k);
+                        if (!mask[d] || mask[d][n]) vel[d].set(i, j, k, comp[d][n]);
+                    }
+        }
+        util->constrain_velocity(solid_a, vel);
+        for (int d = 0; d < 3; ++d) {
+            const shape3 fs = s.face(d);
+            for (int k = 0; k < (int)fs.d; ++k)
+                for (int j = 0; j < (int)fs.h; ++j)
+                    for (int i = 0; i < (int)fs.w; ++i)
+                        comp[d][i + (size_t)fs.w * (j + (size_t)fs.h * k)] = vel[d](i, j, k);
+        }
     });
     return 1;
 }

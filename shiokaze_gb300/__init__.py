@@ -138,6 +138,10 @@ def load_library():
     lib.gbp_advect3_device.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_double, ctypes.POINTER(AdvectParams), vp, vp, vp, vp, vp, vp,
                                        ctypes.c_float, vp]
+    lib.gbp_constrain_velocity3.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, fp, fp, fp,
+                                            fp, u8p, u8p, u8p]
+    lib.gbp_constrain_velocity3_device.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, vp,
+                                                   vp, vp, vp, vp, vp, vp, vp]
     lib.gbp_launch_count.argtypes = [vp]
     lib.gbp_launch_count.restype = ctypes.c_longlong
     lib.gbp_strerror.argtypes = [ctypes.c_int]
@@ -508,6 +512,44 @@ class MacAdvection3:
                                   ptrs[1], ptrs[2], fptr, ptrs[3] if q is not None else None,
                                   None if m is None else m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), bg)
         check(rc)
+
+
+class MacUtility3:
+    """macutility3_interface::constrain_velocity on the GPU
+    (``src/utility/macutility3.cpp:61-86``): the velocity's component into
+    the solid removed at faces inside it, no outflow through the walls.
+    Results equal the reference's bit for bit. Arrays are dense (z, y, x)
+    float32, numpy (copied in and out) or torch CUDA tensors (in place);
+    ``masks`` are the three components' active faces (uint8, None: all),
+    inactive faces holding 0."""
+
+    def __init__(self, nx, ny, nz, dx, context: Context | None = None):
+        self.ctx = context or default_context()
+        self.lib = self.ctx.lib
+        self.nx, self.ny, self.nz, self.dx = nx, ny, nz, dx
+
+    def constrain_velocity(self, solid, velocity, masks=None, stream=None):
+        u, v, w = velocity
+        masks = masks or (None, None, None)
+        if _is_torch_cuda(u):
+            import torch
+            for t in (u, v, w, solid):
+                assert t.dtype == torch.float32 and t.is_contiguous(), "device arrays must be contiguous float32"
+            st = stream if stream is not None else torch.cuda.current_stream(u.device).cuda_stream
+            mp = [None if m is None else m.data_ptr() for m in masks]
+            check(self.lib.gbp_constrain_velocity3_device(self.ctx.handle, self.nx, self.ny, self.nz, self.dx,
+                                                          solid.data_ptr(), u.data_ptr(), v.data_ptr(), w.data_ptr(),
+                                                          *mp, ctypes.c_void_p(st)))
+            return
+        ptrs = []
+        for a in (u, v, w):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
+                raise TypeError("host arrays must be contiguous float32 numpy arrays (updated in place)")
+            ptrs.append(a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        sa, sp = _host_f32(solid)
+        ms = [None if m is None else np.ascontiguousarray(m, dtype=np.uint8) for m in masks]
+        mp = [None if m is None else m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)) for m in ms]
+        check(self.lib.gbp_constrain_velocity3(self.ctx.handle, self.nx, self.ny, self.nz, self.dx, sp, *ptrs, *mp))
 
 
 def projector_for(scene, context: Context | None = None, **config):

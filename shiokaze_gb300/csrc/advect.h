@@ -20,6 +20,7 @@ struct AdvectWork {
     gba::MinMax *vmm = nullptr;  // limiter record per face
     float *q0 = nullptr;   // forward scalar
     gba::MinMax *qmm = nullptr;  // limiter record per cell
+    int *flag = nullptr;         // the solid constraint's levelset_exist flag
 };
 
 cudaError_t advect_reserve(AdvectWork &w, long long faces, long long cells);
@@ -40,5 +41,17 @@ struct AdvectArgs {
 
 // Enqueues the step on `stream`; *launches counts kernel launches.
 cudaError_t advect_run(AdvectWork &w, const AdvectArgs &a, cudaStream_t stream, long long *launches);
+
+// The solid constraint of the velocity (macutility3::constrain_velocity,
+// src/utility/macutility3.cpp:61-86) on device arrays: solid nodal, u, v, w
+// in/out, masks of active faces (NULL: all). Enqueued on `stream`.
+struct ConstrainArgs {
+    int nx, ny, nz;
+    double dx;
+    const float *solid;
+    float *u, *v, *w;
+    const unsigned char *mu, *mv, *mw;
+};
+cudaError_t constrain_run(AdvectWork &w, const ConstrainArgs &a, cudaStream_t stream, long long *launches);
 
 }  // namespace gbp

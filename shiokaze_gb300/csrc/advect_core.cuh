@@ -132,15 +132,16 @@ GBA_HD void corner_minmax(const Shape &s, double px, double py, double pz, float
     hi = h;
 }
 
-// interp(s, p, a) > limit, the narrow-band test. The eight corners' range
-// [mn, mx] usually decides it: the weights are nonnegative and sum to 1
-// within 16 double ulps, and each of the eight float accumulations of
-// interp rounds by at most 2^-24 of a partial sum bounded by M = max|a|,
-// so the interpolant lies in [mn - d, mx + d] for d = 2^-20 M + 1e-38
-// (twice the bound, plus the subnormal spacing eight times over). When
-// the limit falls inside that band, or a value is not finite, the
-// interpolant itself is compared; either way the answer is the reference's.
-GBA_HD bool above_limit(const Shape &s, double px, double py, double pz, const float *a, double limit) {
+// How interp(s, p, a) compares with `limit`: -1 below, 1 above, 0 equal,
+// 2 unordered (NaN). The eight corners' range [mn, mx] usually decides it:
+// the weights are nonnegative and sum to 1 within 16 double ulps, and each
+// of the eight float accumulations of interp rounds by at most 2^-24 of a
+// partial sum bounded by M = max|a|, so the interpolant lies in
+// [mn - d, mx + d] for d = 2^-20 M + 1e-38 (twice the bound, plus the
+// subnormal spacing eight times over). When the limit falls inside that
+// band, or a value is not finite, the interpolant itself is compared;
+// either way the answer is the reference's.
+GBA_HD int compare_interp(const Shape &s, double px, double py, double pz, const float *a, double limit) {
     const Corner c = corner(s, px, py, pz);
     const long long base = at(s, c.i, c.j, c.k);
     const long long sy = s.w, sz = (long long)s.w * s.h;
@@ -158,8 +159,8 @@ GBA_HD bool above_limit(const Shape &s, double px, double py, double pz, const f
     if (sum - sum == 0.0f) {  // every value finite (a NaN or an infinity makes this false)
         const float am = (-mn < mx) ? mx : -mn;
         const double d = (double)am * 9.5367431640625e-07 + 1e-38;
-        if ((double)mx + d <= limit) return false;
-        if ((double)mn - d > limit) return true;
+        if ((double)mx + d < limit) return -1;
+        if ((double)mn - d > limit) return 1;
     }
     // the interpolant, as interp forms it (same corner, weights and order)
     const double ax0 = c.i + 1 - c.x, ax1 = c.x - c.i;
@@ -172,7 +173,13 @@ GBA_HD bool above_limit(const Shape &s, double px, double py, double pz, const f
 #pragma unroll
     for (int n = 0; n < 8; ++n)
         if (coef[n]) value = (float)((double)value + (double)v[n] * coef[n]);
-    return (double)value > limit;
+    const double x = value;
+    return x < limit ? -1 : (x > limit ? 1 : (x == limit ? 0 : 2));
+}
+
+// interp(s, p, a) > limit, the narrow-band test
+GBA_HD bool above_limit(const Shape &s, double px, double py, double pz, const float *a, double limit) {
+    return compare_interp(s, px, py, pz, a, limit) == 1;
 }
 
 // the full velocity at face (i,j,k) of component `dim` (macarray3.h:350-371):
@@ -427,6 +434,102 @@ GBA_HD void cell_backward(const StepArgs &a, unsigned c) {
         bwd = q0[c];
     }
     a.q[c] = maccormack(a.qmm[c], a.q[c], q0[c], bwd);
+}
+
+// ---------------------------------------------------------------------------
+// The solid constraint of the velocity, macutility3::constrain_velocity
+// (src/utility/macutility3.cpp:61-86), per face.
+
+// array_derivative3::derivative (include/shiokaze/array/array_derivative3.h:
+// 51-95, 107-116): the trilinear gradient in index space, every corner
+// included, accumulated in float with double products
+GBA_HD void derivative(const Shape &s, const double p[3], const float *a, float out[3]) {
+    const Corner c = corner(s, p[0], p[1], p[2]);
+    const int i = c.i, j = c.j, k = c.k;
+    const double x = c.x, y = c.y, z = c.z;
+    const double cf[3][8] = {
+        {-(k + 1 - z) * (j + 1 - y), (k + 1 - z) * (j + 1 - y), -(k + 1 - z) * (y - j), (k + 1 - z) * (y - j),
+         -(z - k) * (j + 1 - y), (z - k) * (j + 1 - y), -(z - k) * (y - j), (z - k) * (y - j)},
+        {-(k + 1 - z) * (i + 1 - x), -(k + 1 - z) * (x - i), (k + 1 - z) * (i + 1 - x), (k + 1 - z) * (x - i),
+         -(z - k) * (i + 1 - x), -(z - k) * (x - i), (z - k) * (i + 1 - x), (z - k) * (x - i)},
+        {-(i + 1 - x) * (j + 1 - y), -(x - i) * (j + 1 - y), -(i + 1 - x) * (y - j), -(x - i) * (y - j),
+         (i + 1 - x) * (j + 1 - y), (x - i) * (j + 1 - y), (i + 1 - x) * (y - j), (x - i) * (y - j)}};
+    const long long base = at(s, i, j, k);
+    const long long sy = s.w, sz = (long long)s.w * s.h;
+    const long long off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
+    float v[8];
+#pragma unroll
+    for (int n = 0; n < 8; ++n) v[n] = a[base + off[n]];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float r = 0.0f;
+#pragma unroll
+        for (int n = 0; n < 8; ++n) r = (float)((double)r + cf[d][n] * (double)v[n]);
+        out[d] = r;
+    }
+}
+
+struct ConstrainArgs {
+    Dims g;
+    const float *solid;     // nodal level set (nx+1)(ny+1)(nz+1)
+    const float *save;      // the input velocity, three components back to back at 0, off1, off2
+    long long off1, off2;
+    float *u, *v, *w;       // velocity, written where a face changes
+    const unsigned char *mu, *mv, *mw;  // active faces (NULL: all)
+    const int *exists;      // the solid has a negative value (levelset_exist)
+};
+
+// One face. The reference runs its face loop three times over the same
+// saved velocity (macutility3.cpp:68); the loop is idempotent (the solid
+// branch sets the same value from the saved velocity each time, and the
+// wall clamps are idempotent), so one pass gives its result.
+GBA_HD void constrain_face(const ConstrainArgs &a, int dim, unsigned f) {
+    const Dims &g = a.g;
+    const Shape fs = face_shape(g, dim);
+    if (f >= count(fs) || !*a.exists) return;
+    const unsigned char *mask = dim == 0 ? a.mu : (dim == 1 ? a.mv : a.mw);
+    if (mask && !mask[f]) return;
+    const Idx x = decode(fs, f);
+    const int ip[3] = {x.i, x.j, x.k};
+    const float *save[3] = {a.save, a.save + a.off1, a.save + a.off2};
+    const double p[3] = {ip[0] + 0.5 * (dim != 0), ip[1] + 0.5 * (dim != 1), ip[2] + 0.5 * (dim != 2)};
+    const float in = (dim == 0 ? save[0] : (dim == 1 ? save[1] : save[2]))[f];
+    float val = in;
+    const Shape ns{g.nx + 1, g.ny + 1, g.nz + 1};
+    if (compare_interp(ns, p[0], p[1], p[2], a.solid, 0.0) == -1) {
+        float dr[3];
+        derivative(ns, p, a.solid, dr);
+        double nrm[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) nrm[c] = (double)dr[c] / g.dx;
+        double n2 = 0.0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) n2 += nrm[c] * nrm[c];
+        if (n2 != 0.0) {
+            // macarray_interpolator3::interpolate (macarray_interpolator3.h:49-56)
+            double uu[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float *sc = save[c];
+                uu[c] = interp(face_shape(g, c), p[0] - 0.5 * (c != 0), p[1] - 0.5 * (c != 1), p[2] - 0.5 * (c != 2),
+                               [sc](long long n) { return sc[n]; });
+            }
+            double dot = 0.0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) dot += uu[c] * nrm[c];
+            if (dot < 0.0) val = (float)((dim == 0 ? uu[0] : (dim == 1 ? uu[1] : uu[2])) -
+                                         (dim == 0 ? nrm[0] : (dim == 1 ? nrm[1] : nrm[2])) * dot);
+        }
+    }
+    const int n_dim = dim == 0 ? g.nx : (dim == 1 ? g.ny : g.nz);
+    if (ip[dim] == 0 && val < 0.0f) val = 0.0f;
+    if (ip[dim] == n_dim && val > 0.0f) val = 0.0f;
+    float *io = dim == 0 ? a.u : (dim == 1 ? a.v : a.w);
+    union {
+        float f;
+        unsigned u;
+    } b0{in}, b1{val};
+    if (b0.u != b1.u) io[f] = val;
 }
 
 }  // namespace gba

@@ -54,19 +54,34 @@ __global__ void __launch_bounds__(ADV_THREADS) adv_cell_backward(StepArgs a) {
     gba::cell_backward(a, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-Dims make_dims(const AdvectArgs &a) {
+// levelset_exist (include/shiokaze/array/array_utility3.h:112-122): any
+// negative value of the solid sets the flag
+__global__ void __launch_bounds__(ADV_THREADS) cst_any_negative(const float *__restrict__ solid, long long n,
+                                                               int *flag) {
+    bool neg = false;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        neg |= solid[i] < 0.0f;
+    if (__syncthreads_or(neg) && threadIdx.x == 0) *flag = 1;
+}
+
+// one thread per face, blockIdx.y = component
+__global__ void __launch_bounds__(ADV_THREADS) cst_face(gba::ConstrainArgs a) {
+    gba::constrain_face(a, (int)blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+Dims make_dims(int nx, int ny, int nz, double dx, int trim_narrowband) {
     Dims g{};
-    g.nx = a.nx;
-    g.ny = a.ny;
-    g.nz = a.nz;
-    g.dx = a.dx;
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = nz;
+    g.dx = dx;
     int e = 0;
-    const double m = std::frexp(a.dx, &e);
-    const double inv = 1.0 / a.dx;
+    const double m = std::frexp(dx, &e);
+    const double inv = 1.0 / dx;
     g.pow2 = (m == 0.5 && std::isfinite(inv) && (double)(float)inv == inv) ? 1 : 0;
     g.inv_dx = inv;
     g.inv_dx_f = (float)inv;
-    g.limit = -a.dx * (double)a.trim_narrowband;
+    g.limit = -dx * (double)trim_narrowband;
     return g;
 }
 
@@ -101,6 +116,7 @@ cudaError_t advect_reserve(AdvectWork &w, long long faces, long long cells) {
 }
 
 void advect_release(AdvectWork &w) {
+    cudaFree(w.flag);
     cudaFree(w.v0);
     cudaFree(w.vmm);
     cudaFree(w.q0);
@@ -117,7 +133,7 @@ cudaError_t advect_run(AdvectWork &w, const AdvectArgs &a, cudaStream_t st, long
     cudaError_t e = advect_reserve(w, a.velocity ? nf0 + nf1 + nf2 : 0, a.q ? cells : 0);
     if (e != cudaSuccess) return e;
     StepArgs s{};
-    s.g = make_dims(a);
+    s.g = make_dims(a.nx, a.ny, a.nz, a.dx, a.trim_narrowband);
     s.dt = a.dt;
     s.u = a.u;
     s.v = a.v;
@@ -160,6 +176,45 @@ cudaError_t advect_run(AdvectWork &w, const AdvectArgs &a, cudaStream_t st, long
             if (e != cudaSuccess) return e;
         }
     }
+    return cudaGetLastError();
+}
+
+cudaError_t constrain_run(AdvectWork &w, const ConstrainArgs &a, cudaStream_t st, long long *launches) {
+    const long long nf0 = (long long)(a.nx + 1) * a.ny * a.nz, nf1 = (long long)a.nx * (a.ny + 1) * a.nz,
+                    nf2 = (long long)a.nx * a.ny * (a.nz + 1);
+    long long nfmax = nf0 > nf1 ? nf0 : nf1;
+    if (nf2 > nfmax) nfmax = nf2;
+    cudaError_t e = advect_reserve(w, nf0 + nf1 + nf2, 0);
+    if (e == cudaSuccess && !w.flag) e = cudaMalloc(&w.flag, sizeof(int));
+    if (e != cudaSuccess) return e;
+    // the saved velocity the constraint interpolates (macutility3.cpp:63-64)
+    float *src[3] = {a.u, a.v, a.w};
+    const long long n[3] = {nf0, nf1, nf2}, o[3] = {0, nf0, nf0 + nf1};
+    for (int d = 0; d < 3; ++d) {
+        e = cudaMemcpyAsync(w.v0 + o[d], src[d], sizeof(float) * (size_t)n[d], cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return e;
+    }
+    e = cudaMemsetAsync(w.flag, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    const long long nodes = (long long)(a.nx + 1) * (a.ny + 1) * (a.nz + 1);
+    long long nb = (nodes + ADV_THREADS - 1) / ADV_THREADS;
+    if (nb > 4096) nb = 4096;
+    cst_any_negative<<<(unsigned)nb, ADV_THREADS, 0, st>>>(a.solid, nodes, w.flag);
+    gba::ConstrainArgs c{};
+    c.g = make_dims(a.nx, a.ny, a.nz, a.dx, 0);
+    c.solid = a.solid;
+    c.save = w.v0;
+    c.off1 = nf0;
+    c.off2 = nf0 + nf1;
+    c.u = a.u;
+    c.v = a.v;
+    c.w = a.w;
+    c.mu = a.mu;
+    c.mv = a.mv;
+    c.mw = a.mw;
+    c.exists = w.flag;
+    cst_face<<<dim3(blocks_for(nfmax), 3), ADV_THREADS, 0, st>>>(c);
+    *launches += 2;
     return cudaGetLastError();
 }
 

@@ -753,3 +753,108 @@ int gbp_advect3(gbp_ctx *c, int nx, int ny, int nz, double dx, double dt, const 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Solid constraint of the velocity (macutility3::constrain_velocity,
+// src/utility/macutility3.cpp:61-86)
+
+namespace {
+
+int constrain_check(const char *who, gbp_ctx *c, int nx, int ny, int nz, double dx, const float *solid,
+                    const float *u, const float *v, const float *w) {
+    if (!c) return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": NULL context");
+    if (nx < 2 || ny < 2 || nz < 2)
+        return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": every grid edge must be at least 2 cells");
+    if ((long long)(nx + 1) * (ny + 1) * (nz + 1) >= (1LL << 31))
+        return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": 2^31 nodes or more");
+    if (!(dx > 0.0) || !std::isfinite(dx))
+        return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": dx must be positive and finite");
+    if (!solid || !u || !v || !w) return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": NULL array");
+    return GBP_OK;
+}
+
+ConstrainArgs constrain_args(int nx, int ny, int nz, double dx, const float *solid, float *u, float *v, float *w,
+                             const unsigned char *mu, const unsigned char *mv, const unsigned char *mw) {
+    ConstrainArgs a{};
+    a.nx = nx;
+    a.ny = ny;
+    a.nz = nz;
+    a.dx = dx;
+    a.solid = solid;
+    a.u = u;
+    a.v = v;
+    a.w = w;
+    a.mu = mu;
+    a.mv = mv;
+    a.mw = mw;
+    return a;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbp_constrain_velocity3_device(gbp_ctx *c, int nx, int ny, int nz, double dx, const float *solid, float *u,
+                                   float *v, float *w, const unsigned char *mu, const unsigned char *mv,
+                                   const unsigned char *mw, void *stream) {
+    int rc = constrain_check("gbp_constrain_velocity3_device", c, nx, ny, nz, dx, solid, u, v, w);
+    if (rc) return rc;
+    GBP_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    if (!stream) {
+        GBP_CUDA(cudaEventRecord(c->ev[0], cudaStreamLegacy));
+        GBP_CUDA(cudaStreamWaitEvent(st, c->ev[0], 0));
+    }
+    long long launched = 0;
+    GBP_CUDA(constrain_run(c->adv, constrain_args(nx, ny, nz, dx, solid, u, v, w, mu, mv, mw), st, &launched));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    c->launches += launched;
+    return GBP_OK;
+}
+
+int gbp_constrain_velocity3(gbp_ctx *c, int nx, int ny, int nz, double dx, const float *solid, float *u, float *v,
+                            float *w, const unsigned char *mu, const unsigned char *mv, const unsigned char *mw) {
+    int rc = constrain_check("gbp_constrain_velocity3", c, nx, ny, nz, dx, solid, u, v, w);
+    if (rc) return rc;
+    GBP_CUDA(cudaSetDevice(c->device));
+    const size_t nodes = (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+    const size_t nf[3] = {(size_t)(nx + 1) * ny * nz, (size_t)nx * (ny + 1) * nz, (size_t)nx * ny * (nz + 1)};
+    const unsigned char *masks[3] = {mu, mv, mw};
+    size_t mask_floats = 0;
+    for (int d = 0; d < 3; ++d)
+        if (masks[d]) mask_floats += (nf[d] + 3) / 4;
+    const long long need = (long long)(nodes + nf[0] + nf[1] + nf[2] + mask_floats);
+    if (need > c->adv_stage_floats) {
+        if (c->adv_stage) cudaFree(c->adv_stage);
+        c->adv_stage = nullptr;
+        c->adv_stage_floats = 0;
+        GBP_CUDA(cudaMalloc(&c->adv_stage, sizeof(float) * (size_t)need));
+        c->adv_stage_floats = need;
+    }
+    cudaStream_t st = c->stream;
+    float *ds = c->adv_stage, *dc[3];
+    dc[0] = ds + nodes;
+    dc[1] = dc[0] + nf[0];
+    dc[2] = dc[1] + nf[1];
+    float *next = dc[2] + nf[2];
+    const unsigned char *dm[3] = {nullptr, nullptr, nullptr};
+    float *hc[3] = {u, v, w};
+    GBP_CUDA(cudaMemcpyAsync(ds, solid, 4 * nodes, cudaMemcpyHostToDevice, st));
+    for (int d = 0; d < 3; ++d) {
+        GBP_CUDA(cudaMemcpyAsync(dc[d], hc[d], 4 * nf[d], cudaMemcpyHostToDevice, st));
+        if (masks[d]) {
+            GBP_CUDA(cudaMemcpyAsync(next, masks[d], nf[d], cudaMemcpyHostToDevice, st));
+            dm[d] = (const unsigned char *)next;
+            next += (nf[d] + 3) / 4;
+        }
+    }
+    long long launched = 0;
+    GBP_CUDA(constrain_run(c->adv, constrain_args(nx, ny, nz, dx, ds, dc[0], dc[1], dc[2], dm[0], dm[1], dm[2]), st,
+                           &launched));
+    for (int d = 0; d < 3; ++d) GBP_CUDA(cudaMemcpyAsync(hc[d], dc[d], 4 * nf[d], cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    c->launches += launched;
+    return GBP_OK;
+}
+
+}  // extern "C"
