@@ -255,13 +255,14 @@ def _u8p(m):
     return None if m is None else m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte))
 
 
-def constrain3(solid, u, v, w, dx, masks=(None, None, None), impl="port", solid_mode=0, band=0.0):
+def constrain3(solid, u, v, w, dx, masks=(None, None, None), impl="port", solid_mode=0, band=0.0, extra_kv=""):
     """macutility3::constrain_velocity (src/utility/macutility3.cpp:61-86)
     on dense 3D arrays (z, y, x): solid nodal, u, v, w faces (holding the
     velocity's background, 0, on inactive faces), updated where the
     component's mask is nonzero (all faces for None). By the C restatement
     ("port") or the reference's own macutility3 ("reference"; solid_mode /
-    band say how it builds its solid array). Returns new (u, v, w)."""
+    band say how it builds its solid array; extra_kv adds configuration,
+    MacUtility=<module> loads another module). Returns new (u, v, w)."""
     fp = ctypes.POINTER(ctypes.c_float)
     nz, ny, nx = (d - 1 for d in solid.shape)
     uo, vo, wo = (np.array(a, dtype=np.float32, order="C") for a in (u, v, w))
@@ -271,7 +272,7 @@ def constrain3(solid, u, v, w, dx, masks=(None, None, None), impl="port", solid_
         lib = _ref_lib()
         log = tempfile.NamedTemporaryFile(prefix="ref_constrain_", suffix=".log", delete=False).name
         try:
-            lib.ref_constrain3(nx, ny, nz, dx, b"", sl.ctypes.data_as(fp), solid_mode, band, uo.ctypes.data_as(fp),
+            lib.ref_constrain3(nx, ny, nz, dx, extra_kv.encode(), sl.ctypes.data_as(fp), solid_mode, band, uo.ctypes.data_as(fp),
                                vo.ctypes.data_as(fp), wo.ctypes.data_as(fp), *[_u8p(m) for m in ms], log.encode())
         finally:
             os.unlink(log)

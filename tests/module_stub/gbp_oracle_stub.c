@@ -1,10 +1,12 @@
 /*
  * gbp_oracle_stub.c -- TEST INFRASTRUCTURE: a stand-in for libgbp's
  * advection entry points that runs the oracle (oracle/advect_oracle.c, in
- * liboracle.so) on the CPU. tests/test_oracle.py links the gbadvection3
- * plugin module against it to check the module's boundary (dense copies of
- * the reference's tiled arrays, the active mask, the write-back over active
- * faces and cells) against the reference's own macadvection3 without a GPU.
+ * liboracle.so) on the CPU, and the same for the solid constraint of the
+ * velocity. tests/test_oracle.py links the gbadvection3 and gbutility3
+ * plugin modules against it to check the modules' boundary (dense copies
+ * of the reference's tiled arrays, the active masks, the write-back over
+ * active faces and cells) against the reference's own macadvection3 and
+ * macutility3 without a GPU.
  * The shipped module links the real libgbp.so.
  */
 #include <stdlib.h>
@@ -12,6 +14,8 @@
 
 #include "gbp.h"
 
+int oracle_constrain_velocity3(int nx, int ny, int nz, double dx, const float *solid, float *u, float *v, float *w,
+                               const unsigned char *mu, const unsigned char *mv, const unsigned char *mw);
 int oracle_advect3(int nx, int ny, int nz, double dx, double dt, int maccormack, int trim, float *u, float *v,
                    float *w, const float *fluid, float *q, const unsigned char *q_mask, float q_bg);
 
@@ -52,4 +56,10 @@ int gbp_advect3(gbp_ctx *ctx, int nx, int ny, int nz, double dx, double dt, cons
                             q_bg);
     for (int d = 0; d < 3; ++d) free(c[d]);
     return rc;
+}
+
+int gbp_constrain_velocity3(gbp_ctx *ctx, int nx, int ny, int nz, double dx, const float *solid, float *u, float *v,
+                            float *w, const unsigned char *mu, const unsigned char *mv, const unsigned char *mw) {
+    (void)ctx;
+    return oracle_constrain_velocity3(nx, ny, nz, dx, solid, u, v, w, mu, mv, mw);
 }

@@ -5,6 +5,8 @@ built from its sources (tests/golden/make_golden.py). The restatement must
 reproduce them bit for bit: pressure, projected velocity, the set of unknown
 cells and the CG iteration count.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -218,3 +220,63 @@ def test_advection_module_boundary_matches_reference_module(tmp_path):
         for name, a in zip("uvwq", want[:4]):
             b = got[f"{seed}_{name}"]
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (seed, name)
+
+
+def _stub_module(tmp_path, module, installed_as):
+    """Builds plugin module `module` linked against the oracle-backed
+    stand-in for libgbp (tests/module_stub) and installs it beside the
+    reference's modules as libshiokaze_<installed_as>.so."""
+    import shutil
+    import subprocess
+    root = oracle.HERE.rsplit("/", 1)[0]
+    oracle.build_port()
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-I", f"{root}/include",
+                           f"{root}/tests/module_stub/gbp_oracle_stub.c", "-o", str(tmp_path / "libgbp.so"),
+                           oracle.PORT_SO, f"-Wl,-rpath,{oracle.HERE}"])
+    subprocess.check_call(["make", "-s", "-B", "-C", f"{root}/shiokaze_gb300/module", f"OUT={tmp_path}",
+                           f"LDFLAGS=-shared -L{tmp_path} -lgbp -Wl,-rpath,{tmp_path}",
+                           f"{tmp_path}/libshiokaze_{module}.so"], stdout=subprocess.DEVNULL)
+    shutil.copy(tmp_path / f"libshiokaze_{module}.so", os.path.join(oracle.REF_DIR, f"libshiokaze_{installed_as}.so"))
+    return root
+
+
+UTILITY_MODULE_RUN = r"""
+import glob, os, sys
+import numpy as np
+import oracle
+out = {}
+for p in sorted(glob.glob("tests/golden/constrain/*.npz")):
+    d = dict(np.load(p))
+    name = os.path.basename(p)[:-4]
+    r = oracle.constrain3(d["solid"], d["u"], d["v"], d["w"], float(d["dx"]), masks=(d["mu"], d["mv"], d["mw"]),
+                          impl="reference", solid_mode=int(d["solid_mode"]), band=float(d["band"]),
+                          extra_kv="MacUtility=gbutility3stub")
+    for c, a in zip("uvw", r):
+        out[f"{name}_{c}"] = a
+np.savez(sys.argv[1], **out)
+"""
+
+
+def test_utility_module_constrain_matches_reference_module(tmp_path):
+    """The gbutility3 module (MacUtility=gbutility3) on the CPU: linked to
+    the oracle-backed stand-in for libgbp and loaded by the reference's
+    loader in place of macutility3, its constrain_velocity gives the
+    reference module's results bit for bit on the reference's own arrays
+    (the constraint fixtures: narrow-band solids, masked velocities)."""
+    import subprocess
+    import sys
+    if not oracle.reference_available():
+        pytest.skip("reference oracle not built here")
+    root = _stub_module(tmp_path, "gbutility3", "gbutility3stub")
+    out = tmp_path / "utility.npz"
+    r = subprocess.run([sys.executable, "-c", UTILITY_MODULE_RUN, str(out)], cwd=root, capture_output=True, text=True,
+                       timeout=300, env=dict(os.environ, PYTHONPATH=root))
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    got = dict(np.load(out))
+    import glob
+    names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(root, "tests/golden/constrain/*.npz")))
+    assert len(names) >= 5
+    for name in names:
+        d = dict(np.load(os.path.join(root, "tests/golden/constrain", name + ".npz")))
+        for c in "uvw":
+            assert np.array_equal(got[f"{name}_{c}"].view(np.uint32), d[f"out_{c}"].view(np.uint32)), (name, c)
