@@ -111,6 +111,8 @@ def _port_lib():
                                        ctypes.c_int, ctypes.c_int, fp, fp, fp, fp, fp, ctypes.POINTER(ctypes.c_ubyte),
                                        ctypes.c_float]
         u8 = ctypes.POINTER(ctypes.c_ubyte)
+        lib.oracle_extrapolate3.restype = ctypes.c_longlong
+        lib.oracle_extrapolate3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, u8, ctypes.c_int]
         lib.oracle_constrain_velocity3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, fp, fp,
                                                    fp, fp, u8, u8, u8]
         _port = lib
@@ -196,6 +198,8 @@ def _ref_lib():
                                     ctypes.c_char_p, fp, fp, fp, fp, ctypes.c_int, ctypes.c_float, fp,
                                     ctypes.POINTER(ctypes.c_ubyte), ctypes.c_float, ctypes.c_char_p]
         u8 = ctypes.POINTER(ctypes.c_ubyte)
+        lib.ref_extrapolate3.restype = ctypes.c_longlong
+        lib.ref_extrapolate3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, u8, ctypes.c_int]
         lib.ref_constrain3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_char_p,
                                        fp, ctypes.c_int, ctypes.c_float, fp, fp, fp, u8, u8, u8, ctypes.c_char_p]
         lib.ref_densify_compare.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, ctypes.c_int,
@@ -283,6 +287,24 @@ def constrain3(solid, u, v, w, dx, masks=(None, None, None), impl="port", solid_
         if rc:
             raise ValueError("oracle_constrain_velocity3: grid too small")
     return uo, vo, wo
+
+
+def extrapolate3(values, active, count=1, impl="port"):
+    """array_extrapolator3::extrapolate (include/shiokaze/array/
+    array_extrapolator3.h:36-73) on a dense 3D array (z, y, x) with an
+    active mask: `count` rounds of activating every inactive neighbour of an
+    active cell with the float mean of its active neighbours. By the C
+    restatement ("port") or the reference's own code ("reference"). Returns
+    (values as read back, 0 on inactive cells; active; cells activated)."""
+    d, h, w = values.shape
+    a = np.array(values, dtype=np.float32, order="C")
+    m = np.array(active, dtype=np.uint8, order="C")
+    lib = _ref_lib() if impl == "reference" else _port_lib()
+    fn = lib.ref_extrapolate3 if impl == "reference" else lib.oracle_extrapolate3
+    added = fn(w, h, d, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)),
+               int(count))
+    a = np.where(m != 0, a, np.float32(0)).astype(np.float32)  # inactive cells read the background, 0
+    return a, m, int(added)
 
 
 def ref_advect3(u, v, w, fluid, fluid_mode, band, dx, dt, q=None, q_mask=None, q_bg=0.0, maccormack=True,

@@ -471,3 +471,55 @@ int oracle_constrain_velocity3(int nx, int ny, int nz, double dx, const float *s
     for (int d = 0; d < 3; ++d) free(save[d]);
     return 0;
 }
+
+/* ------------------------------------------------------------------------
+ * array_extrapolator3::extrapolate (include/shiokaze/array/
+ * array_extrapolator3.h:36-73) on one dense array with an active mask, as
+ * array3::dilate runs it (array3.h:1661-1668, src/array/dilate3.h:43-95):
+ * `count` times, every inactive in-bounds 6-neighbour of an active cell
+ * becomes active with the float mean of its active neighbours (summed in
+ * the order +x, -x, +y, -y, -z, +z), all values of one round computed from
+ * the state before it. Returns the number of cells activated. */
+long long oracle_extrapolate3(int w, int h, int d, float *a, unsigned char *active, int count) {
+    const shp3 s = {w, h, d};
+    const long long n = (long long)w * h * d;
+    unsigned char *cand = (unsigned char *)malloc((size_t)n);
+    float *val = (float *)malloc(sizeof(float) * (size_t)n);
+    static const int q[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, -1}, {0, 0, 1}};
+    long long total = 0;
+    for (int it = 0; it < count; ++it) {
+        memset(cand, 0, (size_t)n);
+        for (int k = 0; k < d; ++k)
+            for (int j = 0; j < h; ++j)
+                for (int i = 0; i < w; ++i) {
+                    const long long c = at(s, i, j, k);
+                    if (active[c]) continue;
+                    float sum = 0.0f;
+                    int weight = 0;
+                    for (int m = 0; m < 6; ++m) {
+                        const int qi = i + q[m][0], qj = j + q[m][1], qk = k + q[m][2];
+                        if (qi < 0 || qj < 0 || qk < 0 || qi >= w || qj >= h || qk >= d) continue;
+                        const long long e = at(s, qi, qj, qk);
+                        if (active[e]) {
+                            sum += a[e];
+                            ++weight;
+                        }
+                    }
+                    if (weight) {
+                        cand[c] = 1;
+                        val[c] = sum / weight;
+                    }
+                }
+        long long added = 0;
+        for (long long c = 0; c < n; ++c)
+            if (cand[c]) {
+                active[c] = 1;
+                a[c] = val[c];
+                ++added;
+            }
+        total += added;
+    }
+    free(cand);
+    free(val);
+    return total;
+}

@@ -30,6 +30,7 @@
 #include <shiokaze/projection/macproject2_interface.h>
 #include <shiokaze/advection/macadvection3_interface.h>
 #include <shiokaze/utility/macutility3_interface.h>
+#include <shiokaze/array/array_extrapolator3.h>
 
 #include "gbarray_adapter.h"
 #include <shiokaze/projection/macproject3_interface.h>
@@ -466,6 +467,35 @@ int ref_constrain3(int nx, int ny, int nz, double dx, const char *kv, const floa
         }
     });
     return 1;
+}
+
+/* The reference's array_extrapolator3::extrapolate on a dense 3D array of
+ * shape w x h x d: active where active[c] != 0 (values elsewhere ignored;
+ * the array's background is 0), `count` rounds. On return, a holds the
+ * values read through operator() and active the active set. Returns the
+ * number of cells the reference reports as extrapolated. */
+long long ref_extrapolate3(int w, int h, int d, float *a, unsigned char *active, int count) {
+    install_global_config("");
+    long long added = 0;
+    with_stdout_to("/dev/null", [&]() {
+        shape3 s(w, h, d);
+        array3<Real> arr(s, 0.0);
+        for (int k = 0; k < d; ++k)
+            for (int j = 0; j < h; ++j)
+                for (int i = 0; i < w; ++i) {
+                    const size_t n = i + (size_t)w * (j + (size_t)h * k);
+                    if (active[n]) arr.set(i, j, k, a[n]);
+                }
+        added = (long long)array_extrapolator3::extrapolate<Real>(arr, count);
+        for (int k = 0; k < d; ++k)
+            for (int j = 0; j < h; ++j)
+                for (int i = 0; i < w; ++i) {
+                    const size_t n = i + (size_t)w * (j + (size_t)h * k);
+                    a[n] = arr(i, j, k);
+                    active[n] = arr.active(i, j, k) ? 1 : 0;
+                }
+    });
+    return added;
 }
 
 }  // extern "C"
