@@ -536,6 +536,12 @@ class MacUtility3:
             for t in (u, v, w, solid):
                 assert t.dtype == torch.float32 and t.is_contiguous(), "device arrays must be contiguous float32"
             st = stream if stream is not None else torch.cuda.current_stream(u.device).cuda_stream
+            # masks may be numpy (copied to the device here) or uint8 CUDA tensors
+            masks = [None if m is None else (m if _is_torch_cuda(m) else torch.from_numpy(
+                np.ascontiguousarray(m, dtype=np.uint8)).to(u.device)) for m in masks]
+            for m in masks:
+                if m is not None:
+                    assert m.dtype == torch.uint8 and m.is_contiguous(), "masks must be contiguous uint8"
             mp = [None if m is None else m.data_ptr() for m in masks]
             check(self.lib.gbp_constrain_velocity3_device(self.ctx.handle, self.nx, self.ny, self.nz, self.dx,
                                                           solid.data_ptr(), u.data_ptr(), v.data_ptr(), w.data_ptr(),
