@@ -162,6 +162,22 @@ int gbp_scene_set_target_volume(gbp_scene *scene, double current_volume, double 
 int gbp_project(gbp_scene *scene, double dt, const float *solid, const float *fluid, float *u, float *v, float *w,
                 const gbp_params *params, float *pressure, gbp_stats *stats);
 
+/* gbp_project plus the active sets the reference leaves on its sparse
+ * arrays, for callers that keep them (the Shiokaze plugin modules):
+ *   unknown   nx*ny*nz: 1 on the cells whose pressure the reference sets --
+ *             every unknown, a pressure of 0 included
+ *             (macpressuresolver3.cpp:245-248) -- 0 elsewhere;
+ *   u_active, v_active, w_active  per face: 1 on the faces the reference's
+ *             velocity update keeps active (open faces, and closed faces on
+ *             the domain boundary next to a fluid cell; in 2D only where the
+ *             velocity before the update points out of the domain), 0 on the
+ *             faces it deactivates with set_off (macpressuresolver3.cpp:
+ *             252-267; macpressuresolver2.cpp:221-236). Those read 0.
+ * Host arrays; w_active is ignored in 2D. Otherwise as gbp_project. */
+int gbp_project_active(gbp_scene *scene, double dt, const float *solid, const float *fluid, float *u, float *v,
+                       float *w, const gbp_params *params, float *pressure, gbp_stats *stats, unsigned char *unknown,
+                       unsigned char *u_active, unsigned char *v_active, unsigned char *w_active);
+
 /* The same with DEVICE arrays, on `stream` (a cudaStream_t; NULL = the
  * context's stream). Returns after the solve has finished on the device. */
 int gbp_project_device(gbp_scene *scene, double dt, const float *solid, const float *fluid, float *u, float *v,

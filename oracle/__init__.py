@@ -29,7 +29,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SO = os.path.join(REF_DIR, "libref_harness.so")
-DEFAULT_REFERENCE = "/root/reference"
 
 
 def build_port(force: bool = False) -> str:
@@ -40,18 +39,46 @@ def build_port(force: bool = False) -> str:
 
 
 def build_reference(ref_dir: str | None = None, jobs: int = 8) -> str | None:
-    """Compile the reference (where its sources exist); returns the harness
-    path or None."""
-    ref_dir = ref_dir or os.environ.get("SHIOKAZE_REFERENCE", DEFAULT_REFERENCE)
-    if not os.path.isdir(os.path.join(ref_dir, "src", "projection")):
+    """Compile the reference from its sources in `ref_dir` (default: the
+    SHIOKAZE_REFERENCE environment variable); returns the harness path, or
+    None where neither names a Shiokaze source tree and nothing was built
+    before."""
+    ref_dir = ref_dir or os.environ.get("SHIOKAZE_REFERENCE")
+    if not ref_dir or not os.path.isdir(os.path.join(ref_dir, "src", "projection")):
         return REF_SO if os.path.exists(REF_SO) else None
     subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={ref_dir}", f"-j{jobs}"],
                           stdout=subprocess.DEVNULL)
+    with open(os.path.join(REF_DIR, "SOURCES"), "w") as f:
+        f.write(os.path.abspath(ref_dir) + "\n")
     return REF_SO
 
 
 def reference_available() -> bool:
     return os.path.exists(REF_SO)
+
+
+def reference_sources() -> str | None:
+    """The Shiokaze source tree the reference build was made from (its
+    headers also build the plugin modules), or None."""
+    try:
+        with open(os.path.join(REF_DIR, "SOURCES")) as f:
+            path = f.read().strip()
+        return path if os.path.isdir(path) else None
+    except OSError:
+        return None
+
+
+def build_modules(out: str, *targets: str, ldflags: str | None = None) -> None:
+    """Builds the plugin modules (shiokaze_gb300/module/Makefile) into `out`
+    against the headers of the reference build's source tree."""
+    src = reference_sources()
+    if not src:
+        raise RuntimeError("reference sources unknown: build the reference first (oracle.build_reference)")
+    cmd = ["make", "-s", "-C", os.path.join(os.path.dirname(HERE), "shiokaze_gb300", "module"), f"SHIOKAZE={src}",
+           f"OUT={out}"]
+    if ldflags is not None:
+        cmd += ["-B", f"LDFLAGS={ldflags}"]
+    subprocess.check_call(cmd + list(targets), stdout=subprocess.DEVNULL)
 
 
 class _Params(ctypes.Structure):
@@ -77,6 +104,9 @@ class Result:
     reresid: float
     ms: float = 0.0
     index: np.ndarray | None = None
+    # per face component, 1 where the projection leaves the face active, 0
+    # where the reference deactivates it (set_off); None if not asked for
+    active: tuple | None = None
 
 
 def _f32(a):
@@ -103,6 +133,9 @@ def _port_lib():
         lp = ctypes.POINTER(ctypes.c_longlong)
         lib.oracle_project.argtypes = [ctypes.c_void_p, ctypes.c_double, fp, fp, fp, fp, fp,
                                        ctypes.POINTER(_Params), fp, lp, ctypes.POINTER(_Stats)]
+        u8 = ctypes.POINTER(ctypes.c_ubyte)
+        lib.oracle_project_active.argtypes = [ctypes.c_void_p, ctypes.c_double, fp, fp, fp, fp, fp,
+                                              ctypes.POINTER(_Params), fp, lp, ctypes.POINTER(_Stats), u8, u8, u8]
         lib.oracle_assemble.argtypes = [ctypes.c_void_p, ctypes.c_double, fp, fp, fp, fp, fp,
                                         ctypes.POINTER(_Params), dp, dp, dp, dp, dp, lp]
         lib.oracle_face_fractions.argtypes = [ctypes.c_void_p, fp, fp, ctypes.POINTER(_Params), fp, fp, fp, fp, fp,
@@ -151,9 +184,14 @@ class PortProjector:
         p = np.zeros(fluid.shape, np.float32)
         idx = np.zeros(fluid.shape, np.int64)
         st = _Stats()
-        self.lib.oracle_project(self.ctx, dt, _ptr(solid), _ptr(fluid), _ptr(u), _ptr(v), _ptr(w),
-                                ctypes.byref(self.params), _ptr(p), _ptr(idx, ctypes.c_longlong), ctypes.byref(st))
-        return Result(p, u, v, w, idx >= 0, st.iterations, st.reresid, index=idx)
+        on = [np.zeros(a.shape, np.uint8) for a in (u, v, w) if a is not None]
+        u8 = ctypes.c_ubyte
+        self.lib.oracle_project_active(self.ctx, dt, _ptr(solid), _ptr(fluid), _ptr(u), _ptr(v), _ptr(w),
+                                       ctypes.byref(self.params), _ptr(p), _ptr(idx, ctypes.c_longlong),
+                                       ctypes.byref(st), *[_ptr(a, u8) for a in on],
+                                       *([None] if w is None else []))
+        return Result(p, u, v, w, idx >= 0, st.iterations, st.reresid, index=idx,
+                      active=tuple(a.astype(bool) for a in on))
 
     def assemble(self, dt, solid, fluid, u, v, w=None):
         solid, fluid, u, v = _f32(solid), _f32(fluid), _f32(u), _f32(v)
@@ -185,9 +223,10 @@ def _ref_lib():
         lib.ref_destroy.argtypes = [ctypes.c_void_p]
         lib.ref_set_target_volume.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
         lib.ref_project.restype = ctypes.c_double
+        u8p = ctypes.POINTER(ctypes.c_ubyte)
         lib.ref_project.argtypes = [ctypes.c_void_p, ctypes.c_double, fp, ctypes.c_int, ctypes.c_float, fp,
                                     ctypes.c_int, ctypes.c_float, fp, fp, fp, ctypes.c_double, fp,
-                                    ctypes.POINTER(ctypes.c_ubyte), ctypes.c_char_p]
+                                    u8p, u8p, u8p, u8p, ctypes.c_char_p]
         lib.ref_levelset_roundtrip.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp,
                                                ctypes.c_int, ctypes.c_float, fp]
         dp = ctypes.POINTER(ctypes.c_double)
@@ -343,7 +382,7 @@ class RefProjector:
 
     def __init__(self, dim, nx, ny, nz, dx, residual=1e-6, max_iterations=30000, warm_start=False, eps_fluid=1e-2,
                  eps_solid=1e-2, second_order_fluid=True, second_order_solid=True, gain=1.0, surface_tension=0.0,
-                 threads=None):
+                 threads=None, extra_kv=""):
         self.lib = _ref_lib()
         self.surface_tension = float(surface_tension)  # project()'s argument, not a configuration key
         self.dim, self.nx, self.ny, self.nz, self.dx = dim, nx, ny, (nz if dim == 3 else 1), dx
@@ -353,6 +392,8 @@ class RefProjector:
               f"SecondOrderAccurateSolid={'Yes' if second_order_solid else 'No'} Gain={gain!r}")
         if threads:
             kv += f" Threads={threads}"
+        if extra_kv:
+            kv += " " + extra_kv
         self._log = tempfile.NamedTemporaryFile(prefix="ref_project_", suffix=".log", delete=False).name
         self.ctx = self.lib.ref_create(dim, nx, ny, self.nz, dx, kv.encode(), self._log.encode())
 
@@ -378,15 +419,18 @@ class RefProjector:
         solid, fluid = _f32(solid), _f32(fluid)
         p = np.zeros(fluid.shape, np.float32)
         act = np.zeros(fluid.shape, np.uint8)
+        on = [None if a is None else np.zeros(a.shape, np.uint8) for a in (u, v, w)]
         open(self._log, "w").close()
+        u8 = ctypes.c_ubyte
         ms = self.lib.ref_project(self.ctx, dt, _ptr(solid), solid_mode, band, _ptr(fluid), fluid_mode, band,
                                   _ptr(u), _ptr(v), _ptr(w), self.surface_tension, _ptr(p),
-                                  _ptr(act, ctypes.c_ubyte), self._log.encode())
+                                  _ptr(act, u8), *[_ptr(a, u8) for a in on], self._log.encode())
         with open(self._log, errors="replace") as f:
             log = f.read()
         m = _ITER_RE.findall(log)
         iters, rr = (int(m[-1][0]), float(m[-1][1])) if m else (-1, float("nan"))
-        return Result(p, u, v, w, act.astype(bool), iters, rr, ms=ms)
+        return Result(p, u, v, w, act.astype(bool), iters, rr, ms=ms,
+                      active=tuple(a.astype(bool) for a in on if a is not None))
 
 
 def project_scene(scene, impl="port", **params) -> Result:

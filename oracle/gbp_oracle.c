@@ -445,8 +445,22 @@ static long long label_cells(const oracle_ctx *c, const float *fluid, float *con
  * (w unused in 2D). pressure: cells (float, 0 off the unknowns).
  * index_out (optional): unknown number per cell or -1.
  * Returns 0. */
+/* oracle_project plus, when on_u is not NULL, the faces the reference's
+ * velocity update leaves active (1) or deactivates with set_off (0):
+ * macpressuresolver3.cpp:252-267 and macpressuresolver2.cpp:221-236. */
+int oracle_project_active(oracle_ctx *c, double dt, const float *solid, const float *fluid, float *u, float *v,
+                          float *w, const oracle_params *prm, float *pressure, long long *index_out, oracle_stats *st,
+                          unsigned char *on_u, unsigned char *on_v, unsigned char *on_w);
+
 int oracle_project(oracle_ctx *c, double dt, const float *solid, const float *fluid, float *u, float *v, float *w,
                    const oracle_params *prm, float *pressure, long long *index_out, oracle_stats *st) {
+    return oracle_project_active(c, dt, solid, fluid, u, v, w, prm, pressure, index_out, st, NULL, NULL, NULL);
+}
+
+int oracle_project_active(oracle_ctx *c, double dt, const float *solid, const float *fluid, float *u, float *v,
+                          float *w, const oracle_params *prm, float *pressure, long long *index_out, oracle_stats *st,
+                          unsigned char *on_u, unsigned char *on_v, unsigned char *on_w) {
+    unsigned char *on[3] = {on_u, on_v, on_w};
     const int nx = c->nx, ny = c->ny, nz = c->nz, dim = c->dim;
     const double dx = c->dx;
     const size_t ncell = (size_t)nx * ny * nz;
@@ -594,6 +608,19 @@ int oracle_project(oracle_ctx *c, double dt, const float *solid, const float *fl
                     int pi[3] = {i, j, k};
                     float rho = R[d][fn];
                     float *uu = &vel[d][fn];
+                    if (on[0]) {
+                        int keep = A[d][fn] && rho;
+                        if (!keep && pi[d] == 0) {
+                            size_t cn = (size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k);
+                            keep = fluid[cn] < 0.0f && (dim == 3 || *uu < 0.0f);
+                        } else if (!keep && pi[d] == sh[d]) {
+                            int m[3] = {i, j, k};
+                            m[d] -= 1;
+                            size_t cn = (size_t)m[0] + (size_t)nx * ((size_t)m[1] + (size_t)ny * m[2]);
+                            keep = fluid[cn] < 0.0f && (dim == 3 || *uu > 0.0f);
+                        }
+                        on[d][fn] = (unsigned char)keep;
+                    }
                     if (A[d][fn] && rho) {
                         if (pi[d] == 0 || pi[d] == sh[d]) *uu = 0.0f;
                         else {

@@ -19,7 +19,8 @@
  * After project() the harness reads pressure and velocity back through
  * operator(), which applies background/fill semantics, and reports which
  * pressure cells are active (the reference sets pressure only at unknowns,
- * macpressuresolver3.cpp:245-248).
+ * macpressuresolver3.cpp:245-248) and which velocity faces stay active (its
+ * velocity update deactivates closed faces, :252-267).
  */
 #include <shiokaze/array/array2.h>
 #include <shiokaze/array/array3.h>
@@ -177,14 +178,18 @@ void ref_set_target_volume(void *hp, double current_volume, double target_volume
 /* One projection. Arrays are dense, x fastest:
  *   solid: nodal (nx+1)(ny+1)(nz+1), fluid: cells nx*ny*nz,
  *   u: (nx+1)*ny*nz, v: nx*(ny+1)*nz, w: nx*ny*(nz+1)   (in/out),
- *   pressure: cells (out), active: cells, 1 where pressure is active (out).
+ *   pressure: cells (out), active: cells, 1 where pressure is active (out),
+ *   on_u, on_v, on_w: per face, 1 where the velocity face is still active
+ *   after project() (out, each may be NULL).
  * solid_mode/fluid_mode: 0 = narrow-band level set of half-width band,
  * 1 = constant array (value = first element).
  * surface_tension: project()'s own argument (0 = none).
  * Returns wall-clock milliseconds of project(). */
 double ref_project(void *hp, double dt, const float *solid, int solid_mode, float solid_band,
                    const float *fluid, int fluid_mode, float fluid_band, float *u, float *v, float *w,
-                   double surface_tension, float *pressure, unsigned char *active, const char *log_path) {
+                   double surface_tension, float *pressure, unsigned char *active, unsigned char *on_u,
+                   unsigned char *on_v, unsigned char *on_w, const char *log_path) {
+    unsigned char *on[3] = {on_u, on_v, on_w};
     auto *h = static_cast<harness *>(hp);
     const int nx = h->nx, ny = h->ny, nz = h->nz;
     double ms = 0.0;
@@ -213,8 +218,11 @@ double ref_project(void *hp, double dt, const float *solid, int solid_mode, floa
             const shape3 fs = s.face(d);
             for (int k = 0; k < (int)fs.d; ++k)
                 for (int j = 0; j < (int)fs.h; ++j)
-                    for (int i = 0; i < (int)fs.w; ++i)
-                        comp[d][i + (size_t)fs.w * (j + (size_t)fs.h * k)] = vel[d](i, j, k);
+                    for (int i = 0; i < (int)fs.w; ++i) {
+                        const size_t n = i + (size_t)fs.w * (j + (size_t)fs.h * k);
+                        comp[d][n] = vel[d](i, j, k);
+                        if (on[d]) on[d][n] = vel[d].active(i, j, k) ? 1 : 0;
+                    }
         }
         const array3<Real> &p = *(*h->proj3)->get_pressure();
         for (int k = 0; k < nz; ++k)
@@ -247,7 +255,11 @@ double ref_project(void *hp, double dt, const float *solid, int solid_mode, floa
         for (int d = 0; d < 2; ++d) {
             const shape2 fs = s.face(d);
             for (int j = 0; j < (int)fs.h; ++j)
-                for (int i = 0; i < (int)fs.w; ++i) comp[d][i + (size_t)fs.w * j] = vel[d](i, j);
+                for (int i = 0; i < (int)fs.w; ++i) {
+                    const size_t n = i + (size_t)fs.w * j;
+                    comp[d][n] = vel[d](i, j);
+                    if (on[d]) on[d][n] = vel[d].active(i, j) ? 1 : 0;
+                }
         }
         const array2<Real> &p = *(*h->proj2)->get_pressure();
         for (int j = 0; j < ny; ++j)

@@ -82,7 +82,7 @@ _lib = None
 EXPORTED = ["gbp_params_default", "gbp_create", "gbp_destroy", "gbp_scene_create", "gbp_scene_destroy",
             "gbp_scene_device_bytes", "gbp_scene_set_target_volume", "gbp_project", "gbp_project_device",
             "gbp_debug_assemble", "gbp_bench_kernel", "gbp_launch_count", "gbp_strerror", "gbp_batch_create",
-            "gbp_batch_destroy", "gbp_batch_project_device"]
+            "gbp_batch_destroy", "gbp_batch_project_device", "gbp_project_active"]
 
 
 def library_path() -> str:
@@ -115,6 +115,9 @@ def load_library():
     lib.gbp_scene_set_target_volume.argtypes = [vp, ctypes.c_double, ctypes.c_double]
     lib.gbp_project.argtypes = [vp, ctypes.c_double, fp, fp, fp, fp, fp, ctypes.POINTER(Params), fp,
                                 ctypes.POINTER(Stats)]
+    u8p = ctypes.POINTER(ctypes.c_ubyte)
+    lib.gbp_project_active.argtypes = [vp, ctypes.c_double, fp, fp, fp, fp, fp, ctypes.POINTER(Params), fp,
+                                       ctypes.POINTER(Stats), u8p, u8p, u8p, u8p]
     lib.gbp_project_device.argtypes = [vp, ctypes.c_double, vp, vp, vp, vp, vp, ctypes.POINTER(Params), vp,
                                        ctypes.POINTER(Stats), vp]
     lib.gbp_debug_assemble.argtypes = [vp, ctypes.c_double, fp, fp, fp, fp, fp, ctypes.POINTER(Params), dp, dp, dp,
@@ -273,6 +276,11 @@ class _MacProject:
         check(self.lib.gbp_scene_create(self.ctx.handle, self.dim, nx, ny, self.nz, dx, ctypes.byref(self.scene)))
         self.pressure = None
         self.stats = Stats()
+        # active sets of the last host call made with active_sets=True: the
+        # unknown cells (the pressure's active cells in the reference) and,
+        # per face component, the faces the velocity update leaves active
+        self.unknown = None
+        self.active = None
 
     def configure(self, **config):
         """Sets configuration keys (merged with the ones already set)."""
@@ -300,12 +308,13 @@ class _MacProject:
     def device_bytes(self) -> int:
         return int(self.lib.gbp_scene_device_bytes(self.dim, self.nx, self.ny, self.nz, ctypes.byref(self.params)))
 
-    def project(self, dt, velocity, solid, fluid, pressure_out=None, stream=None):
+    def project(self, dt, velocity, solid, fluid, pressure_out=None, stream=None, active_sets=False):
         """Projects ``velocity`` (tuple of face arrays) in place. numpy arrays
         go through the host call; torch CUDA tensors through the device call.
         Returns the status code (GBP_OK, or GBP_ERR_NOT_CONVERGED /
         GBP_ERR_NAN, after which the last iterate was still applied, as in
-        the reference)."""
+        the reference). With ``active_sets`` (host arrays) the call also
+        fills ``self.unknown`` and ``self.active`` (gbp_project_active)."""
         comps = list(velocity) + [None] * (3 - len(velocity))
         u, v, w = comps[0], comps[1], comps[2] if self.dim == 3 else None
         if _is_torch_cuda(u):
@@ -338,8 +347,16 @@ class _MacProject:
         if self.pressure is None or not isinstance(self.pressure, np.ndarray):
             self.pressure = np.zeros(fluid_a.shape, np.float32)
         pp = self.pressure.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
-        rc = self.lib.gbp_project(self.scene, dt, solid_p, fluid_p, arrs[0][1], arrs[1][1], arrs[2][1],
-                                  ctypes.byref(self.params), pp, ctypes.byref(self.stats))
+        if active_sets:
+            self.unknown = np.zeros(fluid_a.shape, np.uint8)
+            self.active = tuple(np.zeros(a.shape, np.uint8) for a, _ in arrs if a is not None)
+            u8 = ctypes.POINTER(ctypes.c_ubyte)
+            mp = [m.ctypes.data_as(u8) for m in (self.unknown,) + self.active] + [None] * (3 - self.dim)
+            rc = self.lib.gbp_project_active(self.scene, dt, solid_p, fluid_p, arrs[0][1], arrs[1][1], arrs[2][1],
+                                             ctypes.byref(self.params), pp, ctypes.byref(self.stats), *mp)
+        else:
+            rc = self.lib.gbp_project(self.scene, dt, solid_p, fluid_p, arrs[0][1], arrs[1][1], arrs[2][1],
+                                      ctypes.byref(self.params), pp, ctypes.byref(self.stats))
         return check(rc, (GBP_OK, GBP_ERR_NOT_CONVERGED, GBP_ERR_NAN))
 
     def bench_kernel(self, which: int, reps: int = 20, stream=None):
@@ -528,15 +545,34 @@ class MacUtility3:
         self.lib = self.ctx.lib
         self.nx, self.ny, self.nz, self.dx = nx, ny, nz, dx
 
+    def _check_sizes(self, solid, velocity, masks):
+        """Every array must hold exactly its grid's element count: the call
+        hands raw pointers to the library, so a wrong shape would be read or
+        written out of bounds."""
+        nx, ny, nz = self.nx, self.ny, self.nz
+        faces = ((nx + 1) * ny * nz, nx * (ny + 1) * nz, nx * ny * (nz + 1))
+        size = (lambda a: a.numel()) if _is_torch_cuda(velocity[0]) else (lambda a: np.asarray(a).size)
+        if size(solid) != (nx + 1) * (ny + 1) * (nz + 1):
+            raise ValueError(f"solid holds {size(solid)} values, expected {(nx + 1) * (ny + 1) * (nz + 1)} (nodal)")
+        for d, (a, m) in enumerate(zip(velocity, masks)):
+            if size(a) != faces[d]:
+                raise ValueError(f"velocity component {d} holds {size(a)} values, expected {faces[d]}")
+            if m is not None:
+                n = m.numel() if _is_torch_cuda(m) else np.asarray(m).size
+                if n != faces[d]:
+                    raise ValueError(f"mask of component {d} holds {n} values, expected {faces[d]}")
+
     def constrain_velocity(self, solid, velocity, masks=None, stream=None):
         u, v, w = velocity
         masks = masks or (None, None, None)
+        self._check_sizes(solid, velocity, masks)
         if _is_torch_cuda(u):
             import torch
             for t in (u, v, w, solid):
                 assert t.dtype == torch.float32 and t.is_contiguous(), "device arrays must be contiguous float32"
             st = stream if stream is not None else torch.cuda.current_stream(u.device).cuda_stream
-            # masks may be numpy (copied to the device here) or uint8 CUDA tensors
+            # masks may be numpy, copied to the device here by a synchronous
+            # copy (complete before the call), or uint8 CUDA tensors
             masks = [None if m is None else (m if _is_torch_cuda(m) else torch.from_numpy(
                 np.ascontiguousarray(m, dtype=np.uint8)).to(u.device)) for m in masks]
             for m in masks:

@@ -73,6 +73,8 @@ struct gbp_scene {
     // staging for the host-array call
     float *d_solid = nullptr, *d_fluid = nullptr, *d_u = nullptr, *d_v = nullptr, *d_w = nullptr,
           *d_p = nullptr;
+    // active sets of the last gbp_project_active call (unknown cells, kept faces)
+    unsigned char *d_unknown = nullptr, *d_on[3] = {nullptr, nullptr, nullptr};
     // volume correction state (macpressuresolver3.cpp:316-318)
     double current_volume = 0.0, target_volume = 0.0, y_prev = 0.0;
     Solver *solver = nullptr;
@@ -249,6 +251,8 @@ void gbp_scene_destroy(gbp_scene *s) {
     cudaStreamSynchronize(s->ctx->stream);
     for (float *p : {s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, s->d_p})
         if (p) cudaFree(p);
+    for (unsigned char *m : {s->d_unknown, s->d_on[0], s->d_on[1], s->d_on[2]})
+        if (m) cudaFree(m);
     if (s->solver) {
         s->solver->release();
         delete s->solver;
@@ -307,8 +311,17 @@ int validate(const gbp_params &p) {
     return GBP_OK;
 }
 
+int ensure_active_sets(gbp_scene *s) {
+    const Grid &g = s->g;
+    if (!s->d_unknown) GBP_CUDA(cudaMalloc(&s->d_unknown, (size_t)g.ncell));
+    for (int d = 0; d < g.dim; ++d)
+        if (!s->d_on[d]) GBP_CUDA(cudaMalloc(&s->d_on[d], n_face(g, d)));
+    return GBP_OK;
+}
+
 int project_device(gbp_scene *s, double dt, const float *solid, const float *fluid, float *u, float *v, float *w,
-                   const gbp_params &p, float *pressure, gbp_stats *stats, cudaStream_t stream) {
+                   const gbp_params &p, float *pressure, gbp_stats *stats, cudaStream_t stream,
+                   bool active_sets = false) {
     gbp_ctx *c = s->ctx;
     const Grid &g = s->g;
     int rc = validate(p);
@@ -344,6 +357,11 @@ int project_device(gbp_scene *s, double dt, const float *solid, const float *flu
 
     GBP_CUDA(launch_pressure(g, st.diag, st.x, p.warm_start && st.have_prev ? st.prev : nullptr, pressure,
                              p.warm_start ? st.prev : nullptr, c->grid_blocks, stream));
+    if (active_sets) {
+        GBP_CUDA(launch_active_sets(g, st.faces, fluid, u, v, w, st.diag, s->d_unknown, s->d_on[0], s->d_on[1],
+                                    s->d_on[2], st.sc, c->grid_blocks, stream));
+        c->launches += 1;
+    }
     GBP_CUDA(launch_velocity_faces(g, dt, s->dx, sp, pressure, st.faces, u, v, w, st.sc, c->grid_blocks, stream));
     c->launches += 2;
     if (p.warm_start) st.have_prev = true;
@@ -361,6 +379,49 @@ int project_device(gbp_scene *s, double dt, const float *solid, const float *flu
         cudaEventElapsedTime(&stats->ms_update, c->ev[2], c->ev[3]);
     }
     return solve_status;
+}
+
+// The host-array calls: inputs copied to the scene's device staging, the
+// projection, results copied back; with unknown != NULL also the active sets.
+int project_host(const char *who, gbp_scene *s, double dt, const float *solid, const float *fluid, float *u,
+                 float *v, float *w, const gbp_params *params, float *pressure, gbp_stats *stats,
+                 unsigned char *unknown, unsigned char *u_active, unsigned char *v_active,
+                 unsigned char *w_active) {
+    if (!s) return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": NULL scene");
+    auto t0 = std::chrono::steady_clock::now();
+    const Grid &g = s->g;
+    if (!solid || !fluid || !u || !v || (g.dim == 3 && !w))
+        return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": NULL array");
+    gbp_params p;
+    gbp_params_default(&p);
+    if (params) p = *params;
+    GBP_CUDA(cudaSetDevice(s->ctx->device));
+    int rc = ensure_staging(s);
+    if (rc) return rc;
+    const bool sets = unknown != nullptr;
+    if (sets && (rc = ensure_active_sets(s))) return rc;
+    cudaStream_t st = s->ctx->stream;
+    GBP_CUDA(cudaMemcpyAsync(s->d_solid, solid, 4 * n_nodes(g), cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(s->d_fluid, fluid, 4 * (size_t)g.ncell, cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(s->d_u, u, 4 * n_face(g, 0), cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(s->d_v, v, 4 * n_face(g, 1), cudaMemcpyHostToDevice, st));
+    if (g.dim == 3) GBP_CUDA(cudaMemcpyAsync(s->d_w, w, 4 * n_face(g, 2), cudaMemcpyHostToDevice, st));
+    rc = project_device(s, dt, s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, p, s->d_p, stats, st, sets);
+    if (rc != GBP_OK && rc != GBP_ERR_NOT_CONVERGED && rc != GBP_ERR_NAN) return rc;
+    GBP_CUDA(cudaMemcpyAsync(u, s->d_u, 4 * n_face(g, 0), cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaMemcpyAsync(v, s->d_v, 4 * n_face(g, 1), cudaMemcpyDeviceToHost, st));
+    if (g.dim == 3) GBP_CUDA(cudaMemcpyAsync(w, s->d_w, 4 * n_face(g, 2), cudaMemcpyDeviceToHost, st));
+    if (pressure) GBP_CUDA(cudaMemcpyAsync(pressure, s->d_p, 4 * (size_t)g.ncell, cudaMemcpyDeviceToHost, st));
+    if (sets) {
+        unsigned char *out[3] = {u_active, v_active, w_active};
+        GBP_CUDA(cudaMemcpyAsync(unknown, s->d_unknown, (size_t)g.ncell, cudaMemcpyDeviceToHost, st));
+        for (int d = 0; d < g.dim; ++d)
+            GBP_CUDA(cudaMemcpyAsync(out[d], s->d_on[d], n_face(g, d), cudaMemcpyDeviceToHost, st));
+    }
+    GBP_CUDA(cudaStreamSynchronize(st));
+    if (stats)
+        stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
 }
 
 }  // namespace
@@ -396,33 +457,17 @@ int gbp_project_device(gbp_scene *s, double dt, const float *solid, const float 
 
 int gbp_project(gbp_scene *s, double dt, const float *solid, const float *fluid, float *u, float *v, float *w,
                 const gbp_params *params, float *pressure, gbp_stats *stats) {
-    if (!s) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_project: NULL scene");
-    auto t0 = std::chrono::steady_clock::now();
-    const Grid &g = s->g;
-    if (!solid || !fluid || !u || !v || (g.dim == 3 && !w))
-        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_project: NULL array");
-    gbp_params p;
-    gbp_params_default(&p);
-    if (params) p = *params;
-    GBP_CUDA(cudaSetDevice(s->ctx->device));
-    int rc = ensure_staging(s);
-    if (rc) return rc;
-    cudaStream_t st = s->ctx->stream;
-    GBP_CUDA(cudaMemcpyAsync(s->d_solid, solid, 4 * n_nodes(g), cudaMemcpyHostToDevice, st));
-    GBP_CUDA(cudaMemcpyAsync(s->d_fluid, fluid, 4 * (size_t)g.ncell, cudaMemcpyHostToDevice, st));
-    GBP_CUDA(cudaMemcpyAsync(s->d_u, u, 4 * n_face(g, 0), cudaMemcpyHostToDevice, st));
-    GBP_CUDA(cudaMemcpyAsync(s->d_v, v, 4 * n_face(g, 1), cudaMemcpyHostToDevice, st));
-    if (g.dim == 3) GBP_CUDA(cudaMemcpyAsync(s->d_w, w, 4 * n_face(g, 2), cudaMemcpyHostToDevice, st));
-    rc = project_device(s, dt, s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, p, s->d_p, stats, st);
-    if (rc != GBP_OK && rc != GBP_ERR_NOT_CONVERGED && rc != GBP_ERR_NAN) return rc;
-    GBP_CUDA(cudaMemcpyAsync(u, s->d_u, 4 * n_face(g, 0), cudaMemcpyDeviceToHost, st));
-    GBP_CUDA(cudaMemcpyAsync(v, s->d_v, 4 * n_face(g, 1), cudaMemcpyDeviceToHost, st));
-    if (g.dim == 3) GBP_CUDA(cudaMemcpyAsync(w, s->d_w, 4 * n_face(g, 2), cudaMemcpyDeviceToHost, st));
-    if (pressure) GBP_CUDA(cudaMemcpyAsync(pressure, s->d_p, 4 * (size_t)g.ncell, cudaMemcpyDeviceToHost, st));
-    GBP_CUDA(cudaStreamSynchronize(st));
-    if (stats)
-        stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    return rc;
+    return project_host("gbp_project", s, dt, solid, fluid, u, v, w, params, pressure, stats, nullptr, nullptr,
+                        nullptr, nullptr);
+}
+
+int gbp_project_active(gbp_scene *s, double dt, const float *solid, const float *fluid, float *u, float *v, float *w,
+                       const gbp_params *params, float *pressure, gbp_stats *stats, unsigned char *unknown,
+                       unsigned char *u_active, unsigned char *v_active, unsigned char *w_active) {
+    if (s && (!unknown || !u_active || !v_active || (s->g.dim == 3 && !w_active)))
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_project_active: NULL active-set array");
+    return project_host("gbp_project_active", s, dt, solid, fluid, u, v, w, params, pressure, stats, unknown,
+                        u_active, v_active, w_active);
 }
 
 }  // extern "C"

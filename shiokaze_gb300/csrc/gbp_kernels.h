@@ -41,6 +41,12 @@ cudaError_t launch_assemble_faces(const Grid &g, const SetupParams &sp, const fl
 cudaError_t launch_velocity_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *p,
                                   FaceArrays fa, float *u, float *v, float *w, const Scalars *sc, int grid_blocks,
                                   cudaStream_t stream);
+// Active sets the reference leaves: unknown cells (diag != 0) and the faces
+// its velocity update keeps active; on the velocity before the update.
+cudaError_t launch_active_sets(const Grid &g, FaceArrays fa, const float *fluid, const float *u, const float *v,
+                               const float *w, const double *diag, unsigned char *unknown, unsigned char *on_u,
+                               unsigned char *on_v, unsigned char *on_w, const Scalars *sc, int grid_blocks,
+                               cudaStream_t stream);
 // Single-pass path (per cell, fractions recomputed per cell).
 cudaError_t launch_assemble(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
                             const float *fluid, const float *u, const float *v, const float *w, double *diag,

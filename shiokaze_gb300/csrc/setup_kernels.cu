@@ -681,6 +681,59 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_faces_kernel(Grid g, d
     }
 }
 
+// The active sets the reference leaves behind (macpressuresolver3.cpp:
+// 245-266; 2D macpressuresolver2.cpp:214-236), for callers that keep sparse
+// arrays: unknown[c] = 1 on the cells whose pressure the reference sets (the
+// unknowns, diag != 0 as pressure_kernel decides), on[d][f] = 1 on the faces
+// its velocity update keeps active: open faces (area > 0 and rho > 0) and
+// closed faces on the domain boundary next to a fluid cell (in 2D only where
+// the velocity points out of the domain: u < 0 on the low wall, u > 0 on the
+// high one). Every other face is deactivated (set_off) by the reference.
+// Runs before the velocity update, on the velocity it is given.
+__global__ void __launch_bounds__(BLOCK_THREADS) active_sets_kernel(Grid g, FaceArrays fa,
+                                                                    const float *__restrict__ fluid,
+                                                                    const float *__restrict__ u,
+                                                                    const float *__restrict__ v,
+                                                                    const float *__restrict__ w,
+                                                                    const double *__restrict__ diag,
+                                                                    unsigned char *__restrict__ unknown,
+                                                                    unsigned char *on0, unsigned char *on1,
+                                                                    unsigned char *on2,
+                                                                    const Scalars *__restrict__ sc) {
+    const int fluid_exists = sc->fluid_exists;
+    const long long NX = g.nx + 1, NY = g.ny + 1, NZ = g.dim == 3 ? g.nz + 1 : 1;
+    const long long total = NX * NY * NZ;
+    const float *vel[3] = {u, v, w};
+    unsigned char *on[3] = {on0, on1, on2};
+    const int n[3] = {g.nx, g.ny, g.nz};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        node_coords(g, t, i, j, k);
+        const int pi[3] = {i, j, k};
+        if (i < g.nx && j < g.ny && (g.dim == 2 || k < g.nz)) {
+            const long long c = cell_index(g, i, j, k);
+            unknown[c] = __ldg(diag + c) != 0.0 ? 1 : 0;
+        }
+        for (int d = 0; d < g.dim; ++d) {
+            bool exists = true;
+            for (int e = 0; e < g.dim; ++e)
+                if (e != d && pi[e] >= n[e]) exists = false;
+            if (!exists) continue;
+            const long long f = face_index(g, d, i, j, k);
+            const float fr = __ldg(fa.rho[d] + f);
+            bool keep = fluid_exists ? fr > 0.0f : fr != 0.0f;
+            if (!keep && pi[d] == 0) {
+                keep = __ldg(fluid + cell_index(g, i, j, k)) < 0.0f && (g.dim == 3 || __ldg(vel[d] + f) < 0.0f);
+            } else if (!keep && pi[d] == n[d]) {
+                keep = __ldg(fluid + cell_index(g, i - (d == 0), j - (d == 1), k - (d == 2))) < 0.0f &&
+                       (g.dim == 3 || __ldg(vel[d] + f) > 0.0f);
+            }
+            on[d][f] = keep ? 1 : 0;
+        }
+    }
+}
+
 FaceParams face_params(const SetupParams &sp, double dx, double dt) {
     FaceParams fp{sp.eps_solid, sp.eps_fluid, sp.second_order_solid, sp.second_order_fluid, 0, 0.0, 0.0, 0.0, 0, 0.0,
                   0, 0};
@@ -756,6 +809,15 @@ cudaError_t launch_velocity_faces(const Grid &g, double dt, double dx, const Set
                                   cudaStream_t stream) {
     const FaceParams fp = face_params(sp, dx, dt);
     velocity_faces_kernel<<<node_blocks(g, grid_blocks), BLOCK_THREADS, 0, stream>>>(g, dt, dx, fp, p, fa, u, v, w, sc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_active_sets(const Grid &g, FaceArrays fa, const float *fluid, const float *u, const float *v,
+                               const float *w, const double *diag, unsigned char *unknown, unsigned char *on_u,
+                               unsigned char *on_v, unsigned char *on_w, const Scalars *sc, int grid_blocks,
+                               cudaStream_t stream) {
+    active_sets_kernel<<<node_blocks(g, grid_blocks), BLOCK_THREADS, 0, stream>>>(g, fa, fluid, u, v, w, diag, unknown,
+                                                                                  on_u, on_v, on_w, sc);
     return cudaGetLastError();
 }
 

@@ -3,8 +3,11 @@
 // (include/shiokaze/projection/macproject2_interface.h), a drop-in for
 // "macpressuresolver2" (src/projection/macpressuresolver2.cpp). Selected with
 // Projection=gbprojection2. Dense copy with operator()'s values
-// (gbarray_adapter.h), gbp_project, and write-back to the active faces, as
-// in gbprojection3.cpp.
+// (gbarray_adapter.h), gbp_project_active, and the reference's output state
+// as in gbprojection3.cpp: the projected velocity on the active faces, the
+// faces its velocity update deactivates turned off (closed faces other than
+// walls next to fluid with outgoing flow, macpressuresolver2.cpp:233-235),
+// the pressure set on every unknown (:215-218).
 #include <shiokaze/array/array2.h>
 #include <shiokaze/array/macarray2.h>
 #include <shiokaze/core/console.h>
@@ -50,18 +53,22 @@ protected:
             if (m_target_volume) gbp_scene_set_target_volume(m_scene, m_current_volume, m_target_volume);
         }
         gbp_stats st;
-        int rc = gbp_project(m_scene, dt, s.data(), f.data(), vel[0].data(), vel[1].data(), nullptr, &m_params,
-                             p.data(), &st);
-        gbprojection::check(rc, "gbp_project");
+        std::vector<unsigned char> unknown(f.size()), on[2];
+        for (int d = 0; d < 2; ++d) on[d].resize(vel[d].size());
+        int rc = gbp_project_active(m_scene, dt, s.data(), f.data(), vel[0].data(), vel[1].data(), nullptr,
+                                    &m_params, p.data(), &st, unknown.data(), on[0].data(), on[1].data(), nullptr);
+        gbprojection::check(rc, "gbp_project_active");
         m_pressure.clear();
         for (int j = 0; j < ny; ++j)
             for (int i = 0; i < nx; ++i) {
-                const float v = p[i + (size_t)nx * j];
-                if (v) m_pressure.set(i, j, v);
+                const size_t n = i + (size_t)nx * j;
+                if (unknown[n]) m_pressure.set(i, j, p[n]);
             }
         velocity.parallel_actives([&](int dim, int i, int j, auto &it, int tn) {
             const int fx = nx + (dim == 0);
-            it.set(vel[dim][i + (size_t)fx * j]);
+            const size_t n = i + (size_t)fx * j;
+            if (on[dim][n]) it.set(vel[dim][n]);
+            else it.set_off();
         });
     }
 

@@ -8,11 +8,13 @@
 // The reference's arrays are sparse (tiled, narrow band); project() copies
 // them to dense arrays with exactly operator()'s values (background, fill
 // and active values; gbarray_adapter.h, one pass over the filled and active
-// cells instead of one lookup per cell), calls gbp_project, and writes the projected velocity back to the faces
-// that were active, as the reference's velocity update iterates actives
-// (macpressuresolver3.cpp:252). Faces the reference would deactivate
-// (closed faces) are written as 0, which is the value they read back as.
-// Pressure is set on the cells with a nonzero pressure (the unknowns).
+// cells instead of one lookup per cell) and calls gbp_project_active. The
+// output state is the reference's: the projected velocity is written to the
+// faces that were active, as its velocity update iterates actives
+// (macpressuresolver3.cpp:252), and the faces it deactivates there (closed
+// faces that are not walls next to fluid, :264-266) are turned off with
+// set_off; the pressure is set on every unknown, a pressure of 0 included
+// (:245-248), and the other cells are left inactive.
 #include <shiokaze/array/array3.h>
 #include <shiokaze/array/macarray3.h>
 #include <shiokaze/core/console.h>
@@ -58,21 +60,26 @@ protected:
             if (m_target_volume) gbp_scene_set_target_volume(m_scene, m_current_volume, m_target_volume);
         }
         gbp_stats st;
-        int rc = gbp_project(m_scene, dt, s.data(), f.data(), vel[0].data(), vel[1].data(), vel[2].data(), &m_params,
-                             p.data(), &st);
-        gbprojection::check(rc, "gbp_project");
+        std::vector<unsigned char> unknown(f.size()), on[3];
+        for (int d = 0; d < 3; ++d) on[d].resize(vel[d].size());
+        int rc = gbp_project_active(m_scene, dt, s.data(), f.data(), vel[0].data(), vel[1].data(), vel[2].data(),
+                                    &m_params, p.data(), &st, unknown.data(), on[0].data(), on[1].data(),
+                                    on[2].data());
+        gbprojection::check(rc, "gbp_project_active");
         console::dump("gbprojection3: %d iterations, Reresid=%e, %.3f ms\n", st.iterations, st.reresid, st.ms_total);
         console::write(get_argument_name() + "_number_projection_iteration", st.iterations);
         m_pressure.clear();
         for (int k = 0; k < nz; ++k)
             for (int j = 0; j < ny; ++j)
                 for (int i = 0; i < nx; ++i) {
-                    const float v = p[i + (size_t)nx * (j + (size_t)ny * k)];
-                    if (v) m_pressure.set(i, j, k, v);
+                    const size_t n = i + (size_t)nx * (j + (size_t)ny * k);
+                    if (unknown[n]) m_pressure.set(i, j, k, p[n]);
                 }
         velocity.parallel_actives([&](int dim, int i, int j, int k, auto &it, int tn) {
             const int fx = nx + (dim == 0), fy = ny + (dim == 1);
-            it.set(vel[dim][i + (size_t)fx * (j + (size_t)fy * k)]);
+            const size_t n = i + (size_t)fx * (j + (size_t)fy * k);
+            if (on[dim][n]) it.set(vel[dim][n]);
+            else it.set_off();
         });
     }
 

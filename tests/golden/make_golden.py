@@ -10,6 +10,8 @@ stores inputs, settings and outputs in ``<case>.npz``:
   solid_mode, fluid_mode, band    how the harness built the sparse arrays
   steps                           number of project() calls (warm start)
   out_pressure, out_u, out_v[, out_w], out_unknown    after the last call
+  out_u_on, out_v_on[, out_w_on]  faces still active after the last call
+                                  (the velocity update deactivates closed faces)
   iterations, reresid             the reference's CG report (3D only)
 
 Run from the repository root where the reference sources exist:
@@ -129,6 +131,8 @@ def make_case(name, factory, params, steps):
             out[f"w{s}"] = ww
     if res.w is not None:
         out["out_w"] = res.w
+    for c, a in zip("uvw", res.active):
+        out[f"out_{c}_on"] = a.astype(np.uint8)
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
     return res
 

@@ -31,6 +31,8 @@ class Case:
         self.out_v = d["out_v"]
         self.out_w = d["out_w"] if "out_w" in d else None
         self.out_unknown = d["out_unknown"].astype(bool)
+        # faces the reference's velocity update leaves active (closed faces are set_off)
+        self.out_active = tuple(d[f"out_{c}_on"].astype(bool) for c in "uvw"[:self.dim])
         self.iterations = int(d["iterations"])
         self.reresid = float(d["reresid"])
         # (current, target) volumes set before each step, if the case has them

@@ -2,12 +2,14 @@
  * gbp_oracle_stub.c -- TEST INFRASTRUCTURE: a stand-in for libgbp's
  * advection entry points that runs the oracle (oracle/advect_oracle.c, in
  * liboracle.so) on the CPU, and the same for the solid constraint of the
- * velocity. tests/test_oracle.py links the gbadvection3 and gbutility3
- * plugin modules against it to check the modules' boundary (dense copies
- * of the reference's tiled arrays, the active masks, the write-back over
- * active faces and cells) against the reference's own macadvection3 and
- * macutility3 without a GPU.
- * The shipped module links the real libgbp.so.
+ * velocity and for the projection (oracle/gbp_oracle.c: scenes, volume
+ * correction, warm start, gbp_project / gbp_project_active with the active
+ * sets). tests/test_oracle.py links the gbadvection3, gbutility3 and
+ * gbprojection2/3 plugin modules against it to check the modules' boundary
+ * (dense copies of the reference's tiled arrays, the active masks, the
+ * write-back over active faces and cells, the faces turned off, the
+ * pressure's active cells) against the reference's own modules without a
+ * GPU. The shipped modules link the real libgbp.so.
  */
 #include <stdlib.h>
 #include <string.h>
@@ -62,4 +64,112 @@ int gbp_constrain_velocity3(gbp_ctx *ctx, int nx, int ny, int nz, double dx, con
                             float *w, const unsigned char *mu, const unsigned char *mv, const unsigned char *mw) {
     (void)ctx;
     return oracle_constrain_velocity3(nx, ny, nz, dx, solid, u, v, w, mu, mv, mw);
+}
+
+
+/* ---- projection, backed by oracle/gbp_oracle.c ---------------------------- */
+
+typedef struct {
+    double residual;
+    int max_iterations;
+    int warm_start;
+    double eps_fluid;
+    double eps_solid;
+    int second_order_fluid;
+    int second_order_solid;
+    double gain;
+    double surface_tension;
+} oracle_params;
+
+typedef struct {
+    int iterations;
+    int converged;
+    double reresid;
+    long long unknowns;
+    double b_inf;
+} oracle_stats;
+
+typedef struct oracle_ctx oracle_ctx;
+oracle_ctx *oracle_create(int dim, int nx, int ny, int nz, double dx);
+void oracle_destroy(oracle_ctx *c);
+void oracle_set_target_volume(oracle_ctx *c, double current_volume, double target_volume);
+int oracle_project_active(oracle_ctx *c, double dt, const float *solid, const float *fluid, float *u, float *v,
+                          float *w, const oracle_params *prm, float *pressure, long long *index_out, oracle_stats *st,
+                          unsigned char *on_u, unsigned char *on_v, unsigned char *on_w);
+
+struct gbp_scene {
+    oracle_ctx *oc;
+    int dim, nx, ny, nz;
+};
+
+void gbp_params_default(gbp_params *p) {
+    memset(p, 0, sizeof(*p));
+    p->residual = 1e-4;
+    p->max_iterations = 30000;
+    p->eps_fluid = 1e-2;
+    p->eps_solid = 1e-2;
+    p->second_order_fluid = 1;
+    p->second_order_solid = 1;
+    p->gain = 1.0;
+    p->mg_smooth = 1;
+    p->mg_coarsest = 4;
+    p->inner_tolerance = 1e-3;
+    p->iterations_per_sync = 16;
+    p->tile_classes = 1;
+}
+
+int gbp_scene_create(gbp_ctx *ctx, int dim, int nx, int ny, int nz, double dx, gbp_scene **out) {
+    (void)ctx;
+    gbp_scene *s = (gbp_scene *)malloc(sizeof(gbp_scene));
+    s->dim = dim;
+    s->nx = nx;
+    s->ny = ny;
+    s->nz = dim == 3 ? nz : 1;
+    s->oc = oracle_create(dim, nx, ny, s->nz, dx);
+    *out = s;
+    return GBP_OK;
+}
+
+void gbp_scene_destroy(gbp_scene *s) {
+    if (!s) return;
+    oracle_destroy(s->oc);
+    free(s);
+}
+
+int gbp_scene_set_target_volume(gbp_scene *s, double current_volume, double target_volume) {
+    oracle_set_target_volume(s->oc, current_volume, target_volume);
+    return GBP_OK;
+}
+
+int gbp_project_active(gbp_scene *s, double dt, const float *solid, const float *fluid, float *u, float *v, float *w,
+                       const gbp_params *params, float *pressure, gbp_stats *stats, unsigned char *unknown,
+                       unsigned char *u_active, unsigned char *v_active, unsigned char *w_active) {
+    gbp_params p;
+    gbp_params_default(&p);
+    if (params) p = *params;
+    oracle_params op = {p.residual, p.max_iterations, p.warm_start, p.eps_fluid, p.eps_solid,
+                        p.second_order_fluid, p.second_order_solid, p.gain, p.surface_tension};
+    const size_t ncell = (size_t)s->nx * s->ny * s->nz;
+    long long *index = unknown ? (long long *)malloc(sizeof(long long) * ncell) : NULL;
+    oracle_stats st;
+    memset(&st, 0, sizeof(st));
+    oracle_project_active(s->oc, dt, solid, fluid, u, v, s->dim == 3 ? w : NULL, &op, pressure, index, &st,
+                          u_active, v_active, s->dim == 3 ? w_active : NULL);
+    if (unknown)
+        for (size_t n = 0; n < ncell; ++n) unknown[n] = index[n] >= 0 ? 1 : 0;
+    free(index);
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->iterations = st.iterations;
+        stats->outer_iterations = 1;
+        stats->converged = st.converged;
+        stats->reresid = st.reresid;
+        stats->unknowns = st.unknowns;
+    }
+    return st.converged ? GBP_OK : GBP_ERR_NOT_CONVERGED;
+}
+
+int gbp_project(gbp_scene *s, double dt, const float *solid, const float *fluid, float *u, float *v, float *w,
+                const gbp_params *params, float *pressure, gbp_stats *stats) {
+    return gbp_project_active(s, dt, solid, fluid, u, v, w, params, pressure, stats, NULL, NULL, NULL, NULL);
 }

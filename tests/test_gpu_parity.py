@@ -123,3 +123,29 @@ def test_reference_workload_128_divergence(gb):
     assert abs(pj.stats.iterations - want.iterations) <= max(3, int(0.1 * want.iterations))
     assert pj.stats.reresid <= 1e-6
     assert pj.stats.true_resid_inf <= 2e-6
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_active_sets_match_reference_fixture(gb, name):
+    """gbp_project_active: the cells whose pressure the reference sets and
+    the faces its velocity update leaves active (the rest are set_off) equal
+    the reference's own active sets, exactly, for the plain CG and the mixed
+    MGPCG solve alike (the sets depend on the fractions and the velocity
+    before the update, not on the solver)."""
+    c = Case(name)
+    for extra in ({}, {"Solver": "mgpcg", "Precision": "mixed"}):
+        if extra and (c.steps > 1 or c.params.get("max_iterations", 30000) < 30000):
+            continue
+        pj = gb.projector_for(c, **config_from(c.params, **extra))
+        for s in range(c.steps):
+            u, v, w = (None if a is None else a.copy() for a in c.inputs[s])
+            vel = (u, v, w) if c.dim == 3 else (u, v)
+            if c.volume is not None:
+                pj.set_target_volume(*c.volume[s])
+            pj.project(c.dt, vel, c.solid, c.fluid, active_sets=True)
+        assert np.array_equal(pj.unknown.astype(bool), c.out_unknown)
+        assert len(pj.active) == c.dim
+        for got, want, comp in zip(pj.active, c.out_active, vel):
+            assert np.array_equal(got.astype(bool), want), (name, extra)
+            assert not comp[~want].any()
+        pj.close()

@@ -3,7 +3,7 @@
 The golden fixtures were produced by the reference's macpressuresolver{2,3}
 built from its sources (tests/golden/make_golden.py). The restatement must
 reproduce them bit for bit: pressure, projected velocity, the set of unknown
-cells and the CG iteration count.
+cells, the faces left active and the CG iteration count.
 """
 import os
 
@@ -30,9 +30,26 @@ def test_port_matches_reference_fixture(name):
     assert np.array_equal(res.pressure, c.out_pressure)
     assert np.array_equal(res.u, c.out_u)
     assert np.array_equal(res.v, c.out_v)
+    for a, b in zip(res.active, c.out_active):
+        assert np.array_equal(a, b)
     if c.dim == 3:
         assert np.array_equal(res.w, c.out_w)
         assert res.iterations == c.iterations
+
+
+def test_fixtures_deactivate_closed_faces():
+    """The reference's velocity update turns closed faces off
+    (macpressuresolver3.cpp:264-266): in a liquid scene the faces in the air
+    are inactive after the projection, and every inactive face reads 0; in
+    2D a closed wall face stays active only where the flow leaves the domain
+    (macpressuresolver2.cpp:233-235)."""
+    c = Case("liquid3_16")
+    assert all((~a).sum() > a.size // 3 for a in c.out_active)
+    for a, u in zip(c.out_active, (c.out_u, c.out_v, c.out_w)):
+        assert not u[~a].any()
+    c = Case("liquid2_32")
+    on_wall = c.out_active[0][:, 0]
+    assert on_wall.any() and not on_wall.all()
 
 
 def test_known_answer_accuracy():
@@ -79,8 +96,7 @@ def test_plugin_module_loads_through_reference_loader(tmp_path):
     creates, configures and initializes it. (project() needs a GPU.)"""
     import subprocess
     root = oracle.HERE.rsplit("/", 1)[0]
-    subprocess.check_call(["make", "-s", "-C", f"{root}/shiokaze_gb300/module", f"OUT={oracle.REF_DIR}"],
-                          stdout=subprocess.DEVNULL)
+    oracle.build_modules(oracle.REF_DIR)
     lib = oracle._ref_lib()
     for dim in (3, 2):
         log = str(tmp_path / f"load{dim}.log")
@@ -99,8 +115,7 @@ def test_linsolver_module_loads_through_reference_loader(tmp_path):
     the GPU solver module in place of pcg. (solve() needs a GPU.)"""
     import subprocess
     root = oracle.HERE.rsplit("/", 1)[0]
-    subprocess.check_call(["make", "-s", "-C", f"{root}/shiokaze_gb300/module", f"OUT={oracle.REF_DIR}"],
-                          stdout=subprocess.DEVNULL)
+    oracle.build_modules(oracle.REF_DIR)
     lib = oracle._ref_lib()
     for dim in (3, 2):
         log = str(tmp_path / f"lin{dim}.log")
@@ -142,8 +157,7 @@ def test_advection_module_loads_through_reference_loader(tmp_path):
     if not oracle.reference_available():
         pytest.skip("reference oracle not built here")
     root = oracle.HERE.rsplit("/", 1)[0]
-    subprocess.check_call(["make", "-s", "-C", f"{root}/shiokaze_gb300/module", f"OUT={oracle.REF_DIR}"],
-                          stdout=subprocess.DEVNULL)
+    oracle.build_modules(oracle.REF_DIR)
     lib = oracle._ref_lib()
     log = str(tmp_path / "adv.log")
     assert lib.ref_advect_load(16, 16, 16, 1 / 16, b"Advection=gbadvection3 MacCormack=Yes TrimNarrowBand=2",
@@ -205,9 +219,8 @@ def test_advection_module_boundary_matches_reference_module(tmp_path):
     subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-I", f"{root}/include",
                            f"{root}/tests/module_stub/gbp_oracle_stub.c", "-o", str(stub), oracle.PORT_SO,
                            f"-Wl,-rpath,{oracle.HERE}"])
-    subprocess.check_call(["make", "-s", "-B", "-C", f"{root}/shiokaze_gb300/module", f"OUT={tmp_path}",
-                           f"LDFLAGS=-shared -L{tmp_path} -lgbp -Wl,-rpath,{tmp_path}",
-                           f"{tmp_path}/libshiokaze_gbadvection3.so"], stdout=subprocess.DEVNULL)
+    oracle.build_modules(str(tmp_path), f"{tmp_path}/libshiokaze_gbadvection3.so",
+                         ldflags=f"-shared -L{tmp_path} -lgbp -Wl,-rpath,{tmp_path}")
     shutil.copy(tmp_path / "libshiokaze_gbadvection3.so", os.path.join(oracle.REF_DIR,
                                                                       "libshiokaze_gbadvection3stub.so"))
     out = tmp_path / "module.npz"
@@ -233,9 +246,8 @@ def _stub_module(tmp_path, module, installed_as):
     subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-I", f"{root}/include",
                            f"{root}/tests/module_stub/gbp_oracle_stub.c", "-o", str(tmp_path / "libgbp.so"),
                            oracle.PORT_SO, f"-Wl,-rpath,{oracle.HERE}"])
-    subprocess.check_call(["make", "-s", "-B", "-C", f"{root}/shiokaze_gb300/module", f"OUT={tmp_path}",
-                           f"LDFLAGS=-shared -L{tmp_path} -lgbp -Wl,-rpath,{tmp_path}",
-                           f"{tmp_path}/libshiokaze_{module}.so"], stdout=subprocess.DEVNULL)
+    oracle.build_modules(str(tmp_path), f"{tmp_path}/libshiokaze_{module}.so",
+                         ldflags=f"-shared -L{tmp_path} -lgbp -Wl,-rpath,{tmp_path}")
     shutil.copy(tmp_path / f"libshiokaze_{module}.so", os.path.join(oracle.REF_DIR, f"libshiokaze_{installed_as}.so"))
     return root
 
@@ -280,3 +292,67 @@ def test_utility_module_constrain_matches_reference_module(tmp_path):
         d = dict(np.load(os.path.join(root, "tests/golden/constrain", name + ".npz")))
         for c in "uvw":
             assert np.array_equal(got[f"{name}_{c}"].view(np.uint32), d[f"out_{c}"].view(np.uint32)), (name, c)
+
+
+# runs in a process of its own, like the other module checks: the
+# replacement projection module is loaded by the reference's loader beside
+# the reference's own modules
+PROJECTION_MODULE_RUN = r"""
+import json, sys
+import numpy as np
+import oracle
+sys.path.insert(0, "tests")
+from golden_io import Case, case_names
+out = {}
+for name in case_names():
+    c = Case(name)
+    d = np.load(f"tests/golden/{name}.npz")
+    params = dict(c.params)
+    volume = params.pop("volume", None)
+    pj = oracle.RefProjector(c.dim, c.nx, c.ny, c.nz, c.dx, extra_kv=f"Projection=gbprojection{c.dim}stub", **params)
+    for s in range(c.steps):
+        u, v, w = c.inputs[s]
+        if c.volume is not None:
+            pj.set_target_volume(*c.volume[s])
+        r = pj.project(c.dt, c.solid, c.fluid, u, v, w, int(d["solid_mode"]), int(d["fluid_mode"]),
+                       float(d["band"]))
+    pj.close()
+    out[f"{name}/pressure"] = r.pressure
+    out[f"{name}/unknown"] = r.unknown
+    for comp, a, on in zip("uvw", (r.u, r.v, r.w), r.active):
+        out[f"{name}/{comp}"] = a
+        out[f"{name}/{comp}_on"] = on
+np.savez(sys.argv[1], **out)
+"""
+
+
+def test_projection_modules_match_reference_modules(tmp_path):
+    """gbprojection3 / gbprojection2 (Projection=gbprojection3|2) at their
+    boundary, on the CPU: linked to the oracle-backed stand-in for libgbp
+    and loaded by the reference's loader in place of macpressuresolver3 / 2
+    on the reference's own tiled arrays, they leave the reference modules'
+    output state on every golden case, bit for bit: the velocity values,
+    which faces stay active (the closed faces are set_off,
+    macpressuresolver3.cpp:264-266, 2D macpressuresolver2.cpp:233-235), the
+    pressure values and its active cells (every unknown, :245-248), over
+    warm-started and volume-corrected steps too."""
+    import subprocess
+    import sys
+    if not oracle.reference_available():
+        pytest.skip("reference oracle not built here")
+    root = _stub_module(tmp_path, "gbprojection3", "gbprojection3stub")
+    _stub_module(tmp_path, "gbprojection2", "gbprojection2stub")
+    out = tmp_path / "projection.npz"
+    r = subprocess.run([sys.executable, "-c", PROJECTION_MODULE_RUN, str(out)], cwd=root, capture_output=True,
+                       text=True, timeout=600, env=dict(os.environ, PYTHONPATH=root))
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    got = dict(np.load(out))
+    names = case_names()
+    assert len(names) >= 15
+    for name in names:
+        c = Case(name)
+        assert np.array_equal(got[f"{name}/unknown"], c.out_unknown), name
+        assert np.array_equal(got[f"{name}/pressure"].view(np.uint32), c.out_pressure.view(np.uint32)), name
+        for comp, want, on in zip("uvw", (c.out_u, c.out_v, c.out_w), c.out_active):
+            assert np.array_equal(got[f"{name}/{comp}"].view(np.uint32), want.view(np.uint32)), (name, comp)
+            assert np.array_equal(got[f"{name}/{comp}_on"], on), (name, comp)
