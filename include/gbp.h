@@ -248,9 +248,11 @@ int gbp_bench_kernel(gbp_scene *scene, int which, int reps, void *stream, float 
  * At most GBP_STATIC_MAX_CELLS cells (larger grids return
  * GBP_ERR_INVALID_ARGUMENT; gbp_strerror gives the reason); params->solver
  * must be GBP_SOLVER_CG with GBP_PRECISION_FP64, and warm start and volume
- * correction are not available (they need a scene's state). The first call
- * on a device looks up the array's device address once (make that first
- * call before any stream capture on that device). Every call shares the one
+ * correction are not available (they need a scene's state). Every call
+ * looks up the array's device address on the current device (the host-side
+ * name of a __device__ array is not a device address); the first call on a
+ * device also loads the library's module there, so make that first call
+ * before any stream capture on that device. Every call shares the one
  * array, which keeps the last call's contents: calls that overlap on the
  * GPU race, so callers must serialise them. No counterpart in the reference,
  * whose projection allocates on the host on every call. */

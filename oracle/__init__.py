@@ -34,7 +34,8 @@ REF_SO = os.path.join(REF_DIR, "libref_harness.so")
 def build_port(force: bool = False) -> str:
     srcs = [os.path.join(HERE, f) for f in ("gbp_oracle.c", "advect_oracle.c")]
     if force or not os.path.exists(PORT_SO) or os.path.getmtime(PORT_SO) < max(map(os.path.getmtime, srcs)):
-        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", *srcs, "-o", PORT_SO, "-lm"])
+        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", *srcs, "-o",
+                               PORT_SO, "-lm"])
     return PORT_SO
 
 
@@ -131,6 +132,7 @@ def _port_lib():
         fp = ctypes.POINTER(ctypes.c_float)
         dp = ctypes.POINTER(ctypes.c_double)
         lp = ctypes.POINTER(ctypes.c_longlong)
+        lib.oracle_set_threads.argtypes = [ctypes.c_int]
         lib.oracle_project.argtypes = [ctypes.c_void_p, ctypes.c_double, fp, fp, fp, fp, fp,
                                        ctypes.POINTER(_Params), fp, lp, ctypes.POINTER(_Stats)]
         u8 = ctypes.POINTER(ctypes.c_ubyte)
@@ -150,6 +152,16 @@ def _port_lib():
                                                    fp, fp, u8, u8, u8]
         _port = lib
     return _port
+
+
+def set_threads(n: int | None = None) -> int:
+    """Threads for the element-wise loops of the oracle's CG (matrix-vector
+    product, vector updates, maximum norm); its dot products stay serial in
+    index order, so results are bit-identical for every count. None: all
+    host cores. Returns the count set."""
+    n = int(n or os.cpu_count() or 1)
+    _port_lib().oracle_set_threads(n)
+    return n
 
 
 def make_params(residual=1e-6, max_iterations=30000, warm_start=False, eps_fluid=1e-2, eps_solid=1e-2,
@@ -192,6 +204,20 @@ class PortProjector:
                                        *([None] if w is None else []))
         return Result(p, u, v, w, idx >= 0, st.iterations, st.reresid, index=idx,
                       active=tuple(a.astype(bool) for a in on))
+
+    def face_fractions(self, solid, fluid):
+        """Open area and fluid fraction of every face (float32, shaped like
+        the velocity components), as the projection computes them
+        (macutility3.cpp:94-194 with this projector's eps and order flags)."""
+        solid, fluid = _f32(solid), _f32(fluid)
+        shapes = ([(self.nz, self.ny, self.nx + 1), (self.nz, self.ny + 1, self.nx), (self.nz + 1, self.ny, self.nx)]
+                  if self.dim == 3 else [(self.ny, self.nx + 1), (self.ny + 1, self.nx)])
+        area = [np.zeros(sh, np.float32) for sh in shapes]
+        rho = [np.zeros(sh, np.float32) for sh in shapes]
+        pa = [_ptr(a) for a in area] + [None] * (3 - self.dim)
+        pr = [_ptr(a) for a in rho] + [None] * (3 - self.dim)
+        self.lib.oracle_face_fractions(self.ctx, _ptr(solid), _ptr(fluid), ctypes.byref(self.params), *pa, *pr)
+        return area, rho
 
     def assemble(self, dt, solid, fluid, u, v, w=None):
         solid, fluid, u, v = _f32(solid), _f32(fluid), _f32(u), _f32(v)
@@ -431,6 +457,24 @@ class RefProjector:
         iters, rr = (int(m[-1][0]), float(m[-1][1])) if m else (-1, float("nan"))
         return Result(p, u, v, w, act.astype(bool), iters, rr, ms=ms,
                       active=tuple(a.astype(bool) for a in on if a is not None))
+
+
+def divergence(area, velocity, dx, unknown):
+    """max over the unknown cells of |sum over faces of sgn area u / dx| (the
+    discrete divergence the projection removes: the right-hand side of its
+    system with the sign flipped, macpressuresolver3.cpp:190-197), in FP64."""
+    div = np.zeros(unknown.shape, np.float64)
+    nd = len(velocity)
+    for d in range(nd):
+        f = area[d].astype(np.float64) * velocity[d].astype(np.float64)
+        ax = nd - 1 - d  # numpy axis of direction d (arrays are (z,) y, x)
+        hi = [slice(None)] * nd
+        lo = [slice(None)] * nd
+        hi[ax] = slice(1, None)
+        lo[ax] = slice(None, -1)
+        div += f[tuple(hi)] - f[tuple(lo)]
+    div /= dx
+    return float(np.max(np.abs(div[unknown]))) if unknown.any() else 0.0
 
 
 def project_scene(scene, impl="port", **params) -> Result:

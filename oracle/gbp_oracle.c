@@ -336,6 +336,114 @@ static void row_insert(long long *cols, double *vals, int *cnt, long long col, d
     (*cnt)++;
 }
 
+/* ---- worker threads for the element-wise loops of CG ----------------------- *
+ * The matrix-vector product (one row per index, each row summed in its own
+ * order), the vector updates and the maximum norm give the same bits however
+ * their index range is split, so they run on oracle_set_threads(n) threads;
+ * the dot products stay serial, in index order, as the reference sums them
+ * (cblas_ddot). Results are therefore bit-identical for every thread count. */
+#include <pthread.h>
+
+typedef void (*range_fn)(void *arg, long long lo, long long hi, int t);
+static struct {
+    int n;                      /* threads including the caller */
+    pthread_t th[64];
+    pthread_barrier_t start, done;
+    range_fn fn;
+    void *arg;
+    long long count;
+    int quit;
+} g_pool = {1};
+static double g_part[64];       /* per-thread partial maxima */
+
+static void pool_run_part(int t) {
+    const long long n = g_pool.count, per = (n + g_pool.n - 1) / g_pool.n;
+    const long long lo = per * t < n ? per * t : n, hi = lo + per < n ? lo + per : n;
+    g_pool.fn(g_pool.arg, lo, hi, t);
+}
+
+static void *pool_main(void *p) {
+    const int t = (int)(long long)p;
+    for (;;) {
+        pthread_barrier_wait(&g_pool.start);
+        if (g_pool.quit) return NULL;
+        pool_run_part(t);
+        pthread_barrier_wait(&g_pool.done);
+    }
+}
+
+/* Number of threads for the element-wise loops of CG (1 = all serial). */
+void oracle_set_threads(int n) {
+    if (n < 1) n = 1;
+    if (n > 64) n = 64;
+    if (g_pool.n > 1) {
+        g_pool.quit = 1;
+        pthread_barrier_wait(&g_pool.start);
+        for (int t = 1; t < g_pool.n; ++t) pthread_join(g_pool.th[t], NULL);
+        pthread_barrier_destroy(&g_pool.start);
+        pthread_barrier_destroy(&g_pool.done);
+        g_pool.quit = 0;
+    }
+    g_pool.n = n;
+    if (n > 1) {
+        pthread_barrier_init(&g_pool.start, NULL, (unsigned)n);
+        pthread_barrier_init(&g_pool.done, NULL, (unsigned)n);
+        for (int t = 1; t < n; ++t) pthread_create(&g_pool.th[t], NULL, pool_main, (void *)(long long)t);
+    }
+}
+
+static void pool_for(long long count, range_fn fn, void *arg) {
+    g_pool.fn = fn;
+    g_pool.arg = arg;
+    g_pool.count = count;
+    if (g_pool.n == 1 || count < 65536) {
+        for (int t = 0; t < g_pool.n; ++t) g_part[t] = 0.0;
+        fn(arg, 0, count, 0);
+        return;
+    }
+    pthread_barrier_wait(&g_pool.start);
+    pool_run_part(0);
+    pthread_barrier_wait(&g_pool.done);
+}
+
+typedef struct {
+    const csr *A;
+    double *x, *r, *s, *z;
+    double alpha, beta;
+} cg_args;
+
+static void spmv_range(void *p, long long lo, long long hi, int t) {
+    cg_args *a = (cg_args *)p;
+    (void)t;
+    for (long long i = lo; i < hi; ++i) {
+        double acc = 0;
+        for (long long e = a->A->rowstart[i]; e < a->A->rowstart[i + 1]; ++e) acc += a->A->val[e] * a->s[a->A->col[e]];
+        a->z[i] = acc;
+    }
+}
+
+/* x += alpha s; r += (-alpha) z; per-thread max |r| */
+static void update_range(void *p, long long lo, long long hi, int t) {
+    cg_args *a = (cg_args *)p;
+    double m = 0.0;
+    for (long long i = lo; i < hi; ++i) a->x[i] += a->alpha * a->s[i];
+    for (long long i = lo; i < hi; ++i) {
+        a->r[i] += (-a->alpha) * a->z[i];
+        if (fabs(a->r[i]) > m) m = fabs(a->r[i]);
+    }
+    g_part[t] = m;
+}
+
+/* z = r + beta s */
+static void direction_range(void *p, long long lo, long long hi, int t) {
+    cg_args *a = (cg_args *)p;
+    (void)t;
+    for (long long i = lo; i < hi; ++i) {
+        a->z[i] = a->r[i];
+        a->z[i] += a->beta * a->s[i];
+    }
+}
+
 /* PCGSolver<double>::solve with the identity preconditioner
  * (pcg_solver.h:246-295, :379-384). x is zeroed first. */
 static void cg_solve(const csr *A, const double *b, double *x, const oracle_params *prm, oracle_stats *st) {
@@ -361,19 +469,18 @@ static void cg_solve(const csr *A, const double *b, double *x, const oracle_para
     if (rho == 0.0 || rho != rho) { st->converged = 0; free(r); free(s); free(z); return; }
     for (long long i = 0; i < n; ++i) s[i] = z[i];
     int it;
+    cg_args ca = {A, x, r, s, z, 0.0, 0.0};
     for (it = 0; it < prm->max_iterations; ++it) {
-        for (long long i = 0; i < n; ++i) {
-            double acc = 0;
-            for (long long e = A->rowstart[i]; e < A->rowstart[i + 1]; ++e) acc += A->val[e] * s[A->col[e]];
-            z[i] = acc;
-        }
+        ca.s = s;
+        ca.z = z;
+        pool_for(n, spmv_range, &ca);
         double sz = 0.0;
         for (long long i = 0; i < n; ++i) sz += s[i] * z[i];
         double alpha = rho / sz;
-        for (long long i = 0; i < n; ++i) x[i] += alpha * s[i];
-        for (long long i = 0; i < n; ++i) r[i] += (-alpha) * z[i];
+        ca.alpha = alpha;
+        pool_for(n, update_range, &ca);
         res = 0.0;
-        for (long long i = 0; i < n; ++i) if (fabs(r[i]) > res) res = fabs(r[i]);
+        for (int t = 0; t < g_pool.n; ++t) if (g_part[t] > res) res = g_part[t];
         if (res <= tol) {
             st->iterations = it + 1;
             st->reresid = res / res0;
@@ -381,11 +488,11 @@ static void cg_solve(const csr *A, const double *b, double *x, const oracle_para
             free(r); free(s); free(z);
             return;
         }
-        for (long long i = 0; i < n; ++i) z[i] = r[i];
         double rho_new = 0.0;
-        for (long long i = 0; i < n; ++i) rho_new += z[i] * r[i];
+        for (long long i = 0; i < n; ++i) rho_new += r[i] * r[i];
         double beta = rho_new / rho;
-        for (long long i = 0; i < n; ++i) z[i] += beta * s[i];
+        ca.beta = beta;
+        pool_for(n, direction_range, &ca);
         double *t = s; s = z; z = t; /* s = beta*s + z */
         rho = rho_new;
     }

@@ -299,7 +299,11 @@ double volume_correction(gbp_scene *s, double dt, const gbp_params &p) {
     return -(kp * x + ki * y) / (x + 1.0);
 }
 
-int validate(const gbp_params &p) {
+}  // namespace
+
+namespace gbp {
+// Parameter checks shared by every projection entry point.
+int validate_params(const gbp_params &p) {
     if (!(p.residual >= 0.0) || p.max_iterations < 0 || !(p.eps_fluid >= 0.0) || !(p.eps_solid >= 0.0))
         return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_params: negative residual, eps or max_iterations");
     if (p.solver != GBP_SOLVER_CG && p.solver != GBP_SOLVER_MGPCG)
@@ -310,6 +314,9 @@ int validate(const gbp_params &p) {
         return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_params: mixed precision needs the MGPCG solver");
     return GBP_OK;
 }
+}  // namespace gbp
+
+namespace {
 
 int ensure_active_sets(gbp_scene *s) {
     const Grid &g = s->g;
@@ -324,7 +331,7 @@ int project_device(gbp_scene *s, double dt, const float *solid, const float *flu
                    bool active_sets = false) {
     gbp_ctx *c = s->ctx;
     const Grid &g = s->g;
-    int rc = validate(p);
+    int rc = gbp::validate_params(p);
     if (rc) return rc;
     if (!solid || !fluid || !u || !v || (g.dim == 3 && !w) || !pressure)
         return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_project: NULL array");
@@ -511,7 +518,7 @@ int gbp_batch_project_device(gbp_batch *b, const double *dt, const float *const 
     gbp_params p;
     gbp_params_default(&p);
     if (params) p = *params;
-    int rc = validate(p);
+    int rc = gbp::validate_params(p);
     if (rc) return rc;
     if (p.solver != GBP_SOLVER_MGPCG) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_batch_project_device: MGPCG only");
     GBP_CUDA(cudaSetDevice(c->device));
@@ -643,7 +650,7 @@ int gbp_debug_assemble(gbp_scene *s, double dt, const float *solid, const float 
     gbp_params p;
     gbp_params_default(&p);
     if (params) p = *params;
-    int rc = validate(p);
+    int rc = gbp::validate_params(p);
     if (rc) return rc;
     GBP_CUDA(cudaSetDevice(s->ctx->device));
     rc = ensure_staging(s);

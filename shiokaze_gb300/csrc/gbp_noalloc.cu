@@ -19,7 +19,6 @@
 // caller serialises them. What must start at zero (the scalars block with
 // the reduction tickets) is cleared by every call.
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "gbp.h"
@@ -27,7 +26,8 @@
 #include "gbp_kernels.h"
 
 namespace gbp {
-void set_last_error(const std::string &msg);  // gbp_api.cpp
+void set_last_error(const std::string &msg);   // gbp_api.cpp
+int validate_params(const gbp_params &p);      // gbp_api.cpp: the checks of every projection entry point
 }
 
 namespace {
@@ -43,11 +43,6 @@ static_assert(kScratchBytes <= GBP_STATIC_SCRATCH_BYTES, "static scratch too sma
 
 static __device__ __align__(256) unsigned char g_static_scratch[GBP_STATIC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-void *g_scratch_addr[kMaxDevices] = {};
-int g_sm_count[kMaxDevices] = {};
-
 int fail(int code, const std::string &m) {
     gbp::set_last_error(m);  // reported by gbp_strerror(code)
     return code;
@@ -59,21 +54,17 @@ int fail(int code, const std::string &m) {
         if (e_ != cudaSuccess) return fail(GBP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-// Device address of g_static_scratch on the current device (set up once per
-// device; the host-side name is not a device address).
+// Device address of g_static_scratch on the current device. The host-side
+// name is only a stand-in, not a device address, so the address is looked
+// up on every call (cheap, and it allocates nothing): a cached one would go
+// stale if the device's context were reset and the module loaded again.
 int scratch_for_device(int device, unsigned char **addr, int *sms) {
-    if (device < 0 || device >= kMaxDevices) return fail(GBP_ERR_NO_DEVICE, "gbp_project_device_static: device id");
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_addr[device]) {
-        void *p = nullptr;
-        NOALLOC_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
-        int n = 0;
-        NOALLOC_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device));
-        g_scratch_addr[device] = p;
-        g_sm_count[device] = n;
-    }
-    *addr = static_cast<unsigned char *>(g_scratch_addr[device]);
-    *sms = g_sm_count[device];
+    void *p = nullptr;
+    NOALLOC_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
+    int n = 0;
+    NOALLOC_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device));
+    *addr = static_cast<unsigned char *>(p);
+    *sms = n;
     return GBP_OK;
 }
 
@@ -92,12 +83,12 @@ extern "C" int gbp_project_device_static(int dim, int nx, int ny, int nz, double
     gbp_params p;
     gbp_params_default(&p);
     if (params) p = *params;
+    int rc = gbp::validate_params(p);
+    if (rc) return rc;
     if (p.solver != GBP_SOLVER_CG || p.precision != GBP_PRECISION_FP64)
         return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_project_device_static: only the plain FP64 CG solver");
     if (p.warm_start)
         return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_project_device_static: warm start needs a scene (gbp_scene_create)");
-    if (!(p.residual >= 0.0) || p.max_iterations < 0)
-        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_project_device_static: bad residual or max_iterations");
     if (!solid || !fluid || !u || !v || (dim == 3 && !w) || !pressure)
         return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_project_device_static: NULL array");
 
@@ -105,7 +96,7 @@ extern "C" int gbp_project_device_static(int dim, int nx, int ny, int nz, double
     NOALLOC_CUDA(cudaGetDevice(&device));
     unsigned char *base = nullptr;
     int sms = 0;
-    int rc = scratch_for_device(device, &base, &sms);
+    rc = scratch_for_device(device, &base, &sms);
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
 
