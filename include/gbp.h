@@ -211,6 +211,21 @@ int gbp_debug_assemble(gbp_scene *scene, double dt, const float *solid, const fl
                        const float *v, const float *w, const gbp_params *params, double *diag, double *cx,
                        double *cy, double *cz, double *b);
 
+/* Test hook for the bounded device waits (no counterpart in the reference):
+ * in the scene's next MGPCG solve, block `block` of the kernels named by
+ * `what` leaves out its part -- GBP_WAIT_GRID_BARRIER: its arrival at the
+ * grid-wide barriers of the cooperative coarse-level kernels;
+ * GBP_WAIT_TILE: the copies of its first tile in the TMA-staged fine-level
+ * kernels (gbp_params.tma_staging) -- and every bounded wait polls at most
+ * `polls` times (1..2^24; the defaults are 2^24 and 2^22 polls, about a
+ * second). The waits of the other blocks (or of that block) then run out,
+ * the kernels record it and return, and the solve returns GBP_ERR_CUDA with
+ * a message naming the wait; the context stays usable and the next solve
+ * runs normally. Nothing faults and nothing waits without a limit. */
+#define GBP_WAIT_GRID_BARRIER 1
+#define GBP_WAIT_TILE 2
+int gbp_debug_fail_wait(gbp_scene *scene, int what, int block, int polls);
+
 /* Benchmark hook: times `reps` back-to-back launches of one kernel on the
  * scene's last assembled system with CUDA events on `stream` (NULL = the
  * context's stream), after one untimed launch. which: GBP_KERNEL_*. Writes

@@ -32,9 +32,16 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgbp.so")
 
+# status codes of include/gbp.h
 GBP_OK = 0
+GBP_ERR_INVALID_ARGUMENT = 1
+GBP_ERR_CUDA = 2
+GBP_ERR_OUT_OF_MEMORY = 3
 GBP_ERR_NOT_CONVERGED = 4
 GBP_ERR_NAN = 5
+GBP_ERR_NO_DEVICE = 6
+GBP_ERR_BUDGET = 7
+GBP_ERR_TIMEOUT = 8
 SOLVER_CG, SOLVER_MGPCG = 0, 1
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 

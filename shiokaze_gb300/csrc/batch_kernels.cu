@@ -823,13 +823,18 @@ __device__ __forceinline__ bool grid_barrier(BatchCounters *cnt) {
         const unsigned g = *gen;
         __threadfence();
         int good = 1;
-        if (atomicAdd(&cnt->bar_count, 1u) == gridDim.x - 1) {
+        const int limit = cnt->test_polls > 0 ? cnt->test_polls : (1 << 24);
+        if (cnt->test_what == 1 && (int)blockIdx.x == cnt->test_block) {
+            // test hook: this block never arrives (as if it had stopped);
+            // the others' waits run out
+            good = 0;
+        } else if (atomicAdd(&cnt->bar_count, 1u) == gridDim.x - 1) {
             cnt->bar_count = 0;
             __threadfence();
             atomicAdd(&cnt->bar_gen, 1u);
         } else {
             for (int it = 0; *gen == g; ++it) {
-                if (it > (1 << 24)) {
+                if (it > limit) {
                     good = 0;
                     atomicExch(&cnt->bar_err, 1);
                     break;
@@ -1775,9 +1780,10 @@ __device__ __forceinline__ void mbar_init(unsigned long long *b) {
 __device__ __forceinline__ void mbar_expect(unsigned long long *b, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
 }
-// Bounded wait for the phase of the given parity (about a second at most).
-__device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity) {
-    for (int it = 0; it < (1 << 22); ++it) {
+// Bounded wait for the phase of the given parity (about a second at most
+// with the default limit of 2^22 polls).
+__device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity, int limit) {
+    for (int it = 0; it < limit; ++it) {
         unsigned done;
         asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.b32 %0, 1, 0, p; }"
                      : "=r"(done)
@@ -1890,8 +1896,14 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 1)
             tma_box(dst + bx.off, L.tmap + bx.map, x, y, z, &bar[s]);
         }
     };
+    const int polls = cnt->test_polls > 0 ? cnt->test_polls : (1 << 22);
     if (tid == 0) {
-        if (blockIdx.x < n) issue(0, blockIdx.x);
+        if (blockIdx.x < n) {
+            if (cnt->test_what == 2 && (int)blockIdx.x == cnt->test_block)
+                valid[0] = 1;  // test hook: the first tile is awaited but never copied
+            else
+                issue(0, blockIdx.x);
+        }
         if (blockIdx.x + G < n) issue(1, blockIdx.x + G);
     }
     __syncthreads();
@@ -1944,11 +1956,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 1)
             acc.reset();
         }
         if (valid[s]) {
-            const bool ok = mbar_wait(&bar[s], (phase >> s) & 1u);
+            const bool ok = mbar_wait(&bar[s], (phase >> s) & 1u, polls);
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) {
                     atomicExch(&cnt->bar_err, 2);
-                    if (w + G < n && valid[s ^ 1]) mbar_wait(&bar[s ^ 1], (phase >> (s ^ 1)) & 1u);
+                    if (w + G < n && valid[s ^ 1]) mbar_wait(&bar[s ^ 1], (phase >> (s ^ 1)) & 1u, polls);
                 }
                 return;
             }

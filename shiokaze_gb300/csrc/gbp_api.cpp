@@ -640,6 +640,15 @@ int gbp_bench_kernel(gbp_scene *s, int which, int reps, void *stream, float *ms_
     return GBP_OK;
 }
 
+int gbp_debug_fail_wait(gbp_scene *s, int what, int block, int polls) {
+    if (!s || !s->solver) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_debug_fail_wait: NULL scene");
+    if ((what != GBP_WAIT_GRID_BARRIER && what != GBP_WAIT_TILE) || block < 0 || polls < 1 || polls > (1 << 24))
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_debug_fail_wait: what must be GBP_WAIT_GRID_BARRIER or "
+                                              "GBP_WAIT_TILE, block >= 0 and polls in [1, 2^24]");
+    s->solver->set_wait_test(what, block, polls);
+    return GBP_OK;
+}
+
 int gbp_debug_assemble(gbp_scene *s, double dt, const float *solid, const float *fluid, const float *u,
                        const float *v, const float *w, const gbp_params *params, double *diag, double *cx,
                        double *cy, double *cz, double *b) {

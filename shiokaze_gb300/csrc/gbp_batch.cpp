@@ -530,6 +530,10 @@ template <class T> int BatchRunner::solve(const gbp_params &p, cudaStream_t st, 
     auto *sc = static_cast<const BScene<T> *>(d_scenes_);
     std::memset(h_counters_, 0, sizeof(BatchCounters));
     h_counters_->remaining = nscenes_;
+    h_counters_->test_what = test_what_;
+    h_counters_->test_block = test_block_;
+    h_counters_->test_polls = test_polls_;
+    test_what_ = test_block_ = test_polls_ = 0;  // one solve only
     RUN_CUDA(cudaMemcpyAsync(d_counters_, h_counters_, sizeof(BatchCounters), cudaMemcpyHostToDevice, st));
     // initial residual of every scene (also zeroes x64, sets thresholds)
     RUN_CUDA(b_refine_residual<T>(BLaunch{blocks_for(n_fine_pairs_, grid_blocks_), st, 0, d_scene_of_, d_counters_}, lv,

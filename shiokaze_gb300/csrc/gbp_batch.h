@@ -140,7 +140,14 @@ struct BatchCounters {
     unsigned bar_count;   // grid barrier of the coarse-level kernels: arrivals
     unsigned bar_gen;     // ... and generation
     int bar_err;          // a barrier wait ran out (the solve is abandoned)
-    int pad[3];
+    // test hook (gbp_debug_fail_wait), 0 in every ordinary solve: block
+    // test_block of the kernels named by test_what (1: the cooperative
+    // coarse kernels' grid barriers, 2: the TMA-staged fine kernels' tile
+    // waits) leaves out its arrival / the copies of its first tile, and
+    // every bounded wait polls at most test_polls times (0: the default)
+    int test_what;
+    int test_block;
+    int test_polls;
 };
 
 // Work lists of the global coarse levels [first, last] (first >= 1), run by
@@ -213,8 +220,16 @@ public:
         return stage_mask_ && s >= 0 && s < (int)staged_scene_.size() && staged_scene_[s];
     }
     int stage_mask() const { return stage_mask_; }
+    // Test hook for the next solve only (see BatchCounters::test_what):
+    // makes one block's bounded waits run out, polling at most `polls`.
+    void set_wait_test(int what, int block, int polls) {
+        test_what_ = what;
+        test_block_ = block;
+        test_polls_ = polls;
+    }
 
 private:
+    int test_what_ = 0, test_block_ = 0, test_polls_ = 0;
     int fail(int code, const std::string &m) {
         err_ = m;
         return code;

@@ -68,6 +68,8 @@ public:
     bool has_prev() const { return st_.have_prev; }
     // the last single-scene MGPCG solve ran the TMA-staged fine kernels
     bool staged() const { return runner_key_ >= 0 && runner_.scene_staged(0); }
+    // test hook of gbp_debug_fail_wait: the next MGPCG solve's waits run out
+    void set_wait_test(int what, int block, int polls) { runner_.set_wait_test(what, block, polls); }
 
 private:
     int fail(int code, const std::string &m) {
