@@ -464,10 +464,11 @@ def divergence(area, velocity, dx, unknown):
     discrete divergence the projection removes: the right-hand side of its
     system with the sign flipped, macpressuresolver3.cpp:190-197), in FP64."""
     div = np.zeros(unknown.shape, np.float64)
-    nd = len(velocity)
-    for d in range(nd):
-        f = area[d].astype(np.float64) * velocity[d].astype(np.float64)
-        ax = nd - 1 - d  # numpy axis of direction d (arrays are (z,) y, x)
+    for d in range(len(velocity)):
+        f = area[d].astype(np.float64) * velocity[d].astype(np.float64).reshape(area[d].shape)
+        f = f.reshape(f.shape[:0] + (1,) * (unknown.ndim - f.ndim) + f.shape)
+        nd = f.ndim
+        ax = nd - 1 - d  # numpy axis of direction d (arrays are (z,) y, x, x fastest)
         hi = [slice(None)] * nd
         lo = [slice(None)] * nd
         hi[ax] = slice(1, None)
