@@ -329,6 +329,37 @@ int gbp_constrain_velocity3_device(gbp_ctx *ctx, int nx, int ny, int nz, double 
 int gbp_constrain_velocity3(gbp_ctx *ctx, int nx, int ny, int nz, double dx, const float *solid, float *u, float *v,
                             float *w, const unsigned char *mu, const unsigned char *mv, const unsigned char *mw);
 
+/* Extrapolation of an array into its inactive cells: replaces
+ *   array_extrapolator3::extrapolate(array, count)
+ *     include/shiokaze/array/array_extrapolator3.h:36-73
+ *   as the reference's tiled array runs it (array3::dilate,
+ *   src/array/dilate3.h:43-95).
+ * `count` rounds; each activates every inactive in-bounds 6-neighbour of an
+ * active cell with the float mean of its active neighbours (summed in the
+ * order +x, -x, +y, -y, -z, +z), all values of a round computed from the
+ * state before it. a (w*h*d floats, x fastest) and active (1 = active) are
+ * in/out; *activated (may be NULL) receives the number of cells activated,
+ * the count the reference returns. Results equal the reference's bit for
+ * bit. */
+int gbp_extrapolate3_device(gbp_ctx *ctx, int w, int h, int d, float *a, unsigned char *active, int count,
+                            long long *activated, void *stream);
+int gbp_extrapolate3(gbp_ctx *ctx, int w, int h, int d, float *a, unsigned char *active, int count,
+                     long long *activated);
+
+/* The velocity extrapolated by `width` rounds, component by component, then
+ * the solid constraint: replaces
+ *   macutility3_interface::extrapolate_and_constrain_velocity(solid, velocity, width)
+ *   as implemented by src/utility/macutility3.cpp:88-92
+ *   (macarray_extrapolator3::extrapolate, macarray_extrapolator3.h:44-48,
+ *   then constrain_velocity over the grown active set).
+ * HOST arrays as for gbp_constrain_velocity3, inactive faces holding 0;
+ * mu, mv, mw mark the active faces and are updated to the grown sets (all
+ * three NULL: every face is active and only the constraint acts). Results
+ * equal the reference's bit for bit. */
+int gbp_extrapolate_constrain_velocity3(gbp_ctx *ctx, int nx, int ny, int nz, double dx, const float *solid,
+                                        float *u, float *v, float *w, unsigned char *mu, unsigned char *mv,
+                                        unsigned char *mw, int width);
+
 /* Number of kernel launches this context has issued (graph nodes count one
  * each). */
 long long gbp_launch_count(gbp_ctx *ctx);

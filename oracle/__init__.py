@@ -267,6 +267,9 @@ def _ref_lib():
         lib.ref_extrapolate3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, u8, ctypes.c_int]
         lib.ref_constrain3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_char_p,
                                        fp, ctypes.c_int, ctypes.c_float, fp, fp, fp, u8, u8, u8, ctypes.c_char_p]
+        lib.ref_extrapolate_constrain3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                   ctypes.c_char_p, fp, ctypes.c_int, ctypes.c_float, fp, fp, fp,
+                                                   u8, u8, u8, ctypes.c_int, ctypes.c_char_p]
         lib.ref_densify_compare.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, ctypes.c_int,
                                             ctypes.c_float, ctypes.c_int, fp, fp, dp, dp]
         _ref = lib
@@ -352,6 +355,36 @@ def constrain3(solid, u, v, w, dx, masks=(None, None, None), impl="port", solid_
         if rc:
             raise ValueError("oracle_constrain_velocity3: grid too small")
     return uo, vo, wo
+
+
+def extrapolate_constrain3(solid, u, v, w, dx, masks, width, impl="port", solid_mode=0, band=0.0, extra_kv=""):
+    """macutility3::extrapolate_and_constrain_velocity: each velocity
+    component extrapolated `width` rounds over its active faces (masks),
+    then the solid constraint over the grown sets. Inactive faces hold 0.
+    Returns (u, v, w, masks). port: oracle_extrapolate3 per component, then
+    oracle_constrain_velocity3; reference: the reference's module through
+    its loader (extra_kv may select another MacUtility module)."""
+    comps = [np.array(a, dtype=np.float32, order="C") for a in (u, v, w)]
+    ms = [np.array(m, dtype=np.uint8, order="C") for m in masks]
+    sl = np.ascontiguousarray(solid, dtype=np.float32)
+    nz, ny, nx = (d - 1 for d in sl.shape)
+    u8 = ctypes.c_ubyte
+    if impl == "reference":
+        lib = _ref_lib()
+        log = tempfile.NamedTemporaryFile(prefix="ref_extc_", suffix=".log", delete=False).name
+        try:
+            lib.ref_extrapolate_constrain3(nx, ny, nz, dx, extra_kv.encode(), _ptr(sl), solid_mode, band,
+                                           *[_ptr(c) for c in comps], *[_ptr(m, u8) for m in ms], int(width),
+                                           log.encode())
+        finally:
+            os.unlink(log)
+        return comps[0], comps[1], comps[2], tuple(ms)
+    lib = _port_lib()
+    for c, m in zip(comps, ms):
+        d, h, wd = c.shape
+        lib.oracle_extrapolate3(wd, h, d, _ptr(c), _ptr(m, u8), int(width))
+    lib.oracle_constrain_velocity3(nx, ny, nz, dx, _ptr(sl), *[_ptr(c) for c in comps], *[_ptr(m, u8) for m in ms])
+    return comps[0], comps[1], comps[2], tuple(ms)
 
 
 def extrapolate3(values, active, count=1, impl="port"):

@@ -481,6 +481,51 @@ int ref_constrain3(int nx, int ny, int nz, double dx, const char *kv, const floa
     return 1;
 }
 
+/* macutility3::extrapolate_and_constrain_velocity (src/utility/
+ * macutility3.cpp:88-92) through the module loader (kv may select another
+ * MacUtility module): the velocity holds comp values on the faces marked in
+ * mu/mv/mw (in/out: the active sets after the call); the solid as in
+ * ref_constrain3. Values read back through operator(). */
+int ref_extrapolate_constrain3(int nx, int ny, int nz, double dx, const char *kv, const float *solid, int solid_mode,
+                               float solid_band, float *u, float *v, float *w, unsigned char *mu, unsigned char *mv,
+                               unsigned char *mw, int width, const char *log_path) {
+    configuration &config = install_global_config(kv);
+    shape3 s(nx, ny, nz);
+    double dxv = dx;
+    with_stdout_to(log_path, [&]() {
+        macutility3_driver util("macutility3");
+        util.set_environment("shape", &s);
+        util.set_environment("dx", &dxv);
+        util.setup_now(config);
+        array3<Real> solid_a;
+        fill_levelset3(solid_a, s.nodal(), solid, solid_mode, solid_band);
+        macarray3<Real> vel(s);
+        float *comp[3] = {u, v, w};
+        unsigned char *mask[3] = {mu, mv, mw};
+        for (int d = 0; d < 3; ++d) {
+            const shape3 fs = s.face(d);
+            for (int k = 0; k < (int)fs.d; ++k)
+                for (int j = 0; j < (int)fs.h; ++j)
+                    for (int i = 0; i < (int)fs.w; ++i) {
+                        const size_t n = i + (size_t)fs.w * (j + (size_t)fs.h * k);
+                        if (mask[d][n]) vel[d].set(i, j, k, comp[d][n]);
+                    }
+        }
+        util->extrapolate_and_constrain_velocity(solid_a, vel, width);
+        for (int d = 0; d < 3; ++d) {
+            const shape3 fs = s.face(d);
+            for (int k = 0; k < (int)fs.d; ++k)
+                for (int j = 0; j < (int)fs.h; ++j)
+                    for (int i = 0; i < (int)fs.w; ++i) {
+                        const size_t n = i + (size_t)fs.w * (j + (size_t)fs.h * k);
+                        comp[d][n] = vel[d](i, j, k);
+                        mask[d][n] = vel[d].active(i, j, k) ? 1 : 0;
+                    }
+        }
+    });
+    return 1;
+}
+
 /* The reference's array_extrapolator3::extrapolate on a dense 3D array of
  * shape w x h x d: active where active[c] != 0 (values elsewhere ignored;
  * the array's background is 0), `count` rounds. On return, a holds the

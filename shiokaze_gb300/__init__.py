@@ -152,6 +152,11 @@ def load_library():
                                             fp, u8p, u8p, u8p]
     lib.gbp_constrain_velocity3_device.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, vp,
                                                    vp, vp, vp, vp, vp, vp, vp]
+    lib.gbp_extrapolate3.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, u8p, ctypes.c_int, lp]
+    lib.gbp_extrapolate3_device.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, ctypes.c_int, lp,
+                                            vp]
+    lib.gbp_extrapolate_constrain_velocity3.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                        ctypes.c_double, fp, fp, fp, fp, u8p, u8p, u8p, ctypes.c_int]
     lib.gbp_launch_count.argtypes = [vp]
     lib.gbp_launch_count.restype = ctypes.c_longlong
     lib.gbp_strerror.argtypes = [ctypes.c_int]
@@ -599,6 +604,53 @@ class MacUtility3:
         ms = [None if m is None else np.ascontiguousarray(m, dtype=np.uint8) for m in masks]
         mp = [None if m is None else m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)) for m in ms]
         check(self.lib.gbp_constrain_velocity3(self.ctx.handle, self.nx, self.ny, self.nz, self.dx, sp, *ptrs, *mp))
+
+    def extrapolate(self, values, active, count, stream=None):
+        """array_extrapolator3::extrapolate (array_extrapolator3.h:36-73) of
+        one array (z, y, x) with its active mask (uint8), both in place:
+        `count` rounds, each activating every inactive neighbour of an active
+        cell with the float mean of its active neighbours. numpy arrays go
+        through the host call, torch CUDA tensors through the device call.
+        Returns the number of cells activated (the reference's count)."""
+        d, h, w = values.shape
+        added = ctypes.c_longlong(0)
+        if _is_torch_cuda(values):
+            import torch
+            assert values.dtype == torch.float32 and values.is_contiguous(), "values: contiguous float32"
+            assert active.dtype == torch.uint8 and active.is_contiguous() and active.numel() == values.numel()
+            st = stream if stream is not None else torch.cuda.current_stream(values.device).cuda_stream
+            check(self.lib.gbp_extrapolate3_device(self.ctx.handle, w, h, d, values.data_ptr(), active.data_ptr(),
+                                                   int(count), ctypes.byref(added), ctypes.c_void_p(st)))
+            return added.value
+        if not (isinstance(values, np.ndarray) and values.dtype == np.float32 and values.flags.c_contiguous):
+            raise TypeError("values must be a contiguous float32 numpy array (updated in place)")
+        if not (isinstance(active, np.ndarray) and active.dtype == np.uint8 and active.flags.c_contiguous
+                and active.size == values.size):
+            raise TypeError("active must be a contiguous uint8 numpy array of the same size (updated in place)")
+        check(self.lib.gbp_extrapolate3(self.ctx.handle, w, h, d, values.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                        active.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), int(count),
+                                        ctypes.byref(added)))
+        return added.value
+
+    def extrapolate_and_constrain_velocity(self, solid, velocity, masks, width):
+        """macutility3::extrapolate_and_constrain_velocity
+        (src/utility/macutility3.cpp:88-92) on host arrays, in place: each
+        component grown `width` rounds over its inactive faces (masks: uint8
+        active faces, updated to the grown sets; inactive faces hold 0),
+        then the solid constraint over the grown sets."""
+        self._check_sizes(solid, velocity, masks)
+        ptrs = []
+        for a in velocity:
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
+                raise TypeError("host arrays must be contiguous float32 numpy arrays (updated in place)")
+            ptrs.append(a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        for m in masks:
+            if not (isinstance(m, np.ndarray) and m.dtype == np.uint8 and m.flags.c_contiguous):
+                raise TypeError("masks must be contiguous uint8 numpy arrays (updated in place)")
+        sa, sp = _host_f32(solid)
+        mp = [m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)) for m in masks]
+        check(self.lib.gbp_extrapolate_constrain_velocity3(self.ctx.handle, self.nx, self.ny, self.nz, self.dx, sp,
+                                                           *ptrs, *mp, int(width)))
 
 
 def projector_for(scene, context: Context | None = None, **config):

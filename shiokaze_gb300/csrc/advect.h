@@ -21,6 +21,12 @@ struct AdvectWork {
     float *q0 = nullptr;   // forward scalar
     gba::MinMax *qmm = nullptr;  // limiter record per cell
     int *flag = nullptr;         // the solid constraint's levelset_exist flag
+    // extrapolation: the second value and mask buffers of a dilation round,
+    // and the counter of cells it activated
+    long long ext_cap = 0;
+    float *ext_a = nullptr;
+    unsigned char *ext_m = nullptr;
+    unsigned long long *ext_count = nullptr;
 };
 
 cudaError_t advect_reserve(AdvectWork &w, long long faces, long long cells);
@@ -53,5 +59,18 @@ struct ConstrainArgs {
     const unsigned char *mu, *mv, *mw;
 };
 cudaError_t constrain_run(AdvectWork &w, const ConstrainArgs &a, cudaStream_t stream, long long *launches);
+
+// array_extrapolator3::extrapolate (include/shiokaze/array/
+// array_extrapolator3.h:36-73) on a dense W x H x D device array a with its
+// active mask m, as the reference's tiled array runs it (array3::dilate,
+// src/array/dilate3.h:43-95): `count` rounds, each activating every
+// inactive in-bounds 6-neighbour of an active cell with the float mean of
+// its active neighbours, summed in the order +x, -x, +y, -y, -z, +z, all
+// computed from the state before the round. One launch per round into the
+// second buffers (held in w), then the roles swap; the result ends in a and
+// m. When activated_host is not null, the number of cells activated is
+// copied there (valid once the stream is synchronised).
+cudaError_t extrapolate_run(AdvectWork &w, int W, int H, int D, float *a, unsigned char *m, int count,
+                            cudaStream_t stream, long long *launches, unsigned long long *activated_host);
 
 }  // namespace gbp

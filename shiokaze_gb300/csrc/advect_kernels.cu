@@ -20,6 +20,7 @@
 // (counted once, 12). The arithmetic is the reference's: trilinear weights
 // and sums in FP64 on every trace (three per face, two per cell), which on
 // this GPU's FP64 pipe, not DRAM, bounds the kernels.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 
@@ -116,6 +117,9 @@ cudaError_t advect_reserve(AdvectWork &w, long long faces, long long cells) {
 }
 
 void advect_release(AdvectWork &w) {
+    cudaFree(w.ext_a);
+    cudaFree(w.ext_m);
+    cudaFree(w.ext_count);
     cudaFree(w.flag);
     cudaFree(w.v0);
     cudaFree(w.vmm);
@@ -177,6 +181,91 @@ cudaError_t advect_run(AdvectWork &w, const AdvectArgs &a, cudaStream_t st, long
         }
     }
     return cudaGetLastError();
+}
+
+// One dilation round of the extrapolation (see extrapolate_run), one thread
+// per cell: an active cell keeps its value; an inactive one with active
+// neighbours takes sum / weight, the float sum in the reference's neighbour
+// order (array_extrapolator3.h:50-60) divided by the count; the rest keep
+// their value and stay inactive. Activations are counted per warp.
+__global__ void __launch_bounds__(256) ext_round(int W, int H, int D, const float *__restrict__ ain,
+                                                 const unsigned char *__restrict__ min, float *__restrict__ aout,
+                                                 unsigned char *__restrict__ mout, unsigned long long *added) {
+    const long long n = (long long)W * H * D, sy = W, sz = (long long)W * H;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += (long long)gridDim.x * blockDim.x) {
+        const long long c = base + threadIdx.x;
+        bool newly = false;
+        if (c < n) {
+            unsigned char act = min[c];
+            float val = ain[c];
+            if (!act) {
+                const int i = (int)(c % W), j = (int)((c / W) % H), k = (int)(c / sz);
+                float sum = 0.0f;
+                int weight = 0;
+                auto see = [&](bool in, long long e) {
+                    if (in && min[e]) {
+                        sum += ain[e];
+                        ++weight;
+                    }
+                };
+                see(i + 1 < W, c + 1);
+                see(i > 0, c - 1);
+                see(j + 1 < H, c + sy);
+                see(j > 0, c - sy);
+                see(k > 0, c - sz);
+                see(k + 1 < D, c + sz);
+                if (weight) {
+                    val = sum / (float)weight;
+                    act = 1;
+                    newly = true;
+                }
+            }
+            aout[c] = val;
+            mout[c] = act;
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, newly);
+        if ((threadIdx.x & 31) == 0 && b) atomicAdd(added, (unsigned long long)__popc(b));
+    }
+}
+
+cudaError_t extrapolate_run(AdvectWork &w, int W, int H, int D, float *a, unsigned char *m, int count,
+                            cudaStream_t st, long long *launches, unsigned long long *activated_host) {
+    const long long n = (long long)W * H * D;
+    if (n > w.ext_cap) {
+        cudaFree(w.ext_a);
+        cudaFree(w.ext_m);
+        w.ext_a = nullptr;
+        w.ext_m = nullptr;
+        w.ext_cap = 0;
+        cudaError_t e = cudaMalloc(&w.ext_a, sizeof(float) * (size_t)n);
+        if (e == cudaSuccess) e = cudaMalloc(&w.ext_m, (size_t)n);
+        if (e != cudaSuccess) return e;
+        w.ext_cap = n;
+    }
+    if (!w.ext_count) {
+        cudaError_t e = cudaMalloc(&w.ext_count, sizeof(unsigned long long));
+        if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = cudaMemsetAsync(w.ext_count, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    float *ab[2] = {a, w.ext_a};
+    unsigned char *mb[2] = {m, w.ext_m};
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 8);
+    int cur = 0;
+    for (int r = 0; r < count; ++r) {
+        ext_round<<<blocks, 256, 0, st>>>(W, H, D, ab[cur], mb[cur], ab[cur ^ 1], mb[cur ^ 1], w.ext_count);
+        *launches += 1;
+        cur ^= 1;
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (cur) {  // an odd count ended in the second buffers
+        if ((e = cudaMemcpyAsync(a, w.ext_a, sizeof(float) * (size_t)n, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
+            return e;
+        if ((e = cudaMemcpyAsync(m, w.ext_m, (size_t)n, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+    }
+    if (activated_host)
+        e = cudaMemcpyAsync(activated_host, w.ext_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    return e;
 }
 
 cudaError_t constrain_run(AdvectWork &w, const ConstrainArgs &a, cudaStream_t st, long long *launches) {

@@ -21,9 +21,17 @@
 #include <type_traits>
 
 #include "gbp_batch.h"
+#include "gbp_convert.cuh"
 
 namespace gbp {
 namespace {
+
+// FP64 to T; to FP32 by integer instructions (gbp_convert.cuh), off the
+// FP64 pipe
+template <class T> __device__ __forceinline__ T narrow_to(double v) {
+    if constexpr (sizeof(T) == 4) return d2f_rn(v);
+    else return v;
+}
 
 constexpr int SITE_DOT = 4, SITE_SPMV = 5, SITE_UPDATE = 6, SITE_REFINE = 7;
 
@@ -524,7 +532,7 @@ __device__ __forceinline__ void presmooth_items(const BLevel<T> *__restrict__ le
         refresh(ctx, cur, it, levels, scenes, gate);
         cls_next = class_next<T, false>(levels, segs, nseg, n, w + gridDim.x, sgc, it.ref, ctx.L.tcp);
         if (ctx.skip) continue;
-        const BLevel<T> &L = ctx.L;
+        const BLevel<T> L = ctx.L;  // registers: stores through generic pointers would force reloads from shared memory
         const Cpl<T> cw{L.cx, L.cy, L.cz, cls};
         with_vu(L.vec, tile_uniform(cw.u), [&](auto vt, auto ut) {
             constexpr bool V = decltype(vt)::value;
@@ -588,7 +596,7 @@ __device__ __forceinline__ void sweep_items(const BLevel<T> *__restrict__ levels
         refresh(ctx, cur, it, levels, scenes, gate);
         cls_next = class_next<T, false>(levels, segs, nseg, n, w + gridDim.x, sgc, it.ref, ctx.L.tcp);
         if (ctx.skip) continue;
-        const BLevel<T> &L = ctx.L;
+        const BLevel<T> L = ctx.L;  // registers: stores through generic pointers would force reloads from shared memory
         const Cpl<T> cw{L.cx, L.cy, L.cz, cls};
         if (tile_empty(cw.u)) continue;  // x stays 0 (written by the presmoothing)
         with_vu(L.vec, tile_uniform(cw.u), [&](auto vt, auto ut) {
@@ -632,7 +640,7 @@ __device__ __forceinline__ void restrict_items(const BLevel<T> *__restrict__ lev
         refresh(ctx, cur, it, levels, scenes, gate);
         cls_next = class_next<T, true>(levels, segs, nseg, n, w + gridDim.x, sgc, it.ref, ctx.L.tcr);
         if (ctx.skip) continue;
-        const BLevel<T> &L = ctx.L;
+        const BLevel<T> L = ctx.L;  // registers: stores through generic pointers would force reloads from shared memory
         const Cpl<T> cw{L.cx, L.cy, L.cz, cls};
         if (tile_empty(cw.u)) {  // no unknown among the children: b_c = 0
             cell_tile(L.gc, it, [&](int, int, int, long long cc) { L.bc[cc] = T(0); });
@@ -758,7 +766,7 @@ __device__ __forceinline__ void post_black_items(const BLevel<T> *__restrict__ l
         refresh(ctx, cur, it, levels, scenes, gate);
         cls_next = class_next<T, false>(levels, segs, nseg, n, w + gridDim.x, sgc, it.ref, ctx.L.tcp);
         if (ctx.skip) continue;
-        const BLevel<T> &L = ctx.L;
+        const BLevel<T> L = ctx.L;  // registers: stores through generic pointers would force reloads from shared memory
         const Cpl<T> cw{L.cx, L.cy, L.cz, cls};
         if (tile_empty(cw.u)) continue;  // x stays 0 (written by the presmoothing)
         with_vu(L.vec, tile_uniform(cw.u), [&](auto vt, auto ut) {
@@ -1034,7 +1042,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     reduce_items<T, DotAcc<T>>(
         segs, nseg, n, part, levels, scenes, gate, ctx,
         [&](const BItem &it, DotAcc<T> &acc, T cls) {
-            const BLevel<T> &L = ctx.L;
+            const BLevel<T> L = ctx.L;  // registers: stores through generic pointers would force reloads from shared memory
             const Cpl<T> cw{L.cx, L.cy, L.cz, cls};
             if (tile_empty(cw.u)) return;  // z = 0 there: nothing to write or add
             with_vu(L.vec, tile_uniform(cw.u), [&](auto vt, auto ut) {
@@ -1305,8 +1313,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
         refresh(ctx, cur, it, levels, scenes, gate);
         cls_next = class_next<T, false>(levels, segs, nseg, n, w + gridDim.x, sgc, it.ref, ctx.L.tcp);
         if (ctx.skip) continue;
-        const BLevel<T> &L = ctx.L;
-        const BScene<T> &S = ctx.S;
+        const BLevel<T> L = ctx.L;  // registers: stores through generic pointers would force reloads from shared memory
+        const BScene<T> S = ctx.S;
         const T beta = T(ctx.beta);
         const bool empty = tile_empty(cls);
         // no unknown: p = 0, written when a direction starts (beta = 0) and
@@ -1365,8 +1373,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     reduce_items<T, DotAcc<T>>(
         segs, nseg, n, part, levels, scenes, gate, ctx,
         [&](const BItem &it, DotAcc<T> &acc, T cls) {
-            const BLevel<T> &L = ctx.L;
-            const BScene<T> &S = ctx.S;
+            const BLevel<T> L = ctx.L;  // registers: stores through generic pointers would force reloads from shared memory
+            const BScene<T> S = ctx.S;
             const Cpl<T> cw{L.cx, L.cy, L.cz, cls};
             // no unknown: q = A p = 0 there, and q is read nowhere else (the
             // update skips such tiles too)
@@ -1418,8 +1426,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     reduce_items<T, MaxAcc<T>>(
         segs, nseg, n, part, levels, scenes, gate, ctx,
         [&](const BItem &it, MaxAcc<T> &acc, T cls) {
-            const BLevel<T> &L = ctx.L;
-            const BScene<T> &S = ctx.S;
+            const BLevel<T> L = ctx.L;  // registers: stores through generic pointers would force reloads from shared memory
+            const BScene<T> S = ctx.S;
             const T alpha = T(ctx.alpha);
             const bool overwrite = ctx.overwrite != 0;
             // no unknown: p = q = r = 0 there; x = 0 is written by the
@@ -1537,8 +1545,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
         const BItem it = item_at(segs, nseg, w, sgc);
         refresh(ctx, cur, it, levels, scenes, 2);
         if (ctx.skip) continue;
-        const BLevel<T> &L = ctx.L;
-        const BScene<T> &S = ctx.S;
+        const BLevel<T> L = ctx.L;  // registers: stores through generic pointers would force reloads from shared memory
+        const BScene<T> S = ctx.S;
         with_vec(L.vec, [&](auto vt) {
             constexpr bool V = decltype(vt)::value;
             pair_tile(L.g, it, [&](int, int, int, long long c, bool second) {
@@ -1568,8 +1576,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_res
     reduce_items<T, MaxSumAcc<T>>(
         segs, nseg, n, part, levels, scenes, initial ? -1 : 2, ctx,
         [&](const BItem &it, MaxSumAcc<T> &acc, T cls) {
-            const BLevel<T> &L = ctx.L;
-            const BScene<T> &S = ctx.S;
+            const BLevel<T> L = ctx.L;  // registers: stores through generic pointers would force reloads from shared memory
+            const BScene<T> S = ctx.S;
             const Grid &g = L.g;
             const long long sy = g.nx, sz = (long long)g.nx * g.ny;
             const Operator<double> &A = S.A;
@@ -1606,7 +1614,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_res
                 pair_tile(g, it, [&](int i, int j, int k, long long c, bool second) {
                     if (zero_x) {
                         const Pair<double> rv = ld2<double, V>(S.b, c, second);
-                        const Pair<T> rt{T(rv.a), T(rv.b)};
+                        const Pair<T> rt{narrow_to<T>(rv.a), narrow_to<T>(rv.b)};
                         st2<double, V>(S.r64, c, rv, second);
                         st2<T, V>(S.r, c, rt, second);
                         acc.add(rv.a, rt.a);
@@ -1647,7 +1655,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_res
                     }
                     const Pair<double> bb = ld2<double, V>(S.b, c, second);
                     const Pair<double> rv{bb.a - a0, bb.b - a1};
-                    const Pair<T> rt{T(rv.a), T(rv.b)};
+                    const Pair<T> rt{narrow_to<T>(rv.a), narrow_to<T>(rv.b)};
                     st2<double, V>(S.r64, c, rv, second);
                     st2<T, V>(S.r, c, rt, second);
                     acc.add(rv.a, rt.a);
@@ -1965,7 +1973,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 1)
                 return;
             }
             phase ^= 1u << s;
-            const BLevel<float> &L = ctx.L;
+            const BLevel<float> L = ctx.L;
             const Grid &g = L.g;
             const float *st = stage0 + (size_t)s * STAGE_FLOATS;
             const unsigned t = (unsigned)it.tile;

@@ -919,3 +919,129 @@ int gbp_constrain_velocity3(gbp_ctx *c, int nx, int ny, int nz, double dx, const
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Extrapolation (array_extrapolator3::extrapolate, array_extrapolator3.h:
+// 36-73) and macutility3::extrapolate_and_constrain_velocity
+// (src/utility/macutility3.cpp:88-92)
+
+namespace {
+
+int extrapolate_check(const char *who, gbp_ctx *c, int w, int h, int d, const void *a, const void *m, int count) {
+    if (!c) return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": NULL context");
+    if (w < 1 || h < 1 || d < 1 || (long long)w * h * d >= (1LL << 31))
+        return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": bad shape (each edge >= 1, fewer than 2^31 cells)");
+    if (count < 0) return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": negative count");
+    if (!a || !m) return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": NULL array");
+    return GBP_OK;
+}
+
+// device staging of the host-array calls, kept in the context
+int stage_floats(gbp_ctx *c, long long need) {
+    if (need > c->adv_stage_floats) {
+        if (c->adv_stage) cudaFree(c->adv_stage);
+        c->adv_stage = nullptr;
+        c->adv_stage_floats = 0;
+        GBP_CUDA(cudaMalloc(&c->adv_stage, sizeof(float) * (size_t)need));
+        c->adv_stage_floats = need;
+    }
+    return GBP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbp_extrapolate3_device(gbp_ctx *c, int w, int h, int d, float *a, unsigned char *active, int count,
+                            long long *activated, void *stream) {
+    int rc = extrapolate_check("gbp_extrapolate3_device", c, w, h, d, a, active, count);
+    if (rc) return rc;
+    GBP_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    if (!stream) {
+        GBP_CUDA(cudaEventRecord(c->ev[0], cudaStreamLegacy));
+        GBP_CUDA(cudaStreamWaitEvent(st, c->ev[0], 0));
+    }
+    unsigned long long added = 0;
+    long long launched = 0;
+    GBP_CUDA(extrapolate_run(c->adv, w, h, d, a, active, count, st, &launched, activated ? &added : nullptr));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    c->launches += launched;
+    if (activated) *activated = (long long)added;
+    return GBP_OK;
+}
+
+int gbp_extrapolate3(gbp_ctx *c, int w, int h, int d, float *a, unsigned char *active, int count,
+                     long long *activated) {
+    int rc = extrapolate_check("gbp_extrapolate3", c, w, h, d, a, active, count);
+    if (rc) return rc;
+    GBP_CUDA(cudaSetDevice(c->device));
+    const size_t n = (size_t)w * h * d;
+    if ((rc = stage_floats(c, (long long)(n + (n + 3) / 4)))) return rc;
+    float *da = c->adv_stage;
+    unsigned char *dm = reinterpret_cast<unsigned char *>(da + n);
+    cudaStream_t st = c->stream;
+    GBP_CUDA(cudaMemcpyAsync(da, a, 4 * n, cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(dm, active, n, cudaMemcpyHostToDevice, st));
+    unsigned long long added = 0;
+    long long launched = 0;
+    GBP_CUDA(extrapolate_run(c->adv, w, h, d, da, dm, count, st, &launched, activated ? &added : nullptr));
+    GBP_CUDA(cudaMemcpyAsync(a, da, 4 * n, cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaMemcpyAsync(active, dm, n, cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    c->launches += launched;
+    if (activated) *activated = (long long)added;
+    return GBP_OK;
+}
+
+int gbp_extrapolate_constrain_velocity3(gbp_ctx *c, int nx, int ny, int nz, double dx, const float *solid, float *u,
+                                        float *v, float *w, unsigned char *mu, unsigned char *mv, unsigned char *mw,
+                                        int width) {
+    int rc = constrain_check("gbp_extrapolate_constrain_velocity3", c, nx, ny, nz, dx, solid, u, v, w);
+    if (rc) return rc;
+    if (width < 0) return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_extrapolate_constrain_velocity3: negative width");
+    if ((mu != nullptr) != (mv != nullptr) || (mu != nullptr) != (mw != nullptr))
+        return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_extrapolate_constrain_velocity3: give all three masks or none");
+    GBP_CUDA(cudaSetDevice(c->device));
+    const size_t nodes = (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+    const size_t nf[3] = {(size_t)(nx + 1) * ny * nz, (size_t)nx * (ny + 1) * nz, (size_t)nx * ny * (nz + 1)};
+    const bool masked = mu != nullptr;
+    const size_t mask_floats = masked ? (nf[0] + 3) / 4 + (nf[1] + 3) / 4 + (nf[2] + 3) / 4 : 0;
+    if ((rc = stage_floats(c, (long long)(nodes + nf[0] + nf[1] + nf[2] + mask_floats)))) return rc;
+    cudaStream_t st = c->stream;
+    float *ds = c->adv_stage, *dc[3];
+    dc[0] = ds + nodes;
+    dc[1] = dc[0] + nf[0];
+    dc[2] = dc[1] + nf[1];
+    float *next = dc[2] + nf[2];
+    unsigned char *dm[3] = {nullptr, nullptr, nullptr};
+    float *hc[3] = {u, v, w};
+    unsigned char *hm[3] = {mu, mv, mw};
+    GBP_CUDA(cudaMemcpyAsync(ds, solid, 4 * nodes, cudaMemcpyHostToDevice, st));
+    for (int d = 0; d < 3; ++d) {
+        GBP_CUDA(cudaMemcpyAsync(dc[d], hc[d], 4 * nf[d], cudaMemcpyHostToDevice, st));
+        if (masked) {
+            dm[d] = reinterpret_cast<unsigned char *>(next);
+            GBP_CUDA(cudaMemcpyAsync(dm[d], hm[d], nf[d], cudaMemcpyHostToDevice, st));
+            next += (nf[d] + 3) / 4;
+        }
+    }
+    long long launched = 0;
+    // macarray_extrapolator3::extrapolate: each component on its own
+    // (macarray_extrapolator3.h:44-48); with every face active nothing grows
+    if (masked)
+        for (int d = 0; d < 3; ++d)
+            GBP_CUDA(extrapolate_run(c->adv, nx + (d == 0), ny + (d == 1), nz + (d == 2), dc[d], dm[d], width, st,
+                                     &launched, nullptr));
+    GBP_CUDA(constrain_run(c->adv, constrain_args(nx, ny, nz, dx, ds, dc[0], dc[1], dc[2], dm[0], dm[1], dm[2]), st,
+                           &launched));
+    for (int d = 0; d < 3; ++d) {
+        GBP_CUDA(cudaMemcpyAsync(hc[d], dc[d], 4 * nf[d], cudaMemcpyDeviceToHost, st));
+        if (masked) GBP_CUDA(cudaMemcpyAsync(hm[d], dm[d], nf[d], cudaMemcpyDeviceToHost, st));
+    }
+    GBP_CUDA(cudaStreamSynchronize(st));
+    c->launches += launched;
+    return GBP_OK;
+}
+
+}  // extern "C"

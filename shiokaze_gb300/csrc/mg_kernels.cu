@@ -10,7 +10,8 @@
 //                    coupling of two coarse cells = sum of the 4 fine
 //                    couplings across their shared face; diagonal = sum of
 //                    the children's diagonals minus twice their internal
-//                    couplings. Computed in FP64.
+//                    couplings. Computed in FP64 for the FP64
+//                    hierarchy, in float-float for the FP32 one.
 //   V-cycle          pre-smooth red then black Gauss-Seidel (from x = 0),
 //                    residual restricted by summing the 8 children,
 //                    recurse, add `alpha` times the injected correction,
@@ -36,6 +37,7 @@
 //   update           read x, p, r, q; write x, r                      6 s
 #include <algorithm>
 
+#include "gbp_convert.cuh"
 #include "gbp_internal.cuh"
 #include "gbp_kernels.h"
 #include "gbp_mg.h"
@@ -60,7 +62,12 @@ __device__ __forceinline__ bool gated(const Scalars *sc, int gate) {
 // only needs a consistent value).
 template <class T> __device__ __forceinline__ T recip(double d);
 template <> __device__ __forceinline__ double recip<double>(double d) { return 1.0 / d; }
-template <> __device__ __forceinline__ float recip<float>(double d) { return __frcp_rn((float)d); }
+template <> __device__ __forceinline__ float recip<float>(double d) { return __frcp_rn(d2f_rn(d)); }
+
+// FP64 to the level's type; to FP32 by integer instructions (gbp_convert.cuh)
+template <class T> __device__ __forceinline__ T narrow(double v);
+template <> __device__ __forceinline__ double narrow<double>(double v) { return v; }
+template <> __device__ __forceinline__ float narrow<float>(double v) { return d2f_rn(v); }
 
 template <class F> __device__ __forceinline__ void for_each_cell(const Grid &g, F f) {
     const int tx = threadIdx.x & (TILE_X - 1), ty = threadIdx.x / TILE_X;
@@ -101,19 +108,73 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) mg_fine_setup_kernel(Grid g,
         const double d = A.diag[c];
         inv[c] = d > 0.0 ? recip<T>(d) : T(0);
         if (copy) {
-            diag[c] = T(d);
-            cx[c] = T(A.cx[c]);
-            cy[c] = T(A.cy[c]);
-            if (g.dim == 3) cz[c] = T(A.cz[c]);
+            diag[c] = narrow<T>(d);
+            cx[c] = narrow<T>(A.cx[c]);
+            cy[c] = narrow<T>(A.cy[c]);
+            if (g.dim == 3) cz[c] = narrow<T>(A.cz[c]);
         }
     });
 }
 
+// Float-float accumulator (TwoSum of each term into hi, its rounding error
+// summed into lo): about 48 significant bits from FP32 instructions alone.
+struct FloatFloat {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add(float b) {
+        const float sum = __fadd_rn(hi, b);
+        const float bb = __fsub_rn(sum, hi);
+        lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bb)), __fsub_rn(b, bb)));
+        hi = sum;
+    }
+    __device__ __forceinline__ float value() const { return __fadd_rn(hi, lo); }
+};
+
 // Galerkin coarse operator of 2x2x2 aggregation, one thread per coarse cell.
+// The FP32 hierarchy sums in float-float (its terms are floats and 2 w is
+// exact) and rounds once to float: FP32 instructions only, where the FP64
+// sums of every child took most of its setup time on this GPU's scarce
+// FP64 pipe (about one FP64 operation per clock per SM). The FP64
+// hierarchy sums in FP64.
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) mg_coarsen_kernel(MgLevel<T> F, MgLevel<T> C, T *cdiag, T *cinv,
                                                                    T *ccx, T *ccy, T *ccz) {
     const Grid &fg = F.g;
+    if constexpr (sizeof(T) == 4) {
+        for_each_cell(C.g, [&](int I, int J, int K, long long cc) {
+            FloatFloat d, ex, ey, ez;
+            const int kmax = fg.dim == 3 ? 2 : 1;
+            for (int c2 = 0; c2 < kmax; ++c2)
+                for (int b2 = 0; b2 < 2; ++b2)
+                    for (int a2 = 0; a2 < 2; ++a2) {
+                        const int i = 2 * I + a2, j = 2 * J + b2, k = 2 * K + c2;
+                        if (i >= fg.nx || j >= fg.ny || k >= fg.nz) continue;
+                        const long long f = cell_index(fg, i, j, k);
+                        d.add(F.diag[f]);
+                        const float wx = F.cx[f], wy = F.cy[f];
+                        if (a2 == 0) d.add(-2.0f * wx); else ex.add(wx);
+                        if (b2 == 0) d.add(-2.0f * wy); else ey.add(wy);
+                        if (fg.dim == 3) {
+                            const float wz = F.cz[f];
+                            if (c2 == 0) d.add(-2.0f * wz); else ez.add(wz);
+                        }
+                    }
+            float vx = ex.value(), vy = ey.value(), vz = ez.value();
+            if (2 * I + 1 >= fg.nx) vx = 0.0f;
+            if (2 * J + 1 >= fg.ny) vy = 0.0f;
+            if (fg.dim == 3 && 2 * K + 1 >= fg.nz) vz = 0.0f;
+            // an aggregate whose indicator has (numerically) no energy is
+            // dropped (a floating Neumann pocket); its float-float sum of
+            // exactly cancelling terms is 0 or below 2^-40 of the couplings
+            const float dv = d.value();
+            const bool active = dv > 1e-9f * (vx + vy + vz) + 1e-37f;
+            cdiag[cc] = T(active ? dv : 0.0f);
+            cinv[cc] = active ? __frcp_rn(dv) : T(0);
+            ccx[cc] = T(vx);
+            ccy[cc] = T(vy);
+            if (fg.dim == 3) ccz[cc] = T(vz);
+        });
+        return;
+    }
     for_each_cell(C.g, [&](int I, int J, int K, long long cc) {
         double d = 0.0, ex = 0.0, ey = 0.0, ez = 0.0;
         const int kmax = fg.dim == 3 ? 2 : 1;
@@ -140,7 +201,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) mg_coarsen_kernel(MgLevel<T>
         // dropped from the coarse problem: it is a floating Neumann pocket
         const bool active = d > 1e-12 * (ex + ey + ez + 1e-300);
         cdiag[cc] = T(active ? d : 0.0);
-        cinv[cc] = active ? recip<T>(d) : T(0);
+        cinv[cc] = active ? T(1.0 / d) : T(0);
         ccx[cc] = T(ex);
         ccy[cc] = T(ey);
         if (fg.dim == 3) ccz[cc] = T(ez);

@@ -13,6 +13,7 @@
 #include <cfloat>
 #include <cmath>
 
+#include "gbp_convert.cuh"
 #include "gbp_internal.cuh"
 #include "gbp_kernels.h"
 
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) pressure_kernel(Grid g, const d
         const bool unk = __ldg(diag + c) != 0.0;
         double xv = unk ? __ldg(x + c) : 0.0;
         if (prev && unk) xv = xv + prev[c];
-        p[c] = (float)xv;
+        p[c] = d2f_rn(xv);  // (float)xv, by integer instructions
         if (keep) keep[c] = xv;
     }
 }

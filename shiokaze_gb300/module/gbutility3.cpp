@@ -9,13 +9,15 @@
 // the module copies the solid and the velocity to dense arrays with
 // operator()'s values (gbarray_adapter.h), marks the active faces, and writes
 // the result back over them, as the reference's parallel_actives loop does.
-// extrapolate_and_constrain_velocity extrapolates on the host with the
-// reference's own header-only extrapolator, then constrains (:88-92). Every
+// extrapolate_and_constrain_velocity (:88-92) runs
+// gbp_extrapolate_constrain_velocity3: the velocity grown over its inactive
+// faces (array_extrapolator3, as the tiled array's dilate runs it), then
+// constrained over the grown active sets; the faces it activates are set
+// in the reference's arrays. Every
 // other member is forwarded to the reference's macutility3, loaded by the
 // same loader under this module's own key (GBUtilityBase), so the results
 // of the whole interface are the reference's.
 #include <shiokaze/array/array_utility3.h>
-#include <shiokaze/array/macarray_extrapolator3.h>
 #include <shiokaze/core/console.h>
 #include <shiokaze/utility/macutility3_interface.h>
 
@@ -64,8 +66,57 @@ protected:
     }
     virtual void extrapolate_and_constrain_velocity(const array3<Real> &solid, macarray3<Real> &velocity,
                                                     int extrapolate_width) const override {
-        macarray_extrapolator3::extrapolate(velocity, extrapolate_width);
-        constrain_velocity(solid, velocity);
+        // macarray_extrapolator3::extrapolate (each component grown over its
+        // inactive faces, macarray_extrapolator3.h:44-48), then the
+        // constraint over the grown active sets (macutility3.cpp:88-92),
+        // both on the GPU in one call; without a solid level set
+        // (levelset_exist on its active values) only the extrapolation
+        const int nx = m_shape.w, ny = m_shape.h, nz = m_shape.d;
+        const bool constrain = array_utility3::levelset_exist(solid);
+        std::vector<float> vel[3];
+        std::vector<unsigned char> mask[3], was[3];
+        for (int d = 0; d < 3; ++d) {
+            const shape3 fs = m_shape.face(d);
+            expect(velocity[d].shape() == fs, "velocity array has another shape");
+            vel[d].resize(fs.count());
+            gbarray::densify(velocity[d], vel[d].data());
+            mask[d].assign(fs.count(), 0);
+            unsigned char *m = mask[d].data();
+            velocity[d].const_parallel_actives([&](int i, int j, int k, const auto &) {
+                m[i + (size_t)fs.w * (j + (size_t)fs.h * k)] = 1;
+            });
+            was[d] = mask[d];
+        }
+        if (!m_ctx) check(gbp_create(m_device, &m_ctx), "gbp_create");
+        if (constrain) {
+            expect(solid.shape() == m_shape.nodal(), "solid array is not nodal");
+            std::vector<float> s(m_shape.nodal().count());
+            gbarray::densify(solid, s.data());
+            check(gbp_extrapolate_constrain_velocity3(m_ctx, nx, ny, nz, m_dx, s.data(), vel[0].data(), vel[1].data(),
+                                                      vel[2].data(), mask[0].data(), mask[1].data(), mask[2].data(),
+                                                      extrapolate_width),
+                  "gbp_extrapolate_constrain_velocity3");
+        } else {
+            for (int d = 0; d < 3; ++d)
+                check(gbp_extrapolate3(m_ctx, nx + (d == 0), ny + (d == 1), nz + (d == 2), vel[d].data(),
+                                       mask[d].data(), extrapolate_width, nullptr),
+                      "gbp_extrapolate3");
+        }
+        // the faces active before take their new values; the faces the
+        // extrapolation activated are set (which activates them)
+        velocity.parallel_actives([&](int dim, int i, int j, int k, auto &it, int) {
+            const int fx = nx + (dim == 0), fy = ny + (dim == 1);
+            it.set(vel[dim][i + (size_t)fx * (j + (size_t)fy * k)]);
+        });
+        for (int d = 0; d < 3; ++d) {
+            const shape3 fs = m_shape.face(d);
+            for (int k = 0; k < (int)fs.d; ++k)
+                for (int j = 0; j < (int)fs.h; ++j)
+                    for (int i = 0; i < (int)fs.w; ++i) {
+                        const size_t n = i + (size_t)fs.w * (j + (size_t)fs.h * k);
+                        if (mask[d][n] && !was[d][n]) velocity[d].set(i, j, k, vel[d][n]);
+                    }
+        }
     }
 
     // the rest of the interface: the reference's own module

@@ -1,0 +1,11 @@
+// TEST INFRASTRUCTURE: the GPU kernels' integer double -> float conversion
+// (shiokaze_gb300/csrc/gbp_convert.cuh) compiled for the host, for
+// tests/test_kernel_host.py to compare with the compiler's own conversion.
+#define __host__
+#define __device__
+#define __forceinline__ inline
+#include "gbp_convert.cuh"
+
+extern "C" void host_d2f(const double *in, float *out, long long n) {
+    for (long long i = 0; i < n; ++i) out[i] = gbp::d2f_rn(in[i]);
+}

@@ -2,7 +2,7 @@
  * gbp_oracle_stub.c -- TEST INFRASTRUCTURE: a stand-in for libgbp's
  * advection entry points that runs the oracle (oracle/advect_oracle.c, in
  * liboracle.so) on the CPU, and the same for the solid constraint of the
- * velocity and for the projection (oracle/gbp_oracle.c: scenes, volume
+ * velocity, its extrapolation, and the projection (oracle/gbp_oracle.c: scenes, volume
  * correction, warm start, gbp_project / gbp_project_active with the active
  * sets). tests/test_oracle.py links the gbadvection3, gbutility3 and
  * gbprojection2/3 plugin modules against it to check the modules' boundary
@@ -63,6 +63,27 @@ int gbp_advect3(gbp_ctx *ctx, int nx, int ny, int nz, double dx, double dt, cons
 int gbp_constrain_velocity3(gbp_ctx *ctx, int nx, int ny, int nz, double dx, const float *solid, float *u, float *v,
                             float *w, const unsigned char *mu, const unsigned char *mv, const unsigned char *mw) {
     (void)ctx;
+    return oracle_constrain_velocity3(nx, ny, nz, dx, solid, u, v, w, mu, mv, mw);
+}
+
+long long oracle_extrapolate3(int w, int h, int d, float *a, unsigned char *active, int count);
+
+int gbp_extrapolate3(gbp_ctx *ctx, int w, int h, int d, float *a, unsigned char *active, int count,
+                     long long *activated) {
+    (void)ctx;
+    long long n = oracle_extrapolate3(w, h, d, a, active, count);
+    if (activated) *activated = n;
+    return GBP_OK;
+}
+
+int gbp_extrapolate_constrain_velocity3(gbp_ctx *ctx, int nx, int ny, int nz, double dx, const float *solid,
+                                        float *u, float *v, float *w, unsigned char *mu, unsigned char *mv,
+                                        unsigned char *mw, int width) {
+    (void)ctx;
+    float *c[3] = {u, v, w};
+    unsigned char *m[3] = {mu, mv, mw};
+    if (mu)
+        for (int d = 0; d < 3; ++d) oracle_extrapolate3(nx + (d == 0), ny + (d == 1), nz + (d == 2), c[d], m[d], width);
     return oracle_constrain_velocity3(nx, ny, nz, dx, solid, u, v, w, mu, mv, mw);
 }
 

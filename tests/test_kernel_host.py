@@ -116,3 +116,37 @@ def test_kernel_code_matches_oracle_random(host, seed):
     got = host_constrain(host, solid, u, v, w, dx)
     for a, b in zip(got, want):
         assert bits_equal(a, b)
+
+
+def test_integer_double_to_float_conversion_is_exact(tmp_path):
+    """gbp_convert.cuh's d2f_rn (double -> float from integer instructions,
+    used by kernels that narrow FP64 values) equals the hardware conversion
+    (round to nearest, ties to even) bit for bit: random doubles of every
+    exponent, floats and the points halfway between neighbouring floats with
+    the doubles on either side, the edges of the float range (largest
+    finite, the overflow to infinity, the smallest normal and subnormals),
+    zeros, infinities and NaN."""
+    so = str(tmp_path / "libconvert_host.so")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I",
+                           os.path.join(ROOT, "shiokaze_gb300", "csrc"),
+                           os.path.join(ROOT, "tests", "kernel_host", "convert_host_harness.cpp"), "-o", so])
+    lib = ctypes.CDLL(so)
+    lib.host_d2f.argtypes = [ctypes.POINTER(ctypes.c_double), FP, ctypes.c_longlong]
+    rng = np.random.default_rng(5)
+    bits = rng.integers(0, 1 << 63, 1 << 20, dtype=np.uint64) | (rng.integers(0, 2, 1 << 20, dtype=np.uint64) << 63)
+    a = bits.view(np.float64)
+    f = rng.standard_normal(1 << 18).astype(np.float32)
+    fd = f.astype(np.float64)
+    half = (fd + np.nextafter(f, np.float32(np.inf)).astype(np.float64)) / 2
+    special = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 3.4028234663852886e38, 3.4028235677973366e38,
+                        3.4028235677973362e38, 3.402823567797337e38, 1.1754943508222875e-38, 1.1754942e-38,
+                        1e-45, 1.401298464324817e-45, 7e-46, 1e-300, 1e300, -1e300, 0.5, 1.5, 2.5],
+                       dtype=np.float64)
+    x = np.ascontiguousarray(np.concatenate([a, fd, half, np.nextafter(half, np.inf), np.nextafter(half, -np.inf),
+                                             special]))
+    out = np.zeros(x.shape, np.float32)
+    lib.host_d2f(x.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), out.ctypes.data_as(FP), x.size)
+    with np.errstate(over="ignore"):
+        want = x.astype(np.float32)
+    same = (out.view(np.uint32) == want.view(np.uint32)) | (np.isnan(want) & np.isnan(out))
+    assert same.all(), x[~same][:8]

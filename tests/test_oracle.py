@@ -356,3 +356,81 @@ def test_projection_modules_match_reference_modules(tmp_path):
         for comp, want, on in zip("uvw", (c.out_u, c.out_v, c.out_w), c.out_active):
             assert np.array_equal(got[f"{name}/{comp}"].view(np.uint32), want.view(np.uint32)), (name, comp)
             assert np.array_equal(got[f"{name}/{comp}_on"], on), (name, comp)
+
+
+def extrapolate_module_cases():
+    """Seeded liquid scenes with partly active velocities (inactive faces 0),
+    one without a solid level set (only the extrapolation acts)."""
+    for seed in (81, 82, 83, 84):
+        rng = np.random.default_rng(seed)
+        n = tuple(int(x) for x in rng.integers(8, 20, 3))
+        sc = scenes.liquid3(n, seed=seed, pool=float(rng.uniform(0.2, 0.5)))
+        if seed == 84:
+            sc.solid[...] = np.float32(sc.band)
+        masks, comps = [], []
+        for a in (sc.u, sc.v, sc.w):
+            m = (rng.random(a.shape) < rng.uniform(0.2, 0.7)).astype(np.uint8)
+            masks.append(m)
+            comps.append(np.where(m != 0, a, 0).astype(np.float32))
+        yield seed, sc, comps, masks, int(rng.integers(1, 4))
+
+
+EXTRAPOLATE_MODULE_RUN = r"""
+import sys
+import numpy as np
+import oracle
+sys.path.insert(0, "tests")
+from test_oracle import extrapolate_module_cases
+out = {}
+for seed, sc, comps, masks, width in extrapolate_module_cases():
+    r = oracle.extrapolate_constrain3(sc.solid, *comps, sc.dx, masks, width, impl="reference",
+                                      solid_mode=sc.solid_mode, band=sc.band, extra_kv="MacUtility=gbutility3stub")
+    for c, a, m in zip("uvw", r[:3], r[3]):
+        out[f"{seed}_{c}"] = a
+        out[f"{seed}_{c}_on"] = m
+np.savez(sys.argv[1], **out)
+"""
+
+
+def test_utility_module_extrapolate_constrain_matches_reference_module(tmp_path):
+    """gbutility3's extrapolate_and_constrain_velocity (the velocity grown
+    over its inactive faces, then constrained; macutility3.cpp:88-92) on
+    the CPU: linked to the oracle-backed stand-in for libgbp and loaded by
+    the reference's loader in place of macutility3, it leaves the reference
+    module's velocity values and active faces bit for bit on the
+    reference's own arrays, with and without a solid level set."""
+    import subprocess
+    import sys
+    if not oracle.reference_available():
+        pytest.skip("reference oracle not built here")
+    root = _stub_module(tmp_path, "gbutility3", "gbutility3stub")
+    out = tmp_path / "extrapolate.npz"
+    r = subprocess.run([sys.executable, "-c", EXTRAPOLATE_MODULE_RUN, str(out)], cwd=root, capture_output=True,
+                       text=True, timeout=300, env=dict(os.environ, PYTHONPATH=root))
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    got = dict(np.load(out))
+    grew = 0
+    for seed, sc, comps, masks, width in extrapolate_module_cases():
+        want = oracle.extrapolate_constrain3(sc.solid, *comps, sc.dx, masks, width, impl="reference",
+                                             solid_mode=sc.solid_mode, band=sc.band)
+        for c, a, m, m0 in zip("uvw", want[:3], want[3], masks):
+            assert np.array_equal(got[f"{seed}_{c}"].view(np.uint32), a.view(np.uint32)), (seed, c)
+            assert np.array_equal(got[f"{seed}_{c}_on"], m), (seed, c)
+            grew += int(m.sum()) - int(m0.sum())
+    assert grew > 0
+
+
+def test_extrapolate_constrain_port_matches_live_reference():
+    """The oracle's composition (oracle_extrapolate3 per component, then
+    oracle_constrain_velocity3) equals the reference's
+    extrapolate_and_constrain_velocity bit for bit, active sets included."""
+    if not oracle.reference_available():
+        pytest.skip("reference oracle not built here")
+    for seed, sc, comps, masks, width in extrapolate_module_cases():
+        a = oracle.extrapolate_constrain3(sc.solid, *comps, sc.dx, masks, width)
+        b = oracle.extrapolate_constrain3(sc.solid, *comps, sc.dx, masks, width, impl="reference",
+                                          solid_mode=sc.solid_mode, band=sc.band)
+        for x, y in zip(a[:3], b[:3]):
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), seed
+        for x, y in zip(a[3], b[3]):
+            assert np.array_equal(x, y), seed
