@@ -62,7 +62,14 @@ extern "C" {
 /* Arithmetic. FP64: every vector and operator in double.
  * MIXED: FP64 outer iterative refinement (r = b - A x with the FP64
  * operator, FP64 x, FP64 norms and dot products) around an FP32 MGPCG inner
- * solve (FP32 stencil, smoother and transfers). */
+ * solve (FP32 stencil, smoother and transfers). The inner solve's dot
+ * products and norms are not FP64 per term: each thread sums its n terms in
+ * float-float (the product split exactly by an FMA, TwoSum, renormalised
+ * after every term), within gamma_n^2 sum |a_i b_i| of the exact value
+ * (gamma_n = n u / (1 - n u), u = 2^-24; about 1.6e-11 sum |a_i b_i| for the
+ * 72 terms a thread sums at 256^3), and the threads' partials add in FP64.
+ * That is far below the inner solve's own tolerance (1e-3), and the outer
+ * refinement's residual, norms and stopping rule are FP64 throughout. */
 #define GBP_PRECISION_FP64 0
 #define GBP_PRECISION_MIXED 1
 

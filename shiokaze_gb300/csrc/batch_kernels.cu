@@ -22,6 +22,7 @@
 
 #include "gbp_batch.h"
 #include "gbp_convert.cuh"
+#include "gbp_floatfloat.cuh"
 
 namespace gbp {
 namespace {
@@ -367,10 +368,10 @@ __device__ __forceinline__ void reduce_items(const BSeg *__restrict__ segs, int 
 }
 
 // Per-thread partials of the reductions. FP64 path: FP64 FMA per term.
-// FP32 path: each product is split exactly by an FMA (a*b = p + e) and the
-// terms are summed in float-float (TwoSum, renormalised after every term,
-// about 46 significant bits); a partial is converted to FP64 once, when its
-// block flushes, and partials add across threads and blocks in FP64. The
+// FP32 path: FloatFloat::add_product (gbp_floatfloat.cuh: the product split
+// exactly by an FMA, TwoSum, renormalised after every term; a thread's n
+// terms within gamma_n^2 sum |a_i b_i|); a partial is converted to FP64 once,
+// when its block flushes, and partials add across threads and blocks in FP64. The
 // FP32 path then issues no FP64 instruction per cell (the FP64 pipe of this
 // GPU runs at a small fraction of its FP32 rate). It assumes |a b| stays
 // inside the FP32 range, as the FP32 inner solve does for its vectors.
@@ -388,19 +389,10 @@ template <> struct DotAcc<double> {
     }
 };
 template <> struct DotAcc<float> {
-    float hi, lo;
-    __device__ void reset() { hi = lo = 0.0f; }
-    __device__ void add(float a, float b) {
-        const float p = __fmul_rn(a, b);
-        const float e = __fmaf_rn(a, b, -p);
-        const float s = __fadd_rn(hi, p);
-        const float bb = __fsub_rn(s, hi);
-        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-        const float t = __fadd_rn(lo, __fadd_rn(err, e));
-        hi = __fadd_rn(s, t);
-        lo = __fsub_rn(t, __fsub_rn(hi, s));
-    }
-    __device__ double block(double *sh) { return block_sum((double)hi + (double)lo, sh); }
+    FloatFloat f;
+    __device__ void reset() { f.reset(); }
+    __device__ void add(float a, float b) { f.add_product(a, b); }
+    __device__ double block(double *sh) { return block_sum(f.value_fp64(), sh); }
     __device__ void store(double *sh, double *part, int idx, int) {
         const double b = block(sh);
         if (threadIdx.x == 0) part[idx] = b;

@@ -289,6 +289,38 @@ int ensure_staging(gbp_scene *s) {
 
 // Volume-correction constant (macpressuresolver3.cpp:204-217); advances the
 // controller's integral state once per projection.
+// Face fractions, operator and right-hand side of one scene: in 3D one
+// fused pass that also writes level 0 of the solver's hierarchy (o), in 2D
+// the face pass and the cell pass.
+cudaError_t launch_setup(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
+                         const float *fluid, const float *u, const float *v, const float *w, SolverState &st,
+                         Level0Out o, int grid_blocks, cudaStream_t stream, long long *launches) {
+    cudaError_t e;
+    if (g.dim == 3) {
+        e = launch_assemble_cells(g, dt, dx, sp, solid, fluid, u, v, w, st.faces, st.diag, st.cx, st.cy, st.cz, st.b,
+                                  o, st.sc, grid_blocks, stream);
+        *launches += 1;
+        return e;
+    }
+    e = launch_faces(g, dt, dx, sp, solid, fluid, u, v, w, st.faces, grid_blocks, stream);
+    if (e == cudaSuccess)
+        e = launch_assemble_faces(g, sp, fluid, st.faces, st.diag, st.cx, st.cy, st.cz, st.b, st.sc, grid_blocks,
+                                  stream);
+    *launches += 2;
+    return e;
+}
+
+// launch_setup for a solve: level 0 of the solver's hierarchy comes with it
+int setup_for_solve(gbp_scene *s, const Grid &g, double dt, const SetupParams &sp, const gbp_params &p,
+                    const float *solid, const float *fluid, const float *u, const float *v, const float *w,
+                    int grid_blocks, cudaStream_t stream, long long *launches) {
+    const Level0Out o = g.dim == 3 ? s->solver->level0_out(p) : Level0Out{};
+    GBP_CUDA(launch_setup(g, dt, s->dx, sp, solid, fluid, u, v, w, s->solver->state(), o, grid_blocks, stream,
+                          launches));
+    if (o.diag || o.inv64) s->solver->level0_written();
+    return GBP_OK;
+}
+
 double volume_correction(gbp_scene *s, double dt, const gbp_params &p) {
     if (!(p.gain && s->target_volume)) return 0.0;
     double x = (s->current_volume - s->target_volume) / s->target_volume;
@@ -349,10 +381,8 @@ int project_device(gbp_scene *s, double dt, const float *solid, const float *flu
         GBP_CUDA(launch_surface_tension(g, dt, s->dx, sp, p.surface_tension, fluid, u, v, w, c->grid_blocks, stream));
         c->launches += 1;
     }
-    GBP_CUDA(launch_faces(g, dt, s->dx, sp, solid, fluid, u, v, w, st.faces, c->grid_blocks, stream));
-    GBP_CUDA(launch_assemble_faces(g, sp, fluid, st.faces, st.diag, st.cx, st.cy, st.cz, st.b, st.sc,
-                                   c->grid_blocks, stream));
-    c->launches += 2;
+    rc = setup_for_solve(s, g, dt, sp, p, solid, fluid, u, v, w, c->grid_blocks, stream, &c->launches);
+    if (rc) return rc;
     GBP_CUDA(cudaEventRecord(c->ev[1], stream));
 
     long long launched = 0;
@@ -551,11 +581,9 @@ int gbp_batch_project_device(gbp_batch *b, const double *dt, const float *const 
                                             g.dim == 3 ? w[i] : nullptr, c->grid_blocks, st));
             launched += 1;
         }
-        GBP_CUDA(launch_faces(g, dt[i], s->dx, sp, solid[i], fluid[i], u[i], v[i], g.dim == 3 ? w[i] : nullptr,
-                              ss.faces, c->grid_blocks, st));
-        GBP_CUDA(launch_assemble_faces(g, sp, fluid[i], ss.faces, ss.diag, ss.cx, ss.cy, ss.cz, ss.b, ss.sc,
-                                       c->grid_blocks, st));
-        launched += 2;
+        rc = setup_for_solve(s, g, dt[i], sp, p, solid[i], fluid[i], u[i], v[i], g.dim == 3 ? w[i] : nullptr,
+                             c->grid_blocks, st, &launched);
+        if (rc) return rc;
         rc = s->solver->setup_mg(g, p, c->grid_blocks, st, &launched);
         if (rc) return fail(rc, s->solver->error());
         warm_key = warm_key || (p.warm_start && s->solver->has_prev());
@@ -678,11 +706,8 @@ int gbp_debug_assemble(gbp_scene *s, double dt, const float *solid, const float 
     if (p.surface_tension != 0.0)
         GBP_CUDA(launch_surface_tension(g, dt, s->dx, sp, p.surface_tension, s->d_fluid, s->d_u, s->d_v, s->d_w,
                                         s->ctx->grid_blocks, str));
-    GBP_CUDA(launch_faces(g, dt, s->dx, sp, s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, st.faces,
-                          s->ctx->grid_blocks, str));
-    GBP_CUDA(launch_assemble_faces(g, sp, s->d_fluid, st.faces, st.diag, st.cx, st.cy, st.cz, st.b, st.sc,
-                                   s->ctx->grid_blocks, str));
-    s->ctx->launches += 2;
+    GBP_CUDA(launch_setup(g, dt, s->dx, sp, s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, st, Level0Out{},
+                          s->ctx->grid_blocks, str, &s->ctx->launches));
     const size_t bytes = 8 * (size_t)g.ncell;
     GBP_CUDA(cudaMemcpyAsync(diag, st.diag, bytes, cudaMemcpyDeviceToHost, str));
     GBP_CUDA(cudaMemcpyAsync(cx, st.cx, bytes, cudaMemcpyDeviceToHost, str));

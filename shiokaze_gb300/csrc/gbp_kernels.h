@@ -26,6 +26,14 @@ struct FaceArrays {
     float *rho[3]; // rho of open faces, -1 if only rho closes the face, 0 if area == 0
 };
 
+// Level-0 arrays of a multigrid hierarchy that the fused 3D assembly writes
+// with the FP64 operator: the mixed solver's FP32 operator and inverse
+// diagonal, or the FP64 hierarchy's inverse diagonal (unused ones null).
+struct Level0Out {
+    float *diag, *inv, *cx, *cy, *cz;
+    double *inv64;
+};
+
 // ---- setup (setup_kernels.cu) ------------------------------------------------
 // Face-first path: faces, then cells; velocity update from the faces.
 // Surface-tension increment of the face velocities, in place (kappa != 0).
@@ -38,6 +46,13 @@ cudaError_t launch_faces(const Grid &g, double dt, double dx, const SetupParams 
 cudaError_t launch_assemble_faces(const Grid &g, const SetupParams &sp, const float *fluid, FaceArrays fa,
                                   double *diag, double *cx, double *cy, double *cz, double *b, Scalars *sc,
                                   int grid_blocks, cudaStream_t stream);
+// Fused 3D assembly (one pass; only the face fractions fa.rho are stored):
+// the same operator, right-hand side and fractions as launch_faces +
+// launch_assemble_faces, and level 0 of the hierarchy o names.
+cudaError_t launch_assemble_cells(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
+                                  const float *fluid, const float *u, const float *v, const float *w, FaceArrays fa,
+                                  double *diag, double *cx, double *cy, double *cz, double *b, Level0Out o,
+                                  Scalars *sc, int grid_blocks, cudaStream_t stream);
 cudaError_t launch_velocity_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *p,
                                   FaceArrays fa, float *u, float *v, float *w, const Scalars *sc, int grid_blocks,
                                   cudaStream_t stream);

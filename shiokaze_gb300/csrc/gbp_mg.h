@@ -74,10 +74,10 @@ struct MgSettings {
     double alpha;        // scale of the coarse-grid correction
 };
 
-// Level 0 in T from the FP64 operator (and its inverse diagonal), then the
-// Galerkin coarse operators.
+// Level 0 in T from the FP64 operator (and its inverse diagonal) unless the
+// assembly wrote it (level0_done), then the Galerkin coarse operators.
 template <class T>
-cudaError_t mg_setup(const Grid &g0, Operator<double> A, const MgHierarchy<T> &H, int grid_blocks,
+cudaError_t mg_setup(const Grid &g0, Operator<double> A, const MgHierarchy<T> &H, bool level0_done, int grid_blocks,
                      cudaStream_t stream);
 
 }  // namespace gbp

@@ -54,7 +54,7 @@ static size_t face_count(const Grid &g, int d) {
 size_t solver_device_bytes(const Grid &g, const gbp_params &p) {
     const size_t cells = (size_t)g.ncell;
     size_t bytes = 8 * cells * (5 /*operator+b*/ + 4 /*x r s z*/ + (p.warm_start ? 1 : 0));
-    for (int d = 0; d < g.dim; ++d) bytes += 20 * face_count(g, d);  // face arrays
+    for (int d = 0; d < g.dim; ++d) bytes += (g.dim == 2 ? 20 : 4) * face_count(g, d);  // face arrays
     if (p.solver == GBP_SOLVER_MGPCG) {
         bytes += 8 * cells;  // q
         const size_t s = p.precision == GBP_PRECISION_MIXED ? 4 : 8;
@@ -101,10 +101,14 @@ int Solver::prepare(const Grid &g, const gbp_params &p) {
         SOLVER_CUDA(cudaMemset(st_.sc, 0, sizeof(Scalars)));
         SOLVER_CUDA(cudaMalloc(&st_.pt, sizeof(Partials)));
         SOLVER_CUDA(cudaMallocHost(&st_.host_sc, sizeof(Scalars)));
+        // weights and fluxes per face only for the 2D two-pass assembly (the
+        // fused 3D pass keeps them in registers); fractions for both
         for (int d = 0; d < 3; ++d) {
             const size_t nf = d < g.dim ? face_count(g, d) : 1;
-            SOLVER_CUDA(cudaMalloc(&st_.faces.w[d], 8 * nf));
-            SOLVER_CUDA(cudaMalloc(&st_.faces.q[d], 8 * nf));
+            if (g.dim == 2) {
+                SOLVER_CUDA(cudaMalloc(&st_.faces.w[d], 8 * nf));
+                SOLVER_CUDA(cudaMalloc(&st_.faces.q[d], 8 * nf));
+            }
             SOLVER_CUDA(cudaMalloc(&st_.faces.rho[d], 4 * nf));
         }
         allocated_ = true;
@@ -291,14 +295,32 @@ int Solver::solve_cg(const Grid &g, const gbp_params &p, int grid_blocks, cudaSt
     return run_graph(p, chunk, stream, launches);
 }
 
+Level0Out Solver::level0_out(const gbp_params &p) const {
+    Level0Out o{};
+    if (p.solver != GBP_SOLVER_MGPCG) return o;
+    if (p.precision == GBP_PRECISION_MIXED && mg32_ready_) {
+        const MgLevel<float> &L = h32_.levels[0];
+        o.diag = const_cast<float *>(L.diag);
+        o.inv = const_cast<float *>(L.inv);
+        o.cx = const_cast<float *>(L.cx);
+        o.cy = const_cast<float *>(L.cy);
+        o.cz = const_cast<float *>(L.cz);
+    } else if (p.precision == GBP_PRECISION_FP64 && mg64_ready_) {
+        o.inv64 = const_cast<double *>(h64_.levels[0].inv);
+    }
+    return o;
+}
+
 int Solver::setup_mg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches) {
     Operator<double> A{st_.diag, st_.cx, st_.cy, g.dim == 3 ? st_.cz : st_.cy};
+    const bool level0 = level0_written_;
+    level0_written_ = false;
     if (p.precision == GBP_PRECISION_MIXED) {
-        SOLVER_CUDA(mg_setup<float>(g, A, h32_, grid_blocks, stream));
-        *launches += h32_.nlevels;
+        SOLVER_CUDA(mg_setup<float>(g, A, h32_, level0, grid_blocks, stream));
+        *launches += h32_.nlevels - (level0 ? 1 : 0);
     } else {
-        SOLVER_CUDA(mg_setup<double>(g, A, h64_, grid_blocks, stream));
-        *launches += h64_.nlevels;
+        SOLVER_CUDA(mg_setup<double>(g, A, h64_, level0, grid_blocks, stream));
+        *launches += h64_.nlevels - (level0 ? 1 : 0);
     }
     return GBP_OK;
 }

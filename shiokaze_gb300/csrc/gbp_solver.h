@@ -59,6 +59,11 @@ public:
     // Batched MGPCG: per-scene setup (level-0 operator in T, Galerkin
     // hierarchy), then this scene's entries of a batch plan.
     int setup_mg(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches);
+    // Level 0 of the hierarchy p's solve uses, for the fused 3D assembly to
+    // write (all null for plain CG); level0_written() tells the next
+    // setup_mg that the assembly did.
+    Level0Out level0_out(const gbp_params &p) const;
+    void level0_written() { level0_written_ = true; }
     template <class T> void add_to_plan(BatchPlan<T> &plan, const gbp_params &p) const;
     // Reads this scene's scalars after a batched solve.
     int finish_batched(const gbp_params &p, cudaStream_t stream);
@@ -93,6 +98,7 @@ private:
     MgHierarchy<double> h64_;
     MgHierarchy<float> h32_;
     bool mg64_ready_ = false, mg32_ready_ = false;
+    bool level0_written_ = false;
     int mg_coarsest_ = 0;
     int last_precision_ = GBP_PRECISION_FP64;
     // cached graph of solver iterations

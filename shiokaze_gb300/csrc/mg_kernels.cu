@@ -38,6 +38,7 @@
 #include <algorithm>
 
 #include "gbp_convert.cuh"
+#include "gbp_floatfloat.cuh"
 #include "gbp_internal.cuh"
 #include "gbp_kernels.h"
 #include "gbp_mg.h"
@@ -115,19 +116,6 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 6) mg_fine_setup_kernel(Grid g,
         }
     });
 }
-
-// Float-float accumulator (TwoSum of each term into hi, its rounding error
-// summed into lo): about 48 significant bits from FP32 instructions alone.
-struct FloatFloat {
-    float hi = 0.0f, lo = 0.0f;
-    __device__ __forceinline__ void add(float b) {
-        const float sum = __fadd_rn(hi, b);
-        const float bb = __fsub_rn(sum, hi);
-        lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bb)), __fsub_rn(b, bb)));
-        hi = sum;
-    }
-    __device__ __forceinline__ float value() const { return __fadd_rn(hi, lo); }
-};
 
 // Galerkin coarse operator of 2x2x2 aggregation, one thread per coarse cell.
 // The FP32 hierarchy sums in float-float (its terms are floats and 2 w is
@@ -315,13 +303,14 @@ template <class T> int nblocks(const Grid &g, int grid_blocks) {
 }  // namespace
 
 template <class T>
-cudaError_t mg_setup(const Grid &g0, Operator<double> A, const MgHierarchy<T> &H, int grid_blocks,
+cudaError_t mg_setup(const Grid &g0, Operator<double> A, const MgHierarchy<T> &H, bool level0_done, int grid_blocks,
                      cudaStream_t stream) {
     const MgLevel<T> &L0 = H.levels[0];
     const bool copy = !H.fine_aliases_fp64;
-    mg_fine_setup_kernel<T><<<nblocks<T>(g0, grid_blocks), BLOCK_THREADS, 0, stream>>>(
-        g0, A, const_cast<T *>(L0.diag), const_cast<T *>(L0.inv), const_cast<T *>(L0.cx), const_cast<T *>(L0.cy),
-        const_cast<T *>(L0.cz), copy);
+    if (!level0_done)
+        mg_fine_setup_kernel<T><<<nblocks<T>(g0, grid_blocks), BLOCK_THREADS, 0, stream>>>(
+            g0, A, const_cast<T *>(L0.diag), const_cast<T *>(L0.inv), const_cast<T *>(L0.cx), const_cast<T *>(L0.cy),
+            const_cast<T *>(L0.cz), copy);
     for (int l = 0; l + 1 < H.nlevels; ++l) {
         const MgLevel<T> &F = H.levels[l], &C = H.levels[l + 1];
         mg_coarsen_kernel<T><<<nblocks<T>(C.g, grid_blocks), BLOCK_THREADS, 0, stream>>>(
@@ -341,7 +330,9 @@ cudaError_t mg_setup(const Grid &g0, Operator<double> A, const MgHierarchy<T> &H
     return cudaGetLastError();
 }
 
-template cudaError_t mg_setup<double>(const Grid &, Operator<double>, const MgHierarchy<double> &, int, cudaStream_t);
-template cudaError_t mg_setup<float>(const Grid &, Operator<double>, const MgHierarchy<float> &, int, cudaStream_t);
+template cudaError_t mg_setup<double>(const Grid &, Operator<double>, const MgHierarchy<double> &, bool, int,
+                                      cudaStream_t);
+template cudaError_t mg_setup<float>(const Grid &, Operator<double>, const MgHierarchy<float> &, bool, int,
+                                     cudaStream_t);
 
 }  // namespace gbp

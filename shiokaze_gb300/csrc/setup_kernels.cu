@@ -14,6 +14,7 @@
 #include <cmath>
 
 #include "gbp_convert.cuh"
+#include "gbp_exact.cuh"
 #include "gbp_internal.cuh"
 #include "gbp_kernels.h"
 
@@ -86,6 +87,13 @@ struct FaceParams {
     // eps_solid <= 1 (eps_fluid <= 1): a fraction of exactly 0 or 1 is never
     // clamped, so uniform faces skip the FP64 clamp and conversion
     int eps_solid_le1, eps_fluid_le1;
+    // w_sum[n]: 0 + w_unit + ... + w_unit (n terms) in FP64, the diagonal
+    // of a cell whose n open faces all have area = rho = 1; inv_sum[n] its
+    // reciprocal (host-evaluated, the same IEEE operations)
+    double w_sum[7], inv_sum[7];
+    // dt for the velocity update's dt dp / dx by integer instructions
+    // (gbp_exact.cuh), with 1/dx as its power of two
+    MulConst dt_mul;
 };
 
 // (double)u * 2^e for a float u, built from u's bits with integer
@@ -626,6 +634,214 @@ __global__ void __launch_bounds__(BLOCK_THREADS) assemble_faces_kernel(
     }
 }
 
+// ---- fused 3D assembly -------------------------------------------------------------
+//
+// One pass over the cells with the face terms of faces_kernel computed in
+// registers instead of stored: a block takes a 32 x 8 column of cells
+// through zslab planes; each thread computes the three faces at its node
+// (-x, -y and the +z face of its cell, the -z face carried from the plane
+// below), takes its +x face from the next lane (lane 31 computes it) and
+// its +y face from the next row through shared memory (row 7 computes it),
+// and assembles its cell in the reference's face order as
+// assemble_faces_kernel does. Only the face fractions are stored (the
+// velocity update and the active sets read them). The sums use integer
+// instructions where they are exact (gbp_exact.cuh; the diagonal of a cell
+// whose open faces all have area = rho = 1 is FaceParams::w_sum[n]), and
+// the FP32 level-0 operator of the mixed solver (or the FP64 hierarchy's
+// inverse diagonal) is written from the same registers. Bit-identical to
+// faces_kernel + assemble_faces_kernel + mg_fine_setup_kernel.
+struct FaceTerm {
+    float area;  // open fraction (0 on the domain boundary)
+    float r;     // stored fraction: rho if open, -1 if only rho closes it, 0 if area == 0
+    float uf;    // velocity on the face (0 where area == 0: never read)
+};
+
+__device__ __forceinline__ FaceTerm face_term(float area, float f0, float f1, const float *__restrict__ vel,
+                                              long long f, const FaceParams &fp) {
+    FaceTerm t{area, 0.0f, 0.0f};
+    if (area) {
+        const float rho = rho_of(f0, f1, fp);
+        t.r = rho ? rho : -1.0f;
+        t.uf = __ldg(vel + f);
+    }
+    return t;
+}
+
+__device__ __forceinline__ double face_w(const FaceTerm &t, double dt, double dx, const FaceParams &fp) {
+    return (t.area == 1.0f && t.r == 1.0f) ? fp.w_unit : face_weight(dt, (double)t.area, (double)t.r, dx, fp);
+}
+
+// a[n] for n in [0, 7) by selects (an indexed kernel parameter would be
+// copied to local memory)
+__device__ __forceinline__ double pick7(const double (&a)[7], int n) {
+    double r = a[0];
+#pragma unroll
+    for (int q = 1; q < 7; ++q) r = n == q ? a[q] : r;
+    return r;
+}
+
+__device__ __forceinline__ FaceTerm shfl_term(const FaceTerm &t, int delta) {
+    return FaceTerm{__shfl_down_sync(0xffffffffu, t.area, delta), __shfl_down_sync(0xffffffffu, t.r, delta),
+                    __shfl_down_sync(0xffffffffu, t.uf, delta)};
+}
+
+__global__ void __launch_bounds__(BLOCK_THREADS) assemble_cells_kernel(
+    Grid g, double dt, double dx, FaceParams fp, double rhs_correct, int zslab, const float *__restrict__ solid,
+    const float *__restrict__ fluid, const float *__restrict__ u, const float *__restrict__ v,
+    const float *__restrict__ w, float *__restrict__ rho_x, float *__restrict__ rho_y, float *__restrict__ rho_z,
+    double *__restrict__ diag, double *__restrict__ cx, double *__restrict__ cy, double *__restrict__ cz,
+    double *__restrict__ b, Level0Out o, Scalars *sc) {
+    __shared__ FaceTerm sh_y[2][TILE_Y][TILE_X];
+    __shared__ unsigned long long sh_count[BLOCK_THREADS / 32];
+    const int tx = threadIdx.x & (TILE_X - 1), ty = threadIdx.x / TILE_X;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const long long sx = nx + 1, sxy = sx * (ny + 1);  // solid node strides
+    const long long cy_ = nx, cz_ = (long long)nx * ny;  // cell strides
+    const int nzs = (nz + zslab - 1) / zslab;
+    const long long items = (long long)g.ntx * g.nty * nzs;
+    unsigned long long my_count = 0;
+    int my_fluid = 0;
+    auto S = [&](int a, int bb, int c) { return __ldg(solid + a + sx * bb + sxy * c); };
+    auto F = [&](int a, int bb, int c) { return __ldg(fluid + a + cy_ * bb + cz_ * c); };
+    // the face at node (i, j, k) normal to x / y / z (it exists: the caller checks)
+    auto xface = [&](int i, int j, int k) {
+        const float area = (i > 0 && i < nx) ? area3(S(i, j, k), S(i, j + 1, k), S(i, j + 1, k + 1), S(i, j, k + 1), fp)
+                                             : 0.0f;
+        return face_term(area, F(min(i, nx - 1), j, k), F(max(i - 1, 0), j, k), u, face_index(g, 0, i, j, k), fp);
+    };
+    auto yface = [&](int i, int j, int k) {
+        const float area = (j > 0 && j < ny) ? area3(S(i, j, k), S(i + 1, j, k), S(i + 1, j, k + 1), S(i, j, k + 1), fp)
+                                             : 0.0f;
+        return face_term(area, F(i, min(j, ny - 1), k), F(i, max(j - 1, 0), k), v, face_index(g, 1, i, j, k), fp);
+    };
+    auto zface = [&](int i, int j, int k) {
+        const float area = (k > 0 && k < nz) ? area3(S(i, j, k), S(i + 1, j, k), S(i + 1, j + 1, k), S(i, j + 1, k), fp)
+                                             : 0.0f;
+        return face_term(area, F(i, j, min(k, nz - 1)), F(i, j, max(k - 1, 0)), w, face_index(g, 2, i, j, k), fp);
+    };
+    for (long long t = blockIdx.x; t < items; t += gridDim.x) {
+        const long long tz = t / ((long long)g.ntx * g.nty);
+        const long long rem = t - tz * g.ntx * g.nty;
+        const int i = (int)(rem % g.ntx) * TILE_X + tx, j = (int)(rem / g.ntx) * TILE_Y + ty;
+        const int kb = (int)tz * zslab, ke = min(kb + zslab, nz);
+        const bool cell_ij = i < nx && j < ny;
+        const bool xf = i <= nx && j < ny, yf = i < nx && j <= ny;
+        FaceTerm zlo{0.0f, 0.0f, 0.0f};
+        if (cell_ij) {
+            zlo = zface(i, j, kb);
+            if (kb == 0) rho_z[face_index(g, 2, i, j, 0)] = zlo.r;
+        }
+        for (int k = kb; k < ke; ++k) {
+            FaceTerm xo{0.0f, 0.0f, 0.0f}, yo{0.0f, 0.0f, 0.0f}, zhi{0.0f, 0.0f, 0.0f};
+            if (xf) xo = xface(i, j, k);
+            if (yf) yo = yface(i, j, k);
+            if (cell_ij) zhi = zface(i, j, k + 1);
+            FaceTerm xhi = shfl_term(xo, 1);
+            if (tx == TILE_X - 1 && i + 1 <= nx && j < ny) {
+                xhi = xface(i + 1, j, k);
+                if (i + 1 == nx) rho_x[face_index(g, 0, nx, j, k)] = xhi.r;
+            }
+            sh_y[k & 1][ty][tx] = yo;
+            __syncthreads();
+            FaceTerm yhi{0.0f, 0.0f, 0.0f};
+            if (ty + 1 < TILE_Y) {
+                yhi = sh_y[k & 1][ty + 1][tx];
+            } else if (i < nx && j + 1 <= ny) {
+                yhi = yface(i, j + 1, k);
+                if (j + 1 == ny) rho_y[face_index(g, 1, i, ny, k)] = yhi.r;
+            }
+            if (xf) rho_x[face_index(g, 0, i, j, k)] = xo.r;
+            if (yf) rho_y[face_index(g, 1, i, j, k)] = yo.r;
+            if (cell_ij) {
+                rho_z[face_index(g, 2, i, j, k + 1)] = zhi.r;
+                const long long c = i + cy_ * j + cz_ * k;
+                const float fc = __ldg(fluid + c);
+                double dg = 0.0, rhs = 0.0, cpl[3] = {0.0, 0.0, 0.0};
+                bool unknown = false, unit = true;
+                int nopen = 0;
+                if (fc < 0.0f) {
+                    my_fluid = 1;
+                    // faces in the reference's order +x, -x, +y, -y, +z, -z
+                    const FaceTerm fs[6] = {xhi, xo, yhi, yo, zhi, zlo};
+                    const bool has[6] = {i + 1 < nx, i > 0, j + 1 < ny, j > 0, k + 1 < nz, k > 0};
+                    const long long nb[6] = {c + 1, c - 1, c + cy_, c - cy_, c + cz_, c - cz_};
+                    // the right-hand side's terms -+u/dx by face (0 where a face has
+                    // no term or area 0: adding +-0 changes no sum)
+                    float terms[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+                    bool qexact = fp.dx_pow2 != 0;
+#pragma unroll
+                    for (int nq = 0; nq < 6; ++nq) {
+                        if (!has[nq]) continue;
+                        const FaceTerm ft = fs[nq];
+                        if (ft.r > 0.0f) {  // open face
+                            nopen++;
+                            unit = unit && ft.area == 1.0f && ft.r == 1.0f;
+                            if (__ldg(fluid + nb[nq]) < 0.0f) {
+                                unknown = true;
+                                if ((nq & 1) == 0) cpl[nq >> 1] = face_w(ft, dt, dx, fp);
+                            }
+                        }
+                        if (ft.area == 1.0f) terms[nq] = ft.uf;
+                        else if (ft.area != 0.0f) qexact = false;
+                    }
+                    if (unknown) {
+                        if (unit) {
+                            dg = pick7(fp.w_sum, nopen);
+                        } else {
+#pragma unroll
+                            for (int nq = 0; nq < 6; ++nq)
+                                if (has[nq] && fs[nq].r > 0.0f) dg += face_w(fs[nq], dt, dx, fp);
+                        }
+                        if (!(qexact && exact_sum(terms, 6, 0x15u, fp.inv_dx_exp, rhs))) {  // 0x15: the + faces negate
+                            rhs = 0.0;
+#pragma unroll
+                            for (int nq = 0; nq < 6; ++nq) {
+                                if (!has[nq]) continue;
+                                const FaceTerm ft = fs[nq];
+                                const double q = ft.area ? div_dx((double)ft.area * (double)ft.uf, dx, fp) : 0.0;
+                                rhs += (nq & 1) == 0 ? -q : q;
+                            }
+                        }
+                    }
+                }
+                if (unknown) {
+                    my_count++;
+                    if (rhs_correct) rhs += rhs_correct;  // macpressuresolver3.cpp:212-214
+                } else {
+                    dg = rhs = 0.0;
+                    cpl[0] = cpl[1] = cpl[2] = 0.0;
+                }
+                diag[c] = dg;
+                b[c] = rhs;
+                cx[c] = cpl[0];
+                cy[c] = cpl[1];
+                cz[c] = cpl[2];
+                if (o.diag) {
+                    const float d32 = d2f_rn(dg);
+                    o.diag[c] = d32;
+                    o.inv[c] = dg > 0.0 ? __frcp_rn(d32) : 0.0f;
+                    o.cx[c] = d2f_rn(cpl[0]);
+                    o.cy[c] = d2f_rn(cpl[1]);
+                    o.cz[c] = d2f_rn(cpl[2]);
+                }
+                if (o.inv64) o.inv64[c] = dg > 0.0 ? (unit ? pick7(fp.inv_sum, nopen) : 1.0 / dg) : 0.0;
+            }
+            zlo = zhi;
+        }
+    }
+    unsigned long long wsum = my_count;
+#pragma unroll
+    for (int q = 16; q > 0; q >>= 1) wsum += __shfl_down_sync(0xffffffffu, wsum, q);
+    if ((threadIdx.x & 31) == 0) sh_count[threadIdx.x >> 5] = wsum;
+    const int any_fluid = __syncthreads_or(my_fluid);
+    if (threadIdx.x == 0) {
+        unsigned long long s = 0;
+        for (int q = 0; q < BLOCK_THREADS / 32; ++q) s += sh_count[q];
+        if (s) atomicAdd(&sc->unknowns, s);
+        if (any_fluid) atomicOr(&sc->fluid_exists, 1);
+    }
+}
+
 // Velocity update from the stored face fractions (same rule as
 // velocity_kernel): open faces inside the domain get the pressure gradient,
 // every other face 0; with no fluid anywhere every face with area > 0 is open
@@ -648,7 +864,10 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_faces_kernel(Grid g, d
         const float rho = fluid_exists ? fr : 1.0f;
         if (!open || !interior) return 0.0f;
         const float dp = pc - pm;
-        // rho * dx == dx exactly when rho == 1
+        // rho * dx == dx exactly when rho == 1; (float)(dt dp / dx) by integer
+        // instructions where they decide (gbp_exact.cuh)
+        float vv;
+        if (rho == 1.0f && mul_round(fp.dt_mul, dp, vv)) return uf - vv;
         const double val = rho == 1.0f ? div_dx(dt * (double)dp, dx, fp) : dt * (double)dp / ((double)rho * dx);
         return uf - (float)val;
     };
@@ -666,8 +885,9 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_faces_kernel(Grid g, d
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             ex[d] = d < g.dim;
-            for (int e = 0; e < g.dim; ++e)
-                if (e != d && pi[e] >= n[e]) ex[d] = false;
+#pragma unroll
+            for (int e = 0; e < 3; ++e)
+                if (e < g.dim && e != d && pi[e] >= n[e]) ex[d] = false;
             in[d] = ex[d] && pi[d] > 0 && pi[d] < n[d];
             any_in = any_in || in[d];
             f[d] = ex[d] ? face_index(g, d, i, j, k) : 0;
@@ -754,6 +974,14 @@ FaceParams face_params(const SetupParams &sp, double dx, double dt) {
     const double num = dt * 1.0;
     volatile double denom = dx * dx;
     fp.w_unit = fp.dx_pow2 ? num * fp.inv_dx2 : num / (denom * 1.0);
+    volatile double acc = 0.0;
+    for (int n = 0; n < 7; ++n) {
+        fp.w_sum[n] = acc;
+        fp.inv_sum[n] = n ? 1.0 / acc : 0.0;
+        acc = acc + fp.w_unit;
+    }
+    fp.dt_mul = make_mul_const(dt, fp.dx_pow2 ? fp.inv_dx_exp : 0);
+    fp.dt_mul.ok = fp.dt_mul.ok && fp.dx_pow2;
     return fp;
 }
 
@@ -802,6 +1030,24 @@ cudaError_t launch_assemble_faces(const Grid &g, const SetupParams &sp, const fl
     if (blocks < 1) blocks = 1;
     assemble_faces_kernel<<<blocks, BLOCK_THREADS, 0, stream>>>(g, sp.rhs_correct, fluid, fa, diag, cx, cy,
                                                                 g.dim == 3 ? cz : cy, b, sc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_assemble_cells(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
+                                  const float *fluid, const float *u, const float *v, const float *w, FaceArrays fa,
+                                  double *diag, double *cx, double *cy, double *cz, double *b, Level0Out o,
+                                  Scalars *sc, int grid_blocks, cudaStream_t stream) {
+    if (g.dim != 3) return cudaErrorInvalidValue;
+    const FaceParams fp = face_params(sp, dx, dt);
+    // slabs deep enough to amortise the first plane's extra z face, thin
+    // enough for two items per block
+    int zslab = 32;
+    while (zslab > 4 && (long long)g.ntx * g.nty * ((g.nz + zslab - 1) / zslab) < 2LL * grid_blocks) zslab /= 2;
+    const long long items = (long long)g.ntx * g.nty * ((g.nz + zslab - 1) / zslab);
+    const int blocks = (int)(items < grid_blocks ? items : grid_blocks);
+    assemble_cells_kernel<<<blocks < 1 ? 1 : blocks, BLOCK_THREADS, 0, stream>>>(
+        g, dt, dx, fp, sp.rhs_correct, zslab, solid, fluid, u, v, w, fa.rho[0], fa.rho[1], fa.rho[2], diag, cx, cy, cz,
+        b, o, sc);
     return cudaGetLastError();
 }
 

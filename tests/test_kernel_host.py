@@ -150,3 +150,145 @@ def test_integer_double_to_float_conversion_is_exact(tmp_path):
         want = x.astype(np.float32)
     same = (out.view(np.uint32) == want.view(np.uint32)) | (np.isnan(want) & np.isnan(out))
     assert same.all(), x[~same][:8]
+
+
+def test_float_float_dot_error_bound(tmp_path):
+    """gbp_floatfloat.cuh's add_product (the FP32 inner solve's dot products
+    and norms, one thread's partial) is within gamma_n^2 sum |a_i b_i| of the
+    exact dot product (gamma_n = n u / (1 - n u), u = 2^-24), plus the one
+    FP64 rounding of hi + lo; add (the coarsening's sums of at most 27
+    terms) rounds the exact sum correctly or within one float ulp. The exact
+    values come from math.fsum of the products, each exact in FP64. The
+    cases: random vectors, sums that cancel to a tiny fraction of sum |a b|,
+    terms spread over 60 binary orders, and n up to 2^20 terms (a thread
+    sums about cells / resident threads terms: 72 at 256^3)."""
+    import math
+    so = str(tmp_path / "libff_host.so")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I",
+                           os.path.join(ROOT, "shiokaze_gb300", "csrc"),
+                           os.path.join(ROOT, "tests", "kernel_host", "floatfloat_host_harness.cpp"), "-o", so])
+    lib = ctypes.CDLL(so)
+    lib.host_ff_dot.argtypes = [FP, FP, ctypes.c_longlong]
+    lib.host_ff_dot.restype = ctypes.c_double
+    lib.host_ff_sum.argtypes = [FP, ctypes.c_longlong]
+    lib.host_ff_sum.restype = ctypes.c_float
+    rng = np.random.default_rng(11)
+    u = 2.0 ** -24
+    worst = 0.0
+    for n in (1, 7, 72, 1000, 1 << 14, 1 << 20):
+        for kind in ("normal", "cancel", "spread", "square"):
+            a = rng.standard_normal(n).astype(np.float32)
+            b = rng.standard_normal(n).astype(np.float32)
+            if kind == "cancel" and n > 1:
+                h = n // 2
+                a[h:2 * h], b[h:2 * h] = a[:h], -b[:h]
+                b[:h] *= np.float32(1 + 2 ** -20)
+            elif kind == "spread":
+                a *= np.exp2(rng.integers(-30, 30, n)).astype(np.float32)
+            elif kind == "square":
+                b = a
+            a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+            prod = a.astype(np.float64) * b.astype(np.float64)
+            exact = math.fsum(prod)
+            got = lib.host_ff_dot(a.ctypes.data_as(FP), b.ctypes.data_as(FP), n)
+            g = n * u / (1 - n * u)
+            bound = g * g * float(np.abs(prod).sum()) + 2.0 ** -53 * abs(exact)
+            err = abs(got - exact)
+            assert err <= bound, (n, kind, err, bound)
+            if bound > 0:
+                worst = max(worst, err / bound)
+    for n in (2, 8, 27):
+        for _ in range(2000):
+            x = (rng.standard_normal(n) * np.exp2(rng.integers(-12, 12, n))).astype(np.float32)
+            exact = math.fsum(x.astype(np.float64))
+            got = lib.host_ff_sum(np.ascontiguousarray(x).ctypes.data_as(FP), n)
+            lo = np.nextafter(np.float32(exact), np.float32(-np.inf))
+            hi = np.nextafter(np.float32(exact), np.float32(np.inf))
+            assert lo <= got <= hi, (x, got, exact)
+    print(f"largest dot error / bound: {worst:.3g}")
+
+
+@pytest.fixture(scope="module")
+def exact_lib(tmp_path_factory):
+    so = str(tmp_path_factory.mktemp("exact_host") / "libexact_host.so")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I",
+                           os.path.join(ROOT, "shiokaze_gb300", "csrc"),
+                           os.path.join(ROOT, "tests", "kernel_host", "exact_host_harness.cpp"), "-o", so])
+    lib = ctypes.CDLL(so)
+    U32 = ctypes.POINTER(ctypes.c_uint)
+    I32 = ctypes.POINTER(ctypes.c_int)
+    DP = ctypes.POINTER(ctypes.c_double)
+    lib.host_exact_sum.argtypes = [FP, U32, I32, ctypes.c_int, ctypes.c_longlong, DP, U8]
+    lib.host_mul_round.argtypes = [ctypes.c_double, ctypes.c_int, FP, ctypes.c_longlong, FP, U8]
+    return lib
+
+
+def _sequential_sum(f, neg, n, k):
+    """0 + t_0 + t_1 + ... in FP64, t_i = +-f_i 2^k, one rounding per addition."""
+    s = np.zeros(f.shape[0])
+    for i in range(6):
+        t = np.ldexp(f[:, i].astype(np.float64), k)
+        t = np.where((neg >> i) & 1, -t, t)
+        s = np.where(i < n, s + t, s)
+    return s
+
+
+def test_exact_sum_equals_sequential_fp64(exact_lib):
+    """gbp_exact.cuh's exact_sum (the assembly's right-hand side: six face
+    fluxes u/dx added in FP64 in the reference's face order) equals the
+    sequential FP64 sum bit for bit wherever it decides, and decides for
+    terms within a few binary orders of each other (the common case); terms
+    far apart, cancellation, zeros of both signs, 1..6 terms."""
+    rng = np.random.default_rng(21)
+    rows = 1 << 18
+    f = rng.standard_normal((rows, 6)).astype(np.float32)
+    scale = rng.integers(0, 4, rows)
+    f *= np.exp2(rng.integers(-40, 40, (rows, 6)) * (scale[:, None] == 3)).astype(np.float32)
+    f[rows // 8: rows // 4, 3] = -f[rows // 8: rows // 4, 0]          # exact cancellation
+    f[rows // 4: rows // 3, :] = np.float32(0.0)                      # all zeros
+    f[rows // 4: rows // 3: 2, 2] = np.float32(-0.0)
+    # near-equal terms of full 24-bit significands
+    f[rows // 3: rows // 2] = (1.0 + 2.0 ** -23 * rng.integers(0, 4, (rows // 2 - rows // 3, 6))).astype(np.float32)
+    neg = rng.integers(0, 64, rows).astype(np.uint32)
+    n = rng.integers(1, 7, rows).astype(np.int32)
+    n[: rows // 2] = 6
+    for k in (0, 7, -3):
+        out = np.zeros(rows)
+        ok = np.zeros(rows, np.uint8)
+        fa = np.ascontiguousarray(f)
+        exact_lib.host_exact_sum(fa.ctypes.data_as(FP), neg.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)),
+                                 n.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), k, rows,
+                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ok.ctypes.data_as(U8))
+        want = _sequential_sum(f, neg, n, k)
+        sel = ok != 0
+        assert np.array_equal(out[sel].view(np.uint64), want[sel].view(np.uint64))
+        near = scale != 3
+        assert sel[near].mean() > 0.999, sel[near].mean()
+
+
+def test_mul_round_equals_fp64_product(exact_lib):
+    """gbp_exact.cuh's mul_round (the velocity update's dt dp / dx with dx a
+    power of two) equals (float)((dt * (double)dp) * 2^s) bit for bit
+    wherever it decides, and decides for every normal result: random
+    time steps and pressure differences over every float exponent, the
+    products whose 77-bit significand lies halfway between two doubles or
+    whose double lies halfway between two floats (both tie rules), zeros of
+    both signs, subnormals and the float overflow edge."""
+    rng = np.random.default_rng(22)
+    n = 1 << 20
+    f = (rng.standard_normal(n) * np.exp2(rng.integers(-60, 60, n))).astype(np.float32)
+    f[:64] = [0.0, -0.0, 1e-45, -1e-40, np.float32(3.4e38), 1.0, -1.0, 0.5] * 8
+    # significands with few bits: products land on ties of both roundings
+    f[64:4096] = (rng.integers(1, 1 << 12, 4032) * np.exp2(rng.integers(-20, 0, 4032))).astype(np.float32)
+    for a in (0.01, 1.0 / 3.0, 0.004, -0.0125, 1.0 + 2 ** -30 + 2 ** -52, 3.0, 1e-3 * (1 + 2 ** -29),
+              float(rng.uniform(1e-4, 1e-1)), 1.5 * 2 ** -29):
+        for s in (0, 7, 9, -2, 100):
+            out = np.zeros(n, np.float32)
+            ok = np.zeros(n, np.uint8)
+            exact_lib.host_mul_round(a, s, f.ctypes.data_as(FP), n, out.ctypes.data_as(FP), ok.ctypes.data_as(U8))
+            with np.errstate(over="ignore", under="ignore"):
+                want = (np.ldexp(np.float64(a) * f.astype(np.float64), s)).astype(np.float32)
+            sel = ok != 0
+            assert np.array_equal(out[sel].view(np.uint32), want[sel].view(np.uint32)), (a, s)
+            normal = (np.abs(want) >= np.finfo(np.float32).tiny) & np.isfinite(want) & (np.abs(f) >= np.finfo(np.float32).tiny)
+            assert sel[normal].all(), (a, s, f[normal & ~sel][:4])
