@@ -190,6 +190,56 @@ int gbp_project_active(gbp_scene *scene, double dt, const float *solid, const fl
 int gbp_project_device(gbp_scene *scene, double dt, const float *solid, const float *fluid, float *u, float *v,
                        float *w, const gbp_params *params, float *pressure, gbp_stats *stats, void *stream);
 
+/* ---- sparse 3D arrays in bricks -------------------------------------------
+ * The reference's arrays are tiled and sparse (src/array/tiledarray3.cpp:
+ * tiles allocated where cells are active or partly filled; a cell reads its
+ * value if active, else the fill value if filled, else the background,
+ * include/shiokaze/array/array3.h:796-800). A gbp_bricks carries such an
+ * array of extent nx x ny x nz (cells, nodes or faces) in bricks of
+ * GBP_BRICK^3 cells: brick (bx, by, bz) holds cells [8 bx, 8 bx + 8) x
+ * [8 by, ..) x [8 bz, ..) and is numbered bx + nbx (by + nby bz), nbx =
+ * ceil(nx / 8) (nby, nbz likewise). slot[b] says what brick b holds:
+ *   GBP_BRICK_BACKGROUND  every cell reads `background`;
+ *   GBP_BRICK_FILL        every cell reads `fill`;
+ *   s >= 0                its cells read values[s * GBP_BRICK_CELLS + x +
+ *                         8 (y + 8 z)] (cells beyond the extent ignored).
+ * Only the listed bricks travel to the GPU, which expands them; the
+ * outputs come back the same way, for the bricks a gbp_bricks_out lists. */
+#define GBP_BRICK 8
+#define GBP_BRICK_CELLS 512
+#define GBP_BRICK_BACKGROUND (-1)
+#define GBP_BRICK_FILL (-2)
+typedef struct gbp_bricks {
+    float background, fill;
+    const int *slot;      /* one per brick */
+    long long count;      /* bricks with a slot >= 0; their slots are 0 .. count-1 */
+    const float *values;  /* count * GBP_BRICK_CELLS */
+} gbp_bricks;
+
+typedef struct gbp_bricks_out {
+    const int *slot;        /* one per brick: s >= 0 copies the brick out to slot s, < 0 skips it */
+    long long count;        /* bricks copied out; their slots are 0 .. count-1 */
+    float *values;          /* count * GBP_BRICK_CELLS, written */
+    unsigned char *active;  /* count * GBP_BRICK_CELLS (or NULL): the active sets of gbp_project_active */
+} gbp_bricks_out;
+
+/* gbp_project_active with its inputs and outputs in bricks (3D scenes):
+ * solid (nodes), fluid (cells), u, v, w (faces) in; pressure with the
+ * unknown cells, and u, v, w with the faces the reference keeps active, out
+ * for the listed bricks (any output may be NULL). The velocities are
+ * updated on the GPU in the expanded arrays; only the listed output bricks
+ * are copied back. Equal, cell for cell, to gbp_project_active on the
+ * expanded arrays. */
+int gbp_project_bricks(gbp_scene *scene, double dt, const gbp_bricks *solid, const gbp_bricks *fluid,
+                       const gbp_bricks *u, const gbp_bricks *v, const gbp_bricks *w, const gbp_params *params,
+                       gbp_bricks_out *pressure, gbp_bricks_out *u_out, gbp_bricks_out *v_out, gbp_bricks_out *w_out,
+                       gbp_stats *stats);
+
+/* The expansion alone: `dense` (a DEVICE array of nx*ny*nz floats, x
+ * fastest) receives the cell values of `in`, on `stream` (NULL = the
+ * context's stream; returns after the copy has finished). */
+int gbp_bricks_expand(gbp_ctx *ctx, int nx, int ny, int nz, const gbp_bricks *in, float *dense, void *stream);
+
 /* Batched projection: many independent scenes of uneven sizes solved
  * together. Every kernel of the multigrid-preconditioned CG iteration runs
  * once per iteration for the whole batch, over a work list of tiles of all

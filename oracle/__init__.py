@@ -272,6 +272,9 @@ def _ref_lib():
                                                    u8, u8, u8, ctypes.c_int, ctypes.c_char_p]
         lib.ref_densify_compare.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, ctypes.c_int,
                                             ctypes.c_float, ctypes.c_int, fp, fp, dp, dp]
+        lib.ref_bricks_compare.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, ctypes.c_int, ctypes.c_float,
+                                           fp, fp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_int),
+                                           fp, fp]
         _ref = lib
     return _ref
 
@@ -293,6 +296,29 @@ def ref_densify_compare(values: np.ndarray, mode: int, band: float, reps: int = 
     lib.ref_densify_compare(dim, sx, sy, sz, v.ctypes.data_as(fp), mode, band, reps, a.ctypes.data_as(fp),
                             b.ctypes.data_as(fp), ctypes.byref(ma), ctypes.byref(ml))
     return a, b, ma.value, ml.value
+
+
+def ref_bricks_compare(values: np.ndarray, mode: int, band: float):
+    """The plugin modules' bricks (gbarray_adapter.h to_bricks) of a 3D
+    reference array built as in ref_densify_compare. Returns (expanded,
+    lookup, counts, slot, listed_values, background, fill): the bricks
+    expanded by gbp.h's rule, operator()'s reads, the (listed, fill,
+    background) brick counts, and the bricks themselves."""
+    lib = _ref_lib()
+    v = np.ascontiguousarray(values, dtype=np.float32)
+    sz, sy, sx = v.shape
+    nb = ((sx + 7) // 8) * ((sy + 7) // 8) * ((sz + 7) // 8)
+    fp = ctypes.POINTER(ctypes.c_float)
+    a, b = np.empty_like(v), np.empty_like(v)
+    counts = np.zeros(3, np.int64)
+    slot = np.zeros(nb, np.int32)
+    vals = np.zeros(nb * 512, np.float32)
+    bgf = np.zeros(2, np.float32)
+    lib.ref_bricks_compare(sx, sy, sz, v.ctypes.data_as(fp), mode, ctypes.c_float(band), a.ctypes.data_as(fp),
+                           b.ctypes.data_as(fp), counts.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                           slot.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), vals.ctypes.data_as(fp),
+                           bgf.ctypes.data_as(fp))
+    return a, b, counts, slot, vals[: int(counts[0]) * 512].copy(), float(bgf[0]), float(bgf[1])
 
 
 def advect3(u, v, w, fluid, dx, dt, q=None, q_mask=None, q_bg=0.0, maccormack=True, trim_narrowband=1,

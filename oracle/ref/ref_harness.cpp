@@ -353,6 +353,48 @@ void ref_densify_compare(int dim, int sx, int sy, int sz, const float *in, int m
     }
 }
 
+/* The plugin modules' bricks (gbarray_adapter.h to_bricks) of a 3D array
+ * built as in ref_densify_compare: the bricks expanded by the rule of
+ * include/gbp.h (gbp_bricks) into out_expanded, every cell read through
+ * operator() into out_lookup, the brick counts (listed, fill, background)
+ * into counts, and the bricks themselves (slot per brick, listed values,
+ * background and fill) for the GPU's expansion test. values_out holds up to
+ * one brick per brick of the array. */
+void ref_bricks_compare(int sx, int sy, int sz, const float *in, int mode, float band, float *out_expanded,
+                        float *out_lookup, long long *counts, int *slot_out, float *values_out, float *bg_fill) {
+    if (!g_config_ready) install_global_config("");
+    array3<Real> a;
+    shape3 s(sx, sy, sz);
+    if (mode == 2) {
+        a.initialize(s, band);
+        for (int k = 0; k < sz; ++k)
+            for (int j = 0; j < sy; ++j)
+                for (int i = 0; i < sx; ++i) {
+                    const float x = in[i + (size_t)sx * (j + (size_t)sy * k)];
+                    if (std::abs(x) < band) a.set(i, j, k, x);
+                }
+    } else {
+        fill_levelset3(a, s, in, mode, band);
+    }
+    gbarray::Bricks b;
+    gbarray::to_bricks(a, b);
+    counts[0] = counts[1] = counts[2] = 0;
+    for (int sl : b.slot) counts[sl >= 0 ? 0 : sl == GBP_BRICK_FILL ? 1 : 2] += 1;
+    for (int k = 0; k < sz; ++k)
+        for (int j = 0; j < sy; ++j)
+            for (int i = 0; i < sx; ++i) {
+                const int sl = b.slot[b.brick(i, j, k)];
+                const size_t n = i + (size_t)sx * (j + (size_t)sy * k);
+                out_expanded[n] = sl >= 0 ? b.values[(size_t)sl * GBP_BRICK_CELLS + gbarray::Bricks::offset(i, j, k)]
+                                          : sl == GBP_BRICK_FILL ? b.fill : b.background;
+                out_lookup[n] = a(i, j, k);
+            }
+    std::copy(b.slot.begin(), b.slot.end(), slot_out);
+    std::copy(b.values.begin(), b.values.end(), values_out);
+    bg_fill[0] = b.background;
+    bg_fill[1] = b.fill;
+}
+
 /* The reference's macadvection3 (src/advection/macadvection3.cpp), loaded
  * by name, on dense 3D arrays, in macsmoke3::idle's order
  * (src/smoke/macsmoke3.cpp:270-281): the scalar (if q is given) advected by

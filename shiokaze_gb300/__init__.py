@@ -79,6 +79,75 @@ class AdvectParams(ctypes.Structure):
     _fields_ = [("maccormack", ctypes.c_int), ("trim_narrowband", ctypes.c_int), ("advect_velocity", ctypes.c_int)]
 
 
+class Bricks(ctypes.Structure):
+    """gbp_bricks: a sparse 3D array in bricks of 8^3 cells (include/gbp.h)."""
+    _fields_ = [("background", ctypes.c_float), ("fill", ctypes.c_float), ("slot", ctypes.POINTER(ctypes.c_int)),
+                ("count", ctypes.c_longlong), ("values", ctypes.POINTER(ctypes.c_float))]
+
+
+class BricksOut(ctypes.Structure):
+    """gbp_bricks_out: the bricks an output is copied back for."""
+    _fields_ = [("slot", ctypes.POINTER(ctypes.c_int)), ("count", ctypes.c_longlong),
+                ("values", ctypes.POINTER(ctypes.c_float)), ("active", ctypes.POINTER(ctypes.c_ubyte))]
+
+
+BRICK = 8
+BRICK_CELLS = 512
+BRICK_BACKGROUND = -1
+BRICK_FILL = -2
+
+
+def _brick_view(a, fill_value=0):
+    """(nbz, nby, nbx, 8, 8, 8) view of a 3D array padded to whole bricks."""
+    nz, ny, nx = a.shape
+    pz, py, px = (-nz) % 8, (-ny) % 8, (-nx) % 8
+    p = np.pad(a, ((0, pz), (0, py), (0, px)), constant_values=fill_value)
+    nbz, nby, nbx = p.shape[0] // 8, p.shape[1] // 8, p.shape[2] // 8
+    return p.reshape(nbz, 8, nby, 8, nbx, 8).transpose(0, 2, 4, 1, 3, 5)
+
+
+def to_bricks(values, active, filled=None, background=0.0, fill=0.0):
+    """The bricks of a sparse 3D array given densely (z, y, x): cells where
+    ``active`` read ``values``, other ``filled`` cells read ``fill``, the
+    rest ``background`` (the reference's tiled-array rule). A brick with an
+    active cell or some but not all cells filled is listed; one with every
+    cell filled and none active is BRICK_FILL; the rest BRICK_BACKGROUND
+    (the plugin modules' rule, gbarray_adapter.h). Returns (slot,
+    listed_values, background, fill) and the dense array those bricks
+    stand for."""
+    values = np.asarray(values, np.float32)
+    active = np.asarray(active, bool)
+    filled = np.zeros_like(active) if filled is None else np.asarray(filled, bool)
+    dense = np.where(active, values, np.where(filled, np.float32(fill), np.float32(background))).astype(np.float32)
+    inside = _brick_view(np.ones(values.shape, bool), False)
+    na = _brick_view(active, False).sum(axis=(3, 4, 5))
+    nf = _brick_view(filled, False).sum(axis=(3, 4, 5))
+    cells = inside.sum(axis=(3, 4, 5))
+    listed = (na > 0) | ((nf > 0) & (nf < cells))
+    slot = np.full(na.shape, BRICK_BACKGROUND, np.int32)
+    slot[(na == 0) & (nf == cells)] = BRICK_FILL
+    slot[listed] = np.arange(int(listed.sum()), dtype=np.int32)
+    bv = _brick_view(dense, np.float32(background))
+    listed_values = np.ascontiguousarray(bv[listed].reshape(-1), dtype=np.float32)
+    return (np.ascontiguousarray(slot.reshape(-1)), listed_values, float(background), float(fill)), dense
+
+
+def _bricks_struct(b):
+    slot, vals, bg, fill = b
+    return Bricks(bg, fill, slot.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(vals) // BRICK_CELLS,
+                  vals.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+
+
+def bricks_expand(nx, ny, nz, bricks, dense, context: "Context | None" = None, stream=None):
+    """gbp_bricks_expand: ``dense`` (a contiguous float32 torch CUDA tensor
+    of nz*ny*nx) receives the cell values of ``bricks`` (as to_bricks
+    returns them)."""
+    ctx = context or default_context()
+    b = _bricks_struct(bricks)
+    check(load_library().gbp_bricks_expand(ctx.ctx, nx, ny, nz, ctypes.byref(b), dense.data_ptr(),
+                                           ctypes.c_void_p(stream) if stream else None))
+
+
 class GBPError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"gbp error {code}: {msg}")
@@ -89,7 +158,8 @@ _lib = None
 EXPORTED = ["gbp_params_default", "gbp_create", "gbp_destroy", "gbp_scene_create", "gbp_scene_destroy",
             "gbp_scene_device_bytes", "gbp_scene_set_target_volume", "gbp_project", "gbp_project_device",
             "gbp_debug_assemble", "gbp_bench_kernel", "gbp_launch_count", "gbp_strerror", "gbp_batch_create",
-            "gbp_batch_destroy", "gbp_batch_project_device", "gbp_project_active"]
+            "gbp_batch_destroy", "gbp_batch_project_device", "gbp_project_active", "gbp_project_bricks",
+            "gbp_bricks_expand"]
 
 
 def library_path() -> str:
@@ -157,6 +227,10 @@ def load_library():
                                             vp]
     lib.gbp_extrapolate_constrain_velocity3.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                         ctypes.c_double, fp, fp, fp, fp, u8p, u8p, u8p, ctypes.c_int]
+    lib.gbp_bricks_expand.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(Bricks), vp, vp]
+    bp, bo = ctypes.POINTER(Bricks), ctypes.POINTER(BricksOut)
+    lib.gbp_project_bricks.argtypes = [vp, ctypes.c_double, bp, bp, bp, bp, bp, ctypes.POINTER(Params), bo, bo, bo, bo,
+                                       ctypes.POINTER(Stats)]
     lib.gbp_launch_count.argtypes = [vp]
     lib.gbp_launch_count.restype = ctypes.c_longlong
     lib.gbp_strerror.argtypes = [ctypes.c_int]
@@ -370,6 +444,26 @@ class _MacProject:
             rc = self.lib.gbp_project(self.scene, dt, solid_p, fluid_p, arrs[0][1], arrs[1][1], arrs[2][1],
                                       ctypes.byref(self.params), pp, ctypes.byref(self.stats))
         return check(rc, (GBP_OK, GBP_ERR_NOT_CONVERGED, GBP_ERR_NAN))
+
+    def project_bricks(self, dt, solid, fluid, velocity, out_slots):
+        """gbp_project_bricks (3D): inputs as to_bricks returns them (solid
+        nodes, fluid cells, the three face components); out_slots: slot per
+        brick (-1 = not copied out) for the pressure and u, v, w. Returns
+        the status and, per output, (values, active) of its listed bricks."""
+        ins = [_bricks_struct(b) for b in (solid, fluid) + tuple(velocity)]
+        outs, keep = [], []
+        for sl in out_slots:
+            sl = np.ascontiguousarray(sl, np.int32)
+            count = int((sl >= 0).sum())
+            vals = np.zeros(count * BRICK_CELLS, np.float32)
+            act = np.zeros(count * BRICK_CELLS, np.uint8)
+            keep.append((sl, vals, act))
+            outs.append(BricksOut(sl.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), count,
+                                  vals.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                  act.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte))))
+        rc = self.lib.gbp_project_bricks(self.scene, dt, *[ctypes.byref(b) for b in ins], ctypes.byref(self.params),
+                                         *[ctypes.byref(o) for o in outs], ctypes.byref(self.stats))
+        return check(rc, (GBP_OK, GBP_ERR_NOT_CONVERGED, GBP_ERR_NAN)), [(v, a) for _, v, a in keep]
 
     def bench_kernel(self, which: int, reps: int = 20, stream=None):
         """Mean ms per launch and algorithmic bytes per launch of one kernel."""

@@ -24,7 +24,7 @@ LIB = os.path.join(HERE, "libgbp.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["setup_kernels.cu", "cg_kernels.cu", "mg_kernels.cu", "batch_kernels.cu", "gbp_batch.cpp",
            "gbp_solver.cpp", "gbp_api.cpp", "gbp_noalloc.cu", "csr_solver.cu",
-           "advect_kernels.cu"]
+           "advect_kernels.cu", "brick_kernels.cu"]
 FMAD_OFF = {"setup_kernels.cu", "advect_kernels.cu"}
 
 

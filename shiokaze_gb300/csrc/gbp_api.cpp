@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "advect.h"
+#include "brick_kernels.h"
 #include "csr_solver.h"
 #include "gbp_kernels.h"
 #include "gbp_solver.h"
@@ -78,6 +79,13 @@ struct gbp_scene {
     // volume correction state (macpressuresolver3.cpp:316-318)
     double current_volume = 0.0, target_volume = 0.0, y_prev = 0.0;
     Solver *solver = nullptr;
+    // device copies of gbp_project_bricks' brick lists (5 in, 4 out: slots
+    // or slot-to-brick maps, values, flags), grown on demand
+    struct DevBuf {
+        void *p = nullptr;
+        size_t cap = 0;
+    };
+    DevBuf brick_buf[9][3];
 };
 
 extern "C" {
@@ -253,6 +261,9 @@ void gbp_scene_destroy(gbp_scene *s) {
         if (p) cudaFree(p);
     for (unsigned char *m : {s->d_unknown, s->d_on[0], s->d_on[1], s->d_on[2]})
         if (m) cudaFree(m);
+    for (auto &row : s->brick_buf)
+        for (auto &b : row)
+            if (b.p) cudaFree(b.p);
     if (s->solver) {
         s->solver->release();
         delete s->solver;
@@ -392,15 +403,25 @@ int project_device(gbp_scene *s, double dt, const float *solid, const float *flu
     int solve_status = rc;
     GBP_CUDA(cudaEventRecord(c->ev[2], stream));
 
-    GBP_CUDA(launch_pressure(g, st.diag, st.x, p.warm_start && st.have_prev ? st.prev : nullptr, pressure,
-                             p.warm_start ? st.prev : nullptr, c->grid_blocks, stream));
+    // 3D without warm start: the float pressure and the velocity update in
+    // one pass (after the active sets, which read the velocity before it)
+    const bool fused = g.dim == 3 && !p.warm_start;
+    if (!fused) {
+        GBP_CUDA(launch_pressure(g, st.diag, st.x, p.warm_start && st.have_prev ? st.prev : nullptr, pressure,
+                                 p.warm_start ? st.prev : nullptr, c->grid_blocks, stream));
+        c->launches += 1;
+    }
     if (active_sets) {
         GBP_CUDA(launch_active_sets(g, st.faces, fluid, u, v, w, st.diag, s->d_unknown, s->d_on[0], s->d_on[1],
                                     s->d_on[2], st.sc, c->grid_blocks, stream));
         c->launches += 1;
     }
-    GBP_CUDA(launch_velocity_faces(g, dt, s->dx, sp, pressure, st.faces, u, v, w, st.sc, c->grid_blocks, stream));
-    c->launches += 2;
+    if (fused)
+        GBP_CUDA(launch_pressure_velocity(g, dt, s->dx, sp, st.diag, st.x, pressure, st.faces, u, v, w, st.sc,
+                                          c->grid_blocks, stream));
+    else
+        GBP_CUDA(launch_velocity_faces(g, dt, s->dx, sp, pressure, st.faces, u, v, w, st.sc, c->grid_blocks, stream));
+    c->launches += 1;
     if (p.warm_start) st.have_prev = true;
     GBP_CUDA(cudaEventRecord(c->ev[3], stream));
     GBP_CUDA(cudaStreamSynchronize(stream));
@@ -505,6 +526,162 @@ int gbp_project_active(gbp_scene *s, double dt, const float *solid, const float 
         return fail(GBP_ERR_INVALID_ARGUMENT, "gbp_project_active: NULL active-set array");
     return project_host("gbp_project_active", s, dt, solid, fluid, u, v, w, params, pressure, stats, unknown,
                         u_active, v_active, w_active);
+}
+
+}  // extern "C"
+
+// ---- sparse arrays in bricks -------------------------------------------------------
+
+namespace {
+
+size_t brick_count(int nx, int ny, int nz) {
+    return (size_t)((nx + 7) / 8) * (size_t)((ny + 7) / 8) * (size_t)((nz + 7) / 8);
+}
+
+int grow(gbp_scene::DevBuf &b, size_t bytes) {
+    if (bytes <= b.cap) return GBP_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+    GBP_CUDA(cudaMalloc(&b.p, bytes));
+    b.cap = bytes;
+    return GBP_OK;
+}
+
+// Every slot is a brick kind or a listed slot, so no expansion reads
+// outside `values`.
+int check_bricks(const char *who, const char *what, const gbp_bricks *b, size_t nb) {
+    if (!b || !b->slot || b->count < 0 || (b->count > 0 && !b->values))
+        return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": bad " + what + " bricks");
+    for (size_t q = 0; q < nb; ++q) {
+        const int sl = b->slot[q];
+        if (sl < GBP_BRICK_FILL || sl >= b->count)
+            return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": " + what + " brick " + std::to_string(q) +
+                                                      " has slot " + std::to_string(sl));
+    }
+    return GBP_OK;
+}
+
+// brick_of[s] for the output slots; each slot 0 .. count-1 names exactly
+// one brick.
+int output_map(const char *who, const char *what, const gbp_bricks_out *o, size_t nb, std::vector<long long> &brick_of) {
+    if (!o->slot || o->count < 0 || (o->count > 0 && !o->values))
+        return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": bad " + what + " output bricks");
+    brick_of.assign((size_t)o->count, -1);
+    for (size_t q = 0; q < nb; ++q) {
+        const int sl = o->slot[q];
+        if (sl < 0) continue;
+        if (sl >= o->count || brick_of[(size_t)sl] >= 0)
+            return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": " + what + " output slot " +
+                                                      std::to_string(sl) + " out of range or repeated");
+        brick_of[(size_t)sl] = (long long)q;
+    }
+    for (long long b : brick_of)
+        if (b < 0) return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": " + what + " output slot unused");
+    return GBP_OK;
+}
+
+// Uploads one brick list into buf[0] (slots) and buf[1] (values) and
+// expands it into dense.
+int expand_on(gbp_ctx *c, int nx, int ny, int nz, const gbp_bricks *in, gbp_scene::DevBuf *buf, float *dense,
+              cudaStream_t st) {
+    const size_t nb = brick_count(nx, ny, nz);
+    int rc;
+    if ((rc = grow(buf[0], 4 * nb)) || (rc = grow(buf[1], 4 * (size_t)in->count * GBP_BRICK_CELLS))) return rc;
+    GBP_CUDA(cudaMemcpyAsync(buf[0].p, in->slot, 4 * nb, cudaMemcpyHostToDevice, st));
+    if (in->count)
+        GBP_CUDA(cudaMemcpyAsync(buf[1].p, in->values, 4 * (size_t)in->count * GBP_BRICK_CELLS,
+                                 cudaMemcpyHostToDevice, st));
+    GBP_CUDA(launch_brick_expand(nx, ny, nz, in->background, in->fill, static_cast<const int *>(buf[0].p),
+                                 static_cast<const float *>(buf[1].p), dense, c->grid_blocks, st));
+    c->launches += 1;
+    return GBP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbp_bricks_expand(gbp_ctx *c, int nx, int ny, int nz, const gbp_bricks *in, float *dense, void *stream) {
+    const char *who = "gbp_bricks_expand";
+    if (!c || !dense || nx < 1 || ny < 1 || nz < 1) return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": bad arguments");
+    int rc = check_bricks(who, "input", in, brick_count(nx, ny, nz));
+    if (rc) return rc;
+    GBP_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    gbp_scene::DevBuf buf[2];
+    rc = expand_on(c, nx, ny, nz, in, buf, dense, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    for (auto &b : buf)
+        if (b.p) cudaFree(b.p);
+    if (rc) return rc;
+    GBP_CUDA(e);
+    return GBP_OK;
+}
+
+int gbp_project_bricks(gbp_scene *s, double dt, const gbp_bricks *solid, const gbp_bricks *fluid, const gbp_bricks *u,
+                       const gbp_bricks *v, const gbp_bricks *w, const gbp_params *params, gbp_bricks_out *pressure,
+                       gbp_bricks_out *u_out, gbp_bricks_out *v_out, gbp_bricks_out *w_out, gbp_stats *stats) {
+    const char *who = "gbp_project_bricks";
+    if (!s) return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": NULL scene");
+    auto t0 = std::chrono::steady_clock::now();
+    const Grid &g = s->g;
+    if (g.dim != 3) return fail(GBP_ERR_INVALID_ARGUMENT, std::string(who) + ": 3D scenes only");
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    // extents of solid (nodes), fluid (cells), u, v, w (faces)
+    const int ext[5][3] = {{nx + 1, ny + 1, nz + 1}, {nx, ny, nz}, {nx + 1, ny, nz}, {nx, ny + 1, nz}, {nx, ny, nz + 1}};
+    const gbp_bricks *in[5] = {solid, fluid, u, v, w};
+    const char *names[5] = {"solid", "fluid", "u", "v", "w"};
+    int rc;
+    for (int a = 0; a < 5; ++a)
+        if ((rc = check_bricks(who, names[a], in[a], brick_count(ext[a][0], ext[a][1], ext[a][2])))) return rc;
+    gbp_bricks_out *outs[4] = {pressure, u_out, v_out, w_out};
+    const int oext[4] = {1, 2, 3, 4};  // extents of the outputs: fluid's, u's, v's, w's
+    std::vector<long long> brick_of[4];
+    bool sets = false;
+    for (int o = 0; o < 4; ++o) {
+        if (!outs[o]) continue;
+        const int *e = ext[oext[o]];
+        if ((rc = output_map(who, names[oext[o]], outs[o], brick_count(e[0], e[1], e[2]), brick_of[o]))) return rc;
+        sets = sets || outs[o]->active;
+    }
+    gbp_params p;
+    gbp_params_default(&p);
+    if (params) p = *params;
+    GBP_CUDA(cudaSetDevice(s->ctx->device));
+    if ((rc = ensure_staging(s))) return rc;
+    if (sets && (rc = ensure_active_sets(s))) return rc;
+    cudaStream_t st = s->ctx->stream;
+    float *dense[5] = {s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w};
+    for (int a = 0; a < 5; ++a)
+        if ((rc = expand_on(s->ctx, ext[a][0], ext[a][1], ext[a][2], in[a], s->brick_buf[a], dense[a], st))) return rc;
+    rc = project_device(s, dt, s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, p, s->d_p, stats, st, sets);
+    if (rc != GBP_OK && rc != GBP_ERR_NOT_CONVERGED && rc != GBP_ERR_NAN) return rc;
+    const float *src[4] = {s->d_p, s->d_u, s->d_v, s->d_w};
+    const unsigned char *flags[4] = {s->d_unknown, s->d_on[0], s->d_on[1], s->d_on[2]};
+    for (int o = 0; o < 4; ++o) {
+        gbp_bricks_out *out = outs[o];
+        if (!out || out->count == 0) continue;
+        gbp_scene::DevBuf *buf = s->brick_buf[5 + o];
+        const size_t cells = (size_t)out->count * GBP_BRICK_CELLS;
+        int r2;
+        if ((r2 = grow(buf[0], 8 * (size_t)out->count)) || (r2 = grow(buf[1], 4 * cells)) ||
+            (out->active && (r2 = grow(buf[2], cells))))
+            return r2;
+        GBP_CUDA(cudaMemcpyAsync(buf[0].p, brick_of[o].data(), 8 * (size_t)out->count, cudaMemcpyHostToDevice, st));
+        const int *e = ext[oext[o]];
+        GBP_CUDA(launch_brick_gather(e[0], e[1], e[2], static_cast<const long long *>(buf[0].p), out->count, src[o],
+                                     out->active ? flags[o] : nullptr, static_cast<float *>(buf[1].p),
+                                     out->active ? static_cast<unsigned char *>(buf[2].p) : nullptr,
+                                     s->ctx->grid_blocks, st));
+        s->ctx->launches += 1;
+        GBP_CUDA(cudaMemcpyAsync(out->values, buf[1].p, 4 * cells, cudaMemcpyDeviceToHost, st));
+        if (out->active) GBP_CUDA(cudaMemcpyAsync(out->active, buf[2].p, cells, cudaMemcpyDeviceToHost, st));
+    }
+    GBP_CUDA(cudaStreamSynchronize(st));
+    if (stats)
+        stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
 }
 
 }  // extern "C"
@@ -624,11 +801,17 @@ int gbp_batch_project_device(gbp_batch *b, const double *dt, const float *const 
         if (status != GBP_OK && first_bad == GBP_OK) first_bad = status;
         float *pout = pressure && pressure[i] ? pressure[i] : s->d_p;
         SetupParams sp{p.eps_solid, p.eps_fluid, p.second_order_solid, p.second_order_fluid, 0.0};
-        GBP_CUDA(launch_pressure(g, ss.diag, ss.x, p.warm_start && ss.have_prev ? ss.prev : nullptr, pout,
-                                 p.warm_start ? ss.prev : nullptr, c->grid_blocks, st));
-        GBP_CUDA(launch_velocity_faces(g, dt[i], s->dx, sp, pout, ss.faces, u[i], v[i], g.dim == 3 ? w[i] : nullptr,
-                                       ss.sc, c->grid_blocks, st));
-        launched += 2;
+        if (g.dim == 3 && !p.warm_start) {
+            GBP_CUDA(launch_pressure_velocity(g, dt[i], s->dx, sp, ss.diag, ss.x, pout, ss.faces, u[i], v[i], w[i],
+                                              ss.sc, c->grid_blocks, st));
+            launched += 1;
+        } else {
+            GBP_CUDA(launch_pressure(g, ss.diag, ss.x, p.warm_start && ss.have_prev ? ss.prev : nullptr, pout,
+                                     p.warm_start ? ss.prev : nullptr, c->grid_blocks, st));
+            GBP_CUDA(launch_velocity_faces(g, dt[i], s->dx, sp, pout, ss.faces, u[i], v[i],
+                                           g.dim == 3 ? w[i] : nullptr, ss.sc, c->grid_blocks, st));
+            launched += 2;
+        }
         if (p.warm_start) ss.have_prev = true;
     }
     GBP_CUDA(cudaEventRecord(c->ev[3], st));

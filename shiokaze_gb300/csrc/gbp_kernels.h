@@ -53,6 +53,10 @@ cudaError_t launch_assemble_cells(const Grid &g, double dt, double dx, const Set
                                   const float *fluid, const float *u, const float *v, const float *w, FaceArrays fa,
                                   double *diag, double *cx, double *cy, double *cz, double *b, Level0Out o,
                                   Scalars *sc, int grid_blocks, cudaStream_t stream);
+// Fused 3D pressure_kernel + velocity_faces_kernel (no warm start).
+cudaError_t launch_pressure_velocity(const Grid &g, double dt, double dx, const SetupParams &sp, const double *diag,
+                                     const double *x, float *p, FaceArrays fa, float *u, float *v, float *w,
+                                     const Scalars *sc, int grid_blocks, cudaStream_t stream);
 cudaError_t launch_velocity_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *p,
                                   FaceArrays fa, float *u, float *v, float *w, const Scalars *sc, int grid_blocks,
                                   cudaStream_t stream);

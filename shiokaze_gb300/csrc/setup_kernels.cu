@@ -637,18 +637,19 @@ __global__ void __launch_bounds__(BLOCK_THREADS) assemble_faces_kernel(
 // ---- fused 3D assembly -------------------------------------------------------------
 //
 // One pass over the cells with the face terms of faces_kernel computed in
-// registers instead of stored: a block takes a 32 x 8 column of cells
-// through zslab planes; each thread computes the three faces at its node
-// (-x, -y and the +z face of its cell, the -z face carried from the plane
-// below), takes its +x face from the next lane (lane 31 computes it) and
-// its +y face from the next row through shared memory (row 7 computes it),
-// and assembles its cell in the reference's face order as
-// assemble_faces_kernel does. Only the face fractions are stored (the
-// velocity update and the active sets read them). The sums use integer
+// registers instead of stored. A thread walks the column of cells (i, j)
+// through zslab planes; at each plane it computes the five faces it does not
+// carry (-x, +x, -y, +y and +z; the -z face is the previous plane's +z) and
+// assembles its cell in the reference's face order as assemble_faces_kernel
+// does. A plane's loads (4 solid nodes, 5 fluid cells, 5 face velocities)
+// are all issued before its arithmetic, and the solid nodes and fluid cells
+// of the plane below are carried, so each value is read about once and a
+// warp waits once per plane. Threads never exchange data (no barrier). Only the face fractions are stored (the
+// velocity update and the active sets read them). Sums use integer
 // instructions where they are exact (gbp_exact.cuh; the diagonal of a cell
-// whose open faces all have area = rho = 1 is FaceParams::w_sum[n]), and
-// the FP32 level-0 operator of the mixed solver (or the FP64 hierarchy's
-// inverse diagonal) is written from the same registers. Bit-identical to
+// whose open faces all have area = rho = 1 is FaceParams::w_sum[n]), and the
+// FP32 level-0 operator of the mixed solver (or the FP64 hierarchy's inverse
+// diagonal) is written from the same registers. Bit-identical to
 // faces_kernel + assemble_faces_kernel + mg_fine_setup_kernel.
 struct FaceTerm {
     float area;  // open fraction (0 on the domain boundary)
@@ -656,13 +657,14 @@ struct FaceTerm {
     float uf;    // velocity on the face (0 where area == 0: never read)
 };
 
-__device__ __forceinline__ FaceTerm face_term(float area, float f0, float f1, const float *__restrict__ vel,
-                                              long long f, const FaceParams &fp) {
+// A face from its open fraction, the fluid levels of its two cells and its
+// velocity (faces_kernel's emit).
+__device__ __forceinline__ FaceTerm face_term(float area, float f0, float f1, float uf, const FaceParams &fp) {
     FaceTerm t{area, 0.0f, 0.0f};
     if (area) {
         const float rho = rho_of(f0, f1, fp);
         t.r = rho ? rho : -1.0f;
-        t.uf = __ldg(vel + f);
+        t.uf = uf;
     }
     return t;
 }
@@ -680,152 +682,168 @@ __device__ __forceinline__ double pick7(const double (&a)[7], int n) {
     return r;
 }
 
-__device__ __forceinline__ FaceTerm shfl_term(const FaceTerm &t, int delta) {
-    return FaceTerm{__shfl_down_sync(0xffffffffu, t.area, delta), __shfl_down_sync(0xffffffffu, t.r, delta),
-                    __shfl_down_sync(0xffffffffu, t.uf, delta)};
-}
+// The loads of one plane k of a column: solid nodes (i..i+1, j..j+1) at
+// plane k+1, the fluid cells -x, +x, -y, +y at plane k and +z (clamped as
+// face_rho clamps), the velocities u(i), u(i+1), v(j), v(j+1) at plane k and
+// w at node k+1.
+struct PlaneLoads {
+    float s00, s10, s01, s11;
+    float fx0, fx1, fy0, fy1, fz1;
+    float u0, u1, v0, v1, w1;
+};
 
-__global__ void __launch_bounds__(BLOCK_THREADS) assemble_cells_kernel(
+__global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_cells_kernel(
     Grid g, double dt, double dx, FaceParams fp, double rhs_correct, int zslab, const float *__restrict__ solid,
     const float *__restrict__ fluid, const float *__restrict__ u, const float *__restrict__ v,
     const float *__restrict__ w, float *__restrict__ rho_x, float *__restrict__ rho_y, float *__restrict__ rho_z,
     double *__restrict__ diag, double *__restrict__ cx, double *__restrict__ cy, double *__restrict__ cz,
     double *__restrict__ b, Level0Out o, Scalars *sc) {
-    __shared__ FaceTerm sh_y[2][TILE_Y][TILE_X];
     __shared__ unsigned long long sh_count[BLOCK_THREADS / 32];
     const int tx = threadIdx.x & (TILE_X - 1), ty = threadIdx.x / TILE_X;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const long long sx = nx + 1, sxy = sx * (ny + 1);  // solid node strides
-    const long long cy_ = nx, cz_ = (long long)nx * ny;  // cell strides
+    const long long sx = nx + 1, sxy = sx * (ny + 1);        // solid nodes
+    const long long cy_ = nx, cz_ = (long long)nx * ny;      // cells
+    const long long uy = nx + 1, uz = uy * ny;               // u faces
+    const long long vy = nx, vz = (long long)nx * (ny + 1);  // v faces
     const int nzs = (nz + zslab - 1) / zslab;
     const long long items = (long long)g.ntx * g.nty * nzs;
     unsigned long long my_count = 0;
     int my_fluid = 0;
-    auto S = [&](int a, int bb, int c) { return __ldg(solid + a + sx * bb + sxy * c); };
-    auto F = [&](int a, int bb, int c) { return __ldg(fluid + a + cy_ * bb + cz_ * c); };
-    // the face at node (i, j, k) normal to x / y / z (it exists: the caller checks)
-    auto xface = [&](int i, int j, int k) {
-        const float area = (i > 0 && i < nx) ? area3(S(i, j, k), S(i, j + 1, k), S(i, j + 1, k + 1), S(i, j, k + 1), fp)
-                                             : 0.0f;
-        return face_term(area, F(min(i, nx - 1), j, k), F(max(i - 1, 0), j, k), u, face_index(g, 0, i, j, k), fp);
-    };
-    auto yface = [&](int i, int j, int k) {
-        const float area = (j > 0 && j < ny) ? area3(S(i, j, k), S(i + 1, j, k), S(i + 1, j, k + 1), S(i, j, k + 1), fp)
-                                             : 0.0f;
-        return face_term(area, F(i, min(j, ny - 1), k), F(i, max(j - 1, 0), k), v, face_index(g, 1, i, j, k), fp);
-    };
-    auto zface = [&](int i, int j, int k) {
-        const float area = (k > 0 && k < nz) ? area3(S(i, j, k), S(i + 1, j, k), S(i + 1, j + 1, k), S(i, j + 1, k), fp)
-                                             : 0.0f;
-        return face_term(area, F(i, j, min(k, nz - 1)), F(i, j, max(k - 1, 0)), w, face_index(g, 2, i, j, k), fp);
-    };
     for (long long t = blockIdx.x; t < items; t += gridDim.x) {
         const long long tz = t / ((long long)g.ntx * g.nty);
         const long long rem = t - tz * g.ntx * g.nty;
         const int i = (int)(rem % g.ntx) * TILE_X + tx, j = (int)(rem / g.ntx) * TILE_Y + ty;
+        if (i >= nx || j >= ny) continue;  // no barrier below: idle threads may leave
         const int kb = (int)tz * zslab, ke = min(kb + zslab, nz);
-        const bool cell_ij = i < nx && j < ny;
-        const bool xf = i <= nx && j < ny, yf = i < nx && j <= ny;
-        FaceTerm zlo{0.0f, 0.0f, 0.0f};
-        if (cell_ij) {
-            zlo = zface(i, j, kb);
-            if (kb == 0) rho_z[face_index(g, 2, i, j, 0)] = zlo.r;
-        }
+        const int im = max(i - 1, 0), ip = min(i + 1, nx - 1), jm = max(j - 1, 0), jp = min(j + 1, ny - 1);
+        const float *s0 = solid + i + sx * j;
+        const float *fcol = fluid + i + cy_ * j;
+        auto load = [&](int k) {
+            PlaneLoads L;
+            const float *sk = s0 + sxy * (k + 1);
+            L.s00 = __ldg(sk);
+            L.s10 = __ldg(sk + 1);
+            L.s01 = __ldg(sk + sx);
+            L.s11 = __ldg(sk + sx + 1);
+            const long long ck = cz_ * k;
+            L.fx0 = __ldg(fluid + im + cy_ * j + ck);
+            L.fx1 = __ldg(fluid + ip + cy_ * j + ck);
+            L.fy0 = __ldg(fluid + i + cy_ * jm + ck);
+            L.fy1 = __ldg(fluid + i + cy_ * jp + ck);
+            L.fz1 = __ldg(fcol + cz_ * min(k + 1, nz - 1));
+            const long long uk = i + uy * j + uz * k;
+            L.u0 = __ldg(u + uk);
+            L.u1 = __ldg(u + uk + 1);
+            const long long vk = i + vy * j + vz * k;
+            L.v0 = __ldg(v + vk);
+            L.v1 = __ldg(v + vk + vy);
+            L.w1 = __ldg(w + i + cy_ * j + cz_ * (k + 1));
+            return L;
+        };
+        // the carried state at plane kb: solid nodes of the plane, the cell's
+        // and the one below's fluid level, the -z face
+        float c00 = __ldg(s0 + sxy * kb), c10 = __ldg(s0 + sxy * kb + 1), c01 = __ldg(s0 + sxy * kb + sx),
+              c11 = __ldg(s0 + sxy * kb + sx + 1);
+        float fk = __ldg(fcol + cz_ * kb), fm = __ldg(fcol + cz_ * max(kb - 1, 0));
+        const float wlo = __ldg(w + i + cy_ * j + cz_ * kb);
+        FaceTerm zlo = face_term(kb > 0 ? area3(c00, c10, c11, c01, fp) : 0.0f, fk, fm, wlo, fp);
+        if (kb == 0) rho_z[i + cy_ * j] = zlo.r;
         for (int k = kb; k < ke; ++k) {
-            FaceTerm xo{0.0f, 0.0f, 0.0f}, yo{0.0f, 0.0f, 0.0f}, zhi{0.0f, 0.0f, 0.0f};
-            if (xf) xo = xface(i, j, k);
-            if (yf) yo = yface(i, j, k);
-            if (cell_ij) zhi = zface(i, j, k + 1);
-            FaceTerm xhi = shfl_term(xo, 1);
-            if (tx == TILE_X - 1 && i + 1 <= nx && j < ny) {
-                xhi = xface(i + 1, j, k);
-                if (i + 1 == nx) rho_x[face_index(g, 0, nx, j, k)] = xhi.r;
-            }
-            sh_y[k & 1][ty][tx] = yo;
-            __syncthreads();
-            FaceTerm yhi{0.0f, 0.0f, 0.0f};
-            if (ty + 1 < TILE_Y) {
-                yhi = sh_y[k & 1][ty + 1][tx];
-            } else if (i < nx && j + 1 <= ny) {
-                yhi = yface(i, j + 1, k);
-                if (j + 1 == ny) rho_y[face_index(g, 1, i, ny, k)] = yhi.r;
-            }
-            if (xf) rho_x[face_index(g, 0, i, j, k)] = xo.r;
-            if (yf) rho_y[face_index(g, 1, i, j, k)] = yo.r;
-            if (cell_ij) {
-                rho_z[face_index(g, 2, i, j, k + 1)] = zhi.r;
-                const long long c = i + cy_ * j + cz_ * k;
-                const float fc = __ldg(fluid + c);
-                double dg = 0.0, rhs = 0.0, cpl[3] = {0.0, 0.0, 0.0};
-                bool unknown = false, unit = true;
-                int nopen = 0;
-                if (fc < 0.0f) {
-                    my_fluid = 1;
-                    // faces in the reference's order +x, -x, +y, -y, +z, -z
-                    const FaceTerm fs[6] = {xhi, xo, yhi, yo, zhi, zlo};
-                    const bool has[6] = {i + 1 < nx, i > 0, j + 1 < ny, j > 0, k + 1 < nz, k > 0};
-                    const long long nb[6] = {c + 1, c - 1, c + cy_, c - cy_, c + cz_, c - cz_};
-                    // the right-hand side's terms -+u/dx by face (0 where a face has
-                    // no term or area 0: adding +-0 changes no sum)
-                    float terms[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-                    bool qexact = fp.dx_pow2 != 0;
+            // every load of the plane first, independent of the arithmetic
+            const PlaneLoads L = load(k);
+            // faces at the nodes of this cell (corner order of face_area)
+            const FaceTerm xlo = face_term(i > 0 ? area3(c00, c01, L.s01, L.s00, fp) : 0.0f, fk, L.fx0, L.u0, fp);
+            const FaceTerm xhi =
+                face_term(i + 1 < nx ? area3(c10, c11, L.s11, L.s10, fp) : 0.0f, L.fx1, fk, L.u1, fp);
+            const FaceTerm ylo = face_term(j > 0 ? area3(c00, c10, L.s10, L.s00, fp) : 0.0f, fk, L.fy0, L.v0, fp);
+            const FaceTerm yhi =
+                face_term(j + 1 < ny ? area3(c01, c11, L.s11, L.s01, fp) : 0.0f, L.fy1, fk, L.v1, fp);
+            const FaceTerm zhi =
+                face_term(k + 1 < nz ? area3(L.s00, L.s10, L.s11, L.s01, fp) : 0.0f, L.fz1, fk, L.w1, fp);
+            rho_x[i + uy * j + uz * k] = xlo.r;
+            if (i + 1 == nx) rho_x[nx + uy * j + uz * k] = xhi.r;
+            rho_y[i + vy * j + vz * k] = ylo.r;
+            if (j + 1 == ny) rho_y[i + vy * ny + vz * k] = yhi.r;
+            rho_z[i + cy_ * j + cz_ * (k + 1)] = zhi.r;
+            const long long c = i + cy_ * j + cz_ * k;
+            double dg = 0.0, rhs = 0.0, cpl[3] = {0.0, 0.0, 0.0};
+            bool unknown = false, unit = true;
+            int nopen = 0;
+            if (fk < 0.0f) {
+                my_fluid = 1;
+                // faces in the reference's order +x, -x, +y, -y, +z, -z, with
+                // the fluid level across each
+                const FaceTerm fs[6] = {xhi, xlo, yhi, ylo, zhi, zlo};
+                const bool has[6] = {i + 1 < nx, i > 0, j + 1 < ny, j > 0, k + 1 < nz, k > 0};
+                const float fn[6] = {L.fx1, L.fx0, L.fy1, L.fy0, L.fz1, fm};
+                // the right-hand side's terms -+u/dx by face (0 where a face
+                // has no term or area 0: adding +-0 changes no sum)
+                float terms[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+                bool qexact = fp.dx_pow2 != 0;
 #pragma unroll
-                    for (int nq = 0; nq < 6; ++nq) {
-                        if (!has[nq]) continue;
-                        const FaceTerm ft = fs[nq];
-                        if (ft.r > 0.0f) {  // open face
-                            nopen++;
-                            unit = unit && ft.area == 1.0f && ft.r == 1.0f;
-                            if (__ldg(fluid + nb[nq]) < 0.0f) {
-                                unknown = true;
-                                if ((nq & 1) == 0) cpl[nq >> 1] = face_w(ft, dt, dx, fp);
-                            }
-                        }
-                        if (ft.area == 1.0f) terms[nq] = ft.uf;
-                        else if (ft.area != 0.0f) qexact = false;
-                    }
-                    if (unknown) {
-                        if (unit) {
-                            dg = pick7(fp.w_sum, nopen);
-                        } else {
-#pragma unroll
-                            for (int nq = 0; nq < 6; ++nq)
-                                if (has[nq] && fs[nq].r > 0.0f) dg += face_w(fs[nq], dt, dx, fp);
-                        }
-                        if (!(qexact && exact_sum(terms, 6, 0x15u, fp.inv_dx_exp, rhs))) {  // 0x15: the + faces negate
-                            rhs = 0.0;
-#pragma unroll
-                            for (int nq = 0; nq < 6; ++nq) {
-                                if (!has[nq]) continue;
-                                const FaceTerm ft = fs[nq];
-                                const double q = ft.area ? div_dx((double)ft.area * (double)ft.uf, dx, fp) : 0.0;
-                                rhs += (nq & 1) == 0 ? -q : q;
-                            }
+                for (int nq = 0; nq < 6; ++nq) {
+                    if (!has[nq]) continue;
+                    const FaceTerm ft = fs[nq];
+                    if (ft.r > 0.0f) {  // open face
+                        nopen++;
+                        unit = unit && ft.area == 1.0f && ft.r == 1.0f;
+                        if (fn[nq] < 0.0f) {
+                            unknown = true;
+                            if ((nq & 1) == 0) cpl[nq >> 1] = face_w(ft, dt, dx, fp);
                         }
                     }
+                    if (ft.area == 1.0f) terms[nq] = ft.uf;
+                    else if (ft.area != 0.0f) qexact = false;
                 }
                 if (unknown) {
-                    my_count++;
-                    if (rhs_correct) rhs += rhs_correct;  // macpressuresolver3.cpp:212-214
-                } else {
-                    dg = rhs = 0.0;
-                    cpl[0] = cpl[1] = cpl[2] = 0.0;
+                    if (unit) {
+                        dg = pick7(fp.w_sum, nopen);
+                    } else {
+#pragma unroll
+                        for (int nq = 0; nq < 6; ++nq)
+                            if (has[nq] && fs[nq].r > 0.0f) dg += face_w(fs[nq], dt, dx, fp);
+                    }
+                    // 0x15: the + faces' terms are negated
+                    if (!(qexact && exact_sum(terms, 6, 0x15u, fp.inv_dx_exp, rhs))) {
+                        rhs = 0.0;
+#pragma unroll
+                        for (int nq = 0; nq < 6; ++nq) {
+                            if (!has[nq]) continue;
+                            const FaceTerm ft = fs[nq];
+                            const double q = ft.area ? div_dx((double)ft.area * (double)ft.uf, dx, fp) : 0.0;
+                            rhs += (nq & 1) == 0 ? -q : q;
+                        }
+                    }
                 }
-                diag[c] = dg;
-                b[c] = rhs;
-                cx[c] = cpl[0];
-                cy[c] = cpl[1];
-                cz[c] = cpl[2];
-                if (o.diag) {
-                    const float d32 = d2f_rn(dg);
-                    o.diag[c] = d32;
-                    o.inv[c] = dg > 0.0 ? __frcp_rn(d32) : 0.0f;
-                    o.cx[c] = d2f_rn(cpl[0]);
-                    o.cy[c] = d2f_rn(cpl[1]);
-                    o.cz[c] = d2f_rn(cpl[2]);
-                }
-                if (o.inv64) o.inv64[c] = dg > 0.0 ? (unit ? pick7(fp.inv_sum, nopen) : 1.0 / dg) : 0.0;
             }
+            if (unknown) {
+                my_count++;
+                if (rhs_correct) rhs += rhs_correct;  // macpressuresolver3.cpp:212-214
+            } else {
+                dg = rhs = 0.0;
+                cpl[0] = cpl[1] = cpl[2] = 0.0;
+            }
+            diag[c] = dg;
+            b[c] = rhs;
+            cx[c] = cpl[0];
+            cy[c] = cpl[1];
+            cz[c] = cpl[2];
+            if (o.diag) {
+                const float d32 = d2f_rn(dg);
+                o.diag[c] = d32;
+                o.inv[c] = dg > 0.0 ? __frcp_rn(d32) : 0.0f;
+                o.cx[c] = d2f_rn(cpl[0]);
+                o.cy[c] = d2f_rn(cpl[1]);
+                o.cz[c] = d2f_rn(cpl[2]);
+            }
+            if (o.inv64) o.inv64[c] = dg > 0.0 ? (unit ? pick7(fp.inv_sum, nopen) : 1.0 / dg) : 0.0;
+            // carry: this plane's top nodes, levels and +z face
+            c00 = L.s00;
+            c10 = L.s10;
+            c01 = L.s01;
+            c11 = L.s11;
+            fm = fk;
+            fk = L.fz1;
             zlo = zhi;
         }
     }
@@ -839,6 +857,77 @@ __global__ void __launch_bounds__(BLOCK_THREADS) assemble_cells_kernel(
         for (int q = 0; q < BLOCK_THREADS / 32; ++q) s += sh_count[q];
         if (s) atomicAdd(&sc->unknowns, s);
         if (any_fluid) atomicOr(&sc->fluid_exists, 1);
+    }
+}
+
+// The new velocity of one face from its stored fraction (fr), the pressures
+// on its two sides and its velocity; interior: not on the domain boundary.
+// Open faces get u - (float)(dt (pc - pm) / (rho dx)), every other face 0.
+__device__ __forceinline__ float face_update(float fr, bool interior, float pc, float pm, float uf,
+                                             int fluid_exists, double dt, double dx, const FaceParams &fp) {
+    const bool open = fluid_exists ? fr > 0.0f : fr != 0.0f;
+    const float rho = fluid_exists ? fr : 1.0f;
+    if (!open || !interior) return 0.0f;
+    const float dp = pc - pm;
+    // rho * dx == dx exactly when rho == 1; (float)(dt dp / dx) by integer
+    // instructions where they decide (gbp_exact.cuh)
+    float vv;
+    if (rho == 1.0f && mul_round(fp.dt_mul, dp, vv)) return uf - vv;
+    const double val = rho == 1.0f ? div_dx(dt * (double)dp, dx, fp) : dt * (double)dp / ((double)rho * dx);
+    return uf - (float)val;
+}
+
+// Float pressure and velocity update in one pass (3D, no warm start): a
+// thread walks the column of cells (i, j) through zslab planes, writes
+// p = (float)x on the unknowns (0 elsewhere, as pressure_kernel) and
+// updates the -x, -y and -z faces of its cell (and the domain-boundary
+// faces at nx, ny, nz of the last column, row and plane) as
+// velocity_faces_kernel does. The pressures across the -x and -y faces are
+// formed again from x and the diagonal (the same integer conversion), the
+// one across -z is carried from the plane below.
+__global__ void __launch_bounds__(BLOCK_THREADS) pressure_velocity_kernel(
+    Grid g, double dt, double dx, FaceParams fp, int zslab, const double *__restrict__ diag,
+    const double *__restrict__ x, float *__restrict__ p, const float *__restrict__ rho_x,
+    const float *__restrict__ rho_y, const float *__restrict__ rho_z, float *__restrict__ u, float *__restrict__ v,
+    float *__restrict__ w, const Scalars *__restrict__ sc) {
+    const int fluid_exists = sc->fluid_exists;
+    const int tx = threadIdx.x & (TILE_X - 1), ty = threadIdx.x / TILE_X;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const long long cy_ = nx, cz_ = (long long)nx * ny;      // cells, w faces
+    const long long uy = nx + 1, uz = uy * ny;               // u faces
+    const long long vy = nx, vz = (long long)nx * (ny + 1);  // v faces
+    const int nzs = (nz + zslab - 1) / zslab;
+    const long long items = (long long)g.ntx * g.nty * nzs;
+    auto pres = [&](long long c) {  // pressure_kernel's p at cell c
+        const double d = __ldg(diag + c), xv = __ldg(x + c);
+        return d != 0.0 ? d2f_rn(xv) : 0.0f;
+    };
+    for (long long t = blockIdx.x; t < items; t += gridDim.x) {
+        const long long tz = t / ((long long)g.ntx * g.nty);
+        const long long rem = t - tz * g.ntx * g.nty;
+        const int i = (int)(rem % g.ntx) * TILE_X + tx, j = (int)(rem / g.ntx) * TILE_Y + ty;
+        if (i >= nx || j >= ny) continue;
+        const int kb = (int)tz * zslab, ke = min(kb + zslab, nz);
+        float pdown = kb > 0 ? pres(i + cy_ * j + cz_ * (kb - 1)) : 0.0f;
+        for (int k = kb; k < ke; ++k) {
+            const long long c = i + cy_ * j + cz_ * k;
+            const long long fu = i + uy * j + uz * k, fv = i + vy * j + vz * k;
+            // every load of the plane first
+            const float pc = pres(c);
+            const float px = i > 0 ? pres(c - 1) : 0.0f;
+            const float py = j > 0 ? pres(c - cy_) : 0.0f;
+            const float rx = __ldg(rho_x + fu), ry = __ldg(rho_y + fv), rz = __ldg(rho_z + c);
+            const float ux = u[fu], vy_ = v[fv], wz = w[c];
+            p[c] = pc;
+            u[fu] = face_update(rx, i > 0, pc, px, ux, fluid_exists, dt, dx, fp);
+            v[fv] = face_update(ry, j > 0, pc, py, vy_, fluid_exists, dt, dx, fp);
+            w[c] = face_update(rz, k > 0, pc, pdown, wz, fluid_exists, dt, dx, fp);
+            // the domain-boundary faces above the last column, row and plane
+            if (i + 1 == nx) u[fu + 1] = 0.0f;
+            if (j + 1 == ny) v[fv + vy] = 0.0f;
+            if (k + 1 == nz) w[c + cz_] = 0.0f;
+            pdown = pc;
+        }
     }
 }
 
@@ -856,20 +945,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_faces_kernel(Grid g, d
     const long long total = NX * NY * NZ;
     float *vel[3] = {u, v, w};
     const int n[3] = {g.nx, g.ny, g.nz};
-    // the new velocity of one face from its stored fraction (fr), the
-    // pressures on its two sides and its velocity; interior: not on the
-    // domain boundary
     auto update = [&](float fr, bool interior, float pc, float pm, float uf) {
-        const bool open = fluid_exists ? fr > 0.0f : fr != 0.0f;
-        const float rho = fluid_exists ? fr : 1.0f;
-        if (!open || !interior) return 0.0f;
-        const float dp = pc - pm;
-        // rho * dx == dx exactly when rho == 1; (float)(dt dp / dx) by integer
-        // instructions where they decide (gbp_exact.cuh)
-        float vv;
-        if (rho == 1.0f && mul_round(fp.dt_mul, dp, vv)) return uf - vv;
-        const double val = rho == 1.0f ? div_dx(dt * (double)dp, dx, fp) : dt * (double)dp / ((double)rho * dx);
-        return uf - (float)val;
+        return face_update(fr, interior, pc, pm, uf, fluid_exists, dt, dx, fp);
     };
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
@@ -1048,6 +1125,20 @@ cudaError_t launch_assemble_cells(const Grid &g, double dt, double dx, const Set
     assemble_cells_kernel<<<blocks < 1 ? 1 : blocks, BLOCK_THREADS, 0, stream>>>(
         g, dt, dx, fp, sp.rhs_correct, zslab, solid, fluid, u, v, w, fa.rho[0], fa.rho[1], fa.rho[2], diag, cx, cy, cz,
         b, o, sc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pressure_velocity(const Grid &g, double dt, double dx, const SetupParams &sp, const double *diag,
+                                     const double *x, float *p, FaceArrays fa, float *u, float *v, float *w,
+                                     const Scalars *sc, int grid_blocks, cudaStream_t stream) {
+    if (g.dim != 3) return cudaErrorInvalidValue;
+    const FaceParams fp = face_params(sp, dx, dt);
+    int zslab = 32;
+    while (zslab > 4 && (long long)g.ntx * g.nty * ((g.nz + zslab - 1) / zslab) < 2LL * grid_blocks) zslab /= 2;
+    const long long items = (long long)g.ntx * g.nty * ((g.nz + zslab - 1) / zslab);
+    const int blocks = (int)(items < grid_blocks ? items : grid_blocks);
+    pressure_velocity_kernel<<<blocks < 1 ? 1 : blocks, BLOCK_THREADS, 0, stream>>>(
+        g, dt, dx, fp, zslab, diag, x, p, fa.rho[0], fa.rho[1], fa.rho[2], u, v, w, sc);
     return cudaGetLastError();
 }
 

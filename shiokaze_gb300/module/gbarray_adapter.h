@@ -25,9 +25,13 @@
 #include <shiokaze/array/array3.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstddef>
+#include <cstring>
 #include <thread>
 #include <vector>
+
+#include "gbp.h"
 
 namespace gbarray {
 
@@ -86,5 +90,94 @@ template <class T> void densify(const shiokaze_v1::array2<T> &a, float *out) {
     for (int j = 0; j < (int)s.h; ++j)
         for (int i = 0; i < (int)s.w; ++i) out[n++] = (float)a(i, j);
 }
+
+// ---- bricks: the sparse form that travels to the GPU (include/gbp.h) ----
+//
+// to_bricks() cuts a 3D tiled array into bricks of 8^3 cells: a brick with
+// an active cell, or with some but not all of its cells filled, is listed
+// with its 512 values (operator()'s: stored values of active cells, the
+// fill value on filled cells, the background elsewhere; cells beyond the
+// extent hold the background); a brick whose cells are all filled and none
+// active is GBP_BRICK_FILL; the rest GBP_BRICK_BACKGROUND. Two passes over
+// the active and the filled cells (counting, then writing); the cost
+// follows the band and the filled region, and nothing is written for
+// background bricks.
+struct Bricks {
+    std::vector<int> slot;
+    std::vector<float> values;
+    float background = 0.0f, fill = 0.0f;
+    int nbx = 0, nby = 0, nbz = 0;
+    long long count() const { return (long long)(values.size() / GBP_BRICK_CELLS); }
+    gbp_bricks view() const { return gbp_bricks{background, fill, slot.data(), count(), values.data()}; }
+    size_t brick(int i, int j, int k) const { return (size_t)(i >> 3) + (size_t)nbx * ((j >> 3) + (size_t)nby * (k >> 3)); }
+    static int offset(int i, int j, int k) { return (i & 7) + 8 * ((j & 7) + 8 * (k & 7)); }
+};
+
+template <class T> void to_bricks(const shiokaze_v1::array3<T> &a, Bricks &out) {
+    const shiokaze_v1::shape3 s = a.shape();
+    out.nbx = ((int)s.w + 7) / 8;
+    out.nby = ((int)s.h + 7) / 8;
+    out.nbz = ((int)s.d + 7) / 8;
+    const size_t nb = (size_t)out.nbx * out.nby * out.nbz;
+    out.background = (float)a.get_background_value();
+    std::vector<std::atomic<int>> nact(nb), nfill(nb);
+    std::atomic<unsigned> fill_bits{0};
+    using It = typename shiokaze_v1::array3<T>::const_iterator;
+    a.const_parallel_actives([&](int i, int j, int k, const It &) {
+        nact[out.brick(i, j, k)].fetch_add(1, std::memory_order_relaxed);
+    });
+    a.const_parallel_inside([&](int i, int j, int k, const It &it) {
+        nfill[out.brick(i, j, k)].fetch_add(1, std::memory_order_relaxed);
+        if (!it.active()) {  // a filled cell reads the fill value
+            const float f = (float)it();
+            unsigned b;
+            std::memcpy(&b, &f, sizeof b);
+            fill_bits.store(b, std::memory_order_relaxed);
+        }
+    });
+    const unsigned fb = fill_bits.load();
+    std::memcpy(&out.fill, &fb, sizeof fb);
+    out.slot.assign(nb, GBP_BRICK_BACKGROUND);
+    long long count = 0;
+    for (int bz = 0; bz < out.nbz; ++bz)
+        for (int by = 0; by < out.nby; ++by)
+            for (int bx = 0; bx < out.nbx; ++bx) {
+                const size_t b = (size_t)bx + (size_t)out.nbx * (by + (size_t)out.nby * bz);
+                const int cells = std::min(8, (int)s.w - 8 * bx) * std::min(8, (int)s.h - 8 * by) *
+                                  std::min(8, (int)s.d - 8 * bz);
+                const int na = nact[b].load(), nf = nfill[b].load();
+                if (!na && !nf) continue;
+                out.slot[b] = (!na && nf == cells) ? GBP_BRICK_FILL : (int)count++;
+            }
+    out.values.assign((size_t)count * GBP_BRICK_CELLS, out.background);
+    a.const_parallel_inside([&](int i, int j, int k, const It &it) {
+        const int sl = out.slot[out.brick(i, j, k)];
+        if (sl >= 0 && !it.active()) out.values[(size_t)sl * GBP_BRICK_CELLS + Bricks::offset(i, j, k)] = (float)it();
+    });
+    a.const_parallel_actives([&](int i, int j, int k, const It &it) {
+        const int sl = out.slot[out.brick(i, j, k)];
+        out.values[(size_t)sl * GBP_BRICK_CELLS + Bricks::offset(i, j, k)] = (float)it();
+    });
+}
+
+// Output bricks: the slots, and the values and flags gbp_project_bricks
+// fills.
+struct BricksOut {
+    std::vector<int> slot;
+    std::vector<float> values;
+    std::vector<unsigned char> active;
+    int nbx = 0, nby = 0;
+    gbp_bricks_out view() {
+        return gbp_bricks_out{slot.data(), (long long)(values.size() / GBP_BRICK_CELLS), values.data(), active.data()};
+    }
+    size_t index(int i, int j, int k) const {
+        const size_t b = (size_t)(i >> 3) + (size_t)nbx * ((j >> 3) + (size_t)nby * (k >> 3));
+        return (size_t)slot[b] * GBP_BRICK_CELLS + Bricks::offset(i, j, k);
+    }
+    void resize(long long count) {
+        values.assign((size_t)count * GBP_BRICK_CELLS, 0.0f);
+        active.assign((size_t)count * GBP_BRICK_CELLS, 0);
+    }
+};
 
 }  // namespace gbarray

@@ -5,11 +5,12 @@
 // with Projection=gbprojection3; compiled against the reference's headers
 // and linked to libgbp.so.
 //
-// The reference's arrays are sparse (tiled, narrow band); project() copies
-// them to dense arrays with exactly operator()'s values (background, fill
-// and active values; gbarray_adapter.h, one pass over the filled and active
-// cells instead of one lookup per cell) and calls gbp_project_active. The
-// output state is the reference's: the projected velocity is written to the
+// The reference's arrays are sparse (tiled, narrow band); project() cuts
+// them into bricks of 8^3 cells with exactly operator()'s values
+// (background, fill and active values; gbarray_adapter.h, passes over the
+// filled and active cells only) and calls gbp_project_bricks, which ships
+// the listed bricks, expands them on the GPU and returns the listed output
+// bricks. The output state is the reference's: the projected velocity is written to the
 // faces that were active, as its velocity update iterates actives
 // (macpressuresolver3.cpp:252), and the faces it deactivates there (closed
 // faces that are not walls next to fluid, :264-266) are turned off with
@@ -20,6 +21,7 @@
 #include <shiokaze/core/console.h>
 #include <shiokaze/projection/macproject3_interface.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "gbarray_adapter.h"
@@ -42,17 +44,37 @@ protected:
                          double surface_tension, const std::vector<signed_rigidbody3_interface *> *) override {
         const int nx = m_shape.w, ny = m_shape.h, nz = m_shape.d;
         m_params.surface_tension = surface_tension;
-        std::vector<float> s((size_t)(nx + 1) * (ny + 1) * (nz + 1)), f((size_t)nx * ny * nz), p(f.size());
         expect_shape(solid.shape(), nx + 1, ny + 1, nz + 1, "solid");
         expect_shape(fluid.shape(), nx, ny, nz, "fluid");
-        gbarray::densify(solid, s.data());
-        gbarray::densify(fluid, f.data());
-        std::vector<float> vel[3];
+        // the inputs as bricks (only the listed ones travel; the GPU expands them)
+        gbarray::Bricks bs, bf, bv[3];
+        gbarray::to_bricks(solid, bs);
+        gbarray::to_bricks(fluid, bf);
         for (int d = 0; d < 3; ++d) {
-            const int fx = nx + (d == 0), fy = ny + (d == 1), fz = nz + (d == 2);
-            expect_shape(velocity[d].shape(), fx, fy, fz, "velocity");
-            vel[d].resize((size_t)fx * fy * fz);
-            gbarray::densify(velocity[d], vel[d].data());
+            expect_shape(velocity[d].shape(), nx + (d == 0), ny + (d == 1), nz + (d == 2), "velocity");
+            gbarray::to_bricks(velocity[d], bv[d]);
+        }
+        // outputs: the velocity where it has active faces (its listed
+        // bricks); the pressure where a cell can be fluid (a listed brick of
+        // the fluid level set, or a filled or background one whose value is
+        // negative)
+        gbarray::BricksOut po, vo[3];
+        po.nbx = bf.nbx;
+        po.nby = bf.nby;
+        po.slot.assign(bf.slot.size(), -1);
+        long long pc = 0;
+        for (size_t b = 0; b < bf.slot.size(); ++b) {
+            const int sl = bf.slot[b];
+            if (sl >= 0 || (sl == GBP_BRICK_FILL && bf.fill < 0.0f) || (sl == GBP_BRICK_BACKGROUND && bf.background < 0.0f))
+                po.slot[b] = (int)pc++;
+        }
+        po.resize(pc);
+        for (int d = 0; d < 3; ++d) {
+            vo[d].nbx = bv[d].nbx;
+            vo[d].nby = bv[d].nby;
+            vo[d].slot.resize(bv[d].slot.size());
+            for (size_t b = 0; b < bv[d].slot.size(); ++b) vo[d].slot[b] = bv[d].slot[b] >= 0 ? bv[d].slot[b] : -1;
+            vo[d].resize(bv[d].count());
         }
         if (!m_scene) {
             gbprojection::check(gbp_create(m_device, &m_ctx), "gbp_create");
@@ -60,25 +82,30 @@ protected:
             if (m_target_volume) gbp_scene_set_target_volume(m_scene, m_current_volume, m_target_volume);
         }
         gbp_stats st;
-        std::vector<unsigned char> unknown(f.size()), on[3];
-        for (int d = 0; d < 3; ++d) on[d].resize(vel[d].size());
-        int rc = gbp_project_active(m_scene, dt, s.data(), f.data(), vel[0].data(), vel[1].data(), vel[2].data(),
-                                    &m_params, p.data(), &st, unknown.data(), on[0].data(), on[1].data(),
-                                    on[2].data());
-        gbprojection::check(rc, "gbp_project_active");
+        const gbp_bricks in_s = bs.view(), in_f = bf.view(), in_u = bv[0].view(), in_v = bv[1].view(),
+                         in_w = bv[2].view();
+        gbp_bricks_out out_p = po.view(), out_u = vo[0].view(), out_v = vo[1].view(), out_w = vo[2].view();
+        int rc = gbp_project_bricks(m_scene, dt, &in_s, &in_f, &in_u, &in_v, &in_w, &m_params, &out_p, &out_u, &out_v,
+                                    &out_w, &st);
+        gbprojection::check(rc, "gbp_project_bricks");
         console::dump("gbprojection3: %d iterations, Reresid=%e, %.3f ms\n", st.iterations, st.reresid, st.ms_total);
         console::write(get_argument_name() + "_number_projection_iteration", st.iterations);
         m_pressure.clear();
-        for (int k = 0; k < nz; ++k)
-            for (int j = 0; j < ny; ++j)
-                for (int i = 0; i < nx; ++i) {
-                    const size_t n = i + (size_t)nx * (j + (size_t)ny * k);
-                    if (unknown[n]) m_pressure.set(i, j, k, p[n]);
+        for (int bz = 0; bz < bf.nbz; ++bz)
+            for (int by = 0; by < bf.nby; ++by)
+                for (int bx = 0; bx < bf.nbx; ++bx) {
+                    const int sl = po.slot[(size_t)bx + (size_t)bf.nbx * (by + (size_t)bf.nby * bz)];
+                    if (sl < 0) continue;
+                    for (int k = 8 * bz; k < std::min(8 * bz + 8, nz); ++k)
+                        for (int j = 8 * by; j < std::min(8 * by + 8, ny); ++j)
+                            for (int i = 8 * bx; i < std::min(8 * bx + 8, nx); ++i) {
+                                const size_t n = po.index(i, j, k);
+                                if (po.active[n]) m_pressure.set(i, j, k, po.values[n]);
+                            }
                 }
         velocity.parallel_actives([&](int dim, int i, int j, int k, auto &it, int tn) {
-            const int fx = nx + (dim == 0), fy = ny + (dim == 1);
-            const size_t n = i + (size_t)fx * (j + (size_t)fy * k);
-            if (on[dim][n]) it.set(vel[dim][n]);
+            const size_t n = vo[dim].index(i, j, k);
+            if (vo[dim].active[n]) it.set(vo[dim].values[n]);
             else it.set_off();
         });
     }

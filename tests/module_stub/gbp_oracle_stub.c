@@ -4,7 +4,7 @@
  * liboracle.so) on the CPU, and the same for the solid constraint of the
  * velocity, its extrapolation, and the projection (oracle/gbp_oracle.c: scenes, volume
  * correction, warm start, gbp_project / gbp_project_active with the active
- * sets). tests/test_oracle.py links the gbadvection3, gbutility3 and
+ * sets, gbp_project_bricks on the expanded bricks). tests/test_oracle.py links the gbadvection3, gbutility3 and
  * gbprojection2/3 plugin modules against it to check the modules' boundary
  * (dense copies of the reference's tiled arrays, the active masks, the
  * write-back over active faces and cells, the faces turned off, the
@@ -193,4 +193,71 @@ int gbp_project_active(gbp_scene *s, double dt, const float *solid, const float 
 int gbp_project(gbp_scene *s, double dt, const float *solid, const float *fluid, float *u, float *v, float *w,
                 const gbp_params *params, float *pressure, gbp_stats *stats) {
     return gbp_project_active(s, dt, solid, fluid, u, v, w, params, pressure, stats, NULL, NULL, NULL, NULL);
+}
+
+/* gbp_project_bricks / gbp_bricks_expand on the CPU: the bricks expanded
+ * to dense arrays (the rule of include/gbp.h), gbp_project_active above on
+ * them, and the listed output bricks gathered back. */
+static void stub_expand(int nx, int ny, int nz, const gbp_bricks *in, float *dense) {
+    const int nbx = (nx + 7) / 8, nby = (ny + 7) / 8;
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const int sl = in->slot[(i >> 3) + (size_t)nbx * ((j >> 3) + (size_t)nby * (k >> 3))];
+                float val = in->background;
+                if (sl >= 0) val = in->values[(size_t)sl * GBP_BRICK_CELLS + (i & 7) + 8 * ((j & 7) + 8 * (k & 7))];
+                else if (sl == GBP_BRICK_FILL) val = in->fill;
+                dense[i + (size_t)nx * (j + (size_t)ny * k)] = val;
+            }
+}
+
+static void stub_gather(int nx, int ny, int nz, const float *dense, const unsigned char *flags, gbp_bricks_out *o) {
+    const int nbx = (nx + 7) / 8, nby = (ny + 7) / 8, nbz = (nz + 7) / 8;
+    for (int bz = 0; bz < nbz; ++bz)
+        for (int by = 0; by < nby; ++by)
+            for (int bx = 0; bx < nbx; ++bx) {
+                const int sl = o->slot[bx + (size_t)nbx * (by + (size_t)nby * bz)];
+                if (sl < 0) continue;
+                for (int c = 0; c < GBP_BRICK_CELLS; ++c) {
+                    const int i = 8 * bx + (c & 7), j = 8 * by + ((c >> 3) & 7), k = 8 * bz + (c >> 6);
+                    const size_t n = (size_t)sl * GBP_BRICK_CELLS + c;
+                    const int in = i < nx && j < ny && k < nz;
+                    const size_t d = i + (size_t)nx * (j + (size_t)ny * k);
+                    o->values[n] = in ? dense[d] : 0.0f;
+                    if (o->active) o->active[n] = in ? flags[d] : 0;
+                }
+            }
+}
+
+int gbp_bricks_expand(gbp_ctx *ctx, int nx, int ny, int nz, const gbp_bricks *in, float *dense, void *stream) {
+    (void)ctx;
+    (void)stream;
+    stub_expand(nx, ny, nz, in, dense);
+    return GBP_OK;
+}
+
+int gbp_project_bricks(gbp_scene *s, double dt, const gbp_bricks *solid, const gbp_bricks *fluid, const gbp_bricks *u,
+                       const gbp_bricks *v, const gbp_bricks *w, const gbp_params *params, gbp_bricks_out *pressure,
+                       gbp_bricks_out *u_out, gbp_bricks_out *v_out, gbp_bricks_out *w_out, gbp_stats *stats) {
+    const int nx = s->nx, ny = s->ny, nz = s->nz;
+    const int ext[5][3] = {{nx + 1, ny + 1, nz + 1}, {nx, ny, nz}, {nx + 1, ny, nz}, {nx, ny + 1, nz}, {nx, ny, nz + 1}};
+    const gbp_bricks *in[5] = {solid, fluid, u, v, w};
+    float *dense[5];
+    unsigned char *flags[4];
+    for (int a = 0; a < 5; ++a) {
+        dense[a] = (float *)malloc(sizeof(float) * (size_t)ext[a][0] * ext[a][1] * ext[a][2]);
+        stub_expand(ext[a][0], ext[a][1], ext[a][2], in[a], dense[a]);
+    }
+    for (int o = 0; o < 4; ++o) flags[o] = (unsigned char *)malloc((size_t)ext[o + 1][0] * ext[o + 1][1] * ext[o + 1][2]);
+    float *p = (float *)malloc(sizeof(float) * (size_t)nx * ny * nz);
+    const int rc = gbp_project_active(s, dt, dense[0], dense[1], dense[2], dense[3], dense[4], params, p, stats,
+                                      flags[0], flags[1], flags[2], flags[3]);
+    gbp_bricks_out *outs[4] = {pressure, u_out, v_out, w_out};
+    const float *src[4] = {p, dense[2], dense[3], dense[4]};
+    for (int o = 0; o < 4; ++o)
+        if (outs[o]) stub_gather(ext[o + 1][0], ext[o + 1][1], ext[o + 1][2], src[o], flags[o], outs[o]);
+    for (int a = 0; a < 5; ++a) free(dense[a]);
+    for (int o = 0; o < 4; ++o) free(flags[o]);
+    free(p);
+    return rc;
 }

@@ -127,6 +127,26 @@ def test_linsolver_module_loads_through_reference_loader(tmp_path):
 
 
 @pytest.mark.skipif(not oracle.reference_available(), reason="reference oracle not built here")
+@pytest.mark.parametrize("kind,n", [("liquid3", 48), ("liquid3", (40, 33, 37)), ("smoke3", 40), ("liquid3", 64)])
+def test_module_bricks_match_operator_reads(kind, n):
+    """The plugin modules' bricks of the reference's tiled arrays
+    (gbarray_adapter.h to_bricks: listed bricks where a cell is active or
+    some cells are filled, whole-fill and background bricks by kind),
+    expanded by gbp.h's rule, equal reading every cell through the
+    reference's operator() bit for bit; a narrow-band level set lists only
+    a fraction of its bricks (its filled interior travels as fill bricks)."""
+    sc = getattr(scenes, kind)(n, seed=5)
+    vel_band = float(np.quantile(np.abs(sc.u), 0.4))
+    for arr, mode, band in ((sc.solid, sc.solid_mode, sc.band), (sc.fluid, sc.fluid_mode, sc.band),
+                            (sc.u, 2, vel_band), (sc.w, 2, vel_band)):
+        a, b, counts, _, _, _, _ = oracle.ref_bricks_compare(arr, mode, band)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    if kind == "liquid3":
+        _, _, counts, _, _, _, _ = oracle.ref_bricks_compare(sc.fluid, sc.fluid_mode, sc.band)
+        assert counts[1] > 0 and counts[2] > 0 and counts[0] < 0.6 * counts.sum(), counts
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference oracle not built here")
 @pytest.mark.parametrize("kind,n", [("liquid3", 48), ("liquid3", (40, 33, 37)), ("smoke3", 40), ("liquid2", 160),
                                     ("liquid2", (150, 97))])
 def test_module_densify_matches_operator_reads(kind, n):
