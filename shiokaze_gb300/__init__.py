@@ -144,7 +144,7 @@ def bricks_expand(nx, ny, nz, bricks, dense, context: "Context | None" = None, s
     returns them)."""
     ctx = context or default_context()
     b = _bricks_struct(bricks)
-    check(load_library().gbp_bricks_expand(ctx.ctx, nx, ny, nz, ctypes.byref(b), dense.data_ptr(),
+    check(load_library().gbp_bricks_expand(ctx.handle, nx, ny, nz, ctypes.byref(b), dense.data_ptr(),
                                            ctypes.c_void_p(stream) if stream else None))
 
 

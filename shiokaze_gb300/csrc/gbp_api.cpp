@@ -300,23 +300,15 @@ int ensure_staging(gbp_scene *s) {
 
 // Volume-correction constant (macpressuresolver3.cpp:204-217); advances the
 // controller's integral state once per projection.
-// Face fractions, operator and right-hand side of one scene: in 3D one
-// fused pass that also writes level 0 of the solver's hierarchy (o), in 2D
-// the face pass and the cell pass.
+// Face fractions, operator and right-hand side of one scene (the face pass
+// and the cell pass), and level 0 of the solver's hierarchy o names.
 cudaError_t launch_setup(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
                          const float *fluid, const float *u, const float *v, const float *w, SolverState &st,
                          Level0Out o, int grid_blocks, cudaStream_t stream, long long *launches) {
-    cudaError_t e;
-    if (g.dim == 3) {
-        e = launch_assemble_cells(g, dt, dx, sp, solid, fluid, u, v, w, st.faces, st.diag, st.cx, st.cy, st.cz, st.b,
-                                  o, st.sc, grid_blocks, stream);
-        *launches += 1;
-        return e;
-    }
-    e = launch_faces(g, dt, dx, sp, solid, fluid, u, v, w, st.faces, grid_blocks, stream);
+    cudaError_t e = launch_faces(g, dt, dx, sp, solid, fluid, u, v, w, st.faces, grid_blocks, stream);
     if (e == cudaSuccess)
-        e = launch_assemble_faces(g, sp, fluid, st.faces, st.diag, st.cx, st.cy, st.cz, st.b, st.sc, grid_blocks,
-                                  stream);
+        e = launch_assemble_faces(g, dt, dx, sp, fluid, u, v, w, st.faces, st.diag, st.cx, st.cy, st.cz, st.b, o,
+                                  st.sc, grid_blocks, stream);
     *launches += 2;
     return e;
 }
@@ -325,7 +317,7 @@ cudaError_t launch_setup(const Grid &g, double dt, double dx, const SetupParams 
 int setup_for_solve(gbp_scene *s, const Grid &g, double dt, const SetupParams &sp, const gbp_params &p,
                     const float *solid, const float *fluid, const float *u, const float *v, const float *w,
                     int grid_blocks, cudaStream_t stream, long long *launches) {
-    const Level0Out o = g.dim == 3 ? s->solver->level0_out(p) : Level0Out{};
+    const Level0Out o = s->solver->level0_out(p);
     GBP_CUDA(launch_setup(g, dt, s->dx, sp, solid, fluid, u, v, w, s->solver->state(), o, grid_blocks, stream,
                           launches));
     if (o.diag || o.inv64) s->solver->level0_written();
@@ -403,25 +395,15 @@ int project_device(gbp_scene *s, double dt, const float *solid, const float *flu
     int solve_status = rc;
     GBP_CUDA(cudaEventRecord(c->ev[2], stream));
 
-    // 3D without warm start: the float pressure and the velocity update in
-    // one pass (after the active sets, which read the velocity before it)
-    const bool fused = g.dim == 3 && !p.warm_start;
-    if (!fused) {
-        GBP_CUDA(launch_pressure(g, st.diag, st.x, p.warm_start && st.have_prev ? st.prev : nullptr, pressure,
-                                 p.warm_start ? st.prev : nullptr, c->grid_blocks, stream));
-        c->launches += 1;
-    }
+    GBP_CUDA(launch_pressure(g, st.diag, st.x, p.warm_start && st.have_prev ? st.prev : nullptr, pressure,
+                             p.warm_start ? st.prev : nullptr, c->grid_blocks, stream));
     if (active_sets) {
         GBP_CUDA(launch_active_sets(g, st.faces, fluid, u, v, w, st.diag, s->d_unknown, s->d_on[0], s->d_on[1],
                                     s->d_on[2], st.sc, c->grid_blocks, stream));
         c->launches += 1;
     }
-    if (fused)
-        GBP_CUDA(launch_pressure_velocity(g, dt, s->dx, sp, st.diag, st.x, pressure, st.faces, u, v, w, st.sc,
-                                          c->grid_blocks, stream));
-    else
-        GBP_CUDA(launch_velocity_faces(g, dt, s->dx, sp, pressure, st.faces, u, v, w, st.sc, c->grid_blocks, stream));
-    c->launches += 1;
+    GBP_CUDA(launch_velocity_faces(g, dt, s->dx, sp, pressure, st.faces, u, v, w, st.sc, c->grid_blocks, stream));
+    c->launches += 2;
     if (p.warm_start) st.have_prev = true;
     GBP_CUDA(cudaEventRecord(c->ev[3], stream));
     GBP_CUDA(cudaStreamSynchronize(stream));
@@ -801,17 +783,11 @@ int gbp_batch_project_device(gbp_batch *b, const double *dt, const float *const 
         if (status != GBP_OK && first_bad == GBP_OK) first_bad = status;
         float *pout = pressure && pressure[i] ? pressure[i] : s->d_p;
         SetupParams sp{p.eps_solid, p.eps_fluid, p.second_order_solid, p.second_order_fluid, 0.0};
-        if (g.dim == 3 && !p.warm_start) {
-            GBP_CUDA(launch_pressure_velocity(g, dt[i], s->dx, sp, ss.diag, ss.x, pout, ss.faces, u[i], v[i], w[i],
-                                              ss.sc, c->grid_blocks, st));
-            launched += 1;
-        } else {
-            GBP_CUDA(launch_pressure(g, ss.diag, ss.x, p.warm_start && ss.have_prev ? ss.prev : nullptr, pout,
-                                     p.warm_start ? ss.prev : nullptr, c->grid_blocks, st));
-            GBP_CUDA(launch_velocity_faces(g, dt[i], s->dx, sp, pout, ss.faces, u[i], v[i],
-                                           g.dim == 3 ? w[i] : nullptr, ss.sc, c->grid_blocks, st));
-            launched += 2;
-        }
+        GBP_CUDA(launch_pressure(g, ss.diag, ss.x, p.warm_start && ss.have_prev ? ss.prev : nullptr, pout,
+                                 p.warm_start ? ss.prev : nullptr, c->grid_blocks, st));
+        GBP_CUDA(launch_velocity_faces(g, dt[i], s->dx, sp, pout, ss.faces, u[i], v[i], g.dim == 3 ? w[i] : nullptr,
+                                       ss.sc, c->grid_blocks, st));
+        launched += 2;
         if (p.warm_start) ss.have_prev = true;
     }
     GBP_CUDA(cudaEventRecord(c->ev[3], st));

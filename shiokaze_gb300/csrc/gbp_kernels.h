@@ -21,9 +21,14 @@ template <class T> struct Operator {
 // Per-face results of the face-first assembly, one array per face
 // direction, sized like that direction's face velocities.
 struct FaceArrays {
-    double *w[3];  // weight dt*area/(dx^2 rho) of open faces, -1 otherwise
-    double *q[3];  // area*u/dx (0 where area == 0)
-    float *rho[3]; // rho of open faces, -1 if only rho closes the face, 0 if area == 0
+    float *rho[3];   // rho of open faces, -1 if only rho closes the face, 0 if area == 0
+    float *area[3];  // open (solid) fraction, 0 on the domain boundary
+    // written only where the cell pass cannot form them from rho, area and
+    // the face velocity: the weight dt*area/(dx^2 rho) of an open face that
+    // is not area = rho = 1, the flux area*u/dx of a face with 0 < area and
+    // not (area = 1 with dx a power of two)
+    double *w[3];
+    double *q[3];
 };
 
 // Level-0 arrays of a multigrid hierarchy that the fused 3D assembly writes
@@ -43,20 +48,12 @@ cudaError_t launch_surface_tension(const Grid &g, double dt, double dx, const Se
 cudaError_t launch_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
                          const float *fluid, const float *u, const float *v, const float *w, FaceArrays fa,
                          int grid_blocks, cudaStream_t stream);
-cudaError_t launch_assemble_faces(const Grid &g, const SetupParams &sp, const float *fluid, FaceArrays fa,
-                                  double *diag, double *cx, double *cy, double *cz, double *b, Scalars *sc,
+// The cell pass; also writes level 0 of the hierarchy o names (null
+// pointers: nothing).
+cudaError_t launch_assemble_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *fluid,
+                                  const float *u, const float *v, const float *w, FaceArrays fa, double *diag,
+                                  double *cx, double *cy, double *cz, double *b, Level0Out o, Scalars *sc,
                                   int grid_blocks, cudaStream_t stream);
-// Fused 3D assembly (one pass; only the face fractions fa.rho are stored):
-// the same operator, right-hand side and fractions as launch_faces +
-// launch_assemble_faces, and level 0 of the hierarchy o names.
-cudaError_t launch_assemble_cells(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
-                                  const float *fluid, const float *u, const float *v, const float *w, FaceArrays fa,
-                                  double *diag, double *cx, double *cy, double *cz, double *b, Level0Out o,
-                                  Scalars *sc, int grid_blocks, cudaStream_t stream);
-// Fused 3D pressure_kernel + velocity_faces_kernel (no warm start).
-cudaError_t launch_pressure_velocity(const Grid &g, double dt, double dx, const SetupParams &sp, const double *diag,
-                                     const double *x, float *p, FaceArrays fa, float *u, float *v, float *w,
-                                     const Scalars *sc, int grid_blocks, cudaStream_t stream);
 cudaError_t launch_velocity_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *p,
                                   FaceArrays fa, float *u, float *v, float *w, const Scalars *sc, int grid_blocks,
                                   cudaStream_t stream);

@@ -54,7 +54,7 @@ static size_t face_count(const Grid &g, int d) {
 size_t solver_device_bytes(const Grid &g, const gbp_params &p) {
     const size_t cells = (size_t)g.ncell;
     size_t bytes = 8 * cells * (5 /*operator+b*/ + 4 /*x r s z*/ + (p.warm_start ? 1 : 0));
-    for (int d = 0; d < g.dim; ++d) bytes += (g.dim == 2 ? 20 : 4) * face_count(g, d);  // face arrays
+    for (int d = 0; d < g.dim; ++d) bytes += 24 * face_count(g, d);  // face arrays
     if (p.solver == GBP_SOLVER_MGPCG) {
         bytes += 8 * cells;  // q
         const size_t s = p.precision == GBP_PRECISION_MIXED ? 4 : 8;
@@ -101,15 +101,12 @@ int Solver::prepare(const Grid &g, const gbp_params &p) {
         SOLVER_CUDA(cudaMemset(st_.sc, 0, sizeof(Scalars)));
         SOLVER_CUDA(cudaMalloc(&st_.pt, sizeof(Partials)));
         SOLVER_CUDA(cudaMallocHost(&st_.host_sc, sizeof(Scalars)));
-        // weights and fluxes per face only for the 2D two-pass assembly (the
-        // fused 3D pass keeps them in registers); fractions for both
         for (int d = 0; d < 3; ++d) {
             const size_t nf = d < g.dim ? face_count(g, d) : 1;
-            if (g.dim == 2) {
-                SOLVER_CUDA(cudaMalloc(&st_.faces.w[d], 8 * nf));
-                SOLVER_CUDA(cudaMalloc(&st_.faces.q[d], 8 * nf));
-            }
             SOLVER_CUDA(cudaMalloc(&st_.faces.rho[d], 4 * nf));
+            SOLVER_CUDA(cudaMalloc(&st_.faces.area[d], 4 * nf));
+            SOLVER_CUDA(cudaMalloc(&st_.faces.w[d], 8 * nf));
+            SOLVER_CUDA(cudaMalloc(&st_.faces.q[d], 8 * nf));
         }
         allocated_ = true;
     }
@@ -214,6 +211,7 @@ void Solver::release() {
         if (st_.faces.w[d]) cudaFree(st_.faces.w[d]);
         if (st_.faces.q[d]) cudaFree(st_.faces.q[d]);
         if (st_.faces.rho[d]) cudaFree(st_.faces.rho[d]);
+        if (st_.faces.area[d]) cudaFree(st_.faces.area[d]);
     }
     st_ = SolverState();
     allocated_ = false;

@@ -96,27 +96,13 @@ struct FaceParams {
     MulConst dt_mul;
 };
 
-// (double)u * 2^e for a float u, built from u's bits with integer
-// instructions (exact: the product of a float and a power of two is a
-// double with u's mantissa and a shifted exponent). ok = false for
-// subnormal, infinite and NaN u, and for exponents out of range; the
-// caller then takes the FP64 path.
-__device__ __forceinline__ double scaled_to_double(float u, int e, bool &ok) {
-    const unsigned b = __float_as_uint(u);
-    const unsigned ex = (b >> 23) & 0xffu, man = b & 0x7fffffu;
-    const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
-    ok = true;
-    if (ex == 0u) {
-        if (man == 0u) return __longlong_as_double((long long)sign);  // +-0
-        ok = false;
-        return 0.0;
-    }
-    const int de = (int)ex + (1023 - 127) + e;
-    if (ex == 0xffu || de <= 0 || de >= 2047) {
-        ok = false;
-        return 0.0;
-    }
-    return __longlong_as_double((long long)(sign | ((unsigned long long)de << 52) | ((unsigned long long)man << 29)));
+// a[n] for n in [0, 7) by selects (an indexed kernel parameter would be
+// copied to local memory)
+__device__ __forceinline__ double pick7(const double (&a)[7], int n) {
+    double r = a[0];
+#pragma unroll
+    for (int q = 1; q < 7; ++q) r = n == q ? a[q] : r;
+    return r;
 }
 
 // x / dx, bit-identical either way (see FaceParams::dx_pow2)
@@ -463,16 +449,21 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_kernel(Grid g, double 
 // ---- face-first assembly ----------------------------------------------------------
 //
 // Pass 1, one thread per node of the (nx+1)(ny+1)(nz+1) lattice, for the x-,
-// y- and z-face with that lower corner: the face's weight, flux and
-// fraction, computed once per face:
-//   fw  = dt*area/(dx*dx*rho) if the face is open (area > 0, rho > 0), else -1
-//   fq  = area*u/dx (0 if area == 0): the face's term of b is -fq on a
-//         cell's +d face and +fq on its -d face, exactly the reference's
-//         -sgn*area*u/dx since negation is exact
-//   frho = rho if open, -1 if area > 0 but rho == 0, 0 if area == 0
-// Pass 2, one thread per cell, sums them in the reference's face order
-// (+x, -x, +y, -y, +z, -z), so diag, couplings and b are bit-identical to
-// the single-pass assemble_kernel (and to the reference).
+// y- and z-face with that lower corner: the face's fractions, computed once
+// per face, stored as
+//   rho  = rho if the face is open (area > 0, rho > 0), -1 if area > 0 but
+//          rho == 0, 0 if area == 0
+//   area = the open fraction
+// and, only where pass 2 cannot form them from these and the face velocity
+// (cut faces, or dx not a power of two), the FP64 weight dt*area/(dx*dx*rho)
+// and flux area*u/dx. Pass 2, one thread per cell, forms its row from its
+// faces in the reference's order (+x, -x, +y, -y, +z, -z): weight w_unit on
+// faces with area = rho = 1, flux u 2^k when area = 1 and 1/dx = 2^k (an
+// exact double), and the sums in integers where they are exact
+// (gbp_exact.cuh), so diag, couplings and b are bit-identical to the
+// single-pass assemble_kernel (and to the reference); it also writes level 0
+// of the multigrid hierarchy (the FP32 operator of the mixed solver, or the
+// FP64 inverse diagonal) from the same registers.
 __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt, double dx, FaceParams fp,
                                                               const float *__restrict__ solid,
                                                               const float *__restrict__ fluid,
@@ -486,14 +477,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt,
     // One face's outputs from its fractions and velocity.
     auto emit = [&](int d, long long f, float area, float rho, float uf) {
         const bool open = area && rho;
-        fa.w[d][f] = !open ? -1.0 : (area == 1.0f && rho == 1.0f) ? fp.w_unit
-                                                                    : face_weight(dt, (double)area, (double)rho, dx, fp);
-        double q = 0.0;
-        bool fast = false;
-        if (area == 1.0f && fp.dx_pow2) q = scaled_to_double(uf, fp.inv_dx_exp, fast);  // (1 * u) / dx, exactly
-        if (!fast) q = area ? div_dx((double)area * (double)uf, dx, fp) : 0.0;
-        fa.q[d][f] = q;
         fa.rho[d][f] = open ? rho : (area ? -1.0f : 0.0f);
+        fa.area[d][f] = area;
+        // the FP64 weight and flux only where the cell pass cannot form them
+        if (open && !(area == 1.0f && rho == 1.0f)) fa.w[d][f] = face_weight(dt, (double)area, (double)rho, dx, fp);
+        if (area != 0.0f && !(area == 1.0f && fp.dx_pow2)) fa.q[d][f] = div_dx((double)area * (double)uf, dx, fp);
     };
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
@@ -549,14 +537,17 @@ __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt,
     }
 }
 
-__global__ void __launch_bounds__(BLOCK_THREADS) assemble_faces_kernel(
-    Grid g, double rhs_correct, const float *__restrict__ fluid, FaceArrays fa, double *__restrict__ diag,
-    double *__restrict__ cx, double *__restrict__ cy, double *__restrict__ cz, double *__restrict__ b, Scalars *sc) {
+__global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_faces_kernel(
+    Grid g, double dt, double dx, FaceParams fp, double rhs_correct, const float *__restrict__ fluid,
+    const float *__restrict__ u, const float *__restrict__ v, const float *__restrict__ w, FaceArrays fa,
+    double *__restrict__ diag, double *__restrict__ cx, double *__restrict__ cy, double *__restrict__ cz,
+    double *__restrict__ b, Level0Out o, Scalars *sc) {
     __shared__ unsigned long long sh_count[BLOCK_THREADS / 32];
     const int tx = threadIdx.x & (TILE_X - 1), ty = threadIdx.x / TILE_X;
     unsigned long long my_count = 0;
     int my_fluid = 0;
     double *cp[3] = {cx, cy, cz};
+    const float *vel[3] = {u, v, w};
     for (long long t = blockIdx.x; t < g.ntiles; t += gridDim.x) {
         int i0, j0, k0;
         tile_origin(g, t, i0, j0, k0);
@@ -567,15 +558,22 @@ __global__ void __launch_bounds__(BLOCK_THREADS) assemble_faces_kernel(
             if (k >= g.nz) break;
             const long long c = cell_index(g, i, j, k);
             double dg = 0.0, rhs = 0.0, cpl[3] = {0.0, 0.0, 0.0};
-            bool unknown = false;
+            bool unknown = false, unit = true;
+            int nopen = 0;
             // every load of the cell's row first (its own level, and per face
-            // in the order +x, -x, +y, -y, +z, -z: fraction, weight, flux and
-            // the neighbour's level), then the row in that order
+            // in the order +x, -x, +y, -y, +z, -z: fraction, area, velocity
+            // and the neighbour's level), then the row in that order
             const int n[3] = {g.nx, g.ny, g.nz};
             const float fc = __ldg(fluid + c);
-            float fr[6], fq[6];
-            double wv[6], qv[6];
+            float fr[6], ar[6], uv[6], fq[6];
             bool has[6];
+            // the index of face nq (formed again where needed: fewer registers)
+            auto findex = [&](int nq) {
+                const int d = nq >> 1;
+                int f[3] = {i, j, k};
+                if ((nq & 1) == 0) f[d] += 1;
+                return face_index(g, d, f[0], f[1], f[2]);
+            };
 #pragma unroll
             for (int nq = 0; nq < 6; ++nq) {
                 const int d = nq >> 1;
@@ -583,199 +581,18 @@ __global__ void __launch_bounds__(BLOCK_THREADS) assemble_faces_kernel(
                 int q[3] = {i, j, k};
                 q[d] += plus ? 1 : -1;
                 has[nq] = d < g.dim && q[d] >= 0 && q[d] < n[d];
-                int f[3] = {i, j, k};
-                if (plus) f[d] += 1;
-                const long long fi = has[nq] ? face_index(g, d, f[0], f[1], f[2]) : 0;
+                const long long fi = has[nq] ? findex(nq) : 0;
                 fr[nq] = has[nq] ? __ldg(fa.rho[d] + fi) : 0.0f;
-                wv[nq] = has[nq] ? __ldg(fa.w[d] + fi) : 0.0;
-                qv[nq] = has[nq] ? __ldg(fa.q[d] + fi) : 0.0;
+                ar[nq] = has[nq] ? __ldg(fa.area[d] + fi) : 0.0f;
+                uv[nq] = has[nq] ? __ldg(vel[d] + fi) : 0.0f;
                 fq[nq] = has[nq] ? __ldg(fluid + cell_index(g, q[0], q[1], q[2])) : 0.0f;
             }
+            // the weight of an open face
+            auto wface = [&](int nq) {
+                return (ar[nq] == 1.0f && fr[nq] == 1.0f) ? fp.w_unit : __ldg(fa.w[nq >> 1] + findex(nq));
+            };
             if (fc < 0.0f) {
                 my_fluid = 1;
-#pragma unroll
-                for (int nq = 0; nq < 6; ++nq) {
-                    if (!has[nq]) continue;
-                    const int d = nq >> 1;
-                    const bool plus = (nq & 1) == 0;
-                    if (fr[nq] > 0.0f) {  // open face
-                        if (fq[nq] < 0.0f) {
-                            unknown = true;
-                            if (plus) cpl[d] = wv[nq];
-                        }
-                        dg += wv[nq];
-                    }
-                    rhs += plus ? -qv[nq] : qv[nq];
-                }
-            }
-            if (unknown) {
-                my_count++;
-                if (rhs_correct) rhs += rhs_correct;
-            } else {
-                dg = 0.0;
-                rhs = 0.0;
-                cpl[0] = cpl[1] = cpl[2] = 0.0;
-            }
-            diag[c] = dg;
-            b[c] = rhs;
-            for (int d = 0; d < g.dim; ++d) cp[d][c] = cpl[d];
-        }
-    }
-    unsigned long long wsum = my_count;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) wsum += __shfl_down_sync(0xffffffffu, wsum, o);
-    if ((threadIdx.x & 31) == 0) sh_count[threadIdx.x >> 5] = wsum;
-    int any_fluid = __syncthreads_or(my_fluid);
-    if (threadIdx.x == 0) {
-        unsigned long long s = 0;
-        for (int q = 0; q < BLOCK_THREADS / 32; ++q) s += sh_count[q];
-        if (s) atomicAdd(&sc->unknowns, s);
-        if (any_fluid) atomicOr(&sc->fluid_exists, 1);
-    }
-}
-
-// ---- fused 3D assembly -------------------------------------------------------------
-//
-// One pass over the cells with the face terms of faces_kernel computed in
-// registers instead of stored. A thread walks the column of cells (i, j)
-// through zslab planes; at each plane it computes the five faces it does not
-// carry (-x, +x, -y, +y and +z; the -z face is the previous plane's +z) and
-// assembles its cell in the reference's face order as assemble_faces_kernel
-// does. A plane's loads (4 solid nodes, 5 fluid cells, 5 face velocities)
-// are all issued before its arithmetic, and the solid nodes and fluid cells
-// of the plane below are carried, so each value is read about once and a
-// warp waits once per plane. Threads never exchange data (no barrier). Only the face fractions are stored (the
-// velocity update and the active sets read them). Sums use integer
-// instructions where they are exact (gbp_exact.cuh; the diagonal of a cell
-// whose open faces all have area = rho = 1 is FaceParams::w_sum[n]), and the
-// FP32 level-0 operator of the mixed solver (or the FP64 hierarchy's inverse
-// diagonal) is written from the same registers. Bit-identical to
-// faces_kernel + assemble_faces_kernel + mg_fine_setup_kernel.
-struct FaceTerm {
-    float area;  // open fraction (0 on the domain boundary)
-    float r;     // stored fraction: rho if open, -1 if only rho closes it, 0 if area == 0
-    float uf;    // velocity on the face (0 where area == 0: never read)
-};
-
-// A face from its open fraction, the fluid levels of its two cells and its
-// velocity (faces_kernel's emit).
-__device__ __forceinline__ FaceTerm face_term(float area, float f0, float f1, float uf, const FaceParams &fp) {
-    FaceTerm t{area, 0.0f, 0.0f};
-    if (area) {
-        const float rho = rho_of(f0, f1, fp);
-        t.r = rho ? rho : -1.0f;
-        t.uf = uf;
-    }
-    return t;
-}
-
-__device__ __forceinline__ double face_w(const FaceTerm &t, double dt, double dx, const FaceParams &fp) {
-    return (t.area == 1.0f && t.r == 1.0f) ? fp.w_unit : face_weight(dt, (double)t.area, (double)t.r, dx, fp);
-}
-
-// a[n] for n in [0, 7) by selects (an indexed kernel parameter would be
-// copied to local memory)
-__device__ __forceinline__ double pick7(const double (&a)[7], int n) {
-    double r = a[0];
-#pragma unroll
-    for (int q = 1; q < 7; ++q) r = n == q ? a[q] : r;
-    return r;
-}
-
-// The loads of one plane k of a column: solid nodes (i..i+1, j..j+1) at
-// plane k+1, the fluid cells -x, +x, -y, +y at plane k and +z (clamped as
-// face_rho clamps), the velocities u(i), u(i+1), v(j), v(j+1) at plane k and
-// w at node k+1.
-struct PlaneLoads {
-    float s00, s10, s01, s11;
-    float fx0, fx1, fy0, fy1, fz1;
-    float u0, u1, v0, v1, w1;
-};
-
-__global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_cells_kernel(
-    Grid g, double dt, double dx, FaceParams fp, double rhs_correct, int zslab, const float *__restrict__ solid,
-    const float *__restrict__ fluid, const float *__restrict__ u, const float *__restrict__ v,
-    const float *__restrict__ w, float *__restrict__ rho_x, float *__restrict__ rho_y, float *__restrict__ rho_z,
-    double *__restrict__ diag, double *__restrict__ cx, double *__restrict__ cy, double *__restrict__ cz,
-    double *__restrict__ b, Level0Out o, Scalars *sc) {
-    __shared__ unsigned long long sh_count[BLOCK_THREADS / 32];
-    const int tx = threadIdx.x & (TILE_X - 1), ty = threadIdx.x / TILE_X;
-    const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const long long sx = nx + 1, sxy = sx * (ny + 1);        // solid nodes
-    const long long cy_ = nx, cz_ = (long long)nx * ny;      // cells
-    const long long uy = nx + 1, uz = uy * ny;               // u faces
-    const long long vy = nx, vz = (long long)nx * (ny + 1);  // v faces
-    const int nzs = (nz + zslab - 1) / zslab;
-    const long long items = (long long)g.ntx * g.nty * nzs;
-    unsigned long long my_count = 0;
-    int my_fluid = 0;
-    for (long long t = blockIdx.x; t < items; t += gridDim.x) {
-        const long long tz = t / ((long long)g.ntx * g.nty);
-        const long long rem = t - tz * g.ntx * g.nty;
-        const int i = (int)(rem % g.ntx) * TILE_X + tx, j = (int)(rem / g.ntx) * TILE_Y + ty;
-        if (i >= nx || j >= ny) continue;  // no barrier below: idle threads may leave
-        const int kb = (int)tz * zslab, ke = min(kb + zslab, nz);
-        const int im = max(i - 1, 0), ip = min(i + 1, nx - 1), jm = max(j - 1, 0), jp = min(j + 1, ny - 1);
-        const float *s0 = solid + i + sx * j;
-        const float *fcol = fluid + i + cy_ * j;
-        auto load = [&](int k) {
-            PlaneLoads L;
-            const float *sk = s0 + sxy * (k + 1);
-            L.s00 = __ldg(sk);
-            L.s10 = __ldg(sk + 1);
-            L.s01 = __ldg(sk + sx);
-            L.s11 = __ldg(sk + sx + 1);
-            const long long ck = cz_ * k;
-            L.fx0 = __ldg(fluid + im + cy_ * j + ck);
-            L.fx1 = __ldg(fluid + ip + cy_ * j + ck);
-            L.fy0 = __ldg(fluid + i + cy_ * jm + ck);
-            L.fy1 = __ldg(fluid + i + cy_ * jp + ck);
-            L.fz1 = __ldg(fcol + cz_ * min(k + 1, nz - 1));
-            const long long uk = i + uy * j + uz * k;
-            L.u0 = __ldg(u + uk);
-            L.u1 = __ldg(u + uk + 1);
-            const long long vk = i + vy * j + vz * k;
-            L.v0 = __ldg(v + vk);
-            L.v1 = __ldg(v + vk + vy);
-            L.w1 = __ldg(w + i + cy_ * j + cz_ * (k + 1));
-            return L;
-        };
-        // the carried state at plane kb: solid nodes of the plane, the cell's
-        // and the one below's fluid level, the -z face
-        float c00 = __ldg(s0 + sxy * kb), c10 = __ldg(s0 + sxy * kb + 1), c01 = __ldg(s0 + sxy * kb + sx),
-              c11 = __ldg(s0 + sxy * kb + sx + 1);
-        float fk = __ldg(fcol + cz_ * kb), fm = __ldg(fcol + cz_ * max(kb - 1, 0));
-        const float wlo = __ldg(w + i + cy_ * j + cz_ * kb);
-        FaceTerm zlo = face_term(kb > 0 ? area3(c00, c10, c11, c01, fp) : 0.0f, fk, fm, wlo, fp);
-        if (kb == 0) rho_z[i + cy_ * j] = zlo.r;
-        for (int k = kb; k < ke; ++k) {
-            // every load of the plane first, independent of the arithmetic
-            const PlaneLoads L = load(k);
-            // faces at the nodes of this cell (corner order of face_area)
-            const FaceTerm xlo = face_term(i > 0 ? area3(c00, c01, L.s01, L.s00, fp) : 0.0f, fk, L.fx0, L.u0, fp);
-            const FaceTerm xhi =
-                face_term(i + 1 < nx ? area3(c10, c11, L.s11, L.s10, fp) : 0.0f, L.fx1, fk, L.u1, fp);
-            const FaceTerm ylo = face_term(j > 0 ? area3(c00, c10, L.s10, L.s00, fp) : 0.0f, fk, L.fy0, L.v0, fp);
-            const FaceTerm yhi =
-                face_term(j + 1 < ny ? area3(c01, c11, L.s11, L.s01, fp) : 0.0f, L.fy1, fk, L.v1, fp);
-            const FaceTerm zhi =
-                face_term(k + 1 < nz ? area3(L.s00, L.s10, L.s11, L.s01, fp) : 0.0f, L.fz1, fk, L.w1, fp);
-            rho_x[i + uy * j + uz * k] = xlo.r;
-            if (i + 1 == nx) rho_x[nx + uy * j + uz * k] = xhi.r;
-            rho_y[i + vy * j + vz * k] = ylo.r;
-            if (j + 1 == ny) rho_y[i + vy * ny + vz * k] = yhi.r;
-            rho_z[i + cy_ * j + cz_ * (k + 1)] = zhi.r;
-            const long long c = i + cy_ * j + cz_ * k;
-            double dg = 0.0, rhs = 0.0, cpl[3] = {0.0, 0.0, 0.0};
-            bool unknown = false, unit = true;
-            int nopen = 0;
-            if (fk < 0.0f) {
-                my_fluid = 1;
-                // faces in the reference's order +x, -x, +y, -y, +z, -z, with
-                // the fluid level across each
-                const FaceTerm fs[6] = {xhi, xlo, yhi, ylo, zhi, zlo};
-                const bool has[6] = {i + 1 < nx, i > 0, j + 1 < ny, j > 0, k + 1 < nz, k > 0};
-                const float fn[6] = {L.fx1, L.fx0, L.fy1, L.fy0, L.fz1, fm};
                 // the right-hand side's terms -+u/dx by face (0 where a face
                 // has no term or area 0: adding +-0 changes no sum)
                 float terms[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
@@ -783,17 +600,16 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_cells_kernel(
 #pragma unroll
                 for (int nq = 0; nq < 6; ++nq) {
                     if (!has[nq]) continue;
-                    const FaceTerm ft = fs[nq];
-                    if (ft.r > 0.0f) {  // open face
+                    if (fr[nq] > 0.0f) {  // open face
                         nopen++;
-                        unit = unit && ft.area == 1.0f && ft.r == 1.0f;
-                        if (fn[nq] < 0.0f) {
+                        unit = unit && ar[nq] == 1.0f && fr[nq] == 1.0f;
+                        if (fq[nq] < 0.0f) {
                             unknown = true;
-                            if ((nq & 1) == 0) cpl[nq >> 1] = face_w(ft, dt, dx, fp);
+                            if ((nq & 1) == 0) cpl[nq >> 1] = wface(nq);
                         }
                     }
-                    if (ft.area == 1.0f) terms[nq] = ft.uf;
-                    else if (ft.area != 0.0f) qexact = false;
+                    if (ar[nq] == 1.0f) terms[nq] = uv[nq];
+                    else if (ar[nq] != 0.0f) qexact = false;
                 }
                 if (unknown) {
                     if (unit) {
@@ -801,7 +617,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_cells_kernel(
                     } else {
 #pragma unroll
                         for (int nq = 0; nq < 6; ++nq)
-                            if (has[nq] && fs[nq].r > 0.0f) dg += face_w(fs[nq], dt, dx, fp);
+                            if (has[nq] && fr[nq] > 0.0f) dg += wface(nq);
                     }
                     // 0x15: the + faces' terms are negated
                     if (!(qexact && exact_sum(terms, 6, 0x15u, fp.inv_dx_exp, rhs))) {
@@ -809,8 +625,9 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_cells_kernel(
 #pragma unroll
                         for (int nq = 0; nq < 6; ++nq) {
                             if (!has[nq]) continue;
-                            const FaceTerm ft = fs[nq];
-                            const double q = ft.area ? div_dx((double)ft.area * (double)ft.uf, dx, fp) : 0.0;
+                            double q = 0.0;
+                            if (ar[nq] == 1.0f && fp.dx_pow2) q = div_dx((double)uv[nq], dx, fp);
+                            else if (ar[nq] != 0.0f) q = __ldg(fa.q[nq >> 1] + findex(nq));
                             rhs += (nq & 1) == 0 ? -q : q;
                         }
                     }
@@ -820,38 +637,31 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_cells_kernel(
                 my_count++;
                 if (rhs_correct) rhs += rhs_correct;  // macpressuresolver3.cpp:212-214
             } else {
-                dg = rhs = 0.0;
+                dg = 0.0;
+                rhs = 0.0;
                 cpl[0] = cpl[1] = cpl[2] = 0.0;
             }
             diag[c] = dg;
             b[c] = rhs;
-            cx[c] = cpl[0];
-            cy[c] = cpl[1];
-            cz[c] = cpl[2];
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                if (d < g.dim) cp[d][c] = cpl[d];
             if (o.diag) {
                 const float d32 = d2f_rn(dg);
                 o.diag[c] = d32;
                 o.inv[c] = dg > 0.0 ? __frcp_rn(d32) : 0.0f;
                 o.cx[c] = d2f_rn(cpl[0]);
                 o.cy[c] = d2f_rn(cpl[1]);
-                o.cz[c] = d2f_rn(cpl[2]);
+                if (g.dim == 3) o.cz[c] = d2f_rn(cpl[2]);
             }
             if (o.inv64) o.inv64[c] = dg > 0.0 ? (unit ? pick7(fp.inv_sum, nopen) : 1.0 / dg) : 0.0;
-            // carry: this plane's top nodes, levels and +z face
-            c00 = L.s00;
-            c10 = L.s10;
-            c01 = L.s01;
-            c11 = L.s11;
-            fm = fk;
-            fk = L.fz1;
-            zlo = zhi;
         }
     }
     unsigned long long wsum = my_count;
 #pragma unroll
     for (int q = 16; q > 0; q >>= 1) wsum += __shfl_down_sync(0xffffffffu, wsum, q);
     if ((threadIdx.x & 31) == 0) sh_count[threadIdx.x >> 5] = wsum;
-    const int any_fluid = __syncthreads_or(my_fluid);
+    int any_fluid = __syncthreads_or(my_fluid);
     if (threadIdx.x == 0) {
         unsigned long long s = 0;
         for (int q = 0; q < BLOCK_THREADS / 32; ++q) s += sh_count[q];
@@ -875,60 +685,6 @@ __device__ __forceinline__ float face_update(float fr, bool interior, float pc, 
     if (rho == 1.0f && mul_round(fp.dt_mul, dp, vv)) return uf - vv;
     const double val = rho == 1.0f ? div_dx(dt * (double)dp, dx, fp) : dt * (double)dp / ((double)rho * dx);
     return uf - (float)val;
-}
-
-// Float pressure and velocity update in one pass (3D, no warm start): a
-// thread walks the column of cells (i, j) through zslab planes, writes
-// p = (float)x on the unknowns (0 elsewhere, as pressure_kernel) and
-// updates the -x, -y and -z faces of its cell (and the domain-boundary
-// faces at nx, ny, nz of the last column, row and plane) as
-// velocity_faces_kernel does. The pressures across the -x and -y faces are
-// formed again from x and the diagonal (the same integer conversion), the
-// one across -z is carried from the plane below.
-__global__ void __launch_bounds__(BLOCK_THREADS) pressure_velocity_kernel(
-    Grid g, double dt, double dx, FaceParams fp, int zslab, const double *__restrict__ diag,
-    const double *__restrict__ x, float *__restrict__ p, const float *__restrict__ rho_x,
-    const float *__restrict__ rho_y, const float *__restrict__ rho_z, float *__restrict__ u, float *__restrict__ v,
-    float *__restrict__ w, const Scalars *__restrict__ sc) {
-    const int fluid_exists = sc->fluid_exists;
-    const int tx = threadIdx.x & (TILE_X - 1), ty = threadIdx.x / TILE_X;
-    const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const long long cy_ = nx, cz_ = (long long)nx * ny;      // cells, w faces
-    const long long uy = nx + 1, uz = uy * ny;               // u faces
-    const long long vy = nx, vz = (long long)nx * (ny + 1);  // v faces
-    const int nzs = (nz + zslab - 1) / zslab;
-    const long long items = (long long)g.ntx * g.nty * nzs;
-    auto pres = [&](long long c) {  // pressure_kernel's p at cell c
-        const double d = __ldg(diag + c), xv = __ldg(x + c);
-        return d != 0.0 ? d2f_rn(xv) : 0.0f;
-    };
-    for (long long t = blockIdx.x; t < items; t += gridDim.x) {
-        const long long tz = t / ((long long)g.ntx * g.nty);
-        const long long rem = t - tz * g.ntx * g.nty;
-        const int i = (int)(rem % g.ntx) * TILE_X + tx, j = (int)(rem / g.ntx) * TILE_Y + ty;
-        if (i >= nx || j >= ny) continue;
-        const int kb = (int)tz * zslab, ke = min(kb + zslab, nz);
-        float pdown = kb > 0 ? pres(i + cy_ * j + cz_ * (kb - 1)) : 0.0f;
-        for (int k = kb; k < ke; ++k) {
-            const long long c = i + cy_ * j + cz_ * k;
-            const long long fu = i + uy * j + uz * k, fv = i + vy * j + vz * k;
-            // every load of the plane first
-            const float pc = pres(c);
-            const float px = i > 0 ? pres(c - 1) : 0.0f;
-            const float py = j > 0 ? pres(c - cy_) : 0.0f;
-            const float rx = __ldg(rho_x + fu), ry = __ldg(rho_y + fv), rz = __ldg(rho_z + c);
-            const float ux = u[fu], vy_ = v[fv], wz = w[c];
-            p[c] = pc;
-            u[fu] = face_update(rx, i > 0, pc, px, ux, fluid_exists, dt, dx, fp);
-            v[fv] = face_update(ry, j > 0, pc, py, vy_, fluid_exists, dt, dx, fp);
-            w[c] = face_update(rz, k > 0, pc, pdown, wz, fluid_exists, dt, dx, fp);
-            // the domain-boundary faces above the last column, row and plane
-            if (i + 1 == nx) u[fu + 1] = 0.0f;
-            if (j + 1 == ny) v[fv + vy] = 0.0f;
-            if (k + 1 == nz) w[c + cz_] = 0.0f;
-            pdown = pc;
-        }
-    }
 }
 
 // Velocity update from the stored face fractions (same rule as
@@ -1100,45 +856,16 @@ cudaError_t launch_faces(const Grid &g, double dt, double dx, const SetupParams 
     return cudaGetLastError();
 }
 
-cudaError_t launch_assemble_faces(const Grid &g, const SetupParams &sp, const float *fluid, FaceArrays fa,
-                                  double *diag, double *cx, double *cy, double *cz, double *b, Scalars *sc,
+cudaError_t launch_assemble_faces(const Grid &g, double dt, double dx, const SetupParams &sp, const float *fluid,
+                                  const float *u, const float *v, const float *w, FaceArrays fa, double *diag,
+                                  double *cx, double *cy, double *cz, double *b, Level0Out o, Scalars *sc,
                                   int grid_blocks, cudaStream_t stream) {
+    const FaceParams fp = face_params(sp, dx, dt);
     int blocks = (int)(g.ntiles < grid_blocks ? g.ntiles : grid_blocks);
     if (blocks < 1) blocks = 1;
-    assemble_faces_kernel<<<blocks, BLOCK_THREADS, 0, stream>>>(g, sp.rhs_correct, fluid, fa, diag, cx, cy,
-                                                                g.dim == 3 ? cz : cy, b, sc);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_assemble_cells(const Grid &g, double dt, double dx, const SetupParams &sp, const float *solid,
-                                  const float *fluid, const float *u, const float *v, const float *w, FaceArrays fa,
-                                  double *diag, double *cx, double *cy, double *cz, double *b, Level0Out o,
-                                  Scalars *sc, int grid_blocks, cudaStream_t stream) {
-    if (g.dim != 3) return cudaErrorInvalidValue;
-    const FaceParams fp = face_params(sp, dx, dt);
-    // slabs deep enough to amortise the first plane's extra z face, thin
-    // enough for two items per block
-    int zslab = 32;
-    while (zslab > 4 && (long long)g.ntx * g.nty * ((g.nz + zslab - 1) / zslab) < 2LL * grid_blocks) zslab /= 2;
-    const long long items = (long long)g.ntx * g.nty * ((g.nz + zslab - 1) / zslab);
-    const int blocks = (int)(items < grid_blocks ? items : grid_blocks);
-    assemble_cells_kernel<<<blocks < 1 ? 1 : blocks, BLOCK_THREADS, 0, stream>>>(
-        g, dt, dx, fp, sp.rhs_correct, zslab, solid, fluid, u, v, w, fa.rho[0], fa.rho[1], fa.rho[2], diag, cx, cy, cz,
-        b, o, sc);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_pressure_velocity(const Grid &g, double dt, double dx, const SetupParams &sp, const double *diag,
-                                     const double *x, float *p, FaceArrays fa, float *u, float *v, float *w,
-                                     const Scalars *sc, int grid_blocks, cudaStream_t stream) {
-    if (g.dim != 3) return cudaErrorInvalidValue;
-    const FaceParams fp = face_params(sp, dx, dt);
-    int zslab = 32;
-    while (zslab > 4 && (long long)g.ntx * g.nty * ((g.nz + zslab - 1) / zslab) < 2LL * grid_blocks) zslab /= 2;
-    const long long items = (long long)g.ntx * g.nty * ((g.nz + zslab - 1) / zslab);
-    const int blocks = (int)(items < grid_blocks ? items : grid_blocks);
-    pressure_velocity_kernel<<<blocks < 1 ? 1 : blocks, BLOCK_THREADS, 0, stream>>>(
-        g, dt, dx, fp, zslab, diag, x, p, fa.rho[0], fa.rho[1], fa.rho[2], u, v, w, sc);
+    assemble_faces_kernel<<<blocks, BLOCK_THREADS, 0, stream>>>(g, dt, dx, fp, sp.rhs_correct, fluid, u, v,
+                                                                g.dim == 3 ? w : v, fa, diag, cx, cy,
+                                                                g.dim == 3 ? cz : cy, b, o, sc);
     return cudaGetLastError();
 }
 
