@@ -363,6 +363,15 @@ int gbp_advect3_device(gbp_ctx *ctx, int nx, int ny, int nz, double dx, double d
 /* HOST arrays, copied in and out on the context's stream. */
 int gbp_advect3(gbp_ctx *ctx, int nx, int ny, int nz, double dx, double dt, const gbp_advect_params *params, float *u,
                 float *v, float *w, const float *fluid, float *q, const unsigned char *q_mask, float q_bg);
+/* The 2D step: replaces macadvection2_interface::advect_scalar /
+ * advect_vector (include/shiokaze/advection/macadvection2_interface.h:
+ * 52-71) as implemented by src/advection/macadvection2.cpp (bilinear), in
+ * macsmoke2's order (src/smoke/macsmoke2.cpp:244-254). u (nx+1)*ny,
+ * v nx*(ny+1), fluid and q nx*ny, x fastest; otherwise as gbp_advect3. */
+int gbp_advect2_device(gbp_ctx *ctx, int nx, int ny, double dx, double dt, const gbp_advect_params *params, float *u,
+                       float *v, const float *fluid, float *q, const unsigned char *q_mask, float q_bg, void *stream);
+int gbp_advect2(gbp_ctx *ctx, int nx, int ny, double dx, double dt, const gbp_advect_params *params, float *u,
+                float *v, const float *fluid, float *q, const unsigned char *q_mask, float q_bg);
 
 /* Solid constraint of the velocity, the step after the projection in the
  * liquid and smoke solvers (src/liquid/macliquid3.cpp:316,

@@ -145,6 +145,8 @@ def _port_lib():
         lib.oracle_advect3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                        ctypes.c_int, ctypes.c_int, fp, fp, fp, fp, fp, ctypes.POINTER(ctypes.c_ubyte),
                                        ctypes.c_float]
+        lib.oracle_advect2.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                       ctypes.c_int, fp, fp, fp, fp, ctypes.POINTER(ctypes.c_ubyte), ctypes.c_float]
         u8 = ctypes.POINTER(ctypes.c_ubyte)
         lib.oracle_extrapolate3.restype = ctypes.c_longlong
         lib.oracle_extrapolate3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, u8, ctypes.c_int]
@@ -258,6 +260,12 @@ def _ref_lib():
         dp = ctypes.POINTER(ctypes.c_double)
         lib.ref_advect_load.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_char_p,
                                         ctypes.c_char_p]
+        lib.ref_advect2.restype = ctypes.c_double
+        lib.ref_advect2.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_char_p,
+                                    fp, fp, fp, ctypes.c_int, ctypes.c_float, fp, ctypes.POINTER(ctypes.c_ubyte),
+                                    ctypes.c_float, ctypes.c_char_p]
+        lib.ref_advect2_load.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_char_p,
+                                         ctypes.c_char_p]
         lib.ref_advect3.restype = ctypes.c_double
         lib.ref_advect3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_char_p, fp, fp, fp, fp, ctypes.c_int, ctypes.c_float, fp,
@@ -347,6 +355,40 @@ def advect3(u, v, w, fluid, dx, dt, q=None, q_mask=None, q_bg=0.0, maccormack=Tr
     if rc:
         raise ValueError("oracle_advect3: grid too small")
     return uo, vo, wo, qo, ms
+
+
+def advect2(u, v, fluid, dx, dt, q=None, q_mask=None, q_bg=0.0, maccormack=True, trim_narrowband=1, impl="port",
+            fluid_mode=0, band=0.0, extra_kv=""):
+    """macsmoke2's advection step on dense 2D arrays (y, x): the scalar q (if
+    given) by the velocity, then the velocity by itself, by the C
+    restatement ("port") or the reference's own macadvection2
+    ("reference"; fluid_mode / band say how it builds its fluid array,
+    extra_kv adds configuration). Returns (u, v, q, ms) as new arrays."""
+    fp = ctypes.POINTER(ctypes.c_float)
+    ny, nx = fluid.shape
+    uo, vo = (np.array(a, dtype=np.float32, order="C") for a in (u, v))
+    fl = np.ascontiguousarray(fluid, dtype=np.float32)
+    qo = None if q is None else np.array(q, dtype=np.float32, order="C")
+    qm = None if q_mask is None else np.ascontiguousarray(q_mask, dtype=np.uint8)
+    qp = None if qo is None else qo.ctypes.data_as(fp)
+    if impl == "reference":
+        lib = _ref_lib()
+        kv = f"MacCormack={'Yes' if maccormack else 'No'} TrimNarrowBand={int(trim_narrowband)} {extra_kv}".strip()
+        log = tempfile.NamedTemporaryFile(prefix="ref_advect_", suffix=".log", delete=False).name
+        try:
+            ms = lib.ref_advect2(nx, ny, dx, dt, kv.encode(), uo.ctypes.data_as(fp), vo.ctypes.data_as(fp),
+                                 fl.ctypes.data_as(fp), fluid_mode, band, qp, _u8p(qm), q_bg, log.encode())
+        finally:
+            os.unlink(log)
+        return uo, vo, qo, ms
+    lib = _port_lib()
+    t0 = time.perf_counter()
+    rc = lib.oracle_advect2(nx, ny, dx, dt, int(maccormack), int(trim_narrowband), uo.ctypes.data_as(fp),
+                            vo.ctypes.data_as(fp), fl.ctypes.data_as(fp), qp, _u8p(qm), q_bg)
+    ms = 1000.0 * (time.perf_counter() - t0)
+    if rc:
+        raise ValueError("oracle_advect2: grid too small")
+    return uo, vo, qo, ms
 
 
 def _u8p(m):

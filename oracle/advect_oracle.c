@@ -361,6 +361,311 @@ int oracle_advect3(int nx, int ny, int nz, double dx, double dt, int maccormack,
 }
 
 /* ------------------------------------------------------------------------
+ * The 2D module, src/advection/macadvection2.cpp (WENO off): the same
+ * passes as the 3D one on (nx, ny) grids --
+ *   advect_vector :47-54, advect_u :133-165, advect_semiLagrangian_u :66-131
+ *   advect_scalar :38-45, advect_cell :219-249, advect_semiLagrangian_cell :167-217
+ * with bilinear interpolation (include/shiokaze/array/array_interpolator2.h:
+ * 50-89) and the full vectors of include/shiokaze/array/macarray2.h:302-367.
+ * Two differences of order from the 3D restatement, kept: the face full
+ * vector sums its four faces with x outer, y inner (macarray2.h:359-360);
+ * the interpolation weights are (i+1-x)(j+1-y), (x-i)(j+1-y), (i+1-x)(y-j),
+ * (x-i)(y-j). Same scope: every velocity face active (src/smoke/
+ * macsmoke2.cpp), the scalar's inactive cells reading its background. */
+
+typedef struct {
+    int w, h;
+} shp2;
+
+static shp2 face_shape2(int nx, int ny, int dim) {
+    shp2 s = {nx + (dim == 0), ny + (dim == 1)};
+    return s;
+}
+
+static long long at2(shp2 s, int i, int j) { return i + (long long)s.w * j; }
+
+/* array_interpolator2::interpolate_coef (array_interpolator2.h:50-63) */
+static void interp_coef2(shp2 s, const double p[2], int idx[4][2], double coef[4]) {
+    const double x = smax(0.0, smin(s.w - 1., p[0]));
+    const double y = smax(0.0, smin(s.h - 1., p[1]));
+    const int i = (int)smin(x, s.w - 2.);
+    const int j = (int)smin(y, s.h - 2.);
+    for (int n = 0; n < 4; ++n) {
+        idx[n][0] = i + (n & 1);
+        idx[n][1] = j + ((n >> 1) & 1);
+    }
+    coef[0] = (i + 1 - x) * (j + 1 - y);
+    coef[1] = (x - i) * (j + 1 - y);
+    coef[2] = (i + 1 - x) * (y - j);
+    coef[3] = (x - i) * (y - j);
+}
+
+/* array_interpolator2::interpolate<float> (:77-89, only_actives false) */
+static float interp2(const float *a, shp2 s, const double p[2]) {
+    int idx[4][2];
+    double coef[4];
+    interp_coef2(s, p, idx, coef);
+    float value = 0.0f;
+    for (int n = 0; n < 4; ++n)
+        if (coef[n]) value = (float)((double)value + (double)a[at2(s, idx[n][0], idx[n][1])] * coef[n]);
+    return value;
+}
+
+/* macarray2::convert_to_full onto faces (macarray2.h:347-367): full[dim][f*2 + c] */
+static void face_full2(const float *comp[2], int nx, int ny, float *full[2]) {
+    for (int dim = 0; dim < 2; ++dim) {
+        const shp2 fs = face_shape2(nx, ny, dim);
+        for (int j = 0; j < fs.h; ++j)
+            for (int i = 0; i < fs.w; ++i) {
+                double u[2] = {0.0, 0.0};
+                for (int ud = 0; ud < 2; ++ud) {
+                    if (ud == dim) {
+                        u[ud] = comp[ud][at2(fs, i, j)];
+                    } else {
+                        const shp2 s = face_shape2(nx, ny, ud);
+                        const int pi[2] = {i - (dim == 0), j - (dim == 1)};
+                        for (int ii = 0; ii < 2; ++ii)
+                            for (int jj = 0; jj < 2; ++jj) {
+                                int q0 = pi[0] + ii, q1 = pi[1] + jj;
+                                /* shape2::clamp */
+                                if (q0 < 0) q0 = 0;
+                                if (q0 > s.w - 1) q0 = s.w - 1;
+                                if (q1 < 0) q1 = 0;
+                                if (q1 > s.h - 1) q1 = s.h - 1;
+                                u[ud] += comp[ud][at2(s, q0, q1)];
+                            }
+                        u[ud] /= 4.0;
+                    }
+                }
+                float *o = full[dim] + 2 * at2(fs, i, j);
+                o[0] = (float)u[0];
+                o[1] = (float)u[1];
+            }
+    }
+}
+
+/* advect_semiLagrangian_u (:66-87), the trace in float as vec2r does */
+static void semi_lagrangian_u2(const float *vin[2], int nx, int ny, double dx, double dt, float *out[2],
+                               float *full[2]) {
+    face_full2(vin, nx, ny, full);
+    for (int dim = 0; dim < 2; ++dim) {
+        const shp2 fs = face_shape2(nx, ny, dim);
+        for (int j = 0; j < fs.h; ++j)
+            for (int i = 0; i < fs.w; ++i) {
+                const long long f = at2(fs, i, j);
+                const float *u = full[dim] + 2 * f;
+                if (u[0] || u[1]) {
+                    const int ip[2] = {i, j};
+                    double p[2];
+                    for (int c = 0; c < 2; ++c) {
+                        const float t = (float)(u[c] * dt);
+                        const float t2 = (float)(t / dx);
+                        p[c] = (double)ip[c] - (double)t2;
+                    }
+                    out[dim][f] = interp2(vin[dim], fs, p);
+                } else {
+                    out[dim][f] = vin[dim][f];
+                }
+            }
+    }
+}
+
+/* the forward pass's min/max and narrow-band flag per face (:89-129) */
+static void minmax_u2(const float *vin[2], float *full[2], const float *fluid, int nx, int ny, double dx, double dt,
+                      int trim, minmax_t *mm[2]) {
+    const shp2 cs = {nx, ny};
+    const double limit = -dx * (double)trim;
+    for (int dim = 0; dim < 2; ++dim) {
+        const shp2 fs = face_shape2(nx, ny, dim);
+        for (int j = 0; j < fs.h; ++j)
+            for (int i = 0; i < fs.w; ++i) {
+                const long long f = at2(fs, i, j);
+                const float *uf = full[dim] + 2 * f;
+                const double u[2] = {uf[0], uf[1]};
+                const int ip[2] = {i, j};
+                minmax_t r;
+                double fp[2];
+                if (u[0] || u[1]) {
+                    double p[2];
+                    for (int c = 0; c < 2; ++c) {
+                        const double disp = u[c] * dt / dx;
+                        p[c] = (double)ip[c] - disp;
+                        fp[c] = (ip[c] + 0.5 * (dim != c)) - disp;
+                    }
+                    int idx[4][2];
+                    double coef[4];
+                    interp_coef2(fs, p, idx, coef);
+                    double lo = DBL_MAX, hi = DBL_MIN;
+                    for (int n = 0; n < 4; ++n) {
+                        const double val = vin[dim][at2(fs, idx[n][0], idx[n][1])];
+                        lo = smin(lo, val);
+                        hi = smax(hi, val);
+                    }
+                    r.lo = (float)lo;
+                    r.hi = (float)hi;
+                } else {
+                    for (int c = 0; c < 2; ++c) fp[c] = ip[c] + 0.5 * (dim != c);
+                    r.lo = r.hi = vin[dim][f];
+                }
+                const double cp[2] = {fp[0] - 0.5, fp[1] - 0.5};
+                r.within = (double)interp2(fluid, cs, cp) > limit;
+                mm[dim][f] = r;
+            }
+    }
+}
+
+static void advect_u2(float *vel[2], int nx, int ny, double dx, double dt, int maccormack, int trim,
+                      const float *fluid) {
+    long long nf[2];
+    float *vin[2], *v0[2], *v1[2], *full[2];
+    minmax_t *mm[2];
+    for (int d = 0; d < 2; ++d) {
+        const shp2 fs = face_shape2(nx, ny, d);
+        nf[d] = (long long)fs.w * fs.h;
+        vin[d] = (float *)malloc(sizeof(float) * nf[d]);
+        memcpy(vin[d], vel[d], sizeof(float) * nf[d]);
+        v0[d] = (float *)malloc(sizeof(float) * nf[d]);
+        v1[d] = (float *)malloc(sizeof(float) * nf[d]);
+        full[d] = (float *)malloc(sizeof(float) * 2 * nf[d]);
+        mm[d] = (minmax_t *)malloc(sizeof(minmax_t) * nf[d]);
+    }
+    const float *cvin[2] = {vin[0], vin[1]};
+    if (!maccormack) {
+        semi_lagrangian_u2(cvin, nx, ny, dx, dt, vel, full);
+    } else {
+        semi_lagrangian_u2(cvin, nx, ny, dx, dt, v0, full);
+        minmax_u2(cvin, full, fluid, nx, ny, dx, dt, trim, mm);
+        const float *cv0[2] = {v0[0], v0[1]};
+        semi_lagrangian_u2(cv0, nx, ny, dx, -dt, v1, full);
+        for (int d = 0; d < 2; ++d)
+            for (long long f = 0; f < nf[d]; ++f) {
+                if (mm[d][f].within) {
+                    vel[d][f] = v0[d][f];
+                } else {
+                    const double lo = mm[d][f].lo, hi = mm[d][f].hi, x0 = v0[d][f];
+                    const double corr = 0.5 * (float)(vin[d][f] - v1[d][f]);
+                    if (x0 + corr < lo) vel[d][f] = (float)lo;
+                    else if (x0 + corr > hi) vel[d][f] = (float)hi;
+                    else vel[d][f] = (float)(x0 + corr);
+                }
+            }
+    }
+    for (int d = 0; d < 2; ++d) {
+        free(vin[d]);
+        free(v0[d]);
+        free(v1[d]);
+        free(full[d]);
+        free(mm[d]);
+    }
+}
+
+/* macarray2::convert_to_full onto cells (macarray2.h:302-340): full[c*2 + dim] */
+static void cell_full2(const float *comp[2], int nx, int ny, float *full) {
+    const shp2 cs = {nx, ny};
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            float *o = full + 2 * at2(cs, i, j);
+            for (int dim = 0; dim < 2; ++dim) {
+                const shp2 fs = face_shape2(nx, ny, dim);
+                double value = 0.0;
+                value += comp[dim][at2(fs, i, j)];
+                value += comp[dim][at2(fs, i + (dim == 0), j + (dim == 1))];
+                o[dim] = (float)(0.5 * value);
+            }
+        }
+}
+
+/* advect_semiLagrangian_cell (:167-217) */
+static void semi_lagrangian_cell2(const float *qin, const float *full, const unsigned char *mask, float bg, int nx,
+                                  int ny, double dx, double dt, float *out, minmax_t *mm, const float *fluid,
+                                  int trim) {
+    const shp2 cs = {nx, ny};
+    const double limit = -dx * (double)trim;
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const long long c = at2(cs, i, j);
+            if (mask && !mask[c]) {
+                out[c] = bg;
+                continue;
+            }
+            const float *uf = full + 2 * c;
+            const double u[2] = {uf[0], uf[1]};
+            const int ip[2] = {i, j};
+            const int moving = u[0] || u[1];
+            double p[2];
+            if (moving)
+                for (int d = 0; d < 2; ++d) p[d] = (double)ip[d] - u[d] * dt / dx;
+            out[c] = moving ? interp2(qin, cs, p) : qin[c];
+            if (!mm) continue;
+            minmax_t r;
+            if (moving) {
+                int idx[4][2];
+                double coef[4];
+                interp_coef2(cs, p, idx, coef);
+                double lo = FLT_MAX, hi = FLT_MIN;
+                for (int n = 0; n < 4; ++n) {
+                    const double val = qin[at2(cs, idx[n][0], idx[n][1])];
+                    lo = smin(lo, val);
+                    hi = smax(hi, val);
+                }
+                r.lo = (float)lo;
+                r.hi = (float)hi;
+                r.within = (double)interp2(fluid, cs, p) > limit;
+            } else {
+                r.lo = r.hi = qin[c];
+                r.within = (double)fluid[c] > limit;
+            }
+            mm[c] = r;
+        }
+}
+
+static void advect_cell2(float *q, const unsigned char *mask, float bg, const float *vel[2], int nx, int ny,
+                         double dx, double dt, int maccormack, int trim, const float *fluid) {
+    const long long n = (long long)nx * ny;
+    float *qin = (float *)malloc(sizeof(float) * n), *q0 = (float *)malloc(sizeof(float) * n);
+    float *q1 = (float *)malloc(sizeof(float) * n), *full = (float *)malloc(sizeof(float) * 2 * n);
+    minmax_t *mm = (minmax_t *)malloc(sizeof(minmax_t) * n);
+    for (long long c = 0; c < n; ++c) qin[c] = (mask && !mask[c]) ? bg : q[c];
+    cell_full2(vel, nx, ny, full);
+    if (!maccormack) {
+        semi_lagrangian_cell2(qin, full, mask, bg, nx, ny, dx, dt, q, NULL, fluid, trim);
+    } else {
+        semi_lagrangian_cell2(qin, full, mask, bg, nx, ny, dx, dt, q0, mm, fluid, trim);
+        semi_lagrangian_cell2(q0, full, mask, bg, nx, ny, dx, -dt, q1, NULL, fluid, trim);
+        for (long long c = 0; c < n; ++c) {
+            if (mask && !mask[c]) {
+                q[c] = bg;
+            } else if (mm[c].within) {
+                q[c] = q0[c];
+            } else {
+                const double lo = mm[c].lo, hi = mm[c].hi, x0 = q0[c];
+                const double corr = 0.5 * (float)(qin[c] - q1[c]);
+                if (x0 + corr < lo) q[c] = (float)lo;
+                else if (x0 + corr > hi) q[c] = (float)hi;
+                else q[c] = (float)(x0 + corr);
+            }
+        }
+    }
+    free(qin);
+    free(q0);
+    free(q1);
+    free(full);
+    free(mm);
+}
+
+/* macsmoke2's advection step: the scalar q (if not NULL) by u, v, then u, v
+ * by themselves. u (nx+1)*ny, v nx*(ny+1), fluid and q nx*ny, x fastest. */
+int oracle_advect2(int nx, int ny, double dx, double dt, int maccormack, int trim, float *u, float *v,
+                   const float *fluid, float *q, const unsigned char *q_mask, float q_bg) {
+    if (nx < 2 || ny < 2) return 1;
+    float *vel[2] = {u, v};
+    const float *cvel[2] = {u, v};
+    if (q) advect_cell2(q, q_mask, q_bg, cvel, nx, ny, dx, dt, maccormack, trim, fluid);
+    advect_u2(vel, nx, ny, dx, dt, maccormack, trim, fluid);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------
  * macutility3::constrain_velocity (src/utility/macutility3.cpp:61-86): the
  * velocity's normal component into the solid removed at faces inside it,
  * and outflow through the domain's walls set to 0. */

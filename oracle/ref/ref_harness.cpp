@@ -29,6 +29,7 @@
 #include <shiokaze/core/configuration.h>
 #include <shiokaze/core/configurable.h>
 #include <shiokaze/projection/macproject2_interface.h>
+#include <shiokaze/advection/macadvection2_interface.h>
 #include <shiokaze/advection/macadvection3_interface.h>
 #include <shiokaze/utility/macutility3_interface.h>
 #include <shiokaze/array/array_extrapolator3.h>
@@ -460,6 +461,77 @@ double ref_advect3(int nx, int ny, int nz, double dx, double dt, const char *kv,
                     for (int i = 0; i < nx; ++i) q[i + (size_t)nx * (j + (size_t)ny * k)] = qa(i, j, k);
     });
     return ms;
+}
+
+/* The reference's macadvection2 (src/advection/macadvection2.cpp) on dense
+ * 2D arrays, in macsmoke2's order (src/smoke/macsmoke2.cpp:244-254): the
+ * scalar (if q is given) by the velocity, then the velocity by itself. As
+ * ref_advect3 otherwise: u, v every face active, in/out; fluid built as in
+ * ref_project; q background q_bg, active where q_mask (all if NULL). */
+double ref_advect2(int nx, int ny, double dx, double dt, const char *kv, float *u, float *v, const float *fluid,
+                   int fluid_mode, float fluid_band, float *q, const unsigned char *q_mask, float q_bg,
+                   const char *log_path) {
+    configuration &config = install_global_config(kv);
+    shape2 s(nx, ny);
+    double dxv = dx, ms = 0.0;
+    with_stdout_to(log_path, [&]() {
+        macadvection2_driver adv("macadvection2");
+        adv.set_environment("shape", &s);
+        adv.set_environment("dx", &dxv);
+        adv.setup_now(config);
+        array2<Real> fluid_a;
+        fill_levelset2(fluid_a, s, fluid, fluid_mode, fluid_band);
+        macarray2<Real> vel(s), save(s);
+        vel.activate_all();
+        save.activate_all();
+        float *comp[2] = {u, v};
+        for (int d = 0; d < 2; ++d) {
+            const shape2 fs = s.face(d);
+            for (int j = 0; j < (int)fs.h; ++j)
+                for (int i = 0; i < (int)fs.w; ++i) {
+                    const float x = comp[d][i + (size_t)fs.w * j];
+                    vel[d].set(i, j, x);
+                    save[d].set(i, j, x);
+                }
+        }
+        array2<Real> qa;
+        if (q) {
+            qa.initialize(s, q_bg);
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const size_t n = i + (size_t)nx * j;
+                    if (!q_mask || q_mask[n]) qa.set(i, j, q[n]);
+                }
+        }
+        auto t0 = std::chrono::steady_clock::now();
+        if (q) adv->advect_scalar(qa, vel, fluid_a, dt);
+        adv->advect_vector(vel, save, fluid_a, dt);
+        ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        for (int d = 0; d < 2; ++d) {
+            const shape2 fs = s.face(d);
+            for (int j = 0; j < (int)fs.h; ++j)
+                for (int i = 0; i < (int)fs.w; ++i) comp[d][i + (size_t)fs.w * j] = vel[d](i, j);
+        }
+        if (q)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) q[i + (size_t)nx * j] = qa(i, j);
+    });
+    return ms;
+}
+
+/* Loads, configures and initializes the 2D advection module the
+ * configuration names (Advection=<name>, default macadvection2); returns 1. */
+int ref_advect2_load(int nx, int ny, double dx, const char *kv, const char *log_path) {
+    configuration &config = install_global_config(kv);
+    shape2 s(nx, ny);
+    double dxv = dx;
+    with_stdout_to(log_path, [&]() {
+        macadvection2_driver adv("macadvection2");
+        adv.set_environment("shape", &s);
+        adv.set_environment("dx", &dxv);
+        adv.setup_now(config);
+    });
+    return 1;
 }
 
 /* Loads, configures and initializes the advection module the

@@ -218,6 +218,10 @@ def load_library():
     lib.gbp_advect3_device.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_double, ctypes.POINTER(AdvectParams), vp, vp, vp, vp, vp, vp,
                                        ctypes.c_float, vp]
+    lib.gbp_advect2.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                ctypes.POINTER(AdvectParams), fp, fp, fp, fp, u8p, ctypes.c_float]
+    lib.gbp_advect2_device.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                       ctypes.POINTER(AdvectParams), vp, vp, vp, vp, vp, ctypes.c_float, vp]
     lib.gbp_constrain_velocity3.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, fp, fp, fp,
                                             fp, u8p, u8p, u8p]
     lib.gbp_constrain_velocity3_device.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, vp,
@@ -633,6 +637,46 @@ class MacAdvection3:
         m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
         rc = self.lib.gbp_advect3(self.ctx.handle, self.nx, self.ny, self.nz, self.dx, dt, ctypes.byref(p), ptrs[0],
                                   ptrs[1], ptrs[2], fptr, ptrs[3] if q is not None else None,
+                                  None if m is None else m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), bg)
+        check(rc)
+
+
+class MacAdvection2(MacAdvection3):
+    """macadvection2_interface on the GPU
+    (``include/shiokaze/advection/macadvection2_interface.h:38-85``, the
+    reference's ``macadvection2`` module, ``src/advection/macadvection2.cpp``,
+    bilinear). Arrays dense (y, x) float32; otherwise as MacAdvection3.
+    ``velocity`` is (u, v)."""
+
+    def __init__(self, nx, ny, dx, context: Context | None = None, **config):
+        super().__init__(nx, ny, 1, dx, context, **config)
+
+    def _run(self, velocity, fluid, dt, q, mask, bg, do_velocity, stream):
+        u, v = velocity[0], velocity[1]
+        p = AdvectParams(self.params.maccormack, self.params.trim_narrowband, 1 if do_velocity else 0)
+        if _is_torch_cuda(u):
+            import torch
+            for t in (u, v, fluid, q):
+                if t is not None:
+                    assert t.dtype == torch.float32 and t.is_contiguous(), "device arrays must be contiguous float32"
+            if mask is not None:
+                assert mask.dtype == torch.uint8 and mask.is_contiguous(), "mask must be contiguous uint8"
+            st = stream if stream is not None else torch.cuda.current_stream(u.device).cuda_stream
+            rc = self.lib.gbp_advect2_device(self.ctx.handle, self.nx, self.ny, self.dx, dt, ctypes.byref(p),
+                                             u.data_ptr(), v.data_ptr(), fluid.data_ptr(),
+                                             q.data_ptr() if q is not None else None,
+                                             mask.data_ptr() if mask is not None else None, bg, ctypes.c_void_p(st))
+            check(rc)
+            return
+        ptrs = []
+        for a in (u, v) + ((q,) if q is not None else ()):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
+                raise TypeError("host arrays must be contiguous float32 numpy arrays (updated in place)")
+            ptrs.append(a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        fa, fptr = _host_f32(fluid)
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        rc = self.lib.gbp_advect2(self.ctx.handle, self.nx, self.ny, self.dx, dt, ctypes.byref(p), ptrs[0], ptrs[1],
+                                  fptr, ptrs[2] if q is not None else None,
                                   None if m is None else m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), bg)
         check(rc)
 

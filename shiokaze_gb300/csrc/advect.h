@@ -47,6 +47,9 @@ struct AdvectArgs {
 
 // Enqueues the step on `stream`; *launches counts kernel launches.
 cudaError_t advect_run(AdvectWork &w, const AdvectArgs &a, cudaStream_t stream, long long *launches);
+// The 2D step (src/advection/macadvection2.cpp, macsmoke2's order): nz and
+// w unused, u (nx+1)*ny, v nx*(ny+1), fluid and q nx*ny.
+cudaError_t advect_run2(AdvectWork &w, const AdvectArgs &a, cudaStream_t stream, long long *launches);
 
 // The solid constraint of the velocity (macutility3::constrain_velocity,
 // src/utility/macutility3.cpp:61-86) on device arrays: solid nodal, u, v, w

@@ -437,6 +437,287 @@ GBA_HD void cell_backward(const StepArgs &a, unsigned c) {
 }
 
 // ---------------------------------------------------------------------------
+// The 2D step, src/advection/macadvection2.cpp (WENO off): the same passes
+// on (nx, ny) grids with bilinear interpolation (include/shiokaze/array/
+// array_interpolator2.h:50-89: weights (i+1-x)(j+1-y), (x-i)(j+1-y),
+// (i+1-x)(y-j), (x-i)(y-j)) and the full vectors of macarray2.h:302-367 (the
+// face's other component summed over its four faces with x outer, y inner).
+// Every face of the velocity is active (src/smoke/macsmoke2.cpp:106).
+
+struct Shape2 {
+    int w, h;
+};
+
+GBA_HD Shape2 face_shape2(const Dims &g, int dim) { return Shape2{g.nx + (dim == 0), g.ny + (dim == 1)}; }
+
+GBA_HD long long at2(const Shape2 &s, int i, int j) { return (long long)i + (long long)s.w * j; }
+
+struct Corner2 {
+    int i, j;
+    double x, y;
+};
+
+GBA_HD Corner2 corner2(const Shape2 &s, double px, double py) {
+    Corner2 c;
+    c.x = smax(0.0, smin(s.w - 1., px));
+    c.y = smax(0.0, smin(s.h - 1., py));
+    c.i = (int)smin(c.x, s.w - 2.);
+    c.j = (int)smin(c.y, s.h - 2.);
+    return c;
+}
+
+GBA_HD void coef2(const Corner2 &c, double coef[4]) {
+    coef[0] = (c.i + 1 - c.x) * (c.j + 1 - c.y);
+    coef[1] = (c.x - c.i) * (c.j + 1 - c.y);
+    coef[2] = (c.i + 1 - c.x) * (c.y - c.j);
+    coef[3] = (c.x - c.i) * (c.y - c.j);
+}
+
+// array_interpolator2::interpolate<float> (:77-89)
+template <class Read>
+GBA_HD float interp2(const Shape2 &s, double px, double py, Read read) {
+    const Corner2 c = corner2(s, px, py);
+    double coef[4];
+    coef2(c, coef);
+    const long long base = at2(s, c.i, c.j);
+    const long long off[4] = {0, 1, s.w, (long long)s.w + 1};
+    float value = 0.0f;
+#pragma unroll
+    for (int n = 0; n < 4; ++n)
+        if (coef[n]) value = (float)((double)value + (double)read(base + off[n]) * coef[n]);
+    return value;
+}
+
+// the four corners' min and max (see corner_minmax)
+template <class Read>
+GBA_HD void corner_minmax2(const Shape2 &s, double px, double py, float lo0, float hi0, Read read, float &lo,
+                           float &hi) {
+    const Corner2 c = corner2(s, px, py);
+    const long long base = at2(s, c.i, c.j);
+    const long long off[4] = {0, 1, s.w, (long long)s.w + 1};
+    float l = lo0, h = hi0;
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+        const float v = read(base + off[n]);
+        l = (v < l) ? v : l;
+        h = (h < v) ? v : h;
+    }
+    lo = l;
+    hi = h;
+}
+
+// interp2(s, p, a) > limit (the bound of compare_interp holds for four
+// corners as for eight)
+GBA_HD bool above_limit2(const Shape2 &s, double px, double py, const float *a, double limit) {
+    const Corner2 c = corner2(s, px, py);
+    const long long base = at2(s, c.i, c.j);
+    const long long off[4] = {0, 1, s.w, (long long)s.w + 1};
+    float v[4];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) v[n] = a[base + off[n]];
+    float mn = v[0], mx = v[0], sum = v[0];
+#pragma unroll
+    for (int n = 1; n < 4; ++n) {
+        mn = v[n] < mn ? v[n] : mn;
+        mx = mx < v[n] ? v[n] : mx;
+        sum += v[n];
+    }
+    if (sum - sum == 0.0f) {
+        const float am = (-mn < mx) ? mx : -mn;
+        const double d = (double)am * 9.5367431640625e-07 + 1e-38;
+        if ((double)mx + d < limit) return false;
+        if ((double)mn - d > limit) return true;
+    }
+    double coef[4];
+    coef2(c, coef);
+    float value = 0.0f;
+#pragma unroll
+    for (int n = 0; n < 4; ++n)
+        if (coef[n]) value = (float)((double)value + (double)v[n] * coef[n]);
+    return (double)value > limit;
+}
+
+// the full velocity at face (i,j) of component dim (macarray2.h:347-367)
+GBA_HD void face_full2(const Dims &g, const float *const comp[2], int dim, int i, int j, float u[2]) {
+    const int ud = 1 - dim;
+    const Shape2 s = face_shape2(g, ud);
+    const int p0 = i - (dim == 0), p1 = j - (dim == 1);
+    double sum = 0.0;
+#pragma unroll
+    for (int ii = 0; ii < 2; ++ii)
+#pragma unroll
+        for (int jj = 0; jj < 2; ++jj) {
+            int q0 = p0 + ii, q1 = p1 + jj;
+            // shape2::clamp
+            q0 = q0 < 0 ? 0 : (q0 > s.w - 1 ? s.w - 1 : q0);
+            q1 = q1 < 0 ? 0 : (q1 > s.h - 1 ? s.h - 1 : q1);
+            sum += comp[ud][at2(s, q0, q1)];
+        }
+    u[dim] = comp[dim][at2(face_shape2(g, dim), i, j)];
+    u[ud] = (float)(sum / 4.0);
+}
+
+// the full velocity at cell (i,j) (macarray2.h:302-340)
+GBA_HD void cell_full2(const Dims &g, const float *const comp[2], int i, int j, float u[2]) {
+#pragma unroll
+    for (int dim = 0; dim < 2; ++dim) {
+        const Shape2 s = face_shape2(g, dim);
+        double value = 0.0;
+        value += comp[dim][at2(s, i, j)];
+        value += comp[dim][at2(s, i + (dim == 0), j + (dim == 1))];
+        u[dim] = (float)(0.5 * value);
+    }
+}
+
+GBA_HD Idx decode2(const Shape2 &s, unsigned f) {
+    const unsigned t = f / (unsigned)s.w;
+    return Idx{(int)(f - t * (unsigned)s.w), (int)t, 0};
+}
+
+GBA_HD unsigned count2(const Shape2 &s) { return (unsigned)s.w * (unsigned)s.h; }
+
+// the 2D passes take StepArgs with w unused and off2 = 0
+
+// forward pass at face f of component dim (advect_semiLagrangian_u,
+// macadvection2.cpp:66-131)
+template <bool MAC>
+GBA_HD void face_forward2(const StepArgs &a, int dim, unsigned f) {
+    const Dims &g = a.g;
+    const Shape2 fs = face_shape2(g, dim);
+    if (f >= count2(fs)) return;
+    const Idx x = decode2(fs, f);
+    const int ip[2] = {x.i, x.j};
+    const float *const comp[2] = {a.u, a.v};
+    const float *src = dim == 0 ? a.u : a.v;
+    const long long o = dim == 0 ? 0 : a.off1;
+    auto rd = [src](long long n) { return src[n]; };
+    float uf[2];
+    face_full2(g, comp, dim, x.i, x.j, uf);
+    const bool moving = uf[0] != 0.0f || uf[1] != 0.0f;
+    float out;
+    if (moving) {
+        double p[2];
+        for (int c = 0; c < 2; ++c) p[c] = (double)ip[c] - (double)trace_f(g, uf[c], a.dt);
+        out = interp2(fs, p[0], p[1], rd);
+    } else {
+        out = src[f];
+    }
+    a.v0[o + f] = out;
+    if (!MAC) return;
+    MinMax m;
+    double fp[2];
+    if (moving) {
+        double p[2];
+        for (int c = 0; c < 2; ++c) {
+            const double disp = trace_d(g, (double)uf[c], a.dt);
+            p[c] = (double)ip[c] - disp;
+            fp[c] = (ip[c] + 0.5 * (dim != c)) - disp;
+        }
+        corner_minmax2(fs, p[0], p[1], INFINITY, 0.0f, rd, m.lo, m.hi);  // DBL_MAX, DBL_MIN
+    } else {
+        for (int c = 0; c < 2; ++c) fp[c] = ip[c] + 0.5 * (dim != c);
+        m.lo = m.hi = src[f];
+    }
+    const Shape2 cs{g.nx, g.ny};
+    if (above_limit2(cs, fp[0] - 0.5, fp[1] - 0.5, a.fluid, g.limit)) m.lo = nan_mark();
+    a.vmm[o + f] = m;
+}
+
+// backward pass and the limited correction at face f (macadvection2.cpp:
+// 133-165), over the input face
+GBA_HD void face_backward2(const StepArgs &a, int dim, unsigned f) {
+    const Dims &g = a.g;
+    const Shape2 fs = face_shape2(g, dim);
+    if (f >= count2(fs)) return;
+    const Idx x = decode2(fs, f);
+    const int ip[2] = {x.i, x.j};
+    const float *const comp[2] = {a.v0, a.v0 + a.off1};
+    const float *src = dim == 0 ? comp[0] : comp[1];
+    float *io = dim == 0 ? a.u : a.v;
+    const long long o = dim == 0 ? 0 : a.off1;
+    float uf[2];
+    face_full2(g, comp, dim, x.i, x.j, uf);
+    const bool moving = uf[0] != 0.0f || uf[1] != 0.0f;
+    float bwd;
+    if (moving) {
+        double p[2];
+        for (int c = 0; c < 2; ++c) p[c] = (double)ip[c] - (double)trace_f(g, uf[c], -a.dt);
+        bwd = interp2(fs, p[0], p[1], [src](long long n) { return src[n]; });
+    } else {
+        bwd = src[f];
+    }
+    io[f] = maccormack(a.vmm[o + f], io[f], src[f], bwd);
+}
+
+// forward pass at cell c (advect_semiLagrangian_cell, macadvection2.cpp:
+// 167-217); inactive cells take the background
+template <bool MAC>
+GBA_HD void cell_forward2(const StepArgs &a, unsigned c) {
+    const Dims &g = a.g;
+    const Shape2 cs{g.nx, g.ny};
+    if (c >= count2(cs)) return;
+    const unsigned char *mask = a.mask;
+    const float bg = a.bg;
+    if (mask && !mask[c]) {
+        a.q0[c] = bg;
+        return;
+    }
+    const Idx x = decode2(cs, c);
+    const int ip[2] = {x.i, x.j};
+    const float *const comp[2] = {a.u, a.v};
+    const float *q = a.q;
+    auto rq = [q, mask, bg](long long n) { return (mask && !mask[n]) ? bg : q[n]; };
+    float uc[2];
+    cell_full2(g, comp, x.i, x.j, uc);
+    const bool moving = uc[0] != 0.0f || uc[1] != 0.0f;
+    double p[2] = {0.0, 0.0};
+    if (moving)
+        for (int d = 0; d < 2; ++d) p[d] = (double)ip[d] - trace_d(g, (double)uc[d], a.dt);
+    const float qc = q[c];
+    a.q0[c] = moving ? interp2(cs, p[0], p[1], rq) : qc;
+    if (!MAC) return;
+    MinMax m;
+    bool within;
+    if (moving) {
+        corner_minmax2(cs, p[0], p[1], FLT_MAX, FLT_MIN, rq, m.lo, m.hi);
+        within = above_limit2(cs, p[0], p[1], a.fluid, g.limit);
+    } else {
+        m.lo = m.hi = qc;
+        within = (double)a.fluid[c] > g.limit;
+    }
+    if (within) m.lo = nan_mark();
+    a.qmm[c] = m;
+}
+
+// backward pass and the limited correction at cell c (macadvection2.cpp:
+// 219-249), over the input scalar
+GBA_HD void cell_backward2(const StepArgs &a, unsigned c) {
+    const Dims &g = a.g;
+    const Shape2 cs{g.nx, g.ny};
+    if (c >= count2(cs)) return;
+    if (a.mask && !a.mask[c]) {
+        a.q[c] = a.bg;
+        return;
+    }
+    const Idx x = decode2(cs, c);
+    const int ip[2] = {x.i, x.j};
+    const float *const comp[2] = {a.u, a.v};
+    float uc[2];
+    cell_full2(g, comp, x.i, x.j, uc);
+    const bool moving = uc[0] != 0.0f || uc[1] != 0.0f;
+    const float *q0 = a.q0;
+    float bwd;
+    if (moving) {
+        double p[2];
+        for (int d = 0; d < 2; ++d) p[d] = (double)ip[d] - trace_d(g, (double)uc[d], -a.dt);
+        bwd = interp2(cs, p[0], p[1], [q0](long long n) { return q0[n]; });
+    } else {
+        bwd = q0[c];
+    }
+    a.q[c] = maccormack(a.qmm[c], a.q[c], q0[c], bwd);
+}
+
+// ---------------------------------------------------------------------------
 // The solid constraint of the velocity, macutility3::constrain_velocity
 // (src/utility/macutility3.cpp:61-86), per face.
 

@@ -55,6 +55,25 @@ __global__ void __launch_bounds__(ADV_THREADS) adv_cell_backward(StepArgs a) {
     gba::cell_backward(a, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// the 2D passes: one thread per face (blockIdx.y = component) or cell
+template <bool MAC>
+__global__ void __launch_bounds__(ADV_THREADS) adv2_face_forward(StepArgs a) {
+    gba::face_forward2<MAC>(a, (int)blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(ADV_THREADS) adv2_face_backward(StepArgs a) {
+    gba::face_backward2(a, (int)blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+template <bool MAC>
+__global__ void __launch_bounds__(ADV_THREADS) adv2_cell_forward(StepArgs a) {
+    gba::cell_forward2<MAC>(a, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(ADV_THREADS) adv2_cell_backward(StepArgs a) {
+    gba::cell_backward2(a, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // levelset_exist (include/shiokaze/array/array_utility3.h:112-122): any
 // negative value of the solid sets the flag
 __global__ void __launch_bounds__(ADV_THREADS) cst_any_negative(const float *__restrict__ solid, long long n,
@@ -179,6 +198,57 @@ cudaError_t advect_run(AdvectWork &w, const AdvectArgs &a, cudaStream_t st, long
             e = cudaMemcpyAsync(dst[d], w.v0 + o[d], sizeof(float) * (size_t)n[d], cudaMemcpyDeviceToDevice, st);
             if (e != cudaSuccess) return e;
         }
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t advect_run2(AdvectWork &w, const AdvectArgs &a, cudaStream_t st, long long *launches) {
+    const long long cells = (long long)a.nx * a.ny;
+    const long long nf0 = (long long)(a.nx + 1) * a.ny, nf1 = (long long)a.nx * (a.ny + 1);
+    const long long nfmax = nf0 > nf1 ? nf0 : nf1;
+    cudaError_t e = advect_reserve(w, a.velocity ? nf0 + nf1 : 0, a.q ? cells : 0);
+    if (e != cudaSuccess) return e;
+    StepArgs s{};
+    s.g = make_dims(a.nx, a.ny, 1, a.dx, a.trim_narrowband);
+    s.dt = a.dt;
+    s.u = a.u;
+    s.v = a.v;
+    s.w = nullptr;
+    s.fluid = a.fluid;
+    s.q = a.q;
+    s.mask = a.q_mask;
+    s.bg = a.q_bg;
+    s.v0 = w.v0;
+    s.vmm = w.vmm;
+    s.off1 = nf0;
+    s.off2 = 0;
+    s.q0 = w.q0;
+    s.qmm = w.qmm;
+    if (a.q) {
+        if (a.maccormack) {
+            adv2_cell_forward<true><<<blocks_for(cells), ADV_THREADS, 0, st>>>(s);
+            adv2_cell_backward<<<blocks_for(cells), ADV_THREADS, 0, st>>>(s);
+            *launches += 2;
+        } else {
+            adv2_cell_forward<false><<<blocks_for(cells), ADV_THREADS, 0, st>>>(s);
+            *launches += 1;
+            e = cudaMemcpyAsync(a.q, w.q0, sizeof(float) * (size_t)cells, cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) return e;
+        }
+    }
+    if (!a.velocity) return cudaGetLastError();
+    const dim3 fgrid(blocks_for(nfmax), 2);
+    if (a.maccormack) {
+        adv2_face_forward<true><<<fgrid, ADV_THREADS, 0, st>>>(s);
+        adv2_face_backward<<<fgrid, ADV_THREADS, 0, st>>>(s);
+        *launches += 2;
+    } else {
+        adv2_face_forward<false><<<fgrid, ADV_THREADS, 0, st>>>(s);
+        *launches += 1;
+        e = cudaMemcpyAsync(a.u, w.v0, sizeof(float) * (size_t)nf0, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(a.v, w.v0 + nf0, sizeof(float) * (size_t)nf1, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();
 }

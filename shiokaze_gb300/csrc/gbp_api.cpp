@@ -997,6 +997,67 @@ int gbp_advect3(gbp_ctx *c, int nx, int ny, int nz, double dx, double dt, const 
     return GBP_OK;
 }
 
+// The 2D step: advect_check with nz = 2 and w = u stands for the 2D checks
+// (edges of at least 2 cells, sizes, arrays, parameters).
+int gbp_advect2_device(gbp_ctx *c, int nx, int ny, double dx, double dt, const gbp_advect_params *params, float *u,
+                       float *v, const float *fluid, float *q, const unsigned char *q_mask, float q_bg,
+                       void *stream) {
+    gbp_advect_params p;
+    int rc = advect_check("gbp_advect2_device", c, nx, ny, 2, dx, dt, params, u, v, u, fluid, q, &p);
+    if (rc) return rc;
+    GBP_CUDA(cudaSetDevice(c->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    if (!stream) {
+        GBP_CUDA(cudaEventRecord(c->ev[0], cudaStreamLegacy));
+        GBP_CUDA(cudaStreamWaitEvent(st, c->ev[0], 0));
+    }
+    long long launched = 0;
+    GBP_CUDA(advect_run2(c->adv, advect_args(nx, ny, 1, dx, dt, p, u, v, nullptr, fluid, q, q_mask, q_bg), st,
+                         &launched));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    c->launches += launched;
+    return GBP_OK;
+}
+
+int gbp_advect2(gbp_ctx *c, int nx, int ny, double dx, double dt, const gbp_advect_params *params, float *u, float *v,
+                const float *fluid, float *q, const unsigned char *q_mask, float q_bg) {
+    gbp_advect_params p;
+    int rc = advect_check("gbp_advect2", c, nx, ny, 2, dx, dt, params, u, v, u, fluid, q, &p);
+    if (rc) return rc;
+    GBP_CUDA(cudaSetDevice(c->device));
+    const size_t cells = (size_t)nx * ny;
+    const size_t nf[2] = {(size_t)(nx + 1) * ny, (size_t)nx * (ny + 1)};
+    const size_t mask_floats = q && q_mask ? (cells + 3) / 4 : 0;
+    const long long need = (long long)(nf[0] + nf[1] + cells + (q ? cells : 0) + mask_floats);
+    if (need > c->adv_stage_floats) {
+        if (c->adv_stage) cudaFree(c->adv_stage);
+        c->adv_stage = nullptr;
+        c->adv_stage_floats = 0;
+        GBP_CUDA(cudaMalloc(&c->adv_stage, sizeof(float) * (size_t)need));
+        c->adv_stage_floats = need;
+    }
+    float *du = c->adv_stage, *dv = du + nf[0], *df = dv + nf[1];
+    float *dq = q ? df + cells : nullptr;
+    unsigned char *dm = mask_floats ? (unsigned char *)(df + 2 * cells) : nullptr;
+    cudaStream_t st = c->stream;
+    GBP_CUDA(cudaMemcpyAsync(du, u, 4 * nf[0], cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(dv, v, 4 * nf[1], cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(df, fluid, 4 * cells, cudaMemcpyHostToDevice, st));
+    if (dq) GBP_CUDA(cudaMemcpyAsync(dq, q, 4 * cells, cudaMemcpyHostToDevice, st));
+    if (dm) GBP_CUDA(cudaMemcpyAsync(dm, q_mask, cells, cudaMemcpyHostToDevice, st));
+    long long launched = 0;
+    GBP_CUDA(advect_run2(c->adv, advect_args(nx, ny, 1, dx, dt, p, du, dv, nullptr, df, dq, dm, q_bg), st,
+                         &launched));
+    if (p.advect_velocity) {
+        GBP_CUDA(cudaMemcpyAsync(u, du, 4 * nf[0], cudaMemcpyDeviceToHost, st));
+        GBP_CUDA(cudaMemcpyAsync(v, dv, 4 * nf[1], cudaMemcpyDeviceToHost, st));
+    }
+    if (dq) GBP_CUDA(cudaMemcpyAsync(q, dq, 4 * cells, cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    c->launches += launched;
+    return GBP_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

@@ -153,6 +153,24 @@ def liquid2(n: int | tuple = 128, seed: int = 1, pool: float = 0.3, drop_c=(0.5,
                  v.astype(np.float32), None, 0, 0, band_of(dx), f"liquid2_{nx}x{ny}", {"seed": seed})
 
 
+def smoke2(n: int | tuple = 128, seed: int = 3, circ_c=(0.5, 0.5), circ_r: float = 0.1, sigma: float = 1.0,
+           dt: float = 1.0 / 60.0) -> Scene:
+    """2D smoke: every cell fluid (constant -1, no band, as src/smoke/
+    macsmoke2.cpp:97 builds it), a solid circle, face velocities
+    N(0, sigma^2)."""
+    nx, ny = (n, n) if isinstance(n, int) else n
+    dx = 1.0 / max(nx, ny)
+    xn = np.arange(nx + 1) * dx
+    yn = np.arange(ny + 1) * dx
+    solid_phi = np.sqrt((xn[None, :] - circ_c[0]) ** 2 + (yn[:, None] - circ_c[1]) ** 2) - circ_r
+    rng = np.random.default_rng(seed)
+    u = rng.normal(0.0, sigma, size=(1, ny, nx + 1)).astype(np.float32)
+    v = rng.normal(0.0, sigma, size=(1, ny + 1, nx)).astype(np.float32)
+    return Scene(2, nx, ny, 1, dx, dt, clamp_band(solid_phi, dx).reshape(1, ny + 1, nx + 1),
+                 np.full((1, ny, nx), -1.0, dtype=np.float32), u, v, None, 0, 1, band_of(dx), f"smoke2_{nx}x{ny}",
+                 {"seed": seed})
+
+
 def batch_liquid3(count: int = 64, seed: int = 4, edge_lo: int = 32, edge_hi: int = 160) -> list[Scene]:
     """Batch of independent 3D liquid scenes: edge log-uniform in
     [edge_lo, edge_hi] (cubic), fluid fraction ~ U[0.1, 0.6] set by the pool

@@ -12,8 +12,11 @@ advected by the velocity, then the velocity by itself. Stored per case in
   fluid_mode, band                                    how the harness built fluid
   out_u, out_v, out_w, out_q                          the reference's outputs
 
+The 2D cases (``advect2/<case>.npz``, arrays y, x, no w) run the
+reference's ``macadvection2`` in macsmoke2's order the same way.
+
 Run from the repository root where the reference sources exist:
-    python tests/golden/make_golden_advect.py
+    python tests/golden/make_golden_advect.py [--2d-only]
 """
 from __future__ import annotations
 
@@ -53,9 +56,52 @@ def cases():
     yield "liquid3_19x23x16_fast", sc, rng.random(sc.fluid.shape, dtype=np.float32), m, 0.0, True, 2
 
 
+OUT2 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "advect2")
+
+
+def cases2():
+    """2D cases for the reference's macadvection2 (arrays y, x)."""
+    rng = np.random.default_rng(12)
+    sc = scenes.smoke2((40, 32), seed=3)
+    yield "smoke2_40x32", sc, rng.random(sc.fluid.shape[1:], dtype=np.float32), None, 0.0, True, 1
+    sc = scenes.smoke2((33, 45), seed=4, sigma=2.0)
+    m = (rng.random(sc.fluid.shape[1:]) > 0.4).astype(np.uint8)
+    yield "smoke2_33x45_mask", sc, rng.random(sc.fluid.shape[1:], dtype=np.float32), m, 0.25, True, 1
+    sc = scenes.smoke2(32, seed=5)
+    yield "smoke2_32_semilagrangian", sc, rng.random(sc.fluid.shape[1:], dtype=np.float32), None, 0.0, False, 1
+    sc = scenes.liquid2(48, seed=2, noise=1.0)
+    m = (sc.fluid[0] < sc.band).astype(np.uint8)
+    yield "liquid2_48_band", sc, rng.random(sc.fluid.shape[1:], dtype=np.float32), m, 0.0, True, 1
+    # traces that leave the grid (CFL ~ 4), faces and cells at rest, -0.0
+    sc = scenes.liquid2((37, 29), seed=9, noise=1.0)
+    for a in (sc.u, sc.v):
+        a *= 15.0
+        a[:, :, :5] = 0.0
+        a[:, :3] = -0.0
+    m = (rng.random(sc.fluid.shape[1:]) > 0.5).astype(np.uint8)
+    yield "liquid2_37x29_fast", sc, rng.random(sc.fluid.shape[1:], dtype=np.float32), m, 0.0, True, 2
+
+
 def main():
     if oracle.build_reference() is None:
         sys.exit("the reference sources are needed (oracle/ref/Makefile)")
+    os.makedirs(OUT2, exist_ok=True)
+    for name, sc, q, m, bg, mac, trim in cases2():
+        q = q.astype(np.float32)
+        if m is not None:
+            q = np.where(m != 0, q, np.float32(bg)).astype(np.float32)
+        u2, v2, fl2 = sc.u[0], sc.v[0], sc.fluid[0]
+        u, v, qo, _ = oracle.advect2(u2, v2, fl2, sc.dx, sc.dt, q=q, q_mask=m, q_bg=bg, maccormack=mac,
+                                     trim_narrowband=trim, impl="reference", fluid_mode=sc.fluid_mode, band=sc.band)
+        ny, nx = fl2.shape
+        np.savez_compressed(
+            os.path.join(OUT2, name + ".npz"), shape=np.array([nx, ny]), dx=sc.dx, dt=sc.dt, maccormack=mac,
+            trim=trim, u=u2, v=v2, fluid=fl2, fluid_mode=sc.fluid_mode, band=sc.band, q=q,
+            q_mask=np.ones(fl2.shape, np.uint8) if m is None else m, q_bg=np.float32(bg), out_u=u, out_v=v,
+            out_q=qo)
+        print(name, "written")
+    if "--2d-only" in sys.argv:
+        return
     os.makedirs(OUT, exist_ok=True)
     for name, sc, q, m, bg, mac, trim in cases():
         q = q.astype(np.float32)

@@ -1,6 +1,6 @@
 /*
  * gbp_oracle_stub.c -- TEST INFRASTRUCTURE: a stand-in for libgbp's
- * advection entry points that runs the oracle (oracle/advect_oracle.c, in
+ * advection entry points (2D and 3D) that runs the oracle (oracle/advect_oracle.c, in
  * liboracle.so) on the CPU, and the same for the solid constraint of the
  * velocity, its extrapolation, and the projection (oracle/gbp_oracle.c: scenes, volume
  * correction, warm start, gbp_project / gbp_project_active with the active
@@ -57,6 +57,26 @@ int gbp_advect3(gbp_ctx *ctx, int nx, int ny, int nz, double dx, double dt, cons
     int rc = oracle_advect3(nx, ny, nz, dx, dt, p->maccormack, p->trim_narrowband, c[0], c[1], c[2], fluid, q, q_mask,
                             q_bg);
     for (int d = 0; d < 3; ++d) free(c[d]);
+    return rc;
+}
+
+int oracle_advect2(int nx, int ny, double dx, double dt, int maccormack, int trim, float *u, float *v,
+                   const float *fluid, float *q, const unsigned char *q_mask, float q_bg);
+
+int gbp_advect2(gbp_ctx *ctx, int nx, int ny, double dx, double dt, const gbp_advect_params *p, float *u, float *v,
+                const float *fluid, float *q, const unsigned char *q_mask, float q_bg) {
+    (void)ctx;
+    if (p->advect_velocity)
+        return oracle_advect2(nx, ny, dx, dt, p->maccormack, p->trim_narrowband, u, v, fluid, q, q_mask, q_bg);
+    const size_t n[2] = {(size_t)(nx + 1) * ny, (size_t)nx * (ny + 1)};
+    float *c[2];
+    const float *src[2] = {u, v};
+    for (int d = 0; d < 2; ++d) {
+        c[d] = (float *)malloc(sizeof(float) * n[d]);
+        memcpy(c[d], src[d], sizeof(float) * n[d]);
+    }
+    int rc = oracle_advect2(nx, ny, dx, dt, p->maccormack, p->trim_narrowband, c[0], c[1], fluid, q, q_mask, q_bg);
+    for (int d = 0; d < 2; ++d) free(c[d]);
     return rc;
 }
 

@@ -67,3 +67,50 @@ def test_port_matches_live_reference_advect(seed):
                        band=sc.band, **kw)
     for x, y in zip(a[:4], b[:4]):
         assert bits_equal(x, y)
+
+
+# ---- 2D (src/advection/macadvection2.cpp) -----------------------------------------
+GOLDEN2 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "advect2")
+
+
+def advect2_cases():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN2, "*.npz")))
+
+
+@pytest.mark.parametrize("name", advect2_cases())
+def test_port_matches_reference_advect2_fixture(name):
+    """The 2D restatement reproduces the reference's macadvection2 fixtures
+    (tests/golden/make_golden_advect.py) bit for bit."""
+    d = dict(np.load(os.path.join(GOLDEN2, name + ".npz")))
+    u, v, q, _ = oracle.advect2(d["u"], d["v"], d["fluid"], float(d["dx"]), float(d["dt"]), q=d["q"],
+                                q_mask=d["q_mask"], q_bg=float(d["q_bg"]), maccormack=bool(d["maccormack"]),
+                                trim_narrowband=int(d["trim"]))
+    assert bits_equal(u, d["out_u"]) and bits_equal(v, d["out_v"]) and bits_equal(q, d["out_q"])
+
+
+def test_advect2_fixtures_cover_the_branches():
+    names = advect2_cases()
+    assert len(names) >= 5
+    d = dict(np.load(os.path.join(GOLDEN2, "liquid2_37x29_fast.npz")))
+    assert (d["u"][:, :5] == 0).all()
+    assert np.abs(d["u"]).max() * float(d["dt"]) / float(d["dx"]) > 2.0
+    d = dict(np.load(os.path.join(GOLDEN2, "smoke2_33x45_mask.npz")))
+    assert (d["q_mask"] == 0).any() and (d["out_q"][d["q_mask"] == 0] == np.float32(d["q_bg"])).all()
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference oracle not built here")
+@pytest.mark.parametrize("seed", [41, 42, 43, 44])
+def test_port_matches_live_reference_advect2(seed):
+    rng = np.random.default_rng(seed)
+    n = tuple(int(x) for x in rng.integers(6, 60, 2))
+    sc = (scenes.liquid2(n, seed=seed, noise=float(rng.uniform(0.2, 3.0))) if seed % 2
+          else scenes.smoke2(n, seed=seed, sigma=float(rng.uniform(0.5, 4.0))))
+    fl = sc.fluid[0]
+    m = (rng.random(fl.shape) > rng.uniform(0.0, 0.6)).astype(np.uint8)
+    q = np.where(m != 0, rng.normal(0, 1, fl.shape), 0.5).astype(np.float32)
+    kw = dict(q=q, q_mask=m, q_bg=0.5, maccormack=seed != 43, trim_narrowband=int(rng.integers(0, 3)))
+    a = oracle.advect2(sc.u[0], sc.v[0], fl, sc.dx, sc.dt, **kw)
+    b = oracle.advect2(sc.u[0], sc.v[0], fl, sc.dx, sc.dt, impl="reference", fluid_mode=sc.fluid_mode,
+                       band=sc.band, **kw)
+    for x, y in zip(a[:3], b[:3]):
+        assert bits_equal(x, y)

@@ -34,6 +34,8 @@ def host(tmp_path_factory):
     lib.host_advect3.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 2 + [ctypes.c_int] * 2 + [FP] * 5 + \
         [U8, ctypes.c_float]
     lib.host_constrain3.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] + [FP] * 4 + [U8] * 3
+    lib.host_advect2.argtypes = [ctypes.c_int] * 2 + [ctypes.c_double] * 2 + [ctypes.c_int] * 2 + [FP] * 4 + \
+        [U8, ctypes.c_float]
     return lib
 
 
@@ -76,6 +78,53 @@ def test_advect_kernel_code_matches_reference_fixture(host, path):
                       trim_narrowband=int(d["trim"]))
     for a, key in zip(out, ("out_u", "out_v", "out_w", "out_q")):
         assert bits_equal(a, d[key])
+
+
+def host_advect2(lib, u, v, fluid, dx, dt, q=None, q_mask=None, q_bg=0.0, maccormack=True, trim_narrowband=1):
+    ny, nx = fluid.shape
+    uo, vo = (np.array(a, dtype=np.float32, order="C") for a in (u, v))
+    fl = np.ascontiguousarray(fluid, dtype=np.float32)
+    qo = None if q is None else np.array(q, dtype=np.float32, order="C")
+    qm = None if q_mask is None else np.ascontiguousarray(q_mask, dtype=np.uint8)
+    lib.host_advect2(nx, ny, dx, dt, int(maccormack), int(trim_narrowband), uo.ctypes.data_as(FP),
+                     vo.ctypes.data_as(FP), fl.ctypes.data_as(FP), None if qo is None else qo.ctypes.data_as(FP),
+                     _u8(qm), q_bg)
+    return uo, vo, qo
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "advect2", "*.npz"))),
+                         ids=lambda p: os.path.basename(p)[:-4])
+def test_advect2_kernel_code_matches_reference_fixture(host, path):
+    """The 2D passes (advect_core.cuh face_forward2 ... cell_backward2)
+    reproduce the reference's macadvection2 fixtures bit for bit."""
+    d = dict(np.load(path))
+    out = host_advect2(host, d["u"], d["v"], d["fluid"], float(d["dx"]), float(d["dt"]), q=d["q"],
+                       q_mask=d["q_mask"], q_bg=float(d["q_bg"]), maccormack=bool(d["maccormack"]),
+                       trim_narrowband=int(d["trim"]))
+    for a, key in zip(out, ("out_u", "out_v", "out_q")):
+        assert bits_equal(a, d[key])
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_advect2_kernel_code_matches_oracle_random(host, seed):
+    rng = np.random.default_rng(100 + seed)
+    n = tuple(int(x) for x in rng.integers(2, 40, 2))
+    sc = (scenes.liquid2(n, seed=seed, noise=float(rng.uniform(0.2, 3.0))) if seed % 2
+          else scenes.smoke2(n, seed=seed, sigma=float(rng.uniform(0.5, 4.0))))
+    dx = sc.dx if seed % 3 else float(rng.uniform(0.01, 0.2))
+    fl = sc.fluid[0]
+    m = (rng.random(fl.shape) > rng.uniform(0.0, 0.6)).astype(np.uint8) if seed % 4 else None
+    q = rng.normal(0, 1, fl.shape).astype(np.float32)
+    u, v = (a[0] * np.float32(rng.uniform(0.5, 30)) for a in (sc.u, sc.v))
+    if seed % 5 == 0:
+        u[:, :2] = 0.0
+        v[:, :2] = 0.0
+    trim = int(rng.integers(0, 3))
+    kw = dict(q=q, q_mask=m, q_bg=float(rng.normal()), maccormack=seed % 7 != 3, trim_narrowband=trim)
+    want = oracle.advect2(u, v, fl, dx, sc.dt, **kw)
+    got = host_advect2(host, u, v, fl, dx, sc.dt, **kw)
+    for a, b in zip(got, want[:3]):
+        assert bits_equal(a, b)
 
 
 @pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "constrain", "*.npz"))),

@@ -255,6 +255,61 @@ def test_advection_module_boundary_matches_reference_module(tmp_path):
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (seed, name)
 
 
+def advect2_module_cases():
+    for seed in (51, 52, 53, 54):
+        rng = np.random.default_rng(seed)
+        n = tuple(int(x) for x in rng.integers(6, 48, 2))
+        sc = (scenes.liquid2(n, seed=seed, noise=float(rng.uniform(0.2, 3.0))) if seed % 2
+              else scenes.smoke2(n, seed=seed, sigma=float(rng.uniform(0.5, 4.0))))
+        fl = sc.fluid[0]
+        m = (rng.random(fl.shape) > 0.4).astype(np.uint8) if seed != 52 else None
+        q = rng.random(fl.shape, dtype=np.float32)
+        if m is not None:
+            q = np.where(m != 0, q, np.float32(0.25)).astype(np.float32)
+        kw = dict(q=q, q_mask=m, q_bg=0.25 if m is not None else 0.0, maccormack=seed != 53,
+                  trim_narrowband=int(rng.integers(0, 3)))
+        yield seed, sc, kw
+
+
+ADVECT2_MODULE_RUN = r"""
+import sys
+import numpy as np
+import oracle
+sys.path.insert(0, "tests")
+from test_oracle import advect2_module_cases
+out = {}
+for seed, sc, kw in advect2_module_cases():
+    r = oracle.advect2(sc.u[0], sc.v[0], sc.fluid[0], sc.dx, sc.dt, impl="reference", fluid_mode=sc.fluid_mode,
+                       band=sc.band, extra_kv="Advection=gbadvection2stub", **kw)
+    for name, a in zip("uvq", r[:3]):
+        out[f"{seed}_{name}"] = a
+np.savez(sys.argv[1], **out)
+"""
+
+
+def test_advection2_module_boundary_matches_reference_module(tmp_path):
+    """The gbadvection2 module (Advection=gbadvection2) on the CPU: linked
+    to the oracle-backed stand-in for libgbp and loaded by the reference's
+    loader in place of macadvection2, on the reference's own 2D tiled arrays,
+    it gives the reference module's results bit for bit."""
+    import subprocess
+    import sys
+    if not oracle.reference_available():
+        pytest.skip("reference oracle not built here")
+    root = _stub_module(tmp_path, "gbadvection2", "gbadvection2stub")
+    out = tmp_path / "module2.npz"
+    r = subprocess.run([sys.executable, "-c", ADVECT2_MODULE_RUN, str(out)], cwd=root, capture_output=True,
+                       text=True, timeout=300, env=dict(os.environ, PYTHONPATH=root))
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    got = dict(np.load(out))
+    for seed, sc, kw in advect2_module_cases():
+        want = oracle.advect2(sc.u[0], sc.v[0], sc.fluid[0], sc.dx, sc.dt, impl="reference",
+                              fluid_mode=sc.fluid_mode, band=sc.band, **kw)
+        for name, a in zip("uvq", want[:3]):
+            b = got[f"{seed}_{name}"]
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (seed, name)
+
+
 def _stub_module(tmp_path, module, installed_as):
     """Builds plugin module `module` linked against the oracle-backed
     stand-in for libgbp (tests/module_stub) and installs it beside the
