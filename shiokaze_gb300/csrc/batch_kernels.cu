@@ -27,6 +27,11 @@
 namespace gbp {
 namespace {
 
+// T -> double: exact; from integer instructions for FP32 (gbp_convert.cuh),
+// off the FP64 pipe
+__device__ __forceinline__ double widen(double v) { return v; }
+__device__ __forceinline__ double widen(float v) { return f2d_exact(v); }
+
 // FP64 to T; to FP32 by integer instructions (gbp_convert.cuh), off the
 // FP64 pipe
 template <class T> __device__ __forceinline__ T narrow_to(double v) {
@@ -1544,9 +1549,81 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
             pair_tile(L.g, it, [&](int, int, int, long long c, bool second) {
                 const Pair<T> d2 = ld2<T, V>(S.x, c, second);
                 const Pair<double> o = ld2<double, V>(S.x64, c, second);
-                st2<double, V>(S.x64, c, Pair<double>{o.a + (double)d2.a, o.b + (double)d2.b}, second);
+                st2<double, V>(S.x64, c, Pair<double>{o.a + widen(d2.a), o.b + widen(d2.b)}, second);
             });
         });
+    }
+}
+
+// The refinement residual over two planes k, k+1 of a pair column (no
+// warm-start pressure, x64 present): every load of the two planes first,
+// then per cell diag x minus the neighbour terms in the order -x, +x, -y,
+// +y, -z, +z, as the plane-by-plane form computes them (the same FP64
+// operations in the same order). On this GPU the FP64 pipe issues about two
+// operations per clock per SM: the plane form waited on its loads between
+// short FP64 chains; here four independent chains (two cells, two planes)
+// have their operands ready.
+template <class T>
+__device__ __forceinline__ void refine_col2(const Grid &g, const BScene<T> &S, int i, int j, int k, long long c,
+                                            MaxSumAcc<T> &acc) {
+    const Operator<double> &A = S.A;
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const Pair<double> zero{0.0, 0.0};
+    const double *x = S.x64;
+    Pair<double> xc[2], xym[2], xyp[2], dg[2], cxp[2], cym[2], cyp[2], bb[2];
+    double xm[2], xp[2], cxm[2];
+    const Pair<double> xlo = k > 0 ? ld2<double, true>(x, c - sz, true) : zero;
+    const Pair<double> xhi = k + 2 < g.nz ? ld2<double, true>(x, c + 2 * sz, true) : zero;
+    const Pair<double> czl = k > 0 ? ld2<double, true>(A.cz, c - sz, true) : zero;
+    const Pair<double> czc = ld2<double, true>(A.cz, c, true);
+    const Pair<double> czh = k + 2 < g.nz ? ld2<double, true>(A.cz, c + sz, true) : zero;
+#pragma unroll
+    for (int z = 0; z < 2; ++z) {
+        const long long cz_ = c + z * sz;
+        xc[z] = ld2<double, true>(x, cz_, true);
+        xym[z] = j > 0 ? ld2<double, true>(x, cz_ - sy, true) : zero;
+        xyp[z] = j + 1 < g.ny ? ld2<double, true>(x, cz_ + sy, true) : zero;
+        xm[z] = i > 0 ? __ldg(x + cz_ - 1) : 0.0;
+        xp[z] = i + 2 < g.nx ? __ldg(x + cz_ + 2) : 0.0;
+        dg[z] = ld2<double, true>(A.diag, cz_, true);
+        cxp[z] = ld2<double, true>(A.cx, cz_, true);
+        cxm[z] = i > 0 ? __ldg(A.cx + cz_ - 1) : 0.0;
+        cym[z] = j > 0 ? ld2<double, true>(A.cy, cz_ - sy, true) : zero;
+        cyp[z] = j + 1 < g.ny ? ld2<double, true>(A.cy, cz_, true) : zero;
+        bb[z] = ld2<double, true>(S.b, cz_, true);
+    }
+#pragma unroll
+    for (int z = 0; z < 2; ++z) {
+        const int kz = k + z;
+        const Pair<double> xzm = z == 0 ? xlo : xc[0], xzp = z == 0 ? xc[1] : xhi;
+        const Pair<double> czm = z == 0 ? czl : czc, czp = z == 0 ? czc : czh;
+        double a0 = dg[z].a * xc[z].a, a1 = dg[z].b * xc[z].b;
+        if (i > 0) a0 -= cxm[z] * xm[z];
+        a0 -= cxp[z].a * xc[z].b;
+        a1 -= cxp[z].a * xc[z].a;
+        if (i + 2 < g.nx) a1 -= cxp[z].b * xp[z];
+        if (j > 0) {
+            a0 -= cym[z].a * xym[z].a;
+            a1 -= cym[z].b * xym[z].b;
+        }
+        if (j + 1 < g.ny) {
+            a0 -= cyp[z].a * xyp[z].a;
+            a1 -= cyp[z].b * xyp[z].b;
+        }
+        if (kz > 0) {
+            a0 -= czm.a * xzm.a;
+            a1 -= czm.b * xzm.b;
+        }
+        if (kz + 1 < g.nz) {
+            a0 -= czp.a * xzp.a;
+            a1 -= czp.b * xzp.b;
+        }
+        const Pair<double> rv{bb[z].a - a0, bb[z].b - a1};
+        const Pair<T> rt{narrow_to<T>(rv.a), narrow_to<T>(rv.b)};
+        st2<double, true>(S.r64, c + z * sz, rv, true);
+        st2<T, true>(S.r, c + z * sz, rt, true);
+        acc.add(rv.a, rt.a);
+        acc.add(rv.b, rt.b);
     }
 }
 
@@ -1558,7 +1635,9 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
 // solution. Each cell's residual is accumulated as diag X minus the
 // neighbour terms one by one (-x, +x, -y, +y, -z, +z), in FP64.
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_residual_kernel(
+// Two blocks per SM: the FP64 pipe, not occupancy, bounds this kernel, and
+// the gather-first column needs the registers.
+__global__ void __launch_bounds__(BLOCK_THREADS, 2) refine_residual_kernel(
     const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
     const BScene<T> *__restrict__ scenes, double *part, int initial, double residual, int max_iter,
     double inner_rel, int inner_max, BatchCounters *cnt, const int *__restrict__ scene_of) {
@@ -1603,6 +1682,54 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks) refine_res
                     return v;
                 };
                 const bool zero_x = initial && S.prev == nullptr;  // r = b exactly
+                if constexpr (V) {
+                    if (!initial && S.prev == nullptr && it.ntiles == 1 && g.tz == 4) {
+                        // 4-plane tiles: two gather-first pairs of planes
+                        pair_tile_z4(g, it, [&](int i, int j, int k0, long long c0) {
+                            refine_col2<T>(g, S, i, j, k0, c0, acc);
+                            refine_col2<T>(g, S, i, j, k0 + 2, c0 + 2 * sz, acc);
+                        }, [&](int i, int j, int k, long long c, bool second) {
+                            // a partial last tile: the plane form below
+                            const Pair<double> xc = X2(c, second), dg = ld2<double, V>(A.diag, c, second);
+                            const Pair<double> cxp = ld2<double, V>(A.cx, c, second);
+                            double a0 = dg.a * xc.a, a1 = dg.b * xc.b;
+                            if (i > 0) a0 -= __ldg(A.cx + c - 1) * X1(c - 1);
+                            if (second) {
+                                a0 -= cxp.a * xc.b;
+                                a1 -= cxp.a * xc.a;
+                                if (i + 2 < g.nx) a1 -= cxp.b * X1(c + 2);
+                            }
+                            if (j > 0) {
+                                const Pair<double> w = ld2<double, V>(A.cy, c - sy, second), v = X2(c - sy, second);
+                                a0 -= w.a * v.a;
+                                a1 -= w.b * v.b;
+                            }
+                            if (j + 1 < g.ny) {
+                                const Pair<double> w = ld2<double, V>(A.cy, c, second), v = X2(c + sy, second);
+                                a0 -= w.a * v.a;
+                                a1 -= w.b * v.b;
+                            }
+                            if (k > 0) {
+                                const Pair<double> w = ld2<double, V>(A.cz, c - sz, second), v = X2(c - sz, second);
+                                a0 -= w.a * v.a;
+                                a1 -= w.b * v.b;
+                            }
+                            if (k + 1 < g.nz) {
+                                const Pair<double> w = ld2<double, V>(A.cz, c, second), v = X2(c + sz, second);
+                                a0 -= w.a * v.a;
+                                a1 -= w.b * v.b;
+                            }
+                            const Pair<double> bb = ld2<double, V>(S.b, c, second);
+                            const Pair<double> rv{bb.a - a0, bb.b - a1};
+                            const Pair<T> rt{narrow_to<T>(rv.a), narrow_to<T>(rv.b)};
+                            st2<double, V>(S.r64, c, rv, second);
+                            st2<T, V>(S.r, c, rt, second);
+                            acc.add(rv.a, rt.a);
+                            if (second) acc.add(rv.b, rt.b);
+                        });
+                        return;
+                    }
+                }
                 pair_tile(g, it, [&](int i, int j, int k, long long c, bool second) {
                     if (zero_x) {
                         const Pair<double> rv = ld2<double, V>(S.b, c, second);

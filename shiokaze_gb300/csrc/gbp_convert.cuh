@@ -12,7 +12,7 @@
 // result is not a normal float before rounding (zero, float subnormals,
 // overflow, infinities, NaN) take the hardware conversion. The result equals
 // (float)d bit for bit for every double; tests/test_kernel_host.py checks
-// that on the host.
+// that on the host (and f2d_exact against (double)f).
 #pragma once
 
 #include <cstring>
@@ -39,6 +39,29 @@ __host__ __device__ __forceinline__ float d2f_from_bits(unsigned u) {
 #endif
 }
 
+// The hardware conversions, for the rare operands the integer forms leave
+// to them. On the device they are volatile inline PTX: the compiler may not
+// execute them speculatively on every lane (a plain cast in the untaken
+// branch was if-converted and issued for every element, on the FP64 pipe).
+__host__ __device__ __forceinline__ float d2f_hw(double d) {
+#ifdef __CUDA_ARCH__
+    float r;
+    asm volatile("cvt.rn.f32.f64 %0, %1;" : "=f"(r) : "d"(d));
+    return r;
+#else
+    return (float)d;
+#endif
+}
+__host__ __device__ __forceinline__ double f2d_hw(float f) {
+#ifdef __CUDA_ARCH__
+    double r;
+    asm volatile("cvt.f64.f32 %0, %1;" : "=d"(r) : "f"(f));
+    return r;
+#else
+    return (double)f;
+#endif
+}
+
 __host__ __device__ __forceinline__ float d2f_rn(double d) {
     const unsigned long long b = d2f_bits_of(d);
     const int e32 = (int)((b >> 52) & 0x7ffu) - 1023 + 127;
@@ -50,7 +73,51 @@ __host__ __device__ __forceinline__ float d2f_rn(double d) {
         const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
         return d2f_from_bits(sign | (((unsigned)e32 << 23) + mm));
     }
-    return (float)d;
+    if ((b << 1) == 0) return d2f_from_bits((unsigned)(b >> 32) & 0x80000000u);  // +-0
+    return d2f_hw(d);
+}
+
+// (double)f exactly, from integer instructions for normal floats and zeros
+// (the exponent re-biased, the 23 mantissa bits moved up); subnormals,
+// infinities and NaN take the hardware conversion.
+__host__ __device__ __forceinline__ double f2d_exact(float f) {
+#ifdef __CUDA_ARCH__
+    const unsigned u = __float_as_uint(f);
+#else
+    unsigned u;
+    std::memcpy(&u, &f, sizeof u);
+#endif
+    const unsigned ex = (u >> 23) & 0xffu;
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    if (ex != 0u && ex != 0xffu) {
+        const unsigned long long bits =
+            sign | ((unsigned long long)(ex + (1023 - 127)) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+#ifdef __CUDA_ARCH__
+        return __longlong_as_double((long long)bits);
+#else
+        double d;
+        std::memcpy(&d, &bits, sizeof d);
+        return d;
+#endif
+    }
+    if ((u << 1) == 0u) {
+#ifdef __CUDA_ARCH__
+        return __longlong_as_double((long long)sign);
+#else
+        double d;
+        std::memcpy(&d, &sign, sizeof d);
+        return d;
+#endif
+    }
+    return f2d_hw(f);
+}
+
+// d != 0.0 and d > 0.0 from the bit pattern (no FP64 comparison; a NaN is
+// nonzero and not positive, as the comparisons have it)
+__host__ __device__ __forceinline__ bool nonzero_bits(double d) { return (d2f_bits_of(d) << 1) != 0; }
+__host__ __device__ __forceinline__ bool positive_bits(double d) {
+    const unsigned long long b = d2f_bits_of(d);
+    return !(b >> 63) && b != 0 && b <= 0x7ff0000000000000ull;
 }
 
 }  // namespace gbp

@@ -118,24 +118,42 @@ __device__ __forceinline__ double face_weight(double dt, double area, double rho
     return num / (dx * dx * rho);
 }
 
+// face_weight and the flux area*u/dx of a cut face, not inlined (see
+// area3_fp64): the same operations as face_weight and div_dx.
+__device__ __noinline__ double face_weight_fp64(double dt, float area, float rho, double dx, int dx_pow2,
+                                                double inv_dx2) {
+    const double num = dt * (double)area;
+    if (dx_pow2 && (double)rho == 1.0) return num * inv_dx2;
+    return num / (dx * dx * (double)rho);
+}
+__device__ __noinline__ double face_flux_fp64(float area, float uf, double dx, int dx_pow2, double inv_dx) {
+    const double x = (double)area * (double)uf;
+    return dx_pow2 ? x * inv_dx : x / dx;
+}
+
 // face_area of an interior 3D face from its four corner levels (q00, q10,
 // q11, q01 in the corner order of face_area).
+// The FP64 tail of area3 (a cut square, or eps_solid above 1): not inlined,
+// so that the compiler cannot issue its FP64 instructions speculatively for
+// the uniform squares that return early.
+__device__ __noinline__ float area3_fp64(float q00, float q10, float q11, float q01, bool uniform, double eps_solid,
+                                         int second_order_solid) {
+    double area = uniform ? 1.0 : 1.0 - solid_area(q00, q10, q11, q01);
+    if (area && area < eps_solid) area = eps_solid;
+    float a = (float)area;
+    if (!second_order_solid && a) a = 1.0f;  // macpressuresolver3.cpp:76-80
+    return a;
+}
+
 __device__ __forceinline__ float area3(float q00, float q10, float q11, float q01, const FaceParams &fp) {
-    double area;
     // uniform squares decided in float (the same comparisons as in double);
     // their fraction (1 or 0) is final unless eps_solid exceeds 1
     if (q00 >= 0.0f && q10 >= 0.0f && q11 >= 0.0f && q01 >= 0.0f) {
         if (fp.eps_solid_le1) return 1.0f;
-        area = 1.0;
-    } else if (q00 < 0.0f && q10 < 0.0f && q11 < 0.0f && q01 < 0.0f) {
-        return 0.0f;
-    } else {
-        area = 1.0 - solid_area(q00, q10, q11, q01);
+        return area3_fp64(q00, q10, q11, q01, true, fp.eps_solid, fp.second_order_solid);
     }
-    if (area && area < fp.eps_solid) area = fp.eps_solid;
-    float a = (float)area;
-    if (!fp.second_order_solid && a) a = 1.0f;  // macpressuresolver3.cpp:76-80
-    return a;
+    if (q00 < 0.0f && q10 < 0.0f && q11 < 0.0f && q01 < 0.0f) return 0.0f;
+    return area3_fp64(q00, q10, q11, q01, false, fp.eps_solid, fp.second_order_solid);
 }
 
 // Open (non-solid) fraction of face (i,j,k) normal to d
@@ -173,11 +191,20 @@ __device__ float face_area(const Grid &g, const float *__restrict__ solid, int d
 }
 
 // face_rho of a face between cells of levels f0 and f1, with fluid present.
+// The FP64 tail of rho_of (a cut face, or eps_fluid above 1), not inlined
+// (see area3_fp64).
+__device__ __noinline__ float rho_fp64(float f0, float f1, bool uniform, double eps_fluid, int second_order_fluid) {
+    double rho = uniform ? 1.0 : fraction(f0, f1);
+    if (rho && rho < eps_fluid) rho = eps_fluid;
+    float r = (float)rho;
+    if (!second_order_fluid && r) r = 1.0f;  // macpressuresolver3.cpp:70-74
+    return r;
+}
+
 __device__ __forceinline__ float rho_of(float f0, float f1, const FaceParams &fp) {
     // Same sign (or a zero): fraction() returns 1 or 0. The double product
     // of two floats never underflows to 0, so its sign test equals this
     // float sign test.
-    double rho;
     if (!((f0 < 0.0f && f1 > 0.0f) || (f0 > 0.0f && f1 < 0.0f))) {
         // 1 or 0, final unless eps_fluid exceeds 1
         const bool wet = f0 < 0.0f || f1 < 0.0f;
@@ -186,14 +213,9 @@ __device__ __forceinline__ float rho_of(float f0, float f1, const FaceParams &fp
             if (!fp.second_order_fluid && r) r = 1.0f;
             return r;
         }
-        rho = 1.0;
-    } else {
-        rho = fraction(f0, f1);
+        return rho_fp64(f0, f1, true, fp.eps_fluid, fp.second_order_fluid);
     }
-    if (rho && rho < fp.eps_fluid) rho = fp.eps_fluid;
-    float r = (float)rho;
-    if (!fp.second_order_fluid && r) r = 1.0f;  // macpressuresolver3.cpp:70-74
-    return r;
+    return rho_fp64(f0, f1, false, fp.eps_fluid, fp.second_order_fluid);
 }
 
 // Liquid fraction of face (i,j,k) normal to d, between the clamped cells
@@ -376,15 +398,18 @@ __global__ void __launch_bounds__(BLOCK_THREADS) assemble_kernel(
 // Float pressure of every cell (0 off the unknowns, macpressuresolver3.cpp:
 // 245-248). With warm start the solve found the correction x to the kept
 // pressure prev; the result is x + prev (:239-242), which is kept again.
+template <bool WARM>
 __global__ void __launch_bounds__(BLOCK_THREADS) pressure_kernel(Grid g, const double *__restrict__ diag,
                                                                  const double *__restrict__ x,
                                                                  const double *prev, float *__restrict__ p,
                                                                  double *keep) {
+    // WARM (prev != NULL) is a template argument so that the FP64 addition
+    // is not issued, predicated off, for every cell of a cold start
     const long long n = g.ncell;
     for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-        const bool unk = __ldg(diag + c) != 0.0;
+        const bool unk = nonzero_bits(__ldg(diag + c));  // diag != 0, as integers
         double xv = unk ? __ldg(x + c) : 0.0;
-        if (prev && unk) xv = xv + prev[c];
+        if (WARM && unk) xv = xv + prev[c];
         p[c] = d2f_rn(xv);  // (float)xv, by integer instructions
         if (keep) keep[c] = xv;
     }
@@ -464,6 +489,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_kernel(Grid g, double 
 // single-pass assemble_kernel (and to the reference); it also writes level 0
 // of the multigrid hierarchy (the FP32 operator of the mixed solver, or the
 // FP64 inverse diagonal) from the same registers.
+// DIM is a template argument: the 3D instantiation holds no FP64 code of
+// the 2D path, which the compiler would otherwise issue predicated off for
+// every node (a predicated-off FP64 instruction still takes its FP64-pipe
+// slot on this GPU).
+template <int DIM>
 __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt, double dx, FaceParams fp,
                                                               const float *__restrict__ solid,
                                                               const float *__restrict__ fluid,
@@ -480,14 +510,15 @@ __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt,
         fa.rho[d][f] = open ? rho : (area ? -1.0f : 0.0f);
         fa.area[d][f] = area;
         // the FP64 weight and flux only where the cell pass cannot form them
-        if (open && !(area == 1.0f && rho == 1.0f)) fa.w[d][f] = face_weight(dt, (double)area, (double)rho, dx, fp);
-        if (area != 0.0f && !(area == 1.0f && fp.dx_pow2)) fa.q[d][f] = div_dx((double)area * (double)uf, dx, fp);
+        if (open && !(area == 1.0f && rho == 1.0f))
+            fa.w[d][f] = face_weight_fp64(dt, area, rho, dx, fp.dx_pow2, fp.inv_dx2);
+        if (area != 0.0f && !(area == 1.0f && fp.dx_pow2)) fa.q[d][f] = face_flux_fp64(area, uf, dx, fp.dx_pow2, fp.inv_dx);
     };
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         node_coords(g, t, i, j, k);
-        if (g.dim == 3) {
+        if constexpr (DIM == 3) {
             // The node's three faces with every load issued first (the
             // per-face form waits for each face's loads in turn: its stores
             // could alias the next face's inputs). A face exists when its
@@ -523,20 +554,66 @@ __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt,
             if (ex[0]) emit(0, f[0], in[0] ? area3(S000, S010, S011, S001, fp) : 0.0f, rho_of(fA, fB0, fp), uf[0]);
             if (ex[1]) emit(1, f[1], in[1] ? area3(S000, S100, S101, S001, fp) : 0.0f, rho_of(fA, fB1, fp), uf[1]);
             if (ex[2]) emit(2, f[2], in[2] ? area3(S000, S100, S110, S010, fp) : 0.0f, rho_of(fA, fB2, fp), uf[2]);
-            continue;
-        }
-        const int pi[3] = {i, j, k};
-        for (int d = 0; d < g.dim; ++d) {
-            bool exists = true;
-            for (int e = 0; e < g.dim; ++e)
-                if (e != d && pi[e] >= n[e]) exists = false;
-            if (!exists) continue;
-            const long long f = face_index(g, d, i, j, k);
-            emit(d, f, face_area(g, solid, d, i, j, k, fp), face_rho(g, fluid, d, i, j, k, fp, 1), __ldg(vel[d] + f));
+        } else {
+            const int pi[3] = {i, j, k};
+            for (int d = 0; d < 2; ++d) {
+                bool exists = true;
+                for (int e = 0; e < 2; ++e)
+                    if (e != d && pi[e] >= n[e]) exists = false;
+                if (!exists) continue;
+                const long long f = face_index(g, d, i, j, k);
+                emit(d, f, face_area(g, solid, d, i, j, k, fp), face_rho(g, fluid, d, i, j, k, fp, 1),
+                     __ldg(vel[d] + f));
+            }
         }
     }
 }
 
+// The FP64 fallbacks of the cell pass, out of line (see faces_kernel):
+// the diagonal as the sequential sum of the open faces' weights, and the
+// right-hand side as the sequential sum of -+area*u/dx, in the order +x,
+// -x, +y, -y, +z, -z, for a cell the integer forms leave.
+__device__ __noinline__ double diag_fp64(const Grid g, const FaceArrays fa, int i, int j, int k, double w_unit) {
+    const int n[3] = {g.nx, g.ny, g.nz};
+    double dg = 0.0;
+    for (int nq = 0; nq < 2 * g.dim; ++nq) {
+        const int d = nq >> 1;
+        int q[3] = {i, j, k}, f[3] = {i, j, k};
+        q[d] += (nq & 1) == 0 ? 1 : -1;
+        if (q[d] < 0 || q[d] >= n[d]) continue;
+        if ((nq & 1) == 0) f[d] += 1;
+        const long long fi = face_index(g, d, f[0], f[1], f[2]);
+        const float r = fa.rho[d][fi], a = fa.area[d][fi];
+        if (r > 0.0f) dg += (a == 1.0f && r == 1.0f) ? w_unit : fa.w[d][fi];
+    }
+    return dg;
+}
+__device__ __noinline__ double rhs_fp64(const Grid g, const FaceArrays fa, const float *u, const float *v,
+                                        const float *w, int i, int j, int k, int dx_pow2, double inv_dx) {
+    const int n[3] = {g.nx, g.ny, g.nz};
+    const float *vel[3] = {u, v, w};
+    double rhs = 0.0;
+    for (int nq = 0; nq < 2 * g.dim; ++nq) {
+        const int d = nq >> 1;
+        int q[3] = {i, j, k}, f[3] = {i, j, k};
+        q[d] += (nq & 1) == 0 ? 1 : -1;
+        if (q[d] < 0 || q[d] >= n[d]) continue;
+        if ((nq & 1) == 0) f[d] += 1;
+        const long long fi = face_index(g, d, f[0], f[1], f[2]);
+        const float a = fa.area[d][fi];
+        double qv = 0.0;
+        if (a == 1.0f && dx_pow2) qv = (double)vel[d][fi] * inv_dx;  // u / dx, exact
+        else if (a != 0.0f) qv = fa.q[d][fi];
+        rhs += (nq & 1) == 0 ? -qv : qv;
+    }
+    return rhs;
+}
+__device__ __noinline__ double add_fp64(double a, double b) { return a + b; }
+__device__ __noinline__ double recip_fp64(double a) { return 1.0 / a; }
+
+// RC: a volume-correction constant is added to every unknown's b (a
+// template argument, so that no FP64 addition is issued predicated off)
+template <bool RC>
 __global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_faces_kernel(
     Grid g, double dt, double dx, FaceParams fp, double rhs_correct, const float *__restrict__ fluid,
     const float *__restrict__ u, const float *__restrict__ v, const float *__restrict__ w, FaceArrays fa,
@@ -612,30 +689,15 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_faces_kernel(
                     else if (ar[nq] != 0.0f) qexact = false;
                 }
                 if (unknown) {
-                    if (unit) {
-                        dg = pick7(fp.w_sum, nopen);
-                    } else {
-#pragma unroll
-                        for (int nq = 0; nq < 6; ++nq)
-                            if (has[nq] && fr[nq] > 0.0f) dg += wface(nq);
-                    }
+                    dg = unit ? pick7(fp.w_sum, nopen) : diag_fp64(g, fa, i, j, k, fp.w_unit);
                     // 0x15: the + faces' terms are negated
-                    if (!(qexact && exact_sum(terms, 6, 0x15u, fp.inv_dx_exp, rhs))) {
-                        rhs = 0.0;
-#pragma unroll
-                        for (int nq = 0; nq < 6; ++nq) {
-                            if (!has[nq]) continue;
-                            double q = 0.0;
-                            if (ar[nq] == 1.0f && fp.dx_pow2) q = div_dx((double)uv[nq], dx, fp);
-                            else if (ar[nq] != 0.0f) q = __ldg(fa.q[nq >> 1] + findex(nq));
-                            rhs += (nq & 1) == 0 ? -q : q;
-                        }
-                    }
+                    if (!(qexact && exact_sum(terms, 6, 0x15u, fp.inv_dx_exp, rhs)))
+                        rhs = rhs_fp64(g, fa, u, v, w, i, j, k, fp.dx_pow2, fp.inv_dx);
                 }
             }
             if (unknown) {
                 my_count++;
-                if (rhs_correct) rhs += rhs_correct;  // macpressuresolver3.cpp:212-214
+                if constexpr (RC) rhs = add_fp64(rhs, rhs_correct);  // macpressuresolver3.cpp:212-214
             } else {
                 dg = 0.0;
                 rhs = 0.0;
@@ -649,12 +711,12 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_faces_kernel(
             if (o.diag) {
                 const float d32 = d2f_rn(dg);
                 o.diag[c] = d32;
-                o.inv[c] = dg > 0.0 ? __frcp_rn(d32) : 0.0f;
+                o.inv[c] = positive_bits(dg) ? __frcp_rn(d32) : 0.0f;
                 o.cx[c] = d2f_rn(cpl[0]);
                 o.cy[c] = d2f_rn(cpl[1]);
                 if (g.dim == 3) o.cz[c] = d2f_rn(cpl[2]);
             }
-            if (o.inv64) o.inv64[c] = dg > 0.0 ? (unit ? pick7(fp.inv_sum, nopen) : 1.0 / dg) : 0.0;
+            if (o.inv64) o.inv64[c] = positive_bits(dg) ? (unit ? pick7(fp.inv_sum, nopen) : recip_fp64(dg)) : 0.0;
         }
     }
     unsigned long long wsum = my_count;
@@ -767,7 +829,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) active_sets_kernel(Grid g, Face
         const int pi[3] = {i, j, k};
         if (i < g.nx && j < g.ny && (g.dim == 2 || k < g.nz)) {
             const long long c = cell_index(g, i, j, k);
-            unknown[c] = __ldg(diag + c) != 0.0 ? 1 : 0;
+            unknown[c] = nonzero_bits(__ldg(diag + c)) ? 1 : 0;
         }
         for (int d = 0; d < g.dim; ++d) {
             bool exists = true;
@@ -852,7 +914,12 @@ cudaError_t launch_faces(const Grid &g, double dt, double dx, const SetupParams 
                          const float *fluid, const float *u, const float *v, const float *w, FaceArrays fa,
                          int grid_blocks, cudaStream_t stream) {
     const FaceParams fp = face_params(sp, dx, dt);
-    faces_kernel<<<node_blocks(g, grid_blocks), BLOCK_THREADS, 0, stream>>>(g, dt, dx, fp, solid, fluid, u, v, w, fa);
+    if (g.dim == 3)
+        faces_kernel<3><<<node_blocks(g, grid_blocks), BLOCK_THREADS, 0, stream>>>(g, dt, dx, fp, solid, fluid, u, v, w,
+                                                                                   fa);
+    else
+        faces_kernel<2><<<node_blocks(g, grid_blocks), BLOCK_THREADS, 0, stream>>>(g, dt, dx, fp, solid, fluid, u, v, w,
+                                                                                   fa);
     return cudaGetLastError();
 }
 
@@ -863,9 +930,14 @@ cudaError_t launch_assemble_faces(const Grid &g, double dt, double dx, const Set
     const FaceParams fp = face_params(sp, dx, dt);
     int blocks = (int)(g.ntiles < grid_blocks ? g.ntiles : grid_blocks);
     if (blocks < 1) blocks = 1;
-    assemble_faces_kernel<<<blocks, BLOCK_THREADS, 0, stream>>>(g, dt, dx, fp, sp.rhs_correct, fluid, u, v,
-                                                                g.dim == 3 ? w : v, fa, diag, cx, cy,
-                                                                g.dim == 3 ? cz : cy, b, o, sc);
+    if (sp.rhs_correct != 0.0)
+        assemble_faces_kernel<true><<<blocks, BLOCK_THREADS, 0, stream>>>(
+            g, dt, dx, fp, sp.rhs_correct, fluid, u, v, g.dim == 3 ? w : v, fa, diag, cx, cy, g.dim == 3 ? cz : cy, b, o,
+            sc);
+    else
+        assemble_faces_kernel<false><<<blocks, BLOCK_THREADS, 0, stream>>>(
+            g, dt, dx, fp, sp.rhs_correct, fluid, u, v, g.dim == 3 ? w : v, fa, diag, cx, cy, g.dim == 3 ? cz : cy, b, o,
+            sc);
     return cudaGetLastError();
 }
 
@@ -891,7 +963,8 @@ cudaError_t launch_pressure(const Grid &g, const double *diag, const double *x, 
     long long need = (g.ncell + BLOCK_THREADS - 1) / BLOCK_THREADS;
     int blocks = (int)(need < grid_blocks ? need : grid_blocks);
     if (blocks < 1) blocks = 1;
-    pressure_kernel<<<blocks, BLOCK_THREADS, 0, stream>>>(g, diag, x, prev, p, keep);
+    if (prev) pressure_kernel<true><<<blocks, BLOCK_THREADS, 0, stream>>>(g, diag, x, prev, p, keep);
+    else pressure_kernel<false><<<blocks, BLOCK_THREADS, 0, stream>>>(g, diag, x, prev, p, keep);
     return cudaGetLastError();
 }
 

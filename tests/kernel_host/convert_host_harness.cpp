@@ -9,3 +9,14 @@
 extern "C" void host_d2f(const double *in, float *out, long long n) {
     for (long long i = 0; i < n; ++i) out[i] = gbp::d2f_rn(in[i]);
 }
+
+extern "C" void host_f2d(const float *in, double *out, long long n) {
+    for (long long i = 0; i < n; ++i) out[i] = gbp::f2d_exact(in[i]);
+}
+
+extern "C" void host_bits_tests(const double *in, unsigned char *nonzero, unsigned char *positive, long long n) {
+    for (long long i = 0; i < n; ++i) {
+        nonzero[i] = gbp::nonzero_bits(in[i]) ? 1 : 0;
+        positive[i] = gbp::positive_bits(in[i]) ? 1 : 0;
+    }
+}

@@ -169,7 +169,9 @@ def test_kernel_code_matches_oracle_random(host, seed):
 
 def test_integer_double_to_float_conversion_is_exact(tmp_path):
     """gbp_convert.cuh's d2f_rn (double -> float from integer instructions,
-    used by kernels that narrow FP64 values) equals the hardware conversion
+    used by kernels that narrow FP64 values) and f2d_exact (float -> double)
+    equal the hardware conversions, and nonzero_bits / positive_bits the FP64
+    comparisons d != 0 and d > 0; d2f_rn equals the hardware conversion
     (round to nearest, ties to even) bit for bit: random doubles of every
     exponent, floats and the points halfway between neighbouring floats with
     the doubles on either side, the edges of the float range (largest
@@ -199,6 +201,25 @@ def test_integer_double_to_float_conversion_is_exact(tmp_path):
         want = x.astype(np.float32)
     same = (out.view(np.uint32) == want.view(np.uint32)) | (np.isnan(want) & np.isnan(out))
     assert same.all(), x[~same][:8]
+    # f2d_exact: float -> double from integer instructions equals the cast
+    lib.host_f2d.argtypes = [FP, ctypes.POINTER(ctypes.c_double), ctypes.c_longlong]
+    fl = np.concatenate([rng.integers(0, 1 << 32, 1 << 20, dtype=np.uint64).astype(np.uint32).view(np.float32),
+                         np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1e-45, -1e-40, 3.4e38], np.float32)])
+    fl = np.ascontiguousarray(fl)
+    d = np.zeros(fl.shape, np.float64)
+    lib.host_f2d(fl.ctypes.data_as(FP), d.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), fl.size)
+    wd = fl.astype(np.float64)
+    same = (d.view(np.uint64) == wd.view(np.uint64)) | (np.isnan(wd) & np.isnan(d))
+    assert same.all()
+    # the integer tests for d != 0 and d > 0
+    U8P = ctypes.POINTER(ctypes.c_ubyte)
+    lib.host_bits_tests.argtypes = [ctypes.POINTER(ctypes.c_double), U8P, U8P, ctypes.c_longlong]
+    nz = np.zeros(x.size, np.uint8)
+    po = np.zeros(x.size, np.uint8)
+    lib.host_bits_tests(x.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nz.ctypes.data_as(U8P),
+                        po.ctypes.data_as(U8P), x.size)
+    with np.errstate(invalid="ignore"):
+        assert np.array_equal(nz != 0, x != 0.0) and np.array_equal(po != 0, x > 0.0)
 
 
 def test_float_float_dot_error_bound(tmp_path):
