@@ -60,9 +60,14 @@ extern "C" {
 #define GBP_SOLVER_MGPCG 1
 
 /* Arithmetic. FP64: every vector and operator in double.
- * MIXED: FP64 outer iterative refinement (r = b - A x with the FP64
- * operator, FP64 x, FP64 norms and dot products) around an FP32 MGPCG inner
- * solve (FP32 stencil, smoother and transfers). The inner solve's dot
+ * MIXED: outer iterative refinement in FP64 storage (x and r in double,
+ * FP64 norms and stopping rule) around an FP32 MGPCG inner solve (FP32
+ * stencil, smoother and transfers). After each inner solve with correction
+ * d: x += d and r -= A d, the product with the FP64 operator formed in
+ * float pairs (each coupling as its float rounding plus the float of the
+ * remainder, 48 bits; products split exactly by FMA, TwoSum sums; within
+ * about 2^-47 |A||d|) and subtracted in FP64: three FP64 additions per cell
+ * instead of the eight FP64 operations of b - A x. The inner solve's dot
  * products and norms are not FP64 per term: each thread sums its n terms in
  * float-float (the product split exactly by an FMA, TwoSum, renormalised
  * after every term), within gamma_n^2 sum |a_i b_i| of the exact value
@@ -108,7 +113,9 @@ typedef struct gbp_stats {
     int outer_iterations;   /* refinement steps (1 unless MIXED) */
     int converged;          /* stopping rule met */
     double reresid;         /* |r|_inf / |b|_inf at exit, r the solver's residual (pcg_solver.h:292) */
-    double true_resid_inf;  /* |b - A x|_inf / |b|_inf recomputed in FP64 at exit */
+    double true_resid_inf;  /* |b - A x|_inf / |b|_inf at exit: recomputed in FP64, or for MIXED MGPCG the
+                               refinement's residual, updated r -= A d after each inner solve with float-pair
+                               products (within about 2^-47 |A||x| of the recomputed value) */
     double true_resid_l2;   /* |b - A x|_2 / |b|_2 */
     double b_inf;           /* |b|_inf of the system solved (after warm-start shift) */
     long long unknowns;     /* pressure unknowns (cells in the linear system) */

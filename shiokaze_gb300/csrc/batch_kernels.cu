@@ -15,9 +15,10 @@
 //
 // Algorithmic DRAM bytes per fine cell (s = sizeof(T)): presmooth 6 s,
 // sweep 7 s, restrict 6 s + s/8, post_black 7 s + s/8, red_dot 7 s,
-// direction 3 s, spmv 6 s, update 6 s, refine_accumulate 12 B (d f32 read,
-// x64 read+write), refine_residual 8+32+8+8+4 = 60 B (x64, operator, b, r64
-// write, r_f write).
+// direction 3 s, spmv 6 s, update 6 s; the mixed refinement after an inner
+// solve (refine_residual, refine_update_pair) 4 (d) + 32 (level-0 operator
+// and its low floats) + 8 + 8 (r64 read and write) + 4 (r_f) + 16 (x64 read
+// and write) = 72 B.
 #include <type_traits>
 
 #include "gbp_batch.h"
@@ -1529,114 +1530,93 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
 
 // ---- mixed precision: FP64 refinement -------------------------------------------------
 
-template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
-    refine_accumulate_kernel(const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
-                             const BScene<T> *__restrict__ scenes, const BatchCounters *cnt) {
-    // no scene has finished an inner solve in this iteration
-    if (*(const volatile int *)&cnt->refine <= 0) return;
-    __shared__ ItemCtx<T> ctx;
-    int cur = -1;
-    int sgc = 0;
-    for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        const BItem it = item_at(segs, nseg, w, sgc);
-        refresh(ctx, cur, it, levels, scenes, 2);
-        if (ctx.skip) continue;
-        const BLevel<T> L = ctx.L;  // registers: stores through generic pointers would force reloads from shared memory
-        const BScene<T> S = ctx.S;
-        with_vec(L.vec, [&](auto vt) {
-            constexpr bool V = decltype(vt)::value;
-            pair_tile(L.g, it, [&](int, int, int, long long c, bool second) {
-                const Pair<T> d2 = ld2<T, V>(S.x, c, second);
-                const Pair<double> o = ld2<double, V>(S.x64, c, second);
-                st2<double, V>(S.x64, c, Pair<double>{o.a + widen(d2.a), o.b + widen(d2.b)}, second);
-            });
-        });
-    }
-}
-
-// The refinement residual over two planes k, k+1 of a pair column (no
-// warm-start pressure, x64 present): every load of the two planes first,
-// then per cell diag x minus the neighbour terms in the order -x, +x, -y,
-// +y, -z, +z, as the plane-by-plane form computes them (the same FP64
-// operations in the same order). On this GPU the FP64 pipe issues about two
-// operations per clock per SM: the plane form waited on its loads between
-// short FP64 chains; here four independent chains (two cells, two planes)
-// have their operands ready.
-template <class T>
-__device__ __forceinline__ void refine_col2(const Grid &g, const BScene<T> &S, int i, int j, int k, long long c,
-                                            MaxSumAcc<T> &acc) {
-    const Operator<double> &A = S.A;
+// The mixed solver's refinement after an inner solve, without FP64
+// multiplications: with d the inner solve's correction (FP32) and A = hi +
+// lo the FP64 operator as level 0's FP32 operator plus the low floats
+// (within 2^-48 of each value),
+//   x64 += d,   r64 -= A d,
+// A d formed per cell in float-float: every product c d as hi*d split
+// exactly by an FMA plus lo*d, summed by TwoSum (about 2^-47 |A||d| from the
+// exact value), then subtracted from r64 in FP64. The result is the FP64
+// residual b - A x64 updated recursively (each update exact to about 2^-47
+// |A||d|, far below the refinement's 1e-6 of |b|), and costs three FP64
+// additions per cell where recomputing b - A x64 costs eight FP64
+// operations (this GPU's FP64 pipe issues about two per clock per SM).
+// Order of the sum: the diagonal, then -x, +x, -y, +y, -z, +z.
+template <class T, bool V>
+__device__ __forceinline__ void refine_update_pair(const Grid &g, const BLevel<T> &L, const BScene<T> &S, int i, int j,
+                                                   int k, long long c, bool second, MaxSumAcc<T> &acc) {
     const long long sy = g.nx, sz = (long long)g.nx * g.ny;
-    const Pair<double> zero{0.0, 0.0};
-    const double *x = S.x64;
-    Pair<double> xc[2], xym[2], xyp[2], dg[2], cxp[2], cym[2], cyp[2], bb[2];
-    double xm[2], xp[2], cxm[2];
-    const Pair<double> xlo = k > 0 ? ld2<double, true>(x, c - sz, true) : zero;
-    const Pair<double> xhi = k + 2 < g.nz ? ld2<double, true>(x, c + 2 * sz, true) : zero;
-    const Pair<double> czl = k > 0 ? ld2<double, true>(A.cz, c - sz, true) : zero;
-    const Pair<double> czc = ld2<double, true>(A.cz, c, true);
-    const Pair<double> czh = k + 2 < g.nz ? ld2<double, true>(A.cz, c + sz, true) : zero;
-#pragma unroll
-    for (int z = 0; z < 2; ++z) {
-        const long long cz_ = c + z * sz;
-        xc[z] = ld2<double, true>(x, cz_, true);
-        xym[z] = j > 0 ? ld2<double, true>(x, cz_ - sy, true) : zero;
-        xyp[z] = j + 1 < g.ny ? ld2<double, true>(x, cz_ + sy, true) : zero;
-        xm[z] = i > 0 ? __ldg(x + cz_ - 1) : 0.0;
-        xp[z] = i + 2 < g.nx ? __ldg(x + cz_ + 2) : 0.0;
-        dg[z] = ld2<double, true>(A.diag, cz_, true);
-        cxp[z] = ld2<double, true>(A.cx, cz_, true);
-        cxm[z] = i > 0 ? __ldg(A.cx + cz_ - 1) : 0.0;
-        cym[z] = j > 0 ? ld2<double, true>(A.cy, cz_ - sy, true) : zero;
-        cyp[z] = j + 1 < g.ny ? ld2<double, true>(A.cy, cz_, true) : zero;
-        bb[z] = ld2<double, true>(S.b, cz_, true);
-    }
-#pragma unroll
-    for (int z = 0; z < 2; ++z) {
-        const int kz = k + z;
-        const Pair<double> xzm = z == 0 ? xlo : xc[0], xzp = z == 0 ? xc[1] : xhi;
-        const Pair<double> czm = z == 0 ? czl : czc, czp = z == 0 ? czc : czh;
-        double a0 = dg[z].a * xc[z].a, a1 = dg[z].b * xc[z].b;
-        if (i > 0) a0 -= cxm[z] * xm[z];
-        a0 -= cxp[z].a * xc[z].b;
-        a1 -= cxp[z].a * xc[z].a;
-        if (i + 2 < g.nx) a1 -= cxp[z].b * xp[z];
-        if (j > 0) {
-            a0 -= cym[z].a * xym[z].a;
-            a1 -= cym[z].b * xym[z].b;
+    const Pair<float> zero{0.0f, 0.0f};
+    const float *d = reinterpret_cast<const float *>(S.x);
+    const float *dh = reinterpret_cast<const float *>(L.diag), *xh = reinterpret_cast<const float *>(L.cx),
+                *yh = reinterpret_cast<const float *>(L.cy), *zh = reinterpret_cast<const float *>(L.cz);
+    // every load of the pair first
+    const Pair<float> dc = ld2<float, V>(d, c, second);
+    const float dxm = i > 0 ? __ldg(d + c - 1) : 0.0f, dxp = (second && i + 2 < g.nx) ? __ldg(d + c + 2) : 0.0f;
+    const Pair<float> dym = j > 0 ? ld2<float, V>(d, c - sy, second) : zero;
+    const Pair<float> dyp = j + 1 < g.ny ? ld2<float, V>(d, c + sy, second) : zero;
+    const bool z3 = g.dim == 3;
+    const Pair<float> dzm = z3 && k > 0 ? ld2<float, V>(d, c - sz, second) : zero;
+    const Pair<float> dzp = z3 && k + 1 < g.nz ? ld2<float, V>(d, c + sz, second) : zero;
+    const Pair<float> ddh = ld2<float, V>(dh, c, second), ddl = ld2<float, V>(S.lo.diag, c, second);
+    const Pair<float> cxh = ld2<float, V>(xh, c, second), cxl = ld2<float, V>(S.lo.cx, c, second);
+    const float cxmh = i > 0 ? __ldg(xh + c - 1) : 0.0f, cxml = i > 0 ? __ldg(S.lo.cx + c - 1) : 0.0f;
+    const Pair<float> cymh = j > 0 ? ld2<float, V>(yh, c - sy, second) : zero;
+    const Pair<float> cyml = j > 0 ? ld2<float, V>(S.lo.cy, c - sy, second) : zero;
+    const Pair<float> cyph = j + 1 < g.ny ? ld2<float, V>(yh, c, second) : zero;
+    const Pair<float> cypl = j + 1 < g.ny ? ld2<float, V>(S.lo.cy, c, second) : zero;
+    const Pair<float> czmh = z3 && k > 0 ? ld2<float, V>(zh, c - sz, second) : zero;
+    const Pair<float> czml = z3 && k > 0 ? ld2<float, V>(S.lo.cz, c - sz, second) : zero;
+    const Pair<float> czph = z3 && k + 1 < g.nz ? ld2<float, V>(zh, c, second) : zero;
+    const Pair<float> czpl = z3 && k + 1 < g.nz ? ld2<float, V>(S.lo.cz, c, second) : zero;
+    const Pair<double> r0 = ld2<double, V>(S.r64, c, second), x0 = ld2<double, V>(S.x64, c, second);
+    // c d into the accumulator, negated for the neighbour terms
+    auto mac = [](FloatFloat &a, float ch, float cl, float dv, bool neg) {
+        float p = __fmul_rn(ch, dv);
+        float e = __fadd_rn(__fmaf_rn(ch, dv, -p), __fmul_rn(cl, dv));
+        if (neg) {
+            p = -p;
+            e = -e;
         }
-        if (j + 1 < g.ny) {
-            a0 -= cyp[z].a * xyp[z].a;
-            a1 -= cyp[z].b * xyp[z].b;
-        }
-        if (kz > 0) {
-            a0 -= czm.a * xzm.a;
-            a1 -= czm.b * xzm.b;
-        }
-        if (kz + 1 < g.nz) {
-            a0 -= czp.a * xzp.a;
-            a1 -= czp.b * xzp.b;
-        }
-        const Pair<double> rv{bb[z].a - a0, bb[z].b - a1};
-        const Pair<T> rt{narrow_to<T>(rv.a), narrow_to<T>(rv.b)};
-        st2<double, true>(S.r64, c + z * sz, rv, true);
-        st2<T, true>(S.r, c + z * sz, rt, true);
-        acc.add(rv.a, rt.a);
-        acc.add(rv.b, rt.b);
-    }
+        a.add(p);
+        a.add(e);
+    };
+    FloatFloat t0, t1;
+    mac(t0, ddh.a, ddl.a, dc.a, false);
+    mac(t1, ddh.b, ddl.b, dc.b, false);
+    // x: cell a's -x face (coupling at c - 1), its +x face shared with b
+    // (coupling at c), b's +x face (coupling at c + 1)
+    mac(t0, cxmh, cxml, dxm, true);
+    mac(t0, cxh.a, cxl.a, dc.b, true);
+    mac(t1, cxh.a, cxl.a, dc.a, true);
+    mac(t1, cxh.b, cxl.b, dxp, true);
+    mac(t0, cymh.a, cyml.a, dym.a, true);
+    mac(t1, cymh.b, cyml.b, dym.b, true);
+    mac(t0, cyph.a, cypl.a, dyp.a, true);
+    mac(t1, cyph.b, cypl.b, dyp.b, true);
+    mac(t0, czmh.a, czml.a, dzm.a, true);
+    mac(t1, czmh.b, czml.b, dzm.b, true);
+    mac(t0, czph.a, czpl.a, dzp.a, true);
+    mac(t1, czph.b, czpl.b, dzp.b, true);
+    // r -= A d and x += d: three FP64 additions per cell
+    const Pair<double> rv{r0.a - (widen(t0.hi) + widen(t0.lo)), r0.b - (widen(t1.hi) + widen(t1.lo))};
+    const Pair<T> rt{narrow_to<T>(rv.a), narrow_to<T>(rv.b)};
+    st2<double, V>(S.r64, c, rv, second);
+    st2<T, V>(S.r, c, rt, second);
+    st2<double, V>(S.x64, c, Pair<double>{x0.a + widen(dc.a), x0.b + widen(dc.b)}, second);
+    acc.add(rv.a, rt.a);
+    if (second) acc.add(rv.b, rt.b);
 }
 
-// r64 = b - A64 (prev + x64) (x64 absent: initial), r_T = r64, |r64|_inf
-// and |r64|_2; the scene's last flush applies the stopping rule and opens
-// the next inner solve. initial: sets the threshold, zeroes x64, and keeps
-// |b - A prev|_2 (with no warm start that is b itself, and the stencil is
-// skipped). The last pass's norms are the true residual of the returned
-// solution. Each cell's residual is accumulated as diag X minus the
-// neighbour terms one by one (-x, +x, -y, +y, -z, +z), in FP64.
+// The mixed solver's outer step. initial: r64 = b - A64 prev (FP64; the
+// stencil skipped without a warm start, r64 = b), x64 = 0, the threshold,
+// |b - A prev|_2 kept. After an inner solve: x64 += d, r64 -= A d
+// (refine_update_pair). Either way r_T = r64 for the next inner solve,
+// |r64|_inf and |r64|_2, and the scene's last flush applies the stopping rule
+// and opens the next inner solve; the last pass's norms are those of the
+// returned solution's residual.
 template <class T>
-// Two blocks per SM: the FP64 pipe, not occupancy, bounds this kernel, and
-// the gather-first column needs the registers.
 __global__ void __launch_bounds__(BLOCK_THREADS, 2) refine_residual_kernel(
     const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
     const BScene<T> *__restrict__ scenes, double *part, int initial, double residual, int max_iter,
@@ -1682,50 +1662,11 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 2) refine_residual_kernel(
                     return v;
                 };
                 const bool zero_x = initial && S.prev == nullptr;  // r = b exactly
-                if constexpr (V) {
-                    if (!initial && S.prev == nullptr && it.ntiles == 1 && g.tz == 4) {
-                        // 4-plane tiles: two gather-first pairs of planes
-                        pair_tile_z4(g, it, [&](int i, int j, int k0, long long c0) {
-                            refine_col2<T>(g, S, i, j, k0, c0, acc);
-                            refine_col2<T>(g, S, i, j, k0 + 2, c0 + 2 * sz, acc);
-                        }, [&](int i, int j, int k, long long c, bool second) {
-                            // a partial last tile: the plane form below
-                            const Pair<double> xc = X2(c, second), dg = ld2<double, V>(A.diag, c, second);
-                            const Pair<double> cxp = ld2<double, V>(A.cx, c, second);
-                            double a0 = dg.a * xc.a, a1 = dg.b * xc.b;
-                            if (i > 0) a0 -= __ldg(A.cx + c - 1) * X1(c - 1);
-                            if (second) {
-                                a0 -= cxp.a * xc.b;
-                                a1 -= cxp.a * xc.a;
-                                if (i + 2 < g.nx) a1 -= cxp.b * X1(c + 2);
-                            }
-                            if (j > 0) {
-                                const Pair<double> w = ld2<double, V>(A.cy, c - sy, second), v = X2(c - sy, second);
-                                a0 -= w.a * v.a;
-                                a1 -= w.b * v.b;
-                            }
-                            if (j + 1 < g.ny) {
-                                const Pair<double> w = ld2<double, V>(A.cy, c, second), v = X2(c + sy, second);
-                                a0 -= w.a * v.a;
-                                a1 -= w.b * v.b;
-                            }
-                            if (k > 0) {
-                                const Pair<double> w = ld2<double, V>(A.cz, c - sz, second), v = X2(c - sz, second);
-                                a0 -= w.a * v.a;
-                                a1 -= w.b * v.b;
-                            }
-                            if (k + 1 < g.nz) {
-                                const Pair<double> w = ld2<double, V>(A.cz, c, second), v = X2(c + sz, second);
-                                a0 -= w.a * v.a;
-                                a1 -= w.b * v.b;
-                            }
-                            const Pair<double> bb = ld2<double, V>(S.b, c, second);
-                            const Pair<double> rv{bb.a - a0, bb.b - a1};
-                            const Pair<T> rt{narrow_to<T>(rv.a), narrow_to<T>(rv.b)};
-                            st2<double, V>(S.r64, c, rv, second);
-                            st2<T, V>(S.r, c, rt, second);
-                            acc.add(rv.a, rt.a);
-                            if (second) acc.add(rv.b, rt.b);
+                if constexpr (sizeof(T) == 4) {
+                    if (!initial && S.lo.diag != nullptr) {
+                        // after an inner solve: x64 += d and r64 -= A d
+                        pair_tile(g, it, [&](int i, int j, int k, long long c, bool second) {
+                            refine_update_pair<T, V>(g, L, S, i, j, k, c, second, acc);
                         });
                         return;
                     }
@@ -2349,12 +2290,6 @@ cudaError_t b_update(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs
     return cudaGetLastError();
 }
 template <class T>
-cudaError_t b_refine_accumulate(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
-                                const BScene<T> *scenes) {
-    refine_accumulate_kernel<T><<<L.blocks, BLOCK_THREADS, 0, L.stream>>>(levels, segs, nseg, n, scenes, L.cnt);
-    return cudaGetLastError();
-}
-template <class T>
 cudaError_t b_refine_residual(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                               const BScene<T> *scenes, double *part, int initial, double residual, int max_iter,
                               double inner_rel, int inner_max, BatchCounters *cnt) {
@@ -2386,8 +2321,6 @@ cudaError_t b_refine_residual(const BLaunch &L, const BLevel<T> *levels, const B
                                    double *);                                                                        \
     template cudaError_t b_update<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int, const BScene<T> *, \
                                      double *, int, BatchCounters *);                                                \
-    template cudaError_t b_refine_accumulate<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,         \
-                                                const BScene<T> *);                                                  \
     template cudaError_t b_refine_residual<T>(const BLaunch &, const BLevel<T> *, const BSeg *, int, int,           \
                                               const BScene<T> *, double *, int, double, int, double, int,            \
                                               BatchCounters *);

@@ -515,11 +515,10 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
     *nodes += 3;
     if (mixed_ && e == cudaSuccess) {
         const BLaunch L2{blocks_for(n_fine_pairs_, grid_blocks_), st, 2, d_scene_of_, d_counters_};
-        e = b_refine_accumulate<T>(L2, lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc);
-        if (e == cudaSuccess)
-            e = b_refine_residual<T>(L2, lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_, 0, p.residual,
-                                     p.max_iterations, inner_rel_, kInnerMax, d_counters_);
-        *nodes += 2;
+        // x64 += d, r64 -= A d and the outer stopping rule, in one pass
+        e = b_refine_residual<T>(L2, lv, d_fine_pairs_, s_fine_pairs_, n_fine_pairs_, sc, d_part_, 0, p.residual,
+                                 p.max_iterations, inner_rel_, kInnerMax, d_counters_);
+        *nodes += 1;
     }
     return e;
 }

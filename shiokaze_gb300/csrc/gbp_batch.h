@@ -67,6 +67,10 @@ template <class T> struct BScene {
     T *x, *r, *z, *p, *q;  // PCG vectors (x: the correction in FP64 mode, d in mixed mode)
     // FP64 operator and refinement state
     Operator<double> A;
+    // FP32 solver: the low floats of A against level 0's operator (A =
+    // level 0 + lo within 2^-48), for the refinement's float-pair products;
+    // null pointers otherwise
+    Operator<float> lo;
     const double *b, *prev;
     double *x64, *r64;
     Scalars *sc;
@@ -324,9 +328,6 @@ cudaError_t b_spmv(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, 
 template <class T>
 cudaError_t b_update(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n, const BScene<T> *scenes,
                      double *part, int mode, BatchCounters *cnt);
-template <class T>
-cudaError_t b_refine_accumulate(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
-                                const BScene<T> *scenes);
 template <class T>
 cudaError_t b_refine_residual(const BLaunch &L, const BLevel<T> *levels, const BSeg *segs, int nseg, int n,
                               const BScene<T> *scenes, double *part, int initial, double residual, int max_iter,

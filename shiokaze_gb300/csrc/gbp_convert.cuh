@@ -62,6 +62,18 @@ __host__ __device__ __forceinline__ double f2d_hw(float f) {
 #endif
 }
 
+#ifdef __CUDA_ARCH__
+// the hardware form of split_lo (volatile: never issued speculatively)
+__device__ __forceinline__ float split_lo_hw(double c, float hi) {
+    double h, dlo;
+    float r;
+    asm volatile("cvt.f64.f32 %0, %1;" : "=d"(h) : "f"(hi));
+    asm volatile("sub.rn.f64 %0, %1, %2;" : "=d"(dlo) : "d"(c), "d"(h));
+    asm volatile("cvt.rn.f32.f64 %0, %1;" : "=f"(r) : "d"(dlo));
+    return r;
+}
+#endif
+
 __host__ __device__ __forceinline__ float d2f_rn(double d) {
     const unsigned long long b = d2f_bits_of(d);
     const int e32 = (int)((b >> 52) & 0x7ffu) - 1023 + 127;
@@ -110,6 +122,58 @@ __host__ __device__ __forceinline__ double f2d_exact(float f) {
 #endif
     }
     return f2d_hw(f);
+}
+
+// The low part of a double c against its float rounding hi = d2f_rn(c):
+// (float)(c - (double)hi), the exact difference (at most 29 significant
+// bits) rounded to nearest even, from integer instructions. c == hi + lo
+// within 2^-48 |c|: a float pair carries c to about 48 bits. Operands whose
+// parts leave the normal float range take the hardware path.
+__host__ __device__ __forceinline__ float split_lo(double c, float hi) {
+    const unsigned long long b = d2f_bits_of(c);
+    const int ec = (int)((b >> 52) & 0x7ffu);  // biased
+#ifdef __CUDA_ARCH__
+    const unsigned hb = __float_as_uint(hi);
+#else
+    unsigned hb;
+    std::memcpy(&hb, &hi, sizeof hb);
+#endif
+    const int eh = (int)((hb >> 23) & 0xffu);  // biased
+    // c and hi normal; the low part's exponent stays normal for |c| >= 2^-97
+    if (ec >= 1023 - 97 && ec <= 1023 + 127 && eh >= 1 && eh <= 254) {
+        const long long mc = (long long)((b & 0xfffffffffffffull) | (1ull << 52));  // c = mc 2^(ec-1075)
+        const int sh = (eh - 127 - 23) - (ec - 1075);                                  // 29, or 30 on a carry
+        const long long mh = (long long)((hb & 0x7fffffu) | 0x800000u) << sh;          // hi in the same unit
+        long long r = mc - mh;  // |c| - |hi| in units of 2^(ec-1075), |r| <= 2^28
+        if (r == 0) return d2f_from_bits(0u);
+        const unsigned sign = ((unsigned)(b >> 32) & 0x80000000u) ^ (r < 0 ? 0x80000000u : 0u);
+        unsigned long long a = (unsigned long long)(r < 0 ? -r : r);
+#ifdef __CUDA_ARCH__
+        const int len = 64 - __clzll((long long)a);  // bit length (at most 29)
+#else
+        const int len = 64 - __builtin_clzll(a);
+#endif
+        int e = ec - 1075 + len - 1;                // unbiased exponent of |r| 2^(ec-1075)
+        unsigned long long m;
+        if (len <= 24) {
+            m = a << (24 - len);
+        } else {
+            const int drop = len - 24;
+            const unsigned long long rem = a & ((1ull << drop) - 1), half = 1ull << (drop - 1);
+            m = a >> drop;
+            m += (rem > half || (rem == half && (m & 1ull))) ? 1ull : 0ull;
+            if (m >> 24) {
+                m >>= 1;
+                e += 1;
+            }
+        }
+        if (e >= -126 && e <= 127) return d2f_from_bits(sign | ((unsigned)(e + 127) << 23) | ((unsigned)m & 0x7fffffu));
+    }
+#ifdef __CUDA_ARCH__
+    return split_lo_hw(c, hi);
+#else
+    return (float)(c - (double)hi);
+#endif
 }
 
 // d != 0.0 and d > 0.0 from the bit pattern (no FP64 comparison; a NaN is

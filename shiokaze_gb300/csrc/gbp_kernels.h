@@ -36,6 +36,9 @@ struct FaceArrays {
 // diagonal, or the FP64 hierarchy's inverse diagonal (unused ones null).
 struct Level0Out {
     float *diag, *inv, *cx, *cy, *cz;
+    // the low floats of the FP64 operator against diag, cx, cy, cz (each
+    // FP64 value = high + low within 2^-48): the mixed refinement's products
+    float *diag_lo, *cx_lo, *cy_lo, *cz_lo;
     double *inv64;
 };
 

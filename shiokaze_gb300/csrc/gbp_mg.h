@@ -46,6 +46,10 @@ template <class T> struct MgHierarchy {
     int tail = 0;
     size_t tail_bytes = 0;
     bool fine_aliases_fp64 = false;  // level 0 operator is the FP64 assembly itself
+    // FP32 hierarchy: the low floats of the FP64 operator against level 0's
+    // diag, cx, cy, cz (the mixed refinement's float-pair products); null
+    // for the FP64 hierarchy
+    T *lo[4] = {nullptr, nullptr, nullptr, nullptr};
     MgLevel<T> levels[MG_MAX_LEVELS];
 };
 

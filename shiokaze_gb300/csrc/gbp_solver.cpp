@@ -60,7 +60,7 @@ size_t solver_device_bytes(const Grid &g, const gbp_params &p) {
         const size_t s = p.precision == GBP_PRECISION_MIXED ? 4 : 8;
         std::vector<Grid> lv = mg_level_grids(g, coarsest_of(p));
         // level 0: inverse diagonal (+ operator copy and 5 vectors in FP32)
-        bytes += s * cells * (p.precision == GBP_PRECISION_MIXED ? 10 : 1);
+        bytes += s * cells * (p.precision == GBP_PRECISION_MIXED ? 14 : 1);  // mixed: + the operator's low floats
         for (size_t l = 1; l < lv.size(); ++l) bytes += s * (size_t)lv[l].ncell * 7;
         // tile classes (a value per tile; rounded up to whole allocations)
         for (size_t l = 0; l + 1 < lv.size(); ++l)
@@ -184,6 +184,8 @@ int Solver::prepare_mg(const Grid &g, const gbp_params &p) {
             }
             H.levels[l] = MgLevel<float>{lv[l], d, iv, x1, y1, lv[l].dim == 3 ? z1 : y1, b, x};
         }
+        for (int q = 0; q < 4; ++q)
+            if ((rc = alloc(&H.lo[q], n))) return rc;
         if ((rc = alloc_classes(H))) return rc;
         mg_plan_tail(H);
         mg32_ready_ = true;
@@ -244,9 +246,9 @@ int Solver::solve(const Grid &g, const gbp_params &p, int grid_blocks, cudaStrea
 
 int Solver::complete(const Grid &g, const gbp_params &p, int grid_blocks, cudaStream_t stream, long long *launches) {
     const bool warm = p.warm_start && st_.have_prev;
-    // A mixed MGPCG solve that stopped on its FP64 refinement check has the
-    // true residual of its solution already (that check computes it); every
-    // other solve gets a separate FP64 pass.
+    // A mixed MGPCG solve that stopped on its refinement check has the
+    // residual of its solution already (that check updates it, see
+    // refine_update_pair); every other solve gets a separate FP64 pass.
     const bool have_true = p.solver == GBP_SOLVER_MGPCG && p.precision == GBP_PRECISION_MIXED &&
                            (st_.host_sc->status == 1 || st_.host_sc->status == 2);
     if (!have_true) {
@@ -303,6 +305,10 @@ Level0Out Solver::level0_out(const gbp_params &p) const {
         o.cx = const_cast<float *>(L.cx);
         o.cy = const_cast<float *>(L.cy);
         o.cz = const_cast<float *>(L.cz);
+        o.diag_lo = h32_.lo[0];
+        o.cx_lo = h32_.lo[1];
+        o.cy_lo = h32_.lo[2];
+        o.cz_lo = h32_.lo[3];
     } else if (p.precision == GBP_PRECISION_FP64 && mg64_ready_) {
         o.inv64 = const_cast<double *>(h64_.levels[0].inv);
     }
@@ -345,6 +351,8 @@ template <class T> void Solver::add_to_plan(BatchPlan<T> &plan, const gbp_params
         sc.q = reinterpret_cast<T *>(st_.q);
     }
     sc.A = Operator<double>{st_.diag, st_.cx, st_.cy, sc.g.dim == 3 ? st_.cz : st_.cy};
+    if (sizeof(T) == 4)
+        sc.lo = Operator<float>{h32_.lo[0], h32_.lo[1], h32_.lo[2], sc.g.dim == 3 ? h32_.lo[3] : h32_.lo[2]};
     sc.b = st_.b;
     sc.prev = warm ? st_.prev : nullptr;
     sc.x64 = st_.x;
@@ -379,6 +387,9 @@ template <class T> void Solver::add_to_plan(BatchPlan<T> &plan, const gbp_params
                                     (const void *)sc.A.cz, (const void *)sc.b, (const void *)sc.prev,
                                     (const void *)sc.x64, (const void *)sc.r64})
                 vec = vec && al(ptr, 2 * sizeof(double));
+            for (const void *ptr : {(const void *)sc.lo.diag, (const void *)sc.lo.cx, (const void *)sc.lo.cy,
+                                    (const void *)sc.lo.cz})
+                vec = vec && al(ptr, 2 * sizeof(float));
         }
         if (l == 0) plan.fine_ref.push_back((int)plan.levels.size());
         plan.levels.push_back(

@@ -104,15 +104,23 @@ __device__ __forceinline__ T neighbour_sum(const MgLevel<T> &L, int i, int j, in
 // Level 0 in T from the FP64 assembly, and the inverse diagonal.
 template <class T>
 __global__ void __launch_bounds__(BLOCK_THREADS, 6) mg_fine_setup_kernel(Grid g, Operator<double> A, T *diag, T *inv,
-                                                                      T *cx, T *cy, T *cz, bool copy) {
+                                                                      T *cx, T *cy, T *cz, bool copy, T *lo0, T *lo1,
+                                                                      T *lo2, T *lo3) {
     for_each_cell(g, [&](int i, int j, int k, long long c) {
         const double d = A.diag[c];
-        inv[c] = d > 0.0 ? recip<T>(d) : T(0);
+        inv[c] = positive_bits(d) ? recip<T>(d) : T(0);
         if (copy) {
-            diag[c] = narrow<T>(d);
-            cx[c] = narrow<T>(A.cx[c]);
-            cy[c] = narrow<T>(A.cy[c]);
-            if (g.dim == 3) cz[c] = narrow<T>(A.cz[c]);
+            const double v[4] = {d, A.cx[c], A.cy[c], g.dim == 3 ? A.cz[c] : 0.0};
+            T *hi[4] = {diag, cx, cy, cz};
+            T *lo[4] = {lo0, lo1, lo2, lo3};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (q == 3 && g.dim != 3) break;
+                const T h = narrow<T>(v[q]);
+                hi[q][c] = h;
+                if constexpr (sizeof(T) == 4)
+                    if (lo0) lo[q][c] = split_lo(v[q], h);
+            }
         }
     });
 }
@@ -310,7 +318,7 @@ cudaError_t mg_setup(const Grid &g0, Operator<double> A, const MgHierarchy<T> &H
     if (!level0_done)
         mg_fine_setup_kernel<T><<<nblocks<T>(g0, grid_blocks), BLOCK_THREADS, 0, stream>>>(
             g0, A, const_cast<T *>(L0.diag), const_cast<T *>(L0.inv), const_cast<T *>(L0.cx), const_cast<T *>(L0.cy),
-            const_cast<T *>(L0.cz), copy);
+            const_cast<T *>(L0.cz), copy, H.lo[0], H.lo[1], H.lo[2], H.lo[3]);
     for (int l = 0; l + 1 < H.nlevels; ++l) {
         const MgLevel<T> &F = H.levels[l], &C = H.levels[l + 1];
         mg_coarsen_kernel<T><<<nblocks<T>(C.g, grid_blocks), BLOCK_THREADS, 0, stream>>>(

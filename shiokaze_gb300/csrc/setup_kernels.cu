@@ -709,12 +709,21 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_faces_kernel(
             for (int d = 0; d < 3; ++d)
                 if (d < g.dim) cp[d][c] = cpl[d];
             if (o.diag) {
-                const float d32 = d2f_rn(dg);
+                const float d32 = d2f_rn(dg), x32 = d2f_rn(cpl[0]), y32 = d2f_rn(cpl[1]);
                 o.diag[c] = d32;
                 o.inv[c] = positive_bits(dg) ? __frcp_rn(d32) : 0.0f;
-                o.cx[c] = d2f_rn(cpl[0]);
-                o.cy[c] = d2f_rn(cpl[1]);
-                if (g.dim == 3) o.cz[c] = d2f_rn(cpl[2]);
+                o.cx[c] = x32;
+                o.cy[c] = y32;
+                if (o.diag_lo) {
+                    o.diag_lo[c] = split_lo(dg, d32);
+                    o.cx_lo[c] = split_lo(cpl[0], x32);
+                    o.cy_lo[c] = split_lo(cpl[1], y32);
+                }
+                if (g.dim == 3) {
+                    const float z32 = d2f_rn(cpl[2]);
+                    o.cz[c] = z32;
+                    if (o.diag_lo) o.cz_lo[c] = split_lo(cpl[2], z32);
+                }
             }
             if (o.inv64) o.inv64[c] = positive_bits(dg) ? (unit ? pick7(fp.inv_sum, nopen) : recip_fp64(dg)) : 0.0;
         }

@@ -20,3 +20,10 @@ extern "C" void host_bits_tests(const double *in, unsigned char *nonzero, unsign
         positive[i] = gbp::positive_bits(in[i]) ? 1 : 0;
     }
 }
+
+extern "C" void host_split(const double *in, float *hi, float *lo, long long n) {
+    for (long long i = 0; i < n; ++i) {
+        hi[i] = gbp::d2f_rn(in[i]);
+        lo[i] = gbp::split_lo(in[i], hi[i]);
+    }
+}

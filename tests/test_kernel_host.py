@@ -220,6 +220,21 @@ def test_integer_double_to_float_conversion_is_exact(tmp_path):
                         po.ctypes.data_as(U8P), x.size)
     with np.errstate(invalid="ignore"):
         assert np.array_equal(nz != 0, x != 0.0) and np.array_equal(po != 0, x > 0.0)
+    # split_lo: the low float of a double against its float rounding
+    lib.host_split.argtypes = [ctypes.POINTER(ctypes.c_double), FP, FP, ctypes.c_longlong]
+    fin = np.isfinite(x) & (np.abs(x) < 3.0e38)
+    xs = np.ascontiguousarray(np.concatenate([x[fin], rng.standard_normal(1 << 18) * np.exp2(rng.integers(-60, 60, 1 << 18)),
+                                              (fd * (1 + 2.0 ** -30)), 1.0 / 3.0 * np.exp2(np.arange(-90, 90.0))]))
+    hi = np.zeros(xs.size, np.float32)
+    lo = np.zeros(xs.size, np.float32)
+    lib.host_split(xs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), hi.ctypes.data_as(FP), lo.ctypes.data_as(FP),
+                   xs.size)
+    with np.errstate(over="ignore", under="ignore", invalid="ignore"):
+        want = (xs - hi.astype(np.float64)).astype(np.float32)
+    ok = (lo.view(np.uint32) == want.view(np.uint32)) | (np.isnan(want) & np.isnan(lo))
+    assert ok.all(), (xs[~ok][:4], lo[~ok][:4], want[~ok][:4])
+    rel = np.abs(hi.astype(np.float64) + lo.astype(np.float64) - xs)[np.abs(xs) > 1e-30]
+    assert (rel <= 2.0 ** -47 * np.abs(xs[np.abs(xs) > 1e-30])).all()
 
 
 def test_float_float_dot_error_bound(tmp_path):
