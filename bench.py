@@ -736,6 +736,35 @@ def run_gbp_advect(args):
     util = gb.MacUtility3(scene.nx, scene.ny, scene.nz, scene.dx, context=ctx)
     constrain_ms = timed(lambda: util.constrain_velocity(solid, (u, v, w), stream=sh))
     cell_ms = timed(lambda: adv.advect_scalar(q, (u, v, w), fluid, scene.dt, stream=sh))
+    # velocity extrapolation (array_extrapolator3, 3 rounds) of the u
+    # component from the faces inside a ball of radius 0.3 (a liquid's
+    # narrow-band velocity), restored from a saved copy before each round of
+    # timing; only the extrapolation is between the events
+    zc, yc, xc = np.meshgrid(*(np.arange(m) for m in scene.u.shape), indexing="ij")
+    ball = (((xc * scene.dx - 0.5) ** 2 + ((yc + 0.5) * scene.dx - 0.5) ** 2 + ((zc + 0.5) * scene.dx - 0.5) ** 2)
+            < 0.3 ** 2)
+    m0 = dev_t(ball.astype(np.uint8))
+    e0 = dev_t(np.where(ball, scene.u, 0.0).astype(np.float32))
+    ev_, em_ = e0.clone(), m0.clone()
+    ext_ms, ext_added = [], 0
+    for r in range(6):
+        ev_.copy_(e0)
+        em_.copy_(m0)
+        a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a_.record(stream)
+        ext_added = util.extrapolate(ev_, em_, 3, stream=sh)
+        b_.record(stream)
+        torch.cuda.synchronize()
+        if r:
+            ext_ms.append(a_.elapsed_time(b_))
+    # the 2D step (macadvection2: velocity and density) on a 2048^2 smoke scene
+    from shiokaze_gb300 import scenes
+    sc2 = scenes.smoke2(2048, seed=3)
+    u2, v2, f2 = dev_t(sc2.u), dev_t(sc2.v), dev_t(sc2.fluid)
+    q2 = dev_t(np.random.default_rng(6).random(sc2.fluid.shape, dtype=np.float32))
+    adv2 = gb.MacAdvection2(sc2.nx, sc2.ny, sc2.dx, context=ctx)
+    advect2_ms = timed(lambda: adv2.advect_step((u2, v2), f2, sc2.dt, scalar=q2, stream=sh))
     faces = scene.u.size + scene.v.size + scene.w.size
     face_bytes_alg = (4 + 4 / 3 + 12 + 20) * faces
     cell_bytes_alg = 64.0 * scene.cells
@@ -768,6 +797,10 @@ def run_gbp_advect(args):
                                                  "GBps": round(cell_bytes_alg / (cell_ms * 1e-3) / 1e9, 1)}},
                      "step_GBps": round(nbytes / (ms_step * 1e-3) / 1e9, 1)},
         "constrain_velocity_ms": round(constrain_ms, 4),
+        "extrapolate": {"ms": round(float(np.median(ext_ms)), 4), "rounds": 3, "activated": int(ext_added),
+                        "array": f"u component {list(scene.u.shape)}, active inside a ball of radius 0.3"},
+        "advect2": {"ms": round(advect2_ms, 4), "grid": [sc2.nx, sc2.ny],
+                    "desc": "2D MacCormack step (velocity, then density), smoke 2048^2"},
         "clocks": clocks,
         "gpu_launches": int(launches),
     }

@@ -34,8 +34,12 @@
 
 #ifdef __CUDACC__
 #define GBA_HD __host__ __device__ __forceinline__
+// out of line on the device: the compiler cannot issue the FP64 work of a
+// rare path speculatively (predicated off) for every element
+#define GBA_HD_OUTLINE __host__ __device__ __noinline__
 #else
 #define GBA_HD inline
+#define GBA_HD_OUTLINE inline
 #endif
 
 namespace gba {
@@ -760,24 +764,54 @@ struct ConstrainArgs {
     const int *exists;      // the solid has a negative value (levelset_exist)
 };
 
-// One face. The reference runs its face loop three times over the same
-// saved velocity (macutility3.cpp:68); the loop is idempotent (the solid
-// branch sets the same value from the saved velocity each time, and the
-// wall clamps are idempotent), so one pass gives its result.
-GBA_HD void constrain_face(const ConstrainArgs &a, int dim, unsigned f) {
+// compare_interp(s, p, a, 0.0) from float comparisons alone when the eight
+// corners lie clearly on one side of 0: -1 (all below) or 1 (all above),
+// else 2 (the full test decides). p2 holds twice the position: whole and
+// half nodes, as the faces' positions are. The corners and the float
+// min/max/sum are compare_interp's; its range test is decided here when
+// |the corner nearest 0| >= max(2^-19 am, 2^-100), am the largest
+// magnitude, which exceeds its margin d = 2^-20 am + 1e-38 (so the double
+// test gives the same answer).
+GBA_HD int sign_corners_fast(const Shape &s, const int p2[3], const float *a) {
+    auto cell = [](int v2, int w) {
+        v2 = v2 < 0 ? 0 : (v2 > 2 * (w - 1) ? 2 * (w - 1) : v2);
+        const int c = v2 >> 1;
+        return c < w - 2 ? c : w - 2;
+    };
+    const int i = cell(p2[0], s.w), j = cell(p2[1], s.h), k = cell(p2[2], s.d);
+    const long long base = at(s, i, j, k);
+    const long long sy = s.w, sz = (long long)s.w * s.h;
+    const long long off[8] = {0, 1, sy, sy + 1, sz, sz + 1, sz + sy, sz + sy + 1};
+    float v[8];
+#pragma unroll
+    for (int n = 0; n < 8; ++n) v[n] = a[base + off[n]];
+    float mn = v[0], mx = v[0], sum = v[0];
+#pragma unroll
+    for (int n = 1; n < 8; ++n) {
+        mn = v[n] < mn ? v[n] : mn;
+        mx = mx < v[n] ? v[n] : mx;
+        sum += v[n];
+    }
+    if (!(sum - sum == 0.0f)) return 2;
+    const float am = (-mn < mx) ? mx : -mn;
+    const float margin = am * 0x1p-19f;
+    if (mx < 0.0f && -mx >= margin && -mx >= 0x1p-100f) return -1;
+    if (mn > 0.0f && mn >= margin && mn >= 0x1p-100f) return 1;
+    return 2;
+}
+
+// The solid branch of one face (macutility3.cpp:70-80): the saved velocity
+// interpolated at the face minus its projection on the solid's gradient
+// when that projection is negative; `in` otherwise.
+GBA_HD_OUTLINE float constrain_solid(const ConstrainArgs a, int dim, int i, int j, int k, float in, int side) {
     const Dims &g = a.g;
-    const Shape fs = face_shape(g, dim);
-    if (f >= count(fs) || !*a.exists) return;
-    const unsigned char *mask = dim == 0 ? a.mu : (dim == 1 ? a.mv : a.mw);
-    if (mask && !mask[f]) return;
-    const Idx x = decode(fs, f);
-    const int ip[3] = {x.i, x.j, x.k};
+    const int ip[3] = {i, j, k};
     const float *save[3] = {a.save, a.save + a.off1, a.save + a.off2};
     const double p[3] = {ip[0] + 0.5 * (dim != 0), ip[1] + 0.5 * (dim != 1), ip[2] + 0.5 * (dim != 2)};
-    const float in = (dim == 0 ? save[0] : (dim == 1 ? save[1] : save[2]))[f];
     float val = in;
     const Shape ns{g.nx + 1, g.ny + 1, g.nz + 1};
-    if (compare_interp(ns, p[0], p[1], p[2], a.solid, 0.0) == -1) {
+    if (side == 2) side = compare_interp(ns, p[0], p[1], p[2], a.solid, 0.0);
+    if (side == -1) {
         float dr[3];
         derivative(ns, p, a.solid, dr);
         double nrm[3];
@@ -802,6 +836,28 @@ GBA_HD void constrain_face(const ConstrainArgs &a, int dim, unsigned f) {
                                          (dim == 0 ? nrm[0] : (dim == 1 ? nrm[1] : nrm[2])) * dot);
         }
     }
+    return val;
+}
+
+// One face. The reference runs its face loop three times over the same
+// saved velocity (macutility3.cpp:68); the loop is idempotent (the solid
+// branch sets the same value from the saved velocity each time, and the
+// wall clamps are idempotent), so one pass gives its result. Faces whose
+// solid corners are all clearly positive skip the FP64 work.
+GBA_HD void constrain_face(const ConstrainArgs &a, int dim, unsigned f) {
+    const Dims &g = a.g;
+    const Shape fs = face_shape(g, dim);
+    if (f >= count(fs) || !*a.exists) return;
+    const unsigned char *mask = dim == 0 ? a.mu : (dim == 1 ? a.mv : a.mw);
+    if (mask && !mask[f]) return;
+    const Idx x = decode(fs, f);
+    const int ip[3] = {x.i, x.j, x.k};
+    const float in = (dim == 0 ? a.save : (dim == 1 ? a.save + a.off1 : a.save + a.off2))[f];
+    float val = in;
+    const Shape ns{g.nx + 1, g.ny + 1, g.nz + 1};
+    const int p2[3] = {2 * ip[0] + (dim != 0), 2 * ip[1] + (dim != 1), 2 * ip[2] + (dim != 2)};
+    const int side = sign_corners_fast(ns, p2, a.solid);
+    if (side != 1) val = constrain_solid(a, dim, ip[0], ip[1], ip[2], in, side);
     const int n_dim = dim == 0 ? g.nx : (dim == 1 ? g.ny : g.nz);
     if (ip[dim] == 0 && val < 0.0f) val = 0.0f;
     if (ip[dim] == n_dim && val > 0.0f) val = 0.0f;

@@ -623,6 +623,81 @@ __global__ void __launch_bounds__(BLOCK_THREADS, OCC)
     sweep_items<T>(levels, segs, nseg, n, scenes, gate, color, ctx);
 }
 
+// b - (d x - s), the residual of a cell from its neighbour sum s, with
+// explicit roundings so that every form of the restriction rounds alike
+__device__ __forceinline__ float resid(float b, float d, float x, float s) { return __fsub_rn(b, __fmaf_rn(d, x, -s)); }
+__device__ __forceinline__ double resid(double b, double d, double x, double s) {
+    return __dsub_rn(b, __fma_rn(d, x, -s));
+}
+
+// The restriction of one coarse cell of a uniform tile (coupling u) on a
+// 3D vector level whose 2 x 2 x 2 children all exist, gather-first: every
+// load of the children (own pairs, their -+x cells, the rows j0-1 and
+// j0+2, the planes k0-1 and k0+2, b and the diagonal) is issued before the
+// arithmetic, which is the plane form's (the same neighbour order and
+// roundings).
+template <class T>
+__device__ __forceinline__ T restrict_col(const Grid &g, T u, const T *x, const T *b, const T *diag, int i, int j0,
+                                          int k0) {
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const long long f0 = cell_index(g, i, j0, k0);
+    const Pair<T> zero{T(0), T(0)};
+    Pair<T> X[2][2], B[2][2], D[2][2], YM[2], YP[2], ZM[2], ZP[2];
+    T XM[2][2], XP[2][2];
+#pragma unroll
+    for (int c2 = 0; c2 < 2; ++c2)
+#pragma unroll
+        for (int b2 = 0; b2 < 2; ++b2) {
+            const long long f = f0 + c2 * sz + b2 * sy;
+            X[c2][b2] = ld2<T, true>(x, f, true);
+            B[c2][b2] = ld2<T, true>(b, f, true);
+            D[c2][b2] = ld2<T, true>(diag, f, true);
+            XM[c2][b2] = i > 0 ? __ldg(x + f - 1) : T(0);
+            XP[c2][b2] = i + 2 < g.nx ? __ldg(x + f + 2) : T(0);
+        }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        YM[q] = j0 > 0 ? ld2<T, true>(x, f0 + q * sz - sy, true) : zero;
+        YP[q] = j0 + 2 < g.ny ? ld2<T, true>(x, f0 + q * sz + 2 * sy, true) : zero;
+        ZM[q] = k0 > 0 ? ld2<T, true>(x, f0 - sz + q * sy, true) : zero;
+        ZP[q] = k0 + 2 < g.nz ? ld2<T, true>(x, f0 + 2 * sz + q * sy, true) : zero;
+    }
+    T sum = T(0);
+#pragma unroll
+    for (int c2 = 0; c2 < 2; ++c2)
+#pragma unroll
+        for (int b2 = 0; b2 < 2; ++b2) {
+            const int j = j0 + b2, k = k0 + c2;
+            const Pair<T> own = X[c2][b2];
+            Pair<T> s{T(0), T(0)};
+            if (i > 0) s.a = fmadd(s.a, u, XM[c2][b2]);
+            s.a = fmadd(s.a, u, own.b);
+            s.b = fmadd(s.b, u, own.a);
+            if (i + 2 < g.nx) s.b = fmadd(s.b, u, XP[c2][b2]);
+            const Pair<T> ym = b2 == 0 ? YM[c2] : X[c2][0], yp = b2 == 0 ? X[c2][1] : YP[c2];
+            const Pair<T> zm = c2 == 0 ? ZM[b2] : X[0][b2], zp = c2 == 0 ? X[1][b2] : ZP[b2];
+            if (j > 0) {
+                s.a = fmadd(s.a, u, ym.a);
+                s.b = fmadd(s.b, u, ym.b);
+            }
+            if (j + 1 < g.ny) {
+                s.a = fmadd(s.a, u, yp.a);
+                s.b = fmadd(s.b, u, yp.b);
+            }
+            if (k > 0) {
+                s.a = fmadd(s.a, u, zm.a);
+                s.b = fmadd(s.b, u, zm.b);
+            }
+            if (k + 1 < g.nz) {
+                s.a = fmadd(s.a, u, zp.a);
+                s.b = fmadd(s.b, u, zp.b);
+            }
+            sum += resid(B[c2][b2].a, D[c2][b2].a, own.a, s.a);
+            sum += resid(B[c2][b2].b, D[c2][b2].b, own.b, s.b);
+        }
+    return sum;
+}
+
 // Items are cell tiles of the coarse grid gc; a thread sums the residuals
 // b - A x of the (up to) 8 children of its coarse cell, child pairs
 // (2I, 2I+1) in order of (z, y).
@@ -651,9 +726,15 @@ __device__ __forceinline__ void restrict_items(const BLevel<T> *__restrict__ lev
             auto nb2 = [&](long long m, int, int, bool sec) { return ld2<T, V>(L.x, m, sec); };
             auto nb1 = [&](long long m, int) { return __ldg(L.x + m); };
             cell_tile(L.gc, it, [&](int I, int J, int K, long long cc) {
+                const int i = 2 * I;
+                if constexpr (U && V) {
+                    if (fg.dim == 3 && 2 * J + 1 < fg.ny && 2 * K + 1 < fg.nz) {
+                        L.bc[cc] = restrict_col<T>(fg, cw.u, L.x, L.b, L.diag, i, 2 * J, 2 * K);
+                        return;
+                    }
+                }
                 T sum = T(0);
                 const int kmax = fg.dim == 3 ? 2 : 1;
-                const int i = 2 * I;
                 const bool second = i + 1 < fg.nx;
                 for (int c2 = 0; c2 < kmax; ++c2)
                     for (int b2 = 0; b2 < 2; ++b2) {
@@ -663,8 +744,8 @@ __device__ __forceinline__ void restrict_items(const BLevel<T> *__restrict__ lev
                         const Pair<T> x2 = ld2<T, V>(L.x, f, second);
                         const Pair<T> s = pair_nsum<T, V, U, 2>(fg, cw, i, j, k, f, second, x2, nb2, nb1);
                         const Pair<T> bb = ld2<T, V>(L.b, f, second), dd = ld2<T, V>(L.diag, f, second);
-                        sum += bb.a - (dd.a * x2.a - s.a);
-                        if (second) sum += bb.b - (dd.b * x2.b - s.b);
+                        sum += resid(bb.a, dd.a, x2.a, s.a);
+                        if (second) sum += resid(bb.b, dd.b, x2.b, s.b);
                     }
                 L.bc[cc] = sum;
             });
@@ -1615,9 +1696,11 @@ __device__ __forceinline__ void refine_update_pair(const Grid &g, const BLevel<T
 // (refine_update_pair). Either way r_T = r64 for the next inner solve,
 // |r64|_inf and |r64|_2, and the scene's last flush applies the stopping rule
 // and opens the next inner solve; the last pass's norms are those of the
-// returned solution's residual.
+// returned solution's residual. Four resident blocks per SM (64 registers,
+// no spill): the float-pair update keeps many loads in flight per thread,
+// and given more registers the compiler takes 125 and halves the warps.
 template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, 2) refine_residual_kernel(
+__global__ void __launch_bounds__(BLOCK_THREADS, 4) refine_residual_kernel(
     const BLevel<T> *__restrict__ levels, const BSeg *__restrict__ segs, int nseg, int n,
     const BScene<T> *__restrict__ scenes, double *part, int initial, double residual, int max_iter,
     double inner_rel, int inner_max, BatchCounters *cnt, const int *__restrict__ scene_of) {

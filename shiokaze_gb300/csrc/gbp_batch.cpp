@@ -298,8 +298,9 @@ static MgSettings settings_of(const gbp_params &p) {
 // more warps to hide latency); the best choice moves with the problem size
 // (at 128^3 most run best with 4, at 256^3 red_dot and spmv with 6). For each
 // tuned kernel this times the three variants on the batch's own work lists
-// (one untimed launch, then the median of three, CUDA events on the solve's
-// stream) and keeps the fastest. The launches run ungated on the scenes'
+// (one untimed launch each, then five rounds over the variants, the median
+// of each variant's rounds, CUDA events on the solve's stream) and keeps the
+// fastest. The launches run ungated on the scenes'
 // arrays before the solve fills them: values do not change the work, every
 // array they write is rewritten by the solve before it is read, and the
 // solve resets the scalars and counters they touch. Choices are kept per
@@ -346,26 +347,34 @@ template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::s
         default: return fine_pass<T>(STAGE_SPMV, p, st, -1);
         }
     };
-    const int variants[3] = {4, 5, 6};
+    // the variants are timed in turn, round after round, and each keeps the
+    // median of its rounds: a drift of the clocks during the tuning (the
+    // first solves after idle) then weighs on every variant alike
+    constexpr int kVariants = 3, kRounds = 5;
+    const int variants[kVariants] = {4, 5, 6};
     for (int k = 0; k < BK_TUNED && err == cudaSuccess; ++k) {
-        float best = 0.f;
-        int pick = 0;
-        for (int v : variants) {
-            occ_[k] = v;
-            float t[3] = {0.f, 0.f, 0.f};
-            err = pass(k);
-            for (int r = 0; r < 3 && err == cudaSuccess; ++r) {
+        float t[kVariants][kRounds] = {};
+        for (int v = 0; v < kVariants && err == cudaSuccess; ++v) {
+            occ_[k] = variants[v];
+            err = pass(k);  // first launch of the variant, untimed
+        }
+        for (int r = 0; r < kRounds && err == cudaSuccess; ++r)
+            for (int v = 0; v < kVariants && err == cudaSuccess; ++v) {
+                occ_[k] = variants[v];
                 err = cudaEventRecord(e0, st);
                 if (err == cudaSuccess) err = pass(k);
                 if (err == cudaSuccess) err = cudaEventRecord(e1, st);
                 if (err == cudaSuccess) err = cudaEventSynchronize(e1);
-                if (err == cudaSuccess) err = cudaEventElapsedTime(&t[r], e0, e1);
+                if (err == cudaSuccess) err = cudaEventElapsedTime(&t[v][r], e0, e1);
             }
-            if (err != cudaSuccess) break;
-            std::sort(t, t + 3);
-            if (!pick || t[1] < best) {
-                best = t[1];
-                pick = v;
+        if (err != cudaSuccess) break;
+        int pick = 0;
+        float best = 0.f;
+        for (int v = 0; v < kVariants; ++v) {
+            std::sort(t[v], t[v] + kRounds);
+            if (!pick || t[v][kRounds / 2] < best) {
+                best = t[v][kRounds / 2];
+                pick = variants[v];
             }
         }
         occ_[k] = pick;

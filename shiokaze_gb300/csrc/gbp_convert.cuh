@@ -169,6 +169,8 @@ __host__ __device__ __forceinline__ float split_lo(double c, float hi) {
         }
         if (e >= -126 && e <= 127) return d2f_from_bits(sign | ((unsigned)(e + 127) << 23) | ((unsigned)m & 0x7fffffu));
     }
+    // c = +-0: hi is the same zero and c - hi = +0
+    if ((b << 1) == 0 && (hb << 1) == 0) return d2f_from_bits(0u);
 #ifdef __CUDA_ARCH__
     return split_lo_hw(c, hi);
 #else

@@ -91,6 +91,12 @@ struct FaceParams {
     // of a cell whose n open faces all have area = rho = 1; inv_sum[n] its
     // reciprocal (host-evaluated, the same IEEE operations)
     double w_sum[7], inv_sum[7];
+    // the FP32 level-0 operator of such a cell, from the same conversions
+    // the kernel applies (host-evaluated): sum_hi[n] = d2f_rn(w_sum[n]),
+    // sum_lo[n] = split_lo(w_sum[n], sum_hi[n]), sum_inv[n] = 1 / sum_hi[n]
+    // rounded to nearest (0 for n = 0), unit_hi / unit_lo the pair of w_unit
+    float sum_hi[7], sum_lo[7], sum_inv[7];
+    float unit_hi, unit_lo;
     // dt for the velocity update's dt dp / dx by integer instructions
     // (gbp_exact.cuh), with 1/dx as its power of two
     MulConst dt_mul;
@@ -98,8 +104,8 @@ struct FaceParams {
 
 // a[n] for n in [0, 7) by selects (an indexed kernel parameter would be
 // copied to local memory)
-__device__ __forceinline__ double pick7(const double (&a)[7], int n) {
-    double r = a[0];
+template <class T> __device__ __forceinline__ T pick7(const T (&a)[7], int n) {
+    T r = a[0];
 #pragma unroll
     for (int q = 1; q < 7; ++q) r = n == q ? a[q] : r;
     return r;
@@ -493,6 +499,32 @@ __global__ void __launch_bounds__(BLOCK_THREADS) velocity_kernel(Grid g, double 
 // the 2D path, which the compiler would otherwise issue predicated off for
 // every node (a predicated-off FP64 instruction still takes its FP64-pipe
 // slot on this GPU).
+// Faces whose fractions need the FP64 forms (a cut square, a cut face,
+// eps above 1) are few and scattered: one per warp would take the warp
+// through the FP64 path with one lane active, and on this GPU every FP64
+// warp instruction costs its pipe slots however few lanes it has. The 3D
+// kernel therefore queues them in shared memory and computes them
+// together, a full warp at a time, when the queue fills and at the end.
+constexpr int FACE_QUEUE = 1024;
+struct FaceQueue {
+    long long f[FACE_QUEUE];
+    float q[4][FACE_QUEUE];  // the square's corners (area3's order)
+    float fa[FACE_QUEUE], fb[FACE_QUEUE], uf[FACE_QUEUE];
+    unsigned char tag[FACE_QUEUE];  // d | interior << 2
+};
+
+// area3 needs area3_fp64 (corners neither all >= 0 with eps_solid <= 1
+// nor all < 0)
+__device__ __forceinline__ bool area3_slow(float q00, float q10, float q11, float q01, const FaceParams &fp) {
+    if (q00 >= 0.0f && q10 >= 0.0f && q11 >= 0.0f && q01 >= 0.0f) return !fp.eps_solid_le1;
+    return !(q00 < 0.0f && q10 < 0.0f && q11 < 0.0f && q01 < 0.0f);
+}
+// rho_of needs rho_fp64 (a cut face, or a wet face with eps_fluid > 1)
+__device__ __forceinline__ bool rho_slow(float f0, float f1, const FaceParams &fp) {
+    if ((f0 < 0.0f && f1 > 0.0f) || (f0 > 0.0f && f1 < 0.0f)) return true;
+    return (f0 < 0.0f || f1 < 0.0f) && !fp.eps_fluid_le1;
+}
+
 template <int DIM>
 __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt, double dx, FaceParams fp,
                                                               const float *__restrict__ solid,
@@ -514,8 +546,31 @@ __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt,
             fa.w[d][f] = face_weight_fp64(dt, area, rho, dx, fp.dx_pow2, fp.inv_dx2);
         if (area != 0.0f && !(area == 1.0f && fp.dx_pow2)) fa.q[d][f] = face_flux_fp64(area, uf, dx, fp.dx_pow2, fp.inv_dx);
     };
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
+    __shared__ FaceQueue Q;
+    __shared__ int qn;
+    if (threadIdx.x == 0) qn = 0;
+    __syncthreads();
+    // the queued faces, a thread each; the fractions by the same functions
+    // the direct path uses
+    auto flush = [&]() {
+        __syncthreads();
+        const int cnt = qn;
+        for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+            const int d = Q.tag[e] & 3;
+            const float area = (Q.tag[e] >> 2) ? area3(Q.q[0][e], Q.q[1][e], Q.q[2][e], Q.q[3][e], fp) : 0.0f;
+            emit(d, Q.f[e], area, rho_of(Q.fa[e], Q.fb[e], fp), Q.uf[e]);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) qn = 0;
+        __syncthreads();
+    };
+    // block-uniform trip count (the queue's flushes are block-wide)
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < total; base += (long long)gridDim.x * blockDim.x) {
+        const long long t = base + threadIdx.x;
+        // room for this round's faces (at most 3 per thread): the barrier's
+        // OR includes the last pusher's own reading, which is the count
+        if (DIM == 3 && __syncthreads_or(qn > FACE_QUEUE - 3 * BLOCK_THREADS)) flush();
+        if (t >= total) continue;
         int i, j, k;
         node_coords(g, t, i, j, k);
         if constexpr (DIM == 3) {
@@ -551,9 +606,27 @@ __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt,
                 f[d] = face_index(g, d, i, j, k);
                 uf[d] = ex[d] ? __ldg(vel[d] + f[d]) : 0.0f;
             }
-            if (ex[0]) emit(0, f[0], in[0] ? area3(S000, S010, S011, S001, fp) : 0.0f, rho_of(fA, fB0, fp), uf[0]);
-            if (ex[1]) emit(1, f[1], in[1] ? area3(S000, S100, S101, S001, fp) : 0.0f, rho_of(fA, fB1, fp), uf[1]);
-            if (ex[2]) emit(2, f[2], in[2] ? area3(S000, S100, S110, S010, fp) : 0.0f, rho_of(fA, fB2, fp), uf[2]);
+            // fractions of 0 or 1 here; a face that needs the FP64 forms is
+            // queued with its inputs
+            auto face = [&](int d, float q00, float q10, float q11, float q01, float fB) {
+                if (in[d] ? area3_slow(q00, q10, q11, q01, fp) || rho_slow(fA, fB, fp) : rho_slow(fA, fB, fp)) {
+                    const int e = atomicAdd(&qn, 1);
+                    Q.f[e] = f[d];
+                    Q.q[0][e] = q00;
+                    Q.q[1][e] = q10;
+                    Q.q[2][e] = q11;
+                    Q.q[3][e] = q01;
+                    Q.fa[e] = fA;
+                    Q.fb[e] = fB;
+                    Q.uf[e] = uf[d];
+                    Q.tag[e] = (unsigned char)(d | (in[d] ? 4 : 0));
+                    return;
+                }
+                emit(d, f[d], in[d] ? area3(q00, q10, q11, q01, fp) : 0.0f, rho_of(fA, fB, fp), uf[d]);
+            };
+            if (ex[0]) face(0, S000, S010, S011, S001, fB0);
+            if (ex[1]) face(1, S000, S100, S101, S001, fB1);
+            if (ex[2]) face(2, S000, S100, S110, S010, fB2);
         } else {
             const int pi[3] = {i, j, k};
             for (int d = 0; d < 2; ++d) {
@@ -567,6 +640,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt,
             }
         }
     }
+    if (DIM == 3) flush();
 }
 
 // The FP64 fallbacks of the cell pass, out of line (see faces_kernel):
@@ -702,6 +776,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_faces_kernel(
                 dg = 0.0;
                 rhs = 0.0;
                 cpl[0] = cpl[1] = cpl[2] = 0.0;
+                unit = true;  // the zero row: table entry 0
+                nopen = 0;
             }
             diag[c] = dg;
             b[c] = rhs;
@@ -709,20 +785,43 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_faces_kernel(
             for (int d = 0; d < 3; ++d)
                 if (d < g.dim) cp[d][c] = cpl[d];
             if (o.diag) {
-                const float d32 = d2f_rn(dg), x32 = d2f_rn(cpl[0]), y32 = d2f_rn(cpl[1]);
+                float d32, i32, x32, y32, z32, dlo, xlo, ylo, zlo;
+                if (unit) {
+                    // every open face unit (or no unknown: all zero): the
+                    // conversions of the table values, computed on the host
+                    d32 = pick7(fp.sum_hi, nopen);
+                    dlo = pick7(fp.sum_lo, nopen);
+                    i32 = pick7(fp.sum_inv, nopen);
+                    const bool bx = nonzero_bits(cpl[0]), by = nonzero_bits(cpl[1]), bz = nonzero_bits(cpl[2]);
+                    x32 = bx ? fp.unit_hi : 0.0f;
+                    xlo = bx ? fp.unit_lo : 0.0f;
+                    y32 = by ? fp.unit_hi : 0.0f;
+                    ylo = by ? fp.unit_lo : 0.0f;
+                    z32 = bz ? fp.unit_hi : 0.0f;
+                    zlo = bz ? fp.unit_lo : 0.0f;
+                } else {
+                    d32 = d2f_rn(dg);
+                    x32 = d2f_rn(cpl[0]);
+                    y32 = d2f_rn(cpl[1]);
+                    z32 = d2f_rn(cpl[2]);
+                    i32 = positive_bits(dg) ? __frcp_rn(d32) : 0.0f;
+                    dlo = split_lo(dg, d32);
+                    xlo = split_lo(cpl[0], x32);
+                    ylo = split_lo(cpl[1], y32);
+                    zlo = split_lo(cpl[2], z32);
+                }
                 o.diag[c] = d32;
-                o.inv[c] = positive_bits(dg) ? __frcp_rn(d32) : 0.0f;
+                o.inv[c] = i32;
                 o.cx[c] = x32;
                 o.cy[c] = y32;
                 if (o.diag_lo) {
-                    o.diag_lo[c] = split_lo(dg, d32);
-                    o.cx_lo[c] = split_lo(cpl[0], x32);
-                    o.cy_lo[c] = split_lo(cpl[1], y32);
+                    o.diag_lo[c] = dlo;
+                    o.cx_lo[c] = xlo;
+                    o.cy_lo[c] = ylo;
                 }
                 if (g.dim == 3) {
-                    const float z32 = d2f_rn(cpl[2]);
                     o.cz[c] = z32;
-                    if (o.diag_lo) o.cz_lo[c] = split_lo(cpl[2], z32);
+                    if (o.diag_lo) o.cz_lo[c] = zlo;
                 }
             }
             if (o.inv64) o.inv64[c] = positive_bits(dg) ? (unit ? pick7(fp.inv_sum, nopen) : recip_fp64(dg)) : 0.0;
@@ -882,8 +981,14 @@ FaceParams face_params(const SetupParams &sp, double dx, double dt) {
     for (int n = 0; n < 7; ++n) {
         fp.w_sum[n] = acc;
         fp.inv_sum[n] = n ? 1.0 / acc : 0.0;
+        fp.sum_hi[n] = d2f_rn(fp.w_sum[n]);
+        fp.sum_lo[n] = split_lo(fp.w_sum[n], fp.sum_hi[n]);
+        volatile float one = 1.0f;
+        fp.sum_inv[n] = n ? one / fp.sum_hi[n] : 0.0f;  // IEEE division: __frcp_rn's value
         acc = acc + fp.w_unit;
     }
+    fp.unit_hi = d2f_rn(fp.w_unit);
+    fp.unit_lo = split_lo(fp.w_unit, fp.unit_hi);
     fp.dt_mul = make_mul_const(dt, fp.dx_pow2 ? fp.inv_dx_exp : 0);
     fp.dt_mul.ok = fp.dt_mul.ok && fp.dx_pow2;
     return fp;
