@@ -387,6 +387,43 @@ def run_gbp(args):
     ranks.barrier()
     e2e_value = ranks.rate(len(e2e_times), 1000.0 * sum(e2e_times))
 
+    # the drop-in module's transport (Projection=gbprojection3): the arrays
+    # as 8^3 bricks (narrow-band level sets: values within the band listed,
+    # whole-fill bricks by flag; a constant array by its background), the
+    # bricked call timed with its host<->device copies; the bricks are built
+    # before the clock, as the module builds them from the reference's
+    # tiled arrays with the reference's own array operations
+    e2e_bricks = None
+    if scene.dim == 3:
+        def level_bricks(a, mode):
+            if mode == 1:  # a constant array: every brick reads its background
+                return gb.to_bricks(a, np.zeros(a.shape, bool), None, background=float(a.flat[0]))[0]
+            return gb.to_bricks(a, np.abs(a) < scene.band, a <= -scene.band, background=scene.band,
+                                fill=-scene.band)[0]
+        b_solid = level_bricks(scene.solid, scene.solid_mode)
+        b_fluid = level_bricks(scene.fluid, scene.fluid_mode)
+        b_vel = [gb.to_bricks(a, np.ones(a.shape, bool), None)[0] for a in (scene.u, scene.v, scene.w)]
+        nbc = b_fluid[0].size
+        out_slots = [np.arange(nbc, dtype=np.int32)] + [np.where(b[0] >= 0, b[0], -1).astype(np.int32) for b in b_vel]
+        bpj = gb.projector_for(scene, ctx, **cfg)
+        b_times, b_out = [], None
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            brc, b_out = bpj.project_bricks(scene.dt, b_solid, b_fluid, b_vel, out_slots, outputs=b_out)
+            t1 = time.perf_counter()
+            if brc != gb.GBP_OK:
+                raise RuntimeError(f"bricked projection returned {brc}")
+            if k >= args.warmup:
+                b_times.append(t1 - t0)
+        bpj.close()
+        h2d_b = sum(b[0].nbytes + b[1].nbytes for b in [b_solid, b_fluid] + b_vel)
+        d2h_b = sum(int((sl >= 0).sum()) * gb.BRICK_CELLS * 5 for sl in out_slots)  # values + active flags
+        e2e_bricks = {"value": round(ranks.rate(len(b_times), 1000.0 * sum(b_times)), 3), "unit": "solves/s",
+                      "h2d_bytes_per_step": int(h2d_b), "d2h_bytes_per_step": int(d2h_b),
+                      "call": "gbp_project_bricks (the plugin module's transport), pageable host buffers",
+                      "listed_bricks": {"solid": int((b_solid[0] >= 0).sum()), "fluid": int((b_fluid[0] >= 0).sum()),
+                                        "velocity": [int((b[0] >= 0).sum()) for b in b_vel], "of": int(nbc)}}
+
     # roofline: the path's fine-level kernels timed alone, each launched once
     # per iteration; the slowest is the dominant one
     if args.solver == "mgpcg":
@@ -430,6 +467,7 @@ def run_gbp(args):
         "compare": compare,
         "e2e": {"value": round(e2e_value, 3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "host_buffers": "pageable numpy arrays"},
+        "e2e_bricks": e2e_bricks,
         "roofline": roofline,
         "clocks": main["clocks"],
         "gpu_launches": int(main["launches"]),

@@ -449,18 +449,23 @@ class _MacProject:
                                       ctypes.byref(self.params), pp, ctypes.byref(self.stats))
         return check(rc, (GBP_OK, GBP_ERR_NOT_CONVERGED, GBP_ERR_NAN))
 
-    def project_bricks(self, dt, solid, fluid, velocity, out_slots):
+    def project_bricks(self, dt, solid, fluid, velocity, out_slots, outputs=None):
         """gbp_project_bricks (3D): inputs as to_bricks returns them (solid
         nodes, fluid cells, the three face components); out_slots: slot per
         brick (-1 = not copied out) for the pressure and u, v, w. Returns
-        the status and, per output, (values, active) of its listed bricks."""
+        the status and, per output, (values, active) of its listed bricks;
+        `outputs`, the list a previous call returned for the same slots, is
+        written again instead of new arrays (as a caller keeps its buffers)."""
         ins = [_bricks_struct(b) for b in (solid, fluid) + tuple(velocity)]
         outs, keep = [], []
-        for sl in out_slots:
+        for n, sl in enumerate(out_slots):
             sl = np.ascontiguousarray(sl, np.int32)
             count = int((sl >= 0).sum())
-            vals = np.zeros(count * BRICK_CELLS, np.float32)
-            act = np.zeros(count * BRICK_CELLS, np.uint8)
+            if outputs is not None and outputs[n][0].size == count * BRICK_CELLS:
+                vals, act = outputs[n]
+            else:
+                vals = np.zeros(count * BRICK_CELLS, np.float32)
+                act = np.zeros(count * BRICK_CELLS, np.uint8)
             keep.append((sl, vals, act))
             outs.append(BricksOut(sl.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), count,
                                   vals.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),

@@ -305,7 +305,7 @@ static MgSettings settings_of(const gbp_params &p) {
 // array they write is rewritten by the solve before it is read, and the
 // solve resets the scalars and counters they touch. Choices are kept per
 // precision and half-octave of the batch's fine cells. The same timing
-// picks the grid of the cooperative coarse-level kernels (2, 3 or 4 blocks
+// picks the grid of the cooperative coarse-level kernels (1, 2, 3 or 4 blocks
 // per SM, or all that stay resident): fewer blocks make each grid-wide
 // barrier cheaper, more hide the loads of the larger coarse levels.
 template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::string &key) {
@@ -386,7 +386,7 @@ template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::s
         float best = 0.f;
         int pick = full;
         coarse_per_sm = 0;
-        for (int f : {2, 3, 4, 0}) {
+        for (int f : {1, 2, 3, 4, 0}) {
             const int nb = f ? std::min(full, sms_ * f) : full;
             if (f && nb >= full) continue;
             auto run = [&]() {

@@ -50,6 +50,9 @@ template <class T> struct MgHierarchy {
     // diag, cx, cy, cz (the mixed refinement's float-pair products); null
     // for the FP64 hierarchy
     T *lo[4] = {nullptr, nullptr, nullptr, nullptr};
+    // scratch of the tile classification (sub-box partials), or null
+    void *class_parts = nullptr;
+    size_t class_parts_bytes = 0;
     MgLevel<T> levels[MG_MAX_LEVELS];
 };
 

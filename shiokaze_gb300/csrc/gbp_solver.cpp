@@ -63,8 +63,10 @@ size_t solver_device_bytes(const Grid &g, const gbp_params &p) {
         bytes += s * cells * (p.precision == GBP_PRECISION_MIXED ? 14 : 1);  // mixed: + the operator's low floats
         for (size_t l = 1; l < lv.size(); ++l) bytes += s * (size_t)lv[l].ncell * 7;
         // tile classes (a value per tile; rounded up to whole allocations)
+        // and the classification's sub-box partials
         for (size_t l = 0; l + 1 < lv.size(); ++l)
             bytes += s * (size_t)(((lv[l].nx + 63) / 64) * (long long)lv[l].nty * lv[l].ntz + lv[l + 1].ntiles) + 1024;
+        if (lv.size() > 1) bytes += 24 * (size_t)((lv[0].nx + 63) / 64) * lv[0].nty * lv[0].nz + 1024;
     }
     return bytes;
 }
@@ -85,6 +87,16 @@ template <class T> int Solver::alloc_classes(MgHierarchy<T> &H) {
         const Grid &C = H.levels[l + 1].g;
         int rc = alloc(&F.tcp, (size_t)(((F.g.nx + 63) / 64) * (long long)F.g.nty * F.g.ntz));
         if (rc || (rc = alloc(&F.tcr, (size_t)C.ntiles))) return rc;
+    }
+    // the classification's sub-box partials (64 x 8 x 1 sub-boxes of level
+    // 0 at most; 3 words each, 8-byte words in the FP64 hierarchy)
+    if (H.nlevels > 1) {
+        const Grid &F0 = H.levels[0].g;
+        const size_t n = (size_t)((F0.nx + 63) / 64) * F0.nty * F0.nz;
+        double *d = nullptr;
+        if (int rc = alloc(&d, 3 * n)) return rc;
+        H.class_parts = d;
+        H.class_parts_bytes = 3 * n * sizeof(double);
     }
     return GBP_OK;
 }

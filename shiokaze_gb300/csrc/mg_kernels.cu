@@ -303,6 +303,123 @@ __global__ void __launch_bounds__(BLOCK_THREADS) mg_classify_kernel(MgLevel<T> L
     }
 }
 
+// One read of a level for both classifications: mg_class_parts_kernel
+// reduces each sub-box of 64 x 8 x gz cells (gz divides both box depths:
+// the pair tiles' tz and the restriction boxes' 2 tz of the coarser grid)
+// to the min and max coupling bit patterns and the any-unknown flag, with
+// mg_classify_kernel's reads; mg_class_combine_kernel then forms each pair
+// tile's and each restriction box's class from its sub-boxes. min, max and
+// or are exact, so the classes equal those of the two-pass form.
+template <class T> struct ClassPart {
+    typename Bits<T>::U lo, hi;
+    int any;
+};
+
+template <class T>
+__global__ void __launch_bounds__(BLOCK_THREADS) mg_class_parts_kernel(MgLevel<T> L, int gz, ClassPart<T> *parts,
+                                                                       int sxn, int syn, long long nsub) {
+    using U = typename Bits<T>::U;
+    __shared__ U slo[BLOCK_THREADS / 32], shi[BLOCK_THREADS / 32];
+    __shared__ int sany[BLOCK_THREADS / 32];
+    const Grid &g = L.g;
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const int nb = 64 * 8 * gz;
+    for (long long b = blockIdx.x; b < nsub; b += gridDim.x) {
+        const long long r = b / sxn;
+        const int i0 = (int)(b - r * sxn) * 64, j0 = (int)(r % syn) * 8, k0 = (int)(r / syn) * gz;
+        U lo = ~U(0), hi = 0;
+        int any = 0;
+        for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+            const int i = i0 + (q & 63), j = j0 + ((q >> 6) & 7), k = k0 + (q >> 9);
+            if (i >= g.nx || j >= g.ny || k >= g.nz) continue;
+            const long long c = cell_index(g, i, j, k);
+            any |= (Bits<T>::of(L.diag[c]) << 1) != 0;  // diag != 0 (either sign of 0)
+            auto see = [&](T v) {
+                const U u = Bits<T>::of(v);
+                lo = u < lo ? u : lo;
+                hi = u > hi ? u : hi;
+            };
+            if (i > 0) see(L.cx[c - 1]);
+            if (i + 1 < g.nx) see(L.cx[c]);
+            if (j > 0) see(L.cy[c - sy]);
+            if (j + 1 < g.ny) see(L.cy[c]);
+            if (g.dim == 3) {
+                if (k > 0) see(L.cz[c - sz]);
+                if (k + 1 < g.nz) see(L.cz[c]);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const U l2 = __shfl_xor_sync(0xffffffffu, lo, o), h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+            lo = l2 < lo ? l2 : lo;
+            hi = h2 > hi ? h2 : hi;
+            any |= __shfl_xor_sync(0xffffffffu, any, o);
+        }
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        if (lane == 0) {
+            slo[wid] = lo;
+            shi[wid] = hi;
+            sany[wid] = any;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < BLOCK_THREADS / 32; ++w) {
+                lo = slo[w] < lo ? slo[w] : lo;
+                hi = shi[w] > hi ? shi[w] : hi;
+                any |= sany[w];
+            }
+            parts[b] = ClassPart<T>{lo, hi, any};
+        }
+        __syncthreads();
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(BLOCK_THREADS) mg_class_combine_kernel(Grid g, Grid gc, int gz,
+                                                                         const ClassPart<T> *parts, int sxn, int syn,
+                                                                         int szn, T *tcp, long long np, T *tcr,
+                                                                         long long nr) {
+    using U = typename Bits<T>::U;
+    const long long ntx2 = (g.nx + 63) / 64;
+    const int bz1 = g.dim == 3 ? 2 * gc.tz : 1;
+    for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < np + nr;
+         b += (long long)gridDim.x * blockDim.x) {
+        int sx, sy0, ny2, sz0, nz2;  // the box's sub-boxes: column sx, rows sy0.., planes sz0..
+        if (b < np) {
+            const long long r = b / ntx2;
+            sx = (int)(b - r * ntx2);
+            sy0 = (int)(r % g.nty);
+            ny2 = 1;
+            sz0 = (int)(r / g.nty) * (g.tz / gz);
+            nz2 = g.tz / gz;
+        } else {
+            int I0, J0, K0;
+            tile_origin(gc, b - np, I0, J0, K0);
+            sx = (2 * I0) / 64;
+            sy0 = (2 * J0) / 8;
+            ny2 = 2;
+            sz0 = (g.dim == 3 ? 2 * K0 : 0) / gz;
+            nz2 = bz1 / gz;
+        }
+        U lo = ~U(0), hi = 0;
+        int any = 0;
+        for (int zz = sz0; zz < sz0 + nz2 && zz < szn; ++zz)
+            for (int yy = sy0; yy < sy0 + ny2 && yy < syn; ++yy) {
+                const ClassPart<T> q = parts[sx + (long long)sxn * (yy + (long long)syn * zz)];
+                lo = q.lo < lo ? q.lo : lo;
+                hi = q.hi > hi ? q.hi : hi;
+                any |= q.any;
+            }
+        // mg_classify_kernel's rule
+        T cls = T(TILE_MIXED);
+        if (!any && lo == 0 && hi == 0) cls = T(TILE_EMPTY);
+        else if (lo == hi) cls = Bits<T>::value(lo);
+        if (!(cls >= T(0)) && cls != T(TILE_EMPTY)) cls = T(TILE_MIXED);
+        if (b < np) tcp[b] = cls;
+        else tcr[b - np] = cls;
+    }
+}
+
 template <class T> int nblocks(const Grid &g, int grid_blocks) {
     long long b = g.ntiles < grid_blocks ? g.ntiles : grid_blocks;
     return b < 1 ? 1 : (int)b;
@@ -325,11 +442,32 @@ cudaError_t mg_setup(const Grid &g0, Operator<double> A, const MgHierarchy<T> &H
             F, C, const_cast<T *>(C.diag), const_cast<T *>(C.inv), const_cast<T *>(C.cx), const_cast<T *>(C.cy),
             const_cast<T *>(C.cz));
     }
-    // tile classes of the levels the global-memory kernels run
+    // tile classes of the levels the global-memory kernels run: one read of
+    // the level into sub-box partials (in the hierarchy's scratch), then the
+    // classes from them; the two-pass form where there is no scratch
     for (int l = 0; l < H.tail && l + 1 < H.nlevels; ++l) {
         const MgLevel<T> &F = H.levels[l], &C = H.levels[l + 1];
         if (!F.tcp || !F.tcr) continue;
         const long long np = (long long)((F.g.nx + 63) / 64) * F.g.nty * F.g.ntz, nr = C.g.ntiles;
+        const int bz1 = F.g.dim == 3 ? 2 * C.g.tz : 1;
+        int gz = F.g.tz;
+        for (int a = bz1; a;) {  // gcd(tz, bz1)
+            const int t = gz % a;
+            gz = a;
+            a = t;
+        }
+        const int sxn = (F.g.nx + 63) / 64, syn = F.g.nty, szn = (F.g.nz + gz - 1) / gz;
+        const long long nsub = (long long)sxn * syn * szn;
+        if (H.class_parts && nsub * (long long)sizeof(ClassPart<T>) <= (long long)H.class_parts_bytes) {
+            auto *parts = static_cast<ClassPart<T> *>(H.class_parts);
+            mg_class_parts_kernel<T><<<(int)std::min<long long>(nsub, grid_blocks), BLOCK_THREADS, 0, stream>>>(
+                F, gz, parts, sxn, syn, nsub);
+            const long long nt = np + nr;
+            mg_class_combine_kernel<T><<<(int)std::min<long long>((nt + BLOCK_THREADS - 1) / BLOCK_THREADS, grid_blocks),
+                                         BLOCK_THREADS, 0, stream>>>(F.g, C.g, gz, parts, sxn, syn, szn, F.tcp, np,
+                                                                     F.tcr, nr);
+            continue;
+        }
         mg_classify_kernel<T><<<(int)std::min<long long>(np, grid_blocks), BLOCK_THREADS, 0, stream>>>(
             F, C.g, 0, F.tcp, np);
         mg_classify_kernel<T><<<(int)std::min<long long>(nr, grid_blocks), BLOCK_THREADS, 0, stream>>>(

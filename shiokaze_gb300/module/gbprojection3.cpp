@@ -46,8 +46,9 @@ protected:
         m_params.surface_tension = surface_tension;
         expect_shape(solid.shape(), nx + 1, ny + 1, nz + 1, "solid");
         expect_shape(fluid.shape(), nx, ny, nz, "fluid");
-        // the inputs as bricks (only the listed ones travel; the GPU expands them)
-        gbarray::Bricks bs, bf, bv[3];
+        // the inputs as bricks (only the listed ones travel; the GPU expands
+        // them); the brick buffers are members, kept from call to call
+        gbarray::Bricks &bs = m_bs, &bf = m_bf, *bv = m_bv;
         gbarray::to_bricks(solid, bs);
         gbarray::to_bricks(fluid, bf);
         for (int d = 0; d < 3; ++d) {
@@ -58,7 +59,7 @@ protected:
         // bricks); the pressure where a cell can be fluid (a listed brick of
         // the fluid level set, or a filled or background one whose value is
         // negative)
-        gbarray::BricksOut po, vo[3];
+        gbarray::BricksOut &po = m_po, *vo = m_vo;
         po.nbx = bf.nbx;
         po.nby = bf.nby;
         po.slot.assign(bf.slot.size(), -1);
@@ -138,6 +139,8 @@ public:
 
 private:
     gbp_params m_params;
+    gbarray::Bricks m_bs, m_bf, m_bv[3];
+    gbarray::BricksOut m_po, m_vo[3];
     int m_device{0};
     gbp_ctx *m_ctx{nullptr};
     gbp_scene *m_scene{nullptr};
