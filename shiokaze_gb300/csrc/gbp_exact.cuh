@@ -97,6 +97,9 @@ __host__ __device__ __forceinline__ bool exact_sum(const float *f, int n, unsign
         return true;
     }
     if (emax - emin > 36 || emin + k < -1000 || emax + k > 1000) return false;
+    // within 26 binades every term is below 2^50 in units of 2^emin, so a
+    // partial sum of at most 7 terms stays below 2^53: none can round
+    const bool spread = emax - emin > 26;
     long long s = 0;
 #pragma unroll
     for (int i = 0; i < n; ++i) {
@@ -107,7 +110,7 @@ __host__ __device__ __forceinline__ bool exact_sum(const float *f, int n, unsign
         // the term's sign: the float's, flipped where neg says
         s += (((b >> 31) ^ (neg >> i)) & 1u) ? -m : m;
         const unsigned long long mag = (unsigned long long)(s < 0 ? -s : s);
-        if ((mag >> 53) && ((mag >> ex_ctz64(mag)) >> 53)) return false;  // this partial sum would round
+        if (spread && (mag >> 53) && ((mag >> ex_ctz64(mag)) >> 53)) return false;  // this partial sum would round
     }
     if (!s) {  // x + (-x) = +0 in round to nearest
         out = 0.0;

@@ -718,12 +718,15 @@ __global__ void __launch_bounds__(BLOCK_THREADS, 3) assemble_faces_kernel(
             const float fc = __ldg(fluid + c);
             float fr[6], ar[6], uv[6], fq[6];
             bool has[6];
-            // the index of face nq (formed again where needed: fewer registers)
+            // the index of face nq from the cell's: the -x face of cell c is
+            // c + j + ny k, the -y face c + nx k, the -z face c; the + faces
+            // one step further (face_index, without its multiplications)
             auto findex = [&](int nq) {
                 const int d = nq >> 1;
-                int f[3] = {i, j, k};
-                if ((nq & 1) == 0) f[d] += 1;
-                return face_index(g, d, f[0], f[1], f[2]);
+                const long long base = c + (d == 0 ? (long long)j + (long long)g.ny * k
+                                                   : (d == 1 ? (long long)g.nx * k : 0ll));
+                const long long step = d == 0 ? 1ll : (d == 1 ? (long long)g.nx : (long long)g.nx * g.ny);
+                return (nq & 1) == 0 ? base + step : base;
             };
 #pragma unroll
             for (int nq = 0; nq < 6; ++nq) {
