@@ -59,6 +59,10 @@ struct gbp_ctx {
     int grid_blocks = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // the host-array call's second stream: the pressure's copy back runs
+    // there while the velocity update runs on the first
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_pressure = nullptr;
     long long launches = 0;
     CsrWork csr;  // device arrays of gbp_csr_cg
     AdvectWork adv;  // device scratch of gbp_advect3*
@@ -145,7 +149,9 @@ int gbp_create(int device, gbp_ctx **out) {
     c->grid_blocks = c->sm_count * 6;
     if (c->grid_blocks > MAX_GRID) c->grid_blocks = MAX_GRID;
     GBP_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    GBP_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
     for (auto &e : c->ev) GBP_CUDA(cudaEventCreate(&e));
+    GBP_CUDA(cudaEventCreateWithFlags(&c->ev_pressure, cudaEventDisableTiming));
     *out = c;
     return GBP_OK;
 }
@@ -158,6 +164,8 @@ void gbp_destroy(gbp_ctx *c) {
     if (c->adv_stage) cudaFree(c->adv_stage);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
+    if (c->ev_pressure) cudaEventDestroy(c->ev_pressure);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -361,9 +369,12 @@ int ensure_active_sets(gbp_scene *s) {
     return GBP_OK;
 }
 
+// pressure_host (host-array calls): the pressure is copied there on the
+// context's copy stream while the velocity update (which only reads it)
+// runs on `stream`; both streams are synchronised before the return.
 int project_device(gbp_scene *s, double dt, const float *solid, const float *fluid, float *u, float *v, float *w,
                    const gbp_params &p, float *pressure, gbp_stats *stats, cudaStream_t stream,
-                   bool active_sets = false) {
+                   bool active_sets = false, float *pressure_host = nullptr) {
     gbp_ctx *c = s->ctx;
     const Grid &g = s->g;
     int rc = gbp::validate_params(p);
@@ -397,6 +408,7 @@ int project_device(gbp_scene *s, double dt, const float *solid, const float *flu
 
     GBP_CUDA(launch_pressure(g, st.diag, st.x, p.warm_start && st.have_prev ? st.prev : nullptr, pressure,
                              p.warm_start ? st.prev : nullptr, c->grid_blocks, stream));
+    if (pressure_host) GBP_CUDA(cudaEventRecord(c->ev_pressure, stream));
     if (active_sets) {
         GBP_CUDA(launch_active_sets(g, st.faces, fluid, u, v, w, st.diag, s->d_unknown, s->d_on[0], s->d_on[1],
                                     s->d_on[2], st.sc, c->grid_blocks, stream));
@@ -406,6 +418,14 @@ int project_device(gbp_scene *s, double dt, const float *solid, const float *flu
     c->launches += 2;
     if (p.warm_start) st.have_prev = true;
     GBP_CUDA(cudaEventRecord(c->ev[3], stream));
+    if (pressure_host) {
+        // enqueued after the velocity update, so that the host, which a copy
+        // into pageable memory holds until it is done, has launched it first
+        GBP_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_pressure, 0));
+        GBP_CUDA(cudaMemcpyAsync(pressure_host, pressure, 4 * (size_t)g.ncell, cudaMemcpyDeviceToHost,
+                                 c->copy_stream));
+        GBP_CUDA(cudaStreamSynchronize(c->copy_stream));
+    }
     GBP_CUDA(cudaStreamSynchronize(stream));
 
     if (stats) {
@@ -446,12 +466,11 @@ int project_host(const char *who, gbp_scene *s, double dt, const float *solid, c
     GBP_CUDA(cudaMemcpyAsync(s->d_u, u, 4 * n_face(g, 0), cudaMemcpyHostToDevice, st));
     GBP_CUDA(cudaMemcpyAsync(s->d_v, v, 4 * n_face(g, 1), cudaMemcpyHostToDevice, st));
     if (g.dim == 3) GBP_CUDA(cudaMemcpyAsync(s->d_w, w, 4 * n_face(g, 2), cudaMemcpyHostToDevice, st));
-    rc = project_device(s, dt, s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, p, s->d_p, stats, st, sets);
+    rc = project_device(s, dt, s->d_solid, s->d_fluid, s->d_u, s->d_v, s->d_w, p, s->d_p, stats, st, sets, pressure);
     if (rc != GBP_OK && rc != GBP_ERR_NOT_CONVERGED && rc != GBP_ERR_NAN) return rc;
     GBP_CUDA(cudaMemcpyAsync(u, s->d_u, 4 * n_face(g, 0), cudaMemcpyDeviceToHost, st));
     GBP_CUDA(cudaMemcpyAsync(v, s->d_v, 4 * n_face(g, 1), cudaMemcpyDeviceToHost, st));
     if (g.dim == 3) GBP_CUDA(cudaMemcpyAsync(w, s->d_w, 4 * n_face(g, 2), cudaMemcpyDeviceToHost, st));
-    if (pressure) GBP_CUDA(cudaMemcpyAsync(pressure, s->d_p, 4 * (size_t)g.ncell, cudaMemcpyDeviceToHost, st));
     if (sets) {
         unsigned char *out[3] = {u_active, v_active, w_active};
         GBP_CUDA(cudaMemcpyAsync(unknown, s->d_unknown, (size_t)g.ncell, cudaMemcpyDeviceToHost, st));
