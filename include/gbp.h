@@ -93,7 +93,7 @@ typedef struct gbp_params {
     int solver;             /* GBP_SOLVER_* (default GBP_SOLVER_CG) */
     int precision;          /* GBP_PRECISION_* (default GBP_PRECISION_FP64) */
     int mg_smooth;          /* red-black sweeps before and after each coarse correction (default 1) */
-    int mg_coarsest;        /* coarsen while any edge exceeds this (default 4) */
+    int mg_coarsest;        /* coarsen while any edge exceeds this (default 7) */
     double inner_tolerance; /* MIXED: relative residual of each inner solve (default 1e-3) */
     int iterations_per_sync;/* CG iterations between host checks of convergence (default 16) */
     double surface_tension; /* the surface_tension argument of macproject3_interface::project

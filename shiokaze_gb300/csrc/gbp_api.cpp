@@ -108,7 +108,7 @@ void gbp_params_default(gbp_params *p) {
     p->solver = GBP_SOLVER_CG;
     p->precision = GBP_PRECISION_FP64;
     p->mg_smooth = 1;
-    p->mg_coarsest = 4;
+    p->mg_coarsest = 7;  // coarsest level 4^3 for power-of-two grids, 6^3 / 5^3 / ... for the others
     p->inner_tolerance = 1e-3;
     p->iterations_per_sync = 16;
     p->surface_tension = 0.0;
