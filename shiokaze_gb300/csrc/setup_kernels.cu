@@ -567,7 +567,7 @@ __global__ void __launch_bounds__(BLOCK_THREADS) faces_kernel(Grid g, double dt,
     // block-uniform trip count (the queue's flushes are block-wide)
     for (long long base = (long long)blockIdx.x * blockDim.x; base < total; base += (long long)gridDim.x * blockDim.x) {
         const long long t = base + threadIdx.x;
-        // room for this round's faces (at most 3 per thread): the barrier's
+        // room for this iteration's faces (at most 3 per thread): the barrier's
         // OR includes the last pusher's own reading, which is the count
         if (DIM == 3 && __syncthreads_or(qn > FACE_QUEUE - 3 * BLOCK_THREADS)) flush();
         if (t >= total) continue;
