@@ -939,8 +939,8 @@ __device__ __forceinline__ bool grid_barrier(BatchCounters *cnt) {
 // Levels first..last top-down: presmooth, extra sweeps, restriction. The
 // idle test at the start reads a counter no block changes during the
 // launch, so either every block returns there or none does.
-template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+template <class T, int OCCB>
+__global__ void __launch_bounds__(BLOCK_THREADS, OCCB)
     coarse_descend_kernel(const BLevel<T> *__restrict__ levels, const CoarseLists cl,
                           const BScene<T> *__restrict__ scenes, int gate, MgSettings ms, BatchCounters *cnt) {
     if (batch_idle(cnt)) return;
@@ -960,8 +960,8 @@ __global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
 
 // Levels last..first bottom-up: prolongation with the black sweep, extra
 // sweeps, the red sweep.
-template <class T>
-__global__ void __launch_bounds__(BLOCK_THREADS, BatchOcc<T>::blocks)
+template <class T, int OCCB>
+__global__ void __launch_bounds__(BLOCK_THREADS, OCCB)
     coarse_ascend_kernel(const BLevel<T> *__restrict__ levels, const CoarseLists cl,
                          const BScene<T> *__restrict__ scenes, int gate, MgSettings ms, T alpha, BatchCounters *cnt) {
     if (batch_idle(cnt)) return;
@@ -2281,7 +2281,9 @@ cudaError_t b_coarse_descend(const BLaunch &L, const BLevel<T> *levels, const Co
     at[0].val.cooperative = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, coarse_descend_kernel<T>, levels, cl, scenes, L.gate, ms, L.cnt);
+    if (L.occ == 2) return cudaLaunchKernelEx(&cfg, coarse_descend_kernel<T, 2>, levels, cl, scenes, L.gate, ms, L.cnt);
+    return cudaLaunchKernelEx(&cfg, coarse_descend_kernel<T, BatchOcc<T>::blocks>, levels, cl, scenes, L.gate, ms,
+                              L.cnt);
 }
 template <class T>
 cudaError_t b_coarse_ascend(const BLaunch &L, const BLevel<T> *levels, const CoarseLists &cl,
@@ -2295,13 +2297,18 @@ cudaError_t b_coarse_ascend(const BLaunch &L, const BLevel<T> *levels, const Coa
     at[0].val.cooperative = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, coarse_ascend_kernel<T>, levels, cl, scenes, L.gate, ms, alpha, L.cnt);
+    if (L.occ == 2)
+        return cudaLaunchKernelEx(&cfg, coarse_ascend_kernel<T, 2>, levels, cl, scenes, L.gate, ms, alpha, L.cnt);
+    return cudaLaunchKernelEx(&cfg, coarse_ascend_kernel<T, BatchOcc<T>::blocks>, levels, cl, scenes, L.gate, ms,
+                              alpha, L.cnt);
 }
 // resident blocks of the two cooperative kernels on `sms` SMs (the smaller)
 template <class T> int b_coarse_capacity(int sms) {
     int a = 0, b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, coarse_descend_kernel<T>, BLOCK_THREADS, 0) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, coarse_ascend_kernel<T>, BLOCK_THREADS, 0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, coarse_descend_kernel<T, BatchOcc<T>::blocks>,
+                                                      BLOCK_THREADS, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, coarse_ascend_kernel<T, BatchOcc<T>::blocks>,
+                                                      BLOCK_THREADS, 0) != cudaSuccess)
         return 0;
     return sms * (a < b ? a : b);
 }

@@ -237,6 +237,7 @@ template <class T> int BatchRunner::build(const BatchPlan<T> &plan, int grid_blo
     // V-cycle half, on at most as many blocks as stay resident
     coarse_ = CoarseLists{};
     coarse_blocks_ = 0;
+    coarse_occ_ = 0;
     if (plan.max_global > 1) {
         coarse_.first = 1;
         coarse_.last = plan.max_global - 1;
@@ -319,6 +320,7 @@ template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::s
             // blocks per SM of the cooperative grid (0: all that stay resident)
             const int f = it->second[BK_TUNED];
             if (f > 0) coarse_blocks_ = std::min(coarse_blocks_, sms_ * f);
+            coarse_occ_ = it->second[BK_TUNED + 1];
             return GBP_OK;
         }
     }
@@ -386,13 +388,21 @@ template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::s
         float best = 0.f;
         int pick = full;
         coarse_per_sm = 0;
-        for (int f : {1, 2, 3, 4, 0}) {
+        // (blocks per SM, register variant): 2 = launch bounds of 2 blocks
+        // per SM (no spills), 0 = the precision's default bounds
+        const int cand[6][2] = {{1, 2}, {2, 2}, {2, 0}, {3, 0}, {4, 0}, {0, 0}};
+        coarse_occ_ = 0;
+        std::vector<std::pair<int, int>> tried;
+        for (const auto &cv : cand) {
+            const int f = cv[0], occ = cv[1];
             const int nb = f ? std::min(full, sms_ * f) : full;
-            if (f && nb >= full) continue;
+            if (occ == 2 && nb > 2 * sms_) continue;  // not all resident with that variant
+            if (std::find(tried.begin(), tried.end(), std::make_pair(nb, occ)) != tried.end()) continue;
+            tried.emplace_back(nb, occ);
             auto run = [&]() {
-                cudaError_t e = b_coarse_descend<T>(BLaunch{nb, st, -1, d_scene_of_, d_counters_}, lv, coarse_, sc, ms);
+                cudaError_t e = b_coarse_descend<T>(BLaunch{nb, st, -1, d_scene_of_, d_counters_, occ}, lv, coarse_, sc, ms);
                 if (e == cudaSuccess)
-                    e = b_coarse_ascend<T>(BLaunch{nb, st, -1, d_scene_of_, d_counters_}, lv, coarse_, sc, ms,
+                    e = b_coarse_ascend<T>(BLaunch{nb, st, -1, d_scene_of_, d_counters_, occ}, lv, coarse_, sc, ms,
                                            T(ms.alpha));
                 return e;
             };
@@ -411,6 +421,7 @@ template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::s
                 best = t[1];
                 pick = nb;
                 coarse_per_sm = f;
+                coarse_occ_ = occ;
             }
         }
         coarse_blocks_ = pick;
@@ -428,6 +439,7 @@ template <class T> int BatchRunner::tune_occupancy(cudaStream_t st, const std::s
     std::lock_guard<std::mutex> lock(mu);
     std::vector<int> choice(occ_, occ_ + BK_TUNED);
     choice.push_back(coarse_per_sm);
+    choice.push_back(coarse_occ_);
     cache[key] = choice;
     return GBP_OK;
 }
@@ -489,7 +501,7 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
         ++*nodes;
     }
     if (e == cudaSuccess && max_global_ > 1) {
-        e = b_coarse_descend<T>(BLaunch{coarse_blocks_, st, gate, d_scene_of_, d_counters_}, lv, coarse_, sc, ms);
+        e = b_coarse_descend<T>(BLaunch{coarse_blocks_, st, gate, d_scene_of_, d_counters_, coarse_occ_}, lv, coarse_, sc, ms);
         ++*nodes;
     }
     if (e == cudaSuccess && tail_bytes_ > 0) {
@@ -498,7 +510,7 @@ template <class T> cudaError_t BatchRunner::enqueue_iteration(const gbp_params &
     }
     // ascend: the coarse global levels in one launch, then the fine level
     if (e == cudaSuccess && max_global_ > 1) {
-        e = b_coarse_ascend<T>(BLaunch{coarse_blocks_, st, gate, d_scene_of_, d_counters_}, lv, coarse_, sc, ms,
+        e = b_coarse_ascend<T>(BLaunch{coarse_blocks_, st, gate, d_scene_of_, d_counters_, coarse_occ_}, lv, coarse_, sc, ms,
                                T(ms.alpha));
         ++*nodes;
     }

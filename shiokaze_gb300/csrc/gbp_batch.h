@@ -259,6 +259,7 @@ private:
     BatchCounters *d_counters_ = nullptr, *h_counters_ = nullptr;
     CoarseLists coarse_{};
     int coarse_blocks_ = 0;
+    int coarse_occ_ = 0;  // register variant of the cooperative kernels: 2 (bounds of 2 blocks per SM) or 0
     // fine levels split by staging: TMA-staged (FP32 levels that qualify) and
     // plain; each a segment list over pair tiles of level 0
     BSeg *d_fine_staged_ = nullptr, *d_fine_plain_ = nullptr;
