@@ -466,7 +466,9 @@ def run_gbp(args):
                      "update": round(stats["ms_update"], 4)},
         "compare": compare,
         "e2e": {"value": round(e2e_value, 3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "host_buffers": "pageable numpy arrays"},
+                "d2h_bytes_per_step": int(d2h), "host_buffers": "pageable numpy arrays",
+                "ms_per_step": {"p50": round(1000.0 * float(np.median(e2e_times)), 3),
+                                "max": round(1000.0 * float(np.max(e2e_times)), 3)}},
         "e2e_bricks": e2e_bricks,
         "roofline": roofline,
         "clocks": main["clocks"],
